@@ -1,0 +1,320 @@
+"""Benchmark of the FedNL round on GB300: rounds/s of the w8a-like workload (d=301, 142 clients,
+n_i ~ U{200..600}, TopLEK k=8d, alpha=1, Option B, FP64 throughout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload w8a|a9a]
+
+A step is one FedNL round over all clients.  Prints one JSON line (rank 0).  ``--impl reference``
+times the reference algorithm's CPU implementation (the C port in oracle/, every host thread)
+on the same workload.  Under torchrun every rank runs an independent replica on its own GPU
+(the round has no cross-GPU exchange); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "FedNL rounds/s & time to ‖∇f‖≤1e-9 (mixed vs FP64 GPU vs host CPU); p99 round ms"
+L2_FLUSH_BYTES = 256 << 20          # > 129 MB L2: every timed round starts cold
+TOL = 1e-9
+
+
+def workload(name: str):
+    from ufednl_gb300 import datagen
+    if name == "a9a":
+        return datagen.workload_a9a_like(), "topk", 8 * 124
+    return datagen.workload_w8a_like(), "toplek", 8 * 301
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as td
+    td.init_process_group("gloo")
+    return td
+
+
+def dist_max(td, v: float) -> float:
+    if td is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(td):
+    if td is not None:
+        td.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return float(j["hbm_gbs"]), float(j["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
+    """Algorithmic HBM bytes of one launch of a round kernel on this workload."""
+    d = prob.d
+    U = d * (d + 1) // 2
+    nc = prob.n_clients
+    S = prob.total_samples
+    words = int(sum(d * ((int(n) + 63) // 64) for n in prob.n_samples))
+    if kernel.startswith("k_hess"):
+        # read every client's shift, write its difference (packed upper FP64), read bitmasks and D
+        return nc * U * 16.0 + words * 8.0 + S * 8.0, "shift read + diff write (packed upper, FP64) per client"
+    if kernel == "k_select":
+        return nc * U * 8.0, "read every client's difference once"
+    if kernel == "k_apply":
+        return nc * (U + 31) // 32 * 4.0 + 2 * U * 8.0, "selection bitmaps + H read/write"
+    if kernel == "k_chol_solve":
+        return U * 8.0 * 3, "H read, factor write/read (packed upper)"
+    return 0.0, "n/a"
+
+
+def traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/<kernel>*.md, if any."""
+    pdir = os.path.join(REPO, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if fn.startswith(kernel) and fn.endswith(".md"):
+            for line in open(os.path.join(pdir, fn)):
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    try:
+                        return float(line.split(":", 1)[1].split()[0])
+                    except ValueError:
+                        return None
+    return None
+
+
+def upload_bytes(prob) -> int:
+    """Host->device bytes fednl_gpu_upload_client_data copies for binary features."""
+    d = prob.d
+    S = prob.total_samples
+    words = int(sum(d * ((int(n) + 63) // 64) for n in prob.n_samples))
+    nnz = int(np.count_nonzero(prob.features))
+    return words * 8 + nnz * 4 + (S + 1) * 4 + prob.n_clients * 8 + S * 8
+
+
+def cpu_port_rounds_per_s(prob, comp, k, threads: int, max_rounds: int, budget_s: float):
+    from oracle import pyoracle
+    pyoracle.build()
+    orc = pyoracle.FedNL(prob, comp, k, 1.0, workers=threads, threads=threads)
+    orc.round()                                           # warm-up round
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_rounds:
+        orc.round()
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    orc.close()
+    return n / dt, n, dt
+
+
+def run_reference(args, ws, rank, td):
+    prob, comp, k = workload(args.workload)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    warm = max(0, args.warmup)
+    from oracle import pyoracle
+    pyoracle.build()
+    orc = pyoracle.FedNL(prob, comp, k, 1.0, workers=threads, threads=threads)
+    for _ in range(min(warm, 2)):
+        orc.round()
+    t0 = time.perf_counter()
+    n = 0
+    while n < args.steps:
+        orc.round()
+        n += 1
+        if time.perf_counter() - t0 > 90.0:
+            break
+    dt = time.perf_counter() - t0
+    orc.close()
+    v = n / dt
+    sample = (f"{n} full rounds of the workload (of {args.steps} requested; 90 s cap), "
+              f"{threads} threads, C port of the reference round (oracle/fednl_oracle.c)")
+    line = {"metric": METRIC, "value": v, "unit": "rounds/s", "n_gpus": args.gpus, "steps": n,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": config_dict(prob, comp, k, threads),
+            "cpu_baseline": {"value": v, "unit": "rounds/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "rounds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config_dict(prob, comp, k, workers):
+    return {"workload": prob.name, "d": prob.d, "clients": prob.n_clients, "samples": prob.total_samples,
+            "compressor": comp, "k": k, "alpha": 1.0, "option": "B", "lambda": prob.lam, "workers": workers,
+            "precision": "fp64", "l2": f"flushed before every timed round ({L2_FLUSH_BYTES >> 20} MB write)",
+            "parallelism": "replicas"}
+
+
+def run_ours(args, ws, rank, local, td):
+    from ufednl_gb300 import build, fednl
+    build.build()
+    prob, comp, k = workload(args.workload)
+    W = args.workers or (os.cpu_count() or 1)
+    fed = fednl.FedNL(prob, comp, k, 1.0, workers=W)
+    # convergence trace: rounds to ||g|| <= 1e-9 from x0 (device-timed below)
+    gtrace = fed.run(max(args.warmup, 3))
+    dist_barrier(td)
+    with ClockSampler(local) as clk:
+        total_ms, per = fed.time_rounds(args.steps, L2_FLUSH_BYTES)
+    clocks = clk.summary()
+    total_ms = dist_max(td, total_ms)
+    dist_barrier(td)
+    value = ws * args.steps / (total_ms / 1000.0)
+    ms_per_step = total_ms / args.steps
+
+    # per-kernel breakdown with CUDA events on the library's stream
+    prof = fed.profile_kernels(min(args.steps, 50), L2_FLUSH_BYTES)
+    kernels = {n: ms for n, ms in prof}
+    dom, dom_ms = max(prof, key=lambda t: t[1])
+    hbm, bf16, src = peaks()
+    abytes, what = algorithmic_bytes(dom, prob, k)
+    ach = abytes / (dom_ms / 1000.0) / 1e9 if abytes else 0.0
+    roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": traffic_from_profiles(dom), "algorithmic_bytes_per_launch": abytes,
+            "algorithmic_bytes": what, "kernel_ms": dom_ms, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)"}
+    fed.close()
+
+    # time to ||g|| <= 1e-9: fresh run, rounds until the tolerance, at the measured ms/round
+    fed2 = fednl.FedNL(prob, comp, k, 1.0, workers=W)
+    g = fed2.run(200)
+    hit = np.nonzero(g <= TOL)[0]
+    rounds_to_tol = int(hit[0]) + 1 if hit.size else None
+    fed2.close()
+
+    # end to end through the C ABI with host buffers: create + upload + init + K rounds (each
+    # returning its statistics to the host) + final iterate readback
+    n_e2e = min(args.steps, 100)
+    t0 = time.perf_counter()
+    fed3 = fednl.FedNL(prob, comp, k, 1.0, workers=W)
+    for _ in range(n_e2e):
+        fed3.round()
+    x = fed3.x()
+    fed3.close()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": n_e2e / e2e_s, "unit": "rounds/s",
+           "h2d_bytes_per_step": upload_bytes(prob) / n_e2e + 0.0,
+           "d2h_bytes_per_step": 16 + 8 + prob.d * 8 / n_e2e,
+           "rounds": n_e2e, "includes": "create + client-data upload + shift init + rounds + x readback"}
+
+    line = {"metric": METRIC, "value": value, "unit": "rounds/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(prob, comp, k, W),
+            "round_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+            "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
+                            "seconds": rounds_to_tol * ms_per_step / 1000.0 if rounds_to_tol else None},
+            "roofline": roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
+            "clocks": clocks, "e2e": e2e}
+    if ws == 1 and rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, dt = cpu_port_rounds_per_s(prob, comp, k, threads, 20, 20.0)
+        line["cpu_baseline"] = {"value": v, "unit": "rounds/s", "cores": threads, "kind": "port",
+                                "sample": f"{n} full rounds of the workload after one warm-up round ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["w8a", "a9a"], default="w8a")
+    ap.add_argument("--workers", type=int, default=0, help="reference --workers (TopLEK streams); 0 = host cores")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    td = dist_init(ws)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, ws, rank, td)
+        return run_ours(args, ws, rank, local, td)
+    finally:
+        if td is not None:
+            td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

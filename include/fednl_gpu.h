@@ -1,0 +1,175 @@
+/*
+ * fednl_gpu.h -- C ABI of the GB300 (sm_103a) FedNL round engine.
+ *
+ * Drop-in for the hot path of u-FedNL (dopt): the per-client L2-logistic oracle, the FedNL
+ * compressors on the upper triangle of H_i - shift_i, the shift update, the master aggregation
+ * and the Option-B Cholesky Newton step.  Plain C types only (no CUDA or torch types); every
+ * entry point returns an int status (FEDNL_OK or a negative fednl_status code) and
+ * fednl_gpu_last_error() describes the last failure of the calling thread.
+ *
+ * Threading: a handle is not thread-safe; calls on one handle are serialised on the handle's
+ * own CUDA stream.  Different handles may be used from different threads.
+ *
+ * Index convention (identical to the reference): a selected Hessian entry (i, j), i <= j, is
+ * reported as the flat column-major index j * lda + i, where lda is the reference build's
+ * leading dimension (d rounded up to 4 in its default AVX2 build).
+ */
+#ifndef FEDNL_GPU_H
+#define FEDNL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fednl_status {
+    FEDNL_OK = 0,
+    FEDNL_EINVAL = -1,     /* bad argument or call order */
+    FEDNL_ENOMEM = -2,     /* device or host allocation failed */
+    FEDNL_ECUDA = -3,      /* a CUDA runtime call failed */
+    FEDNL_ENOTPD = -4,     /* Option-B matrix H + l I not positive definite */
+    FEDNL_ETIMEOUT = -5,   /* a bounded device-side wait ran out */
+    FEDNL_ENODEV = -6      /* no usable CUDA device */
+} fednl_status;
+
+/* Same numbering as the reference's enum Compressor
+ * (dopt/bin_fednl_local/include/UsedTypes.h:18-26). */
+typedef enum fednl_compressor {
+    FEDNL_IDENTITY = 0,
+    FEDNL_RANDK = 1,
+    FEDNL_TOPK = 2,
+    FEDNL_RANDSEQK = 3,
+    FEDNL_TOPLEK = 4,
+    FEDNL_NATURAL = 5
+} fednl_compressor;
+
+typedef enum fednl_feature_format {
+    FEDNL_FEATURES_AUTO = 0,    /* binary if every feature is 0 or 1, dense otherwise */
+    FEDNL_FEATURES_BINARY = 1,  /* {0,1} features: bit-packed per client and feature */
+    FEDNL_FEATURES_DENSE = 2    /* arbitrary FP64 features */
+} fednl_feature_format;
+
+/* Problem description.  Mirrors the reference's train() configuration
+ * (dopt/bin_fednl_local/include/TrainLoop.h:103-735 and Args.h). */
+typedef struct fednl_problem_desc {
+    int32_t d;                  /* dimension including the intercept attribute */
+    int32_t lda;                /* leading dimension for flat indices; 0 = reference default (d up to x4) */
+    int32_t n_clients;
+    const int32_t* n_samples;   /* host [n_clients]; uneven sizes allowed */
+    double lambda;              /* L2 regulariser */
+    int32_t compressor;         /* fednl_compressor */
+    int32_t k;                  /* compressor k (ignored for Identity / Natural, which send all of U) */
+    double alpha;               /* shift learning rate */
+    int32_t workers;            /* reference --workers W: client c runs on worker c mod W (TopLEK streams) */
+    uint32_t seed_base;         /* RandK / RandSeqK client seed = seed_base + c (reference: 123) */
+    uint32_t toplek_seed;       /* initial state of each worker's TopLEK generator (reference: 1234) */
+    int32_t feature_format;     /* fednl_feature_format */
+    int32_t reserved[4];        /* must be zero */
+} fednl_problem_desc;
+
+typedef struct fednl_round_stats {
+    int32_t round;              /* index of the round just completed */
+    int32_t status;             /* FEDNL_OK or FEDNL_ENOTPD for this round */
+    double grad_norm;           /* ||g|| of the aggregated gradient at the round's starting iterate */
+    double l;                   /* Option-B regulariser l = mean_i Lk_i */
+} fednl_round_stats;
+
+typedef struct fednl_handle_s* fednl_handle;
+
+/* ---- lifecycle ---------------------------------------------------------------------------- */
+
+/* Replaces the setup of train() (TrainLoop.h:103-735): sizes, device buffers, stream. */
+int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out);
+int fednl_gpu_destroy(fednl_handle h);
+
+/* Client data, host row-major features [sum n_i][d] (clients concatenated in order) and labels
+ * [sum n_i] in {-1,+1}.  Replaces the per-client L2RegulirizeLogisticRegression construction
+ * (TrainLoop.h:601-605; logistic_regression.h:26-76). */
+int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels);
+
+/* shift_i = H_i(x0), H = mean_i shift_i, x = x0 (x0 NULL = zeros, the reference default).
+ * Replaces TrainLoop.h:639-643 and :732-735. */
+int fednl_gpu_init_shifts(fednl_handle h, const double* x0);
+
+/* One FedNL round (Option B): clients' oracle, compression, shift update; master aggregation,
+ * Cholesky of H + l I and x -= dx.  Replaces one iteration of TrainLoop.h:991-1698. */
+int fednl_gpu_round(fednl_handle h, fednl_round_stats* stats);
+
+/* `rounds` rounds back to back (CUDA-graph replays); grad_norms (host, may be NULL) receives
+ * ||g|| per round.  Returns the status of the first failing round, if any. */
+int fednl_gpu_run(fednl_handle h, int32_t rounds, double* grad_norms);
+
+/* ---- state readback (host buffers) -------------------------------------------------------- */
+int fednl_gpu_get_x(fednl_handle h, double* x);                 /* [d] */
+int fednl_gpu_set_x(fednl_handle h, const double* x);           /* [d] */
+int fednl_gpu_get_grad(fednl_handle h, double* g);              /* [d] aggregated gradient */
+int fednl_gpu_get_H(fednl_handle h, double* H);                 /* [d * lda] column-major, upper current */
+int fednl_gpu_get_shift(fednl_handle h, int32_t client, double* shift);   /* [d * lda] symmetric */
+double fednl_gpu_get_l(fednl_handle h);
+double fednl_gpu_get_lk(fednl_handle h, int32_t client);
+/* Last round's message of a client, exactly as the reference master adds it to H:
+ * flat indices (ascending, except RandSeqK's window order) and values. */
+int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double* val, int32_t* count);
+
+/* ---- operator-level entry points (host buffers in, host buffers out) ----------------------- */
+
+/* getTopKFromUpperDiagonalPart<ignoreSign=true>
+ * (dopt/dopt/math_routines/include/SpecialMathRoutinesForMatrix.h:229-366) on n_mat matrices,
+ * each column-major d x lda.  idx receives n_mat * k flat indices, ascending per matrix. */
+int fednl_gpu_topk(const double* mats, int32_t n_mat, int32_t d, int32_t lda, int32_t k, uint32_t* idx);
+
+/* getTopLEKFromUpperDiagonalPart<ignoreSign=true> (SpecialMathRoutinesForMatrix.h:377-511) with
+ * delta = k / U.  Matrix t draws from worker stream worker_of[t] (NULL = all on stream 0); the
+ * n_workers generator states (RandomGenRealLinear, :383) are read and advanced in place; matrices
+ * of one stream consume it in increasing t.  idx: n_mat * k slots, counts[t] entries used. */
+int fednl_gpu_toplek(const double* mats, int32_t n_mat, int32_t d, int32_t lda, int32_t k,
+                     int32_t n_workers, const int32_t* worker_of, uint32_t* worker_states,
+                     uint32_t* idx, int32_t* counts);
+
+/* generateRandKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:95-107): one draw of
+ * k sorted flat indices per generator; states[n_gen] (RandomGenIntegerLinear) advanced in place. */
+int fednl_gpu_randk(uint32_t* states, int32_t n_gen, int32_t d, int32_t lda, int32_t k, uint32_t* idx);
+
+/* generateRandSeqKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:137-169). */
+int fednl_gpu_randseqk(uint32_t* states, int32_t n_gen, int32_t d, int32_t lda, int32_t k, uint32_t* idx);
+
+/* applyNaturalCompressor (dopt/dopt/linalg_matrices/include/MatrixNMD.h:2009-2031) on n values;
+ * packed (may be NULL) receives the reference wire format of consecutive pairs,
+ * 3 bytes per pair (pack2FP64NoMantissa, dopt/dopt/system/include/FloatUtils.h:193-221). */
+int fednl_gpu_natural(const double* in, int64_t n, double* out, uint8_t* packed);
+
+/* Logistic oracle of one client: evaluateGradient and evaluateHessian<true, 4>
+ * (dopt/dopt/optimization_problems/include/ml/logistic_regression.h:148-547).
+ * features row-major [n][d], labels [n]; grad [d]; hess [d * lda] column-major symmetric. */
+int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_t n, int32_t d,
+                            int32_t lda, double lambda, const double* x, double* grad, double* hess);
+
+/* Option-B solve: choleskyFactorization<.., true, true>(Ltr, H, l) then forward / backward
+ * substitution (CholeskyFactorization.h:153-272, ElementarySolvers.h:71-224).  H column-major
+ * d x lda, only the upper triangle is read.  Returns FEDNL_ENOTPD if H + l I is not positive
+ * definite. */
+int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
+
+/* ---- instrumentation ---------------------------------------------------------------------- */
+
+/* Device time of `rounds` rounds replayed as in fednl_gpu_run, each bracketed by CUDA events on
+ * the handle's stream.  Before each round a buffer of flush_bytes is rewritten outside the
+ * bracket so that every round starts with a cold L2 (0 = no flush).  Replaces the reference's
+ * wall-clock round timer (dopt/bin_fednl_local/include/TrainLoop.h:1669-1670, :1715).
+ * per_round_ms (may be NULL) receives each round's time. */
+int fednl_gpu_time_rounds(fednl_handle h, int32_t rounds, int64_t flush_bytes, double* total_ms,
+                          double* per_round_ms);
+
+/* Per-kernel breakdown of the same rounds: launched kernel by kernel with CUDA events between the
+ * launches on the handle's stream.  kernel_ms[t] (capacity 32) receives the mean time of the t-th
+ * launch of a round; names receives the kernel names separated by ';'. */
+int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_bytes, int32_t* n_kernels,
+                              double* kernel_ms, char* names, int32_t names_len);
+
+const char* fednl_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

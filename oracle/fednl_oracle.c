@@ -1,0 +1,757 @@
+/*
+ * fednl_oracle.c -- CPU restatement of the u-FedNL (dopt) FedNL round.  TEST INFRASTRUCTURE:
+ * the parity checker for the GB300 kernels and the timed CPU port in bench.py.  Nothing in
+ * the product library (libfednl_gpu.so) links or calls this file.
+ *
+ * Each function cites the reference file:line it restates (paths relative to the ufednl
+ * repository root).  Floating-point formulas keep the reference's operation order where the
+ * reference fixes it (per-entry sample order of the Hessian and gradient sums, products as
+ * written); SIMD horizontal-sum orders of dot products and norms are restated as sequential
+ * sums, which changes results by a few ulps only.  The file is compiled with
+ * -ffp-contract=off so that no multiply-add is fused.
+ */
+#include "fednl_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ================================================================================== */
+/* LCG generators                                                                     */
+/* ================================================================================== */
+
+/* RandomGenIntegerLinear: x <- 214013 x + 2531011 (mod 2^32)
+ * dopt/dopt/random/include/RandomGenIntegerLinear.h:107-123, src/RandomGenIntegerLinear.cpp:12-19 */
+uint32_t orc_lcg_int_next(uint32_t* state)
+{
+    *state = 214013u * (*state) + 2531011u;
+    return *state;
+}
+
+/* RandomGenIntegerLinear::generateRealInUnitInterval, RandomGenIntegerLinear.h:49-58 */
+double orc_lcg_int_unit(uint32_t* state)
+{
+    *state = 214013u * (*state) + 2531011u;
+    return (double)(*state) * (1.0 / 4294967295.0);
+}
+
+/* RandomGenRealLinear::generateRealInUnitInterval: (a x + c) mod 2^32, then mod (2^32 - 1)
+ * dopt/dopt/random/include/RandomGenRealLinear.h:54-59, src/RandomGenRealLinear.cpp:5-8 */
+double orc_lcg_real_unit(uint32_t* state)
+{
+    uint32_t t = 214013u * (*state) + 2531011u;
+    *state = t % 4294967295u;
+    return (double)(*state) * (1.0 / 4294967295.0);
+}
+
+/* roundToNearestInt<size_t>, dopt/dopt/math_routines/include/SimpleMathRoutines.h:408-414 */
+size_t orc_round_to_nearest(double v)
+{
+    size_t t = (size_t)v;
+    if (v - (double)t > 0.5)
+        return t + 1;
+    return t;
+}
+
+/* ================================================================================== */
+/* Upper-triangle indices and compressors                                             */
+/* ================================================================================== */
+
+size_t orc_upper_count(int32_t d) { return ((size_t)d * (size_t)(d + 1)) / 2; }
+
+/* indiciesForUpperTriangularPart: column j, rows 0..j, flat index j*LDA + i
+ * dopt/dopt/math_routines/include/SpecialMathRoutinesForMatrix.h:35-64 */
+void orc_upper_indices(int32_t d, int32_t lda, uint32_t* out)
+{
+    size_t w = 0;
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i <= j; ++i)
+            out[w++] = (uint32_t)j * (uint32_t)lda + (uint32_t)i;
+}
+
+/* Partial Fisher-Yates with early stop, dopt/dopt/random/include/Shuffle.h:31-95 (active loop :76-93) */
+void orc_shuffle_partial(uint32_t* arr, size_t n, size_t k, uint32_t* state)
+{
+    size_t n_minus_i_minus_one = n - 1;
+    for (size_t i = 0; i < k; ++i, --n_minus_i_minus_one) {
+        double u = orc_lcg_int_unit(state);
+        size_t r_off = orc_round_to_nearest(u * (double)n_minus_i_minus_one);
+        if (r_off != 0) {
+            uint32_t t = arr[i];
+            arr[i] = arr[i + r_off];
+            arr[i + r_off] = t;
+        }
+    }
+}
+
+static int cmp_u32(const void* a, const void* b)
+{
+    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return (x > y) - (x < y);
+}
+
+/* generateRandKItemsInUpperTriangularPart, SpecialMathRoutinesForMatrix.h:95-107 */
+void orc_randk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out)
+{
+    uint32_t* tmp = (uint32_t*)malloc(U * sizeof(uint32_t));
+    memcpy(tmp, upper, U * sizeof(uint32_t));
+    orc_shuffle_partial(tmp, U, (size_t)k, state);
+    memcpy(out, tmp, (size_t)k * sizeof(uint32_t));
+    qsort(out, (size_t)k, sizeof(uint32_t), cmp_u32);
+    free(tmp);
+}
+
+/* generateRandSeqKItemsInUpperTriangularPart, SpecialMathRoutinesForMatrix.h:137-169 */
+void orc_randseqk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out)
+{
+    uint32_t r = (uint32_t)((size_t)orc_lcg_int_next(state) % U);
+    for (int32_t t = 0; t < k; ++t) {
+        size_t p = (size_t)r + (size_t)t;
+        if (p >= U)
+            p -= U;
+        out[t] = upper[p];
+    }
+}
+
+/* ---- 4-ary min-heap of flat indices keyed by |m[index]| --------------------------- */
+/* dopt/dopt/math_routines/include/MinHeap.h (D = 4) */
+typedef struct {
+    uint32_t* data;
+    size_t size;
+    const double* m;
+} orc_heap;
+
+static inline double hkey(const orc_heap* h, uint32_t idx) { return fabs(h->m[idx]); }
+
+/* minHeapify, MinHeap.h:255-290: leftmost strictly-smaller child wins */
+static void heap_sift(orc_heap* h, size_t i, size_t heap_size)
+{
+    double lowest_value = hkey(h, h->data[i]);
+    for (;;) {
+        size_t lowest = i;
+        size_t first = 4 * i + 1;
+        size_t last = first + 4 < heap_size ? first + 4 : heap_size;
+        for (size_t c = first; c < last; ++c) {
+            double cv = hkey(h, h->data[c]);
+            if (lowest_value > cv) {
+                lowest = c;
+                lowest_value = cv;
+            }
+        }
+        if (lowest != i) {
+            uint32_t t = h->data[i];
+            h->data[i] = h->data[lowest];
+            h->data[lowest] = t;
+            i = lowest;
+        } else {
+            break;
+        }
+    }
+}
+
+/* buildMinHeap, MinHeap.h:147-191: Floyd build starting at (sz + D - 2) / D */
+static void heap_build(orc_heap* h)
+{
+    size_t i = (h->size + 4 - 2) / 4;
+    for (;;) {
+        heap_sift(h, i, h->size);
+        if (i == 0)
+            break;
+        --i;
+    }
+}
+
+/* extracFromMinHeap, MinHeap.h:125-141 */
+static uint32_t heap_extract(orc_heap* h)
+{
+    uint32_t res = h->data[0];
+    size_t n = h->size;
+    uint32_t t = h->data[0];
+    h->data[0] = h->data[n - 1];
+    h->data[n - 1] = t;
+    heap_sift(h, 0, n - 1);
+    h->size = n - 1;
+    return res;
+}
+
+/* insertInMinHeap, MinHeap.h:92-103 */
+static void heap_insert(orc_heap* h, uint32_t v)
+{
+    size_t i = h->size++;
+    h->data[i] = v;
+    while (i != 0 && hkey(h, h->data[(i - 1) / 4]) > hkey(h, h->data[i])) {
+        size_t p = (i - 1) / 4;
+        uint32_t t = h->data[p];
+        h->data[p] = h->data[i];
+        h->data[i] = t;
+        i = p;
+    }
+}
+
+/* Heap phase shared by TopK and TopLEK: SpecialMathRoutinesForMatrix.h:291-318 (TopK) and
+ * :406-433 (TopLEK).  Seeds the heap with the first k upper indices, then replaces the root
+ * by every later entry whose magnitude is strictly larger. */
+static void topk_heap_scan(orc_heap* h, int32_t k, size_t U, const uint32_t* upper)
+{
+    memcpy(h->data, upper, (size_t)k * sizeof(uint32_t));
+    h->size = (size_t)k;
+    heap_build(h);
+    double min_value = hkey(h, h->data[0]);
+    for (size_t i = (size_t)k; i < U; ++i) {
+        uint32_t cand = upper[i];
+        if (hkey(h, cand) > min_value) {
+            h->data[0] = cand;                 /* increaseMinimumInMinHeap, MinHeap.h:78-85 */
+            heap_sift(h, 0, h->size);
+            min_value = hkey(h, h->data[0]);
+        }
+    }
+}
+
+/* getTopKFromUpperDiagonalPart<ignoreSign=true>, SpecialMathRoutinesForMatrix.h:229-366 */
+int32_t orc_topk(const double* m, int32_t k, size_t U, const uint32_t* upper, uint32_t* out)
+{
+    if ((size_t)k >= U) {
+        memcpy(out, upper, U * sizeof(uint32_t));
+        return (int32_t)U;
+    }
+    orc_heap h;
+    h.data = out;
+    h.m = m;
+    topk_heap_scan(&h, k, U, upper);
+    qsort(out, (size_t)k, sizeof(uint32_t), cmp_u32);
+    return k;
+}
+
+/* getTopLEKFromUpperDiagonalPart<ignoreSign=true>, SpecialMathRoutinesForMatrix.h:377-511.
+ * rng_state is the calling worker thread's RandomGenRealLinear state (thread_local, :383). */
+int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                   double delta, double frob_sq, uint32_t* rng_state, uint32_t* out)
+{
+    double one_minus_delta = 1.0 - delta;
+    double one_minus_delta_xf = one_minus_delta * frob_sq;
+    double eps = 1e-1 * frob_sq;
+
+    if ((size_t)k >= U) {
+        memcpy(out, upper, U * sizeof(uint32_t));
+        return (int32_t)U;
+    }
+
+    orc_heap h;
+    h.data = out;
+    h.m = m;
+    topk_heap_scan(&h, k, U, upper);
+
+    /* numerator = ||M||^2 - sum over the heap array (:435-451) */
+    double numerator = frob_sq;
+    for (size_t i = 0; i < h.size; ++i) {
+        uint32_t index = h.data[i];
+        double item = m[index];
+        uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
+        if (ir == jc)
+            numerator -= item * item;
+        else
+            numerator -= 2.0 * item * item;
+    }
+
+    /* extraction with randomized rounding (:453-503) */
+    do {
+        double prev = numerator;
+        uint32_t min_index = heap_extract(&h);
+        double item = m[min_index];
+        uint32_t jc = min_index / (uint32_t)lda, ir = min_index - jc * (uint32_t)lda;
+        if (ir == jc)
+            numerator += item * item;
+        else
+            numerator += 2.0 * item * item;
+        double next = numerator;
+        if (one_minus_delta_xf + eps > prev && one_minus_delta_xf < next + eps) {
+            double p = (one_minus_delta_xf - prev + eps) / (next - prev + eps);
+            if (orc_lcg_real_unit(rng_state) > p)
+                heap_insert(&h, min_index);
+            break;
+        }
+    } while (h.size != 0);
+
+    qsort(out, h.size, sizeof(uint32_t), cmp_u32);
+    return (int32_t)h.size;
+}
+
+/* applyNaturalCompressorNaive: sign and exponent kept, mantissa zeroed, MatrixNMD.h:2013-2031 */
+double orc_natural(double v)
+{
+    uint64_t b;
+    memcpy(&b, &v, 8);
+    b &= ~((((uint64_t)1) << 52) - 1);
+    memcpy(&v, &b, 8);
+    return v;
+}
+
+/* pack2FP64NoMantissa: [signA(1) expA(11) signB(1) expB(11)], dopt/dopt/system/include/FloatUtils.h:193-221 */
+uint32_t orc_pack2_natural(double a, double b)
+{
+    uint64_t ba, bb;
+    memcpy(&ba, &a, 8);
+    memcpy(&bb, &b, 8);
+    uint32_t sa = (uint32_t)(ba >> 63), ea = (uint32_t)((ba >> 52) & 0x7FF);
+    uint32_t sb = (uint32_t)(bb >> 63), eb = (uint32_t)((bb >> 52) & 0x7FF);
+    return (sa << 23) | (ea << 12) | (sb << 11) | eb;
+}
+
+double orc_l2sq(const double* v, size_t n)
+{
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i)
+        s += v[i] * v[i];
+    return s;
+}
+
+/* ================================================================================== */
+/* Logistic-regression oracle                                                         */
+/* dopt/dopt/optimization_problems/include/ml/logistic_regression.h                   */
+/* ================================================================================== */
+
+/* evaluateClassificationMargin, :88-92 (m = Atr^T x) */
+void orc_margin(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x, double* m)
+{
+    for (int32_t s = 0; s < n; ++s) {
+        const double* col = atr + (size_t)s * lda;
+        double acc = 0.0;
+        for (int32_t i = 0; i < d; ++i)
+            acc += col[i] * x[i];
+        m[s] = acc;
+    }
+}
+
+/* elementwiseSigmoid, dopt/dopt/linalg_vectors/include_internal/VectorND_Raw_SIMD_double.h:1596-1650 */
+void orc_sigmoid(const double* m, int32_t n, double* sig)
+{
+    for (int32_t s = 0; s < n; ++s)
+        sig[s] = 1.0 / (1.0 + exp(-m[s]));
+}
+
+/* evaluateGradient(x, margin, sigmoid), :148-161:
+ * q_s = (1 - sigma_s) * (-1/n); g = lambda x + sum_s Atr[:,s] q_s (samples in order) */
+void orc_gradient(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x,
+                  const double* sig, double lambda, double* g)
+{
+    double inv_m = 1.0 / (double)n;
+    double minus_inv_m = -inv_m;
+    for (int32_t i = 0; i < d; ++i)
+        g[i] = x[i] * lambda;
+    for (int32_t s = 0; s < n; ++s) {
+        double q = (1.0 - sig[s]) * minus_inv_m;
+        const double* col = atr + (size_t)s * lda;
+        for (int32_t i = 0; i < d; ++i)
+            g[i] += col[i] * q;
+    }
+}
+
+/* evaluateHessian<true, 4>, :163-547 (algorithm 4 :365-547): per entry (i <= j) the sum over
+ * samples in order of u_i * (D_s * v_j), D_s = (1/n) * ((1 - sigma_s) * sigma_s); then the
+ * lower triangle is mirrored and lambda is added to the diagonal. */
+void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const double* sig,
+                 double lambda, double* h)
+{
+    double inv_m = 1.0 / (double)n;
+    memset(h, 0, (size_t)d * (size_t)lda * sizeof(double));
+    for (int32_t s = 0; s < n; ++s) {
+        double z1 = 1.0 - sig[s];
+        double z2 = z1 * sig[s];
+        double d_s = inv_m * z2;
+        const double* u = atr + (size_t)s * lda;
+        for (int32_t j = 0; j < d; ++j) {
+            double vj = d_s * u[j];
+            double* col = h + (size_t)j * lda;
+            for (int32_t i = 0; i <= j; ++i)
+                col[i] += u[i] * vj;
+        }
+    }
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i < j; ++i)
+            h[(size_t)i * lda + j] = h[(size_t)j * lda + i];
+    for (int32_t j = 0; j < d; ++j)
+        h[(size_t)j * lda + j] += lambda;
+}
+
+/* ================================================================================== */
+/* Option-B solve                                                                     */
+/* ================================================================================== */
+
+/* choleskyFactorization<Mat, fill_L_factor=true, in_input_symmetric=true>
+ * dopt/dopt/linalg_matrices/include/factorization/CholeskyFactorization.h:153-272 */
+int orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr)
+{
+    memset(ltr, 0, (size_t)d * (size_t)lda * sizeof(double));
+    for (int32_t i = 0; i < d; ++i) {
+        double* ci = ltr + (size_t)i * lda;
+        for (int32_t j = 0; j < i; ++j) {
+            const double* cj = ltr + (size_t)j * lda;
+            double squares = 0.0;
+            for (int32_t t = 0; t < j; ++t)
+                squares += ci[t] * cj[t];
+            double ljj = cj[j];
+            double in_ij = h[(size_t)i * lda + j];
+            double result = (1.0 / ljj) * (in_ij - squares);
+            ci[j] = result;
+            ltr[(size_t)j * lda + i] = result;
+        }
+        double squares = 0.0;
+        for (int32_t t = 0; t < i; ++t)
+            squares += ci[t] * ci[t];
+        double in_ii = h[(size_t)i * lda + i] + l;
+        double result = in_ii - squares;
+        if (result < 0) {
+            if (result > -0.0)
+                result = 0.0;
+            else
+                return 0;
+        }
+        ci[i] = sqrt(result);
+    }
+    return 1;
+}
+
+/* forwardSubstitutionWithATranspose then backwardSubstitutionWithATranspose
+ * dopt/dopt/linalg_linsolvers/include/ElementarySolvers.h:186-224 and :71-128 */
+void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
+{
+    double* y = (double*)malloc((size_t)d * sizeof(double));
+    y[0] = b[0] / ltr[0];
+    for (int32_t i = 1; i < d; ++i) {
+        const double* ci = ltr + (size_t)i * lda;
+        double acc = 0.0;
+        for (int32_t j = 0; j < i; ++j)
+            acc += ci[j] * y[j];
+        y[i] = (b[i] - acc) / ci[i];
+    }
+    for (int32_t i = d - 1; i >= 0; --i) {
+        const double* ci = ltr + (size_t)i * lda;
+        double acc = 0.0;
+        for (int32_t j = i + 1; j < d; ++j)
+            acc += ci[j] * x[j];
+        x[i] = (y[i] - acc) / ci[i];
+    }
+    free(y);
+}
+
+/* ================================================================================== */
+/* Whole FedNL run                                                                    */
+/* dopt/bin_fednl_local/include/TrainLoop.h:103-1863 with --debug forcesequpdate      */
+/* ================================================================================== */
+
+typedef struct {
+    double* atr;        /* d x n, lda */
+    int32_t n;
+    double* shift;      /* d x lda */
+    double* grad;       /* d */
+    double lk;
+    uint32_t rng;       /* RandK / RandSeqK generator (seed_base + c) */
+    uint32_t* msg_idx;  /* flat indices */
+    double* msg_val;    /* values exactly as the master adds them to H */
+    int32_t msg_count;
+} orc_client;
+
+struct orc_state {
+    orc_problem p;
+    size_t U;
+    uint32_t* upper;
+    orc_client* clients;
+    uint32_t* worker_rng;  /* TopLEK thread_local generator per logical worker */
+    double* x;
+    double* H;             /* master, d x lda, upper current */
+    double* g;
+    double l;
+    double* ltr;
+    double prescale;       /* alpha / n (TrainLoop.h:531) */
+    int32_t k_eff;
+};
+
+/* Worker side of one client for one round: LocalWorkerForFedNL_*.h, bodies of the per-context loops */
+static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* hbuf, double* diff,
+                         double* mtmp, double* stmp)
+{
+    const orc_problem* P = &S->p;
+    orc_client* C = &S->clients[c];
+    int32_t d = P->d, lda = P->lda, n = C->n;
+    size_t full = (size_t)d * (size_t)lda;
+    size_t U = S->U;
+
+    /* RandK / RandSeqK draw their indices before the round starts (RandK.h:46-62, RandSeqK.h:46-62) */
+    if (P->compressor == ORC_RANDK)
+        orc_randk(&C->rng, S->k_eff, U, S->upper, C->msg_idx);
+    else if (P->compressor == ORC_RANDSEQK)
+        orc_randseqk(&C->rng, S->k_eff, U, S->upper, C->msg_idx);
+
+    orc_margin(C->atr, d, lda, n, S->x, mtmp);
+    orc_sigmoid(mtmp, n, stmp);
+    orc_gradient(C->atr, d, lda, n, S->x, stmp, P->lambda, C->grad);
+    orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
+    for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
+        diff[t] = hbuf[t] - C->shift[t];
+    double frob_sq = orc_l2sq(diff, full);
+    C->lk = sqrt(frob_sq);                      /* Lk = ||diff||_F (TopK.h:74-78) */
+
+    double alpha = P->alpha, pre = S->prescale;
+    int32_t k = S->k_eff;
+
+    if (P->compressor == ORC_TOPK || P->compressor == ORC_TOPLEK) {
+        int32_t cnt;
+        if (P->compressor == ORC_TOPK) {
+            cnt = orc_topk(diff, k, U, S->upper, C->msg_idx);
+        } else {
+            double delta = (double)k * (1.0 / (double)U);   /* TopLEK.h:205, :244 */
+            cnt = orc_toplek(diff, lda, k, U, S->upper, delta, frob_sq, toplek_rng, C->msg_idx);
+        }
+        C->msg_count = cnt;
+        for (int32_t t = 0; t < cnt; ++t) {     /* TopK.h:94-129 */
+            uint32_t idx = C->msg_idx[t];
+            double item = diff[idx];
+            C->msg_val[t] = item * pre;
+            uint32_t jc = idx / (uint32_t)lda, ir = idx - jc * (uint32_t)lda;
+            C->shift[idx] += alpha * item;
+            if (ir != jc)
+                C->shift[(size_t)ir * lda + jc] += alpha * item;
+        }
+    } else if (P->compressor == ORC_RANDK || P->compressor == ORC_RANDSEQK) {
+        double mult = (double)U / (double)k;    /* RandK.h:90 */
+        C->msg_count = k;
+        for (int32_t t = 0; t < k; ++t) {       /* RandK.h:127-162 */
+            uint32_t idx = C->msg_idx[t];
+            double item = diff[idx] * mult;
+            C->msg_val[t] = item * pre;
+            uint32_t jc = idx / (uint32_t)lda, ir = idx - jc * (uint32_t)lda;
+            C->shift[idx] += alpha * item;
+            if (ir != jc)
+                C->shift[(size_t)ir * lda + jc] += alpha * item;
+        }
+    } else if (P->compressor == ORC_IDENTITY) {
+        /* Identical.h:80-94: message = diff * preScale over the upper part; shift += alpha * sym(diff) */
+        C->msg_count = (int32_t)U;
+        for (size_t t = 0; t < U; ++t) {
+            C->msg_idx[t] = S->upper[t];
+            C->msg_val[t] = diff[S->upper[t]] * pre;
+        }
+        for (int32_t j = 0; j < d; ++j)
+            for (int32_t i = 0; i <= j; ++i) {
+                double item = diff[(size_t)j * lda + i];
+                double upd = alpha * item;
+                C->shift[(size_t)j * lda + i] += upd;
+                if (i != j)
+                    C->shift[(size_t)i * lda + j] += upd;
+            }
+    } else { /* ORC_NATURAL, Natural.h:79-147: master adds preScale * trunc(diff) (TrainLoop.h:1169-1196) */
+        C->msg_count = (int32_t)U;
+        for (size_t t = 0; t < U; ++t) {
+            C->msg_idx[t] = S->upper[t];
+            C->msg_val[t] = pre * orc_natural(diff[S->upper[t]]);
+        }
+        for (int32_t j = 0; j < d; ++j)         /* learningHessian += alpha * trunc(diff), full matrix */
+            for (int32_t i = 0; i < d; ++i) {
+                size_t t = (size_t)j * lda + i;
+                C->shift[t] += alpha * orc_natural(diff[t]);
+            }
+    }
+}
+
+typedef struct {
+    orc_state* S;
+    int32_t tid, nthreads;
+} orc_job;
+
+static void* client_phase_thread(void* arg)
+{
+    orc_job* J = (orc_job*)arg;
+    orc_state* S = J->S;
+    int32_t d = S->p.d, lda = S->p.lda;
+    size_t full = (size_t)d * (size_t)lda;
+    int32_t nmax = 1;
+    for (int32_t c = 0; c < S->p.n_clients; ++c)
+        if (S->clients[c].n > nmax)
+            nmax = S->clients[c].n;
+    double* hbuf = (double*)malloc(full * sizeof(double));
+    double* diff = (double*)malloc(full * sizeof(double));
+    double* mtmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* stmp = (double*)malloc((size_t)nmax * sizeof(double));
+    int32_t W = S->p.workers;
+    /* logical workers w = tid, tid + nthreads, ...; each processes its clients c = w, w + W, ... in order
+     * (static round-robin distribution, TrainLoop.h:664-686) */
+    for (int32_t w = J->tid; w < W; w += J->nthreads)
+        for (int32_t c = w; c < S->p.n_clients; c += W)
+            client_round(S, c, &S->worker_rng[w], hbuf, diff, mtmp, stmp);
+    free(hbuf);
+    free(diff);
+    free(mtmp);
+    free(stmp);
+    return NULL;
+}
+
+orc_state* orc_create(const orc_problem* p, const double* x0)
+{
+    orc_state* S = (orc_state*)calloc(1, sizeof(orc_state));
+    S->p = *p;
+    int32_t d = p->d, lda = p->lda, nc = p->n_clients;
+    if (S->p.workers > nc)                      /* TrainLoop.h:194-199 */
+        S->p.workers = nc;
+    if (S->p.workers < 1)
+        S->p.workers = 1;
+    if (S->p.threads < 1 || S->p.threads > S->p.workers)
+        S->p.threads = S->p.workers;
+    size_t full = (size_t)d * (size_t)lda;
+    S->U = orc_upper_count(d);
+    S->upper = (uint32_t*)malloc(S->U * sizeof(uint32_t));
+    orc_upper_indices(d, lda, S->upper);
+    S->k_eff = (p->compressor == ORC_IDENTITY || p->compressor == ORC_NATURAL) ? (int32_t)S->U : p->k;
+    S->prescale = (1.0 / (double)nc) * p->alpha;
+    S->x = (double*)malloc((size_t)d * sizeof(double));
+    memcpy(S->x, x0, (size_t)d * sizeof(double));
+    S->H = (double*)calloc(full, sizeof(double));
+    S->ltr = (double*)calloc(full, sizeof(double));
+    S->g = (double*)calloc((size_t)d, sizeof(double));
+    S->worker_rng = (uint32_t*)malloc((size_t)S->p.workers * sizeof(uint32_t));
+    for (int32_t w = 0; w < S->p.workers; ++w)
+        S->worker_rng[w] = p->toplek_seed;
+    S->clients = (orc_client*)calloc((size_t)nc, sizeof(orc_client));
+
+    size_t msg_cap = S->U;
+    size_t off = 0;
+    int32_t nmax = 1;
+    for (int32_t c = 0; c < nc; ++c)
+        if (p->n_samples[c] > nmax)
+            nmax = p->n_samples[c];
+    double* mtmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* stmp = (double*)malloc((size_t)nmax * sizeof(double));
+    for (int32_t c = 0; c < nc; ++c) {
+        orc_client* C = &S->clients[c];
+        int32_t n = p->n_samples[c];
+        C->n = n;
+        /* L2RegulirizeLogisticRegression ctor stores column s = b_s * a_s (logistic_regression.h:26-76) */
+        C->atr = (double*)calloc((size_t)n * (size_t)lda, sizeof(double));
+        for (int32_t s = 0; s < n; ++s) {
+            double b = p->labels[off + s];
+            const double* a = p->features + (off + (size_t)s) * (size_t)d;
+            double* col = C->atr + (size_t)s * lda;
+            for (int32_t i = 0; i < d; ++i)
+                col[i] = (b == 1.0) ? a[i] : a[i] * -1.0;
+        }
+        off += (size_t)n;
+        C->shift = (double*)malloc(full * sizeof(double));
+        C->grad = (double*)calloc((size_t)d, sizeof(double));
+        C->msg_idx = (uint32_t*)malloc(msg_cap * sizeof(uint32_t));
+        C->msg_val = (double*)malloc(msg_cap * sizeof(double));
+        C->rng = p->seed_base + (uint32_t)c;    /* TrainLoop.h:632 */
+        /* learningHessian = H_i(x0); H += learningHessian (TrainLoop.h:639-643) */
+        orc_margin(C->atr, d, lda, n, S->x, mtmp);
+        orc_sigmoid(mtmp, n, stmp);
+        orc_hessian(C->atr, d, lda, n, stmp, p->lambda, C->shift);
+        for (size_t t = 0; t < full; ++t)
+            S->H[t] += C->shift[t];
+    }
+    free(mtmp);
+    free(stmp);
+    double inv_n = 1.0 / (double)nc;
+    for (size_t t = 0; t < full; ++t)           /* H *= 1/n (TrainLoop.h:732-735) */
+        S->H[t] *= inv_n;
+    return S;
+}
+
+void orc_destroy(orc_state* S)
+{
+    if (!S)
+        return;
+    for (int32_t c = 0; c < S->p.n_clients; ++c) {
+        orc_client* C = &S->clients[c];
+        free(C->atr);
+        free(C->shift);
+        free(C->grad);
+        free(C->msg_idx);
+        free(C->msg_val);
+    }
+    free(S->clients);
+    free(S->upper);
+    free(S->worker_rng);
+    free(S->x);
+    free(S->H);
+    free(S->ltr);
+    free(S->g);
+    free(S);
+}
+
+int orc_round(orc_state* S, double* grad_norm)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d, lda = P->lda, nc = P->n_clients;
+    int32_t T = S->p.threads;
+
+    /* client phase */
+    pthread_t* th = (pthread_t*)malloc((size_t)T * sizeof(pthread_t));
+    orc_job* jobs = (orc_job*)malloc((size_t)T * sizeof(orc_job));
+    for (int32_t t = 0; t < T; ++t) {
+        jobs[t].S = S;
+        jobs[t].tid = t;
+        jobs[t].nthreads = T;
+    }
+    if (T == 1) {
+        client_phase_thread(&jobs[0]);
+    } else {
+        for (int32_t t = 0; t < T; ++t)
+            pthread_create(&th[t], NULL, client_phase_thread, &jobs[t]);
+        for (int32_t t = 0; t < T; ++t)
+            pthread_join(th[t], NULL);
+    }
+    free(th);
+    free(jobs);
+
+    /* master phase, clients merged in order (TrainLoop.h:1092-1334 with forcesequpdate) */
+    double inv_n = 1.0 / (double)nc;
+    for (int32_t i = 0; i < d; ++i)
+        S->g[i] = 0.0;
+    double l = 0.0;
+    for (int32_t c = 0; c < nc; ++c) {
+        orc_client* C = &S->clients[c];
+        for (int32_t i = 0; i < d; ++i)
+            S->g[i] += C->grad[i];
+        for (int32_t t = 0; t < C->msg_count; ++t)
+            S->H[C->msg_idx[t]] += C->msg_val[t];
+        l += C->lk;
+    }
+    for (int32_t i = 0; i < d; ++i)
+        S->g[i] *= inv_n;
+    l *= inv_n;
+    S->l = l;
+
+    /* Option B: chol(H + l I), two triangular solves, x -= dx (TrainLoop.h:1431-1508) */
+    double* dx = (double*)malloc((size_t)d * sizeof(double));
+    int ok = orc_cholesky(S->H, d, lda, l, S->ltr);
+    if (ok) {
+        orc_solve_chol(S->ltr, d, lda, S->g, dx);
+        for (int32_t i = 0; i < d; ++i)
+            S->x[i] -= dx[i];
+    }
+    free(dx);
+    if (grad_norm)
+        *grad_norm = sqrt(orc_l2sq(S->g, (size_t)d));
+    return ok ? 0 : -1;
+}
+
+void orc_get_x(const orc_state* S, double* x) { memcpy(x, S->x, (size_t)S->p.d * sizeof(double)); }
+void orc_get_H(const orc_state* S, double* h)
+{
+    memcpy(h, S->H, (size_t)S->p.d * (size_t)S->p.lda * sizeof(double));
+}
+void orc_get_shift(const orc_state* S, int32_t c, double* sh)
+{
+    memcpy(sh, S->clients[c].shift, (size_t)S->p.d * (size_t)S->p.lda * sizeof(double));
+}
+double orc_get_l(const orc_state* S) { return S->l; }
+void orc_get_grad(const orc_state* S, double* g) { memcpy(g, S->g, (size_t)S->p.d * sizeof(double)); }
+int32_t orc_get_message(const orc_state* S, int32_t c, uint32_t* idx, double* val)
+{
+    const orc_client* C = &S->clients[c];
+    if (idx)
+        memcpy(idx, C->msg_idx, (size_t)C->msg_count * sizeof(uint32_t));
+    if (val)
+        memcpy(val, C->msg_val, (size_t)C->msg_count * sizeof(double));
+    return C->msg_count;
+}
+double orc_get_lk(const orc_state* S, int32_t c) { return S->clients[c].lk; }

@@ -1,0 +1,105 @@
+/*
+ * fednl_oracle.h -- CPU restatement of the u-FedNL (dopt) FedNL round, used as TEST
+ * INFRASTRUCTURE ONLY.
+ *
+ * This library is the parity checker for the GB300 kernels in ufednl_gb300/csrc.  Only the
+ * test-suite, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it; the product
+ * path (libfednl_gpu.so) never links, loads or calls it.
+ *
+ * Every function restates the reference algorithm in plain C and cites the reference file:line
+ * it follows (paths relative to the ufednl repository root).  The restatement is pinned by the
+ * golden vectors in tests/golden/, which were produced by compiling the reference's own headers
+ * (oracle/ref_harness.cpp, built by oracle/Makefile into oracle/_ref/).
+ */
+#ifndef FEDNL_ORACLE_H
+#define FEDNL_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Compressor ids: same numbering as enum Compressor, dopt/bin_fednl_local/include/UsedTypes.h:18-26 */
+#define ORC_IDENTITY 0
+#define ORC_RANDK    1
+#define ORC_TOPK     2
+#define ORC_RANDSEQK 3
+#define ORC_TOPLEK   4
+#define ORC_NATURAL  5
+
+typedef struct orc_problem {
+    int32_t d;                 /* dimension including the intercept column */
+    int32_t lda;               /* leading dimension of d x d matrices (AVX2 build: d rounded up to 4) */
+    int32_t n_clients;
+    const int32_t* n_samples;  /* [n_clients] */
+    const double* features;    /* [sum n_i][d] row-major, clients concatenated in order */
+    const double* labels;      /* [sum n_i], values in {-1,+1} */
+    double lambda;
+    int32_t compressor;        /* ORC_* */
+    int32_t k;                 /* compressor k (Identity/Natural: ignored, U is used) */
+    double alpha;              /* shift learning rate */
+    int32_t workers;           /* reference --workers W (client c runs on worker c mod W) */
+    int32_t threads;           /* OS threads this oracle uses for the client phase (<= workers) */
+    uint32_t seed_base;        /* RandK/RandSeqK client seed = seed_base + c (reference: 123) */
+    uint32_t toplek_seed;      /* initial seed of each worker's TopLEK generator (reference: 1234) */
+} orc_problem;
+
+typedef struct orc_state orc_state;
+
+/* ---- LCG generators (dopt/dopt/random) ------------------------------------------------- */
+uint32_t orc_lcg_int_next(uint32_t* state);          /* RandomGenIntegerLinear::generateInteger */
+double   orc_lcg_int_unit(uint32_t* state);          /* RandomGenIntegerLinear::generateRealInUnitInterval */
+double   orc_lcg_real_unit(uint32_t* state);         /* RandomGenRealLinear::generateRealInUnitInterval */
+size_t   orc_round_to_nearest(double v);             /* roundToNearestInt<size_t> */
+
+/* ---- index helpers and compressors ---------------------------------------------------- */
+size_t orc_upper_count(int32_t d);
+void   orc_upper_indices(int32_t d, int32_t lda, uint32_t* out);
+void   orc_shuffle_partial(uint32_t* arr, size_t n, size_t k, uint32_t* state);
+void   orc_randk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
+void   orc_randseqk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
+/* TopK over |m[upper[..]]| of a full d x lda column-major matrix; writes k sorted flat indices */
+int32_t orc_topk(const double* m, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
+/* TopLEK; frob_sq = squared L2 norm of the whole d x lda buffer; returns the count written */
+int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                   double delta, double frob_sq, uint32_t* rng_state, uint32_t* out);
+double  orc_natural(double v);                       /* mantissa truncation, MatrixNMD.h:2013-2031 */
+uint32_t orc_pack2_natural(double a, double b);      /* pack2FP64NoMantissa, FloatUtils.h:193-221 */
+double  orc_l2sq(const double* v, size_t n);
+
+/* ---- logistic-regression oracle (one client) ------------------------------------------ */
+/* atr: d x n col-major with leading dimension lda, column s = b_s * a_s */
+void orc_margin(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x, double* m);
+void orc_sigmoid(const double* m, int32_t n, double* sig);
+void orc_gradient(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x,
+                  const double* sig, double lambda, double* g);
+/* full symmetric d x lda Hessian (+lambda on the diagonal) */
+void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const double* sig,
+                 double lambda, double* h);
+
+/* ---- Option-B solve -------------------------------------------------------------------- */
+/* Cholesky of (upper(h) + l I) into ltr (d x lda, upper = R, lower = R^T); 1 on success */
+int  orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr);
+void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x);
+
+/* ---- whole FedNL run (forcesequpdate semantics: master merges clients in order) -------- */
+orc_state* orc_create(const orc_problem* p, const double* x0);
+void   orc_destroy(orc_state* s);
+/* one round; *grad_norm = ||aggregated gradient at the round's starting iterate|| */
+int    orc_round(orc_state* s, double* grad_norm);
+void   orc_get_x(const orc_state* s, double* x);
+void   orc_get_H(const orc_state* s, double* h);            /* master H, d x lda */
+void   orc_get_shift(const orc_state* s, int32_t c, double* sh);
+double orc_get_l(const orc_state* s);
+void   orc_get_grad(const orc_state* s, double* g);
+/* last round's message of client c: indices (flat) and values; returns count */
+int32_t orc_get_message(const orc_state* s, int32_t c, uint32_t* idx, double* val);
+/* last round's Lk of client c */
+double orc_get_lk(const orc_state* s, int32_t c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,327 @@
+// ref_harness.cpp -- drives the REFERENCE implementation (u-FedNL / dopt headers, compiled from
+// the reference source tree by oracle/Makefile into oracle/_ref/) to produce golden vectors for
+// tests/golden/.  TEST INFRASTRUCTURE ONLY: it is never part of the product library.
+//
+// The per-client step restates the worker loop of dopt/bin_fednl_local/include/
+// LocalWorkerForFedNL_{TopK,TopLEK,RandK,RandSeqK,Natural,Identical}.h and the master merge of
+// dopt/bin_fednl_local/include/TrainLoop.h:1092-1508 (with --debug forcesequpdate, i.e. the
+// master merges clients in order), calling the reference's own operators for every computation.
+// Worker threads are real std::threads that persist across rounds, so the TopLEK generator
+// (thread_local in SpecialMathRoutinesForMatrix.h:383) has exactly the reference's per-worker
+// streams.
+//
+// Binary formats are little-endian; see tests/golden/make_golden.py for the writer/reader.
+
+#include "dopt/linalg_vectors/include/VectorND_Raw.h"
+#include "dopt/linalg_matrices/include/MatrixNMD.h"
+#include "dopt/optimization_problems/include/ml/logistic_regression.h"
+#include "dopt/math_routines/include/SpecialMathRoutinesForMatrix.h"
+#include "dopt/linalg_matrices/include/factorization/CholeskyFactorization.h"
+#include "dopt/linalg_linsolvers/include/ElementarySolvers.h"
+#include "dopt/random/include/RandomGenIntegerLinear.h"
+#include "dopt/system/include/FloatUtils.h"
+
+#include <barrier>
+#include <cstdio>
+#include <cstring>
+#include <cstdint>
+#include <functional>
+#include <thread>
+#include <vector>
+
+typedef dopt::VectorNDRaw_d Vec;
+typedef dopt::MatrixNMD<Vec> Mat;
+typedef dopt::L2RegulirizeLogisticRegression<Mat, Vec, double> Problem;
+
+enum { kIdentity = 0, kRandK = 1, kTopK = 2, kRandSeqK = 3, kTopLEK = 4, kNatural = 5 };
+
+struct Reader {
+    FILE* f;
+    template <class T> T get() { T v; if (fread(&v, sizeof(T), 1, f) != 1) { fprintf(stderr, "short read\n"); exit(2); } return v; }
+    template <class T> void get(T* p, size_t n) { if (n && fread(p, sizeof(T), n, f) != n) { fprintf(stderr, "short read\n"); exit(2); } }
+};
+struct Writer {
+    FILE* f;
+    template <class T> void put(T v) { fwrite(&v, sizeof(T), 1, f); }
+    template <class T> void put(const T* p, size_t n) { if (n) fwrite(p, sizeof(T), n, f); }
+};
+
+struct Client {
+    Problem* prob = nullptr;
+    Mat shift;
+    Vec grad;
+    double lk = 0.0;
+    std::vector<uint32_t> idx;
+    std::vector<double> val;
+    dopt::RandomGenIntegerLinear rng;
+};
+
+// ---- run: whole FedNL (Option B) ---------------------------------------------------------
+static int cmd_run(const char* in_path, const char* out_path)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    Reader R{fi};
+    Writer W{fo};
+    int32_t d = R.get<int32_t>(), nc = R.get<int32_t>(), comp = R.get<int32_t>(), k = R.get<int32_t>();
+    int32_t nworkers = R.get<int32_t>(), rounds = R.get<int32_t>(), dump_rounds = R.get<int32_t>();
+    double lambda = R.get<double>(), alpha = R.get<double>();
+    std::vector<int32_t> ns(nc);
+    R.get(ns.data(), nc);
+    size_t S = 0;
+    for (int32_t c = 0; c < nc; ++c) S += ns[c];
+    std::vector<double> feat(S * d), lab(S);
+    R.get(feat.data(), feat.size());
+    R.get(lab.data(), lab.size());
+
+    if (nworkers > nc) nworkers = nc;
+    size_t U = ((size_t)d * (d + 1)) / 2;
+    if (comp == kIdentity || comp == kNatural) k = (int32_t)U;
+    double inv_n = 1.0 / double(nc);
+    double prescale = inv_n * alpha;
+
+    Vec x(d);                                   // x0 = 0 (RuntimeCfg x0 generator on [0,0])
+    Mat H = Mat::getZeroSquareMatrix(d);
+    std::vector<Client> cl(nc);
+    size_t off = 0;
+    for (int32_t c = 0; c < nc; ++c) {
+        Mat xt(d, ns[c]);
+        Vec b(ns[c]);
+        for (int32_t s = 0; s < ns[c]; ++s) {
+            for (int32_t i = 0; i < d; ++i) xt.set(i, s, feat[(off + s) * d + i]);
+            b.set(s, lab[off + s]);
+        }
+        off += ns[c];
+        cl[c].prob = new Problem(xt, b, lambda);
+        cl[c].rng.setSeed(uint32_t(123 + c));
+        cl[c].shift = cl[c].prob->evaluateHessian(x);
+        H += cl[c].shift;
+    }
+    H *= inv_n;
+    std::vector<uint32_t> upper = dopt::indiciesForUpperTriangularPart(H);
+    W.put<int32_t>((int32_t)H.LDA);
+
+    auto client_step = [&](Client& C) {
+        Problem* P = C.prob;
+        if (comp == kRandK)
+            C.idx = dopt::generateRandKItemsInUpperTriangularPart(C.rng, k, C.shift, upper);
+        else if (comp == kRandSeqK)
+            C.idx = dopt::generateRandSeqKItemsInUpperTriangularPart(C.rng, k, C.shift, upper);
+        Vec margin = P->evaluateClassificationMargin(x);
+        Vec sig = P->evaluateClassificationMarginSigmoid(margin);
+        C.grad = P->evaluateGradient(x, margin, sig);
+        Mat hess = P->evaluateHessian(x, margin, sig);
+        Mat diff = hess - C.shift;
+        C.lk = diff.frobeniusNormForSymmetricMatrixFromUpPart();
+        C.val.clear();
+        if (comp == kTopK || comp == kTopLEK) {
+            if (comp == kTopK) {
+                C.idx = dopt::getTopKFromUpperDiagonalPart<true>(diff, k, upper);
+            } else {
+                double delta = double(k) * (1.0 / double(U));
+                C.idx = dopt::getTopLEKFromUpperDiagonalPart<true>(diff, k, upper, delta);
+            }
+            for (uint32_t index : C.idx) {
+                double item = diff.matrixByCols.get(index);
+                C.val.push_back(item * prescale);
+                size_t ir = 0, jc = 0;
+                diff.getPositionFromFlatternIndex(ir, jc, index);
+                C.shift.matrixByCols[index] += alpha * item;
+                if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
+            }
+        } else if (comp == kRandK || comp == kRandSeqK) {
+            double mult = double(U) / double(k);
+            for (uint32_t index : C.idx) {
+                double item = diff.matrixByCols.get(index) * mult;
+                C.val.push_back(item * prescale);
+                size_t ir = 0, jc = 0;
+                diff.getPositionFromFlatternIndex(ir, jc, index);
+                C.shift.matrixByCols[index] += alpha * item;
+                if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
+            }
+        } else if (comp == kIdentity) {
+            C.idx = upper;
+            Mat sp = Mat::getZeroSquareMatrix(d);
+            for (int32_t j = 0; j < d; ++j)
+                for (int32_t i = 0; i <= j; ++i) {
+                    double item = diff.get(i, j);
+                    C.val.push_back(item * prescale);
+                    sp.set(i, j, item);
+                    sp.set(j, i, item);
+                }
+            C.shift += alpha * sp;
+        } else {  // natural: the master adds preScale * unpacked value
+            C.idx = upper;
+            Mat sp = diff;
+            sp.applyNaturalCompressor();
+            for (int32_t j = 0; j < d; ++j)
+                for (int32_t i = 0; i <= j; ++i) {
+                    auto pa = dopt::getFloatPointPack<DOPT_ARCH_LITTLE_ENDIAN>(sp.get(i, j));
+                    auto pb = pa;
+                    uint32_t packed = dopt::pack2FP64NoMantissa(pa, pb);
+                    dopt::FPComponentsPack<DOPT_ARCH_LITTLE_ENDIAN, double> un[2];
+                    dopt::unpack2FP64NoMantissa(un, packed);
+                    C.val.push_back(prescale * un[0].real_value_repr);
+                }
+            C.shift += alpha * sp;
+        }
+    };
+
+    // persistent worker threads, clients round-robin c -> c mod W (TrainLoop.h:664-686)
+    std::barrier start_bar(nworkers + 1), done_bar(nworkers + 1);
+    bool stop = false;
+    std::vector<std::thread> th;
+    for (int32_t w = 0; w < nworkers; ++w)
+        th.emplace_back([&, w]() {
+            for (;;) {
+                start_bar.arrive_and_wait();
+                if (stop) {
+                    // dopt vectors come from a thread_local pool: free them on the thread that made them
+                    for (int32_t c = w; c < nc; c += nworkers) cl[c].grad = Vec();
+                    return;
+                }
+                for (int32_t c = w; c < nc; c += nworkers) client_step(cl[c]);
+                done_bar.arrive_and_wait();
+            }
+        });
+
+    Mat Ltr;
+    for (int32_t r = 0; r < rounds; ++r) {
+        start_bar.arrive_and_wait();
+        done_bar.arrive_and_wait();
+        Vec g(d);
+        double l = 0.0;
+        for (int32_t c = 0; c < nc; ++c) {
+            g += cl[c].grad;
+            for (size_t t = 0; t < cl[c].idx.size(); ++t) H.matrixByCols[cl[c].idx[t]] += cl[c].val[t];
+            l += cl[c].lk;
+        }
+        g *= inv_n;
+        l *= inv_n;
+        bool ok = dopt::cholFactorization::choleskyFactorization<Mat, true, true>(Ltr, H, l);
+        Vec dx(d);
+        if (ok) {
+            Vec y = dopt::forwardSubstitutionWithATranspose(Ltr, g);
+            dx = dopt::backwardSubstitutionWithATranspose(Ltr, y);
+        }
+        x -= dx;
+        W.put<int32_t>(ok ? 1 : 0);
+        W.put<double>(g.vectorL2Norm());
+        W.put<double>(l);
+        W.put(x.dataConst(), (size_t)d);
+        if (r < dump_rounds) {
+            for (int32_t c = 0; c < nc; ++c) {
+                W.put<int32_t>((int32_t)cl[c].idx.size());
+                W.put(cl[c].idx.data(), cl[c].idx.size());
+                W.put(cl[c].val.data(), cl[c].val.size());
+                W.put<double>(cl[c].lk);
+            }
+        }
+    }
+    stop = true;
+    start_bar.arrive_and_wait();
+    for (auto& t : th) t.join();
+    for (auto& c : cl) delete c.prob;
+    fclose(fi);
+    fclose(fo);
+    return 0;
+}
+
+// ---- topk / toplek on given matrices (one OS thread => one TopLEK stream) ------------------
+static int cmd_select(const char* in_path, const char* out_path, bool lek)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    Reader R{fi};
+    Writer W{fo};
+    int32_t d = R.get<int32_t>(), k = R.get<int32_t>(), nm = R.get<int32_t>();
+    Mat m(d, d);
+    size_t U = ((size_t)d * (d + 1)) / 2;
+    std::vector<uint32_t> upper = dopt::indiciesForUpperTriangularPart(m);
+    W.put<int32_t>((int32_t)m.LDA);
+    std::vector<double> buf((size_t)d * d);
+    for (int32_t t = 0; t < nm; ++t) {
+        R.get(buf.data(), buf.size());          // column-major d x d (unpadded)
+        for (int32_t j = 0; j < d; ++j)
+            for (int32_t i = 0; i < d; ++i) m.set(i, j, buf[(size_t)j * d + i]);
+        std::vector<uint32_t> idx;
+        if (lek) idx = dopt::getTopLEKFromUpperDiagonalPart<true>(m, k, upper, double(k) * (1.0 / double(U)));
+        else idx = dopt::getTopKFromUpperDiagonalPart<true>(m, k, upper);
+        W.put<int32_t>((int32_t)idx.size());
+        W.put(idx.data(), idx.size());
+    }
+    fclose(fi);
+    fclose(fo);
+    return 0;
+}
+
+// ---- randk / randseqk draws for one client generator -------------------------------------
+static int cmd_rand(const char* out_path, int32_t d, int32_t k, uint32_t seed, int32_t draws, bool seq)
+{
+    FILE* fo = fopen(out_path, "wb");
+    if (!fo) return 1;
+    Writer W{fo};
+    Mat m(d, d);
+    std::vector<uint32_t> upper = dopt::indiciesForUpperTriangularPart(m);
+    dopt::RandomGenIntegerLinear g;
+    g.setSeed(seed);
+    W.put<int32_t>((int32_t)m.LDA);
+    for (int32_t t = 0; t < draws; ++t) {
+        std::vector<uint32_t> idx = seq ? dopt::generateRandSeqKItemsInUpperTriangularPart(g, k, m, upper)
+                                        : dopt::generateRandKItemsInUpperTriangularPart(g, k, m, upper);
+        W.put(idx.data(), idx.size());
+    }
+    fclose(fo);
+    return 0;
+}
+
+// ---- Cholesky Option-B solve on a given matrix --------------------------------------------
+static int cmd_chol(const char* in_path, const char* out_path)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    Reader R{fi};
+    Writer W{fo};
+    int32_t d = R.get<int32_t>();
+    double l = R.get<double>();
+    std::vector<double> buf((size_t)d * d), b(d);
+    R.get(buf.data(), buf.size());
+    R.get(b.data(), b.size());
+    Mat h(d, d);
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i < d; ++i) h.set(i, j, buf[(size_t)j * d + i]);
+    Vec g(d);
+    for (int32_t i = 0; i < d; ++i) g.set(i, b[i]);
+    Mat Ltr;
+    bool ok = dopt::cholFactorization::choleskyFactorization<Mat, true, true>(Ltr, h, l);
+    Vec x(d);
+    if (ok) {
+        Vec y = dopt::forwardSubstitutionWithATranspose(Ltr, g);
+        x = dopt::backwardSubstitutionWithATranspose(Ltr, y);
+    }
+    W.put<int32_t>(ok ? 1 : 0);
+    W.put(x.dataConst(), (size_t)d);
+    fclose(fi);
+    fclose(fo);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 3) {
+        fprintf(stderr, "usage: ref_harness run|topk|toplek|chol IN OUT | randk|randseqk OUT d k seed draws\n");
+        return 2;
+    }
+    if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3]);
+    if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
+    if (!strcmp(argv[1], "toplek")) return cmd_select(argv[2], argv[3], true);
+    if (!strcmp(argv[1], "chol")) return cmd_chol(argv[2], argv[3]);
+    if ((!strcmp(argv[1], "randk") || !strcmp(argv[1], "randseqk")) && argc >= 7)
+        return cmd_rand(argv[2], atoi(argv[3]), atoi(argv[4]), (uint32_t)strtoul(argv[5], 0, 10), atoi(argv[6]),
+                        !strcmp(argv[1], "randseqk"));
+    fprintf(stderr, "bad command\n");
+    return 2;
+}

@@ -1,0 +1,195 @@
+"""Regenerates the golden fixtures in this folder by running the REFERENCE implementation.
+
+The reference (u-FedNL / dopt) is compiled from its own sources into ``oracle/_ref/ref_harness``
+by ``make -C oracle ref`` (needs the reference source tree; this script never runs on the GPU
+box).  Each fixture stores seeded inputs and the reference's outputs:
+
+* ``run_<name>.npz``   whole FedNL runs (Option B, clients merged in order): per-round iterate,
+  ||g||, l and, for the first rounds, every client's message (indices and values) and Lk;
+* ``select_<name>.npz`` TopK / TopLEK index sets on given matrices (ties included);
+* ``rand_<name>.npz``   RandK / RandSeqK index draws of one client generator;
+* ``chol.npz``          Option-B Cholesky solves.
+
+Usage:  python tests/golden/make_golden.py [--ref-root PATH]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from ufednl_gb300 import datagen  # noqa: E402
+
+COMP = {"identity": 0, "randk": 1, "topk": 2, "randseqk": 3, "toplek": 4, "natural": 5}
+HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
+
+
+def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([prob.d, prob.n_clients, COMP[comp], k, workers, rounds, dump_rounds],
+                     dtype="<i4").tofile(f)
+            np.array([prob.lam, alpha], dtype="<f8").tofile(f)
+            prob.n_samples.astype("<i4").tofile(f)
+            prob.features.astype("<f8").tofile(f)
+            prob.labels.astype("<f8").tofile(f)
+        subprocess.run([HARNESS, "run", fin, fout], check=True)
+        raw = open(fout, "rb").read()
+    pos = 0
+
+    def take(dt, n):
+        nonlocal pos
+        a = np.frombuffer(raw, dtype=dt, count=n, offset=pos)
+        pos += a.nbytes
+        return a.copy()
+
+    lda = int(take("<i4", 1)[0])
+    d, nc = prob.d, prob.n_clients
+    ok, gnorm, lval, xs = [], [], [], []
+    msg_idx, msg_val, lks, msg_cnt = [], [], [], []
+    for r in range(rounds):
+        ok.append(int(take("<i4", 1)[0]))
+        gnorm.append(float(take("<f8", 1)[0]))
+        lval.append(float(take("<f8", 1)[0]))
+        xs.append(take("<f8", d))
+        if r < dump_rounds:
+            for c in range(nc):
+                cnt = int(take("<i4", 1)[0])
+                msg_cnt.append(cnt)
+                msg_idx.append(take("<u4", cnt))
+                msg_val.append(take("<f8", cnt))
+                lks.append(float(take("<f8", 1)[0]))
+    assert pos == len(raw)
+    np.savez_compressed(
+        os.path.join(HERE, f"run_{name}.npz"),
+        d=d, lda=lda, n_samples=prob.n_samples, features=prob.features, labels=prob.labels,
+        lam=prob.lam, compressor=comp, k=k, alpha=alpha, workers=workers, rounds=rounds,
+        dump_rounds=dump_rounds, ok=np.array(ok), gnorm=np.array(gnorm), l=np.array(lval),
+        x=np.array(xs), msg_count=np.array(msg_cnt, dtype=np.int32),
+        msg_idx=np.concatenate(msg_idx).astype(np.uint32), msg_val=np.concatenate(msg_val),
+        lk=np.array(lks))
+
+
+def select_case(name, mats, d, k, lek):
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([d, k, len(mats)], dtype="<i4").tofile(f)
+            for m in mats:
+                m.astype("<f8").T.copy().tofile(f)          # column-major d x d
+        subprocess.run([HARNESS, "toplek" if lek else "topk", fin, fout], check=True)
+        raw = open(fout, "rb").read()
+    lda = int(np.frombuffer(raw, "<i4", 1, 0)[0])
+    pos = 4
+    counts, idx = [], []
+    for _ in mats:
+        cnt = int(np.frombuffer(raw, "<i4", 1, pos)[0])
+        pos += 4
+        idx.append(np.frombuffer(raw, "<u4", cnt, pos).copy())
+        pos += 4 * cnt
+        counts.append(cnt)
+    np.savez_compressed(os.path.join(HERE, f"select_{name}.npz"), d=d, lda=lda, k=k,
+                        toplek=int(lek), mats=np.array(mats), counts=np.array(counts, dtype=np.int32),
+                        idx=np.concatenate(idx).astype(np.uint32))
+
+
+def rand_case(name, d, k, seed, draws, seq):
+    with tempfile.TemporaryDirectory() as td:
+        fout = os.path.join(td, "out.bin")
+        subprocess.run([HARNESS, "randseqk" if seq else "randk", fout, str(d), str(k), str(seed),
+                        str(draws)], check=True)
+        raw = open(fout, "rb").read()
+    lda = int(np.frombuffer(raw, "<i4", 1, 0)[0])
+    idx = np.frombuffer(raw, "<u4", draws * k, 4).reshape(draws, k).copy()
+    np.savez_compressed(os.path.join(HERE, f"rand_{name}.npz"), d=d, lda=lda, k=k, seed=seed,
+                        draws=draws, seq=int(seq), idx=idx)
+
+
+def chol_cases(rng):
+    outs = []
+    with tempfile.TemporaryDirectory() as td:
+        for d, l in ((9, 0.1), (33, 1e-3), (70, 0.0)):
+            a = rng.standard_normal((d, d + 4))
+            h = a @ a.T / d
+            b = rng.standard_normal(d)
+            fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+            with open(fin, "wb") as f:
+                np.array([d], dtype="<i4").tofile(f)
+                np.array([l], dtype="<f8").tofile(f)
+                h.astype("<f8").T.copy().tofile(f)
+                b.astype("<f8").tofile(f)
+            subprocess.run([HARNESS, "chol", fin, fout], check=True)
+            raw = open(fout, "rb").read()
+            ok = int(np.frombuffer(raw, "<i4", 1, 0)[0])
+            x = np.frombuffer(raw, "<f8", d, 4).copy()
+            outs.append((d, l, h, b, ok, x))
+    np.savez_compressed(os.path.join(HERE, "chol.npz"),
+                        **{f"h{i}": o[2] for i, o in enumerate(outs)},
+                        **{f"b{i}": o[3] for i, o in enumerate(outs)},
+                        **{f"x{i}": o[5] for i, o in enumerate(outs)},
+                        l=np.array([o[1] for o in outs]), ok=np.array([o[4] for o in outs]),
+                        n=len(outs))
+
+
+def tie_matrices(rng, d, count, levels):
+    mats = []
+    for t in range(count):
+        m = rng.integers(-levels, levels + 1, size=(d, d)).astype(np.float64) * 0.25
+        m = np.triu(m) + np.triu(m, 1).T
+        mats.append(m)
+    return mats
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-root", default=os.environ.get("REF_ROOT", "/root/reference/dopt"))
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_ROOT={args.ref_root}"],
+                   check=True)
+    rng = np.random.default_rng(20241203)
+
+    # whole runs: uneven clients, LDA padding (d=13 -> LDA 16), every compressor
+    small = datagen.binary_problem(11, 13, [20, 31, 17, 25, 40], 0.3, 1e-3)
+    U = 13 * 14 // 2
+    run_case("topk_d13", small, "topk", 26, 1.0, 2, 12, 4)
+    run_case("toplek_d13", small, "toplek", 39, 1.0, 2, 12, 4)
+    run_case("randk_d13", small, "randk", 26, 26 / U, 2, 12, 4)
+    run_case("randseqk_d13", small, "randseqk", 13, 13 / U, 2, 12, 4)
+    run_case("natural_d13", small, "natural", U, 1.0 / (1.0 + 1.0 / 8.0), 2, 12, 4)
+    run_case("identity_d13", small, "identity", U, 1.0, 2, 12, 4)
+    mid = datagen.binary_problem(12, 40, [60, 45, 80, 52, 71, 66, 49], 0.12, 1e-3)
+    run_case("topk_d40", mid, "topk", 320, 1.0, 3, 10, 3)
+    run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 10, 3)
+    dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
+    run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
+
+    # selections on tie-heavy and continuous matrices (one OS thread => one TopLEK stream)
+    ties = tie_matrices(rng, 12, 12, 3)
+    select_case("topk_ties_d12", ties, 12, 10, False)
+    select_case("toplek_ties_d12", ties, 12, 10, True)
+    cont = [np.triu(m) + np.triu(m, 1).T for m in rng.standard_normal((8, 30, 30))]
+    select_case("topk_cont_d30", cont, 30, 60, False)
+    select_case("toplek_cont_d30", cont, 30, 60, True)
+    few = tie_matrices(rng, 9, 10, 1)                 # values in {-0.25, 0, 0.25}: huge tie classes
+    select_case("topk_few_d9", few, 9, 7, False)
+    select_case("toplek_few_d9", few, 9, 7, True)
+
+    rand_case("randk_d20", 20, 40, 123, 6, False)
+    rand_case("randk_d301", 301, 2408, 124, 3, False)
+    rand_case("randseqk_d20", 20, 40, 125, 6, True)
+    rand_case("randseqk_d69", 69, 69, 126, 8, True)
+    chol_cases(rng)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,294 @@
+"""Parity of the GB300 kernels (through the C ABI) with the reference's own outputs (golden
+fixtures) and with the CPU oracle on the same seeded inputs.
+
+Bars: compressor index sets and RandK/RandSeqK draws bit-exact; shift updates and messages
+bit-exact given identical input matrices; FP64 iterates within 1e-10 relative (the sigmoid's exp
+differs between CUDA and glibc by at most an ulp, which is the only source of difference)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_path
+from ufednl_gb300 import datagen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from ufednl_gb300 import build, fednl
+    build.build()
+    fednl.load()
+    return fednl
+
+
+def _full(m, d, lda):
+    full = np.zeros((d, lda))
+    full[:, :d] = m.T
+    return full.reshape(-1)
+
+
+def _problem(z):
+    return datagen.Problem(int(z["d"]), z["n_samples"], z["features"], z["labels"], float(z["lam"]))
+
+
+# ---- compressors against the reference's golden vectors -----------------------------------
+
+@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("select_*.npz"))), ids=os.path.basename)
+def test_selection_golden(gpu, path):
+    z = np.load(path)
+    d, lda, k = int(z["d"]), int(z["lda"]), int(z["k"])
+    mats = np.stack([_full(m, d, lda) for m in z["mats"]])
+    pos = 0
+    if int(z["toplek"]):
+        ws = np.array([1234], dtype=np.uint32)         # one reference thread => one stream
+        got = gpu.get_toplek_from_upper_diagonal_part(mats, d, lda, k, ws)
+        for t, g in enumerate(got):
+            cnt = int(z["counts"][t])
+            np.testing.assert_array_equal(g, z["idx"][pos:pos + cnt])
+            pos += cnt
+    else:
+        got = gpu.get_topk_from_upper_diagonal_part(mats, d, lda, k)
+        for t in range(len(mats)):
+            np.testing.assert_array_equal(got[t], z["idx"][pos:pos + k])
+            pos += k
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("rand_*.npz"))), ids=os.path.basename)
+def test_random_draws_golden(gpu, path):
+    z = np.load(path)
+    d, lda, k = int(z["d"]), int(z["lda"]), int(z["k"])
+    st = np.array([int(z["seed"])], dtype=np.uint32)
+    for t in range(int(z["draws"])):
+        if int(z["seq"]):
+            got = gpu.generate_randseqk_items_in_upper_triangular_part(st, d, lda, k)
+        else:
+            got = gpu.generate_randk_items_in_upper_triangular_part(st, d, lda, k)
+        np.testing.assert_array_equal(got[0], z["idx"][t])
+
+
+def test_cholesky_golden(gpu):
+    z = np.load(golden_path("chol.npz"))
+    for i in range(int(z["n"])):
+        h = z[f"h{i}"]
+        d = h.shape[0]
+        dx = gpu.cholesky_option_b_solve(_full(h, d, d), d, d, float(z["l"][i]), z[f"b{i}"])
+        ref = z[f"x{i}"]
+        np.testing.assert_allclose(dx, ref, rtol=1e-10, atol=1e-10 * np.max(np.abs(ref)))
+
+
+def test_cholesky_known_answer_and_not_pd(gpu):
+    """CholeskyFactorizationGTest.cpp:11-40: L L^T with L = [[1,0,0],[4,7,0],[1,2,5]] is solved
+    exactly; [[1,2],[2,1]] is rejected as not positive definite."""
+    L = np.array([[1.0, 0, 0], [4, 7, 0], [1, 2, 5]])
+    A = L @ L.T
+    b = np.array([1.0, 2.0, 3.0])
+    dx = gpu.cholesky_option_b_solve(A.T.copy().ravel(), 3, 3, 0.0, b)
+    np.testing.assert_allclose(A @ dx, b, rtol=1e-14)
+    with pytest.raises(gpu.FedNLError) as e:
+        gpu.cholesky_option_b_solve(np.array([[1.0, 2.0], [2.0, 1.0]]).ravel(), 2, 2, 0.0, np.ones(2))
+    assert e.value.code == -4
+
+
+# ---- compressors against the oracle on larger, tie-heavy and continuous inputs -------------
+
+@pytest.mark.parametrize("d,k,kind", [(124, 992, "ties"), (301, 2408, "cont"), (301, 2408, "ties"),
+                                      (69, 69, "zeros"), (40, 1, "cont"), (40, 819, "cont"), (40, 820, "ties"),
+                                      (33, 560, "few")])
+def test_topk_toplek_vs_oracle(gpu, oracle, d, k, kind):
+    rng = np.random.default_rng(d * 1000 + k)
+    lda = (d + 3) // 4 * 4
+    mats = []
+    for t in range(6):
+        if kind == "ties":
+            m = rng.integers(-4, 5, size=(d, d)) * 0.125
+        elif kind == "few":
+            m = rng.integers(-1, 2, size=(d, d)) * 1.0
+        elif kind == "zeros":
+            m = rng.standard_normal((d, d)) * (rng.random((d, d)) < 0.02)
+        else:
+            m = rng.standard_normal((d, d))
+        m = np.triu(m) + np.triu(m, 1).T
+        mats.append(_full(m, d, lda))
+    mats = np.stack(mats)
+    got = gpu.get_topk_from_upper_diagonal_part(mats, d, lda, k)
+    for t in range(len(mats)):
+        np.testing.assert_array_equal(got[t], oracle.topk(mats[t], d, lda, k))
+    # TopLEK with two worker streams, matrices alternating between them
+    ws = np.array([1234, 1234], dtype=np.uint32)
+    wo = np.arange(len(mats)) % 2
+    got = gpu.get_toplek_from_upper_diagonal_part(mats, d, lda, k, ws, wo)
+    st = [np.array([1234], dtype=np.uint32), np.array([1234], dtype=np.uint32)]
+    for t in range(len(mats)):
+        np.testing.assert_array_equal(got[t], oracle.toplek(mats[t], d, lda, k, st[t % 2]))
+    assert ws[0] == st[0][0] and ws[1] == st[1][0]
+
+
+@pytest.mark.parametrize("d,k", [(301, 2408), (124, 992), (1024, 4096), (13, 91)])
+@pytest.mark.parametrize("seq", [False, True])
+def test_randk_randseqk_vs_oracle(gpu, oracle, d, k, seq):
+    lda = (d + 3) // 4 * 4
+    g_states = np.array([123 + c for c in range(5)], dtype=np.uint32)
+    o_states = [np.array([123 + c], dtype=np.uint32) for c in range(5)]
+    for _ in range(3):
+        if seq:
+            got = gpu.generate_randseqk_items_in_upper_triangular_part(g_states, d, lda, k)
+        else:
+            got = gpu.generate_randk_items_in_upper_triangular_part(g_states, d, lda, k)
+        for c in range(5):
+            ref = oracle.randseqk(o_states[c], d, lda, k) if seq else oracle.randk(o_states[c], d, lda, k)
+            np.testing.assert_array_equal(got[c], ref)
+            assert g_states[c] == o_states[c][0]
+
+
+def test_natural_vs_oracle(gpu, oracle):
+    rng = np.random.default_rng(7)
+    v = np.concatenate([rng.standard_normal(1001) * 10.0 ** rng.integers(-300, 300, 1001),
+                        [0.0, -0.0, 5e-324, -1e-310, np.inf, -np.inf]])
+    out, packed = gpu.apply_natural_compressor(v, with_packed=True)
+    L = oracle.lib()
+    ref = np.array([L.orc_natural(float(x)) for x in v])
+    np.testing.assert_array_equal(out.view(np.uint64), ref.view(np.uint64))
+    n = v.size
+    words = packed.reshape(-1, 3).astype(np.uint32)
+    words = words[:, 0] | (words[:, 1] << 8) | (words[:, 2] << 16)
+    for q in range(n // 2):
+        assert words[q] == L.orc_pack2_natural(float(v[2 * q]), float(v[2 * q + 1]))
+    # trailing block: (last, second-to-last) for an odd count
+    assert n % 2 == 1 and words[n // 2] == L.orc_pack2_natural(float(v[n - 1]), float(v[n - 2]))
+
+
+# ---- logistic oracle ------------------------------------------------------------------------
+
+@pytest.mark.parametrize("kind", ["binary", "dense"])
+def test_logreg_oracle_vs_cpu(gpu, oracle, kind):
+    d, n, lam = 37, 53, 1e-3
+    p = (datagen.binary_problem(3, d, [n], 0.2, lam) if kind == "binary" else datagen.dense_problem(3, d, [n], lam))
+    x = np.random.default_rng(1).standard_normal(d) * 0.3
+    g, h = gpu.evaluate_gradient_and_hessian(p.features, p.labels, lam, x)
+    lda = (d + 3) // 4 * 4
+    import ctypes as C
+    L = oracle.lib()
+    dp = C.POINTER(C.c_double)
+    atr = np.zeros((n, lda))
+    atr[:, :d] = p.features * p.labels[:, None]
+    atr = np.ascontiguousarray(atr.ravel())
+    m = np.empty(n)
+    sig = np.empty(n)
+    L.orc_margin(atr.ctypes.data_as(dp), d, lda, n, x.ctypes.data_as(dp), m.ctypes.data_as(dp))
+    L.orc_sigmoid(m.ctypes.data_as(dp), n, sig.ctypes.data_as(dp))
+    gr = np.empty(d)
+    hr = np.empty(d * lda)
+    L.orc_gradient(atr.ctypes.data_as(dp), d, lda, n, x.ctypes.data_as(dp), sig.ctypes.data_as(dp), lam,
+                   gr.ctypes.data_as(dp))
+    L.orc_hessian(atr.ctypes.data_as(dp), d, lda, n, sig.ctypes.data_as(dp), lam, hr.ctypes.data_as(dp))
+    np.testing.assert_allclose(g, gr, rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(h, hr, rtol=1e-13, atol=1e-15)
+
+
+# ---- whole runs -------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("run_*.npz"))), ids=os.path.basename)
+def test_run_golden(gpu, path):
+    z = np.load(path)
+    prob = _problem(z)
+    fed = gpu.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
+                    workers=int(z["workers"]))
+    pos = mi = 0
+    for r in range(int(z["rounds"])):
+        g = fed.round()
+        xr = z["x"][r]
+        np.testing.assert_allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
+        assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
+        assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + 1e-12 * np.max(z["l"])
+        if r < int(z["dump_rounds"]):
+            for c in range(prob.n_clients):
+                cnt = int(z["msg_count"][mi])
+                idx, val = fed.message(c)
+                np.testing.assert_array_equal(idx, z["msg_idx"][pos:pos + cnt])
+                ref = z["msg_val"][pos:pos + cnt]
+                if cnt:
+                    np.testing.assert_allclose(val, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
+                assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-12 * np.max(z["lk"])
+                pos += cnt
+                mi += 1
+    fed.close()
+
+
+def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None):
+    threads = threads or min(workers, os.cpu_count() or 1)
+    orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads)
+    fed = gpu.FedNL(prob, comp, k, alpha, workers=workers)
+    for r in range(rounds):
+        go = orc.round()
+        gg = fed.round()
+        xo = orc.x()
+        np.testing.assert_allclose(fed.x(), xo, rtol=1e-10, atol=1e-10 * np.max(np.abs(xo)),
+                                   err_msg=f"round {r}")
+        assert abs(gg - go) <= 1e-8 * go + 1e-13 * max(go, 1e-300) + 1e-15
+        for c in range(0, prob.n_clients, max(1, prob.n_clients // 7)):
+            io, vo = orc.message(c)
+            ig, vg = fed.message(c)
+            np.testing.assert_array_equal(ig, io, err_msg=f"round {r} client {c}")
+    fed.close()
+    orc.close()
+
+
+@pytest.mark.parametrize("comp", ["topk", "toplek", "randk", "randseqk", "natural", "identity"])
+def test_run_vs_oracle_small(gpu, oracle, comp):
+    prob = datagen.binary_problem(21, 30, [37, 52, 29, 61, 44, 33], 0.15, 1e-3)
+    U = 30 * 31 // 2
+    k = {"topk": 120, "toplek": 150, "randk": 60, "randseqk": 30, "natural": U, "identity": U}[comp]
+    alpha = {"randk": k / U, "randseqk": k / U, "natural": 8 / 9}.get(comp, 1.0)
+    _compare_runs(gpu, oracle, prob, comp, k, alpha, 8, workers=4)
+
+
+def test_run_vs_oracle_dense(gpu, oracle):
+    prob = datagen.dense_problem(22, 18, [31, 27, 40], 1e-2)
+    _compare_runs(gpu, oracle, prob, "topk", 36, 1.0, 6, workers=2)
+
+
+def test_run_vs_oracle_a9a_like_full_size(gpu, oracle):
+    """The a9a-like workload at its full size (d=124, 80 x 407, TopK k=8d, alpha=1)."""
+    prob = datagen.workload_a9a_like()
+    _compare_runs(gpu, oracle, prob, "topk", 8 * 124, 1.0, 4, workers=8, threads=os.cpu_count())
+
+
+def test_run_vs_oracle_w8a_like_full_size(gpu, oracle):
+    """The w8a-like workload at its full size (d=301, 142 clients, n_i 200-600, TopLEK k=8d)."""
+    prob = datagen.workload_w8a_like()
+    _compare_runs(gpu, oracle, prob, "toplek", 8 * 301, 1.0, 3, workers=8, threads=os.cpu_count())
+
+
+def test_run_is_deterministic(gpu):
+    prob = datagen.binary_problem(23, 40, [50, 61, 47, 55], 0.2, 1e-3)
+    xs = []
+    for _ in range(2):
+        fed = gpu.FedNL(prob, "toplek", 300, 1.0, workers=3)
+        g = fed.run(6)
+        xs.append((fed.x(), g))
+        fed.close()
+    assert xs[0][0].tobytes() == xs[1][0].tobytes()
+    assert xs[0][1].tobytes() == xs[1][1].tobytes()
+
+
+def test_run_converges_to_tolerance(gpu):
+    """FedNL with TopK on the a9a-like workload reaches ||grad|| <= 1e-9."""
+    prob = datagen.workload_a9a_like()
+    fed = gpu.FedNL(prob, "topk", 8 * 124, 1.0, workers=8)
+    g = fed.run(60)
+    assert np.min(g) <= 1e-9, g[-5:]
+    fed.close()
+
+
+def test_edge_cases(gpu, oracle):
+    # single-sample clients, k >= U for TopK/TopLEK, d = 1
+    prob = datagen.binary_problem(24, 6, [1, 3, 1], 0.5, 1e-2)
+    U = 21
+    for comp, k in (("topk", U), ("toplek", U + 5), ("topk", 1), ("toplek", 1)):
+        _compare_runs(gpu, oracle, prob, comp, k, 1.0, 3, workers=2)
+    one = datagen.Problem(1, np.array([4, 2], dtype=np.int32), np.ones((6, 1)),
+                          np.array([1.0, -1, 1, 1, -1, 1]), 1e-2)
+    _compare_runs(gpu, oracle, one, "topk", 1, 1.0, 3, workers=1)

@@ -1,0 +1,140 @@
+"""Pins the CPU oracle against golden vectors produced by the reference implementation itself
+(tests/golden/make_golden.py drives the reference's own operators) and against the reference
+test-suite's known answers.  Index sets must match bit for bit; FP64 values to within the
+ulp-level differences of SIMD summation order and exp (1e-12 relative); iterates to 1e-10."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_path
+from ufednl_gb300 import datagen
+
+RUNS = sorted(glob.glob(golden_path("run_*.npz")))
+SELECTS = sorted(glob.glob(golden_path("select_*.npz")))
+RANDS = sorted(glob.glob(golden_path("rand_*.npz")))
+
+
+def _problem(z):
+    return datagen.Problem(int(z["d"]), z["n_samples"], z["features"], z["labels"], float(z["lam"]))
+
+
+def _full(m, d, lda):
+    full = np.zeros((d, lda))
+    full[:, :d] = m.T          # full[j] = column j (column-major storage)
+    return full.reshape(-1)
+
+
+@pytest.mark.parametrize("path", RUNS, ids=lambda p: os.path.basename(p))
+def test_run_matches_reference(oracle, path):
+    z = np.load(path)
+    prob = _problem(z)
+    fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
+                       workers=int(z["workers"]))
+    pos = mi = 0
+    for r in range(int(z["rounds"])):
+        g = fed.round()
+        xr = z["x"][r]
+        np.testing.assert_allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
+        # ||g|| is compared relatively while it is well above the cancellation floor of the
+        # per-client gradient sums (~1e-15 of the first round's norm)
+        assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
+        # l = mean ||H_i - shift_i||_F cancels like ||g||: floor at 1e-12 of its largest value
+        lscale = 1e-12 * np.max(z["l"])
+        assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + lscale
+        if r < int(z["dump_rounds"]):
+            for c in range(prob.n_clients):
+                cnt = int(z["msg_count"][mi])
+                idx, val = fed.message(c)
+                np.testing.assert_array_equal(idx, z["msg_idx"][pos:pos + cnt])
+                ref = z["msg_val"][pos:pos + cnt]
+                if cnt:
+                    np.testing.assert_allclose(val, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
+                assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-12 * np.max(z["lk"])
+                pos += cnt
+                mi += 1
+    fed.close()
+
+
+@pytest.mark.parametrize("path", SELECTS, ids=lambda p: os.path.basename(p))
+def test_selection_matches_reference(oracle, path):
+    z = np.load(path)
+    d, lda, k = int(z["d"]), int(z["lda"]), int(z["k"])
+    state = np.array([1234], dtype=np.uint32)      # one reference worker thread => one stream
+    pos = 0
+    for t, m in enumerate(z["mats"]):
+        full = _full(m, d, lda)
+        got = oracle.toplek(full, d, lda, k, state) if int(z["toplek"]) else oracle.topk(full, d, lda, k)
+        cnt = int(z["counts"][t])
+        np.testing.assert_array_equal(got, z["idx"][pos:pos + cnt])
+        pos += cnt
+
+
+@pytest.mark.parametrize("path", RANDS, ids=lambda p: os.path.basename(p))
+def test_random_draws_match_reference(oracle, path):
+    z = np.load(path)
+    d, lda, k = int(z["d"]), int(z["lda"]), int(z["k"])
+    state = np.array([int(z["seed"])], dtype=np.uint32)
+    for t in range(int(z["draws"])):
+        got = oracle.randseqk(state, d, lda, k) if int(z["seq"]) else oracle.randk(state, d, lda, k)
+        np.testing.assert_array_equal(got, z["idx"][t])
+
+
+def test_cholesky_matches_reference(oracle):
+    z = np.load(golden_path("chol.npz"))
+    for i in range(int(z["n"])):
+        h = z[f"h{i}"]
+        d = h.shape[0]
+        ok, x = oracle.cholesky_solve(_full(h, d, d), d, d, float(z["l"][i]), z[f"b{i}"])
+        assert ok == bool(z["ok"][i])
+        np.testing.assert_allclose(x, z[f"x{i}"], rtol=1e-10, atol=1e-10 * np.max(np.abs(z[f"x{i}"])))
+
+
+def test_cholesky_known_answer(oracle):
+    """Known-answer case of dopt/bin_tests/src/linalg_matrices/CholeskyFactorizationGTest.cpp:11-40:
+    L = [[1,0,0],[4,7,0],[1,2,5]], A = L L^T is factored back into L exactly; [[1,2],[2,1]] is
+    rejected as not positive definite."""
+    L = np.array([[1.0, 0, 0], [4, 7, 0], [1, 2, 5]])
+    A = L @ L.T
+    lib = oracle.lib()
+    ltr = np.zeros(9)
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    assert lib.orc_cholesky(A.T.copy().ctypes.data_as(dp), 3, 3, 0.0, ltr.ctypes.data_as(dp)) == 1
+    R = ltr.reshape(3, 3).T           # row-major view: R[i][j] = ltr[j*3+i]
+    np.testing.assert_array_equal(np.triu(R), L.T)
+    bad = np.array([[1.0, 2.0], [2.0, 1.0]])
+    assert lib.orc_cholesky(bad.T.copy().ctypes.data_as(dp), 2, 2, 0.0, np.zeros(4).ctypes.data_as(dp)) == 0
+
+
+def test_natural_pack_layout(oracle):
+    """pack2FP64NoMantissa layout [signA(1) expA(11) signB(1) expB(11)] (FloatUtils.h:193-221)."""
+    lib = oracle.lib()
+    a, b = -3.75, 0.3
+    packed = lib.orc_pack2_natural(a, b)
+    assert packed >> 24 == 0
+    assert (packed >> 23) & 1 == 1 and (packed >> 11) & 1 == 0
+    assert (packed >> 12) & 0x7FF == 1024 and packed & 0x7FF == 1021
+    assert lib.orc_natural(a) == -2.0 and lib.orc_natural(b) == 0.25
+    assert lib.orc_natural(0.0) == 0.0
+
+
+def test_topk_structure(oracle):
+    """TopK returns min(k, U) distinct ascending upper flat indices; with k >= U every upper index.
+    The reference's heap (MinHeap.h:255-290) compares a node's children with the value that moved
+    up on the previous level, so the kept set is not always the k largest magnitudes; the golden
+    tests above pin that behaviour, and this test records one concrete instance of it."""
+    rng = np.random.default_rng(5)
+    d, lda = 17, 20
+    U = d * (d + 1) // 2
+    up = oracle.upper_indices(d, lda)
+    not_exact = 0
+    for k in (1, 5, 40, U - 1, U, U + 3):
+        m = rng.standard_normal((d, lda)).reshape(-1)
+        got = oracle.topk(m, d, lda, k)
+        assert len(got) == min(k, U)
+        assert np.all(np.diff(got.astype(np.int64)) > 0) and np.all(np.isin(got, up))
+        true = np.sort(up[np.argsort(-np.abs(m[up]), kind="stable")[:min(k, U)]])
+        not_exact += int(not np.array_equal(got, true))
+    assert not_exact >= 1

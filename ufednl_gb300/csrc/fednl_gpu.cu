@@ -1,0 +1,1009 @@
+// fednl_gpu.cu -- host side of the GB300 FedNL round engine behind the C ABI of
+// include/fednl_gpu.h.  One handle = one FedNL problem resident in HBM, one CUDA stream; a round
+// is a fixed sequence of kernel launches that is captured once into a CUDA graph and replayed.
+//
+// The host code replaces the reference's train() driver (dopt/bin_fednl_local/include/
+// TrainLoop.h:103-1863): client setup, the round loop and the master update; the worker
+// threads and message buffers of the reference become device kernels and device buffers.
+
+#include "fednl_gpu.h"
+#include "fednl_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace fednl;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(FEDNL_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                 \
+    } while (0)
+
+#define CKL()                                                                                      \
+    do {                                                                                           \
+        cudaError_t e_ = cudaGetLastError();                                                       \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(FEDNL_ECUDA, "kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_),   \
+                        __FILE__, __LINE__);                                                       \
+    } while (0)
+
+// device arena: one cudaMalloc, 256-byte aligned sub-buffers
+struct Arena {
+    char* base = nullptr;
+    size_t cap = 0, used = 0;
+    std::vector<std::pair<void**, size_t>> plan;
+    template <class T> void want(T** p, size_t count) { plan.push_back({(void**)p, count * sizeof(T)}); }
+    int commit()
+    {
+        size_t total = 0;
+        for (auto& q : plan) total += (q.second + 255) / 256 * 256;
+        if (total == 0) total = 256;
+        cudaError_t e = cudaMalloc((void**)&base, total);
+        if (e != cudaSuccess) return fail(FEDNL_ENOMEM, "cudaMalloc(%zu) failed: %s", total, cudaGetErrorString(e));
+        cap = total;
+        size_t off = 0;
+        for (auto& q : plan) {
+            *q.first = q.second ? (void*)(base + off) : nullptr;
+            off += (q.second + 255) / 256 * 256;
+        }
+        plan.clear();
+        return FEDNL_OK;
+    }
+    void release()
+    {
+        if (base) cudaFree(base);
+        base = nullptr;
+    }
+};
+
+int ensure_device()
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(FEDNL_ENODEV, "no CUDA device available");
+    return FEDNL_OK;
+}
+
+size_t select_smem(int k) { return (size_t)k * (sizeof(double) + sizeof(unsigned)); }
+
+}  // namespace
+
+struct fednl_handle_s {
+    fednl_problem_desc desc{};
+    std::vector<int32_t> ns, soff;
+    int d = 0, lda = 0, U = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
+    int binary = 0, maxn = 0, nfpart = 0, hcap = 0;
+    bool data_ready = false, shifts_ready = false;
+    cudaStream_t stream = nullptr;
+    Arena state, feat;
+    Dev dev{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    size_t hess_smem = 0;
+    bool hess_smem_bits = true;
+    int rounds_done = 0;
+    void* flush_buf = nullptr;
+    size_t flush_cap = 0;
+};
+
+namespace {
+
+struct Marks {
+    std::vector<cudaEvent_t>* ev = nullptr;   // one event per mark, recorded in order
+    std::vector<std::string>* names = nullptr;
+    size_t next = 0;
+};
+
+int mark(fednl_handle h, Marks* m, const char* name)
+{
+    if (!m) return FEDNL_OK;
+    if (m->names && m->names->size() <= m->next) m->names->push_back(name);
+    CK(cudaEventRecord((*m->ev)[m->next], h->stream));
+    m->next += 1;
+    return FEDNL_OK;
+}
+
+#define MARK(name)                                                                                 \
+    do {                                                                                           \
+        int rc_ = mark(h, M, name);                                                                \
+        if (rc_) return rc_;                                                                       \
+    } while (0)
+
+int launch_round(fednl_handle h, Marks* M = nullptr)
+{
+    Dev& P = h->dev;
+    cudaStream_t st = h->stream;
+    int S = h->S;
+    MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
+    if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    CKL();
+    MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
+    dim3 gg((h->d + 127) / 128, h->nc);
+    if (h->binary) k_grad_binary<<<gg, 128, 0, st>>>(P);
+    else k_grad_dense<<<gg, 128, 0, st>>>(P);
+    CKL();
+    MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
+    dim3 hg(h->nfpart, h->nc);
+    if (h->binary) {
+        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, 0);
+        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, 0);
+    } else {
+        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, 0);
+    }
+    CKL();
+    MARK("k_fsum");
+    k_fsum<<<(h->nc + 127) / 128, 128, 0, st>>>(P);
+    CKL();
+    int comp = h->comp;
+    if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
+        MARK("k_select");
+        double delta = (double)h->k * (1.0 / (double)h->U);
+        k_select<<<h->nc, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(P.diff, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F,
+                                                                  P.sel, h->SW, P.cnt, P.needs, P.pdraw, P.minidx);
+        CKL();
+        if (comp == FEDNL_TOPLEK) {
+            MARK("k_toplek_rng");
+            k_toplek_rng<<<(h->W + 31) / 32, 32, 0, st>>>(h->nc, h->W, nullptr, P.wstate, P.needs, P.pdraw, P.minidx,
+                                                         P.sel, h->SW, P.cnt);
+            CKL();
+        }
+    } else if (comp == FEDNL_RANDK) {
+        MARK("k_randk");
+        k_randk<<<h->nc, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.hmap, h->hcap, P.sel, h->SW, P.cnt);
+        CKL();
+    } else if (comp == FEDNL_RANDSEQK) {
+        MARK("k_randseqk");
+        k_randseqk<<<h->nc, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt);
+        CKL();
+    }
+    MARK("k_apply");
+    k_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
+    CKL();
+    MARK("k_aggregate");
+    k_aggregate<<<1, kAggThreads, 0, st>>>(P);
+    CKL();
+    MARK("k_chol_solve");
+    k_chol_solve<<<1, kCholThreads, 0, st>>>(P, P.H, P.stats + 1, 0.0, P.g, P.dx, P.x, 1);
+    CKL();
+    MARK("end");
+    return FEDNL_OK;
+}
+
+int build_graph(fednl_handle h)
+{
+    if (h->gexec) return FEDNL_OK;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_round(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc != FEDNL_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(FEDNL_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    h->graph = g;
+    CK(cudaGraphInstantiate(&h->gexec, g, 0));
+    return FEDNL_OK;
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+const char* fednl_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
+{
+    if (!desc || !out) return fail(FEDNL_EINVAL, "null argument");
+    *out = nullptr;
+    int rc = ensure_device();
+    if (rc) return rc;
+    const fednl_problem_desc& D = *desc;
+    if (D.d < 1 || D.n_clients < 1 || !D.n_samples) return fail(FEDNL_EINVAL, "d and n_clients must be >= 1");
+    if (D.compressor < 0 || D.compressor > 5) return fail(FEDNL_EINVAL, "unknown compressor %d", D.compressor);
+    for (int i = 0; i < 4; ++i)
+        if (D.reserved[i]) return fail(FEDNL_EINVAL, "reserved fields must be zero");
+    int lda = D.lda ? D.lda : (D.d + 3) / 4 * 4;
+    if (lda < D.d) return fail(FEDNL_EINVAL, "lda %d < d %d", lda, D.d);
+    long long U = (long long)D.d * (D.d + 1) / 2;
+    if (U >= (1ll << 31) || (long long)D.d * lda >= (1ll << 32))
+        return fail(FEDNL_EINVAL, "d too large for 32-bit flat indices");
+    int k = (D.compressor == FEDNL_IDENTITY || D.compressor == FEDNL_NATURAL) ? (int)U : D.k;
+    if (k < 1) return fail(FEDNL_EINVAL, "k must be >= 1");
+    if ((D.compressor == FEDNL_RANDK || D.compressor == FEDNL_RANDSEQK) && k > U)
+        return fail(FEDNL_EINVAL, "k %d larger than U %lld", k, U);
+    if ((D.compressor == FEDNL_TOPK || D.compressor == FEDNL_TOPLEK) && k < U && k > kMaxK)
+        return fail(FEDNL_EINVAL, "TopK/TopLEK k %d above the shared-memory heap limit %d", k, kMaxK);
+
+    fednl_handle h = new fednl_handle_s();
+    h->desc = D;
+    h->d = D.d;
+    h->lda = lda;
+    h->U = (int)U;
+    h->nc = D.n_clients;
+    h->k = k;
+    h->comp = D.compressor;
+    h->W = std::max(1, std::min(D.workers < 1 ? 1 : D.workers, D.n_clients));  // TrainLoop.h:194-199
+    h->SW = (h->U + 31) / 32;
+    h->ns.assign(D.n_samples, D.n_samples + D.n_clients);
+    h->soff.assign(h->nc + 1, 0);
+    for (int c = 0; c < h->nc; ++c) {
+        if (h->ns[c] < 1) {
+            delete h;
+            return fail(FEDNL_EINVAL, "client %d has no samples", c);
+        }
+        h->soff[c + 1] = h->soff[c] + h->ns[c];
+        h->maxn = std::max(h->maxn, h->ns[c]);
+    }
+    h->S = h->soff[h->nc];
+    h->nfpart = (h->U + kHessPerBlock - 1) / kHessPerBlock;
+    h->hcap = 1;
+    if (h->comp == FEDNL_RANDK)
+        while (h->hcap < 4 * k) h->hcap <<= 1;
+
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(FEDNL_ECUDA, "cudaStreamCreate failed");
+    }
+    Dev& P = h->dev;
+    P.d = h->d;
+    P.lda = h->lda;
+    P.U = h->U;
+    P.nc = h->nc;
+    P.k = h->k;
+    P.comp = h->comp;
+    P.W = h->W;
+    P.SW = h->SW;
+    P.nfpart = h->nfpart;
+    P.hcap = h->hcap;
+    P.lambda = D.lambda;
+    P.alpha = D.alpha;
+    P.inv_n = 1.0 / (double)h->nc;
+    P.prescale = P.inv_n * D.alpha;                          // TrainLoop.h:531
+    P.mult = (double)h->U / (double)h->k;                    // RandK.h:90
+    P.hist_cap = 1 << 16;
+    size_t ncU = (size_t)h->nc * h->U;
+    Arena& A = h->state;
+    A.want((int**)&P.ns, h->nc);
+    A.want((int**)&P.soff, h->nc + 1);
+    A.want((int**)&P.client_of, h->S);
+    A.want(&P.x, h->d);
+    A.want(&P.H, h->U);
+    A.want(&P.g, h->d);
+    A.want(&P.shift, ncU);
+    A.want(&P.diff, ncU);
+    A.want(&P.Dv, h->S);
+    A.want(&P.qb, h->S);
+    A.want(&P.gc, (size_t)h->nc * h->d);
+    A.want(&P.Fpart, (size_t)h->nc * h->nfpart);
+    A.want(&P.F, h->nc);
+    A.want(&P.lk, h->nc);
+    A.want(&P.sel, (size_t)h->nc * h->SW);
+    A.want(&P.cnt, h->nc);
+    A.want(&P.needs, h->nc);
+    A.want(&P.pdraw, h->nc);
+    A.want(&P.minidx, h->nc);
+    A.want(&P.wstate, h->W);
+    A.want(&P.rstate, h->nc);
+    A.want(&P.rseq, h->nc);
+    A.want(&P.hmap, (size_t)h->nc * h->hcap);
+    A.want(&P.work, h->U);
+    A.want(&P.dx, h->d);
+    A.want(&P.ybuf, h->d);
+    A.want(&P.hist, P.hist_cap);
+    A.want(&P.round_ctr, 1);
+    A.want(&P.status, 1);
+    A.want(&P.stats, 2);
+    rc = A.commit();
+    if (rc) {
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return rc;
+    }
+    std::vector<int> client_of(h->S);
+    for (int c = 0; c < h->nc; ++c)
+        for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) client_of[s] = c;
+    if (cudaMemcpy((void*)P.ns, h->ns.data(), h->nc * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((void*)P.soff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((void*)P.client_of, client_of.data(), (size_t)h->S * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(P.x, 0, h->d * 8) != cudaSuccess || cudaMemset(P.round_ctr, 0, 4) != cudaSuccess ||
+        cudaMemset(P.status, 0, 4) != cudaSuccess) {
+        fednl_gpu_destroy(h);
+        return fail(FEDNL_ECUDA, "initial copies failed");
+    }
+    if (select_smem(h->k) > 48 * 1024 && h->k < h->U)
+        cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(h->k));
+    *out = h;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_destroy(fednl_handle h)
+{
+    if (!h) return FEDNL_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->state.release();
+    h->feat.release();
+    if (h->flush_buf) cudaFree(h->flush_buf);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
+{
+    if (!h || !features || !labels) return fail(FEDNL_EINVAL, "null argument");
+    int d = h->d, S = h->S;
+    for (int s = 0; s < S; ++s)
+        if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
+    int fmt = h->desc.feature_format;
+    if (fmt == FEDNL_FEATURES_AUTO) {
+        fmt = FEDNL_FEATURES_BINARY;
+        for (size_t t = 0; t < (size_t)S * d; ++t)
+            if (features[t] != 0.0 && features[t] != 1.0) {
+                fmt = FEDNL_FEATURES_DENSE;
+                break;
+            }
+    }
+    h->feat.release();
+    Dev& P = h->dev;
+    P.rowptr = nullptr;
+    P.colidx = nullptr;
+    P.fbits = nullptr;
+    P.A = nullptr;
+    double* lab = nullptr;
+    if (fmt == FEDNL_FEATURES_BINARY) {
+        std::vector<int> rowptr(S + 1, 0), colidx;
+        std::vector<long long> fboff(h->nc);
+        long long words = 0;
+        for (int c = 0; c < h->nc; ++c) {
+            fboff[c] = words;
+            words += (long long)d * ((h->ns[c] + 63) / 64);
+        }
+        std::vector<unsigned long long> fbits(words, 0ull);
+        for (int c = 0; c < h->nc; ++c) {
+            int W = (h->ns[c] + 63) / 64;
+            for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+                const double* a = features + (size_t)s * d;
+                int ls = s - h->soff[c];
+                for (int i = 0; i < d; ++i) {
+                    if (a[i] == 1.0) {
+                        colidx.push_back(i);
+                        fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
+                    } else if (a[i] != 0.0) {
+                        return fail(FEDNL_EINVAL, "feature (%d,%d) is not 0/1 in binary format", s, i);
+                    }
+                }
+                rowptr[s + 1] = (int)colidx.size();
+            }
+        }
+        int *d_rowptr, *d_colidx;
+        long long* d_fboff;
+        unsigned long long* d_fbits;
+        h->feat.want(&d_rowptr, S + 1);
+        h->feat.want(&d_colidx, std::max<size_t>(1, colidx.size()));
+        h->feat.want(&d_fboff, h->nc);
+        h->feat.want(&d_fbits, std::max<long long>(1, words));
+        h->feat.want(&lab, S);
+        int rc = h->feat.commit();
+        if (rc) return rc;
+        CK(cudaMemcpy(d_rowptr, rowptr.data(), (S + 1) * 4, cudaMemcpyHostToDevice));
+        if (!colidx.empty()) CK(cudaMemcpy(d_colidx, colidx.data(), colidx.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_fboff, fboff.data(), h->nc * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_fbits, fbits.data(), words * 8, cudaMemcpyHostToDevice));
+        P.rowptr = d_rowptr;
+        P.colidx = d_colidx;
+        P.fboff = d_fboff;
+        P.fbits = d_fbits;
+        int maxW = (h->maxn + 63) / 64;
+        size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8;
+        h->hess_smem_bits = need <= 200 * 1024;
+        h->hess_smem = h->hess_smem_bits ? need : (size_t)h->maxn * 8;
+        if (h->hess_smem > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
+        if (h->hess_smem_bits)
+            CK(cudaFuncSetAttribute(k_hess_binary<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
+        else
+            CK(cudaFuncSetAttribute(k_hess_binary<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
+        h->binary = 1;
+    } else {
+        double* dA;
+        h->feat.want(&dA, (size_t)S * d);
+        h->feat.want(&lab, S);
+        int rc = h->feat.commit();
+        if (rc) return rc;
+        CK(cudaMemcpy(dA, features, (size_t)S * d * 8, cudaMemcpyHostToDevice));
+        P.A = dA;
+        h->binary = 0;
+    }
+    CK(cudaMemcpy(lab, labels, (size_t)S * 8, cudaMemcpyHostToDevice));
+    P.lab = lab;
+    h->data_ready = true;
+    h->shifts_ready = false;
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
+    }
+    return FEDNL_OK;
+}
+
+int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->data_ready) return fail(FEDNL_EINVAL, "upload client data first");
+    Dev& P = h->dev;
+    cudaStream_t st = h->stream;
+    if (x0) CK(cudaMemcpyAsync(P.x, x0, h->d * 8, cudaMemcpyHostToDevice, st));
+    else CK(cudaMemsetAsync(P.x, 0, h->d * 8, st));
+    int S = h->S;
+    if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    CKL();
+    dim3 hg(h->nfpart, h->nc);
+    if (h->binary) {
+        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, 1);
+        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, 1);
+    } else {
+        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, 1);
+    }
+    CKL();
+    k_h_init<<<(h->U + 255) / 256, 256, 0, st>>>(P);
+    CKL();
+    std::vector<unsigned> ws(h->W, h->desc.toplek_seed), rs(h->nc);
+    for (int c = 0; c < h->nc; ++c) rs[c] = h->desc.seed_base + (unsigned)c;   // TrainLoop.h:632
+    CK(cudaMemcpyAsync(P.wstate, ws.data(), h->W * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(P.rstate, rs.data(), h->nc * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(P.round_ctr, 0, 4, st));
+    CK(cudaMemsetAsync(P.status, 0, 4, st));
+    CK(cudaStreamSynchronize(st));
+    h->shifts_ready = true;
+    h->rounds_done = 0;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_run(fednl_handle h, int32_t rounds, double* grad_norms)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    if (rounds < 0) return fail(FEDNL_EINVAL, "rounds < 0");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(h->dev.status, 0, 4, h->stream));
+    for (int r = 0; r < rounds; ++r) CK(cudaGraphLaunch(h->gexec, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int first = h->rounds_done;
+    h->rounds_done += rounds;
+    if (grad_norms && rounds > 0) {
+        int have = std::max(0, std::min(rounds, h->dev.hist_cap - first));
+        if (have > 0) CK(cudaMemcpy(grad_norms, h->dev.hist + first, (size_t)have * 8, cudaMemcpyDeviceToHost));
+        for (int r = have; r < rounds; ++r) grad_norms[r] = NAN;
+    }
+    int status = 0;
+    CK(cudaMemcpy(&status, h->dev.status, 4, cudaMemcpyDeviceToHost));
+    if (status) return fail(status, "Option-B matrix not positive definite in one of the rounds");
+    return FEDNL_OK;
+}
+
+int fednl_gpu_round(fednl_handle h, fednl_round_stats* stats)
+{
+    double gn = 0.0;
+    int rc = fednl_gpu_run(h, 1, &gn);
+    if (stats) {
+        stats->round = h ? h->rounds_done - 1 : -1;
+        stats->status = rc == FEDNL_ENOTPD ? FEDNL_ENOTPD : FEDNL_OK;
+        double st[2] = {0, 0};
+        if (h) cudaMemcpy(st, h->dev.stats, 16, cudaMemcpyDeviceToHost);
+        stats->grad_norm = st[0];
+        stats->l = st[1];
+    }
+    return rc;
+}
+
+int fednl_gpu_get_x(fednl_handle h, double* x)
+{
+    if (!h || !x) return fail(FEDNL_EINVAL, "null argument");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(x, h->dev.x, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_set_x(fednl_handle h, const double* x)
+{
+    if (!h || !x) return fail(FEDNL_EINVAL, "null argument");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(h->dev.x, x, h->d * 8, cudaMemcpyHostToDevice));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_grad(fednl_handle h, double* g)
+{
+    if (!h || !g) return fail(FEDNL_EINVAL, "null argument");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(g, h->dev.g, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+static int packed_to_full(fednl_handle h, const double* dsrc, double* out)
+{
+    std::vector<double> up(h->U);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(up.data(), dsrc, (size_t)h->U * 8, cudaMemcpyDeviceToHost));
+    int d = h->d, lda = h->lda;
+    std::fill(out, out + (size_t)d * lda, 0.0);
+    size_t p = 0;
+    for (int j = 0; j < d; ++j)
+        for (int i = 0; i <= j; ++i, ++p) {
+            out[(size_t)j * lda + i] = up[p];
+            out[(size_t)i * lda + j] = up[p];
+        }
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_H(fednl_handle h, double* H)
+{
+    if (!h || !H) return fail(FEDNL_EINVAL, "null argument");
+    return packed_to_full(h, h->dev.H, H);
+}
+
+int fednl_gpu_get_shift(fednl_handle h, int32_t client, double* shift)
+{
+    if (!h || !shift || client < 0 || client >= h->nc) return fail(FEDNL_EINVAL, "bad argument");
+    return packed_to_full(h, h->dev.shift + (size_t)client * h->U, shift);
+}
+
+double fednl_gpu_get_l(fednl_handle h)
+{
+    if (!h) return NAN;
+    double st[2] = {NAN, NAN};
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(st, h->dev.stats, 16, cudaMemcpyDeviceToHost);
+    return st[1];
+}
+
+double fednl_gpu_get_lk(fednl_handle h, int32_t client)
+{
+    if (!h || client < 0 || client >= h->nc) return NAN;
+    double v = NAN;
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(&v, h->dev.lk + client, 8, cudaMemcpyDeviceToHost);
+    return v;
+}
+
+int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double* val, int32_t* count)
+{
+    if (!h || client < 0 || client >= h->nc || !count) return fail(FEDNL_EINVAL, "bad argument");
+    CK(cudaStreamSynchronize(h->stream));
+    int U = h->U, lda = h->lda;
+    std::vector<double> dv(U);
+    std::vector<unsigned> sel(h->SW);
+    CK(cudaMemcpy(dv.data(), h->dev.diff + (size_t)client * U, (size_t)U * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sel.data(), h->dev.sel + (size_t)client * h->SW, (size_t)h->SW * 4, cudaMemcpyDeviceToHost));
+    std::vector<int> order;
+    int comp = h->comp;
+    if (comp == FEDNL_IDENTITY || comp == FEDNL_NATURAL) {
+        order.resize(U);
+        for (int p = 0; p < U; ++p) order[p] = p;
+    } else if (comp == FEDNL_RANDSEQK) {
+        int r = 0;
+        CK(cudaMemcpy(&r, h->dev.rseq + client, 4, cudaMemcpyDeviceToHost));
+        for (int t = 0; t < h->k; ++t) order.push_back((r + t) % U);
+    } else {
+        for (int p = 0; p < U; ++p)
+            if ((sel[p >> 5] >> (p & 31)) & 1u) order.push_back(p);
+    }
+    const Dev& P = h->dev;
+    // positions -> flat indices j * lda + i
+    std::vector<int> colj(U), rowi(U);
+    {
+        int p = 0;
+        for (int j = 0; j < h->d; ++j)
+            for (int i = 0; i <= j; ++i, ++p) {
+                colj[p] = j;
+                rowi[p] = i;
+            }
+    }
+    *count = (int32_t)order.size();
+    for (size_t t = 0; t < order.size(); ++t) {
+        int p = order[t];
+        if (idx) idx[t] = (uint32_t)colj[p] * (uint32_t)lda + (uint32_t)rowi[p];
+        if (val) {
+            double item = dv[p];
+            if (comp == FEDNL_NATURAL) {
+                uint64_t b;
+                memcpy(&b, &item, 8);
+                b &= ~((1ull << 52) - 1);
+                memcpy(&item, &b, 8);
+                val[t] = P.prescale * item;
+            } else {
+                if (comp == FEDNL_RANDK || comp == FEDNL_RANDSEQK) item = item * P.mult;
+                val[t] = item * P.prescale;
+            }
+        }
+    }
+    return FEDNL_OK;
+}
+
+// ---- operator-level entry points -------------------------------------------------------------
+
+namespace {
+struct Scratch {
+    Arena a;
+    cudaStream_t st = nullptr;
+    ~Scratch()
+    {
+        if (st) cudaStreamSynchronize(st);
+        a.release();
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek, int n_workers,
+                  const int32_t* worker_of, uint32_t* wstates, uint32_t* idx, int32_t* counts)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!mats || !idx || n_mat < 1 || d < 1 || lda < d || k < 1) return fail(FEDNL_EINVAL, "bad argument");
+    long long U = (long long)d * (d + 1) / 2;
+    if (k < U && k > kMaxK) return fail(FEDNL_EINVAL, "k above %d", kMaxK);
+    int SW = (int)((U + 31) / 32);
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *dfull, *dpack, *dF, *dp;
+    unsigned *dsel, *dws = nullptr;
+    int *dcnt, *dneeds, *dmi, *dwo = nullptr;
+    size_t full = (size_t)d * lda;
+    s.a.want(&dfull, (size_t)n_mat * full);
+    s.a.want(&dpack, (size_t)n_mat * U);
+    s.a.want(&dF, n_mat);
+    s.a.want(&dp, n_mat);
+    s.a.want(&dsel, (size_t)n_mat * SW);
+    s.a.want(&dcnt, n_mat);
+    s.a.want(&dneeds, n_mat);
+    s.a.want(&dmi, n_mat);
+    if (lek) {
+        s.a.want(&dws, std::max(1, n_workers));
+        s.a.want(&dwo, n_mat);
+    }
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dfull, mats, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
+    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), n_mat), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
+    CKL();
+    k_l2sq_full<<<n_mat, 256, 0, s.st>>>(dfull, (long long)full, dF);
+    CKL();
+    if (select_smem(k) > 48 * 1024 && k < U)
+        CK(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(k)));
+    double delta = (double)k * (1.0 / (double)U);
+    k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)U, k, lek ? 1 : 0, delta, dF, dsel, SW,
+                                                                      dcnt, dneeds, dp, dmi);
+    CKL();
+    if (lek) {
+        int W = std::max(1, n_workers);
+        std::vector<int> wo(n_mat);
+        for (int t = 0; t < n_mat; ++t) {
+            wo[t] = worker_of ? worker_of[t] : 0;
+            if (wo[t] < 0 || wo[t] >= W) return fail(FEDNL_EINVAL, "worker_of[%d] out of range", t);
+        }
+        CK(cudaMemcpyAsync(dwo, wo.data(), n_mat * 4, cudaMemcpyHostToDevice, s.st));
+        CK(cudaMemcpyAsync(dws, wstates, W * 4, cudaMemcpyHostToDevice, s.st));
+        k_toplek_rng<<<(W + 31) / 32, 32, 0, s.st>>>(n_mat, W, dwo, dws, dneeds, dp, dmi, dsel, SW, dcnt);
+        CKL();
+        CK(cudaMemcpyAsync(wstates, dws, W * 4, cudaMemcpyDeviceToHost, s.st));
+    }
+    std::vector<unsigned> sel((size_t)n_mat * SW);
+    CK(cudaMemcpyAsync(sel.data(), dsel, sel.size() * 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    for (int t = 0; t < n_mat; ++t) {
+        int w = 0;
+        long long p = 0;
+        uint32_t* o = idx + (size_t)t * k;
+        for (int j = 0; j < d; ++j)
+            for (int i = 0; i <= j; ++i, ++p)
+                if ((sel[(size_t)t * SW + (p >> 5)] >> (p & 31)) & 1u) {
+                    if (w < k) o[w] = (uint32_t)j * (uint32_t)lda + (uint32_t)i;
+                    ++w;
+                }
+        if (counts) counts[t] = w;
+    }
+    return FEDNL_OK;
+}
+
+int rand_common(uint32_t* states, int n_gen, int d, int lda, int k, uint32_t* idx, bool seq)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    long long U = (long long)d * (d + 1) / 2;
+    if (!states || !idx || n_gen < 1 || d < 1 || lda < d || k < 1 || k > U) return fail(FEDNL_EINVAL, "bad argument");
+    int SW = (int)((U + 31) / 32);
+    int hcap = 1;
+    while (hcap < 4 * k) hcap <<= 1;
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    unsigned *dst, *dsel;
+    int *dcnt, *drseq;
+    unsigned long long* dmap = nullptr;
+    s.a.want(&dst, n_gen);
+    s.a.want(&dsel, (size_t)n_gen * SW);
+    s.a.want(&dcnt, n_gen);
+    s.a.want(&drseq, n_gen);
+    if (!seq) s.a.want(&dmap, (size_t)n_gen * hcap);
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dst, states, n_gen * 4, cudaMemcpyHostToDevice, s.st));
+    if (seq) k_randseqk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, drseq, dsel, SW, dcnt);
+    else k_randk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, dmap, hcap, dsel, SW, dcnt);
+    CKL();
+    std::vector<unsigned> sel((size_t)n_gen * SW);
+    std::vector<int> rseq(n_gen);
+    CK(cudaMemcpyAsync(sel.data(), dsel, sel.size() * 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(rseq.data(), drseq, n_gen * 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(states, dst, n_gen * 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    std::vector<uint32_t> flat(U);
+    {
+        long long p = 0;
+        for (int j = 0; j < d; ++j)
+            for (int i = 0; i <= j; ++i, ++p) flat[p] = (uint32_t)j * (uint32_t)lda + (uint32_t)i;
+    }
+    for (int t = 0; t < n_gen; ++t) {
+        uint32_t* o = idx + (size_t)t * k;
+        if (seq) {
+            for (int q = 0; q < k; ++q) o[q] = flat[(rseq[t] + (long long)q) % U];
+        } else {
+            int w = 0;
+            for (long long p = 0; p < U; ++p)
+                if ((sel[(size_t)t * SW + (p >> 5)] >> (p & 31)) & 1u) o[w++] = flat[p];
+        }
+    }
+    return FEDNL_OK;
+}
+}  // namespace
+
+int fednl_gpu_topk(const double* mats, int32_t n_mat, int32_t d, int32_t lda, int32_t k, uint32_t* idx)
+{
+    return select_common(mats, n_mat, d, lda, k, false, 1, nullptr, nullptr, idx, nullptr);
+}
+
+int fednl_gpu_toplek(const double* mats, int32_t n_mat, int32_t d, int32_t lda, int32_t k, int32_t n_workers,
+                     const int32_t* worker_of, uint32_t* worker_states, uint32_t* idx, int32_t* counts)
+{
+    if (!worker_states || n_workers < 1) return fail(FEDNL_EINVAL, "worker states required");
+    return select_common(mats, n_mat, d, lda, k, true, n_workers, worker_of, worker_states, idx, counts);
+}
+
+int fednl_gpu_randk(uint32_t* states, int32_t n_gen, int32_t d, int32_t lda, int32_t k, uint32_t* idx)
+{
+    return rand_common(states, n_gen, d, lda, k, idx, false);
+}
+
+int fednl_gpu_randseqk(uint32_t* states, int32_t n_gen, int32_t d, int32_t lda, int32_t k, uint32_t* idx)
+{
+    return rand_common(states, n_gen, d, lda, k, idx, true);
+}
+
+int fednl_gpu_natural(const double* in, int64_t n, double* out, uint8_t* packed)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!in || !out || n < 1) return fail(FEDNL_EINVAL, "bad argument");
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *din, *dout;
+    unsigned char* dpk = nullptr;
+    long long nb = n / 2 + 1;
+    s.a.want(&din, n);
+    s.a.want(&dout, n);
+    if (packed) s.a.want(&dpk, 3 * nb);
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(din, in, n * 8, cudaMemcpyHostToDevice, s.st));
+    k_natural<<<(unsigned)((n + 255) / 256), 256, 0, s.st>>>(din, n, dout);
+    CKL();
+    if (packed) {
+        k_natural_pack<<<(unsigned)((nb + 255) / 256), 256, 0, s.st>>>(din, n, dpk);
+        CKL();
+        CK(cudaMemcpyAsync(packed, dpk, 3 * nb, cudaMemcpyDeviceToHost, s.st));
+    }
+    CK(cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_t n, int32_t d, int32_t lda,
+                            double lambda, const double* x, double* grad, double* hess)
+{
+    if (!features || !labels || !x || n < 1 || d < 1) return fail(FEDNL_EINVAL, "bad argument");
+    fednl_problem_desc D{};
+    D.d = d;
+    D.lda = lda;
+    D.n_clients = 1;
+    D.n_samples = &n;
+    D.lambda = lambda;
+    D.compressor = FEDNL_IDENTITY;
+    D.k = 1;
+    D.alpha = 1.0;
+    D.workers = 1;
+    fednl_handle h = nullptr;
+    int rc = fednl_gpu_create(&D, &h);
+    if (rc) return rc;
+    rc = fednl_gpu_upload_client_data(h, features, labels);
+    if (!rc) rc = fednl_gpu_init_shifts(h, x);      // shift_0 = H(x)
+    if (!rc && grad) {
+        Dev& P = h->dev;
+        dim3 gg((d + 127) / 128, 1);
+        if (h->binary) k_grad_binary<<<gg, 128, 0, h->stream>>>(P);
+        else k_grad_dense<<<gg, 128, 0, h->stream>>>(P);
+        cudaError_t e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = fail(FEDNL_ECUDA, "gradient kernel failed: %s", cudaGetErrorString(e));
+        else if (cudaMemcpy(grad, P.gc, d * 8, cudaMemcpyDeviceToHost) != cudaSuccess) rc = fail(FEDNL_ECUDA, "copy failed");
+    }
+    if (!rc && hess) rc = fednl_gpu_get_shift(h, 0, hess);
+    fednl_gpu_destroy(h);
+    return rc;
+}
+
+int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!H || !g || !dx || d < 1 || lda < d) return fail(FEDNL_EINVAL, "bad argument");
+    long long U = (long long)d * (d + 1) / 2;
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    Dev P{};
+    double *dfull, *dpack, *dg;
+    s.a.want(&dfull, (size_t)d * lda);
+    s.a.want(&dpack, U);
+    s.a.want(&dg, d);
+    s.a.want(&P.work, U);
+    s.a.want(&P.dx, d);
+    s.a.want(&P.ybuf, d);
+    s.a.want(&P.status, 1);
+    rc = s.a.commit();
+    if (rc) return rc;
+    P.d = d;
+    P.U = (int)U;
+    CK(cudaMemcpyAsync(dfull, H, (size_t)d * lda * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dg, g, d * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemsetAsync(P.status, 0, 4, s.st));
+    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
+    CKL();
+    k_chol_solve<<<1, kCholThreads, 0, s.st>>>(P, dpack, nullptr, l, dg, P.dx, nullptr, 0);
+    CKL();
+    int status = 0;
+    CK(cudaMemcpyAsync(&status, P.status, 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    if (status) return fail(FEDNL_ENOTPD, "H + l I is not positive definite");
+    CK(cudaMemcpy(dx, P.dx, d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+// ---- instrumentation ---------------------------------------------------------------------------
+
+static int flush_l2(fednl_handle h, int64_t bytes)
+{
+    if (bytes <= 0) return FEDNL_OK;
+    if ((size_t)bytes > h->flush_cap) {
+        if (h->flush_buf) cudaFree(h->flush_buf);
+        h->flush_buf = nullptr;
+        h->flush_cap = 0;
+        CK(cudaMalloc(&h->flush_buf, (size_t)bytes));
+        h->flush_cap = (size_t)bytes;
+    }
+    CK(cudaMemsetAsync(h->flush_buf, h->rounds_done & 0xFF, (size_t)bytes, h->stream));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_time_rounds(fednl_handle h, int32_t rounds, int64_t flush_bytes, double* total_ms, double* per_round_ms)
+{
+    if (!h || rounds < 1 || !total_ms) return fail(FEDNL_EINVAL, "bad argument");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev(2 * (size_t)rounds, nullptr);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    CK(cudaMemsetAsync(h->dev.status, 0, 4, h->stream));
+    for (int r = 0; r < rounds; ++r) {
+        rc = flush_l2(h, flush_bytes);
+        if (rc) break;
+        if ((rc = cudaEventRecord(ev[2 * r], h->stream)) != cudaSuccess) break;
+        if ((rc = cudaGraphLaunch(h->gexec, h->stream)) != cudaSuccess) break;
+        if ((rc = cudaEventRecord(ev[2 * r + 1], h->stream)) != cudaSuccess) break;
+    }
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    double tot = 0.0;
+    if (rc == 0 && e == cudaSuccess) {
+        for (int r = 0; r < rounds; ++r) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]);
+            tot += ms;
+            if (per_round_ms) per_round_ms[r] = ms;
+        }
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (rc) return fail(FEDNL_ECUDA, "timed replay failed (%d)", rc);
+    if (e != cudaSuccess) return fail(FEDNL_ECUDA, "timed replay failed: %s", cudaGetErrorString(e));
+    h->rounds_done += rounds;
+    *total_ms = tot;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_bytes, int32_t* n_kernels,
+                              double* kernel_ms, char* names, int32_t names_len)
+{
+    if (!h || rounds < 1 || !n_kernels || !kernel_ms) return fail(FEDNL_EINVAL, "bad argument");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    const int kMaxMarks = 33;
+    std::vector<std::vector<cudaEvent_t>> ev(rounds, std::vector<cudaEvent_t>(kMaxMarks, nullptr));
+    for (auto& v : ev)
+        for (auto& e : v) CK(cudaEventCreate(&e));
+    std::vector<std::string> nm;
+    size_t nmarks = 0;
+    int rc = FEDNL_OK;
+    for (int r = 0; r < rounds && rc == FEDNL_OK; ++r) {
+        rc = flush_l2(h, flush_bytes);
+        if (rc) break;
+        Marks M;
+        M.ev = &ev[r];
+        M.names = &nm;
+        rc = launch_round(h, &M);
+        nmarks = M.next;
+    }
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    int nk = (int)nmarks - 1;
+    if (rc == FEDNL_OK && e == cudaSuccess) {
+        for (int t = 0; t < nk && t < 32; ++t) {
+            double acc = 0.0;
+            for (int r = 0; r < rounds; ++r) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[r][t], ev[r][t + 1]);
+                acc += ms;
+            }
+            kernel_ms[t] = acc / rounds;
+        }
+        *n_kernels = std::min(nk, 32);
+        if (names && names_len > 0) {
+            std::string all;
+            for (int t = 0; t < nk && t < 32; ++t) {
+                if (t) all += ";";
+                all += nm[t];
+            }
+            snprintf(names, (size_t)names_len, "%s", all.c_str());
+        }
+    }
+    for (auto& v : ev)
+        for (auto& x : v) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(FEDNL_ECUDA, "profiled rounds failed: %s", cudaGetErrorString(e));
+    h->rounds_done += rounds;
+    return FEDNL_OK;
+}
+
+}  // extern "C"

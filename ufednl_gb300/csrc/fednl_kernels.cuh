@@ -1,0 +1,823 @@
+// fednl_kernels.cuh -- sm_103a kernels of one FedNL round.
+//
+// Storage (one problem, resident in HBM):
+//   * symmetric d x d matrices (client shifts, differences, the master H, the Cholesky factor)
+//     are stored as their packed upper triangle: position p = j (j + 1) / 2 + i for i <= j.
+//     This is exactly the order of the reference's upper-index list (column j, rows 0..j,
+//     dopt/dopt/math_routines/include/SpecialMathRoutinesForMatrix.h:35-64), so "scan order",
+//     "ascending flat index j * lda + i" and "ascending p" coincide.  Half the bytes of the
+//     reference's full d x lda buffers; the lower triangle is its mirror.
+//   * binary {0,1} features: per client and attribute one bit per sample (feature-major
+//     bitmasks) plus a per-sample CSR list of nonzero attributes;
+//   * dense features: row-major [sample][d] FP64.
+//
+// Floating-point discipline: wherever the reference fixes an operation order, the kernels
+// perform the same IEEE operations in the same order with explicit __d*_rn intrinsics (no
+// fused multiply-add), so that values match the CPU oracle bit for bit given identical inputs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fednl {
+
+constexpr int kMaxK = 16384;            // largest TopK/TopLEK k held in shared memory
+constexpr unsigned kDiagBit = 0x80000000u;
+
+struct Dev {
+    // sizes and scalars
+    int d, lda, U, nc, k, comp, W, SW, nfpart;
+    double lambda, alpha, prescale, inv_n, mult;
+    // clients
+    const int* ns;          // [nc]
+    const int* soff;        // [nc + 1]
+    const int* client_of;   // [S]
+    const long long* fboff; // [nc] u64 offset of the client's d x words bitmask block
+    // features
+    const int* rowptr;      // [S + 1]  binary: nonzero attributes of each sample
+    const int* colidx;      // [nnz]
+    const unsigned long long* fbits;
+    const double* A;        // dense [S][d]
+    const double* lab;      // [S]
+    // state
+    double* x;              // [d]
+    double* H;              // [U] master
+    double* g;              // [d]
+    double* shift;          // [nc][U]
+    double* diff;           // [nc][U]
+    double* Dv;             // [S] Hessian weights D_s
+    double* qb;             // [S] gradient weights b_s * q_s
+    double* gc;             // [nc][d]
+    double* Fpart;          // [nc][nfpart]
+    double* F;              // [nc] ||diff||_F^2
+    double* lk;             // [nc]
+    unsigned* sel;          // [nc][SW] selection bitmaps over p
+    int* cnt;               // [nc]
+    int* needs;             // [nc] TopLEK: rounding draw needed
+    double* pdraw;          // [nc]
+    int* minidx;            // [nc]
+    unsigned* wstate;       // [W] TopLEK generators
+    unsigned* rstate;       // [nc] RandK / RandSeqK generators
+    int* rseq;              // [nc] RandSeqK window start
+    unsigned long long* hmap; // [nc][hcap] RandK virtual-shuffle map
+    int hcap;
+    double* work;           // [U] Cholesky factor
+    double* dx;             // [d]
+    double* ybuf;           // [d]
+    double* hist;           // [max_rounds] ||g|| history
+    int* round_ctr;         // [1]
+    int* status;            // [1]
+    double* stats;          // [2] ||g||, l
+    int hist_cap;
+};
+
+// ---- helpers -------------------------------------------------------------------------------
+
+// p -> (i, j) with p = j (j + 1) / 2 + i, i <= j; FP32 square root plus exact integer correction
+__device__ __forceinline__ void upper_ij(int p, int& i, int& j)
+{
+    int jj = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+    while (jj > 0 && (long long)jj * (jj + 1) / 2 > p) --jj;
+    while ((long long)(jj + 1) * (jj + 2) / 2 <= p) ++jj;
+    j = jj;
+    i = p - (int)((long long)jj * (jj + 1) / 2);
+}
+
+__device__ __forceinline__ bool upper_is_diag(int p)
+{
+    int i, j;
+    upper_ij(p, i, j);
+    return i == j;
+}
+
+// RandomGenIntegerLinear step (dopt/dopt/random/include/RandomGenIntegerLinear.h:107-123)
+__device__ __forceinline__ unsigned lcg_int_next(unsigned& s)
+{
+    s = 214013u * s + 2531011u;
+    return s;
+}
+
+// RandomGenIntegerLinear::generateRealInUnitInterval (RandomGenIntegerLinear.h:49-58)
+__device__ __forceinline__ double lcg_int_unit(unsigned& s)
+{
+    s = 214013u * s + 2531011u;
+    return __dmul_rn((double)s, 1.0 / 4294967295.0);
+}
+
+// RandomGenRealLinear::generateRealInUnitInterval (RandomGenRealLinear.h:54-59)
+__device__ __forceinline__ double lcg_real_unit(unsigned& s)
+{
+    unsigned t = 214013u * s + 2531011u;
+    s = t % 4294967295u;
+    return __dmul_rn((double)s, 1.0 / 4294967295.0);
+}
+
+// roundToNearestInt<size_t> (dopt/dopt/math_routines/include/SimpleMathRoutines.h:408-414)
+__device__ __forceinline__ unsigned long long round_to_nearest(double v)
+{
+    unsigned long long t = (unsigned long long)v;
+    if (__dsub_rn(v, (double)t) > 0.5) return t + 1;
+    return t;
+}
+
+__device__ __forceinline__ double natural_trunc(double v)
+{
+    return __longlong_as_double(__double_as_longlong(v) & ~((1ll << 52) - 1));
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) r += red[w];
+    return r;  // valid in thread 0
+}
+
+// ---- 1. margins, sigmoid and the per-sample weights ----------------------------------------
+// logistic_regression.h:88-101 (margin, sigmoid), :148-161 (q_s = (1 - sigma_s)(-1/n)),
+// :387-393 (D_s = (1/n)((1 - sigma_s) sigma_s)).  Binary features: the margin is the sequential
+// sum of x over the sample's nonzero attributes in ascending order, times the label -- the same
+// IEEE additions as the reference's dot product with the +-1 / 0 column.
+__global__ void k_margin_binary(Dev P, int S)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    int c = P.client_of[s];
+    double acc = 0.0;
+    for (int t = P.rowptr[s]; t < P.rowptr[s + 1]; ++t) acc = __dadd_rn(acc, P.x[P.colidx[t]]);
+    double b = P.lab[s];
+    double m = (b == 1.0) ? acc : -acc;
+    double sig = 1.0 / (1.0 + exp(-m));
+    double inv_m = 1.0 / (double)P.ns[c];
+    double z1 = __dsub_rn(1.0, sig);
+    P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
+    double q = __dmul_rn(z1, -inv_m);
+    P.qb[s] = (b == 1.0) ? q : __dmul_rn(-1.0, q);
+}
+
+// dense features: column s of Atr is b_s * a_s (logistic_regression.h:45-75)
+__global__ void k_margin_dense(Dev P, int S)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    int c = P.client_of[s];
+    double b = P.lab[s];
+    const double* a = P.A + (size_t)s * P.d;
+    double acc = 0.0;
+    for (int i = 0; i < P.d; ++i) {
+        double u = (b == 1.0) ? a[i] : __dmul_rn(a[i], -1.0);
+        acc = __dadd_rn(acc, __dmul_rn(u, P.x[i]));
+    }
+    double sig = 1.0 / (1.0 + exp(-acc));
+    double inv_m = 1.0 / (double)P.ns[c];
+    double z1 = __dsub_rn(1.0, sig);
+    P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
+    P.qb[s] = __dmul_rn(z1, -inv_m);   // dense: the label enters through u
+}
+
+// ---- 2. client gradients g_c = lambda x + sum_s Atr[:, s] q_s (samples in order) ----------
+__global__ void k_grad_binary(Dev P)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (j >= P.d) return;
+    int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
+    double g = __dmul_rn(P.x[j], P.lambda);
+    for (int w = 0; w < W; ++w) {
+        unsigned long long m = fb[w];
+        while (m) {
+            int b = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            g = __dadd_rn(g, P.qb[off + w * 64 + b]);
+        }
+    }
+    P.gc[(size_t)c * P.d + j] = g;
+}
+
+__global__ void k_grad_dense(Dev P)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (j >= P.d) return;
+    int n = P.ns[c], off = P.soff[c];
+    double g = __dmul_rn(P.x[j], P.lambda);
+    for (int s = 0; s < n; ++s) {
+        double a = P.A[(size_t)(off + s) * P.d + j];
+        double u = (P.lab[off + s] == 1.0) ? a : __dmul_rn(a, -1.0);
+        g = __dadd_rn(g, __dmul_rn(u, P.qb[off + s]));
+    }
+    P.gc[(size_t)c * P.d + j] = g;
+}
+
+// ---- 3. client Hessians fused with the difference and its Frobenius norm ------------------
+// evaluateHessian<true,4> (logistic_regression.h:365-547): entry (i, j) is the sum over samples
+// in order of u_i (D_s u_j); for {0,1} features every nonzero term equals D_s exactly, so the
+// entry is the in-order sum of D_s over the samples where both attributes are set (bitmask
+// AND).  Then + lambda on the diagonal.  mode 0: diff = H_i - shift_i (TopK.h:70-71) and the
+// partial sums of ||diff||_F^2 over the full symmetric matrix; mode 1: shift_i = H_i(x0).
+constexpr int kHessThreads = 256;
+constexpr int kHessPerBlock = 4096;     // upper entries per block
+
+template <bool SMEM_BITS>
+__global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
+{
+    extern __shared__ unsigned long long s_fb[];
+    __shared__ double red[kHessThreads / 32];
+    int c = blockIdx.y;
+    int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    const unsigned long long* gfb = P.fbits + P.fboff[c];
+    double* s_D;
+    const unsigned long long* fb;
+    if (SMEM_BITS) {
+        for (int t = threadIdx.x; t < P.d * W; t += blockDim.x) s_fb[t] = gfb[t];
+        s_D = (double*)(s_fb + (size_t)P.d * W);
+        fb = s_fb;
+    } else {
+        s_D = (double*)s_fb;
+        fb = gfb;
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s_D[t] = P.Dv[off + t];
+    __syncthreads();
+
+    size_t base = (size_t)c * P.U;
+    double fs = 0.0;
+    int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
+    for (int p = blockIdx.x * kHessPerBlock + threadIdx.x; p < p_end; p += blockDim.x) {
+        int i, j;
+        upper_ij(p, i, j);
+        const unsigned long long* mi = fb + (size_t)i * W;
+        const unsigned long long* mj = fb + (size_t)j * W;
+        double h = 0.0;
+        for (int w = 0; w < W; ++w) {
+            unsigned long long m = mi[w] & mj[w];
+            while (m) {
+                int b = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                h = __dadd_rn(h, s_D[w * 64 + b]);
+            }
+        }
+        if (i == j) h = __dadd_rn(h, P.lambda);
+        if (mode == 1) {
+            P.shift[base + p] = h;
+        } else {
+            double df = __dsub_rn(h, P.shift[base + p]);
+            P.diff[base + p] = df;
+            double t = df * df;
+            fs += (i == j) ? t : 2.0 * t;
+        }
+    }
+    if (mode == 0) {
+        double tot = block_sum<kHessThreads>(fs, red);
+        if (threadIdx.x == 0) P.Fpart[(size_t)c * P.nfpart + blockIdx.x] = tot;
+    }
+}
+
+// dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
+__global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
+{
+    __shared__ double red[kHessThreads / 32];
+    int c = blockIdx.y;
+    int n = P.ns[c], off = P.soff[c];
+    size_t base = (size_t)c * P.U;
+    double fs = 0.0;
+    int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
+    for (int p = blockIdx.x * kHessPerBlock + threadIdx.x; p < p_end; p += blockDim.x) {
+        int i, j;
+        upper_ij(p, i, j);
+        double h = 0.0;
+        for (int s = 0; s < n; ++s) {
+            const double* a = P.A + (size_t)(off + s) * P.d;
+            bool pos = P.lab[off + s] == 1.0;
+            double ui = pos ? a[i] : __dmul_rn(a[i], -1.0);
+            double uj = pos ? a[j] : __dmul_rn(a[j], -1.0);
+            h = __dadd_rn(h, __dmul_rn(ui, __dmul_rn(P.Dv[off + s], uj)));
+        }
+        if (i == j) h = __dadd_rn(h, P.lambda);
+        if (mode == 1) {
+            P.shift[base + p] = h;
+        } else {
+            double df = __dsub_rn(h, P.shift[base + p]);
+            P.diff[base + p] = df;
+            double t = df * df;
+            fs += (i == j) ? t : 2.0 * t;
+        }
+    }
+    if (mode == 0) {
+        double tot = block_sum<kHessThreads>(fs, red);
+        if (threadIdx.x == 0) P.Fpart[(size_t)c * P.nfpart + blockIdx.x] = tot;
+    }
+}
+
+// per-client ||diff||_F^2 and Lk = ||diff||_F (TopK.h:74-78)
+__global__ void k_fsum(Dev P)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.nc) return;
+    double f = 0.0;
+    for (int b = 0; b < P.nfpart; ++b) f += P.Fpart[(size_t)c * P.nfpart + b];
+    P.F[c] = f;
+    P.lk[c] = sqrt(f);
+}
+
+// master H = mean_i shift_i after the initial shifts (TrainLoop.h:639-643, :732-735)
+__global__ void k_h_init(Dev P)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.U) return;
+    double h = 0.0;
+    for (int c = 0; c < P.nc; ++c) h = __dadd_rn(h, P.shift[(size_t)c * P.U + p]);
+    P.H[p] = __dmul_rn(h, P.inv_n);
+}
+
+// ---- 4. TopK / TopLEK: exact emulation of the reference's 4-ary heap ------------------------
+// dopt/dopt/math_routines/include/MinHeap.h (D = 4) as used by getTopKFromUpperDiagonalPart and
+// getTopLEKFromUpperDiagonalPart (SpecialMathRoutinesForMatrix.h:229-511).  The reference's
+// minHeapify keeps comparing a node's children with the value that moved up on the previous
+// level (MinHeap.h:259-286), so its "heap" is not a true heap and the selected set is not the
+// plain top-k by magnitude; every comparison, swap and tie is reproduced here step by step.
+// One warp per matrix performs the sequential heap work in shared memory; the scan over the
+// remaining entries is done 32 entries at a time with a warp ballot against the current root.
+struct HeapS {
+    double* key;     // |value|
+    unsigned* hid;   // p | kDiagBit
+};
+
+__device__ __forceinline__ void heap_swap(HeapS& h, int a, int b)
+{
+    double tk = h.key[a];
+    h.key[a] = h.key[b];
+    h.key[b] = tk;
+    unsigned ti = h.hid[a];
+    h.hid[a] = h.hid[b];
+    h.hid[b] = ti;
+}
+
+// minHeapify, MinHeap.h:255-290 (lowest value carried across levels as in the reference)
+__device__ void heap_sift(HeapS& h, int i, int heap_size)
+{
+    double lowest_value = h.key[i];
+    for (;;) {
+        int lowest = i;
+        int first = 4 * i + 1;
+        int last = min(first + 4, heap_size);
+        for (int c = first; c < last; ++c) {
+            double cv = h.key[c];
+            if (lowest_value > cv) {
+                lowest = c;
+                lowest_value = cv;
+            }
+        }
+        if (lowest != i) {
+            heap_swap(h, i, lowest);
+            i = lowest;
+        } else {
+            break;
+        }
+    }
+}
+
+__device__ void heap_insert(HeapS& h, int& size, double key, unsigned id)
+{
+    int i = size++;
+    h.key[i] = key;
+    h.hid[i] = id;
+    while (i != 0 && h.key[(i - 1) / 4] > h.key[i]) {
+        heap_swap(h, (i - 1) / 4, i);
+        i = (i - 1) / 4;
+    }
+}
+
+constexpr int kSelThreads = 128;
+
+// vals: [n_mat][U] packed upper values (signed); F: [n_mat] squared Frobenius norm of the full
+// matrix.  Output: sel bitmap per matrix, cnt (entries left in the heap), TopLEK draw request.
+__global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict__ vals, int U, int k, int lek,
+                                                        double delta, const double* __restrict__ F,
+                                                        unsigned* sel, int SW, int* cnt, int* needs,
+                                                        double* pdraw, int* minidx)
+{
+    extern __shared__ double s_key[];
+    __shared__ int s_size;
+    int c = blockIdx.x;
+    const double* v = vals + (size_t)c * U;
+    unsigned* sc = sel + (size_t)c * SW;
+    for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
+    if (k >= U) {       // SpecialMathRoutinesForMatrix.h:279-280 / :395-396: every upper index
+        __syncthreads();
+        for (int w = threadIdx.x; w < SW; w += blockDim.x) {
+            int lo = w * 32, n = min(32, U - lo);
+            sc[w] = (n == 32) ? 0xffffffffu : ((1u << n) - 1u);
+        }
+        if (threadIdx.x == 0) {
+            cnt[c] = U;
+            if (needs) needs[c] = 0;
+        }
+        return;
+    }
+    HeapS h;
+    h.key = s_key;
+    h.hid = (unsigned*)(s_key + k);
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        h.key[t] = fabs(v[t]);
+        h.hid[t] = (unsigned)t | (upper_is_diag(t) ? kDiagBit : 0u);
+    }
+    __syncthreads();
+    int size = k;
+    int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        if (lane == 0) {   // buildMinHeap, MinHeap.h:147-191
+            int i = (k + 4 - 2) / 4;
+            for (;;) {
+                heap_sift(h, i, k);
+                if (i == 0) break;
+                --i;
+            }
+        }
+        __syncwarp();
+        double root = *(volatile double*)&h.key[0];
+        // scan, SpecialMathRoutinesForMatrix.h:300-318
+        double nxt = (k + lane < U) ? fabs(v[k + lane]) : -1.0;
+        for (int base = k; base < U; base += 32) {
+            double vv = nxt;
+            int tn = base + 32 + lane;
+            nxt = (tn < U) ? fabs(v[tn]) : -1.0;
+            unsigned mask = __ballot_sync(0xffffffffu, vv > root);
+            while (mask) {
+                int l = __ffs(mask) - 1;
+                double cand = __shfl_sync(0xffffffffu, vv, l);
+                if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
+                    int p = base + l;
+                    h.key[0] = cand;
+                    h.hid[0] = (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u);
+                    heap_sift(h, 0, k);
+                }
+                __syncwarp();
+                root = *(volatile double*)&h.key[0];
+                // the root of this heap can also decrease (a deeper element may move up), so the
+                // remaining lanes are tested again against the new root, not filtered by the old one
+                mask = __ballot_sync(0xffffffffu, vv > root) & ~((2u << l) - 1u);
+            }
+        }
+        if (lek && lane == 0) {
+            // getTopLEKFromUpperDiagonalPart, SpecialMathRoutinesForMatrix.h:385-503
+            double fr = F[c];
+            double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
+            double eps = __dmul_rn(1e-1, fr);
+            double num = fr;
+            for (int t = 0; t < k; ++t) {
+                double kk = h.key[t];
+                double term = __dmul_rn(kk, kk);
+                if (!(h.hid[t] & kDiagBit)) term = __dmul_rn(term, 2.0);
+                num = __dsub_rn(num, term);
+            }
+            int need = 0;
+            double pd = 0.0;
+            int mi = 0;
+            do {
+                double prev = num;
+                double mk = h.key[0];
+                unsigned mh = h.hid[0];
+                heap_swap(h, 0, size - 1);          // extracFromMinHeap, MinHeap.h:125-141
+                heap_sift(h, 0, size - 1);
+                size -= 1;
+                double term = __dmul_rn(mk, mk);
+                if (!(mh & kDiagBit)) term = __dmul_rn(term, 2.0);
+                num = __dadd_rn(num, term);
+                double next = num;
+                if (__dadd_rn(omd, eps) > prev && omd < __dadd_rn(next, eps)) {
+                    pd = __dadd_rn(__dsub_rn(omd, prev), eps) / __dadd_rn(__dsub_rn(next, prev), eps);
+                    need = 1;
+                    mi = (int)(mh & ~kDiagBit);
+                    break;
+                }
+            } while (size != 0);
+            needs[c] = need;
+            pdraw[c] = pd;
+            minidx[c] = mi;
+        }
+        if (lane == 0) s_size = size;
+    }
+    __syncthreads();
+    size = s_size;
+    for (int t = threadIdx.x; t < size; t += blockDim.x) {
+        unsigned p = h.hid[t] & ~kDiagBit;
+        atomicOr(&sc[p >> 5], 1u << (p & 31));
+    }
+    if (threadIdx.x == 0) cnt[c] = size;
+}
+
+// TopLEK rounding draws: each reference worker w owns one thread_local RandomGenRealLinear
+// (SpecialMathRoutinesForMatrix.h:383) and visits its clients c = w, w + W, ... in order
+// (TrainLoop.h:664-686); a draw happens only when the rounding window was reached (:475-501).
+__global__ void k_toplek_rng(int n_mat, int W, const int* worker_of, unsigned* wstate, const int* needs,
+                             const double* pdraw, const int* minidx, unsigned* sel, int SW, int* cnt)
+{
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    unsigned st = wstate[w];
+    for (int c = 0; c < n_mat; ++c) {
+        int owner = worker_of ? worker_of[c] : (c % W);
+        if (owner != w || !needs[c]) continue;
+        double u = lcg_real_unit(st);
+        if (u > pdraw[c]) {     // w.p. 1 - p keep the element (insertInMinHeap)
+            unsigned p = (unsigned)minidx[c];
+            sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
+            cnt[c] += 1;
+        }
+    }
+    wstate[w] = st;
+}
+
+// ---- 5. RandK / RandSeqK ---------------------------------------------------------------------
+// generateRandKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:95-107): partial
+// Fisher-Yates over a copy of the upper-index list (dopt/dopt/random/include/Shuffle.h:76-93)
+// with the client's RandomGenIntegerLinear; the shuffled array is virtual: only displaced
+// positions are kept, in an open-addressing map in global scratch.  The first k entries, sorted,
+// are the selection -- set as bits of the selection bitmap, whose ascending order is the sort.
+__device__ __forceinline__ unsigned hmap_get(unsigned long long* m, int cap, unsigned key)
+{
+    unsigned hsh = (key * 2654435761u) & (unsigned)(cap - 1);
+    for (;;) {
+        unsigned long long e = m[hsh];
+        if (e == ~0ull) return key;                    // untouched: identity
+        if ((unsigned)(e >> 32) == key) return (unsigned)e;
+        hsh = (hsh + 1) & (unsigned)(cap - 1);
+    }
+}
+
+__device__ __forceinline__ void hmap_put(unsigned long long* m, int cap, unsigned key, unsigned val)
+{
+    unsigned hsh = (key * 2654435761u) & (unsigned)(cap - 1);
+    for (;;) {
+        unsigned long long e = m[hsh];
+        if (e == ~0ull || (unsigned)(e >> 32) == key) {
+            m[hsh] = ((unsigned long long)key << 32) | val;
+            return;
+        }
+        hsh = (hsh + 1) & (unsigned)(cap - 1);
+    }
+}
+
+__global__ void k_randk(unsigned* states, int n_gen, int U, int k, unsigned long long* hmap, int hcap,
+                        unsigned* sel, int SW, int* cnt)
+{
+    int c = blockIdx.x;
+    unsigned long long* m = hmap + (size_t)c * hcap;
+    unsigned* sc = sel + (size_t)c * SW;
+    for (int t = threadIdx.x; t < hcap; t += blockDim.x) m[t] = ~0ull;
+    for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned st = states[c];
+        unsigned long long n_minus_i_minus_one = (unsigned long long)U - 1;
+        for (int i = 0; i < k; ++i, --n_minus_i_minus_one) {
+            double u = lcg_int_unit(st);
+            unsigned long long r_off = round_to_nearest(__dmul_rn(u, (double)n_minus_i_minus_one));
+            if (r_off != 0) {
+                unsigned r = (unsigned)(i + r_off);
+                unsigned vi = hmap_get(m, hcap, (unsigned)i);
+                unsigned vr = hmap_get(m, hcap, r);
+                hmap_put(m, hcap, (unsigned)i, vr);
+                hmap_put(m, hcap, r, vi);
+            }
+        }
+        states[c] = st;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        unsigned p = hmap_get(m, hcap, (unsigned)i);
+        atomicOr(&sc[p >> 5], 1u << (p & 31));
+    }
+    if (threadIdx.x == 0) cnt[c] = k;
+}
+
+// generateRandSeqKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:137-169)
+__global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq, unsigned* sel, int SW, int* cnt)
+{
+    int c = blockIdx.x;
+    unsigned* sc = sel + (size_t)c * SW;
+    for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
+    __shared__ unsigned s_r;
+    if (threadIdx.x == 0) {
+        unsigned st = states[c];
+        s_r = (unsigned)((unsigned long long)lcg_int_next(st) % (unsigned long long)U);
+        states[c] = st;
+        rseq[c] = (int)s_r;
+        cnt[c] = k;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        unsigned p = s_r + t;
+        if (p >= (unsigned)U) p -= U;
+        atomicOr(&sc[p >> 5], 1u << (p & 31));
+    }
+}
+
+// ---- 6. shift update + master merge, clients in order ----------------------------------------
+// Worker: shift[idx] += alpha * item (TopK.h:103-129, RandK.h:136-162; Identical/Natural: the
+// whole symmetric difference).  Master: H[idx] += item * preScale in client order
+// (TrainLoop.h:1126-1276 with forcesequpdate).  One thread per upper position, looping over the
+// clients in order, so H receives exactly the reference's sequence of additions.
+__global__ void k_apply(Dev P)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.U) return;
+    double h = P.H[p];
+    bool all = (P.comp == 0 || P.comp == 5);
+    for (int c = 0; c < P.nc; ++c) {
+        if (!all && !((P.sel[(size_t)c * P.SW + (p >> 5)] >> (p & 31)) & 1u)) continue;
+        size_t q = (size_t)c * P.U + p;
+        double dv = P.diff[q];
+        double item, sent;
+        if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
+            item = natural_trunc(dv);
+            sent = __dmul_rn(P.prescale, item);
+        } else {
+            item = (P.comp == 1 || P.comp == 3) ? __dmul_rn(dv, P.mult) : dv;
+            sent = __dmul_rn(item, P.prescale);
+        }
+        P.shift[q] = __dadd_rn(P.shift[q], __dmul_rn(P.alpha, item));
+        h = __dadd_rn(h, sent);
+    }
+    P.H[p] = h;
+}
+
+// ---- 7. master: g = (1/n) sum_c g_c, l = (1/n) sum_c Lk_c (TrainLoop.h:1100-1333) ------------
+constexpr int kAggThreads = 256;
+__global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
+{
+    __shared__ double red[kAggThreads / 32];
+    double ss = 0.0;
+    for (int j = threadIdx.x; j < P.d; j += blockDim.x) {
+        double g = 0.0;
+        for (int c = 0; c < P.nc; ++c) g = __dadd_rn(g, P.gc[(size_t)c * P.d + j]);
+        g = __dmul_rn(g, P.inv_n);
+        P.g[j] = g;
+        ss += g * g;
+    }
+    double tot = block_sum<kAggThreads>(ss, red);
+    if (threadIdx.x == 0) {
+        double l = 0.0;
+        for (int c = 0; c < P.nc; ++c) l = __dadd_rn(l, P.lk[c]);
+        l = __dmul_rn(l, P.inv_n);
+        P.stats[0] = sqrt(tot);
+        P.stats[1] = l;
+    }
+}
+
+// ---- 8. Option-B solve: Cholesky of H + l I, two triangular solves, x -= dx ------------------
+// choleskyFactorization<.., true, true> (CholeskyFactorization.h:153-272) computes R = L^T with
+// H + l I = R^T R reading only the upper triangle; forwardSubstitutionWithATranspose and
+// backwardSubstitutionWithATranspose (ElementarySolvers.h:186-224, :71-128) solve R^T y = g and
+// R dx = y.  Here the factor is formed right-looking in one CTA on the packed upper triangle.
+constexpr int kCholThreads = 1024;
+__device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j + 1) / 2 + i; }
+
+// l is read from lptr when given (the round's device-side l), else lval is used.
+__global__ void __launch_bounds__(kCholThreads) k_chol_solve(Dev P, const double* __restrict__ Hin,
+                                                             const double* lptr, double lval,
+                                                             const double* __restrict__ gin, double* dxout,
+                                                             double* xupd, int record)
+{
+    double l = lptr ? *lptr : lval;
+    __shared__ double s_r;
+    __shared__ int s_fail;
+    double* A = P.work;
+    int d = P.d, U = P.U;
+    for (int p = threadIdx.x; p < U; p += blockDim.x) {
+        int i, j;
+        upper_ij(p, i, j);
+        A[p] = (i == j) ? __dadd_rn(Hin[p], l) : Hin[p];
+    }
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int kk = 0; kk < d; ++kk) {
+        if (threadIdx.x == 0) {
+            double a = A[up_pos(kk, kk)];
+            if (a < 0) {
+                if (a > -0.0) a = 0.0;
+                else s_fail = 1;
+            }
+            double r = sqrt(a);
+            A[up_pos(kk, kk)] = r;
+            s_r = 1.0 / r;
+        }
+        __syncthreads();
+        if (s_fail) break;
+        double inv = s_r;
+        for (int j = kk + 1 + threadIdx.x; j < d; j += blockDim.x) A[up_pos(kk, j)] *= inv;
+        __syncthreads();
+        for (int j = kk + 1 + warp; j < d; j += nw) {
+            double rkj = A[up_pos(kk, j)];
+            double* col = A + up_pos(0, j);
+            for (int i = kk + 1 + lane; i <= j; i += 32) col[i] -= A[up_pos(kk, i)] * rkj;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (s_fail) {
+        if (threadIdx.x == 0) {
+            if (P.status) *P.status = -4;
+            if (record) *P.round_ctr += 1;
+        }
+        return;
+    }
+    // R^T y = g (column-oriented forward substitution)
+    double* y = P.ybuf;
+    for (int i = threadIdx.x; i < d; i += blockDim.x) y[i] = gin[i];
+    __syncthreads();
+    for (int t = 0; t < d; ++t) {
+        if (threadIdx.x == 0) y[t] = y[t] / A[up_pos(t, t)];
+        __syncthreads();
+        double yt = y[t];
+        for (int i = t + 1 + threadIdx.x; i < d; i += blockDim.x) y[i] -= A[up_pos(t, i)] * yt;
+        __syncthreads();
+    }
+    // R dx = y (column-oriented backward substitution)
+    for (int t = d - 1; t >= 0; --t) {
+        if (threadIdx.x == 0) y[t] = y[t] / A[up_pos(t, t)];
+        __syncthreads();
+        double yt = y[t];
+        for (int i = threadIdx.x; i < t; i += blockDim.x) y[i] -= A[up_pos(i, t)] * yt;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < d; i += blockDim.x) {
+        double dxi = y[i];
+        if (dxout) dxout[i] = dxi;
+        if (xupd) xupd[i] = __dsub_rn(xupd[i], dxi);    // x -= dx (TrainLoop.h:1504-1508)
+    }
+    if (record && threadIdx.x == 0) {
+        int r = *P.round_ctr;
+        if (r < P.hist_cap) P.hist[r] = P.stats[0];
+        *P.round_ctr = r + 1;
+    }
+}
+
+// ---- operator-level helpers -----------------------------------------------------------------
+// pack the upper triangle of n column-major d x lda matrices and their full squared norms
+__global__ void k_pack_upper(const double* full, int d, int lda, int U, double* packed)
+{
+    int t = blockIdx.y;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < U; p += gridDim.x * blockDim.x) {
+        int i, j;
+        upper_ij(p, i, j);
+        packed[(size_t)t * U + p] = full[(size_t)t * d * lda + (size_t)j * lda + i];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_l2sq_full(const double* full, long long len, double* out)
+{
+    __shared__ double red[8];
+    int t = blockIdx.x;
+    const double* m = full + (size_t)t * len;
+    double s = 0.0;
+    for (long long e = threadIdx.x; e < len; e += blockDim.x) s += m[e] * m[e];
+    double tot = block_sum<256>(s, red);
+    if (threadIdx.x == 0) out[t] = tot;
+}
+
+__global__ void k_natural(const double* in, long long n, double* out)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) out[e] = natural_trunc(in[e]);
+}
+
+// Reference wire format of the Natural message (LocalWorkerForFedNL_Natural.h:92-126): entries
+// are packed pairwise, 3 bytes per pair [signA(1) expA(11) signB(1) expB(11)]
+// (pack2FP64NoMantissa, FloatUtils.h:193-221), followed by one trailing block made of the
+// packer's two slots as they stand: (last, second-to-last) for odd n, the final pair again for
+// even n.  Block q < n/2 packs (2q, 2q+1); block n/2 is the trailing one.
+__global__ void k_natural_pack(const double* in, long long n, unsigned char* packed)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nb = n / 2 + 1;
+    if (q >= nb || n < 1) return;
+    long long ia, ib;
+    if (q < n / 2) {
+        ia = 2 * q;
+        ib = 2 * q + 1;
+    } else if (n & 1) {
+        ia = n - 1;
+        ib = (n >= 2) ? n - 2 : n - 1;
+    } else {
+        ia = n - 2;
+        ib = n - 1;
+    }
+    unsigned long long a = (unsigned long long)__double_as_longlong(in[ia]);
+    unsigned long long b = (unsigned long long)__double_as_longlong(in[ib]);
+    unsigned v = ((unsigned)(a >> 63) << 23) | ((unsigned)((a >> 52) & 0x7FF) << 12) |
+                 ((unsigned)(b >> 63) << 11) | (unsigned)((b >> 52) & 0x7FF);
+    packed[3 * q + 0] = (unsigned char)(v & 0xFF);
+    packed[3 * q + 1] = (unsigned char)((v >> 8) & 0xFF);
+    packed[3 * q + 2] = (unsigned char)((v >> 16) & 0xFF);
+}
+
+}  // namespace fednl

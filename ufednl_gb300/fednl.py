@@ -1,0 +1,300 @@
+"""Python host API over the C ABI of libfednl_gpu.so (include/fednl_gpu.h).
+
+Names follow the reference's operator surface (dopt): ``get_topk_from_upper_diagonal_part``,
+``get_toplek_from_upper_diagonal_part``, ``generate_randk_items_in_upper_triangular_part``,
+``generate_randseqk_items_in_upper_triangular_part``, ``apply_natural_compressor``,
+``evaluate_gradient_and_hessian`` and ``cholesky_option_b_solve``, plus ``FedNL`` for whole runs
+(the reference's ``train()`` loop).  Matrices are NumPy arrays in the reference's column-major
+d x lda layout (flattened), indices are the reference's flat indices j * lda + i.
+
+Errors raise ``FedNLError`` with the library's message; the native library is mandatory (there
+is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL = 0, 1, 2, 3, 4, 5
+COMPRESSORS = {"identity": IDENTITY, "randk": RANDK, "topk": TOPK, "randseqk": RANDSEQK,
+               "seqk": RANDSEQK, "toplek": TOPLEK, "natural": NATURAL}
+STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTPD", -5: "ETIMEOUT", -6: "ENODEV"}
+
+
+class FedNLError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("d", C.c_int32), ("lda", C.c_int32), ("n_clients", C.c_int32),
+                ("n_samples", C.POINTER(C.c_int32)), ("lambda_", C.c_double),
+                ("compressor", C.c_int32), ("k", C.c_int32), ("alpha", C.c_double),
+                ("workers", C.c_int32), ("seed_base", C.c_uint32), ("toplek_seed", C.c_uint32),
+                ("feature_format", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
+class RoundStats(C.Structure):
+    _fields_ = [("round", C.c_int32), ("status", C.c_int32), ("grad_norm", C.c_double), ("l", C.c_double)]
+
+
+# every symbol declared in include/fednl_gpu.h
+EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_data", "fednl_gpu_init_shifts",
+           "fednl_gpu_round", "fednl_gpu_run", "fednl_gpu_get_x", "fednl_gpu_set_x", "fednl_gpu_get_grad",
+           "fednl_gpu_get_H", "fednl_gpu_get_shift", "fednl_gpu_get_l", "fednl_gpu_get_lk",
+           "fednl_gpu_get_message", "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
+           "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
+           "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels", "fednl_gpu_last_error"]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Loads the in-tree libfednl_gpu.so (building it with nvcc if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB_PATH):
+        if not build_if_missing:
+            raise FedNLError(-6, f"native library missing: {_build.LIB_PATH}")
+        _build.build()
+    L = C.CDLL(_build.LIB_PATH)
+    vp, dp, up, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint32), C.POINTER(C.c_int32)
+    sig = {
+        "fednl_gpu_create": [C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)],
+        "fednl_gpu_destroy": [vp],
+        "fednl_gpu_upload_client_data": [vp, dp, dp],
+        "fednl_gpu_init_shifts": [vp, dp],
+        "fednl_gpu_round": [vp, C.POINTER(RoundStats)],
+        "fednl_gpu_run": [vp, C.c_int32, dp],
+        "fednl_gpu_get_x": [vp, dp], "fednl_gpu_set_x": [vp, dp], "fednl_gpu_get_grad": [vp, dp],
+        "fednl_gpu_get_H": [vp, dp], "fednl_gpu_get_shift": [vp, C.c_int32, dp],
+        "fednl_gpu_get_message": [vp, C.c_int32, up, dp, ip],
+        "fednl_gpu_topk": [dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
+        "fednl_gpu_toplek": [dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, up, up, ip],
+        "fednl_gpu_randk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
+        "fednl_gpu_randseqk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
+        "fednl_gpu_natural": [dp, C.c_int64, dp, C.POINTER(C.c_uint8)],
+        "fednl_gpu_logreg_oracle": [dp, dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, dp, dp, dp],
+        "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
+        "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
+        "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.fednl_gpu_get_l.argtypes = [vp]
+    L.fednl_gpu_get_l.restype = C.c_double
+    L.fednl_gpu_get_lk.argtypes = [vp, C.c_int32]
+    L.fednl_gpu_get_lk.restype = C.c_double
+    L.fednl_gpu_last_error.argtypes = []
+    L.fednl_gpu_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise FedNLError(rc, load().fednl_gpu_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _up(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def reference_lda(d: int) -> int:
+    return (d + 3) // 4 * 4
+
+
+# ---- operator surface ------------------------------------------------------------------------
+
+def get_topk_from_upper_diagonal_part(mats: np.ndarray, d: int, lda: int, k: int) -> np.ndarray:
+    """mats: [n, d*lda] column-major matrices -> [n, k] ascending flat indices."""
+    m = np.ascontiguousarray(mats, dtype=np.float64).reshape(-1, d * lda)
+    U = d * (d + 1) // 2
+    kk = min(k, U)
+    out = np.zeros((m.shape[0], max(k, 1)), dtype=np.uint32)
+    _check(load().fednl_gpu_topk(_dp(m), m.shape[0], d, lda, k, _up(out)))
+    return out[:, :kk]
+
+
+def get_toplek_from_upper_diagonal_part(mats: np.ndarray, d: int, lda: int, k: int, worker_states: np.ndarray,
+                                        worker_of=None):
+    """Returns a list of index arrays; worker_states (uint32[W]) is advanced in place."""
+    m = np.ascontiguousarray(mats, dtype=np.float64).reshape(-1, d * lda)
+    n = m.shape[0]
+    out = np.zeros((n, k), dtype=np.uint32)
+    counts = np.zeros(n, dtype=np.int32)
+    wo = None if worker_of is None else np.ascontiguousarray(worker_of, dtype=np.int32)
+    ws = worker_states
+    assert ws.dtype == np.uint32 and ws.flags.c_contiguous
+    _check(load().fednl_gpu_toplek(_dp(m), n, d, lda, k, ws.size,
+                                   _ip(wo) if wo is not None else None, _up(ws), _up(out), _ip(counts)))
+    return [out[t, :counts[t]].copy() for t in range(n)]
+
+
+def generate_randk_items_in_upper_triangular_part(states: np.ndarray, d: int, lda: int, k: int) -> np.ndarray:
+    assert states.dtype == np.uint32 and states.flags.c_contiguous
+    out = np.zeros((states.size, k), dtype=np.uint32)
+    _check(load().fednl_gpu_randk(_up(states), states.size, d, lda, k, _up(out)))
+    return out
+
+
+def generate_randseqk_items_in_upper_triangular_part(states: np.ndarray, d: int, lda: int, k: int) -> np.ndarray:
+    assert states.dtype == np.uint32 and states.flags.c_contiguous
+    out = np.zeros((states.size, k), dtype=np.uint32)
+    _check(load().fednl_gpu_randseqk(_up(states), states.size, d, lda, k, _up(out)))
+    return out
+
+
+def apply_natural_compressor(values: np.ndarray, with_packed: bool = False):
+    v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    out = np.empty_like(v)
+    packed = np.zeros(3 * (v.size // 2 + 1), dtype=np.uint8) if with_packed else None
+    _check(load().fednl_gpu_natural(_dp(v), v.size, _dp(out),
+                                    packed.ctypes.data_as(C.POINTER(C.c_uint8)) if with_packed else None))
+    return (out, packed) if with_packed else out
+
+
+def evaluate_gradient_and_hessian(features, labels, lam: float, x, lda: int | None = None):
+    f = np.ascontiguousarray(features, dtype=np.float64)
+    b = np.ascontiguousarray(labels, dtype=np.float64)
+    n, d = f.shape
+    lda = lda or reference_lda(d)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    g = np.empty(d)
+    h = np.empty(d * lda)
+    _check(load().fednl_gpu_logreg_oracle(_dp(f), _dp(b), n, d, lda, lam, _dp(xx), _dp(g), _dp(h)))
+    return g, h
+
+
+def cholesky_option_b_solve(H: np.ndarray, d: int, lda: int, l: float, g: np.ndarray) -> np.ndarray:
+    hh = np.ascontiguousarray(H, dtype=np.float64).ravel()
+    gg = np.ascontiguousarray(g, dtype=np.float64)
+    dx = np.empty(d)
+    _check(load().fednl_gpu_optionb_solve(_dp(hh), d, lda, l, _dp(gg), _dp(dx)))
+    return dx
+
+
+# ---- whole runs ------------------------------------------------------------------------------
+
+class FedNL:
+    """One FedNL problem resident on the GPU (reference: bin_fednl_local train())."""
+
+    def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
+                 seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0):
+        self.d = prob.d
+        self.lda = lda or reference_lda(prob.d)
+        self.n_clients = prob.n_clients
+        self._ns = np.ascontiguousarray(prob.n_samples, dtype=np.int32)
+        comp = COMPRESSORS[compressor] if isinstance(compressor, str) else int(compressor)
+        self.compressor = comp
+        desc = ProblemDesc(self.d, self.lda, self.n_clients, _ip(self._ns), float(prob.lam), comp, int(k),
+                           float(alpha), int(workers), int(seed_base), int(toplek_seed), int(feature_format),
+                           (C.c_int32 * 4)(0, 0, 0, 0))
+        h = C.c_void_p()
+        _check(load().fednl_gpu_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        try:
+            f = np.ascontiguousarray(prob.features, dtype=np.float64)
+            b = np.ascontiguousarray(prob.labels, dtype=np.float64)
+            _check(load().fednl_gpu_upload_client_data(self._h, _dp(f), _dp(b)))
+            xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+            _check(load().fednl_gpu_init_shifts(self._h, _dp(xx) if xx is not None else None))
+        except Exception:
+            self.close()
+            raise
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().fednl_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def round(self) -> float:
+        st = RoundStats()
+        _check(load().fednl_gpu_round(self._h, C.byref(st)))
+        return st.grad_norm
+
+    def run(self, rounds: int) -> np.ndarray:
+        out = np.empty(rounds)
+        _check(load().fednl_gpu_run(self._h, rounds, _dp(out)))
+        return out
+
+    def time_rounds(self, rounds: int, flush_bytes: int = 0):
+        """Device-timed rounds (CUDA events on the library's stream); returns (total_ms, per_round_ms)."""
+        tot = C.c_double(0.0)
+        per = np.empty(rounds)
+        _check(load().fednl_gpu_time_rounds(self._h, rounds, flush_bytes, C.byref(tot), _dp(per)))
+        return tot.value, per
+
+    def profile_kernels(self, rounds: int, flush_bytes: int = 0):
+        """Mean per-launch time of every kernel of a round: {name: ms}, in launch order."""
+        n = np.zeros(1, dtype=np.int32)
+        ms = np.zeros(32)
+        buf = C.create_string_buffer(2048)
+        _check(load().fednl_gpu_profile_kernels(self._h, rounds, flush_bytes, _ip(n), _dp(ms), buf, 2048))
+        names = buf.value.decode().split(";")
+        return [(names[t], float(ms[t])) for t in range(int(n[0]))]
+
+    def x(self) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_gpu_get_x(self._h, _dp(out)))
+        return out
+
+    def set_x(self, x):
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        _check(load().fednl_gpu_set_x(self._h, _dp(xx)))
+
+    def grad(self) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_gpu_get_grad(self._h, _dp(out)))
+        return out
+
+    def H(self) -> np.ndarray:
+        out = np.empty(self.d * self.lda)
+        _check(load().fednl_gpu_get_H(self._h, _dp(out)))
+        return out
+
+    def shift(self, c: int) -> np.ndarray:
+        out = np.empty(self.d * self.lda)
+        _check(load().fednl_gpu_get_shift(self._h, c, _dp(out)))
+        return out
+
+    def l(self) -> float:
+        return load().fednl_gpu_get_l(self._h)
+
+    def lk(self, c: int) -> float:
+        return load().fednl_gpu_get_lk(self._h, c)
+
+    def message(self, c: int):
+        U = self.d * (self.d + 1) // 2
+        idx = np.empty(U, dtype=np.uint32)
+        val = np.empty(U)
+        cnt = np.zeros(1, dtype=np.int32)
+        _check(load().fednl_gpu_get_message(self._h, c, _up(idx), _dp(val), _ip(cnt)))
+        n = int(cnt[0])
+        return idx[:n].copy(), val[:n].copy()
