@@ -298,11 +298,53 @@ uint32_t orc_pack2_natural(double a, double b)
     return (sa << 23) | (ea << 12) | (sb << 11) | eb;
 }
 
+/* Sum of t[0..n) in a fixed order: chunks of 32 consecutive terms (the last one zero-padded)
+ * are each reduced by the halving tree v[l] += v[l + h], h = 16, 8, 4, 2, 1, and the chunk sums
+ * are added in order.  The reference's norm (VectorND_Raw_SIMD_double.h:749-800) sums in its
+ * SIMD lane order; any fixed order agrees with it to a few ulps, and this one is also the order
+ * of the GB300 kernels (a warp-shuffle tree per 32 entries). */
+static double chunked_sum(const double* t, size_t n)
+{
+    double total = 0.0;
+    for (size_t base = 0; base < n; base += 32) {
+        double v[32];
+        for (int l = 0; l < 32; ++l)
+            v[l] = (base + (size_t)l < n) ? t[base + (size_t)l] : 0.0;
+        for (int h = 16; h > 0; h >>= 1)
+            for (int l = 0; l < h; ++l)
+                v[l] = v[l] + v[l + h];
+        total = total + v[0];
+    }
+    return total;
+}
+
+/* squared L2 norm of a buffer (frobeniusNormSquareForSymmetricMatrixFromUpPart on the full
+ * d x lda buffer, MatrixNMD.h:486-488) */
 double orc_l2sq(const double* v, size_t n)
 {
-    double s = 0.0;
+    double* t = (double*)malloc((n ? n : 1) * sizeof(double));
     for (size_t i = 0; i < n; ++i)
-        s += v[i] * v[i];
+        t[i] = v[i] * v[i];
+    double s = chunked_sum(t, n);
+    free(t);
+    return s;
+}
+
+/* ||M||_F^2 of a symmetric d x lda matrix from its upper part: term (i, j) is m_ij^2, doubled off
+ * the diagonal, taken in upper-index order (column j, rows 0..j) */
+double orc_frob_sym(const double* m, int32_t d, int32_t lda)
+{
+    size_t U = orc_upper_count(d);
+    double* t = (double*)malloc(U * sizeof(double));
+    size_t p = 0;
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i <= j; ++i, ++p) {
+            double v = m[(size_t)j * lda + i];
+            double q = v * v;
+            t[p] = (i == j) ? q : q * 2.0;
+        }
+    double s = chunked_sum(t, U);
+    free(t);
     return s;
 }
 
@@ -323,11 +365,88 @@ void orc_margin(const double* atr, int32_t d, int32_t lda, int32_t n, const doub
     }
 }
 
+/* exp(x), own implementation (the GB300 kernels run the identical operation sequence, so both
+ * give the same bits on every platform).  Method: Cody-Waite reduction x = k ln2 + r with ln2 split
+ * into a 32-bit head and a tail, r kept as a double-double (r_hi, r_lo); exp(r) = 1 + r + r^2/2 +
+ * r^3/6 + r^4 P(r), the first four terms summed with exact two-sum / two-product error terms and
+ * the Taylor tail P (1/24 ... 1/13!) in double; one final rounding; then scaling by 2^k.  The error
+ * before the final rounding is about 1e-3 ulp, so results are correctly rounded except in rare
+ * near-halfway cases.  The reference's sigmoid uses the vectorclass exp in SIMD lanes and libm exp
+ * for the tail (VectorND_Raw_SIMD_double.h:1596-1650), both within an ulp of this. */
+static double pow2i(int k)
+{
+    uint64_t b = (uint64_t)(k + 1023) << 52;
+    double v;
+    memcpy(&v, &b, 8);
+    return v;
+}
+
+static void two_sum(double a, double b, double* s, double* e)
+{
+    double t = a + b;
+    double bb = t - a;
+    *e = (a - (t - bb)) + (b - bb);
+    *s = t;
+}
+
+double orc_exp(double x)
+{
+    if (x != x)
+        return x;
+    if (x > 709.782712893384)
+        return 1.0 / 0.0;
+    if (x < -745.1332191019412)
+        return 0.0;
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    double kd = rint(x * 1.4426950408889634);
+    double t = fma(-kd, ln2_hi, x);                 /* exact */
+    double pl_hi = kd * ln2_lo;
+    double pl_lo = fma(kd, ln2_lo, -pl_hi);
+    double r_hi, e0;
+    two_sum(t, -pl_hi, &r_hi, &e0);
+    double r_lo = e0 - pl_lo;
+    /* r^2 and r^3 with their rounding errors */
+    double r2 = r_hi * r_hi;
+    double r2e = fma(r_hi, r_hi, -r2);
+    double r3 = r2 * r_hi;
+    double r3e = fma(r2, r_hi, -r3) + r2e * r_hi;
+    /* tail r^4 (1/24 + r/120 + ... + r^9/13!) */
+    double q = 1.6059043836821613e-10;
+    q = fma(q, r_hi, 2.0876756987868100e-09);
+    q = fma(q, r_hi, 2.5052108385441720e-08);
+    q = fma(q, r_hi, 2.7557319223985893e-07);
+    q = fma(q, r_hi, 2.7557319223985888e-06);
+    q = fma(q, r_hi, 2.4801587301587302e-05);
+    q = fma(q, r_hi, 1.9841269841269841e-04);
+    q = fma(q, r_hi, 1.3888888888888889e-03);
+    q = fma(q, r_hi, 8.3333333333333332e-03);
+    q = fma(q, r_hi, 4.1666666666666664e-02);
+    double tail = (r2 * r2) * q;
+    /* r^3 / 6 as head + error (1/6 = c6 + c6e) */
+    const double c6 = 1.6666666666666666e-01, c6e = 9.2518585385429707e-18;
+    double s3 = r3 * c6;
+    double s3e = fma(r3, c6, -s3) + (r3e * c6 + r3 * c6e);
+    /* 1 + r_hi + r2/2 + s3, exactly as double-doubles, then all small terms */
+    double s, e1, e2, e3;
+    two_sum(1.0, r_hi, &s, &e1);
+    two_sum(s, r2 * 0.5, &s, &e2);
+    two_sum(s, s3, &s, &e3);
+    double lo = ((e1 + e2) + e3) + ((r2e * 0.5 + s3e) + tail);
+    lo = fma(r_lo, 1.0 + r_hi, lo);                  /* exp(r_hi + r_lo) ~ exp(r_hi)(1 + r_lo) */
+    double p = s + lo;
+    int k = (int)kd;
+    if (k > 1000)
+        return (p * pow2i(k - 1000)) * pow2i(1000);
+    if (k < -1000)
+        return (p * pow2i(k + 1000)) * pow2i(-1000);
+    return p * pow2i(k);
+}
+
 /* elementwiseSigmoid, dopt/dopt/linalg_vectors/include_internal/VectorND_Raw_SIMD_double.h:1596-1650 */
 void orc_sigmoid(const double* m, int32_t n, double* sig)
 {
     for (int32_t s = 0; s < n; ++s)
-        sig[s] = 1.0 / (1.0 + exp(-m[s]));
+        sig[s] = 1.0 / (1.0 + orc_exp(-m[s]));
 }
 
 /* evaluateGradient(x, margin, sigmoid), :148-161:
@@ -379,60 +498,63 @@ void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const dou
 /* ================================================================================== */
 
 /* choleskyFactorization<Mat, fill_L_factor=true, in_input_symmetric=true>
- * dopt/dopt/linalg_matrices/include/factorization/CholeskyFactorization.h:153-272 */
+ * dopt/dopt/linalg_matrices/include/factorization/CholeskyFactorization.h:153-272:
+ * H + l I = R^T R reading only the upper triangle; R is written to the upper triangle of ltr and
+ * mirrored into the lower one.  Restated in right-looking order: a_ij starts at h_ij (+ l on the
+ * diagonal) and receives a_ij = fma(-r_ki, r_kj, a_ij) for k = 0, 1, ... in order; then
+ * r_ii = sqrt(a_ii) and r_ij = (1 / r_ii) a_ij.  The reference accumulates each dot product first
+ * and subtracts it once, which differs by a few ulps; the GB300 kernel follows this order. */
 int orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr)
 {
     memset(ltr, 0, (size_t)d * (size_t)lda * sizeof(double));
-    for (int32_t i = 0; i < d; ++i) {
-        double* ci = ltr + (size_t)i * lda;
-        for (int32_t j = 0; j < i; ++j) {
-            const double* cj = ltr + (size_t)j * lda;
-            double squares = 0.0;
-            for (int32_t t = 0; t < j; ++t)
-                squares += ci[t] * cj[t];
-            double ljj = cj[j];
-            double in_ij = h[(size_t)i * lda + j];
-            double result = (1.0 / ljj) * (in_ij - squares);
-            ci[j] = result;
-            ltr[(size_t)j * lda + i] = result;
-        }
-        double squares = 0.0;
-        for (int32_t t = 0; t < i; ++t)
-            squares += ci[t] * ci[t];
-        double in_ii = h[(size_t)i * lda + i] + l;
-        double result = in_ii - squares;
-        if (result < 0) {
-            if (result > -0.0)
-                result = 0.0;
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i <= j; ++i)
+            ltr[(size_t)j * lda + i] = (i == j) ? h[(size_t)j * lda + i] + l : h[(size_t)j * lda + i];
+    for (int32_t k = 0; k < d; ++k) {
+        double a = ltr[(size_t)k * lda + k];
+        if (a < 0) {
+            if (a > -0.0)
+                a = 0.0;
             else
                 return 0;
         }
-        ci[i] = sqrt(result);
+        double r = sqrt(a);
+        ltr[(size_t)k * lda + k] = r;
+        double inv = 1.0 / r;
+        for (int32_t j = k + 1; j < d; ++j)
+            ltr[(size_t)j * lda + k] *= inv;
+        for (int32_t j = k + 1; j < d; ++j) {
+            double rkj = ltr[(size_t)j * lda + k];
+            double* col = ltr + (size_t)j * lda;
+            for (int32_t i = k + 1; i <= j; ++i)
+                col[i] = fma(-ltr[(size_t)i * lda + k], rkj, col[i]);
+        }
     }
+    for (int32_t j = 0; j < d; ++j)
+        for (int32_t i = 0; i < j; ++i)
+            ltr[(size_t)i * lda + j] = ltr[(size_t)j * lda + i];
     return 1;
 }
 
 /* forwardSubstitutionWithATranspose then backwardSubstitutionWithATranspose
- * dopt/dopt/linalg_linsolvers/include/ElementarySolvers.h:186-224 and :71-128 */
+ * dopt/dopt/linalg_linsolvers/include/ElementarySolvers.h:186-224 and :71-128: R^T y = b, R x = y.
+ * Restated column-oriented: y_t /= r_tt, then y_i = fma(-r_ti, y_t, y_i) for the remaining i. */
 void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
 {
-    double* y = (double*)malloc((size_t)d * sizeof(double));
-    y[0] = b[0] / ltr[0];
-    for (int32_t i = 1; i < d; ++i) {
-        const double* ci = ltr + (size_t)i * lda;
-        double acc = 0.0;
-        for (int32_t j = 0; j < i; ++j)
-            acc += ci[j] * y[j];
-        y[i] = (b[i] - acc) / ci[i];
+    for (int32_t i = 0; i < d; ++i)
+        x[i] = b[i];
+    for (int32_t t = 0; t < d; ++t) {
+        x[t] = x[t] / ltr[(size_t)t * lda + t];
+        double yt = x[t];
+        for (int32_t i = t + 1; i < d; ++i)
+            x[i] = fma(-ltr[(size_t)i * lda + t], yt, x[i]);
     }
-    for (int32_t i = d - 1; i >= 0; --i) {
-        const double* ci = ltr + (size_t)i * lda;
-        double acc = 0.0;
-        for (int32_t j = i + 1; j < d; ++j)
-            acc += ci[j] * x[j];
-        x[i] = (y[i] - acc) / ci[i];
+    for (int32_t t = d - 1; t >= 0; --t) {
+        x[t] = x[t] / ltr[(size_t)t * lda + t];
+        double yt = x[t];
+        for (int32_t i = 0; i < t; ++i)
+            x[i] = fma(-ltr[(size_t)t * lda + i], yt, x[i]);
     }
-    free(y);
 }
 
 /* ================================================================================== */
@@ -489,7 +611,7 @@ static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* 
     orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
     for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
         diff[t] = hbuf[t] - C->shift[t];
-    double frob_sq = orc_l2sq(diff, full);
+    double frob_sq = orc_frob_sym(diff, d, lda);
     C->lk = sqrt(frob_sq);                      /* Lk = ||diff||_F (TopK.h:74-78) */
 
     double alpha = P->alpha, pre = S->prescale;
@@ -729,8 +851,12 @@ int orc_round(orc_state* S, double* grad_norm)
             S->x[i] -= dx[i];
     }
     free(dx);
-    if (grad_norm)
-        *grad_norm = sqrt(orc_l2sq(S->g, (size_t)d));
+    if (grad_norm) {
+        double gs = 0.0;
+        for (int32_t i = 0; i < d; ++i)
+            gs += S->g[i] * S->g[i];
+        *grad_norm = sqrt(gs);
+    }
     return ok ? 0 : -1;
 }
 

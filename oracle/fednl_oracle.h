@@ -67,7 +67,9 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
                    double delta, double frob_sq, uint32_t* rng_state, uint32_t* out);
 double  orc_natural(double v);                       /* mantissa truncation, MatrixNMD.h:2013-2031 */
 uint32_t orc_pack2_natural(double a, double b);      /* pack2FP64NoMantissa, FloatUtils.h:193-221 */
-double  orc_l2sq(const double* v, size_t n);
+double  orc_l2sq(const double* v, size_t n);          /* fixed chunked order, see the .c file */
+double  orc_frob_sym(const double* m, int32_t d, int32_t lda);
+double  orc_exp(double x);
 
 /* ---- logistic-regression oracle (one client) ------------------------------------------ */
 /* atr: d x n col-major with leading dimension lda, column s = b_s * a_s */

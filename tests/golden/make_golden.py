@@ -160,15 +160,15 @@ def main():
     # whole runs: uneven clients, LDA padding (d=13 -> LDA 16), every compressor
     small = datagen.binary_problem(11, 13, [20, 31, 17, 25, 40], 0.3, 1e-3)
     U = 13 * 14 // 2
-    run_case("topk_d13", small, "topk", 26, 1.0, 2, 12, 4)
-    run_case("toplek_d13", small, "toplek", 39, 1.0, 2, 12, 4)
+    run_case("topk_d13", small, "topk", 26, 1.0, 2, 30, 4)
+    run_case("toplek_d13", small, "toplek", 39, 1.0, 2, 30, 4)
     run_case("randk_d13", small, "randk", 26, 26 / U, 2, 12, 4)
     run_case("randseqk_d13", small, "randseqk", 13, 13 / U, 2, 12, 4)
     run_case("natural_d13", small, "natural", U, 1.0 / (1.0 + 1.0 / 8.0), 2, 12, 4)
     run_case("identity_d13", small, "identity", U, 1.0, 2, 12, 4)
     mid = datagen.binary_problem(12, 40, [60, 45, 80, 52, 71, 66, 49], 0.12, 1e-3)
-    run_case("topk_d40", mid, "topk", 320, 1.0, 3, 10, 3)
-    run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 10, 3)
+    run_case("topk_d40", mid, "topk", 320, 1.0, 3, 40, 3)
+    run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 60, 3)
     dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
     run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
 

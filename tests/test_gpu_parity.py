@@ -192,46 +192,36 @@ def test_logreg_oracle_vs_cpu(gpu, oracle, kind):
 
 @pytest.mark.parametrize("path", sorted(glob.glob(golden_path("run_*.npz"))), ids=os.path.basename)
 def test_run_golden(gpu, path):
+    """Whole runs against the reference's golden runs, same contract as the CPU oracle's."""
+    from test_oracle_golden import check_run_against_reference
     z = np.load(path)
     prob = _problem(z)
     fed = gpu.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
                     workers=int(z["workers"]))
-    pos = mi = 0
-    for r in range(int(z["rounds"])):
-        g = fed.round()
-        xr = z["x"][r]
-        np.testing.assert_allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
-        assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
-        assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + 1e-12 * np.max(z["l"])
-        if r < int(z["dump_rounds"]):
-            for c in range(prob.n_clients):
-                cnt = int(z["msg_count"][mi])
-                idx, val = fed.message(c)
-                np.testing.assert_array_equal(idx, z["msg_idx"][pos:pos + cnt])
-                ref = z["msg_val"][pos:pos + cnt]
-                if cnt:
-                    np.testing.assert_allclose(val, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
-                assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-12 * np.max(z["lk"])
-                pos += cnt
-                mi += 1
+    check_run_against_reference(fed, z, prob)
     fed.close()
 
 
 def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None):
+    """GPU and CPU oracle perform the same IEEE operations in the same order: every round's
+    iterate, aggregated gradient, l and every client's message must agree bit for bit."""
     threads = threads or min(workers, os.cpu_count() or 1)
     orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads)
     fed = gpu.FedNL(prob, comp, k, alpha, workers=workers)
     for r in range(rounds):
         go = orc.round()
         gg = fed.round()
-        xo = orc.x()
-        np.testing.assert_allclose(fed.x(), xo, rtol=1e-10, atol=1e-10 * np.max(np.abs(xo)),
-                                   err_msg=f"round {r}")
-        assert abs(gg - go) <= 1e-8 * go + 1e-13 * max(go, 1e-300) + 1e-15
+        np.testing.assert_array_equal(fed.x(), orc.x(), err_msg=f"round {r}: iterate")
+        np.testing.assert_array_equal(fed.grad(), orc.grad(), err_msg=f"round {r}: gradient")
+        assert fed.l() == orc.l(), f"round {r}: l"
+        assert abs(gg - go) <= 1e-14 * go + 1e-300
         for c in range(0, prob.n_clients, max(1, prob.n_clients // 7)):
             io, vo = orc.message(c)
             ig, vg = fed.message(c)
-            np.testing.assert_array_equal(ig, io, err_msg=f"round {r} client {c}")
+            np.testing.assert_array_equal(ig, io, err_msg=f"round {r} client {c}: indices")
+            np.testing.assert_array_equal(vg, vo, err_msg=f"round {r} client {c}: values")
+            assert fed.lk(c) == orc.lk(c)
+    np.testing.assert_array_equal(fed.shift(0), orc.shift(0))
     fed.close()
     orc.close()
 

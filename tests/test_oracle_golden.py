@@ -26,34 +26,64 @@ def _full(m, d, lda):
     return full.reshape(-1)
 
 
+def check_run_against_reference(fed, z, prob):
+    """Shared contract of a whole run against the reference's golden run.
+
+    RandK / RandSeqK / Natural / Identity pick their entries independently of ulp-level noise, so
+    every round must match: messages bit-exact, iterates within 1e-10.  TopK / TopLEK run the
+    reference's heap, whose comparisons hit near-ties a few ulps apart (H_ii and H_i,intercept
+    differ only through the rounding of lambda), so two correct FP64 implementations whose
+    iterates differ in the last bit may pick different entries from some round on.  For them the
+    rounds up to the first differing selection must match exactly, and after convergence both runs
+    must sit on the same unique minimiser (||x - x_ref|| <= (||g|| + ||g_ref||) / lambda + 1e-12)."""
+    chaotic = str(z["compressor"]) in ("topk", "toplek")
+    rounds, dump = int(z["rounds"]), int(z["dump_rounds"])
+    pos = mi = 0
+    diverged_at = None
+    g = None
+    for r in range(rounds):
+        g = fed.round()
+        xr = z["x"][r]
+        same = np.allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
+        if r < dump:
+            for c in range(prob.n_clients):
+                cnt = int(z["msg_count"][mi])
+                idx, val = fed.message(c)
+                ref_i, ref_v = z["msg_idx"][pos:pos + cnt], z["msg_val"][pos:pos + cnt]
+                if diverged_at is None:
+                    if len(idx) == cnt and np.array_equal(idx, ref_i):
+                        if cnt:
+                            np.testing.assert_allclose(val, ref_v, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref_v)))
+                        assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-12 * np.max(z["lk"])
+                    else:
+                        assert chaotic, f"round {r} client {c}: message indices differ"
+                        diverged_at = r
+                pos += cnt
+                mi += 1
+        if diverged_at is None and not same:
+            assert chaotic, f"round {r}: iterate differs"
+            diverged_at = r
+        # beyond the dumped rounds a chaotic run's selections are not observed; its l then
+        # depends on the selection history and only the iterate is compared
+        if diverged_at is None and (r < dump or not chaotic):
+            assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
+            assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + 1e-12 * np.max(z["l"])
+    if diverged_at is not None:
+        assert diverged_at >= 1                 # round 0 never diverges
+        gref = z["gnorm"][-1]
+        assert g <= 1e-9 and gref <= 1e-9, (g, gref)
+        bound = (g + gref) / float(z["lam"]) + 1e-12
+        assert np.linalg.norm(fed.x() - z["x"][-1]) <= bound
+    return diverged_at
+
+
 @pytest.mark.parametrize("path", RUNS, ids=lambda p: os.path.basename(p))
 def test_run_matches_reference(oracle, path):
     z = np.load(path)
     prob = _problem(z)
     fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
                        workers=int(z["workers"]))
-    pos = mi = 0
-    for r in range(int(z["rounds"])):
-        g = fed.round()
-        xr = z["x"][r]
-        np.testing.assert_allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
-        # ||g|| is compared relatively while it is well above the cancellation floor of the
-        # per-client gradient sums (~1e-15 of the first round's norm)
-        assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
-        # l = mean ||H_i - shift_i||_F cancels like ||g||: floor at 1e-12 of its largest value
-        lscale = 1e-12 * np.max(z["l"])
-        assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + lscale
-        if r < int(z["dump_rounds"]):
-            for c in range(prob.n_clients):
-                cnt = int(z["msg_count"][mi])
-                idx, val = fed.message(c)
-                np.testing.assert_array_equal(idx, z["msg_idx"][pos:pos + cnt])
-                ref = z["msg_val"][pos:pos + cnt]
-                if cnt:
-                    np.testing.assert_allclose(val, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
-                assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-12 * np.max(z["lk"])
-                pos += cnt
-                mi += 1
+    check_run_against_reference(fed, z, prob)
     fed.close()
 
 

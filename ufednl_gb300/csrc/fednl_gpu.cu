@@ -95,7 +95,7 @@ struct fednl_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;
     int d = 0, lda = 0, U = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
-    int binary = 0, maxn = 0, nfpart = 0, hcap = 0;
+    int binary = 0, maxn = 0, nfpart = 0, nchunk = 0, hcap = 0;
     bool data_ready = false, shifts_ready = false;
     cudaStream_t stream = nullptr;
     Arena state, feat;
@@ -262,6 +262,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     }
     h->S = h->soff[h->nc];
     h->nfpart = (h->U + kHessPerBlock - 1) / kHessPerBlock;
+    h->nchunk = (h->U + 31) / 32;
     h->hcap = 1;
     if (h->comp == FEDNL_RANDK)
         while (h->hcap < 4 * k) h->hcap <<= 1;
@@ -280,6 +281,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.W = h->W;
     P.SW = h->SW;
     P.nfpart = h->nfpart;
+    P.nchunk = h->nchunk;
     P.hcap = h->hcap;
     P.lambda = D.lambda;
     P.alpha = D.alpha;
@@ -300,7 +302,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.Dv, h->S);
     A.want(&P.qb, h->S);
     A.want(&P.gc, (size_t)h->nc * h->d);
-    A.want(&P.Fpart, (size_t)h->nc * h->nfpart);
+    A.want(&P.Fpart, (size_t)h->nc * h->nchunk);
     A.want(&P.F, h->nc);
     A.want(&P.lk, h->nc);
     A.want(&P.sel, (size_t)h->nc * h->SW);
@@ -675,7 +677,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     int SW = (int)((U + 31) / 32);
     Scratch s;
     CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
-    double *dfull, *dpack, *dF, *dp;
+    double *dfull, *dpack, *dF, *dp, *dcs;
     unsigned *dsel, *dws = nullptr;
     int *dcnt, *dneeds, *dmi, *dwo = nullptr;
     size_t full = (size_t)d * lda;
@@ -683,6 +685,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     s.a.want(&dpack, (size_t)n_mat * U);
     s.a.want(&dF, n_mat);
     s.a.want(&dp, n_mat);
+    s.a.want(&dcs, (size_t)n_mat * ((full + 31) / 32));
     s.a.want(&dsel, (size_t)n_mat * SW);
     s.a.want(&dcnt, n_mat);
     s.a.want(&dneeds, n_mat);
@@ -696,7 +699,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     CK(cudaMemcpyAsync(dfull, mats, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
     k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), n_mat), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
     CKL();
-    k_l2sq_full<<<n_mat, 256, 0, s.st>>>(dfull, (long long)full, dF);
+    k_l2sq_full<<<n_mat, 256, 0, s.st>>>(dfull, (long long)full, dcs, dF);
     CKL();
     if (select_smem(k) > 48 * 1024 && k < U)
         CK(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(k)));

@@ -26,7 +26,7 @@ constexpr unsigned kDiagBit = 0x80000000u;
 
 struct Dev {
     // sizes and scalars
-    int d, lda, U, nc, k, comp, W, SW, nfpart;
+    int d, lda, U, nc, k, comp, W, SW, nfpart, nchunk;
     double lambda, alpha, prescale, inv_n, mult;
     // clients
     const int* ns;          // [nc]
@@ -48,7 +48,7 @@ struct Dev {
     double* Dv;             // [S] Hessian weights D_s
     double* qb;             // [S] gradient weights b_s * q_s
     double* gc;             // [nc][d]
-    double* Fpart;          // [nc][nfpart]
+    double* Fpart;          // [nc][nchunk] sums of 32-entry chunks of ||diff||_F^2 terms
     double* F;              // [nc] ||diff||_F^2
     double* lk;             // [nc]
     unsigned* sel;          // [nc][SW] selection bitmaps over p
@@ -125,6 +125,79 @@ __device__ __forceinline__ double natural_trunc(double v)
     return __longlong_as_double(__double_as_longlong(v) & ~((1ll << 52) - 1));
 }
 
+// exp(x), own implementation with the same IEEE operation sequence as the CPU oracle: Cody-Waite
+// reduction x = k ln2 + r (ln2 = 32-bit head + tail), r as a double-double, exp(r) = 1 + r + r^2/2
+// + r^3/6 + r^4 P(r) with the leading terms summed through exact two-sum / two-product errors and
+// the Taylor tail in double, one final rounding, scaling by 2^k.  Error before the last rounding
+// about 1e-3 ulp.
+__device__ __forceinline__ double pow2i(int k) { return __longlong_as_double((long long)(k + 1023) << 52); }
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e)
+{
+    double t = __dadd_rn(a, b);
+    double bb = __dsub_rn(t, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(t, bb)), __dsub_rn(b, bb));
+    s = t;
+}
+
+__device__ __forceinline__ double fednl_exp(double x)
+{
+    if (x != x) return x;
+    if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000ll);
+    if (x < -745.1332191019412) return 0.0;
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    double kd = rint(__dmul_rn(x, 1.4426950408889634));
+    double t = fma(-kd, ln2_hi, x);
+    double pl_hi = __dmul_rn(kd, ln2_lo);
+    double pl_lo = fma(kd, ln2_lo, -pl_hi);
+    double r_hi, e0;
+    two_sum(t, -pl_hi, r_hi, e0);
+    double r_lo = __dsub_rn(e0, pl_lo);
+    double r2 = __dmul_rn(r_hi, r_hi);
+    double r2e = fma(r_hi, r_hi, -r2);
+    double r3 = __dmul_rn(r2, r_hi);
+    double r3e = __dadd_rn(fma(r2, r_hi, -r3), __dmul_rn(r2e, r_hi));
+    double q = 1.6059043836821613e-10;
+    q = fma(q, r_hi, 2.0876756987868100e-09);
+    q = fma(q, r_hi, 2.5052108385441720e-08);
+    q = fma(q, r_hi, 2.7557319223985893e-07);
+    q = fma(q, r_hi, 2.7557319223985888e-06);
+    q = fma(q, r_hi, 2.4801587301587302e-05);
+    q = fma(q, r_hi, 1.9841269841269841e-04);
+    q = fma(q, r_hi, 1.3888888888888889e-03);
+    q = fma(q, r_hi, 8.3333333333333332e-03);
+    q = fma(q, r_hi, 4.1666666666666664e-02);
+    double tail = __dmul_rn(__dmul_rn(r2, r2), q);
+    const double c6 = 1.6666666666666666e-01, c6e = 9.2518585385429707e-18;
+    double s3 = __dmul_rn(r3, c6);
+    double s3e = __dadd_rn(fma(r3, c6, -s3), __dadd_rn(__dmul_rn(r3e, c6), __dmul_rn(r3, c6e)));
+    double s, e1, e2, e3;
+    two_sum(1.0, r_hi, s, e1);
+    two_sum(s, __dmul_rn(r2, 0.5), s, e2);
+    two_sum(s, s3, s, e3);
+    double lo = __dadd_rn(__dadd_rn(__dadd_rn(e1, e2), e3), __dadd_rn(__dadd_rn(__dmul_rn(r2e, 0.5), s3e), tail));
+    lo = fma(r_lo, __dadd_rn(1.0, r_hi), lo);
+    double p = __dadd_rn(s, lo);
+    int k = (int)kd;
+    if (k > 1000) return __dmul_rn(__dmul_rn(p, pow2i(k - 1000)), pow2i(1000));
+    if (k < -1000) return __dmul_rn(__dmul_rn(p, pow2i(k + 1000)), pow2i(-1000));
+    return __dmul_rn(p, pow2i(k));
+}
+
+__device__ __forceinline__ double fednl_sigmoid(double m)
+{
+    return __ddiv_rn(1.0, __dadd_rn(1.0, fednl_exp(-m)));
+}
+
+// Sum of one aligned 32-term chunk held one term per lane: the halving tree
+// v[l] += v[l + h], h = 16, 8, 4, 2, 1 (valid in lane 0).  Chunk sums are then added in order by
+// one thread.  The CPU oracle sums in exactly this order.
+__device__ __forceinline__ double chunk_tree(double v)
+{
+    for (int h = 16; h > 0; h >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, h));
+    return v;
+}
+
 template <int NT>
 __device__ __forceinline__ double block_sum(double v, double* red)
 {
@@ -153,7 +226,7 @@ __global__ void k_margin_binary(Dev P, int S)
     for (int t = P.rowptr[s]; t < P.rowptr[s + 1]; ++t) acc = __dadd_rn(acc, P.x[P.colidx[t]]);
     double b = P.lab[s];
     double m = (b == 1.0) ? acc : -acc;
-    double sig = 1.0 / (1.0 + exp(-m));
+    double sig = fednl_sigmoid(m);
     double inv_m = 1.0 / (double)P.ns[c];
     double z1 = __dsub_rn(1.0, sig);
     P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
@@ -174,7 +247,7 @@ __global__ void k_margin_dense(Dev P, int S)
         double u = (b == 1.0) ? a[i] : __dmul_rn(a[i], -1.0);
         acc = __dadd_rn(acc, __dmul_rn(u, P.x[i]));
     }
-    double sig = 1.0 / (1.0 + exp(-acc));
+    double sig = fednl_sigmoid(acc);
     double inv_m = 1.0 / (double)P.ns[c];
     double z1 = __dsub_rn(1.0, sig);
     P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
@@ -229,7 +302,6 @@ template <bool SMEM_BITS>
 __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
 {
     extern __shared__ unsigned long long s_fb[];
-    __shared__ double red[kHessThreads / 32];
     int c = blockIdx.y;
     int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
     const unsigned long long* gfb = P.fbits + P.fboff[c];
@@ -247,71 +319,79 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
     __syncthreads();
 
     size_t base = (size_t)c * P.U;
-    double fs = 0.0;
+    int lane = threadIdx.x & 31;
     int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
-    for (int p = blockIdx.x * kHessPerBlock + threadIdx.x; p < p_end; p += blockDim.x) {
-        int i, j;
-        upper_ij(p, i, j);
-        const unsigned long long* mi = fb + (size_t)i * W;
-        const unsigned long long* mj = fb + (size_t)j * W;
-        double h = 0.0;
-        for (int w = 0; w < W; ++w) {
-            unsigned long long m = mi[w] & mj[w];
-            while (m) {
-                int b = __ffsll((long long)m) - 1;
-                m &= m - 1;
-                h = __dadd_rn(h, s_D[w * 64 + b]);
+    // warp-uniform loop: each iteration of a warp covers one aligned chunk of 32 positions
+    for (int p0 = blockIdx.x * kHessPerBlock + (threadIdx.x & ~31); p0 < p_end; p0 += blockDim.x) {
+        int p = p0 + lane;
+        double term = 0.0;
+        if (p < p_end) {
+            int i, j;
+            upper_ij(p, i, j);
+            const unsigned long long* mi = fb + (size_t)i * W;
+            const unsigned long long* mj = fb + (size_t)j * W;
+            double h = 0.0;
+            for (int w = 0; w < W; ++w) {
+                unsigned long long m = mi[w] & mj[w];
+                while (m) {
+                    int b = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    h = __dadd_rn(h, s_D[w * 64 + b]);
+                }
+            }
+            if (i == j) h = __dadd_rn(h, P.lambda);
+            if (mode == 1) {
+                P.shift[base + p] = h;
+            } else {
+                double df = __dsub_rn(h, P.shift[base + p]);
+                P.diff[base + p] = df;
+                double q = __dmul_rn(df, df);
+                term = (i == j) ? q : __dmul_rn(q, 2.0);
             }
         }
-        if (i == j) h = __dadd_rn(h, P.lambda);
-        if (mode == 1) {
-            P.shift[base + p] = h;
-        } else {
-            double df = __dsub_rn(h, P.shift[base + p]);
-            P.diff[base + p] = df;
-            double t = df * df;
-            fs += (i == j) ? t : 2.0 * t;
+        if (mode == 0) {
+            double cs = chunk_tree(term);
+            if (lane == 0) P.Fpart[(size_t)c * P.nchunk + (p0 >> 5)] = cs;
         }
-    }
-    if (mode == 0) {
-        double tot = block_sum<kHessThreads>(fs, red);
-        if (threadIdx.x == 0) P.Fpart[(size_t)c * P.nfpart + blockIdx.x] = tot;
     }
 }
 
 // dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
 __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
 {
-    __shared__ double red[kHessThreads / 32];
     int c = blockIdx.y;
     int n = P.ns[c], off = P.soff[c];
     size_t base = (size_t)c * P.U;
-    double fs = 0.0;
+    int lane = threadIdx.x & 31;
     int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
-    for (int p = blockIdx.x * kHessPerBlock + threadIdx.x; p < p_end; p += blockDim.x) {
-        int i, j;
-        upper_ij(p, i, j);
-        double h = 0.0;
-        for (int s = 0; s < n; ++s) {
-            const double* a = P.A + (size_t)(off + s) * P.d;
-            bool pos = P.lab[off + s] == 1.0;
-            double ui = pos ? a[i] : __dmul_rn(a[i], -1.0);
-            double uj = pos ? a[j] : __dmul_rn(a[j], -1.0);
-            h = __dadd_rn(h, __dmul_rn(ui, __dmul_rn(P.Dv[off + s], uj)));
+    for (int p0 = blockIdx.x * kHessPerBlock + (threadIdx.x & ~31); p0 < p_end; p0 += blockDim.x) {
+        int p = p0 + lane;
+        double term = 0.0;
+        if (p < p_end) {
+            int i, j;
+            upper_ij(p, i, j);
+            double h = 0.0;
+            for (int s = 0; s < n; ++s) {
+                const double* a = P.A + (size_t)(off + s) * P.d;
+                bool pos = P.lab[off + s] == 1.0;
+                double ui = pos ? a[i] : __dmul_rn(a[i], -1.0);
+                double uj = pos ? a[j] : __dmul_rn(a[j], -1.0);
+                h = __dadd_rn(h, __dmul_rn(ui, __dmul_rn(P.Dv[off + s], uj)));
+            }
+            if (i == j) h = __dadd_rn(h, P.lambda);
+            if (mode == 1) {
+                P.shift[base + p] = h;
+            } else {
+                double df = __dsub_rn(h, P.shift[base + p]);
+                P.diff[base + p] = df;
+                double q = __dmul_rn(df, df);
+                term = (i == j) ? q : __dmul_rn(q, 2.0);
+            }
         }
-        if (i == j) h = __dadd_rn(h, P.lambda);
-        if (mode == 1) {
-            P.shift[base + p] = h;
-        } else {
-            double df = __dsub_rn(h, P.shift[base + p]);
-            P.diff[base + p] = df;
-            double t = df * df;
-            fs += (i == j) ? t : 2.0 * t;
+        if (mode == 0) {
+            double cs = chunk_tree(term);
+            if (lane == 0) P.Fpart[(size_t)c * P.nchunk + (p0 >> 5)] = cs;
         }
-    }
-    if (mode == 0) {
-        double tot = block_sum<kHessThreads>(fs, red);
-        if (threadIdx.x == 0) P.Fpart[(size_t)c * P.nfpart + blockIdx.x] = tot;
     }
 }
 
@@ -321,7 +401,7 @@ __global__ void k_fsum(Dev P)
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.nc) return;
     double f = 0.0;
-    for (int b = 0; b < P.nfpart; ++b) f += P.Fpart[(size_t)c * P.nfpart + b];
+    for (int q = 0; q < P.nchunk; ++q) f = __dadd_rn(f, P.Fpart[(size_t)c * P.nchunk + q]);
     P.F[c] = f;
     P.lk[c] = sqrt(f);
 }
@@ -713,12 +793,12 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_solve(Dev P, const double
         __syncthreads();
         if (s_fail) break;
         double inv = s_r;
-        for (int j = kk + 1 + threadIdx.x; j < d; j += blockDim.x) A[up_pos(kk, j)] *= inv;
+        for (int j = kk + 1 + threadIdx.x; j < d; j += blockDim.x) A[up_pos(kk, j)] = __dmul_rn(A[up_pos(kk, j)], inv);
         __syncthreads();
         for (int j = kk + 1 + warp; j < d; j += nw) {
             double rkj = A[up_pos(kk, j)];
             double* col = A + up_pos(0, j);
-            for (int i = kk + 1 + lane; i <= j; i += 32) col[i] -= A[up_pos(kk, i)] * rkj;
+            for (int i = kk + 1 + lane; i <= j; i += 32) col[i] = fma(-A[up_pos(kk, i)], rkj, col[i]);
         }
         __syncthreads();
     }
@@ -735,18 +815,18 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_solve(Dev P, const double
     for (int i = threadIdx.x; i < d; i += blockDim.x) y[i] = gin[i];
     __syncthreads();
     for (int t = 0; t < d; ++t) {
-        if (threadIdx.x == 0) y[t] = y[t] / A[up_pos(t, t)];
+        if (threadIdx.x == 0) y[t] = __ddiv_rn(y[t], A[up_pos(t, t)]);
         __syncthreads();
         double yt = y[t];
-        for (int i = t + 1 + threadIdx.x; i < d; i += blockDim.x) y[i] -= A[up_pos(t, i)] * yt;
+        for (int i = t + 1 + threadIdx.x; i < d; i += blockDim.x) y[i] = fma(-A[up_pos(t, i)], yt, y[i]);
         __syncthreads();
     }
     // R dx = y (column-oriented backward substitution)
     for (int t = d - 1; t >= 0; --t) {
-        if (threadIdx.x == 0) y[t] = y[t] / A[up_pos(t, t)];
+        if (threadIdx.x == 0) y[t] = __ddiv_rn(y[t], A[up_pos(t, t)]);
         __syncthreads();
         double yt = y[t];
-        for (int i = threadIdx.x; i < t; i += blockDim.x) y[i] -= A[up_pos(i, t)] * yt;
+        for (int i = threadIdx.x; i < t; i += blockDim.x) y[i] = fma(-A[up_pos(i, t)], yt, y[i]);
         __syncthreads();
     }
     for (int i = threadIdx.x; i < d; i += blockDim.x) {
@@ -773,15 +853,27 @@ __global__ void k_pack_upper(const double* full, int d, int lda, int U, double* 
     }
 }
 
-__global__ void __launch_bounds__(256) k_l2sq_full(const double* full, long long len, double* out)
+// squared L2 norm of whole d x lda buffers in the chunked order (chunk sums by the warp tree,
+// then in order by one thread); csum: [n_mat][ceil(len / 32)] scratch
+__global__ void __launch_bounds__(256) k_l2sq_full(const double* full, long long len, double* csum, double* out)
 {
-    __shared__ double red[8];
     int t = blockIdx.x;
     const double* m = full + (size_t)t * len;
-    double s = 0.0;
-    for (long long e = threadIdx.x; e < len; e += blockDim.x) s += m[e] * m[e];
-    double tot = block_sum<256>(s, red);
-    if (threadIdx.x == 0) out[t] = tot;
+    long long nch = (len + 31) / 32;
+    double* cs = csum + (size_t)t * nch;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (long long q = warp; q < nch; q += blockDim.x / 32) {
+        long long e = q * 32 + lane;
+        double v = (e < len) ? __dmul_rn(m[e], m[e]) : 0.0;
+        double s = chunk_tree(v);
+        if (lane == 0) cs[q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double f = 0.0;
+        for (long long q = 0; q < nch; ++q) f = __dadd_rn(f, cs[q]);
+        out[t] = f;
+    }
 }
 
 __global__ void k_natural(const double* in, long long n, double* out)
