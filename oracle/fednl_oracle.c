@@ -330,22 +330,50 @@ double orc_l2sq(const double* v, size_t n)
     return s;
 }
 
-/* ||M||_F^2 of a symmetric d x lda matrix from its upper part: term (i, j) is m_ij^2, doubled off
- * the diagonal, taken in upper-index order (column j, rows 0..j) */
+/* ||M||_F^2 of a symmetric d x lda matrix from its upper part (the reference's
+ * frobeniusNormForSymmetricMatrixFromUpPart over the full buffer, MatrixNMD.h:478-488), in a fixed
+ * order that the GB300 kernel follows exactly: upper positions p (column j, rows 0..j) are cut into
+ * segments of 512; inside a segment, lane l = p mod 32 accumulates m_p^2 over its 16 positions in
+ * order, diagonal entries into a_l and off-diagonal ones into b_l; lane l contributes
+ * v_l = a_l + 2 b_l, the 32 lane values are reduced by the halving tree, and the segment sums are
+ * added in order. */
 double orc_frob_sym(const double* m, int32_t d, int32_t lda)
 {
     size_t U = orc_upper_count(d);
-    double* t = (double*)malloc(U * sizeof(double));
+    uint32_t* col = (uint32_t*)malloc(U * sizeof(uint32_t));
+    uint32_t* row = (uint32_t*)malloc(U * sizeof(uint32_t));
     size_t p = 0;
     for (int32_t j = 0; j < d; ++j)
         for (int32_t i = 0; i <= j; ++i, ++p) {
-            double v = m[(size_t)j * lda + i];
-            double q = v * v;
-            t[p] = (i == j) ? q : q * 2.0;
+            col[p] = (uint32_t)j;
+            row[p] = (uint32_t)i;
         }
-    double s = chunked_sum(t, U);
-    free(t);
-    return s;
+    double total = 0.0;
+    for (size_t seg = 0; seg < U; seg += 512) {
+        double v[32];
+        for (int l = 0; l < 32; ++l) {
+            double a = 0.0, b = 0.0;
+            for (int q = 0; q < 16; ++q) {
+                size_t pp = seg + 32 * (size_t)q + (size_t)l;
+                if (pp >= U)
+                    continue;
+                double x = m[(size_t)col[pp] * lda + row[pp]];
+                double t = x * x;
+                if (row[pp] == col[pp])
+                    a = a + t;
+                else
+                    b = b + t;
+            }
+            v[l] = a + b * 2.0;
+        }
+        for (int h = 16; h > 0; h >>= 1)
+            for (int l = 0; l < h; ++l)
+                v[l] = v[l] + v[l + h];
+        total = total + v[0];
+    }
+    free(col);
+    free(row);
+    return total;
 }
 
 /* ================================================================================== */

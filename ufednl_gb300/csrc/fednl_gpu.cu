@@ -87,7 +87,38 @@ int ensure_device()
     return FEDNL_OK;
 }
 
-size_t select_smem(int k) { return (size_t)k * (sizeof(double) + sizeof(unsigned)); }
+size_t select_smem(int k) { return select_smem_bytes(k); }
+
+// CTAs of the cooperative Cholesky: enough threads for the first trailing update, at most one
+// resident CTA per SM
+int chol_grid(int d)
+{
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_coop, kCoopThreads, 0);
+    long long m = d > kCholNB ? d - kCholNB : 1;
+    long long want = (m * (m + 1) / 2 + kCoopThreads - 1) / kCoopThreads;
+    long long g = std::min<long long>(want, (long long)sms * std::max(bps, 1));
+    g = std::min<long long>(g, sms);
+    return (int)std::max<long long>(1, g);
+}
+
+cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* Hin, const double* lptr, double lval,
+                        const double* gin, double* dxout, double* xupd, int record)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kCoopThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, lptr, lval, gin, dxout, xupd, record);
+}
 
 }  // namespace
 
@@ -95,7 +126,7 @@ struct fednl_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;
     int d = 0, lda = 0, U = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
-    int binary = 0, maxn = 0, nfpart = 0, nchunk = 0, hcap = 0;
+    int binary = 0, maxn = 0, nfpart = 0, nseg = 0, hcap = 0;
     bool data_ready = false, shifts_ready = false;
     cudaStream_t stream = nullptr;
     Arena state, feat;
@@ -104,6 +135,7 @@ struct fednl_handle_s {
     cudaGraphExec_t gexec = nullptr;
     size_t hess_smem = 0;
     bool hess_smem_bits = true;
+    int chol_grid = 1;
     int rounds_done = 0;
     void* flush_buf = nullptr;
     size_t flush_cap = 0;
@@ -143,7 +175,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     CKL();
     MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
     dim3 gg((h->d + 127) / 128, h->nc);
-    if (h->binary) k_grad_binary<<<gg, 128, 0, st>>>(P);
+    if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, st>>>(P);
     else k_grad_dense<<<gg, 128, 0, st>>>(P);
     CKL();
     MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
@@ -156,7 +188,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     }
     CKL();
     MARK("k_fsum");
-    k_fsum<<<(h->nc + 127) / 128, 128, 0, st>>>(P);
+    k_fsum<<<(h->nc + 3) / 4, 128, 0, st>>>(P);
     CKL();
     int comp = h->comp;
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
@@ -184,11 +216,10 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     k_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     CKL();
     MARK("k_aggregate");
-    k_aggregate<<<1, kAggThreads, 0, st>>>(P);
+    k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads, kAggThreads, 0, st>>>(P);
     CKL();
-    MARK("k_chol_solve");
-    k_chol_solve<<<1, kCholThreads, 0, st>>>(P, P.H, P.stats + 1, 0.0, P.g, P.dx, P.x, 1);
-    CKL();
+    MARK("k_chol_coop");
+    CK(launch_chol(P, h->chol_grid, st, P.H, P.stats + 1, 0.0, P.g, P.dx, P.x, 1));
     MARK("end");
     return FEDNL_OK;
 }
@@ -262,7 +293,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     }
     h->S = h->soff[h->nc];
     h->nfpart = (h->U + kHessPerBlock - 1) / kHessPerBlock;
-    h->nchunk = (h->U + 31) / 32;
+    h->nseg = (h->U + 511) / 512;
     h->hcap = 1;
     if (h->comp == FEDNL_RANDK)
         while (h->hcap < 4 * k) h->hcap <<= 1;
@@ -281,7 +312,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.W = h->W;
     P.SW = h->SW;
     P.nfpart = h->nfpart;
-    P.nchunk = h->nchunk;
+    P.nseg = h->nseg;
     P.hcap = h->hcap;
     P.lambda = D.lambda;
     P.alpha = D.alpha;
@@ -302,7 +333,8 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.Dv, h->S);
     A.want(&P.qb, h->S);
     A.want(&P.gc, (size_t)h->nc * h->d);
-    A.want(&P.Fpart, (size_t)h->nc * h->nchunk);
+    A.want(&P.Fpart, (size_t)h->nc * h->nseg);
+    A.want(&P.dsum, (size_t)h->nc * h->d);
     A.want(&P.F, h->nc);
     A.want(&P.lk, h->nc);
     A.want(&P.sel, (size_t)h->nc * h->SW);
@@ -321,6 +353,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.round_ctr, 1);
     A.want(&P.status, 1);
     A.want(&P.stats, 2);
+    A.want(&P.bar, 4);
     rc = A.commit();
     if (rc) {
         cudaStreamDestroy(h->stream);
@@ -334,12 +367,13 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
         cudaMemcpy((void*)P.soff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy((void*)P.client_of, client_of.data(), (size_t)h->S * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(P.x, 0, h->d * 8) != cudaSuccess || cudaMemset(P.round_ctr, 0, 4) != cudaSuccess ||
-        cudaMemset(P.status, 0, 4) != cudaSuccess) {
+        cudaMemset(P.status, 0, 4) != cudaSuccess || cudaMemset(P.bar, 0, 16) != cudaSuccess) {
         fednl_gpu_destroy(h);
         return fail(FEDNL_ECUDA, "initial copies failed");
     }
     if (select_smem(h->k) > 48 * 1024 && h->k < h->U)
         cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(h->k));
+    h->chol_grid = chol_grid(h->d);
     *out = h;
     return FEDNL_OK;
 }
@@ -378,6 +412,7 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     P.rowptr = nullptr;
     P.colidx = nullptr;
     P.fbits = nullptr;
+    P.icpt = nullptr;
     P.A = nullptr;
     double* lab = nullptr;
     if (fmt == FEDNL_FEATURES_BINARY) {
@@ -405,9 +440,17 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
                 rowptr[s + 1] = (int)colidx.size();
             }
         }
-        int *d_rowptr, *d_colidx;
+        std::vector<int> icpt(h->nc, 1);
+        for (int c = 0; c < h->nc; ++c)
+            for (int s = h->soff[c]; s < h->soff[c + 1]; ++s)
+                if (features[(size_t)s * d + (d - 1)] != 1.0) {
+                    icpt[c] = 0;
+                    break;
+                }
+        int *d_rowptr, *d_colidx, *d_icpt;
         long long* d_fboff;
         unsigned long long* d_fbits;
+        h->feat.want(&d_icpt, h->nc);
         h->feat.want(&d_rowptr, S + 1);
         h->feat.want(&d_colidx, std::max<size_t>(1, colidx.size()));
         h->feat.want(&d_fboff, h->nc);
@@ -419,6 +462,8 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         if (!colidx.empty()) CK(cudaMemcpy(d_colidx, colidx.data(), colidx.size() * 4, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_fboff, fboff.data(), h->nc * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_fbits, fbits.data(), words * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_icpt, icpt.data(), h->nc * 4, cudaMemcpyHostToDevice));
+        P.icpt = d_icpt;
         P.rowptr = d_rowptr;
         P.colidx = d_colidx;
         P.fboff = d_fboff;
@@ -432,6 +477,8 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
             CK(cudaFuncSetAttribute(k_hess_binary<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
         else
             CK(cudaFuncSetAttribute(k_hess_binary<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
+        if ((size_t)h->maxn * 16 > 48 * 1024)
+            CK(cudaFuncSetAttribute(k_grad_binary, cudaFuncAttributeMaxDynamicSharedMemorySize, h->maxn * 16));
         h->binary = 1;
     } else {
         double* dA;
@@ -468,6 +515,10 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
     if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     CKL();
+    if (h->binary) {    // gradient pass also forms the diagonal sums the Hessian kernel reuses
+        k_grad_binary<<<dim3((h->d + 127) / 128, h->nc), 128, (size_t)h->maxn * 16, st>>>(P);
+        CKL();
+    }
     dim3 hg(h->nfpart, h->nc);
     if (h->binary) {
         if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, 1);
@@ -509,6 +560,7 @@ int fednl_gpu_run(fednl_handle h, int32_t rounds, double* grad_norms)
     }
     int status = 0;
     CK(cudaMemcpy(&status, h->dev.status, 4, cudaMemcpyDeviceToHost));
+    if (status == FEDNL_ETIMEOUT) return fail(status, "grid barrier of the Cholesky timed out");
     if (status) return fail(status, "Option-B matrix not positive definite in one of the rounds");
     return FEDNL_OK;
 }
@@ -861,7 +913,7 @@ int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_
     if (!rc && grad) {
         Dev& P = h->dev;
         dim3 gg((d + 127) / 128, 1);
-        if (h->binary) k_grad_binary<<<gg, 128, 0, h->stream>>>(P);
+        if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, h->stream>>>(P);
         else k_grad_dense<<<gg, 128, 0, h->stream>>>(P);
         cudaError_t e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) rc = fail(FEDNL_ECUDA, "gradient kernel failed: %s", cudaGetErrorString(e));
@@ -889,20 +941,22 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     s.a.want(&P.dx, d);
     s.a.want(&P.ybuf, d);
     s.a.want(&P.status, 1);
+    s.a.want(&P.bar, 4);
     rc = s.a.commit();
     if (rc) return rc;
     P.d = d;
     P.U = (int)U;
+    CK(cudaMemsetAsync(P.bar, 0, 16, s.st));
     CK(cudaMemcpyAsync(dfull, H, (size_t)d * lda * 8, cudaMemcpyHostToDevice, s.st));
     CK(cudaMemcpyAsync(dg, g, d * 8, cudaMemcpyHostToDevice, s.st));
     CK(cudaMemsetAsync(P.status, 0, 4, s.st));
     k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
     CKL();
-    k_chol_solve<<<1, kCholThreads, 0, s.st>>>(P, dpack, nullptr, l, dg, P.dx, nullptr, 0);
-    CKL();
+    CK(launch_chol(P, chol_grid(d), s.st, dpack, nullptr, l, dg, P.dx, nullptr, 0));
     int status = 0;
     CK(cudaMemcpyAsync(&status, P.status, 4, cudaMemcpyDeviceToHost, s.st));
     CK(cudaStreamSynchronize(s.st));
+    if (status == FEDNL_ETIMEOUT) return fail(FEDNL_ETIMEOUT, "grid barrier of the Cholesky timed out");
     if (status) return fail(FEDNL_ENOTPD, "H + l I is not positive definite");
     CK(cudaMemcpy(dx, P.dx, d * 8, cudaMemcpyDeviceToHost));
     return FEDNL_OK;

@@ -21,12 +21,12 @@
 
 namespace fednl {
 
-constexpr int kMaxK = 16384;            // largest TopK/TopLEK k held in shared memory
+constexpr int kMaxK = 9600;             // largest TopK/TopLEK k: heap, chain and staging fit in 227 KB of shared memory
 constexpr unsigned kDiagBit = 0x80000000u;
 
 struct Dev {
     // sizes and scalars
-    int d, lda, U, nc, k, comp, W, SW, nfpart, nchunk;
+    int d, lda, U, nc, k, comp, W, SW, nfpart, nseg;
     double lambda, alpha, prescale, inv_n, mult;
     // clients
     const int* ns;          // [nc]
@@ -48,7 +48,9 @@ struct Dev {
     double* Dv;             // [S] Hessian weights D_s
     double* qb;             // [S] gradient weights b_s * q_s
     double* gc;             // [nc][d]
-    double* Fpart;          // [nc][nchunk] sums of 32-entry chunks of ||diff||_F^2 terms
+    double* dsum;           // [nc][d] sum of D_s over the samples with attribute j set (Hessian diagonal - lambda)
+    const int* icpt;        // [nc] 1 if the client's last attribute is 1 for every sample (intercept)
+    double* Fpart;          // [nc][nseg] segment sums of ||diff||_F^2 (512 upper positions each)
     double* F;              // [nc] ||diff||_F^2
     double* lk;             // [nc]
     unsigned* sel;          // [nc][SW] selection bitmaps over p
@@ -69,6 +71,7 @@ struct Dev {
     int* status;            // [1]
     double* stats;          // [2] ||g||, l
     int hist_cap;
+    unsigned* bar;          // [4] grid barrier: arrival count, generation, error flag
 };
 
 // ---- helpers -------------------------------------------------------------------------------
@@ -255,23 +258,35 @@ __global__ void k_margin_dense(Dev P, int S)
 }
 
 // ---- 2. client gradients g_c = lambda x + sum_s Atr[:, s] q_s (samples in order) ----------
+// One block per (client, range of attributes); the client's weights are staged in shared memory.
+// The same bit loop also forms dsum_j = sum of D_s over the samples with attribute j set, which is
+// bit for bit the Hessian diagonal before lambda (and the intercept column) of evaluateHessian.
 __global__ void k_grad_binary(Dev P)
 {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    int c = blockIdx.y;
+    extern __shared__ double s_w[];    // [n] b_s q_s, then [n] D_s
+    const int c = blockIdx.y;
+    const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        s_w[t] = P.qb[off + t];
+        s_w[n + t] = P.Dv[off + t];
+    }
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= P.d) return;
-    int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
     const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
     double g = __dmul_rn(P.x[j], P.lambda);
+    double hs = 0.0;
     for (int w = 0; w < W; ++w) {
         unsigned long long m = fb[w];
         while (m) {
-            int b = __ffsll((long long)m) - 1;
+            const int b = w * 64 + __ffsll((long long)m) - 1;
             m &= m - 1;
-            g = __dadd_rn(g, P.qb[off + w * 64 + b]);
+            g = __dadd_rn(g, s_w[b]);
+            hs = __dadd_rn(hs, s_w[n + b]);
         }
     }
     P.gc[(size_t)c * P.d + j] = g;
+    P.dsum[(size_t)c * P.d + j] = hs;
 }
 
 __global__ void k_grad_dense(Dev P)
@@ -298,12 +313,17 @@ __global__ void k_grad_dense(Dev P)
 constexpr int kHessThreads = 256;
 constexpr int kHessPerBlock = 4096;     // upper entries per block
 
+// Fixed-order ||diff||_F^2 (the CPU oracle's orc_frob_sym): each warp owns one segment of 512
+// upper positions; lane l accumulates its 16 terms, diagonal (a) and off-diagonal (b) apart, then
+// contributes a + 2 b to the segment's halving tree.
+__device__ __forceinline__ double segment_value(double a, double b) { return __dadd_rn(a, __dmul_rn(b, 2.0)); }
+
 template <bool SMEM_BITS>
 __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
 {
     extern __shared__ unsigned long long s_fb[];
-    int c = blockIdx.y;
-    int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    const int c = blockIdx.y;
+    const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
     const unsigned long long* gfb = P.fbits + P.fboff[c];
     double* s_D;
     const unsigned long long* fb;
@@ -318,92 +338,109 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
     for (int t = threadIdx.x; t < n; t += blockDim.x) s_D[t] = P.Dv[off + t];
     __syncthreads();
 
-    size_t base = (size_t)c * P.U;
-    int lane = threadIdx.x & 31;
-    int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
-    // warp-uniform loop: each iteration of a warp covers one aligned chunk of 32 positions
-    for (int p0 = blockIdx.x * kHessPerBlock + (threadIdx.x & ~31); p0 < p_end; p0 += blockDim.x) {
-        int p = p0 + lane;
-        double term = 0.0;
-        if (p < p_end) {
-            int i, j;
-            upper_ij(p, i, j);
+    const size_t base = (size_t)c * P.U;
+    const double* dsum = P.dsum + (size_t)c * P.d;
+    const bool icpt = P.icpt[c] != 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = blockIdx.x * (kHessThreads / 32) + warp;     // 512 positions per warp
+    const int p_seg = seg * 512;
+    double fa = 0.0, fb2 = 0.0;
+    for (int q = 0; q < 16; ++q) {
+        const int p = p_seg + 32 * q + lane;
+        if (p >= P.U) break;
+        int i, j;
+        upper_ij(p, i, j);
+        double h;
+        if (i == j) {
+            h = __dadd_rn(dsum[i], P.lambda);
+        } else if (icpt && j == P.d - 1) {
+            h = dsum[i];               // samples with attribute i set, all of which have the intercept
+        } else {
             const unsigned long long* mi = fb + (size_t)i * W;
             const unsigned long long* mj = fb + (size_t)j * W;
-            double h = 0.0;
+            h = 0.0;
             for (int w = 0; w < W; ++w) {
                 unsigned long long m = mi[w] & mj[w];
                 while (m) {
-                    int b = __ffsll((long long)m) - 1;
+                    const int b = __ffsll((long long)m) - 1;
                     m &= m - 1;
                     h = __dadd_rn(h, s_D[w * 64 + b]);
                 }
             }
-            if (i == j) h = __dadd_rn(h, P.lambda);
-            if (mode == 1) {
-                P.shift[base + p] = h;
-            } else {
-                double df = __dsub_rn(h, P.shift[base + p]);
-                P.diff[base + p] = df;
-                double q = __dmul_rn(df, df);
-                term = (i == j) ? q : __dmul_rn(q, 2.0);
-            }
         }
-        if (mode == 0) {
-            double cs = chunk_tree(term);
-            if (lane == 0) P.Fpart[(size_t)c * P.nchunk + (p0 >> 5)] = cs;
+        if (mode == 1) {
+            P.shift[base + p] = h;
+        } else {
+            const double df = __dsub_rn(h, P.shift[base + p]);
+            P.diff[base + p] = df;
+            const double t = __dmul_rn(df, df);
+            if (i == j) fa = __dadd_rn(fa, t);
+            else fb2 = __dadd_rn(fb2, t);
         }
+    }
+    if (mode == 0 && p_seg < P.U) {
+        const double cs = chunk_tree(segment_value(fa, fb2));
+        if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
 }
 
 // dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
 __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
 {
-    int c = blockIdx.y;
-    int n = P.ns[c], off = P.soff[c];
-    size_t base = (size_t)c * P.U;
-    int lane = threadIdx.x & 31;
-    int p_end = min(P.U, (blockIdx.x + 1) * kHessPerBlock);
-    for (int p0 = blockIdx.x * kHessPerBlock + (threadIdx.x & ~31); p0 < p_end; p0 += blockDim.x) {
-        int p = p0 + lane;
-        double term = 0.0;
-        if (p < p_end) {
-            int i, j;
-            upper_ij(p, i, j);
-            double h = 0.0;
-            for (int s = 0; s < n; ++s) {
-                const double* a = P.A + (size_t)(off + s) * P.d;
-                bool pos = P.lab[off + s] == 1.0;
-                double ui = pos ? a[i] : __dmul_rn(a[i], -1.0);
-                double uj = pos ? a[j] : __dmul_rn(a[j], -1.0);
-                h = __dadd_rn(h, __dmul_rn(ui, __dmul_rn(P.Dv[off + s], uj)));
-            }
-            if (i == j) h = __dadd_rn(h, P.lambda);
-            if (mode == 1) {
-                P.shift[base + p] = h;
-            } else {
-                double df = __dsub_rn(h, P.shift[base + p]);
-                P.diff[base + p] = df;
-                double q = __dmul_rn(df, df);
-                term = (i == j) ? q : __dmul_rn(q, 2.0);
-            }
+    const int c = blockIdx.y;
+    const int n = P.ns[c], off = P.soff[c];
+    const size_t base = (size_t)c * P.U;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = blockIdx.x * (kHessThreads / 32) + warp;
+    const int p_seg = seg * 512;
+    double fa = 0.0, fb2 = 0.0;
+    for (int q = 0; q < 16; ++q) {
+        const int p = p_seg + 32 * q + lane;
+        if (p >= P.U) break;
+        int i, j;
+        upper_ij(p, i, j);
+        double h = 0.0;
+        for (int s = 0; s < n; ++s) {
+            const double* a = P.A + (size_t)(off + s) * P.d;
+            const bool pos = P.lab[off + s] == 1.0;
+            const double ui = pos ? a[i] : __dmul_rn(a[i], -1.0);
+            const double uj = pos ? a[j] : __dmul_rn(a[j], -1.0);
+            h = __dadd_rn(h, __dmul_rn(ui, __dmul_rn(P.Dv[off + s], uj)));
         }
-        if (mode == 0) {
-            double cs = chunk_tree(term);
-            if (lane == 0) P.Fpart[(size_t)c * P.nchunk + (p0 >> 5)] = cs;
+        if (i == j) h = __dadd_rn(h, P.lambda);
+        if (mode == 1) {
+            P.shift[base + p] = h;
+        } else {
+            const double df = __dsub_rn(h, P.shift[base + p]);
+            P.diff[base + p] = df;
+            const double t = __dmul_rn(df, df);
+            if (i == j) fa = __dadd_rn(fa, t);
+            else fb2 = __dadd_rn(fb2, t);
         }
+    }
+    if (mode == 0 && p_seg < P.U) {
+        const double cs = chunk_tree(segment_value(fa, fb2));
+        if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
 }
 
-// per-client ||diff||_F^2 and Lk = ||diff||_F (TopK.h:74-78)
+// per-client ||diff||_F^2 (segment sums in order) and Lk = ||diff||_F (TopK.h:74-78)
 __global__ void k_fsum(Dev P)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (c >= P.nc) return;
+    const double* fp = P.Fpart + (size_t)c * P.nseg;
     double f = 0.0;
-    for (int q = 0; q < P.nchunk; ++q) f = __dadd_rn(f, P.Fpart[(size_t)c * P.nchunk + q]);
-    P.F[c] = f;
-    P.lk[c] = sqrt(f);
+    for (int q0 = 0; q0 < P.nseg; q0 += 32) {
+        const double v = (q0 + lane < P.nseg) ? fp[q0 + lane] : 0.0;
+        const int cnt = min(32, P.nseg - q0);
+        for (int t = 0; t < cnt; ++t) f = __dadd_rn(f, __shfl_sync(0xffffffffu, v, t));
+    }
+    if (lane == 0) {
+        P.F[c] = f;
+        P.lk[c] = sqrt(f);
+    }
 }
 
 // master H = mean_i shift_i after the initial shifts (TrainLoop.h:639-643, :732-735)
@@ -422,16 +459,27 @@ __global__ void k_h_init(Dev P)
 // minHeapify keeps comparing a node's children with the value that moved up on the previous
 // level (MinHeap.h:259-286), so its "heap" is not a true heap and the selected set is not the
 // plain top-k by magnitude; every comparison, swap and tie is reproduced here step by step.
-// One warp per matrix performs the sequential heap work in shared memory; the scan over the
-// remaining entries is done 32 entries at a time with a warp ballot against the current root.
+//
+// Keys are the IEEE bit patterns of |v| compared as unsigned 64-bit integers: for non-negative
+// doubles this order is exactly the floating-point order (and avoids GB300's slow FP64 compare).
+// One warp per matrix does the sequential heap work in shared memory; the other warps stage the
+// scanned entries into a double buffer.  TopLEK's extraction loop runs to the end recording the
+// extraction order in place (extracFromMinHeap leaves the extracted element at the array's end,
+// MinHeap.h:133-140), its numerator is then one FP64 add chain in the reference's order (heap
+// array order, then extraction order), and the rounding window (:475-476) is found afterwards.
 struct HeapS {
-    double* key;     // |value|
-    unsigned* hid;   // p | kDiagBit
+    unsigned long long* key;   // bits of |value|
+    unsigned* hid;             // p | kDiagBit
 };
+
+__device__ __forceinline__ unsigned long long abs_bits(double v)
+{
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
 
 __device__ __forceinline__ void heap_swap(HeapS& h, int a, int b)
 {
-    double tk = h.key[a];
+    unsigned long long tk = h.key[a];
     h.key[a] = h.key[b];
     h.key[b] = tk;
     unsigned ti = h.hid[a];
@@ -442,13 +490,13 @@ __device__ __forceinline__ void heap_swap(HeapS& h, int a, int b)
 // minHeapify, MinHeap.h:255-290 (lowest value carried across levels as in the reference)
 __device__ void heap_sift(HeapS& h, int i, int heap_size)
 {
-    double lowest_value = h.key[i];
+    unsigned long long lowest_value = h.key[i];
     for (;;) {
         int lowest = i;
-        int first = 4 * i + 1;
-        int last = min(first + 4, heap_size);
+        const int first = 4 * i + 1;
+        const int last = min(first + 4, heap_size);
         for (int c = first; c < last; ++c) {
-            double cv = h.key[c];
+            const unsigned long long cv = h.key[c];
             if (lowest_value > cv) {
                 lowest = c;
                 lowest_value = cv;
@@ -463,134 +511,174 @@ __device__ void heap_sift(HeapS& h, int i, int heap_size)
     }
 }
 
-__device__ void heap_insert(HeapS& h, int& size, double key, unsigned id)
+constexpr int kSelThreads = 128;
+constexpr int kSelStage = 2048;            // staged entries per buffer (two buffers)
+
+__device__ __forceinline__ double term_of(unsigned long long key, unsigned id)
 {
-    int i = size++;
-    h.key[i] = key;
-    h.hid[i] = id;
-    while (i != 0 && h.key[(i - 1) / 4] > h.key[i]) {
-        heap_swap(h, (i - 1) / 4, i);
-        i = (i - 1) / 4;
-    }
+    double v = __longlong_as_double((long long)key);
+    double t = __dmul_rn(v, v);
+    return (id & kDiagBit) ? t : __dmul_rn(t, 2.0);
 }
 
-constexpr int kSelThreads = 128;
+size_t __host__ __device__ inline select_smem_bytes(int k)
+{
+    return (size_t)k * (sizeof(unsigned long long) + sizeof(unsigned)) + (size_t)k * sizeof(double) +
+           2 * kSelStage * sizeof(unsigned long long);
+}
 
-// vals: [n_mat][U] packed upper values (signed); F: [n_mat] squared Frobenius norm of the full
-// matrix.  Output: sel bitmap per matrix, cnt (entries left in the heap), TopLEK draw request.
+// vals: [n_mat][U] packed upper values (signed); F: [n_mat] squared Frobenius norms.  Output:
+// sel bitmap per matrix, cnt (entries kept before the rounding draw), TopLEK draw request.
 __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict__ vals, int U, int k, int lek,
                                                         double delta, const double* __restrict__ F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
                                                         double* pdraw, int* minidx)
 {
-    extern __shared__ double s_key[];
-    __shared__ int s_size;
-    int c = blockIdx.x;
+    extern __shared__ unsigned long long s_dyn[];
+    __shared__ int s_keep;
+    const int c = blockIdx.x;
     const double* v = vals + (size_t)c * U;
     unsigned* sc = sel + (size_t)c * SW;
-    for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int w = tid; w < SW; w += blockDim.x) sc[w] = 0u;
     if (k >= U) {       // SpecialMathRoutinesForMatrix.h:279-280 / :395-396: every upper index
         __syncthreads();
-        for (int w = threadIdx.x; w < SW; w += blockDim.x) {
+        for (int w = tid; w < SW; w += blockDim.x) {
             int lo = w * 32, n = min(32, U - lo);
             sc[w] = (n == 32) ? 0xffffffffu : ((1u << n) - 1u);
         }
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             cnt[c] = U;
             if (needs) needs[c] = 0;
         }
         return;
     }
     HeapS h;
-    h.key = s_key;
-    h.hid = (unsigned*)(s_key + k);
-    for (int t = threadIdx.x; t < k; t += blockDim.x) {
-        h.key[t] = fabs(v[t]);
+    h.key = s_dyn;
+    double* chain = (double*)(s_dyn + k);                        // [k] numerator after each extraction
+    unsigned long long* stage = (unsigned long long*)(chain + k); // [2][kSelStage]
+    h.hid = (unsigned*)(stage + 2 * kSelStage);
+    for (int t = tid; t < k; t += blockDim.x) {
+        h.key[t] = abs_bits(v[t]);
         h.hid[t] = (unsigned)t | (upper_is_diag(t) ? kDiagBit : 0u);
     }
     __syncthreads();
-    int size = k;
-    int lane = threadIdx.x & 31;
-    if (threadIdx.x < 32) {
-        if (lane == 0) {   // buildMinHeap, MinHeap.h:147-191
-            int i = (k + 4 - 2) / 4;
-            for (;;) {
-                heap_sift(h, i, k);
-                if (i == 0) break;
-                --i;
-            }
+    const int n_scan = U - k;
+    const int n_chunks = (n_scan + kSelStage - 1) / kSelStage;
+    // helpers stage chunk 0 while lane 0 of warp 0 builds the heap (buildMinHeap, MinHeap.h:147-191)
+    if (warp != 0) {
+        for (int t = tid - 32; t < min(kSelStage, n_scan); t += blockDim.x - 32) stage[t] = abs_bits(v[k + t]);
+    } else if (lane == 0) {
+        int i = (k + 4 - 2) / 4;
+        for (;;) {
+            heap_sift(h, i, k);
+            if (i == 0) break;
+            --i;
         }
-        __syncwarp();
-        double root = *(volatile double*)&h.key[0];
-        // scan, SpecialMathRoutinesForMatrix.h:300-318
-        double nxt = (k + lane < U) ? fabs(v[k + lane]) : -1.0;
-        for (int base = k; base < U; base += 32) {
-            double vv = nxt;
-            int tn = base + 32 + lane;
-            nxt = (tn < U) ? fabs(v[tn]) : -1.0;
-            unsigned mask = __ballot_sync(0xffffffffu, vv > root);
-            while (mask) {
-                int l = __ffs(mask) - 1;
-                double cand = __shfl_sync(0xffffffffu, vv, l);
-                if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
-                    int p = base + l;
-                    h.key[0] = cand;
-                    h.hid[0] = (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u);
-                    heap_sift(h, 0, k);
-                }
-                __syncwarp();
-                root = *(volatile double*)&h.key[0];
-                // the root of this heap can also decrease (a deeper element may move up), so the
-                // remaining lanes are tested again against the new root, not filtered by the old one
-                mask = __ballot_sync(0xffffffffu, vv > root) & ~((2u << l) - 1u);
-            }
-        }
-        if (lek && lane == 0) {
-            // getTopLEKFromUpperDiagonalPart, SpecialMathRoutinesForMatrix.h:385-503
-            double fr = F[c];
-            double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
-            double eps = __dmul_rn(1e-1, fr);
-            double num = fr;
-            for (int t = 0; t < k; ++t) {
-                double kk = h.key[t];
-                double term = __dmul_rn(kk, kk);
-                if (!(h.hid[t] & kDiagBit)) term = __dmul_rn(term, 2.0);
-                num = __dsub_rn(num, term);
-            }
-            int need = 0;
-            double pd = 0.0;
-            int mi = 0;
-            do {
-                double prev = num;
-                double mk = h.key[0];
-                unsigned mh = h.hid[0];
-                heap_swap(h, 0, size - 1);          // extracFromMinHeap, MinHeap.h:125-141
-                heap_sift(h, 0, size - 1);
-                size -= 1;
-                double term = __dmul_rn(mk, mk);
-                if (!(mh & kDiagBit)) term = __dmul_rn(term, 2.0);
-                num = __dadd_rn(num, term);
-                double next = num;
-                if (__dadd_rn(omd, eps) > prev && omd < __dadd_rn(next, eps)) {
-                    pd = __dadd_rn(__dsub_rn(omd, prev), eps) / __dadd_rn(__dsub_rn(next, prev), eps);
-                    need = 1;
-                    mi = (int)(mh & ~kDiagBit);
-                    break;
-                }
-            } while (size != 0);
-            needs[c] = need;
-            pdraw[c] = pd;
-            minidx[c] = mi;
-        }
-        if (lane == 0) s_size = size;
     }
     __syncthreads();
-    size = s_size;
-    for (int t = threadIdx.x; t < size; t += blockDim.x) {
-        unsigned p = h.hid[t] & ~kDiagBit;
+    unsigned long long root = h.key[0];
+    for (int q = 0; q < n_chunks; ++q) {
+        const int base = k + q * kSelStage;
+        const int len = min(kSelStage, U - base);
+        const unsigned long long* buf = stage + (q & 1) * kSelStage;
+        if (warp != 0) {
+            if (q + 1 < n_chunks) {
+                unsigned long long* nb = stage + ((q + 1) & 1) * kSelStage;
+                const int nbase = base + kSelStage, nlen = min(kSelStage, U - nbase);
+                for (int t = tid - 32; t < nlen; t += blockDim.x - 32) nb[t] = abs_bits(v[nbase + t]);
+            }
+        } else {
+            // scan, SpecialMathRoutinesForMatrix.h:300-318
+            for (int o = 0; o < len; o += 32) {
+                const unsigned long long vv = (o + lane < len) ? buf[o + lane] : 0ull;
+                unsigned mask = __ballot_sync(0xffffffffu, (o + lane < len) && vv > root);
+                while (mask) {
+                    const int l = __ffs(mask) - 1;
+                    const unsigned long long cand = __shfl_sync(0xffffffffu, vv, l);
+                    if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
+                        const int p = base + o + l;
+                        h.key[0] = cand;
+                        h.hid[0] = (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u);
+                        heap_sift(h, 0, k);
+                    }
+                    __syncwarp();
+                    root = *(volatile unsigned long long*)&h.key[0];
+                    // the root of this heap can also decrease (a deeper element may move up), so the
+                    // remaining lanes are tested again against the new root, not filtered by the old one
+                    mask = __ballot_sync(0xffffffffu, (o + lane < len) && vv > root) & ~((2u << l) - 1u);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    int keep = k;
+    if (lek) {
+        if (warp == 0 && lane == 0) {
+            // numerator = ||M||^2 - terms in heap-array order (:435-451)
+            const double fr = F[c];
+            double num = fr;
+            for (int t = 0; t < k; ++t) num = __dsub_rn(num, term_of(h.key[t], h.hid[t]));
+            chain[0] = num;   // temporarily: numerator before the first extraction
+            // extraction to the end (extracFromMinHeap, MinHeap.h:125-141); element m lands at k-1-m
+            for (int size = k; size > 1; --size) {
+                heap_swap(h, 0, size - 1);
+                heap_sift(h, 0, size - 1);
+            }
+            // numerator after each extraction, extraction order
+            double run = num;
+            for (int m = 0; m < k; ++m) {
+                run = __dadd_rn(run, term_of(h.key[k - 1 - m], h.hid[k - 1 - m]));
+                chain[m] = run;
+            }
+            *(double*)&stage[0] = num;    // numerator before the first extraction
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // first extraction m whose window condition holds (:475-476)
+            const double fr = F[c];
+            const double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
+            const double eps = __dmul_rn(1e-1, fr);
+            const double hi = __dadd_rn(omd, eps);
+            const double num0 = *(double*)&stage[0];
+            int first = k;
+            for (int m0 = 0; m0 < k; m0 += 32) {       // warp-uniform bounds
+                const int m = m0 + lane;
+                bool hit = false;
+                if (m < k) {
+                    const double prev = (m == 0) ? num0 : chain[m - 1];
+                    hit = hi > prev && omd < __dadd_rn(chain[m], eps);
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, hit);
+                if (b) {
+                    first = m0 + __ffs(b) - 1;
+                    break;
+                }
+            }
+            if (lane == 0) {
+                if (first < k) {
+                    const double prev = (first == 0) ? num0 : chain[first - 1];
+                    const double next = chain[first];
+                    pdraw[c] = __dadd_rn(__dsub_rn(omd, prev), eps) / __dadd_rn(__dsub_rn(next, prev), eps);
+                    needs[c] = 1;
+                    minidx[c] = (int)(h.hid[k - 1 - first] & ~kDiagBit);
+                    s_keep = k - 1 - first;      // positions [0, k-1-first) stay in the heap
+                } else {
+                    needs[c] = 0;
+                    pdraw[c] = 0.0;
+                    minidx[c] = 0;
+                    s_keep = 0;
+                }
+            }
+        }
+        __syncthreads();
+        keep = s_keep;
+    }
+    for (int t = tid; t < keep; t += blockDim.x) {
+        const unsigned p = h.hid[t] & ~kDiagBit;
         atomicOr(&sc[p >> 5], 1u << (p & 31));
     }
-    if (threadIdx.x == 0) cnt[c] = size;
+    if (tid == 0) cnt[c] = keep;
 }
 
 // TopLEK rounding draws: each reference worker w owns one thread_local RandomGenRealLinear
@@ -707,48 +795,63 @@ __global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq,
 // clients in order, so H receives exactly the reference's sequence of additions.
 __global__ void k_apply(Dev P)
 {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.U) return;
     double h = P.H[p];
-    bool all = (P.comp == 0 || P.comp == 5);
-    for (int c = 0; c < P.nc; ++c) {
-        if (!all && !((P.sel[(size_t)c * P.SW + (p >> 5)] >> (p & 31)) & 1u)) continue;
-        size_t q = (size_t)c * P.U + p;
-        double dv = P.diff[q];
-        double item, sent;
-        if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
-            item = natural_trunc(dv);
-            sent = __dmul_rn(P.prescale, item);
-        } else {
-            item = (P.comp == 1 || P.comp == 3) ? __dmul_rn(dv, P.mult) : dv;
-            sent = __dmul_rn(item, P.prescale);
+    const bool all = (P.comp == 0 || P.comp == 5);
+    const unsigned bit = 1u << (p & 31);
+    for (int c0 = 0; c0 < P.nc; c0 += 16) {
+        unsigned wd[16];
+#pragma unroll
+        for (int t = 0; t < 16; ++t)
+            wd[t] = (c0 + t < P.nc) ? (all ? bit : P.sel[(size_t)(c0 + t) * P.SW + (p >> 5)]) : 0u;
+        for (int t = 0; t < 16; ++t) {
+            if (!(wd[t] & bit)) continue;
+            const size_t q = (size_t)(c0 + t) * P.U + p;
+            const double dv = P.diff[q];
+            double item, sent;
+            if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
+                item = natural_trunc(dv);
+                sent = __dmul_rn(P.prescale, item);
+            } else {
+                item = (P.comp == 1 || P.comp == 3) ? __dmul_rn(dv, P.mult) : dv;
+                sent = __dmul_rn(item, P.prescale);
+            }
+            P.shift[q] = __dadd_rn(P.shift[q], __dmul_rn(P.alpha, item));
+            h = __dadd_rn(h, sent);
         }
-        P.shift[q] = __dadd_rn(P.shift[q], __dmul_rn(P.alpha, item));
-        h = __dadd_rn(h, sent);
     }
     P.H[p] = h;
 }
 
 // ---- 7. master: g = (1/n) sum_c g_c, l = (1/n) sum_c Lk_c (TrainLoop.h:1100-1333) ------------
-constexpr int kAggThreads = 256;
+// One thread per coordinate (32-thread blocks spread over SMs); clients added in order, loads
+// issued in batches ahead of the dependent additions.  Block 0's first warp forms l.
+constexpr int kAggThreads = 32;
 __global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
 {
-    __shared__ double red[kAggThreads / 32];
-    double ss = 0.0;
-    for (int j = threadIdx.x; j < P.d; j += blockDim.x) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < P.d) {
         double g = 0.0;
-        for (int c = 0; c < P.nc; ++c) g = __dadd_rn(g, P.gc[(size_t)c * P.d + j]);
-        g = __dmul_rn(g, P.inv_n);
-        P.g[j] = g;
-        ss += g * g;
+        for (int c0 = 0; c0 < P.nc; c0 += 8) {
+            double v[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) v[t] = (c0 + t < P.nc) ? P.gc[(size_t)(c0 + t) * P.d + j] : 0.0;
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (c0 + t < P.nc) g = __dadd_rn(g, v[t]);
+        }
+        P.g[j] = __dmul_rn(g, P.inv_n);
     }
-    double tot = block_sum<kAggThreads>(ss, red);
-    if (threadIdx.x == 0) {
+    if (blockIdx.x == 0) {
+        const int lane = threadIdx.x & 31;
         double l = 0.0;
-        for (int c = 0; c < P.nc; ++c) l = __dadd_rn(l, P.lk[c]);
-        l = __dmul_rn(l, P.inv_n);
-        P.stats[0] = sqrt(tot);
-        P.stats[1] = l;
+        for (int c0 = 0; c0 < P.nc; c0 += 32) {
+            const double v = (c0 + lane < P.nc) ? P.lk[c0 + lane] : 0.0;
+            const int cnt = min(32, P.nc - c0);
+            for (int t = 0; t < cnt; ++t) l = __dadd_rn(l, __shfl_sync(0xffffffffu, v, t));
+        }
+        if (lane == 0) P.stats[1] = __dmul_rn(l, P.inv_n);
     }
 }
 
@@ -838,6 +941,233 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_solve(Dev P, const double
         int r = *P.round_ctr;
         if (r < P.hist_cap) P.hist[r] = P.stats[0];
         *P.round_ctr = r + 1;
+    }
+}
+
+// ---- 8b. Option-B solve across the whole GPU -------------------------------------------------
+// Blocked right-looking Cholesky in one cooperative launch.  For each panel of kCholNB rows:
+//   1. every CTA factors the kCholNB x kCholNB diagonal block redundantly in shared memory (no
+//      barrier needed; CTA 0 writes it back);
+//   2. the warps of all CTAs finish the panel's rows of R column by column (one column per warp:
+//      lane t holds a_{c0+t,j}; r_kj = a_kj (1 / r_kk), then a_ij = fma(-r_ki, r_kj, a_ij));
+//   3. grid barrier, then all threads apply the panel to the trailing triangle entry by entry
+//      (a_ij = fma(-r_ki, r_kj, a_ij), k over the panel in order); grid barrier.
+// Every entry undergoes exactly the operation sequence of the unblocked right-looking algorithm,
+// so the factor equals the single-CTA (and CPU oracle) factor bit for bit.  The triangular
+// solves run in CTA 0, blocked by 32 rows with the same per-element operation order.
+constexpr int kCholNB = 32;
+constexpr int kCoopThreads = 256;
+constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIMEOUT
+
+// bounded grid barrier; returns false (error flag set) if the other CTAs did not arrive in time
+__device__ bool grid_barrier(unsigned* bar, unsigned nblk)
+{
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        volatile unsigned* verr = bar + 2;
+        unsigned gen = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(bar, 1u) + 1u;
+        int ok = 1;
+        if (arrived == nblk) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long t0 = clock64();
+            while (*vgen == gen) {
+                if (*verr) { ok = 0; break; }
+                if (clock64() - t0 > kBarrierCycles) {
+                    atomicExch(bar + 2, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (*verr) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin,
+                                                            const double* lptr, double lval,
+                                                            const double* __restrict__ gin, double* dxout,
+                                                            double* xupd, int record)
+{
+    __shared__ double Db[kCholNB][kCholNB + 1];
+    __shared__ double s_inv[kCholNB];
+    __shared__ int s_fail;
+    const double l = lptr ? *lptr : lval;
+    const int d = P.d, U = P.U;
+    double* A = P.work;
+    const unsigned G = gridDim.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int gtid = blockIdx.x * blockDim.x + tid, gthreads = G * blockDim.x;
+    for (int p = gtid; p < U; p += gthreads) {
+        int i, j;
+        upper_ij(p, i, j);
+        A[p] = (i == j) ? __dadd_rn(Hin[p], l) : Hin[p];
+    }
+    if (!grid_barrier(P.bar, G)) goto timeout;
+    for (int c0 = 0; c0 < d; c0 += kCholNB) {
+        const int nb = min(kCholNB, d - c0), c1 = c0 + nb;
+        for (int t = tid; t < nb * nb; t += blockDim.x) {
+            int i = t % nb, j = t / nb;
+            if (i <= j) Db[i][j] = A[up_pos(c0 + i, c0 + j)];
+        }
+        if (tid == 0) s_fail = 0;
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
+            if (tid == 0) {
+                double a = Db[k][k];
+                if (a < 0) {
+                    if (a > -0.0) a = 0.0;
+                    else s_fail = 1;
+                }
+                double r = sqrt(a);
+                Db[k][k] = r;
+                s_inv[k] = 1.0 / r;
+            }
+            __syncthreads();
+            if (s_fail) break;
+            const double inv = s_inv[k];
+            for (int j = k + 1 + tid; j < nb; j += blockDim.x) Db[k][j] = __dmul_rn(Db[k][j], inv);
+            __syncthreads();
+            const int m = nb - k - 1;
+            for (int t = tid; t < m * m; t += blockDim.x) {
+                int ii = k + 1 + t % m, jj = k + 1 + t / m;
+                if (ii <= jj) Db[ii][jj] = fma(-Db[k][ii], Db[k][jj], Db[ii][jj]);
+            }
+            __syncthreads();
+        }
+        if (s_fail) {   // identical decision in every CTA: all leave together
+            if (blockIdx.x == 0 && tid == 0) {
+                *P.status = -4;
+                if (record) *P.round_ctr += 1;
+            }
+            return;
+        }
+        if (blockIdx.x == 0)
+            for (int t = tid; t < nb * nb; t += blockDim.x) {
+                int i = t % nb, j = t / nb;
+                if (i <= j) A[up_pos(c0 + i, c0 + j)] = Db[i][j];
+            }
+        // panel rows of R for the columns right of the diagonal block
+        const int gw = gtid >> 5, nwarps = gthreads >> 5;
+        for (int j = c1 + gw; j < d; j += nwarps) {
+            double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
+            for (int k = 0; k < nb; ++k) {
+                if (lane == k) a = __dmul_rn(a, s_inv[k]);
+                double r = __shfl_sync(0xffffffffu, a, k);
+                if (lane > k && lane < nb) a = fma(-Db[k][lane], r, a);
+            }
+            if (lane < nb) A[up_pos(c0 + lane, j)] = a;
+        }
+        if (c1 >= d) break;
+        if (!grid_barrier(P.bar, G)) goto timeout;
+        // trailing update, entries (i, j) with c1 <= i <= j < d
+        {
+            const int m = d - c1;
+            const int T = m * (m + 1) / 2;
+            for (int e = gtid; e < T; e += gthreads) {
+                int ii, jj;
+                upper_ij(e, ii, jj);
+                const int i = c1 + ii, j = c1 + jj;
+                const double* ci = A + up_pos(0, i);
+                const double* cj = A + up_pos(0, j);
+                double a = cj[i];
+                for (int k = c0; k < c1; ++k) a = fma(-ci[k], cj[k], a);
+                A[up_pos(i, j)] = a;
+            }
+        }
+        if (!grid_barrier(P.bar, G)) goto timeout;
+    }
+    if (!grid_barrier(P.bar, G)) goto timeout;
+    if (blockIdx.x != 0) return;
+    {
+        // R^T y = g then R dx = y, blocked by 32 rows (CTA 0)
+        double* y = P.ybuf;
+        double gs = 0.0;
+        for (int i = tid; i < d; i += blockDim.x) {
+            y[i] = gin[i];
+            gs += gin[i] * gin[i];
+        }
+        if (record) {   // ||g|| for the round statistics
+            for (int o = 16; o > 0; o >>= 1) gs += __shfl_down_sync(0xffffffffu, gs, o);
+            __shared__ double s_gs[kCoopThreads / 32];
+            if (lane == 0) s_gs[tid >> 5] = gs;
+            __syncthreads();
+            if (tid == 0) {
+                double t = 0.0;
+                for (int w = 0; w < kCoopThreads / 32; ++w) t += s_gs[w];
+                P.stats[0] = sqrt(t);
+            }
+        }
+        __syncthreads();
+        for (int b0 = 0; b0 < d; b0 += 32) {
+            const int b1 = min(d, b0 + 32);
+            if (tid < 32) {
+                double v = (b0 + lane < b1) ? y[b0 + lane] : 0.0;
+                for (int s = 0; s < b1 - b0; ++s) {
+                    const int t = b0 + s;
+                    if (lane == s) v = __ddiv_rn(v, A[up_pos(t, t)]);
+                    double yt = __shfl_sync(0xffffffffu, v, s);
+                    if (lane > s && b0 + lane < b1) v = fma(-A[up_pos(t, b0 + lane)], yt, v);
+                }
+                if (b0 + lane < b1) y[b0 + lane] = v;
+            }
+            __syncthreads();
+            for (int i = b1 + tid; i < d; i += blockDim.x) {
+                double v = y[i];
+                const double* ci = A + up_pos(0, i);
+                for (int t = b0; t < b1; ++t) v = fma(-ci[t], y[t], v);
+                y[i] = v;
+            }
+            __syncthreads();
+        }
+        for (int b1 = d; b1 > 0; b1 -= 32) {
+            const int b0 = max(0, b1 - 32);
+            if (tid < 32) {
+                const int nbk = b1 - b0;
+                double v = (lane < nbk) ? y[b0 + lane] : 0.0;
+                for (int s = nbk - 1; s >= 0; --s) {
+                    const int t = b0 + s;
+                    if (lane == s) v = __ddiv_rn(v, A[up_pos(t, t)]);
+                    double yt = __shfl_sync(0xffffffffu, v, s);
+                    if (lane < s) v = fma(-A[up_pos(b0 + lane, t)], yt, v);
+                }
+                if (lane < nbk) y[b0 + lane] = v;
+            }
+            __syncthreads();
+            for (int i = tid; i < b0; i += blockDim.x) {
+                double v = y[i];
+                for (int t = b1 - 1; t >= b0; --t) v = fma(-A[up_pos(i, t)], y[t], v);
+                y[i] = v;
+            }
+            __syncthreads();
+        }
+        for (int i = tid; i < d; i += blockDim.x) {
+            const double dxi = y[i];
+            if (dxout) dxout[i] = dxi;
+            if (xupd) xupd[i] = __dsub_rn(xupd[i], dxi);
+        }
+        if (record && tid == 0) {
+            int r = *P.round_ctr;
+            if (r < P.hist_cap) P.hist[r] = P.stats[0];
+            *P.round_ctr = r + 1;
+        }
+    }
+    return;
+timeout:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *P.status = -5;
+        if (record) *P.round_ctr += 1;
     }
 }
 
