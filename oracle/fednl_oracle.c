@@ -189,6 +189,8 @@ static void heap_insert(orc_heap* h, uint32_t v)
     }
 }
 
+static double chunked_sum(const double* t, size_t n);
+
 /* Heap phase shared by TopK and TopLEK: SpecialMathRoutinesForMatrix.h:291-318 (TopK) and
  * :406-433 (TopLEK).  Seeds the heap with the first k upper indices, then replaces the root
  * by every later entry whose magnitude is strictly larger. */
@@ -242,39 +244,72 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
     h.m = m;
     topk_heap_scan(&h, k, U, upper);
 
-    /* numerator = ||M||^2 - sum over the heap array (:435-451) */
-    double numerator = frob_sq;
-    for (size_t i = 0; i < h.size; ++i) {
+    /* Numerator of the rounding window (:435-503).  The reference subtracts the heap's terms from
+     * ||M||^2 one by one in heap-array order and then adds back the extracted terms one by one in
+     * extraction order.  Restated with a fixed order the GB300 kernel also uses: the heap's terms
+     * (c v^2, c = 1 on the diagonal, 2 off it) are summed by chunked_sum in heap-array order and
+     * subtracted once; the prefix sums of the extracted terms are formed per chunk of 32 by the
+     * inclusive doubling scan s_l += s_{l-h} (h = 1, 2, 4, 8, 16) and carried from chunk to chunk
+     * in order.  The values differ from the reference's by a few ulps, which matters only if the
+     * window boundary falls within those ulps.  The heap is extracted to the end; the extracted
+     * element lands at the array's end (MinHeap.h:133-140), so the remaining heap after m
+     * extractions is the array prefix of length k - m. */
+    size_t K = (size_t)k;
+    double* terms = (double*)malloc(K * sizeof(double));
+    for (size_t i = 0; i < K; ++i) {
         uint32_t index = h.data[i];
         double item = m[index];
         uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
-        if (ir == jc)
-            numerator -= item * item;
-        else
-            numerator -= 2.0 * item * item;
+        terms[i] = (ir == jc) ? item * item : (item * item) * 2.0;
     }
-
-    /* extraction with randomized rounding (:453-503) */
-    do {
-        double prev = numerator;
-        uint32_t min_index = heap_extract(&h);
-        double item = m[min_index];
-        uint32_t jc = min_index / (uint32_t)lda, ir = min_index - jc * (uint32_t)lda;
-        if (ir == jc)
-            numerator += item * item;
-        else
-            numerator += 2.0 * item * item;
-        double next = numerator;
-        if (one_minus_delta_xf + eps > prev && one_minus_delta_xf < next + eps) {
-            double p = (one_minus_delta_xf - prev + eps) / (next - prev + eps);
+    double num0 = frob_sq - chunked_sum(terms, K);
+    for (size_t size = K; size > 1; --size) {         /* extracFromMinHeap to the end */
+        uint32_t t = h.data[0];
+        h.data[0] = h.data[size - 1];
+        h.data[size - 1] = t;
+        heap_sift(&h, 0, size - 1);
+    }
+    /* extracted term m is at position K - 1 - m */
+    double* next = (double*)malloc(K * sizeof(double));
+    double carry = num0;
+    for (size_t q = 0; q < K; q += 32) {
+        double v[32], w[32];
+        int n = (int)((K - q) < 32 ? (K - q) : 32);
+        for (int l = 0; l < 32; ++l) {
+            if (l < n) {
+                uint32_t index = h.data[K - 1 - (q + (size_t)l)];
+                double item = m[index];
+                uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
+                v[l] = (ir == jc) ? item * item : (item * item) * 2.0;
+            } else {
+                v[l] = 0.0;
+            }
+        }
+        for (int hh = 1; hh < 32; hh <<= 1) {
+            for (int l = 0; l < 32; ++l)
+                w[l] = (l >= hh) ? v[l] + v[l - hh] : v[l];
+            memcpy(v, w, sizeof(v));
+        }
+        for (int l = 0; l < n; ++l)
+            next[q + (size_t)l] = carry + v[l];
+        carry = carry + v[n - 1];
+    }
+    size_t keep = 0;
+    for (size_t mm = 0; mm < K; ++mm) {
+        double prev = (mm == 0) ? num0 : next[mm - 1];
+        double nx = next[mm];
+        if (one_minus_delta_xf + eps > prev && one_minus_delta_xf < nx + eps) {
+            double p = (one_minus_delta_xf - prev + eps) / (nx - prev + eps);
+            keep = K - 1 - mm;
             if (orc_lcg_real_unit(rng_state) > p)
-                heap_insert(&h, min_index);
+                keep += 1;        /* insertInMinHeap of the extracted element: it is at position K-1-mm */
             break;
         }
-    } while (h.size != 0);
-
-    qsort(out, h.size, sizeof(uint32_t), cmp_u32);
-    return (int32_t)h.size;
+    }
+    free(terms);
+    free(next);
+    qsort(out, keep, sizeof(uint32_t), cmp_u32);
+    return (int32_t)keep;
 }
 
 /* applyNaturalCompressorNaive: sign and exponent kept, mantissa zeroed, MatrixNMD.h:2013-2031 */
@@ -566,19 +601,20 @@ int orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr)
 
 /* forwardSubstitutionWithATranspose then backwardSubstitutionWithATranspose
  * dopt/dopt/linalg_linsolvers/include/ElementarySolvers.h:186-224 and :71-128: R^T y = b, R x = y.
- * Restated column-oriented: y_t /= r_tt, then y_i = fma(-r_ti, y_t, y_i) for the remaining i. */
+ * Restated column-oriented: y_t = y_t * (1 / r_tt) (the factorization's reciprocal; the reference
+ * divides), then y_i = fma(-r_ti, y_t, y_i) for the remaining i. */
 void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
 {
     for (int32_t i = 0; i < d; ++i)
         x[i] = b[i];
     for (int32_t t = 0; t < d; ++t) {
-        x[t] = x[t] / ltr[(size_t)t * lda + t];
+        x[t] = x[t] * (1.0 / ltr[(size_t)t * lda + t]);
         double yt = x[t];
         for (int32_t i = t + 1; i < d; ++i)
             x[i] = fma(-ltr[(size_t)i * lda + t], yt, x[i]);
     }
     for (int32_t t = d - 1; t >= 0; --t) {
-        x[t] = x[t] / ltr[(size_t)t * lda + t];
+        x[t] = x[t] * (1.0 / ltr[(size_t)t * lda + t]);
         double yt = x[t];
         for (int32_t i = 0; i < t; ++i)
             x[i] = fma(-ltr[(size_t)t * lda + i], yt, x[i]);

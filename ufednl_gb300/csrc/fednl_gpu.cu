@@ -125,7 +125,7 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
 struct fednl_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;
-    int d = 0, lda = 0, U = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
+    int d = 0, lda = 0, U = 0, ustr = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
     int binary = 0, maxn = 0, nfpart = 0, nseg = 0, hcap = 0;
     bool data_ready = false, shifts_ready = false;
     cudaStream_t stream = nullptr;
@@ -194,8 +194,9 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
         MARK("k_select");
         double delta = (double)h->k * (1.0 / (double)h->U);
-        k_select<<<h->nc, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(P.diff, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F,
-                                                                  P.sel, h->SW, P.cnt, P.needs, P.pdraw, P.minidx);
+        k_select<<<h->nc, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
+            P.diff, h->ustr, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F, P.sel, h->SW, P.cnt, P.needs, P.pdraw,
+            P.minidx, P.status);
         CKL();
         if (comp == FEDNL_TOPLEK) {
             MARK("k_toplek_rng");
@@ -276,6 +277,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     h->d = D.d;
     h->lda = lda;
     h->U = (int)U;
+    h->ustr = (int)((U + 31) / 32 * 32);
     h->nc = D.n_clients;
     h->k = k;
     h->comp = D.compressor;
@@ -306,6 +308,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.d = h->d;
     P.lda = h->lda;
     P.U = h->U;
+    P.ustr = h->ustr;
     P.nc = h->nc;
     P.k = h->k;
     P.comp = h->comp;
@@ -320,7 +323,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.prescale = P.inv_n * D.alpha;                          // TrainLoop.h:531
     P.mult = (double)h->U / (double)h->k;                    // RandK.h:90
     P.hist_cap = 1 << 16;
-    size_t ncU = (size_t)h->nc * h->U;
+    size_t ncU = (size_t)h->nc * h->ustr;
     Arena& A = h->state;
     A.want((int**)&P.ns, h->nc);
     A.want((int**)&P.soff, h->nc + 1);
@@ -349,6 +352,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.work, h->U);
     A.want(&P.dx, h->d);
     A.want(&P.ybuf, h->d);
+    A.want(&P.rinv, h->d);
     A.want(&P.hist, P.hist_cap);
     A.want(&P.round_ctr, 1);
     A.want(&P.status, 1);
@@ -629,7 +633,7 @@ int fednl_gpu_get_H(fednl_handle h, double* H)
 int fednl_gpu_get_shift(fednl_handle h, int32_t client, double* shift)
 {
     if (!h || !shift || client < 0 || client >= h->nc) return fail(FEDNL_EINVAL, "bad argument");
-    return packed_to_full(h, h->dev.shift + (size_t)client * h->U, shift);
+    return packed_to_full(h, h->dev.shift + (size_t)client * h->ustr, shift);
 }
 
 double fednl_gpu_get_l(fednl_handle h)
@@ -657,7 +661,7 @@ int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double*
     int U = h->U, lda = h->lda;
     std::vector<double> dv(U);
     std::vector<unsigned> sel(h->SW);
-    CK(cudaMemcpy(dv.data(), h->dev.diff + (size_t)client * U, (size_t)U * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dv.data(), h->dev.diff + (size_t)client * h->ustr, (size_t)U * 8, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(sel.data(), h->dev.sel + (size_t)client * h->SW, (size_t)h->SW * 4, cudaMemcpyDeviceToHost));
     std::vector<int> order;
     int comp = h->comp;
@@ -727,14 +731,15 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     long long U = (long long)d * (d + 1) / 2;
     if (k < U && k > kMaxK) return fail(FEDNL_EINVAL, "k above %d", kMaxK);
     int SW = (int)((U + 31) / 32);
+    const long long ustr = (U + 31) / 32 * 32;
     Scratch s;
     CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
     double *dfull, *dpack, *dF, *dp, *dcs;
     unsigned *dsel, *dws = nullptr;
-    int *dcnt, *dneeds, *dmi, *dwo = nullptr;
+    int *dcnt, *dneeds, *dmi, *dwo = nullptr, *derr;
     size_t full = (size_t)d * lda;
     s.a.want(&dfull, (size_t)n_mat * full);
-    s.a.want(&dpack, (size_t)n_mat * U);
+    s.a.want(&dpack, (size_t)n_mat * ustr);
     s.a.want(&dF, n_mat);
     s.a.want(&dp, n_mat);
     s.a.want(&dcs, (size_t)n_mat * ((full + 31) / 32));
@@ -742,6 +747,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     s.a.want(&dcnt, n_mat);
     s.a.want(&dneeds, n_mat);
     s.a.want(&dmi, n_mat);
+    s.a.want(&derr, 1);
     if (lek) {
         s.a.want(&dws, std::max(1, n_workers));
         s.a.want(&dwo, n_mat);
@@ -749,15 +755,17 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     rc = s.a.commit();
     if (rc) return rc;
     CK(cudaMemcpyAsync(dfull, mats, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
-    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), n_mat), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
+    CK(cudaMemsetAsync(derr, 0, 4, s.st));
+    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), n_mat), 256, 0, s.st>>>(dfull, d, lda, (int)U,
+                                                                                                     (int)ustr, dpack);
     CKL();
     k_l2sq_full<<<n_mat, 256, 0, s.st>>>(dfull, (long long)full, dcs, dF);
     CKL();
     if (select_smem(k) > 48 * 1024 && k < U)
         CK(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(k)));
     double delta = (double)k * (1.0 / (double)U);
-    k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)U, k, lek ? 1 : 0, delta, dF, dsel, SW,
-                                                                      dcnt, dneeds, dp, dmi);
+    k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)ustr, (int)U, k, lek ? 1 : 0, delta,
+                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr);
     CKL();
     if (lek) {
         int W = std::max(1, n_workers);
@@ -773,8 +781,11 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
         CK(cudaMemcpyAsync(wstates, dws, W * 4, cudaMemcpyDeviceToHost, s.st));
     }
     std::vector<unsigned> sel((size_t)n_mat * SW);
+    int errflag = 0;
     CK(cudaMemcpyAsync(sel.data(), dsel, sel.size() * 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(&errflag, derr, 4, cudaMemcpyDeviceToHost, s.st));
     CK(cudaStreamSynchronize(s.st));
+    if (errflag) return fail(FEDNL_ETIMEOUT, "bounded wait in the selection kernel ran out");
     for (int t = 0; t < n_mat; ++t) {
         int w = 0;
         long long p = 0;
@@ -940,6 +951,7 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     s.a.want(&P.work, U);
     s.a.want(&P.dx, d);
     s.a.want(&P.ybuf, d);
+    s.a.want(&P.rinv, d);
     s.a.want(&P.status, 1);
     s.a.want(&P.bar, 4);
     rc = s.a.commit();
@@ -950,7 +962,8 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     CK(cudaMemcpyAsync(dfull, H, (size_t)d * lda * 8, cudaMemcpyHostToDevice, s.st));
     CK(cudaMemcpyAsync(dg, g, d * 8, cudaMemcpyHostToDevice, s.st));
     CK(cudaMemsetAsync(P.status, 0, 4, s.st));
-    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U, dpack);
+    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U,
+                                                                                                (int)U, dpack);
     CKL();
     CK(launch_chol(P, chol_grid(d), s.st, dpack, nullptr, l, dg, P.dx, nullptr, 0));
     int status = 0;

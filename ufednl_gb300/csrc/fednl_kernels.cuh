@@ -27,6 +27,7 @@ constexpr unsigned kDiagBit = 0x80000000u;
 struct Dev {
     // sizes and scalars
     int d, lda, U, nc, k, comp, W, SW, nfpart, nseg;
+    int ustr;               // row stride of the per-client [U] arrays (U rounded up to 32)
     double lambda, alpha, prescale, inv_n, mult;
     // clients
     const int* ns;          // [nc]
@@ -43,8 +44,8 @@ struct Dev {
     double* x;              // [d]
     double* H;              // [U] master
     double* g;              // [d]
-    double* shift;          // [nc][U]
-    double* diff;           // [nc][U]
+    double* shift;          // [nc][ustr]
+    double* diff;           // [nc][ustr]
     double* Dv;             // [S] Hessian weights D_s
     double* qb;             // [S] gradient weights b_s * q_s
     double* gc;             // [nc][d]
@@ -66,6 +67,7 @@ struct Dev {
     double* work;           // [U] Cholesky factor
     double* dx;             // [d]
     double* ybuf;           // [d]
+    double* rinv;           // [d] 1 / r_kk of the last factorization
     double* hist;           // [max_rounds] ||g|| history
     int* round_ctr;         // [1]
     int* status;            // [1]
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
     for (int t = threadIdx.x; t < n; t += blockDim.x) s_D[t] = P.Dv[off + t];
     __syncthreads();
 
-    const size_t base = (size_t)c * P.U;
+    const size_t base = (size_t)c * P.ustr;
     const double* dsum = P.dsum + (size_t)c * P.d;
     const bool icpt = P.icpt[c] != 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
 {
     const int c = blockIdx.y;
     const int n = P.ns[c], off = P.soff[c];
-    const size_t base = (size_t)c * P.U;
+    const size_t base = (size_t)c * P.ustr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int seg = blockIdx.x * (kHessThreads / 32) + warp;
     const int p_seg = seg * 512;
@@ -449,7 +451,7 @@ __global__ void k_h_init(Dev P)
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.U) return;
     double h = 0.0;
-    for (int c = 0; c < P.nc; ++c) h = __dadd_rn(h, P.shift[(size_t)c * P.U + p]);
+    for (int c = 0; c < P.nc; ++c) h = __dadd_rn(h, P.shift[(size_t)c * P.ustr + p]);
     P.H[p] = __dmul_rn(h, P.inv_n);
 }
 
@@ -460,13 +462,17 @@ __global__ void k_h_init(Dev P)
 // level (MinHeap.h:259-286), so its "heap" is not a true heap and the selected set is not the
 // plain top-k by magnitude; every comparison, swap and tie is reproduced here step by step.
 //
-// Keys are the IEEE bit patterns of |v| compared as unsigned 64-bit integers: for non-negative
-// doubles this order is exactly the floating-point order (and avoids GB300's slow FP64 compare).
-// One warp per matrix does the sequential heap work in shared memory; the other warps stage the
-// scanned entries into a double buffer.  TopLEK's extraction loop runs to the end recording the
-// extraction order in place (extracFromMinHeap leaves the extracted element at the array's end,
-// MinHeap.h:133-140), its numerator is then one FP64 add chain in the reference's order (heap
-// array order, then extraction order), and the rounding window (:475-476) is found afterwards.
+// * Keys are the IEEE bit patterns of |v| compared as unsigned 64-bit integers: for non-negative
+//   doubles this order is exactly the floating-point order (GB300's FP64 compares are slow).
+// * buildMinHeap runs level by level in parallel: sifts of nodes on one level touch disjoint
+//   subtrees, so the result equals the reference's descending-index order.
+// * The scanned entries stream into shared memory by bulk asynchronous copies (cp.async.bulk with
+//   an mbarrier per buffer, double-buffered); one warp tests them 32 at a time with a ballot.
+// * TopLEK extracts to the end recording the order in place (extracFromMinHeap leaves the
+//   extracted element at the array's end, MinHeap.h:133-140); the top two heap levels live in
+//   registers during the extraction loop.  The window numerator uses the fixed parallel order of
+//   the CPU oracle (chunked tree for the heap's terms, chunked doubling scan plus in-order carries
+//   for the extracted terms).
 struct HeapS {
     unsigned long long* key;   // bits of |value|
     unsigned* hid;             // p | kDiagBit
@@ -487,10 +493,9 @@ __device__ __forceinline__ void heap_swap(HeapS& h, int a, int b)
     h.hid[b] = ti;
 }
 
-// minHeapify, MinHeap.h:255-290 (lowest value carried across levels as in the reference)
-__device__ void heap_sift(HeapS& h, int i, int heap_size)
+// minHeapify, MinHeap.h:255-290, entered at node i with the carried comparison value
+__device__ void heap_sift_from(HeapS& h, int i, int heap_size, unsigned long long lowest_value)
 {
-    unsigned long long lowest_value = h.key[i];
     for (;;) {
         int lowest = i;
         const int first = 4 * i + 1;
@@ -502,17 +507,17 @@ __device__ void heap_sift(HeapS& h, int i, int heap_size)
                 lowest_value = cv;
             }
         }
-        if (lowest != i) {
-            heap_swap(h, i, lowest);
-            i = lowest;
-        } else {
-            break;
-        }
+        if (lowest == i) break;
+        heap_swap(h, i, lowest);
+        i = lowest;
     }
 }
 
+__device__ __forceinline__ void heap_sift(HeapS& h, int i, int heap_size) { heap_sift_from(h, i, heap_size, h.key[i]); }
+
 constexpr int kSelThreads = 128;
-constexpr int kSelStage = 2048;            // staged entries per buffer (two buffers)
+constexpr int kSelStage = 2048;                    // doubles per staging buffer (16 KB)
+constexpr long long kSelWaitCycles = 2000000000ll; // bounded mbarrier wait (~1 s)
 
 __device__ __forceinline__ double term_of(unsigned long long key, unsigned id)
 {
@@ -521,25 +526,61 @@ __device__ __forceinline__ double term_of(unsigned long long key, unsigned id)
     return (id & kDiagBit) ? t : __dmul_rn(t, 2.0);
 }
 
-size_t __host__ __device__ inline select_smem_bytes(int k)
+__host__ __device__ inline size_t select_smem_bytes(int k)
 {
-    return (size_t)k * (sizeof(unsigned long long) + sizeof(unsigned)) + (size_t)k * sizeof(double) +
-           2 * kSelStage * sizeof(unsigned long long);
+    return 2 * (size_t)kSelStage * 8 + (size_t)k * 8 /*key*/ + (size_t)k * 8 /*terms*/ + (size_t)k * 4 /*hid*/ +
+           ((size_t)(k + 31) / 32) * 8 /*chunk sums*/ + 16;
 }
 
-// vals: [n_mat][U] packed upper values (signed); F: [n_mat] squared Frobenius norms.  Output:
-// sel bitmap per matrix, cnt (entries kept before the rounding draw), TopLEK draw request.
-__global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict__ vals, int U, int k, int lek,
-                                                        double delta, const double* __restrict__ F,
-                                                        unsigned* sel, int SW, int* cnt, int* needs,
-                                                        double* pdraw, int* minidx)
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar)
 {
-    extern __shared__ unsigned long long s_dyn[];
-    __shared__ int s_keep;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)));
+}
+
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// bounded wait for the given phase parity; false if it did not complete in time
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kSelWaitCycles) return false;
+    }
+}
+
+// vals: [n_mat][ustr] packed upper values (signed), rows 16-byte aligned (ustr even); F: [n_mat]
+// squared Frobenius norms.  Output: sel bitmap per matrix, cnt (entries kept before the rounding
+// draw), TopLEK draw request.  err: set to 1 if a bounded wait ran out.
+__global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict__ vals, int ustr, int U, int k,
+                                                        int lek, double delta, const double* __restrict__ F,
+                                                        unsigned* sel, int SW, int* cnt, int* needs,
+                                                        double* pdraw, int* minidx, int* err)
+{
+    extern __shared__ __align__(16) unsigned long long s_dyn[];
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ int s_keep, s_fail;
+    __shared__ double s_num0;
     const int c = blockIdx.x;
-    const double* v = vals + (size_t)c * U;
+    const double* v = vals + (size_t)c * ustr;
     unsigned* sc = sel + (size_t)c * SW;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
     for (int w = tid; w < SW; w += blockDim.x) sc[w] = 0u;
     if (k >= U) {       // SpecialMathRoutinesForMatrix.h:279-280 / :395-396: every upper index
         __syncthreads();
@@ -553,51 +594,69 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
         }
         return;
     }
+    double* stage = (double*)s_dyn;                                  // [2][kSelStage]
     HeapS h;
-    h.key = s_dyn;
-    double* chain = (double*)(s_dyn + k);                        // [k] numerator after each extraction
-    unsigned long long* stage = (unsigned long long*)(chain + k); // [2][kSelStage]
-    h.hid = (unsigned*)(stage + 2 * kSelStage);
+    h.key = s_dyn + 2 * kSelStage;                                   // [k]
+    double* terms = (double*)(h.key + k);                            // [k]
+    h.hid = (unsigned*)(terms + k);                                  // [k]
+    double* csum = (double*)(((size_t)(h.hid + k) + 7) & ~(size_t)7);  // [ceil(k/32)]
+
+    // scanned region [k, U) streamed in chunks starting at an even element (16-byte aligned)
+    const int s0 = k & ~1;
+    const int n_chunks = (U - s0 + kSelStage - 1) / kSelStage;
+    if (tid == 0) {
+        s_fail = 0;
+        mbar_init(&s_bar[0]);
+        mbar_init(&s_bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int q = 0; q < 2 && q < n_chunks; ++q) {
+            const int st = s0 + q * kSelStage;
+            const int len = min(kSelStage, ustr - st);
+            tma_load_1d(stage + q * kSelStage, v + st, (unsigned)len * 8u, &s_bar[q]);
+        }
+    }
     for (int t = tid; t < k; t += blockDim.x) {
         h.key[t] = abs_bits(v[t]);
         h.hid[t] = (unsigned)t | (upper_is_diag(t) ? kDiagBit : 0u);
     }
     __syncthreads();
-    const int n_scan = U - k;
-    const int n_chunks = (n_scan + kSelStage - 1) / kSelStage;
-    // helpers stage chunk 0 while lane 0 of warp 0 builds the heap (buildMinHeap, MinHeap.h:147-191)
-    if (warp != 0) {
-        for (int t = tid - 32; t < min(kSelStage, n_scan); t += blockDim.x - 32) stage[t] = abs_bits(v[k + t]);
-    } else if (lane == 0) {
-        int i = (k + 4 - 2) / 4;
-        for (;;) {
-            heap_sift(h, i, k);
-            if (i == 0) break;
-            --i;
+    // buildMinHeap (MinHeap.h:147-191) level by level, deepest first
+    {
+        const int start = (k + 4 - 2) / 4;
+        int lvl = 0, lo = 0;
+        while (lo + (1 << (2 * lvl)) <= start) {   // level of `start`
+            lo += 1 << (2 * lvl);
+            ++lvl;
+        }
+        for (; lvl >= 0; --lvl) {
+            const int first = ((1 << (2 * lvl)) - 1) / 3;
+            const int last = min(first + (1 << (2 * lvl)) - 1, start);
+            for (int i = first + tid; i <= last; i += blockDim.x) heap_sift(h, i, k);
+            __syncthreads();
         }
     }
-    __syncthreads();
-    unsigned long long root = h.key[0];
-    for (int q = 0; q < n_chunks; ++q) {
-        const int base = k + q * kSelStage;
-        const int len = min(kSelStage, U - base);
-        const unsigned long long* buf = stage + (q & 1) * kSelStage;
-        if (warp != 0) {
-            if (q + 1 < n_chunks) {
-                unsigned long long* nb = stage + ((q + 1) & 1) * kSelStage;
-                const int nbase = base + kSelStage, nlen = min(kSelStage, U - nbase);
-                for (int t = tid - 32; t < nlen; t += blockDim.x - 32) nb[t] = abs_bits(v[nbase + t]);
+    // scan, SpecialMathRoutinesForMatrix.h:300-318
+    if (warp == 0) {
+        unsigned long long root = h.key[0];
+        for (int q = 0; q < n_chunks; ++q) {
+            const int b = q & 1;
+            if (!mbar_wait(&s_bar[b], (unsigned)(q >> 1) & 1u)) {
+                if (lane == 0) s_fail = 1;
+                break;
             }
-        } else {
-            // scan, SpecialMathRoutinesForMatrix.h:300-318
+            const int st = s0 + q * kSelStage;
+            const int len = min(kSelStage, U - st);
+            const double* buf = stage + b * kSelStage;
             for (int o = 0; o < len; o += 32) {
-                const unsigned long long vv = (o + lane < len) ? buf[o + lane] : 0ull;
-                unsigned mask = __ballot_sync(0xffffffffu, (o + lane < len) && vv > root);
+                const int e = st + o + lane;
+                const bool ok = (o + lane < len) && e >= k;
+                const unsigned long long vv = ok ? abs_bits(buf[o + lane]) : 0ull;
+                unsigned mask = __ballot_sync(0xffffffffu, ok && vv > root);
                 while (mask) {
                     const int l = __ffs(mask) - 1;
                     const unsigned long long cand = __shfl_sync(0xffffffffu, vv, l);
                     if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
-                        const int p = base + o + l;
+                        const int p = st + o + l;
                         h.key[0] = cand;
                         h.hid[0] = (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u);
                         heap_sift(h, 0, k);
@@ -605,49 +664,142 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
                     __syncwarp();
                     root = *(volatile unsigned long long*)&h.key[0];
                     // the root of this heap can also decrease (a deeper element may move up), so the
-                    // remaining lanes are tested again against the new root, not filtered by the old one
-                    mask = __ballot_sync(0xffffffffu, (o + lane < len) && vv > root) & ~((2u << l) - 1u);
+                    // remaining lanes are tested again against the new root
+                    mask = __ballot_sync(0xffffffffu, ok && vv > root) & ~((2u << l) - 1u);
                 }
             }
+            __syncwarp();
+            if (lane == 0 && q + 2 < n_chunks) {       // refill this buffer with chunk q + 2
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const int nst = s0 + (q + 2) * kSelStage;
+                const int nlen = min(kSelStage, ustr - nst);
+                tma_load_1d(stage + b * kSelStage, v + nst, (unsigned)nlen * 8u, &s_bar[b]);
+            }
         }
-        __syncthreads();
+    }
+    __syncthreads();
+    if (s_fail) {   // a copy never completed: give the copies in flight a bounded chance, report
+        if (tid == 0) {
+            for (int q = 0; q < 2; ++q) mbar_wait(&s_bar[q], 0u);
+            *err = 1;
+            cnt[c] = 0;
+            if (needs) needs[c] = 0;
+        }
+        return;
     }
     int keep = k;
     if (lek) {
-        if (warp == 0 && lane == 0) {
-            // numerator = ||M||^2 - terms in heap-array order (:435-451)
-            const double fr = F[c];
-            double num = fr;
-            for (int t = 0; t < k; ++t) num = __dsub_rn(num, term_of(h.key[t], h.hid[t]));
-            chain[0] = num;   // temporarily: numerator before the first extraction
-            // extraction to the end (extracFromMinHeap, MinHeap.h:125-141); element m lands at k-1-m
-            for (int size = k; size > 1; --size) {
+        const int nch = (k + 31) / 32;
+        // heap terms in heap-array order, chunk trees, then the chunk sums in order
+        for (int t = tid; t < k; t += blockDim.x) terms[t] = term_of(h.key[t], h.hid[t]);
+        __syncthreads();
+        for (int q = warp; q < nch; q += nwarps) {
+            const int t = q * 32 + lane;
+            const double cs = chunk_tree(t < k ? terms[t] : 0.0);
+            if (lane == 0) csum[q] = cs;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double sh = 0.0;
+            for (int q = 0; q < nch; ++q) sh = __dadd_rn(sh, csum[q]);
+            s_num0 = __dsub_rn(F[c], sh);
+            // extraction to the end (extracFromMinHeap, MinHeap.h:125-141); element m lands at k-1-m.
+            // Positions 0..4 are kept in registers while the heap still has more than 21 entries.
+            unsigned long long K0 = h.key[0], K1 = h.key[1], K2 = h.key[2], K3 = h.key[3], K4 = h.key[4];
+            unsigned I0 = h.hid[0], I1 = h.hid[1], I2 = h.hid[2], I3 = h.hid[3], I4 = h.hid[4];
+            int size = k;
+            for (; size > 21; --size) {
+                const int n = size - 1;                    // heap size after the swap
+                const unsigned long long LK = h.key[n];
+                const unsigned LI = h.hid[n];
+                h.key[n] = K0;
+                h.hid[n] = I0;
+                // level 1: leftmost child strictly below the running lowest value
+                unsigned long long lv = LK;
+                int lo = 0;
+                if (lv > K1) { lo = 1; lv = K1; }
+                if (lv > K2) { lo = 2; lv = K2; }
+                if (lv > K3) { lo = 3; lv = K3; }
+                if (lv > K4) { lo = 4; lv = K4; }
+                if (lo == 0) {
+                    K0 = LK;
+                    I0 = LI;
+                    continue;
+                }
+                // root takes the child, the child's slot takes L (still in registers)
+                unsigned ci;
+                if (lo == 1) { K0 = K1; I0 = I1; K1 = LK; I1 = LI; }
+                else if (lo == 2) { K0 = K2; I0 = I2; K2 = LK; I2 = LI; }
+                else if (lo == 3) { K0 = K3; I0 = I3; K3 = LK; I3 = LI; }
+                else { K0 = K4; I0 = I4; K4 = LK; I4 = LI; }
+                (void)ci;
+                // level 2: children of `lo` against the value that moved up (lv)
+                const int f2 = 4 * lo + 1;
+                int g = -1;
+                unsigned long long lv2 = lv;
+                for (int t = 0; t < 4; ++t) {
+                    const unsigned long long cv = h.key[f2 + t];
+                    if (lv2 > cv) { g = t; lv2 = cv; }
+                }
+                if (g < 0) continue;
+                const int gp = f2 + g;
+                const unsigned long long GK = h.key[gp];
+                const unsigned GI = h.hid[gp];
+                h.key[gp] = LK;
+                h.hid[gp] = LI;
+                if (lo == 1) { K1 = GK; I1 = GI; }
+                else if (lo == 2) { K2 = GK; I2 = GI; }
+                else if (lo == 3) { K3 = GK; I3 = GI; }
+                else { K4 = GK; I4 = GI; }
+                heap_sift_from(h, gp, n, lv2);           // deeper levels, carried value as in the reference
+            }
+            h.key[0] = K0; h.key[1] = K1; h.key[2] = K2; h.key[3] = K3; h.key[4] = K4;
+            h.hid[0] = I0; h.hid[1] = I1; h.hid[2] = I2; h.hid[3] = I3; h.hid[4] = I4;
+            for (; size > 1; --size) {
                 heap_swap(h, 0, size - 1);
                 heap_sift(h, 0, size - 1);
             }
-            // numerator after each extraction, extraction order
-            double run = num;
-            for (int m = 0; m < k; ++m) {
-                run = __dadd_rn(run, term_of(h.key[k - 1 - m], h.hid[k - 1 - m]));
-                chain[m] = run;
-            }
-            *(double*)&stage[0] = num;    // numerator before the first extraction
         }
         __syncthreads();
+        // extracted terms (extraction order m = position k-1-m), chunk-local doubling scans
+        for (int q = warp; q < nch; q += nwarps) {
+            const int m = q * 32 + lane;
+            double x = (m < k) ? term_of(h.key[k - 1 - m], h.hid[k - 1 - m]) : 0.0;
+            for (int hh = 1; hh < 32; hh <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, x, hh);
+                if (lane >= hh) x = __dadd_rn(x, y);
+            }
+            if (m < k) terms[m] = x;
+            const int last = min(31, k - 1 - q * 32);
+            const double tot = __shfl_sync(0xffffffffu, x, last);
+            if (lane == 0) csum[q] = tot;
+        }
+        __syncthreads();
+        if (tid == 0) {          // carries in order: carry_q = num0 + totals of chunks < q
+            double carry = s_num0;
+            for (int q = 0; q < nch; ++q) {
+                const double t = csum[q];
+                csum[q] = carry;
+                carry = __dadd_rn(carry, t);
+            }
+        }
+        __syncthreads();
+        for (int m = tid; m < k; m += blockDim.x) terms[m] = __dadd_rn(csum[m >> 5], terms[m]);   // next_m
+        __syncthreads();
         if (warp == 0) {
-            // first extraction m whose window condition holds (:475-476)
+            // first extraction whose window condition holds (SpecialMathRoutinesForMatrix.h:475-476)
             const double fr = F[c];
             const double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
             const double eps = __dmul_rn(1e-1, fr);
             const double hi = __dadd_rn(omd, eps);
-            const double num0 = *(double*)&stage[0];
+            const double num0 = s_num0;
             int first = k;
             for (int m0 = 0; m0 < k; m0 += 32) {       // warp-uniform bounds
                 const int m = m0 + lane;
                 bool hit = false;
                 if (m < k) {
-                    const double prev = (m == 0) ? num0 : chain[m - 1];
-                    hit = hi > prev && omd < __dadd_rn(chain[m], eps);
+                    const double prev = (m == 0) ? num0 : terms[m - 1];
+                    hit = hi > prev && omd < __dadd_rn(terms[m], eps);
                 }
                 const unsigned b = __ballot_sync(0xffffffffu, hit);
                 if (b) {
@@ -657,8 +809,8 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
             }
             if (lane == 0) {
                 if (first < k) {
-                    const double prev = (first == 0) ? num0 : chain[first - 1];
-                    const double next = chain[first];
+                    const double prev = (first == 0) ? num0 : terms[first - 1];
+                    const double next = terms[first];
                     pdraw[c] = __dadd_rn(__dsub_rn(omd, prev), eps) / __dadd_rn(__dsub_rn(next, prev), eps);
                     needs[c] = 1;
                     minidx[c] = (int)(h.hid[k - 1 - first] & ~kDiagBit);
@@ -807,7 +959,7 @@ __global__ void k_apply(Dev P)
             wd[t] = (c0 + t < P.nc) ? (all ? bit : P.sel[(size_t)(c0 + t) * P.SW + (p >> 5)]) : 0u;
         for (int t = 0; t < 16; ++t) {
             if (!(wd[t] & bit)) continue;
-            const size_t q = (size_t)(c0 + t) * P.U + p;
+            const size_t q = (size_t)(c0 + t) * P.ustr + p;
             const double dv = P.diff[q];
             double item, sent;
             if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
@@ -859,90 +1011,8 @@ __global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
 // choleskyFactorization<.., true, true> (CholeskyFactorization.h:153-272) computes R = L^T with
 // H + l I = R^T R reading only the upper triangle; forwardSubstitutionWithATranspose and
 // backwardSubstitutionWithATranspose (ElementarySolvers.h:186-224, :71-128) solve R^T y = g and
-// R dx = y.  Here the factor is formed right-looking in one CTA on the packed upper triangle.
-constexpr int kCholThreads = 1024;
+// R dx = y.
 __device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j + 1) / 2 + i; }
-
-// l is read from lptr when given (the round's device-side l), else lval is used.
-__global__ void __launch_bounds__(kCholThreads) k_chol_solve(Dev P, const double* __restrict__ Hin,
-                                                             const double* lptr, double lval,
-                                                             const double* __restrict__ gin, double* dxout,
-                                                             double* xupd, int record)
-{
-    double l = lptr ? *lptr : lval;
-    __shared__ double s_r;
-    __shared__ int s_fail;
-    double* A = P.work;
-    int d = P.d, U = P.U;
-    for (int p = threadIdx.x; p < U; p += blockDim.x) {
-        int i, j;
-        upper_ij(p, i, j);
-        A[p] = (i == j) ? __dadd_rn(Hin[p], l) : Hin[p];
-    }
-    if (threadIdx.x == 0) s_fail = 0;
-    __syncthreads();
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int kk = 0; kk < d; ++kk) {
-        if (threadIdx.x == 0) {
-            double a = A[up_pos(kk, kk)];
-            if (a < 0) {
-                if (a > -0.0) a = 0.0;
-                else s_fail = 1;
-            }
-            double r = sqrt(a);
-            A[up_pos(kk, kk)] = r;
-            s_r = 1.0 / r;
-        }
-        __syncthreads();
-        if (s_fail) break;
-        double inv = s_r;
-        for (int j = kk + 1 + threadIdx.x; j < d; j += blockDim.x) A[up_pos(kk, j)] = __dmul_rn(A[up_pos(kk, j)], inv);
-        __syncthreads();
-        for (int j = kk + 1 + warp; j < d; j += nw) {
-            double rkj = A[up_pos(kk, j)];
-            double* col = A + up_pos(0, j);
-            for (int i = kk + 1 + lane; i <= j; i += 32) col[i] = fma(-A[up_pos(kk, i)], rkj, col[i]);
-        }
-        __syncthreads();
-    }
-    __syncthreads();
-    if (s_fail) {
-        if (threadIdx.x == 0) {
-            if (P.status) *P.status = -4;
-            if (record) *P.round_ctr += 1;
-        }
-        return;
-    }
-    // R^T y = g (column-oriented forward substitution)
-    double* y = P.ybuf;
-    for (int i = threadIdx.x; i < d; i += blockDim.x) y[i] = gin[i];
-    __syncthreads();
-    for (int t = 0; t < d; ++t) {
-        if (threadIdx.x == 0) y[t] = __ddiv_rn(y[t], A[up_pos(t, t)]);
-        __syncthreads();
-        double yt = y[t];
-        for (int i = t + 1 + threadIdx.x; i < d; i += blockDim.x) y[i] = fma(-A[up_pos(t, i)], yt, y[i]);
-        __syncthreads();
-    }
-    // R dx = y (column-oriented backward substitution)
-    for (int t = d - 1; t >= 0; --t) {
-        if (threadIdx.x == 0) y[t] = __ddiv_rn(y[t], A[up_pos(t, t)]);
-        __syncthreads();
-        double yt = y[t];
-        for (int i = threadIdx.x; i < t; i += blockDim.x) y[i] = fma(-A[up_pos(i, t)], yt, y[i]);
-        __syncthreads();
-    }
-    for (int i = threadIdx.x; i < d; i += blockDim.x) {
-        double dxi = y[i];
-        if (dxout) dxout[i] = dxi;
-        if (xupd) xupd[i] = __dsub_rn(xupd[i], dxi);    // x -= dx (TrainLoop.h:1504-1508)
-    }
-    if (record && threadIdx.x == 0) {
-        int r = *P.round_ctr;
-        if (r < P.hist_cap) P.hist[r] = P.stats[0];
-        *P.round_ctr = r + 1;
-    }
-}
 
 // ---- 8b. Option-B solve across the whole GPU -------------------------------------------------
 // Blocked right-looking Cholesky in one cooperative launch.  For each panel of kCholNB rows:
@@ -1053,11 +1123,13 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             }
             return;
         }
-        if (blockIdx.x == 0)
+        if (blockIdx.x == 0) {
             for (int t = tid; t < nb * nb; t += blockDim.x) {
                 int i = t % nb, j = t / nb;
                 if (i <= j) A[up_pos(c0 + i, c0 + j)] = Db[i][j];
             }
+            for (int t = tid; t < nb; t += blockDim.x) P.rinv[c0 + t] = s_inv[t];
+        }
         // panel rows of R for the columns right of the diagonal block
         const int gw = gtid >> 5, nwarps = gthreads >> 5;
         for (int j = c1 + gw; j < d; j += nwarps) {
@@ -1116,7 +1188,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                 double v = (b0 + lane < b1) ? y[b0 + lane] : 0.0;
                 for (int s = 0; s < b1 - b0; ++s) {
                     const int t = b0 + s;
-                    if (lane == s) v = __ddiv_rn(v, A[up_pos(t, t)]);
+                    if (lane == s) v = __dmul_rn(v, P.rinv[t]);
                     double yt = __shfl_sync(0xffffffffu, v, s);
                     if (lane > s && b0 + lane < b1) v = fma(-A[up_pos(t, b0 + lane)], yt, v);
                 }
@@ -1138,7 +1210,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                 double v = (lane < nbk) ? y[b0 + lane] : 0.0;
                 for (int s = nbk - 1; s >= 0; --s) {
                     const int t = b0 + s;
-                    if (lane == s) v = __ddiv_rn(v, A[up_pos(t, t)]);
+                    if (lane == s) v = __dmul_rn(v, P.rinv[t]);
                     double yt = __shfl_sync(0xffffffffu, v, s);
                     if (lane < s) v = fma(-A[up_pos(b0 + lane, t)], yt, v);
                 }
@@ -1173,13 +1245,17 @@ timeout:
 
 // ---- operator-level helpers -----------------------------------------------------------------
 // pack the upper triangle of n column-major d x lda matrices and their full squared norms
-__global__ void k_pack_upper(const double* full, int d, int lda, int U, double* packed)
+__global__ void k_pack_upper(const double* full, int d, int lda, int U, int ustr, double* packed)
 {
     int t = blockIdx.y;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < U; p += gridDim.x * blockDim.x) {
-        int i, j;
-        upper_ij(p, i, j);
-        packed[(size_t)t * U + p] = full[(size_t)t * d * lda + (size_t)j * lda + i];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ustr; p += gridDim.x * blockDim.x) {
+        double v = 0.0;
+        if (p < U) {
+            int i, j;
+            upper_ij(p, i, j);
+            v = full[(size_t)t * d * lda + (size_t)j * lda + i];
+        }
+        packed[(size_t)t * ustr + p] = v;
     }
 }
 
