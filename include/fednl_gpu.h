@@ -151,6 +151,20 @@ int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_
  * definite. */
 int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
 
+/* Allocation-free Option-B solve (no counterpart in the reference): the same factorisation and
+ * solves as fednl_gpu_optionb_solve for callers that cannot allocate device memory -- code running
+ * inside a stream capture whose memory pool forbids new allocations, latency-critical loops where a
+ * cudaMalloc would stall the device, or hosts whose framework owns all device memory through its
+ * own allocator.  H (column-major d x lda, upper triangle read), g and dx are DEVICE pointers the
+ * caller owns; the call runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it
+ * to read the status.  Scratch comes from one fixed device array of the library (about 1 MB, held
+ * by every device that loads the library until the process exits), so d is limited to 512 (larger
+ * d returns FEDNL_EINVAL).  The first call on a device looks up that array's address, so make it
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU (different
+ * streams or threads at the same time) race and must be serialised by the caller. */
+int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g,
+                                    double* dx, void* stream);
+
 /* ---- instrumentation ---------------------------------------------------------------------- */
 
 /* Device time of `rounds` rounds replayed as in fednl_gpu_run, each bracketed by CUDA events on

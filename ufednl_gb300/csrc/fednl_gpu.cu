@@ -104,8 +104,8 @@ int chol_grid(int d)
     return (int)std::max<long long>(1, g);
 }
 
-cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* Hin, const double* lptr, double lval,
-                        const double* gin, double* dxout, double* xupd, int record)
+cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* Hin, int hin_lda, const double* lptr,
+                        double lval, const double* gin, double* dxout, double* xupd, int record)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -117,7 +117,7 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, lptr, lval, gin, dxout, xupd, record);
+    return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record);
 }
 
 }  // namespace
@@ -220,7 +220,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads, kAggThreads, 0, st>>>(P);
     CKL();
     MARK("k_chol_coop");
-    CK(launch_chol(P, h->chol_grid, st, P.H, P.stats + 1, 0.0, P.g, P.dx, P.x, 1));
+    CK(launch_chol(P, h->chol_grid, st, P.H, 0, P.stats + 1, 0.0, P.g, P.dx, P.x, 1));
     MARK("end");
     return FEDNL_OK;
 }
@@ -965,7 +965,7 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U,
                                                                                                 (int)U, dpack);
     CKL();
-    CK(launch_chol(P, chol_grid(d), s.st, dpack, nullptr, l, dg, P.dx, nullptr, 0));
+    CK(launch_chol(P, chol_grid(d), s.st, dpack, 0, nullptr, l, dg, P.dx, nullptr, 0));
     int status = 0;
     CK(cudaMemcpyAsync(&status, P.status, 4, cudaMemcpyDeviceToHost, s.st));
     CK(cudaStreamSynchronize(s.st));
@@ -1073,6 +1073,63 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
     if (rc) return rc;
     if (e != cudaSuccess) return fail(FEDNL_ECUDA, "profiled rounds failed: %s", cudaGetErrorString(e));
     h->rounds_done += rounds;
+    return FEDNL_OK;
+}
+
+// ---- allocation-free Option-B solve -------------------------------------------------------------
+// For callers that may not allocate device memory: code running while a CUDA graph is being
+// captured into a pool that forbids new allocations, real-time loops where a cudaMalloc would stall
+// the device, or hosts whose framework owns every byte of device memory through its own allocator.
+// The solve's scratch (the packed factor, two d-vectors, the grid-barrier counters and the status
+// word) lives in one fixed device array, allocated when the library's module is loaded on a device
+// and held by that device until the process exits.  Only host code needs the array's device
+// address: cudaGetSymbolAddress resolves it once per device, with that device current, on the
+// first call made on it.
+namespace {
+constexpr int kNoAllocMaxD = 512;
+constexpr size_t kNoAllocMaxU = (size_t)kNoAllocMaxD * (kNoAllocMaxD + 1) / 2;
+constexpr size_t kNoAllocDoubles = kNoAllocMaxU + 2 * kNoAllocMaxD + 4;   // factor, y, 1/r, barrier+status
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+static double* g_noalloc_ptr[kNoAllocMaxDevices];
+static int g_noalloc_grid[kNoAllocMaxDevices];
+}  // namespace
+
+int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
+                                    void* stream)
+{
+    if (!H || !g || !dx || d < 1 || lda < d) return fail(FEDNL_EINVAL, "bad argument");
+    if (d > kNoAllocMaxD)
+        return fail(FEDNL_EINVAL, "d = %d exceeds the allocation-free solve's maximum of %d", d, kNoAllocMaxD);
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(FEDNL_EINVAL, "device ordinal %d out of range", dev);
+    if (!g_noalloc_ptr[dev]) {          // once per device, with that device current
+        void* ptr = nullptr;
+        CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        g_noalloc_grid[dev] = chol_grid(kNoAllocMaxD);
+        g_noalloc_ptr[dev] = (double*)ptr;
+    }
+    double* base = g_noalloc_ptr[dev];
+    const long long U = (long long)d * (d + 1) / 2;
+    Dev P{};
+    P.d = d;
+    P.U = (int)U;
+    P.work = base;
+    P.ybuf = base + kNoAllocMaxU;
+    P.rinv = base + kNoAllocMaxU + kNoAllocMaxD;
+    P.bar = (unsigned*)(base + kNoAllocMaxU + 2 * kNoAllocMaxD);       // 4 x u32 = 2 doubles
+    P.status = (int*)(base + kNoAllocMaxU + 2 * kNoAllocMaxD + 2);
+    cudaStream_t st = (cudaStream_t)stream;
+    // barrier counters and status must start at zero; the factor is overwritten by every call
+    CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(double), st));
+    int grid = std::min(g_noalloc_grid[dev], chol_grid(d));
+    CK(launch_chol(P, grid, st, H, lda, nullptr, l, g, dx, nullptr, 0));
+    int status = 0;
+    CK(cudaMemcpyAsync(&status, P.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (status == FEDNL_ETIMEOUT) return fail(FEDNL_ETIMEOUT, "grid barrier of the Cholesky timed out");
+    if (status) return fail(FEDNL_ENOTPD, "H + l I is not positive definite");
     return FEDNL_OK;
 }
 

@@ -1065,7 +1065,9 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblk)
     return s_ok != 0;
 }
 
-__global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin,
+// Hin is the packed upper triangle, or (hin_lda > 0) a column-major matrix with that leading
+// dimension of which the upper triangle is read.
+__global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin, int hin_lda,
                                                             const double* lptr, double lval,
                                                             const double* __restrict__ gin, double* dxout,
                                                             double* xupd, int record)
@@ -1082,7 +1084,8 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     for (int p = gtid; p < U; p += gthreads) {
         int i, j;
         upper_ij(p, i, j);
-        A[p] = (i == j) ? __dadd_rn(Hin[p], l) : Hin[p];
+        const double hv = hin_lda > 0 ? Hin[(size_t)j * hin_lda + i] : Hin[p];
+        A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
     }
     if (!grid_barrier(P.bar, G)) goto timeout;
     for (int c0 = 0; c0 < d; c0 += kCholNB) {

@@ -49,7 +49,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_get_H", "fednl_gpu_get_shift", "fednl_gpu_get_l", "fednl_gpu_get_lk",
            "fednl_gpu_get_message", "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
-           "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels", "fednl_gpu_last_error"]
+           "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
+           "fednl_gpu_last_error"]
 
 _lib = None
 
@@ -86,6 +87,7 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_natural": [dp, C.c_int64, dp, C.POINTER(C.c_uint8)],
         "fednl_gpu_logreg_oracle": [dp, dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, dp, dp, dp],
         "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
+        "fednl_gpu_optionb_solve_noalloc": [vp, C.c_int32, C.c_int32, C.c_double, vp, vp, vp],
         "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
         "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
     }
