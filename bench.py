@@ -135,8 +135,8 @@ def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
         return nc * U * 8.0, "read every client's difference once"
     if kernel == "k_apply":
         return nc * (U + 31) // 32 * 4.0 + 2 * U * 8.0, "selection bitmaps + H read/write"
-    if kernel == "k_chol_solve":
-        return U * 8.0 * 3, "H read, factor write/read (packed upper)"
+    if kernel == "k_chol_coop":
+        return U * 8.0 + 2 * d * 8.0, "H read (packed upper) + g read + step write; latency-bound FP64 chain"
     return 0.0, "n/a"
 
 
@@ -249,14 +249,27 @@ def run_ours(args, ws, rank, local, td):
     roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
             "traffic": traffic_from_profiles(dom), "algorithmic_bytes_per_launch": abytes,
             "algorithmic_bytes": what, "kernel_ms": dom_ms, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)"}
+    # round-level bound: the shift stream (every client's shift read and written once, packed
+    # upper FP64) at the measured HBM bandwidth, against the measured time per round
+    U = prob.d * (prob.d + 1) // 2
+    shift_bytes = 2.0 * prob.n_clients * U * 8
+    round_roof = {"bound": "hbm", "shift_stream_bytes": shift_bytes,
+                  "lower_bound_ms": shift_bytes / (hbm * 1e9) * 1e3, "round_ms": ms_per_step,
+                  "frac": shift_bytes / (hbm * 1e9) * 1e3 / ms_per_step}
     fed.close()
 
-    # time to ||g|| <= 1e-9: fresh run, rounds until the tolerance, at the measured ms/round
+    # time to ||g|| <= 1e-9: a fresh run finds the round count, a second fresh run times exactly
+    # those rounds on the device (early rounds cost more than converged ones: TopLEK extracts deeper)
     fed2 = fednl.FedNL(prob, comp, k, 1.0, workers=W)
     g = fed2.run(200)
     hit = np.nonzero(g <= TOL)[0]
     rounds_to_tol = int(hit[0]) + 1 if hit.size else None
     fed2.close()
+    tol_ms = None
+    if rounds_to_tol:
+        fed2 = fednl.FedNL(prob, comp, k, 1.0, workers=W)
+        tol_ms, _ = fed2.time_rounds(rounds_to_tol, L2_FLUSH_BYTES)
+        fed2.close()
 
     # end to end through the C ABI with host buffers: create + upload + init + K rounds (each
     # returning its statistics to the host) + final iterate readback
@@ -279,8 +292,9 @@ def run_ours(args, ws, rank, local, td):
             "config": config_dict(prob, comp, k, W),
             "round_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
             "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
-                            "seconds": rounds_to_tol * ms_per_step / 1000.0 if rounds_to_tol else None},
-            "roofline": roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
+                            "seconds": tol_ms / 1000.0 if tol_ms is not None else None,
+                            "timed": "device time of rounds 1..R from x0 = 0"},
+            "roofline": roof, "round_roofline": round_roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
             "clocks": clocks, "e2e": e2e}
     if ws == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -251,9 +251,12 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
      * subtracted once; the prefix sums of the extracted terms are formed per chunk of 32 by the
      * inclusive doubling scan s_l += s_{l-h} (h = 1, 2, 4, 8, 16) and carried from chunk to chunk
      * in order.  The values differ from the reference's by a few ulps, which matters only if the
-     * window boundary falls within those ulps.  The heap is extracted to the end; the extracted
-     * element lands at the array's end (MinHeap.h:133-140), so the remaining heap after m
-     * extractions is the array prefix of length k - m. */
+     * window boundary falls within those ulps.  Every numerator is num0 plus non-negative terms
+     * (monotone rounding), so when the window's upper bound does not exceed num0 no extraction
+     * opens it and none is made.  Otherwise the heap is extracted in chunks of 32; the extracted
+     * element lands at the array's end (MinHeap.h:133-140), so the elements not extracted by step
+     * m are the array prefix of length k - 1 - m whatever later extractions do, and extraction
+     * stops after the chunk that holds the first window hit. */
     size_t K = (size_t)k;
     double* terms = (double*)malloc(K * sizeof(double));
     for (size_t i = 0; i < K; ++i) {
@@ -263,51 +266,59 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
         terms[i] = (ir == jc) ? item * item : (item * item) * 2.0;
     }
     double num0 = frob_sq - chunked_sum(terms, K);
-    for (size_t size = K; size > 1; --size) {         /* extracFromMinHeap to the end */
-        uint32_t t = h.data[0];
-        h.data[0] = h.data[size - 1];
-        h.data[size - 1] = t;
-        heap_sift(&h, 0, size - 1);
-    }
-    /* extracted term m is at position K - 1 - m */
-    double* next = (double*)malloc(K * sizeof(double));
-    double carry = num0;
-    for (size_t q = 0; q < K; q += 32) {
-        double v[32], w[32];
-        int n = (int)((K - q) < 32 ? (K - q) : 32);
-        for (int l = 0; l < 32; ++l) {
-            if (l < n) {
-                uint32_t index = h.data[K - 1 - (q + (size_t)l)];
-                double item = m[index];
-                uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
-                v[l] = (ir == jc) ? item * item : (item * item) * 2.0;
-            } else {
-                v[l] = 0.0;
-            }
-        }
-        for (int hh = 1; hh < 32; hh <<= 1) {
-            for (int l = 0; l < 32; ++l)
-                w[l] = (l >= hh) ? v[l] + v[l - hh] : v[l];
-            memcpy(v, w, sizeof(v));
-        }
-        for (int l = 0; l < n; ++l)
-            next[q + (size_t)l] = carry + v[l];
-        carry = carry + v[n - 1];
-    }
+    double hi = one_minus_delta_xf + eps;
     size_t keep = 0;
-    for (size_t mm = 0; mm < K; ++mm) {
-        double prev = (mm == 0) ? num0 : next[mm - 1];
-        double nx = next[mm];
-        if (one_minus_delta_xf + eps > prev && one_minus_delta_xf < nx + eps) {
-            double p = (one_minus_delta_xf - prev + eps) / (nx - prev + eps);
-            keep = K - 1 - mm;
-            if (orc_lcg_real_unit(rng_state) > p)
-                keep += 1;        /* insertInMinHeap of the extracted element: it is at position K-1-mm */
-            break;
+    if (hi > num0) {
+        double carry = num0, prev_last = num0;
+        size_t size = K;
+        for (size_t q = 0; q < K; q += 32) {
+            size_t target = (K - q > 32) ? K - q - 32 : 1;     /* heap size after this chunk */
+            for (; size > target; --size) {                   /* extracFromMinHeap */
+                uint32_t t = h.data[0];
+                h.data[0] = h.data[size - 1];
+                h.data[size - 1] = t;
+                heap_sift(&h, 0, size - 1);
+            }
+            double v[32], w[32];
+            int n = (int)((K - q) < 32 ? (K - q) : 32);
+            for (int l = 0; l < 32; ++l) {                     /* extracted term m is at K - 1 - m */
+                if (l < n) {
+                    uint32_t index = h.data[K - 1 - (q + (size_t)l)];
+                    double item = m[index];
+                    uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
+                    v[l] = (ir == jc) ? item * item : (item * item) * 2.0;
+                } else {
+                    v[l] = 0.0;
+                }
+            }
+            for (int hh = 1; hh < 32; hh <<= 1) {
+                for (int l = 0; l < 32; ++l)
+                    w[l] = (l >= hh) ? v[l] + v[l - hh] : v[l];
+                memcpy(v, w, sizeof(v));
+            }
+            int hit = -1;
+            double prev = prev_last, nx = 0.0;
+            for (int l = 0; l < n; ++l) {
+                prev = (l == 0) ? prev_last : carry + v[l - 1];
+                nx = carry + v[l];
+                if (hi > prev && one_minus_delta_xf < nx + eps) {
+                    hit = l;
+                    break;
+                }
+            }
+            if (hit >= 0) {
+                size_t mm = q + (size_t)hit;
+                double p = (one_minus_delta_xf - prev + eps) / (nx - prev + eps);
+                keep = K - 1 - mm;
+                if (orc_lcg_real_unit(rng_state) > p)
+                    keep += 1;        /* insertInMinHeap of the extracted element: it is at position K-1-mm */
+                break;
+            }
+            prev_last = carry + v[n - 1];
+            carry = carry + v[n - 1];
         }
     }
     free(terms);
-    free(next);
     qsort(out, keep, sizeof(uint32_t), cmp_u32);
     return (int32_t)keep;
 }

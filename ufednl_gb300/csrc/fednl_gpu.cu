@@ -97,7 +97,7 @@ int chol_grid(int d)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_coop, kCoopThreads, 0);
-    long long m = d > kCholNB ? d - kCholNB : 1;
+    long long m = d + 1 > kCholNB ? d + 1 - kCholNB : 1;
     long long want = (m * (m + 1) / 2 + kCoopThreads - 1) / kCoopThreads;
     long long g = std::min<long long>(want, (long long)sms * std::max(bps, 1));
     g = std::min<long long>(g, sms);
@@ -349,7 +349,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.rstate, h->nc);
     A.want(&P.rseq, h->nc);
     A.want(&P.hmap, (size_t)h->nc * h->hcap);
-    A.want(&P.work, h->U);
+    A.want(&P.work, (size_t)(h->d + 1) * (h->d + 2) / 2);
     A.want(&P.dx, h->d);
     A.want(&P.ybuf, h->d);
     A.want(&P.rinv, h->d);
@@ -948,7 +948,7 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     s.a.want(&dfull, (size_t)d * lda);
     s.a.want(&dpack, U);
     s.a.want(&dg, d);
-    s.a.want(&P.work, U);
+    s.a.want(&P.work, (size_t)(d + 1) * (d + 2) / 2);
     s.a.want(&P.dx, d);
     s.a.want(&P.ybuf, d);
     s.a.want(&P.rinv, d);
@@ -1087,8 +1087,8 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
 // first call made on it.
 namespace {
 constexpr int kNoAllocMaxD = 512;
-constexpr size_t kNoAllocMaxU = (size_t)kNoAllocMaxD * (kNoAllocMaxD + 1) / 2;
-constexpr size_t kNoAllocDoubles = kNoAllocMaxU + 2 * kNoAllocMaxD + 4;   // factor, y, 1/r, barrier+status
+constexpr size_t kNoAllocMaxUA = (size_t)(kNoAllocMaxD + 1) * (kNoAllocMaxD + 2) / 2;   // factor with y column
+constexpr size_t kNoAllocDoubles = kNoAllocMaxUA + 2 * kNoAllocMaxD + 4;   // factor, y, 1/r, barrier+status
 constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 static double* g_noalloc_ptr[kNoAllocMaxDevices];
@@ -1116,10 +1116,10 @@ int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, dou
     P.d = d;
     P.U = (int)U;
     P.work = base;
-    P.ybuf = base + kNoAllocMaxU;
-    P.rinv = base + kNoAllocMaxU + kNoAllocMaxD;
-    P.bar = (unsigned*)(base + kNoAllocMaxU + 2 * kNoAllocMaxD);       // 4 x u32 = 2 doubles
-    P.status = (int*)(base + kNoAllocMaxU + 2 * kNoAllocMaxD + 2);
+    P.ybuf = base + kNoAllocMaxUA;
+    P.rinv = base + kNoAllocMaxUA + kNoAllocMaxD;
+    P.bar = (unsigned*)(base + kNoAllocMaxUA + 2 * kNoAllocMaxD);       // 4 x u32 = 2 doubles
+    P.status = (int*)(base + kNoAllocMaxUA + 2 * kNoAllocMaxD + 2);
     cudaStream_t st = (cudaStream_t)stream;
     // barrier counters and status must start at zero; the factor is overwritten by every call
     CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(double), st));

@@ -467,12 +467,13 @@ __global__ void k_h_init(Dev P)
 // * buildMinHeap runs level by level in parallel: sifts of nodes on one level touch disjoint
 //   subtrees, so the result equals the reference's descending-index order.
 // * The scanned entries stream into shared memory by bulk asynchronous copies (cp.async.bulk with
-//   an mbarrier per buffer, double-buffered); one warp tests them 32 at a time with a ballot.
-// * TopLEK extracts to the end recording the order in place (extracFromMinHeap leaves the
-//   extracted element at the array's end, MinHeap.h:133-140); the top two heap levels live in
-//   registers during the extraction loop.  The window numerator uses the fixed parallel order of
-//   the CPU oracle (chunked tree for the heap's terms, chunked doubling scan plus in-order carries
-//   for the extracted terms).
+//   an mbarrier per buffer, double-buffered); one warp tests them 256 at a time, one vote per
+//   256 when none exceeds the root, one ballot per 32 otherwise.
+// * TopLEK extracts in chunks of 32 recording the order in place (extracFromMinHeap leaves the
+//   extracted element at the array's end, MinHeap.h:133-140) and stops after the chunk that opens
+//   the rounding window; the top two heap levels live in registers during the extraction.  The
+//   window numerator uses the fixed parallel order of the CPU oracle (chunked tree for the heap's
+//   terms, chunked doubling scan plus in-order carries for the extracted terms).
 struct HeapS {
     unsigned long long* key;   // bits of |value|
     unsigned* hid;             // p | kDiagBit
@@ -493,27 +494,57 @@ __device__ __forceinline__ void heap_swap(HeapS& h, int a, int b)
     h.hid[b] = ti;
 }
 
-// minHeapify, MinHeap.h:255-290, entered at node i with the carried comparison value
-__device__ void heap_sift_from(HeapS& h, int i, int heap_size, unsigned long long lowest_value)
+// minHeapify, MinHeap.h:255-290.  The entry (ck, ci) enters at node i with the carried comparison
+// value lv.  The reference walks the children in order and moves to a child whose value is
+// strictly below the running value, so it lands on the leftmost child holding the children's
+// minimum whenever that minimum is strictly below lv; the carried value then becomes that
+// minimum (the value that moved up, not the entry being sifted).  A two-level tree with strict
+// '<' finds the same child.  The key array is placed so that the four children 4i+1..4i+4 of a
+// node start on a 32-byte boundary (two 16-byte loads), the id array so that they start on a
+// 16-byte boundary.  The path moves up one node and (ck, ci) is written where the walk stops,
+// which equals the reference's chain of swaps.
+__device__ __forceinline__ void heap_descend(HeapS& h, int i, int n, unsigned long long lv,
+                                             unsigned long long ck, unsigned ci)
 {
     for (;;) {
-        int lowest = i;
-        const int first = 4 * i + 1;
-        const int last = min(first + 4, heap_size);
-        for (int c = first; c < last; ++c) {
-            const unsigned long long cv = h.key[c];
-            if (lowest_value > cv) {
-                lowest = c;
-                lowest_value = cv;
+        const int f = 4 * i + 1;
+        int lo;
+        unsigned long long m;
+        if (f + 3 < n) {
+            const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(h.key + f);
+            const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(h.key + f + 2);
+            const bool r12 = a.y < a.x, r34 = b.y < b.x;
+            const unsigned long long m12 = r12 ? a.y : a.x, m34 = r34 ? b.y : b.x;
+            const bool r = m34 < m12;
+            m = r ? m34 : m12;
+            lo = f + (r ? (r34 ? 3 : 2) : (r12 ? 1 : 0));
+        } else {
+            if (f >= n) break;
+            lo = f;
+            m = h.key[f];
+            for (int c = f + 1; c < n; ++c) {
+                const unsigned long long cv = h.key[c];
+                if (cv < m) {
+                    m = cv;
+                    lo = c;
+                }
             }
         }
-        if (lowest == i) break;
-        heap_swap(h, i, lowest);
-        i = lowest;
+        if (!(lv > m)) break;
+        h.key[i] = m;
+        h.hid[i] = h.hid[lo];
+        i = lo;
+        lv = m;
     }
+    h.key[i] = ck;
+    h.hid[i] = ci;
 }
 
-__device__ __forceinline__ void heap_sift(HeapS& h, int i, int heap_size) { heap_sift_from(h, i, heap_size, h.key[i]); }
+__device__ __forceinline__ void heap_sift(HeapS& h, int i, int heap_size)
+{
+    const unsigned long long kv = h.key[i];
+    heap_descend(h, i, heap_size, kv, kv, h.hid[i]);
+}
 
 constexpr int kSelThreads = 128;
 constexpr int kSelStage = 2048;                    // doubles per staging buffer (16 KB)
@@ -526,10 +557,18 @@ __device__ __forceinline__ double term_of(unsigned long long key, unsigned id)
     return (id & kDiagBit) ? t : __dmul_rn(t, 2.0);
 }
 
+// dynamic shared memory of k_select: two staging buffers, key[k] (three slots ahead and 32 bytes
+// of alignment slack), terms[k], hid[k] (three slots ahead, 16 bytes of slack), chunk sums
 __host__ __device__ inline size_t select_smem_bytes(int k)
 {
-    return 2 * (size_t)kSelStage * 8 + (size_t)k * 8 /*key*/ + (size_t)k * 8 /*terms*/ + (size_t)k * 4 /*hid*/ +
-           ((size_t)(k + 31) / 32) * 8 /*chunk sums*/ + 16;
+    return 2 * (size_t)kSelStage * 8 + 32 + ((size_t)k + 3) * 8 /*key*/ + (size_t)k * 8 /*terms*/ + 16 +
+           ((size_t)k + 3) * 4 /*hid*/ + 8 + ((size_t)(k + 31) / 32) * 8 /*chunk sums*/;
+}
+
+template <typename T>
+__device__ __forceinline__ T* align_up_ptr(void* p, size_t a)
+{
+    return reinterpret_cast<T*>(((size_t)p + a - 1) & ~(a - 1));
 }
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -567,7 +606,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 // vals: [n_mat][ustr] packed upper values (signed), rows 16-byte aligned (ustr even); F: [n_mat]
 // squared Frobenius norms.  Output: sel bitmap per matrix, cnt (entries kept before the rounding
 // draw), TopLEK draw request.  err: set to 1 if a bounded wait ran out.
-__global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict__ vals, int ustr, int U, int k,
+__global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int ustr, int U, int k,
                                                         int lek, double delta, const double* __restrict__ F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
                                                         double* pdraw, int* minidx, int* err)
@@ -575,7 +614,6 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     __shared__ __align__(8) unsigned long long s_bar[2];
     __shared__ int s_keep, s_fail;
-    __shared__ double s_num0;
     const int c = blockIdx.x;
     const double* v = vals + (size_t)c * ustr;
     unsigned* sc = sel + (size_t)c * SW;
@@ -594,12 +632,12 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
         }
         return;
     }
-    double* stage = (double*)s_dyn;                                  // [2][kSelStage]
+    double* stage = (double*)s_dyn;                                          // [2][kSelStage]
     HeapS h;
-    h.key = s_dyn + 2 * kSelStage;                                   // [k]
-    double* terms = (double*)(h.key + k);                            // [k]
-    h.hid = (unsigned*)(terms + k);                                  // [k]
-    double* csum = (double*)(((size_t)(h.hid + k) + 7) & ~(size_t)7);  // [ceil(k/32)]
+    h.key = align_up_ptr<unsigned long long>(s_dyn + 2 * kSelStage, 32) + 3;  // [k], key+1 32-byte aligned
+    double* terms = (double*)(h.key + k);                                    // [k]
+    h.hid = align_up_ptr<unsigned>(terms + k, 16) + 3;                       // [k], hid+1 16-byte aligned
+    double* csum = align_up_ptr<double>(h.hid + k, 8);                       // [ceil(k/32)]
 
     // scanned region [k, U) streamed in chunks starting at an even element (16-byte aligned)
     const int s0 = k & ~1;
@@ -647,25 +685,35 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
             const int st = s0 + q * kSelStage;
             const int len = min(kSelStage, U - st);
             const double* buf = stage + b * kSelStage;
-            for (int o = 0; o < len; o += 32) {
-                const int e = st + o + lane;
-                const bool ok = (o + lane < len) && e >= k;
-                const unsigned long long vv = ok ? abs_bits(buf[o + lane]) : 0ull;
-                unsigned mask = __ballot_sync(0xffffffffu, ok && vv > root);
-                while (mask) {
-                    const int l = __ffs(mask) - 1;
-                    const unsigned long long cand = __shfl_sync(0xffffffffu, vv, l);
-                    if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
-                        const int p = st + o + l;
-                        h.key[0] = cand;
-                        h.hid[0] = (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u);
-                        heap_sift(h, 0, k);
+            // 256 entries per step (8 per lane, lane-contiguous groups of 32); a step with no entry
+            // above the root costs one vote.  Entries outside [k, U) read as 0, which never exceeds
+            // the root.
+            for (int o = 0; o < len; o += 256) {
+                bool any = false;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int idx = o + j * 32 + lane;
+                    any |= ((idx < len && st + idx >= k) ? abs_bits(buf[idx]) : 0ull) > root;
+                }
+                if (!__any_sync(0xffffffffu, any)) continue;
+#pragma unroll 1
+                for (int j = 0; j < 8; ++j) {     // in order, 32 entries at a time
+                    const int idx = o + j * 32 + lane;
+                    const unsigned long long vv = (idx < len && st + idx >= k) ? abs_bits(buf[idx]) : 0ull;
+                    unsigned mask = __ballot_sync(0xffffffffu, vv > root);
+                    while (mask) {
+                        const int l = __ffs(mask) - 1;
+                        const unsigned long long cand = __shfl_sync(0xffffffffu, vv, l);
+                        if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
+                            const int p = st + o + j * 32 + l;
+                            heap_descend(h, 0, k, cand, cand, (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u));
+                        }
+                        __syncwarp();
+                        root = *(volatile unsigned long long*)&h.key[0];
+                        // the root of this heap can also decrease (a deeper element may move up), so
+                        // the remaining lanes are tested again against the new root
+                        mask = __ballot_sync(0xffffffffu, vv > root) & ~((2u << l) - 1u);
                     }
-                    __syncwarp();
-                    root = *(volatile unsigned long long*)&h.key[0];
-                    // the root of this heap can also decrease (a deeper element may move up), so the
-                    // remaining lanes are tested again against the new root
-                    mask = __ballot_sync(0xffffffffu, ok && vv > root) & ~((2u << l) - 1u);
                 }
             }
             __syncwarp();
@@ -699,119 +747,136 @@ __global__ void __launch_bounds__(kSelThreads) k_select(const double* __restrict
             if (lane == 0) csum[q] = cs;
         }
         __syncthreads();
-        if (tid == 0) {
-            double sh = 0.0;
-            for (int q = 0; q < nch; ++q) sh = __dadd_rn(sh, csum[q]);
-            s_num0 = __dsub_rn(F[c], sh);
-            // extraction to the end (extracFromMinHeap, MinHeap.h:125-141); element m lands at k-1-m.
-            // Positions 0..4 are kept in registers while the heap still has more than 21 entries.
-            unsigned long long K0 = h.key[0], K1 = h.key[1], K2 = h.key[2], K3 = h.key[3], K4 = h.key[4];
-            unsigned I0 = h.hid[0], I1 = h.hid[1], I2 = h.hid[2], I3 = h.hid[3], I4 = h.hid[4];
-            int size = k;
-            for (; size > 21; --size) {
-                const int n = size - 1;                    // heap size after the swap
-                const unsigned long long LK = h.key[n];
-                const unsigned LI = h.hid[n];
-                h.key[n] = K0;
-                h.hid[n] = I0;
-                // level 1: leftmost child strictly below the running lowest value
-                unsigned long long lv = LK;
-                int lo = 0;
-                if (lv > K1) { lo = 1; lv = K1; }
-                if (lv > K2) { lo = 2; lv = K2; }
-                if (lv > K3) { lo = 3; lv = K3; }
-                if (lv > K4) { lo = 4; lv = K4; }
-                if (lo == 0) {
-                    K0 = LK;
-                    I0 = LI;
-                    continue;
-                }
-                // root takes the child, the child's slot takes L (still in registers)
-                unsigned ci;
-                if (lo == 1) { K0 = K1; I0 = I1; K1 = LK; I1 = LI; }
-                else if (lo == 2) { K0 = K2; I0 = I2; K2 = LK; I2 = LI; }
-                else if (lo == 3) { K0 = K3; I0 = I3; K3 = LK; I3 = LI; }
-                else { K0 = K4; I0 = I4; K4 = LK; I4 = LI; }
-                (void)ci;
-                // level 2: children of `lo` against the value that moved up (lv)
-                const int f2 = 4 * lo + 1;
-                int g = -1;
-                unsigned long long lv2 = lv;
-                for (int t = 0; t < 4; ++t) {
-                    const unsigned long long cv = h.key[f2 + t];
-                    if (lv2 > cv) { g = t; lv2 = cv; }
-                }
-                if (g < 0) continue;
-                const int gp = f2 + g;
-                const unsigned long long GK = h.key[gp];
-                const unsigned GI = h.hid[gp];
-                h.key[gp] = LK;
-                h.hid[gp] = LI;
-                if (lo == 1) { K1 = GK; I1 = GI; }
-                else if (lo == 2) { K2 = GK; I2 = GI; }
-                else if (lo == 3) { K3 = GK; I3 = GI; }
-                else { K4 = GK; I4 = GI; }
-                heap_sift_from(h, gp, n, lv2);           // deeper levels, carried value as in the reference
-            }
-            h.key[0] = K0; h.key[1] = K1; h.key[2] = K2; h.key[3] = K3; h.key[4] = K4;
-            h.hid[0] = I0; h.hid[1] = I1; h.hid[2] = I2; h.hid[3] = I3; h.hid[4] = I4;
-            for (; size > 1; --size) {
-                heap_swap(h, 0, size - 1);
-                heap_sift(h, 0, size - 1);
-            }
-        }
-        __syncthreads();
-        // extracted terms (extraction order m = position k-1-m), chunk-local doubling scans
-        for (int q = warp; q < nch; q += nwarps) {
-            const int m = q * 32 + lane;
-            double x = (m < k) ? term_of(h.key[k - 1 - m], h.hid[k - 1 - m]) : 0.0;
-            for (int hh = 1; hh < 32; hh <<= 1) {
-                const double y = __shfl_up_sync(0xffffffffu, x, hh);
-                if (lane >= hh) x = __dadd_rn(x, y);
-            }
-            if (m < k) terms[m] = x;
-            const int last = min(31, k - 1 - q * 32);
-            const double tot = __shfl_sync(0xffffffffu, x, last);
-            if (lane == 0) csum[q] = tot;
-        }
-        __syncthreads();
-        if (tid == 0) {          // carries in order: carry_q = num0 + totals of chunks < q
-            double carry = s_num0;
-            for (int q = 0; q < nch; ++q) {
-                const double t = csum[q];
-                csum[q] = carry;
-                carry = __dadd_rn(carry, t);
-            }
-        }
-        __syncthreads();
-        for (int m = tid; m < k; m += blockDim.x) terms[m] = __dadd_rn(csum[m >> 5], terms[m]);   // next_m
-        __syncthreads();
         if (warp == 0) {
-            // first extraction whose window condition holds (SpecialMathRoutinesForMatrix.h:475-476)
+            double sh = 0.0;
+            if (lane == 0)
+                for (int q = 0; q < nch; ++q) sh = __dadd_rn(sh, csum[q]);
             const double fr = F[c];
+            const double num0 = __dsub_rn(fr, __shfl_sync(0xffffffffu, sh, 0));
+            // window test of SpecialMathRoutinesForMatrix.h:475-476 on the numerators before (prev) and
+            // after (next) extraction m: hi > prev and omd < next + eps
             const double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
             const double eps = __dmul_rn(1e-1, fr);
             const double hi = __dadd_rn(omd, eps);
-            const double num0 = s_num0;
             int first = k;
-            for (int m0 = 0; m0 < k; m0 += 32) {       // warp-uniform bounds
-                const int m = m0 + lane;
-                bool hit = false;
-                if (m < k) {
-                    const double prev = (m == 0) ? num0 : terms[m - 1];
-                    hit = hi > prev && omd < __dadd_rn(terms[m], eps);
+            double prev_hit = 0.0, next_hit = 0.0;
+            // Each numerator is num0 plus non-negative terms, added with monotone rounding, so none is
+            // below num0: if hi > num0 fails no extraction opens the window, and none is made.
+            if (hi > num0) {
+                // Extraction (extracFromMinHeap, MinHeap.h:125-141) in chunks of 32: element m lands at
+                // position k-1-m.  After each chunk the warp forms the chunk's numerators (doubling
+                // scan of its terms, plus the carry of the chunks before it) and stops at the first
+                // chunk holding a window hit.  Extractions after the hit only reorder positions
+                // [0, k-1-first), whose set is what is kept.  While the heap has more than 21
+                // entries, positions 0..4 live in lane 0's registers.
+                unsigned long long K0 = 0, K1 = 0, K2 = 0, K3 = 0, K4 = 0;
+                unsigned I0 = 0, I1 = 0, I2 = 0, I3 = 0, I4 = 0;
+                int size = k;
+                bool live = false;
+                if (lane == 0 && k > 21) {
+                    K0 = h.key[0]; K1 = h.key[1]; K2 = h.key[2]; K3 = h.key[3]; K4 = h.key[4];
+                    I0 = h.hid[0]; I1 = h.hid[1]; I2 = h.hid[2]; I3 = h.hid[3]; I4 = h.hid[4];
+                    live = true;
                 }
-                const unsigned b = __ballot_sync(0xffffffffu, hit);
-                if (b) {
-                    first = m0 + __ffs(b) - 1;
-                    break;
+                double carry = num0, prev_last = num0;
+                for (int q = 0; q < nch; ++q) {
+                    if (lane == 0) {
+                        const int target = max(k - 32 * (q + 1), 1);     // heap size after this chunk
+                        for (; live && size > max(target, 21); --size) {
+                            const int n = size - 1;                      // heap size after the swap
+                            const unsigned long long LK = h.key[n];
+                            const unsigned LI = h.hid[n];
+                            // level-2 keys (positions 5..20), loaded ahead of the level-1 decision
+                            unsigned long long G[16];
+#pragma unroll
+                            for (int t = 0; t < 8; ++t) {
+                                const ulonglong2 g2 = *reinterpret_cast<const ulonglong2*>(h.key + 5 + 2 * t);
+                                G[2 * t] = g2.x;
+                                G[2 * t + 1] = g2.y;
+                            }
+                            h.key[n] = K0;
+                            h.hid[n] = I0;
+                            // level 1, leftmost minimum of the children, moved up if strictly below L
+                            const bool r12 = K2 < K1, r34 = K4 < K3;
+                            const unsigned long long m12 = r12 ? K2 : K1, m34 = r34 ? K4 : K3;
+                            const bool r = m34 < m12;
+                            const unsigned long long lv = r ? m34 : m12;
+                            const int lo = r ? (r34 ? 4 : 3) : (r12 ? 2 : 1);
+                            if (!(LK > lv)) {
+                                K0 = LK;
+                                I0 = LI;
+                                continue;
+                            }
+                            // root takes the child, the child's slot takes L (still in registers)
+                            if (lo == 1) { K0 = K1; I0 = I1; K1 = LK; I1 = LI; }
+                            else if (lo == 2) { K0 = K2; I0 = I2; K2 = LK; I2 = LI; }
+                            else if (lo == 3) { K0 = K3; I0 = I3; K3 = LK; I3 = LI; }
+                            else { K0 = K4; I0 = I4; K4 = LK; I4 = LI; }
+                            // level 2: children of `lo` against the value that moved up (lv)
+                            const int gb = 4 * (lo - 1);
+                            const unsigned long long g0 = lo == 1 ? G[0] : lo == 2 ? G[4] : lo == 3 ? G[8] : G[12];
+                            const unsigned long long g1 = lo == 1 ? G[1] : lo == 2 ? G[5] : lo == 3 ? G[9] : G[13];
+                            const unsigned long long g2 = lo == 1 ? G[2] : lo == 2 ? G[6] : lo == 3 ? G[10] : G[14];
+                            const unsigned long long g3 = lo == 1 ? G[3] : lo == 2 ? G[7] : lo == 3 ? G[11] : G[15];
+                            const bool s01 = g1 < g0, s23 = g3 < g2;
+                            const unsigned long long n01 = s01 ? g1 : g0, n23 = s23 ? g3 : g2;
+                            const bool sr = n23 < n01;
+                            const unsigned long long lv2 = sr ? n23 : n01;
+                            if (!(lv > lv2)) continue;
+                            const int gp = 5 + gb + (sr ? (s23 ? 3 : 2) : (s01 ? 1 : 0));
+                            const unsigned GI = h.hid[gp];
+                            if (lo == 1) { K1 = lv2; I1 = GI; }
+                            else if (lo == 2) { K2 = lv2; I2 = GI; }
+                            else if (lo == 3) { K3 = lv2; I3 = GI; }
+                            else { K4 = lv2; I4 = GI; }
+                            // L enters at gp; deeper levels carry the value that moved up, as the reference
+                            heap_descend(h, gp, n, lv2, LK, LI);
+                        }
+                        if (live && size <= 21) {
+                            h.key[0] = K0; h.key[1] = K1; h.key[2] = K2; h.key[3] = K3; h.key[4] = K4;
+                            h.hid[0] = I0; h.hid[1] = I1; h.hid[2] = I2; h.hid[3] = I3; h.hid[4] = I4;
+                            live = false;
+                        }
+                        for (; size > target; --size) {
+                            const int n = size - 1;
+                            const unsigned long long LK = h.key[n];
+                            const unsigned LI = h.hid[n];
+                            h.key[n] = h.key[0];
+                            h.hid[n] = h.hid[0];
+                            heap_descend(h, 0, n, LK, LK, LI);
+                        }
+                    }
+                    __syncwarp();
+                    const int m = q * 32 + lane;
+                    double x = (m < k) ? term_of(h.key[k - 1 - m], h.hid[k - 1 - m]) : 0.0;
+                    for (int hh = 1; hh < 32; hh <<= 1) {
+                        const double y = __shfl_up_sync(0xffffffffu, x, hh);
+                        if (lane >= hh) x = __dadd_rn(x, y);
+                    }
+                    const double tot = __shfl_sync(0xffffffffu, x, min(31, k - 1 - q * 32));
+                    const double nxt = __dadd_rn(carry, x);
+                    double prv = __shfl_up_sync(0xffffffffu, nxt, 1);
+                    if (lane == 0) prv = prev_last;
+                    const unsigned hits = __ballot_sync(0xffffffffu, m < k && hi > prv && omd < __dadd_rn(nxt, eps));
+                    if (hits) {
+                        const int l = __ffs(hits) - 1;
+                        first = q * 32 + l;
+                        prev_hit = __shfl_sync(0xffffffffu, prv, l);
+                        next_hit = __shfl_sync(0xffffffffu, nxt, l);
+                        break;
+                    }
+                    prev_last = __shfl_sync(0xffffffffu, nxt, 31);
+                    carry = __dadd_rn(carry, tot);
                 }
+                if (lane == 0 && live) {
+                    h.key[0] = K0; h.key[1] = K1; h.key[2] = K2; h.key[3] = K3; h.key[4] = K4;
+                    h.hid[0] = I0; h.hid[1] = I1; h.hid[2] = I2; h.hid[3] = I3; h.hid[4] = I4;
+                }
+                __syncwarp();
             }
             if (lane == 0) {
                 if (first < k) {
-                    const double prev = (first == 0) ? num0 : terms[first - 1];
-                    const double next = terms[first];
-                    pdraw[c] = __dadd_rn(__dsub_rn(omd, prev), eps) / __dadd_rn(__dsub_rn(next, prev), eps);
+                    pdraw[c] = __dadd_rn(__dsub_rn(omd, prev_hit), eps) / __dadd_rn(__dsub_rn(next_hit, prev_hit), eps);
                     needs[c] = 1;
                     minidx[c] = (int)(h.hid[k - 1 - first] & ~kDiagBit);
                     s_keep = k - 1 - first;      // positions [0, k-1-first) stay in the heap
@@ -1023,8 +1088,11 @@ __device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j +
 //   3. grid barrier, then all threads apply the panel to the trailing triangle entry by entry
 //      (a_ij = fma(-r_ki, r_kj, a_ij), k over the panel in order); grid barrier.
 // Every entry undergoes exactly the operation sequence of the unblocked right-looking algorithm,
-// so the factor equals the single-CTA (and CPU oracle) factor bit for bit.  The triangular
-// solves run in CTA 0, blocked by 32 rows with the same per-element operation order.
+// so the factor equals the CPU oracle's factor bit for bit.  g is appended as column d of the
+// packed matrix: the strips and trailing updates then carry out the forward substitution
+// R^T y = g in the column-oriented order (y_t *= 1/r_tt, y_i = fma(-r_ti, y_t, y_i)), and y ends
+// up in column d.  The backward substitution runs in CTA 0, blocked by 32 rows, same order as the
+// oracle's.
 constexpr int kCholNB = 32;
 constexpr int kCoopThreads = 256;
 constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIMEOUT
@@ -1076,16 +1144,22 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     __shared__ double s_inv[kCholNB];
     __shared__ int s_fail;
     const double l = lptr ? *lptr : lval;
-    const int d = P.d, U = P.U;
-    double* A = P.work;
+    const int d = P.d;
+    const int D = d + 1;                       // augmented by the right-hand side
+    const int UA = D * (D + 1) / 2;
+    double* A = P.work;                        // [UA]
     const unsigned G = gridDim.x;
     const int tid = threadIdx.x, lane = tid & 31;
     const int gtid = blockIdx.x * blockDim.x + tid, gthreads = G * blockDim.x;
-    for (int p = gtid; p < U; p += gthreads) {
+    for (int p = gtid; p < UA; p += gthreads) {
         int i, j;
         upper_ij(p, i, j);
-        const double hv = hin_lda > 0 ? Hin[(size_t)j * hin_lda + i] : Hin[p];
-        A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
+        if (j < d) {
+            const double hv = hin_lda > 0 ? Hin[(size_t)j * hin_lda + i] : Hin[p];
+            A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
+        } else {
+            A[p] = (i < d) ? gin[i] : 0.0;
+        }
     }
     if (!grid_barrier(P.bar, G)) goto timeout;
     for (int c0 = 0; c0 < d; c0 += kCholNB) {
@@ -1133,9 +1207,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             }
             for (int t = tid; t < nb; t += blockDim.x) P.rinv[c0 + t] = s_inv[t];
         }
-        // panel rows of R for the columns right of the diagonal block
+        // panel rows of R for the columns right of the diagonal block (and of y in column d)
         const int gw = gtid >> 5, nwarps = gthreads >> 5;
-        for (int j = c1 + gw; j < d; j += nwarps) {
+        for (int j = c1 + gw; j < D; j += nwarps) {
             double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
             for (int k = 0; k < nb; ++k) {
                 if (lane == k) a = __dmul_rn(a, s_inv[k]);
@@ -1146,9 +1220,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         }
         if (c1 >= d) break;
         if (!grid_barrier(P.bar, G)) goto timeout;
-        // trailing update, entries (i, j) with c1 <= i <= j < d
+        // trailing update, entries (i, j) with c1 <= i <= j < D (column d carries y)
         {
-            const int m = d - c1;
+            const int m = D - c1;
             const int T = m * (m + 1) / 2;
             for (int e = gtid; e < T; e += gthreads) {
                 int ii, jj;
@@ -1166,11 +1240,11 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     if (!grid_barrier(P.bar, G)) goto timeout;
     if (blockIdx.x != 0) return;
     {
-        // R^T y = g then R dx = y, blocked by 32 rows (CTA 0)
+        // R dx = y (y in column d), blocked by 32 rows (CTA 0)
         double* y = P.ybuf;
         double gs = 0.0;
         for (int i = tid; i < d; i += blockDim.x) {
-            y[i] = gin[i];
+            y[i] = A[up_pos(i, d)];
             gs += gin[i] * gin[i];
         }
         if (record) {   // ||g|| for the round statistics
@@ -1185,27 +1259,6 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             }
         }
         __syncthreads();
-        for (int b0 = 0; b0 < d; b0 += 32) {
-            const int b1 = min(d, b0 + 32);
-            if (tid < 32) {
-                double v = (b0 + lane < b1) ? y[b0 + lane] : 0.0;
-                for (int s = 0; s < b1 - b0; ++s) {
-                    const int t = b0 + s;
-                    if (lane == s) v = __dmul_rn(v, P.rinv[t]);
-                    double yt = __shfl_sync(0xffffffffu, v, s);
-                    if (lane > s && b0 + lane < b1) v = fma(-A[up_pos(t, b0 + lane)], yt, v);
-                }
-                if (b0 + lane < b1) y[b0 + lane] = v;
-            }
-            __syncthreads();
-            for (int i = b1 + tid; i < d; i += blockDim.x) {
-                double v = y[i];
-                const double* ci = A + up_pos(0, i);
-                for (int t = b0; t < b1; ++t) v = fma(-ci[t], y[t], v);
-                y[i] = v;
-            }
-            __syncthreads();
-        }
         for (int b1 = d; b1 > 0; b1 -= 32) {
             const int b0 = max(0, b1 - 32);
             if (tid < 32) {
