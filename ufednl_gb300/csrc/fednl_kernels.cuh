@@ -22,7 +22,6 @@
 namespace fednl {
 
 constexpr int kMaxK = 9600;             // largest TopK/TopLEK k: heap, chain and staging fit in 227 KB of shared memory
-constexpr unsigned kDiagBit = 0x80000000u;
 
 struct Dev {
     // sizes and scalars
@@ -476,7 +475,7 @@ __global__ void k_h_init(Dev P)
 //   terms, chunked doubling scan plus in-order carries for the extracted terms).
 struct HeapS {
     unsigned long long* key;   // bits of |value|
-    unsigned* hid;             // p | kDiagBit
+    unsigned* hid;             // packed upper position p
 };
 
 __device__ __forceinline__ unsigned long long abs_bits(double v)
@@ -550,11 +549,38 @@ constexpr int kSelThreads = 128;
 constexpr int kSelStage = 2048;                    // doubles per staging buffer (16 KB)
 constexpr long long kSelWaitCycles = 2000000000ll; // bounded mbarrier wait (~1 s)
 
-__device__ __forceinline__ double term_of(unsigned long long key, unsigned id)
+// c v^2 with c = 1 on the diagonal and 2 off it
+__device__ __forceinline__ double term_of(unsigned long long key, unsigned p)
 {
     double v = __longlong_as_double((long long)key);
     double t = __dmul_rn(v, v);
-    return (id & kDiagBit) ? t : __dmul_rn(t, 2.0);
+    return upper_is_diag((int)p) ? t : __dmul_rn(t, 2.0);
+}
+
+// increaseMinimumInMinHeap (MinHeap.h:78-85): the root takes (cand, p) and sifts down; returns the
+// new root value, which the scanning warp compares against next
+__device__ __forceinline__ unsigned long long heap_replace_root(HeapS& h, int k, unsigned long long cand, unsigned p)
+{
+    if (k < 5) {
+        heap_descend(h, 0, k, cand, cand, p);
+        return h.key[0];
+    }
+    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(h.key + 1);
+    const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(h.key + 3);
+    const bool r12 = a.y < a.x, r34 = b.y < b.x;
+    const unsigned long long m12 = r12 ? a.y : a.x, m34 = r34 ? b.y : b.x;
+    const bool r = m34 < m12;
+    const unsigned long long m = r ? m34 : m12;
+    if (!(cand > m)) {
+        h.key[0] = cand;
+        h.hid[0] = p;
+        return cand;
+    }
+    const int lo = 1 + (r ? (r34 ? 3 : 2) : (r12 ? 1 : 0));
+    h.key[0] = m;
+    h.hid[0] = h.hid[lo];
+    heap_descend(h, lo, k, m, cand, p);
+    return m;
 }
 
 // dynamic shared memory of k_select: two staging buffers, key[k] (three slots ahead and 32 bytes
@@ -655,7 +681,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
     }
     for (int t = tid; t < k; t += blockDim.x) {
         h.key[t] = abs_bits(v[t]);
-        h.hid[t] = (unsigned)t | (upper_is_diag(t) ? kDiagBit : 0u);
+        h.hid[t] = (unsigned)t;
     }
     __syncthreads();
     // buildMinHeap (MinHeap.h:147-191) level by level, deepest first
@@ -685,35 +711,43 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
             const int st = s0 + q * kSelStage;
             const int len = min(kSelStage, U - st);
             const double* buf = stage + b * kSelStage;
-            // 256 entries per step (8 per lane, lane-contiguous groups of 32); a step with no entry
-            // above the root costs one vote.  Entries outside [k, U) read as 0, which never exceeds
-            // the root.
+            // 256 entries per step, 8 per lane in lane-contiguous groups of 32 (entry e = 32 j + lane
+            // of the step).  Each pass votes all 8 groups against the root and takes the first entry
+            // above it that comes after the last one taken; lane 0 replaces the root and broadcasts
+            // the new root.  The root of this heap can also decrease (a deeper element may move up),
+            // so every remaining entry is voted again after each replacement.  Entries outside
+            // [k, U) read as 0, which never exceeds the root.
             for (int o = 0; o < len; o += 256) {
-                bool any = false;
+                unsigned long long v[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int idx = o + j * 32 + lane;
-                    any |= ((idx < len && st + idx >= k) ? abs_bits(buf[idx]) : 0ull) > root;
+                    v[j] = (idx < len && st + idx >= k) ? abs_bits(buf[idx]) : 0ull;
                 }
-                if (!__any_sync(0xffffffffu, any)) continue;
-#pragma unroll 1
-                for (int j = 0; j < 8; ++j) {     // in order, 32 entries at a time
-                    const int idx = o + j * 32 + lane;
-                    const unsigned long long vv = (idx < len && st + idx >= k) ? abs_bits(buf[idx]) : 0ull;
-                    unsigned mask = __ballot_sync(0xffffffffu, vv > root);
-                    while (mask) {
-                        const int l = __ffs(mask) - 1;
-                        const unsigned long long cand = __shfl_sync(0xffffffffu, vv, l);
-                        if (lane == 0) {   // increaseMinimumInMinHeap, MinHeap.h:78-85
-                            const int p = st + o + j * 32 + l;
-                            heap_descend(h, 0, k, cand, cand, (unsigned)p | (upper_is_diag(p) ? kDiagBit : 0u));
+                int done = -1;                           // last entry taken in this step
+                for (;;) {
+                    unsigned m[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) m[j] = __ballot_sync(0xffffffffu, v[j] > root && j * 32 + lane > done);
+                    int jf = -1;
+                    unsigned mf = 0u;
+#pragma unroll
+                    for (int j = 7; j >= 0; --j)
+                        if (m[j]) {
+                            jf = j;
+                            mf = m[j];
                         }
-                        __syncwarp();
-                        root = *(volatile unsigned long long*)&h.key[0];
-                        // the root of this heap can also decrease (a deeper element may move up), so
-                        // the remaining lanes are tested again against the new root
-                        mask = __ballot_sync(0xffffffffu, vv > root) & ~((2u << l) - 1u);
-                    }
+                    if (jf < 0) break;
+                    const int l = __ffs(mf) - 1;
+                    unsigned long long mine = v[0];
+#pragma unroll
+                    for (int j = 1; j < 8; ++j)
+                        if (jf == j) mine = v[j];
+                    const unsigned long long cand = __shfl_sync(0xffffffffu, mine, l);
+                    done = jf * 32 + l;
+                    unsigned long long nr = 0ull;
+                    if (lane == 0) nr = heap_replace_root(h, k, cand, (unsigned)(st + o + done));
+                    root = __shfl_sync(0xffffffffu, nr, 0);
                 }
             }
             __syncwarp();
@@ -878,7 +912,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
                 if (first < k) {
                     pdraw[c] = __dadd_rn(__dsub_rn(omd, prev_hit), eps) / __dadd_rn(__dsub_rn(next_hit, prev_hit), eps);
                     needs[c] = 1;
-                    minidx[c] = (int)(h.hid[k - 1 - first] & ~kDiagBit);
+                    minidx[c] = (int)h.hid[k - 1 - first];
                     s_keep = k - 1 - first;      // positions [0, k-1-first) stay in the heap
                 } else {
                     needs[c] = 0;
@@ -892,7 +926,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
         keep = s_keep;
     }
     for (int t = tid; t < keep; t += blockDim.x) {
-        const unsigned p = h.hid[t] & ~kDiagBit;
+        const unsigned p = h.hid[t];
         atomicOr(&sc[p >> 5], 1u << (p & 31));
     }
     if (tid == 0) cnt[c] = keep;
