@@ -647,6 +647,9 @@ typedef struct {
     uint32_t* msg_idx;  /* flat indices */
     double* msg_val;    /* values exactly as the master adds them to H */
     int32_t msg_count;
+    double* dir;        /* FedNL-PP: localGradient = x Lk + shift x - grad (d) */
+    double* ddir;       /* FedNL-PP: the difference last sent to the master (d) */
+    double dlk;         /* FedNL-PP: the Lk difference last sent */
 } orc_client;
 
 struct orc_state {
@@ -662,11 +665,21 @@ struct orc_state {
     double* ltr;
     double prescale;       /* alpha / n (TrainLoop.h:531) */
     int32_t k_eff;
+    /* FedNL-PP */
+    double* g_prev;        /* prev_global_gradient_estimation */
+    double l_prev;         /* prev_global_Li_fednl */
+    double* true_grad;     /* computeFullGradient at the round's starting iterate */
+    uint32_t sampler;      /* clientSampler (RandomGenIntegerLinear) */
+    uint32_t* perm;        /* [n] the sampler's permutation buffer */
+    uint8_t* is_sel;       /* [n] selected this round */
+    int32_t* selected;     /* [tau] ascending */
+    int32_t tau;
 };
 
-/* Worker side of one client for one round: LocalWorkerForFedNL_*.h, bodies of the per-context loops */
-static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* hbuf, double* diff,
-                         double* mtmp, double* stmp)
+/* Worker side of one client, first half: the compressor's index draw, margins, sigmoid, gradient,
+ * Hessian and difference (LocalWorkerForFedNL_*.h, bodies of the per-context loops).  Returns
+ * ||diff||_F^2. */
+static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff, double* mtmp, double* stmp)
 {
     const orc_problem* P = &S->p;
     orc_client* C = &S->clients[c];
@@ -674,7 +687,8 @@ static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* 
     size_t full = (size_t)d * (size_t)lda;
     size_t U = S->U;
 
-    /* RandK / RandSeqK draw their indices before the round starts (RandK.h:46-62, RandSeqK.h:46-62) */
+    /* RandK / RandSeqK draw their indices before the round starts (RandK.h:46-62, RandSeqK.h:46-62;
+     * FedNL-PP: only when the client is selected, bin_fednl_local_pp/.../RandSeqK.h:90-110) */
     if (P->compressor == ORC_RANDK)
         orc_randk(&C->rng, S->k_eff, U, S->upper, C->msg_idx);
     else if (P->compressor == ORC_RANDSEQK)
@@ -686,9 +700,17 @@ static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* 
     orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
     for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
         diff[t] = hbuf[t] - C->shift[t];
-    double frob_sq = orc_frob_sym(diff, d, lda);
-    C->lk = sqrt(frob_sq);                      /* Lk = ||diff||_F (TopK.h:74-78) */
+    return orc_frob_sym(diff, d, lda);
+}
 
+/* Worker side, second half: compression, message and shift update (TopK.h:80-129, TopLEK.h,
+ * RandK.h:86-162, Identical.h:80-94, Natural.h:79-147; the FedNL-PP workers are the same) */
+static void client_compress(orc_state* S, int32_t c, uint32_t* toplek_rng, const double* diff, double frob_sq)
+{
+    const orc_problem* P = &S->p;
+    orc_client* C = &S->clients[c];
+    int32_t d = P->d, lda = P->lda;
+    size_t U = S->U;
     double alpha = P->alpha, pre = S->prescale;
     int32_t k = S->k_eff;
 
@@ -751,6 +773,54 @@ static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* 
     }
 }
 
+/* FedNL: Lk = ||diff||_F before the update (TopK.h:74-78) */
+static void client_round(orc_state* S, int32_t c, uint32_t* toplek_rng, double* hbuf, double* diff,
+                         double* mtmp, double* stmp)
+{
+    double frob_sq = client_prepare(S, c, hbuf, diff, mtmp, stmp);
+    S->clients[c].lk = sqrt(frob_sq);
+    client_compress(S, c, toplek_rng, diff, frob_sq);
+}
+
+/* y = M x for a full d x lda matrix, columns swept in order (MatrixNMD::matrixVectorMultiply,
+ * MatrixNMD.h:1299-1325): y_i = ((0 + m_i0 x_0) + m_i1 x_1) + ... */
+static void matvec_cols(const double* m, int32_t d, int32_t lda, const double* x, double* y)
+{
+    for (int32_t i = 0; i < d; ++i)
+        y[i] = 0.0;
+    for (int32_t j = 0; j < d; ++j) {
+        double xj = x[j];
+        const double* col = m + (size_t)j * lda;
+        for (int32_t i = 0; i < d; ++i)
+            y[i] += col[i] * xj;
+    }
+}
+
+/* FedNL-PP worker (bin_fednl_local_pp/include/LocalWorkerForFedNL_*.h, e.g. RandSeqK.h:90-190):
+ * the same compression and shift update, then Lk = ||shift - H_i||_F after the update (sent as a
+ * difference) and the direction dir = x Lk + shift x - grad (sent as a difference). */
+static void client_round_pp(orc_state* S, int32_t c, uint32_t* toplek_rng, double* hbuf, double* diff,
+                            double* mtmp, double* stmp)
+{
+    const orc_problem* P = &S->p;
+    orc_client* C = &S->clients[c];
+    int32_t d = P->d, lda = P->lda;
+    size_t full = (size_t)d * (size_t)lda;
+    double frob_sq = client_prepare(S, c, hbuf, diff, mtmp, stmp);
+    client_compress(S, c, toplek_rng, diff, frob_sq);
+    for (size_t t = 0; t < full; ++t)
+        diff[t] = C->shift[t] - hbuf[t];
+    double lk_new = sqrt(orc_frob_sym(diff, d, lda));
+    C->dlk = lk_new - C->lk;
+    C->lk = lk_new;
+    matvec_cols(C->shift, d, lda, S->x, mtmp);
+    for (int32_t i = 0; i < d; ++i) {
+        double dir = (S->x[i] * C->lk + mtmp[i]) - C->grad[i];
+        C->ddir[i] = dir - C->dir[i];
+        C->dir[i] = dir;
+    }
+}
+
 typedef struct {
     orc_state* S;
     int32_t tid, nthreads;
@@ -762,7 +832,7 @@ static void* client_phase_thread(void* arg)
     orc_state* S = J->S;
     int32_t d = S->p.d, lda = S->p.lda;
     size_t full = (size_t)d * (size_t)lda;
-    int32_t nmax = 1;
+    int32_t nmax = d;                           /* the sample buffers also hold d-vectors */
     for (int32_t c = 0; c < S->p.n_clients; ++c)
         if (S->clients[c].n > nmax)
             nmax = S->clients[c].n;
@@ -774,8 +844,12 @@ static void* client_phase_thread(void* arg)
     /* logical workers w = tid, tid + nthreads, ...; each processes its clients c = w, w + W, ... in order
      * (static round-robin distribution, TrainLoop.h:664-686) */
     for (int32_t w = J->tid; w < W; w += J->nthreads)
-        for (int32_t c = w; c < S->p.n_clients; c += W)
-            client_round(S, c, &S->worker_rng[w], hbuf, diff, mtmp, stmp);
+        for (int32_t c = w; c < S->p.n_clients; c += W) {
+            if (!S->p.pp)
+                client_round(S, c, &S->worker_rng[w], hbuf, diff, mtmp, stmp);
+            else if (S->is_sel[c])                 /* clientHasBeenSelected, UsedTypes.h:169-182 */
+                client_round_pp(S, c, &S->worker_rng[w], hbuf, diff, mtmp, stmp);
+        }
     free(hbuf);
     free(diff);
     free(mtmp);
@@ -812,7 +886,7 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
 
     size_t msg_cap = S->U;
     size_t off = 0;
-    int32_t nmax = 1;
+    int32_t nmax = d;
     for (int32_t c = 0; c < nc; ++c)
         if (p->n_samples[c] > nmax)
             nmax = p->n_samples[c];
@@ -843,12 +917,44 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
         orc_hessian(C->atr, d, lda, n, stmp, p->lambda, C->shift);
         for (size_t t = 0; t < full; ++t)
             S->H[t] += C->shift[t];
+        if (p->pp) {
+            /* FedNL-PP init (bin_fednl_local_pp/.../LocalWorkerForFedNL_RandSeqK.h:22-31): Lk = 0,
+             * localGradient = shift x0 - grad(x0) */
+            C->dir = (double*)calloc((size_t)d, sizeof(double));
+            C->ddir = (double*)calloc((size_t)d, sizeof(double));
+            orc_gradient(C->atr, d, lda, n, S->x, stmp, p->lambda, C->grad);
+            matvec_cols(C->shift, d, lda, S->x, mtmp);
+            for (int32_t i = 0; i < d; ++i)
+                C->dir[i] = mtmp[i] - C->grad[i];
+            C->lk = 0.0;
+        }
     }
     free(mtmp);
     free(stmp);
     double inv_n = 1.0 / (double)nc;
     for (size_t t = 0; t < full; ++t)           /* H *= 1/n (TrainLoop.h:732-735) */
         S->H[t] *= inv_n;
+    if (p->pp) {
+        /* master (bin_fednl_local_pp/include/TrainLoop.h:1064-1080): H, g_prev and l_prev are the
+         * client means in client order */
+        S->g_prev = (double*)calloc((size_t)d, sizeof(double));
+        S->true_grad = (double*)calloc((size_t)d, sizeof(double));
+        for (int32_t c = 0; c < nc; ++c) {
+            for (int32_t i = 0; i < d; ++i)
+                S->g_prev[i] += S->clients[c].dir[i];
+            S->l_prev += S->clients[c].lk;
+        }
+        for (int32_t i = 0; i < d; ++i)
+            S->g_prev[i] *= inv_n;
+        S->l_prev *= inv_n;
+        S->tau = p->clients_per_round;
+        if (S->tau < 1 || S->tau > nc)
+            S->tau = nc;
+        S->sampler = p->client_seed;
+        S->perm = (uint32_t*)malloc((size_t)nc * sizeof(uint32_t));
+        S->is_sel = (uint8_t*)calloc((size_t)nc, 1);
+        S->selected = (int32_t*)malloc((size_t)S->tau * sizeof(int32_t));
+    }
     return S;
 }
 
@@ -863,7 +969,14 @@ void orc_destroy(orc_state* S)
         free(C->grad);
         free(C->msg_idx);
         free(C->msg_val);
+        free(C->dir);
+        free(C->ddir);
     }
+    free(S->g_prev);
+    free(S->true_grad);
+    free(S->perm);
+    free(S->is_sel);
+    free(S->selected);
     free(S->clients);
     free(S->upper);
     free(S->worker_rng);
@@ -874,11 +987,16 @@ void orc_destroy(orc_state* S)
     free(S);
 }
 
+static int orc_round_pp_master(orc_state* S, double* grad_norm);
+static void pp_select_and_track(orc_state* S);
+
 int orc_round(orc_state* S, double* grad_norm)
 {
     const orc_problem* P = &S->p;
     int32_t d = P->d, lda = P->lda, nc = P->n_clients;
     int32_t T = S->p.threads;
+    if (P->pp)
+        pp_select_and_track(S);
 
     /* client phase */
     pthread_t* th = (pthread_t*)malloc((size_t)T * sizeof(pthread_t));
@@ -898,6 +1016,8 @@ int orc_round(orc_state* S, double* grad_norm)
     }
     free(th);
     free(jobs);
+    if (P->pp)
+        return orc_round_pp_master(S, grad_norm);
 
     /* master phase, clients merged in order (TrainLoop.h:1092-1334 with forcesequpdate) */
     double inv_n = 1.0 / (double)nc;
@@ -933,6 +1053,107 @@ int orc_round(orc_state* S, double* grad_norm)
         *grad_norm = sqrt(gs);
     }
     return ok ? 0 : -1;
+}
+
+/* FedNL-PP round start (bin_fednl_local_pp/include/TrainLoop.h:1150-1166): the sampler shuffles a
+ * fresh 0..n-1 (partial, tau steps), then the true gradient is the mean of every client's gradient
+ * at the current iterate (computeFullGradient, :117-129: sum in client order, then / n). */
+static void pp_select_and_track(orc_state* S)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d, lda = P->lda, nc = P->n_clients;
+    for (int32_t c = 0; c < nc; ++c) {
+        S->perm[c] = (uint32_t)c;
+        S->is_sel[c] = 0;
+    }
+    orc_shuffle_partial(S->perm, (size_t)nc, (size_t)S->tau, &S->sampler);
+    for (int32_t t = 0; t < S->tau; ++t)
+        S->is_sel[S->perm[t]] = 1;
+    int32_t w = 0;
+    for (int32_t c = 0; c < nc; ++c)
+        if (S->is_sel[c])
+            S->selected[w++] = c;
+    int32_t nmax = 1;
+    for (int32_t c = 0; c < nc; ++c)
+        if (S->clients[c].n > nmax)
+            nmax = S->clients[c].n;
+    double* mtmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* stmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* gtmp = (double*)malloc((size_t)d * sizeof(double));
+    for (int32_t i = 0; i < d; ++i)
+        S->true_grad[i] = 0.0;
+    for (int32_t c = 0; c < nc; ++c) {
+        orc_client* C = &S->clients[c];
+        orc_margin(C->atr, d, lda, C->n, S->x, mtmp);
+        orc_sigmoid(mtmp, C->n, stmp);
+        orc_gradient(C->atr, d, lda, C->n, S->x, stmp, P->lambda, gtmp);
+        for (int32_t i = 0; i < d; ++i)
+            S->true_grad[i] += gtmp[i];
+    }
+    for (int32_t i = 0; i < d; ++i)
+        S->true_grad[i] /= (double)nc;
+    free(mtmp);
+    free(stmp);
+    free(gtmp);
+}
+
+/* FedNL-PP master (bin_fednl_local_pp/include/TrainLoop.h:1168-1560 with forcesequpdate): the
+ * selected clients' direction and Lk differences and Hessian messages are merged in client order;
+ * g = sum(ddir) / n + g_prev, l = sum(dLk) / n + l_prev; x = (H + l I)^-1 g by Cholesky. */
+static int orc_round_pp_master(orc_state* S, double* grad_norm)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d, lda = P->lda;
+    double inv_n = 1.0 / (double)P->n_clients;
+    for (int32_t i = 0; i < d; ++i)
+        S->g[i] = 0.0;
+    double l = 0.0;
+    for (int32_t t = 0; t < S->tau; ++t) {
+        orc_client* C = &S->clients[S->selected[t]];
+        for (int32_t i = 0; i < d; ++i)
+            S->g[i] += C->ddir[i];
+        for (int32_t q = 0; q < C->msg_count; ++q)
+            S->H[C->msg_idx[q]] += C->msg_val[q];
+        l += C->dlk;
+    }
+    for (int32_t i = 0; i < d; ++i) {
+        S->g[i] = S->g[i] * inv_n + S->g_prev[i];
+        S->g_prev[i] = S->g[i];
+    }
+    l = l * inv_n + S->l_prev;
+    S->l_prev = l;
+    S->l = l;
+    int ok = orc_cholesky(S->H, d, lda, l, S->ltr);
+    if (ok)
+        orc_solve_chol(S->ltr, d, lda, S->g, S->x);
+    if (grad_norm) {
+        double gs = 0.0;
+        for (int32_t i = 0; i < d; ++i)
+            gs += S->true_grad[i] * S->true_grad[i];
+        *grad_norm = sqrt(gs);
+    }
+    return ok ? 0 : -1;
+}
+
+void orc_get_true_grad(const orc_state* S, double* g)
+{
+    if (S->true_grad)
+        memcpy(g, S->true_grad, (size_t)S->p.d * sizeof(double));
+}
+int32_t orc_get_selected(const orc_state* S, int32_t* out)
+{
+    if (!S->selected)
+        return 0;
+    memcpy(out, S->selected, (size_t)S->tau * sizeof(int32_t));
+    return S->tau;
+}
+void orc_get_dir(const orc_state* S, int32_t c, double* dir, double* ddir)
+{
+    const orc_client* C = &S->clients[c];
+    if (C->dir && dir)
+        memcpy(dir, C->dir, (size_t)S->p.d * sizeof(double));
+    if (C->ddir && ddir)
+        memcpy(ddir, C->ddir, (size_t)S->p.d * sizeof(double));
 }
 
 void orc_get_x(const orc_state* S, double* x) { memcpy(x, S->x, (size_t)S->p.d * sizeof(double)); }

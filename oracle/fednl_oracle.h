@@ -44,6 +44,9 @@ typedef struct orc_problem {
     int32_t threads;           /* OS threads this oracle uses for the client phase (<= workers) */
     uint32_t seed_base;        /* RandK/RandSeqK client seed = seed_base + c (reference: 123) */
     uint32_t toplek_seed;      /* initial seed of each worker's TopLEK generator (reference: 1234) */
+    int32_t pp;                /* 1: FedNL-PP (dopt/bin_fednl_local_pp), 0: FedNL */
+    int32_t clients_per_round; /* FedNL-PP tau (--clients-per-round) */
+    uint32_t client_seed;      /* FedNL-PP client sampler seed (--client-selection-seed, reference: 1234) */
 } orc_problem;
 
 typedef struct orc_state orc_state;
@@ -100,6 +103,15 @@ void   orc_get_grad(const orc_state* s, double* g);
 int32_t orc_get_message(const orc_state* s, int32_t c, uint32_t* idx, double* val);
 /* last round's Lk of client c */
 double orc_get_lk(const orc_state* s, int32_t c);
+
+/* ---- FedNL-PP extras ------------------------------------------------------------------- */
+/* true gradient (mean of every client's gradient at the round's starting iterate; its norm is what
+ * orc_round returns in PP mode) */
+void   orc_get_true_grad(const orc_state* s, double* g);
+/* the round's sampled clients in ascending order; returns tau */
+int32_t orc_get_selected(const orc_state* s, int32_t* out);
+/* client c's running direction (x Lk + shift x - grad) and its last sent difference */
+void   orc_get_dir(const orc_state* s, int32_t c, double* dir, double* ddir);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,8 @@ class Problem(C.Structure):
                 ("labels", C.POINTER(C.c_double)), ("lambda_", C.c_double),
                 ("compressor", C.c_int32), ("k", C.c_int32), ("alpha", C.c_double),
                 ("workers", C.c_int32), ("threads", C.c_int32), ("seed_base", C.c_uint32),
-                ("toplek_seed", C.c_uint32)]
+                ("toplek_seed", C.c_uint32), ("pp", C.c_int32), ("clients_per_round", C.c_int32),
+                ("client_seed", C.c_uint32)]
 
 
 def build() -> str:
@@ -55,6 +56,10 @@ def lib():
         L.orc_get_l.argtypes = [C.c_void_p]
         L.orc_get_lk.restype = C.c_double
         L.orc_get_lk.argtypes = [C.c_void_p, C.c_int32]
+        L.orc_get_true_grad.argtypes = [C.c_void_p, dp]
+        L.orc_get_selected.restype = C.c_int32
+        L.orc_get_selected.argtypes = [C.c_void_p, ip]
+        L.orc_get_dir.argtypes = [C.c_void_p, C.c_int32, dp, dp]
         L.orc_get_message.restype = C.c_int32
         L.orc_get_message.argtypes = [C.c_void_p, C.c_int32, up, dp]
         L.orc_upper_indices.argtypes = [C.c_int32, C.c_int32, up]
@@ -144,7 +149,8 @@ class FedNL:
     """Whole FedNL run on the CPU oracle (master merges clients in order)."""
 
     def __init__(self, prob, compressor, k, alpha, lda=None, workers=1, threads=None,
-                 seed_base=123, toplek_seed=1234, x0=None):
+                 seed_base=123, toplek_seed=1234, x0=None, clients_per_round=None, client_seed=1234):
+        """clients_per_round set: FedNL-PP (bin_fednl_local_pp) with that many clients per round."""
         self.d = prob.d
         self.lda = lda if lda is not None else (prob.d + 3) // 4 * 4
         self._keep = [np.ascontiguousarray(prob.n_samples, dtype=np.int32),
@@ -154,7 +160,9 @@ class FedNL:
         p = Problem(self.d, self.lda, prob.n_clients,
                     self._keep[0].ctypes.data_as(C.POINTER(C.c_int32)),
                     _dp(self._keep[1]), _dp(self._keep[2]), prob.lam, comp, int(k), float(alpha),
-                    int(workers), int(threads if threads else workers), seed_base, toplek_seed)
+                    int(workers), int(threads if threads else workers), seed_base, toplek_seed,
+                    1 if clients_per_round else 0, int(clients_per_round or 0), client_seed)
+        self.pp = bool(clients_per_round)
         x0 = np.zeros(self.d) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
         self._h = lib().orc_create(C.byref(p), _dp(x0))
         self.n_clients = prob.n_clients
@@ -199,6 +207,21 @@ class FedNL:
 
     def l(self) -> float:
         return lib().orc_get_l(self._h)
+
+    def true_grad(self) -> np.ndarray:
+        out = np.empty(self.d)
+        lib().orc_get_true_grad(self._h, _dp(out))
+        return out
+
+    def selected(self) -> np.ndarray:
+        out = np.empty(self.n_clients, dtype=np.int32)
+        n = lib().orc_get_selected(self._h, out.ctypes.data_as(C.POINTER(C.c_int32)))
+        return out[:n].copy()
+
+    def dir(self, c: int):
+        dr, dd = np.empty(self.d), np.empty(self.d)
+        lib().orc_get_dir(self._h, c, _dp(dr), _dp(dd))
+        return dr, dd
 
     def lk(self, c: int) -> float:
         return lib().orc_get_lk(self._h, c)

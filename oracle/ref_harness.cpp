@@ -19,6 +19,7 @@
 #include "dopt/linalg_matrices/include/factorization/CholeskyFactorization.h"
 #include "dopt/linalg_linsolvers/include/ElementarySolvers.h"
 #include "dopt/random/include/RandomGenIntegerLinear.h"
+#include "dopt/random/include/Shuffle.h"
 #include "dopt/system/include/FloatUtils.h"
 
 #include <barrier>
@@ -54,7 +55,68 @@ struct Client {
     std::vector<uint32_t> idx;
     std::vector<double> val;
     dopt::RandomGenIntegerLinear rng;
+    Vec dir, ddir;          // FedNL-PP: localGradient and the last sent difference
+    double dlk = 0.0;       // FedNL-PP: the last sent Lk difference
 };
+
+// compression, message and shift update of one client (LocalWorkerForFedNL_{TopK,TopLEK,RandK,
+// RandSeqK,Identical,Natural}.h; the FedNL-PP workers are the same), on the reference's operators
+static void compress_client(Client& C, const Mat& diff, int32_t comp, int32_t k, size_t U,
+                            const std::vector<uint32_t>& upper, double alpha, double prescale, int32_t d)
+{
+    C.val.clear();
+    if (comp == kTopK || comp == kTopLEK) {
+        if (comp == kTopK) {
+            C.idx = dopt::getTopKFromUpperDiagonalPart<true>(diff, k, upper);
+        } else {
+            double delta = double(k) * (1.0 / double(U));
+            C.idx = dopt::getTopLEKFromUpperDiagonalPart<true>(diff, k, upper, delta);
+        }
+        for (uint32_t index : C.idx) {
+            double item = diff.matrixByCols.get(index);
+            C.val.push_back(item * prescale);
+            size_t ir = 0, jc = 0;
+            diff.getPositionFromFlatternIndex(ir, jc, index);
+            C.shift.matrixByCols[index] += alpha * item;
+            if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
+        }
+    } else if (comp == kRandK || comp == kRandSeqK) {
+        double mult = double(U) / double(k);
+        for (uint32_t index : C.idx) {
+            double item = diff.matrixByCols.get(index) * mult;
+            C.val.push_back(item * prescale);
+            size_t ir = 0, jc = 0;
+            diff.getPositionFromFlatternIndex(ir, jc, index);
+            C.shift.matrixByCols[index] += alpha * item;
+            if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
+        }
+    } else if (comp == kIdentity) {
+        C.idx = upper;
+        Mat sp = Mat::getZeroSquareMatrix(d);
+        for (int32_t j = 0; j < d; ++j)
+            for (int32_t i = 0; i <= j; ++i) {
+                double item = diff.get(i, j);
+                C.val.push_back(item * prescale);
+                sp.set(i, j, item);
+                sp.set(j, i, item);
+            }
+        C.shift += alpha * sp;
+    } else {  // natural: the master adds preScale * unpacked value
+        C.idx = upper;
+        Mat sp = diff;
+        sp.applyNaturalCompressor();
+        for (int32_t j = 0; j < d; ++j)
+            for (int32_t i = 0; i <= j; ++i) {
+                auto pa = dopt::getFloatPointPack<DOPT_ARCH_LITTLE_ENDIAN>(sp.get(i, j));
+                auto pb = pa;
+                uint32_t packed = dopt::pack2FP64NoMantissa(pa, pb);
+                dopt::FPComponentsPack<DOPT_ARCH_LITTLE_ENDIAN, double> un[2];
+                dopt::unpack2FP64NoMantissa(un, packed);
+                C.val.push_back(prescale * un[0].real_value_repr);
+            }
+        C.shift += alpha * sp;
+    }
+}
 
 // ---- run: whole FedNL (Option B) ---------------------------------------------------------
 static int cmd_run(const char* in_path, const char* out_path)
@@ -114,58 +176,7 @@ static int cmd_run(const char* in_path, const char* out_path)
         Mat hess = P->evaluateHessian(x, margin, sig);
         Mat diff = hess - C.shift;
         C.lk = diff.frobeniusNormForSymmetricMatrixFromUpPart();
-        C.val.clear();
-        if (comp == kTopK || comp == kTopLEK) {
-            if (comp == kTopK) {
-                C.idx = dopt::getTopKFromUpperDiagonalPart<true>(diff, k, upper);
-            } else {
-                double delta = double(k) * (1.0 / double(U));
-                C.idx = dopt::getTopLEKFromUpperDiagonalPart<true>(diff, k, upper, delta);
-            }
-            for (uint32_t index : C.idx) {
-                double item = diff.matrixByCols.get(index);
-                C.val.push_back(item * prescale);
-                size_t ir = 0, jc = 0;
-                diff.getPositionFromFlatternIndex(ir, jc, index);
-                C.shift.matrixByCols[index] += alpha * item;
-                if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
-            }
-        } else if (comp == kRandK || comp == kRandSeqK) {
-            double mult = double(U) / double(k);
-            for (uint32_t index : C.idx) {
-                double item = diff.matrixByCols.get(index) * mult;
-                C.val.push_back(item * prescale);
-                size_t ir = 0, jc = 0;
-                diff.getPositionFromFlatternIndex(ir, jc, index);
-                C.shift.matrixByCols[index] += alpha * item;
-                if (ir != jc) C.shift.matrixByCols[diff.getFlattenIndexFromPosition(jc, ir)] += alpha * item;
-            }
-        } else if (comp == kIdentity) {
-            C.idx = upper;
-            Mat sp = Mat::getZeroSquareMatrix(d);
-            for (int32_t j = 0; j < d; ++j)
-                for (int32_t i = 0; i <= j; ++i) {
-                    double item = diff.get(i, j);
-                    C.val.push_back(item * prescale);
-                    sp.set(i, j, item);
-                    sp.set(j, i, item);
-                }
-            C.shift += alpha * sp;
-        } else {  // natural: the master adds preScale * unpacked value
-            C.idx = upper;
-            Mat sp = diff;
-            sp.applyNaturalCompressor();
-            for (int32_t j = 0; j < d; ++j)
-                for (int32_t i = 0; i <= j; ++i) {
-                    auto pa = dopt::getFloatPointPack<DOPT_ARCH_LITTLE_ENDIAN>(sp.get(i, j));
-                    auto pb = pa;
-                    uint32_t packed = dopt::pack2FP64NoMantissa(pa, pb);
-                    dopt::FPComponentsPack<DOPT_ARCH_LITTLE_ENDIAN, double> un[2];
-                    dopt::unpack2FP64NoMantissa(un, packed);
-                    C.val.push_back(prescale * un[0].real_value_repr);
-                }
-            C.shift += alpha * sp;
-        }
+        compress_client(C, diff, comp, k, U, upper, alpha, prescale, d);
     };
 
     // persistent worker threads, clients round-robin c -> c mod W (TrainLoop.h:664-686)
@@ -222,6 +233,142 @@ static int cmd_run(const char* in_path, const char* out_path)
     stop = true;
     start_bar.arrive_and_wait();
     for (auto& t : th) t.join();
+    for (auto& c : cl) delete c.prob;
+    fclose(fi);
+    fclose(fo);
+    return 0;
+}
+
+// ---- pp: whole FedNL-PP (Option B), dopt/bin_fednl_local_pp -----------------------------
+// Workers: LocalWorkerForFedNL_*.h of bin_fednl_local_pp (selected clients only; Lk after the shift
+// update, sent as a difference; direction x Lk + shift x - grad, sent as a difference).  Master:
+// TrainLoop.h:1064-1080 (init means), :1150-1166 (sampler: partial shuffle of a fresh 0..n-1 with
+// the --client-selection-seed generator; true gradient), :1168-1450 (merge in client order with
+// forcesequpdate; g and l as running means), :1560-1600 (x = Cholesky solve).  Single-threaded:
+// one reference worker, so the TopLEK generator is the main thread's.
+static int cmd_pp(const char* in_path, const char* out_path)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    Reader R{fi};
+    Writer W{fo};
+    int32_t d = R.get<int32_t>(), nc = R.get<int32_t>(), comp = R.get<int32_t>(), k = R.get<int32_t>();
+    int32_t tau = R.get<int32_t>(), rounds = R.get<int32_t>(), dump_rounds = R.get<int32_t>();
+    uint32_t sel_seed = R.get<uint32_t>();
+    double lambda = R.get<double>(), alpha = R.get<double>();
+    std::vector<int32_t> ns(nc);
+    R.get(ns.data(), nc);
+    size_t S = 0;
+    for (int32_t c = 0; c < nc; ++c) S += ns[c];
+    std::vector<double> feat(S * d), lab(S);
+    R.get(feat.data(), feat.size());
+    R.get(lab.data(), lab.size());
+
+    size_t U = ((size_t)d * (d + 1)) / 2;
+    if (comp == kIdentity || comp == kNatural) k = (int32_t)U;
+    double inv_n = 1.0 / double(nc);
+    double prescale = inv_n * alpha;
+
+    Vec x(d);
+    Mat H = Mat::getZeroSquareMatrix(d);
+    Vec g_prev(d);
+    double l_prev = 0.0;
+    std::vector<Client> cl(nc);
+    size_t off = 0;
+    for (int32_t c = 0; c < nc; ++c) {
+        Mat xt(d, ns[c]);
+        Vec b(ns[c]);
+        for (int32_t s = 0; s < ns[c]; ++s) {
+            for (int32_t i = 0; i < d; ++i) xt.set(i, s, feat[(off + s) * d + i]);
+            b.set(s, lab[off + s]);
+        }
+        off += ns[c];
+        cl[c].prob = new Problem(xt, b, lambda);
+        cl[c].rng.setSeed(uint32_t(123 + c));
+        cl[c].shift = cl[c].prob->evaluateHessian(x);
+        cl[c].lk = 0.0;
+        cl[c].dir = Mat::matrixVectorMultiply(cl[c].shift, x) - cl[c].prob->evaluateGradient(x);
+        H += cl[c].shift;
+        g_prev += cl[c].dir;
+        l_prev += cl[c].lk;
+    }
+    H *= inv_n;
+    g_prev *= inv_n;
+    l_prev *= inv_n;
+    std::vector<uint32_t> upper = dopt::indiciesForUpperTriangularPart(H);
+    W.put<int32_t>((int32_t)H.LDA);
+
+    dopt::RandomGenIntegerLinear sampler;
+    sampler.setSeed(sel_seed);
+    std::vector<uint32_t> all(nc);
+    for (int32_t c = 0; c < nc; ++c) all[c] = (uint32_t)c;
+    std::vector<char> is_sel(nc);
+    Mat Ltr;
+    for (int32_t r = 0; r < rounds; ++r) {
+        std::vector<uint32_t> selv = all;
+        dopt::shuffle(selv, (size_t)tau, sampler);
+        std::fill(is_sel.begin(), is_sel.end(), 0);
+        for (int32_t t = 0; t < tau; ++t) is_sel[selv[t]] = 1;
+        Vec tg(d);
+        for (int32_t c = 0; c < nc; ++c) tg += cl[c].prob->evaluateGradient(x);
+        tg = tg / double(nc);
+        for (int32_t c = 0; c < nc; ++c) {
+            if (!is_sel[c]) continue;
+            Client& C = cl[c];
+            Problem* P = C.prob;
+            if (comp == kRandK)
+                C.idx = dopt::generateRandKItemsInUpperTriangularPart(C.rng, k, C.shift, upper);
+            else if (comp == kRandSeqK)
+                C.idx = dopt::generateRandSeqKItemsInUpperTriangularPart(C.rng, k, C.shift, upper);
+            Vec margin = P->evaluateClassificationMargin(x);
+            Vec sig = P->evaluateClassificationMarginSigmoid(margin);
+            Mat hess = P->evaluateHessian(x, margin, sig);
+            Mat diff = hess - C.shift;
+            compress_client(C, diff, comp, k, U, upper, alpha, prescale, d);
+            double lk_new = (C.shift - hess).frobeniusNormForSymmetricMatrixFromUpPart();
+            C.dlk = lk_new - C.lk;
+            C.lk = lk_new;
+            Vec dir = (x * C.lk) + Mat::matrixVectorMultiply(C.shift, x) - P->evaluateGradient(x, margin, sig);
+            C.ddir = dir - C.dir;
+            C.dir = dir;
+        }
+        Vec g(d);
+        double l = 0.0;
+        for (int32_t c = 0; c < nc; ++c) {
+            if (!is_sel[c]) continue;
+            g += cl[c].ddir;
+            for (size_t t = 0; t < cl[c].idx.size(); ++t) H.matrixByCols[cl[c].idx[t]] += cl[c].val[t];
+            l += cl[c].dlk;
+        }
+        g *= inv_n;
+        g += g_prev;
+        g_prev = g;
+        l *= inv_n;
+        l += l_prev;
+        l_prev = l;
+        bool ok = dopt::cholFactorization::choleskyFactorization<Mat, true, true>(Ltr, H, l);
+        if (ok) {
+            Vec y = dopt::forwardSubstitutionWithATranspose(Ltr, g);
+            x = dopt::backwardSubstitutionWithATranspose(Ltr, y);
+        }
+        W.put<int32_t>(ok ? 1 : 0);
+        W.put<double>(tg.vectorL2Norm());
+        W.put<double>(l);
+        W.put(x.dataConst(), (size_t)d);
+        for (int32_t c = 0; c < nc; ++c)
+            if (is_sel[c]) W.put<int32_t>(c);
+        if (r < dump_rounds) {
+            for (int32_t c = 0; c < nc; ++c) {
+                if (!is_sel[c]) continue;
+                W.put<int32_t>((int32_t)cl[c].idx.size());
+                W.put(cl[c].idx.data(), cl[c].idx.size());
+                W.put(cl[c].val.data(), cl[c].val.size());
+                W.put<double>(cl[c].lk);
+                W.put(cl[c].dir.dataConst(), (size_t)d);
+            }
+        }
+    }
     for (auto& c : cl) delete c.prob;
     fclose(fi);
     fclose(fo);
@@ -316,6 +463,7 @@ int main(int argc, char** argv)
         return 2;
     }
     if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3]);
+    if (!strcmp(argv[1], "pp")) return cmd_pp(argv[2], argv[3]);
     if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
     if (!strcmp(argv[1], "toplek")) return cmd_select(argv[2], argv[3], true);
     if (!strcmp(argv[1], "chol")) return cmd_chol(argv[2], argv[3]);

@@ -6,6 +6,9 @@ box).  Each fixture stores seeded inputs and the reference's outputs:
 
 * ``run_<name>.npz``   whole FedNL runs (Option B, clients merged in order): per-round iterate,
   ||g||, l and, for the first rounds, every client's message (indices and values) and Lk;
+* ``pp_<name>.npz``    whole FedNL-PP runs (bin_fednl_local_pp, Option B): per-round iterate,
+  ||true gradient||, l, sampled clients and, for the first rounds, each sampled client's message,
+  Lk and direction;
 * ``select_<name>.npz`` TopK / TopLEK index sets on given matrices (ties included);
 * ``rand_<name>.npz``   RandK / RandSeqK index draws of one client generator;
 * ``chol.npz``          Option-B Cholesky solves.
@@ -30,9 +33,16 @@ from ufednl_gb300 import datagen  # noqa: E402
 
 COMP = {"identity": 0, "randk": 1, "topk": 2, "randseqk": 3, "toplek": 4, "natural": 5}
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
+ONLY = None     # --only: fixture kind prefix to regenerate
+
+
+def _skip(kind):
+    return ONLY is not None and not kind.startswith(ONLY)
 
 
 def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
+    if _skip("run"):
+        return
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
@@ -79,7 +89,60 @@ def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
         lk=np.array(lks))
 
 
+def pp_case(name, prob, comp, k, alpha, tau, rounds, dump_rounds, sel_seed=1234):
+    if _skip("pp"):
+        return
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([prob.d, prob.n_clients, COMP[comp], k, tau, rounds, dump_rounds], dtype="<i4").tofile(f)
+            np.array([sel_seed], dtype="<u4").tofile(f)
+            np.array([prob.lam, alpha], dtype="<f8").tofile(f)
+            prob.n_samples.astype("<i4").tofile(f)
+            prob.features.astype("<f8").tofile(f)
+            prob.labels.astype("<f8").tofile(f)
+        subprocess.run([HARNESS, "pp", fin, fout], check=True)
+        raw = open(fout, "rb").read()
+    pos = 0
+
+    def take(dt, n):
+        nonlocal pos
+        a = np.frombuffer(raw, dtype=dt, count=n, offset=pos)
+        pos += a.nbytes
+        return a.copy()
+
+    lda = int(take("<i4", 1)[0])
+    d = prob.d
+    ok, gnorm, lval, xs, sels = [], [], [], [], []
+    msg_idx, msg_val, lks, msg_cnt, dirs = [], [], [], [], []
+    for r in range(rounds):
+        ok.append(int(take("<i4", 1)[0]))
+        gnorm.append(float(take("<f8", 1)[0]))
+        lval.append(float(take("<f8", 1)[0]))
+        xs.append(take("<f8", d))
+        sels.append(take("<i4", tau))
+        if r < dump_rounds:
+            for _ in range(tau):
+                cnt = int(take("<i4", 1)[0])
+                msg_cnt.append(cnt)
+                msg_idx.append(take("<u4", cnt))
+                msg_val.append(take("<f8", cnt))
+                lks.append(float(take("<f8", 1)[0]))
+                dirs.append(take("<f8", d))
+    assert pos == len(raw)
+    np.savez_compressed(
+        os.path.join(HERE, f"pp_{name}.npz"),
+        d=d, lda=lda, n_samples=prob.n_samples, features=prob.features, labels=prob.labels,
+        lam=prob.lam, compressor=comp, k=k, alpha=alpha, tau=tau, sel_seed=sel_seed, rounds=rounds,
+        dump_rounds=dump_rounds, ok=np.array(ok), gnorm=np.array(gnorm), l=np.array(lval),
+        x=np.array(xs), selected=np.array(sels), msg_count=np.array(msg_cnt, dtype=np.int32),
+        msg_idx=np.concatenate(msg_idx).astype(np.uint32), msg_val=np.concatenate(msg_val),
+        lk=np.array(lks), dir=np.array(dirs))
+
+
 def select_case(name, mats, d, k, lek):
+    if _skip("select"):
+        return
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
@@ -103,6 +166,8 @@ def select_case(name, mats, d, k, lek):
 
 
 def rand_case(name, d, k, seed, draws, seq):
+    if _skip("rand"):
+        return
     with tempfile.TemporaryDirectory() as td:
         fout = os.path.join(td, "out.bin")
         subprocess.run([HARNESS, "randseqk" if seq else "randk", fout, str(d), str(k), str(seed),
@@ -115,6 +180,8 @@ def rand_case(name, d, k, seed, draws, seq):
 
 
 def chol_cases(rng):
+    if _skip("chol"):
+        return
     outs = []
     with tempfile.TemporaryDirectory() as td:
         for d, l in ((9, 0.1), (33, 1e-3), (70, 0.0)):
@@ -152,7 +219,10 @@ def tie_matrices(rng, d, count, levels):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", default=os.environ.get("REF_ROOT", "/root/reference/dopt"))
+    ap.add_argument("--only", default=None, help="regenerate only fixtures whose kind starts with this (run, pp, ...)")
     args = ap.parse_args()
+    global ONLY
+    ONLY = args.only
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_ROOT={args.ref_root}"],
                    check=True)
     rng = np.random.default_rng(20241203)
@@ -171,6 +241,19 @@ def main():
     run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 60, 3)
     dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
     run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
+
+    # FedNL-PP runs: uneven-free small federation (the reference's PP binary splits evenly), every
+    # compressor; a phishing-shaped case (d = 69, n_i = 6)
+    ppsmall = datagen.binary_problem(21, 13, [8] * 24, 0.45, 1e-3)
+    pp_case("randseqk_d13", ppsmall, "randseqk", 13, 13 / U, 6, 20, 3)
+    pp_case("randk_d13", ppsmall, "randk", 26, 26 / U, 6, 12, 2)
+    pp_case("natural_d13", ppsmall, "natural", U, 1.0 / (1.0 + 1.0 / 8.0), 6, 12, 2)
+    pp_case("identity_d13", ppsmall, "identity", U, 1.0, 6, 8, 2)
+    pp_case("topk_d13", ppsmall, "topk", 26, 1.0, 6, 10, 2)
+    pp_case("toplek_d13", ppsmall, "toplek", 39, 1.0, 6, 10, 2)
+    ppphish = datagen.binary_problem(3, 69, [6] * 64, 0.45, 1e-3)
+    pp_case("randseqk_d69", ppphish, "randseqk", 69, 69 / (69 * 70 // 2), 8, 10, 2)
+    pp_case("natural_d69", ppphish, "natural", 69 * 70 // 2, 1.0 / (1.0 + 1.0 / 8.0), 8, 6, 1)
 
     # selections on tie-heavy and continuous matrices (one OS thread => one TopLEK stream)
     ties = tie_matrices(rng, 12, 12, 3)

@@ -14,6 +14,7 @@ from ufednl_gb300 import datagen
 RUNS = sorted(glob.glob(golden_path("run_*.npz")))
 SELECTS = sorted(glob.glob(golden_path("select_*.npz")))
 RANDS = sorted(glob.glob(golden_path("rand_*.npz")))
+PPS = sorted(glob.glob(golden_path("pp_*.npz")))
 
 
 def _problem(z):
@@ -84,6 +85,48 @@ def test_run_matches_reference(oracle, path):
     fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
                        workers=int(z["workers"]))
     check_run_against_reference(fed, z, prob)
+    fed.close()
+
+
+def check_pp_against_reference(fed, z, prob):
+    """Shared contract of a whole FedNL-PP run against the reference's golden run: the sampled
+    clients of every round are identical; every sampled client's message indices are bit-exact
+    and its values, Lk and direction agree to 1e-12 / 1e-10; iterates, l and ||true gradient||
+    agree to 1e-10 / 1e-8 every round.  The golden PP runs are short and none of them reaches a
+    heap near-tie, so TopK / TopLEK are held to the same contract."""
+    rounds, dump = int(z["rounds"]), int(z["dump_rounds"])
+    pos = mi = 0
+    for r in range(rounds):
+        g = fed.round()
+        sel = fed.selected()
+        np.testing.assert_array_equal(sel, z["selected"][r])
+        xr = z["x"][r]
+        np.testing.assert_allclose(fed.x(), xr, rtol=1e-10, atol=1e-10 * np.max(np.abs(xr)))
+        assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r]
+        assert abs(fed.l() - z["l"][r]) <= 1e-10 * abs(z["l"][r]) + 1e-14
+        if r < dump:
+            for c in sel:
+                c = int(c)
+                cnt = int(z["msg_count"][mi])
+                idx, val = fed.message(c)
+                ref_v = z["msg_val"][pos:pos + cnt]
+                np.testing.assert_array_equal(idx, z["msg_idx"][pos:pos + cnt])
+                if cnt:
+                    np.testing.assert_allclose(val, ref_v, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref_v)))
+                assert abs(fed.lk(c) - z["lk"][mi]) <= 1e-10 * z["lk"][mi] + 1e-14
+                dref = z["dir"][mi]
+                np.testing.assert_allclose(fed.dir(c)[0], dref, rtol=1e-10, atol=1e-10 * np.max(np.abs(dref)))
+                pos += cnt
+                mi += 1
+
+
+@pytest.mark.parametrize("path", PPS, ids=lambda p: os.path.basename(p))
+def test_pp_run_matches_reference(oracle, path):
+    z = np.load(path)
+    prob = _problem(z)
+    fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
+                       workers=1, clients_per_round=int(z["tau"]), client_seed=int(z["sel_seed"]))
+    check_pp_against_reference(fed, z, prob)
     fed.close()
 
 
