@@ -65,14 +65,20 @@ typedef struct fednl_problem_desc {
     uint32_t seed_base;         /* RandK / RandSeqK client seed = seed_base + c (reference: 123) */
     uint32_t toplek_seed;       /* initial state of each worker's TopLEK generator (reference: 1234) */
     int32_t feature_format;     /* fednl_feature_format */
-    int32_t reserved[4];        /* must be zero */
+    /* FedNL-PP (dopt/bin_fednl_local_pp, TrainLoop.h:279-287): clients_per_round > 0 selects the
+     * partial-participation algorithm with that many sampled clients per round (--clients-per-round);
+     * 0 = plain FedNL (bin_fednl_local) */
+    int32_t clients_per_round;
+    uint32_t client_seed;       /* FedNL-PP sampler seed (--client-selection-seed, reference: 1234) */
+    int32_t reserved[2];        /* must be zero */
 } fednl_problem_desc;
 
 typedef struct fednl_round_stats {
     int32_t round;              /* index of the round just completed */
     int32_t status;             /* FEDNL_OK or FEDNL_ENOTPD for this round */
-    double grad_norm;           /* ||g|| of the aggregated gradient at the round's starting iterate */
-    double l;                   /* Option-B regulariser l = mean_i Lk_i */
+    double grad_norm;           /* ||g|| of the aggregated gradient at the round's starting iterate
+                                   (FedNL-PP: of the true gradient over all clients, TrainLoop.h:1166) */
+    double l;                   /* Option-B regulariser l = mean_i Lk_i (FedNL-PP: running mean) */
 } fednl_round_stats;
 
 typedef struct fednl_handle_s* fednl_handle;
@@ -111,6 +117,15 @@ double fednl_gpu_get_lk(fednl_handle h, int32_t client);
 /* Last round's message of a client, exactly as the reference master adds it to H:
  * flat indices (ascending, except RandSeqK's window order) and values. */
 int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double* val, int32_t* count);
+
+/* FedNL-PP readback (bin_fednl_local_pp): the last round's sampled clients in ascending order
+ * (clientHasBeenSelected, UsedTypes.h:169-182; *count = tau), the true gradient at the round's
+ * starting iterate (computeFullGradient, TrainLoop.h:117-129) and a client's running direction
+ * x Lk + shift x - grad with its last sent difference (LocalWorkerForFedNL_*.h "gradient like
+ * direction").  EINVAL on a handle without FedNL-PP. */
+int fednl_gpu_get_selected(fednl_handle h, int32_t* clients, int32_t* count);
+int fednl_gpu_get_true_grad(fednl_handle h, double* g);                    /* [d] */
+int fednl_gpu_get_dir(fednl_handle h, int32_t client, double* dir, double* ddir);   /* [d] each */
 
 /* ---- operator-level entry points (host buffers in, host buffers out) ----------------------- */
 

@@ -1057,7 +1057,10 @@ int orc_round(orc_state* S, double* grad_norm)
 
 /* FedNL-PP round start (bin_fednl_local_pp/include/TrainLoop.h:1150-1166): the sampler shuffles a
  * fresh 0..n-1 (partial, tau steps), then the true gradient is the mean of every client's gradient
- * at the current iterate (computeFullGradient, :117-129: sum in client order, then / n). */
+ * at the current iterate (computeFullGradient, :117-129: sum over clients, then / n).  The client
+ * sum is restated in a fixed blocked order shared with the GPU: in-order sums over blocks of 32
+ * consecutive clients, then the block sums in order (a few ulps from the reference's running sum;
+ * the value is only reported). */
 static void pp_select_and_track(orc_state* S)
 {
     const orc_problem* P = &S->p;
@@ -1080,6 +1083,7 @@ static void pp_select_and_track(orc_state* S)
     double* mtmp = (double*)malloc((size_t)nmax * sizeof(double));
     double* stmp = (double*)malloc((size_t)nmax * sizeof(double));
     double* gtmp = (double*)malloc((size_t)d * sizeof(double));
+    double* bsum = (double*)calloc((size_t)d, sizeof(double));
     for (int32_t i = 0; i < d; ++i)
         S->true_grad[i] = 0.0;
     for (int32_t c = 0; c < nc; ++c) {
@@ -1088,10 +1092,14 @@ static void pp_select_and_track(orc_state* S)
         orc_sigmoid(mtmp, C->n, stmp);
         orc_gradient(C->atr, d, lda, C->n, S->x, stmp, P->lambda, gtmp);
         for (int32_t i = 0; i < d; ++i)
-            S->true_grad[i] += gtmp[i];
+            bsum[i] = (c % 32 == 0) ? gtmp[i] : bsum[i] + gtmp[i];
+        if (c % 32 == 31 || c == nc - 1)
+            for (int32_t i = 0; i < d; ++i)
+                S->true_grad[i] = (c < 32) ? bsum[i] : S->true_grad[i] + bsum[i];
     }
     for (int32_t i = 0; i < d; ++i)
         S->true_grad[i] /= (double)nc;
+    free(bsum);
     free(mtmp);
     free(stmp);
     free(gtmp);

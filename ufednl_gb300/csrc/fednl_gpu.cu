@@ -127,6 +127,7 @@ struct fednl_handle_s {
     std::vector<int32_t> ns, soff;
     int d = 0, lda = 0, U = 0, ustr = 0, nc = 0, k = 0, comp = 0, W = 1, SW = 0, S = 0;
     int binary = 0, maxn = 0, nfpart = 0, nseg = 0, hcap = 0;
+    int pp = 0, tau = 0, pp_smem_perm = 0;   // FedNL-PP: clients per round, sampler in shared memory
     bool data_ready = false, shifts_ready = false;
     cudaStream_t stream = nullptr;
     Arena state, feat;
@@ -169,6 +170,12 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     Dev& P = h->dev;
     cudaStream_t st = h->stream;
     int S = h->S;
+    if (h->pp) {
+        MARK("k_pp_sample");
+        k_pp_sample<<<1, kPPThreads, h->pp_smem_perm ? (size_t)h->nc * 4 : 0, st>>>(
+            h->nc, h->tau, P.sampler, P.perm, (int*)P.act, P.is_sel, P.needs, h->pp_smem_perm);
+        CKL();
+    }
     MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
     if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
@@ -178,25 +185,35 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, st>>>(P);
     else k_grad_dense<<<gg, 128, 0, st>>>(P);
     CKL();
+    const int na = P.n_act;
+    if (h->pp) {
+        MARK("k_pp_truegrad");
+        k_pp_truegrad<<<(h->d + 3) / 4, 128, 0, st>>>(P);
+        CKL();
+        MARK("k_pp_norm");
+        k_pp_norm<<<1, 32, 0, st>>>(P);
+        CKL();
+    }
     MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
-    dim3 hg(h->nfpart, h->nc);
+    dim3 hg(h->nfpart, na);
+    const int hmode = h->pp ? 2 : 0;
     if (h->binary) {
-        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, 0);
-        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, 0);
+        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, hmode);
+        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, hmode);
     } else {
-        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, 0);
+        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, hmode);
     }
     CKL();
     MARK("k_fsum");
-    k_fsum<<<(h->nc + 3) / 4, 128, 0, st>>>(P);
+    k_fsum<<<(na + 3) / 4, 128, 0, st>>>(P);
     CKL();
     int comp = h->comp;
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
         MARK("k_select");
         double delta = (double)h->k * (1.0 / (double)h->U);
-        k_select<<<h->nc, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
+        k_select<<<na, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
             P.diff, h->ustr, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F, P.sel, h->SW, P.cnt, P.needs, P.pdraw,
-            P.minidx, P.status);
+            P.minidx, P.status, P.act);
         CKL();
         if (comp == FEDNL_TOPLEK) {
             MARK("k_toplek_rng");
@@ -206,16 +223,31 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
         }
     } else if (comp == FEDNL_RANDK) {
         MARK("k_randk");
-        k_randk<<<h->nc, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.hmap, h->hcap, P.sel, h->SW, P.cnt);
+        k_randk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.hmap, h->hcap, P.sel, h->SW, P.cnt, P.act);
         CKL();
     } else if (comp == FEDNL_RANDSEQK) {
         MARK("k_randseqk");
-        k_randseqk<<<h->nc, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt);
+        k_randseqk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt, P.act);
         CKL();
     }
     MARK("k_apply");
     k_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     CKL();
+    if (h->pp) {
+        MARK("k_pp_lkpart");
+        k_pp_lkpart<<<dim3(h->nfpart, na), kHessThreads, 0, st>>>(P);
+        CKL();
+        MARK("k_pp_dir");
+        k_pp_dir<<<na, 128, 0, st>>>(P);
+        CKL();
+        MARK("k_pp_aggregate");
+        k_pp_aggregate<<<(h->d + 127) / 128, 128, 0, st>>>(P);
+        CKL();
+        MARK("k_chol_coop");     // x = (H + l I)^-1 g (bin_fednl_local_pp TrainLoop.h:1560-1600)
+        CK(launch_chol(P, h->chol_grid, st, P.H, 0, P.stats + 1, 0.0, P.g, P.x, nullptr, 0));
+        MARK("end");
+        return FEDNL_OK;
+    }
     MARK("k_aggregate");
     k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads, kAggThreads, 0, st>>>(P);
     CKL();
@@ -258,8 +290,10 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     const fednl_problem_desc& D = *desc;
     if (D.d < 1 || D.n_clients < 1 || !D.n_samples) return fail(FEDNL_EINVAL, "d and n_clients must be >= 1");
     if (D.compressor < 0 || D.compressor > 5) return fail(FEDNL_EINVAL, "unknown compressor %d", D.compressor);
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
         if (D.reserved[i]) return fail(FEDNL_EINVAL, "reserved fields must be zero");
+    if (D.clients_per_round < 0 || D.clients_per_round > D.n_clients)
+        return fail(FEDNL_EINVAL, "clients_per_round %d outside [0, n_clients]", D.clients_per_round);
     int lda = D.lda ? D.lda : (D.d + 3) / 4 * 4;
     if (lda < D.d) return fail(FEDNL_EINVAL, "lda %d < d %d", lda, D.d);
     long long U = (long long)D.d * (D.d + 1) / 2;
@@ -296,6 +330,9 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     h->S = h->soff[h->nc];
     h->nfpart = (h->U + kHessPerBlock - 1) / kHessPerBlock;
     h->nseg = (h->U + 511) / 512;
+    h->pp = D.clients_per_round > 0;
+    h->tau = h->pp ? D.clients_per_round : h->nc;
+    h->pp_smem_perm = h->pp && (size_t)h->nc * 4 <= 48 * 1024;
     h->hcap = 1;
     if (h->comp == FEDNL_RANDK)
         while (h->hcap < 4 * k) h->hcap <<= 1;
@@ -323,6 +360,8 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.prescale = P.inv_n * D.alpha;                          // TrainLoop.h:531
     P.mult = (double)h->U / (double)h->k;                    // RandK.h:90
     P.hist_cap = 1 << 16;
+    P.pp = h->pp;
+    P.n_act = h->tau;
     size_t ncU = (size_t)h->nc * h->ustr;
     Arena& A = h->state;
     A.want((int**)&P.ns, h->nc);
@@ -358,6 +397,19 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.status, 1);
     A.want(&P.stats, 2);
     A.want(&P.bar, 4);
+    if (h->pp) {
+        A.want((int**)&P.act, h->nc);
+        A.want(&P.is_sel, h->nc);
+        A.want(&P.perm, h->nc);
+        A.want(&P.sampler, 1);
+        A.want(&P.hbuf, ncU);
+        A.want(&P.dir, (size_t)h->nc * h->d);
+        A.want(&P.ddir, (size_t)h->nc * h->d);
+        A.want(&P.dlk, h->nc);
+        A.want(&P.gprev, h->d);
+        A.want(&P.lprev, 1);
+        A.want(&P.tg, h->d);
+    }
     rc = A.commit();
     if (rc) {
         cudaStreamDestroy(h->stream);
@@ -524,15 +576,31 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
         CKL();
     }
     dim3 hg(h->nfpart, h->nc);
+    Dev Pall = P;             // every client's initial shift, whatever a round processes
+    Pall.act = nullptr;
+    Pall.n_act = h->nc;
     if (h->binary) {
-        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, 1);
-        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, 1);
+        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(Pall, 1);
+        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(Pall, 1);
     } else {
-        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, 1);
+        k_hess_dense<<<hg, kHessThreads, 0, st>>>(Pall, 1);
     }
     CKL();
     k_h_init<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     CKL();
+    if (h->pp) {
+        if (!h->binary) {
+            k_grad_dense<<<dim3((h->d + 127) / 128, h->nc), 128, 0, st>>>(P);
+            CKL();
+        }
+        k_pp_init_dir<<<h->nc, 128, 0, st>>>(P);
+        CKL();
+        k_pp_init_mean<<<(h->d + 127) / 128, 128, 0, st>>>(P);
+        CKL();
+        const unsigned seed = h->desc.client_seed;
+        CK(cudaMemcpyAsync(P.sampler, &seed, 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(P.stats, 0, 16, st));
+    }
     std::vector<unsigned> ws(h->W, h->desc.toplek_seed), rs(h->nc);
     for (int c = 0; c < h->nc; ++c) rs[c] = h->desc.seed_base + (unsigned)c;   // TrainLoop.h:632
     CK(cudaMemcpyAsync(P.wstate, ws.data(), h->W * 4, cudaMemcpyHostToDevice, st));
@@ -582,6 +650,35 @@ int fednl_gpu_round(fednl_handle h, fednl_round_stats* stats)
         stats->l = st[1];
     }
     return rc;
+}
+
+int fednl_gpu_get_selected(fednl_handle h, int32_t* clients, int32_t* count)
+{
+    if (!h || !count) return fail(FEDNL_EINVAL, "null argument");
+    if (!h->pp) return fail(FEDNL_EINVAL, "handle without FedNL-PP");
+    CK(cudaStreamSynchronize(h->stream));
+    *count = h->tau;
+    if (clients) CK(cudaMemcpy(clients, h->dev.act, (size_t)h->tau * 4, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_true_grad(fednl_handle h, double* g)
+{
+    if (!h || !g) return fail(FEDNL_EINVAL, "null argument");
+    if (!h->pp) return fail(FEDNL_EINVAL, "handle without FedNL-PP");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(g, h->dev.tg, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_dir(fednl_handle h, int32_t client, double* dir, double* ddir)
+{
+    if (!h || client < 0 || client >= h->nc) return fail(FEDNL_EINVAL, "bad argument");
+    if (!h->pp) return fail(FEDNL_EINVAL, "handle without FedNL-PP");
+    CK(cudaStreamSynchronize(h->stream));
+    if (dir) CK(cudaMemcpy(dir, h->dev.dir + (size_t)client * h->d, h->d * 8, cudaMemcpyDeviceToHost));
+    if (ddir) CK(cudaMemcpy(ddir, h->dev.ddir + (size_t)client * h->d, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
 }
 
 int fednl_gpu_get_x(fednl_handle h, double* x)
@@ -765,7 +862,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
         CK(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(k)));
     double delta = (double)k * (1.0 / (double)U);
     k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)ustr, (int)U, k, lek ? 1 : 0, delta,
-                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr);
+                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr);
     CKL();
     if (lek) {
         int W = std::max(1, n_workers);
@@ -823,8 +920,8 @@ int rand_common(uint32_t* states, int n_gen, int d, int lda, int k, uint32_t* id
     rc = s.a.commit();
     if (rc) return rc;
     CK(cudaMemcpyAsync(dst, states, n_gen * 4, cudaMemcpyHostToDevice, s.st));
-    if (seq) k_randseqk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, drseq, dsel, SW, dcnt);
-    else k_randk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, dmap, hcap, dsel, SW, dcnt);
+    if (seq) k_randseqk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, drseq, dsel, SW, dcnt, nullptr);
+    else k_randk<<<n_gen, 256, 0, s.st>>>(dst, n_gen, (int)U, k, dmap, hcap, dsel, SW, dcnt, nullptr);
     CKL();
     std::vector<unsigned> sel((size_t)n_gen * SW);
     std::vector<int> rseq(n_gen);

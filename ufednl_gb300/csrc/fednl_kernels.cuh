@@ -73,6 +73,19 @@ struct Dev {
     double* stats;          // [2] ||g||, l
     int hist_cap;
     unsigned* bar;          // [4] grid barrier: arrival count, generation, error flag
+    // FedNL-PP (bin_fednl_local_pp); act == nullptr: every client takes part (plain FedNL)
+    int pp, n_act;          // n_act: clients processed this round (tau, or nc without PP)
+    const int* act;         // [n_act] processed clients in ascending order
+    int* is_sel;            // [nc]
+    int* perm;              // [nc] the sampler's permutation (when it does not fit in shared memory)
+    unsigned* sampler;      // [1] client sampler (RandomGenIntegerLinear)
+    double* hbuf;           // [nc][ustr] the round's client Hessians (Lk after the update)
+    double* dir;            // [nc][d] localGradient = x Lk + shift x - grad
+    double* ddir;           // [nc][d] its last sent difference
+    double* dlk;            // [nc] last sent Lk difference
+    double* gprev;          // [d] running mean of the directions
+    double* lprev;          // [1] running mean of Lk
+    double* tg;             // [d] true gradient at the round's starting iterate
 };
 
 // ---- helpers -------------------------------------------------------------------------------
@@ -310,7 +323,9 @@ __global__ void k_grad_dense(Dev P)
 // in order of u_i (D_s u_j); for {0,1} features every nonzero term equals D_s exactly, so the
 // entry is the in-order sum of D_s over the samples where both attributes are set (bitmask
 // AND).  Then + lambda on the diagonal.  mode 0: diff = H_i - shift_i (TopK.h:70-71) and the
-// partial sums of ||diff||_F^2 over the full symmetric matrix; mode 1: shift_i = H_i(x0).
+// partial sums of ||diff||_F^2 over the full symmetric matrix; mode 1: shift_i = H_i(x0); mode 2
+// (FedNL-PP): mode 0 and H_i kept for the Lk taken after the shift update.  Grid y runs over the
+// processed clients (P.act).
 constexpr int kHessThreads = 256;
 constexpr int kHessPerBlock = 4096;     // upper entries per block
 
@@ -323,7 +338,7 @@ template <bool SMEM_BITS>
 __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
 {
     extern __shared__ unsigned long long s_fb[];
-    const int c = blockIdx.y;
+    const int c = P.act ? P.act[blockIdx.y] : blockIdx.y;
     const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
     const unsigned long long* gfb = P.fbits + P.fboff[c];
     double* s_D;
@@ -372,6 +387,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
         if (mode == 1) {
             P.shift[base + p] = h;
         } else {
+            if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
             const double t = __dmul_rn(df, df);
@@ -379,7 +395,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
             else fb2 = __dadd_rn(fb2, t);
         }
     }
-    if (mode == 0 && p_seg < P.U) {
+    if (mode != 1 && p_seg < P.U) {
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
@@ -388,7 +404,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
 // dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
 __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
 {
-    const int c = blockIdx.y;
+    const int c = P.act ? P.act[blockIdx.y] : blockIdx.y;
     const int n = P.ns[c], off = P.soff[c];
     const size_t base = (size_t)c * P.ustr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -412,6 +428,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
         if (mode == 1) {
             P.shift[base + p] = h;
         } else {
+            if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
             const double t = __dmul_rn(df, df);
@@ -419,7 +436,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
             else fb2 = __dadd_rn(fb2, t);
         }
     }
-    if (mode == 0 && p_seg < P.U) {
+    if (mode != 1 && p_seg < P.U) {
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
@@ -428,9 +445,10 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
 // per-client ||diff||_F^2 (segment sums in order) and Lk = ||diff||_F (TopK.h:74-78)
 __global__ void k_fsum(Dev P)
 {
-    const int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int slot = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (c >= P.nc) return;
+    if (slot >= P.n_act) return;
+    const int c = P.act ? P.act[slot] : slot;
     const double* fp = P.Fpart + (size_t)c * P.nseg;
     double f = 0.0;
     for (int q0 = 0; q0 < P.nseg; q0 += 32) {
@@ -440,7 +458,7 @@ __global__ void k_fsum(Dev P)
     }
     if (lane == 0) {
         P.F[c] = f;
-        P.lk[c] = sqrt(f);
+        if (!P.pp) P.lk[c] = sqrt(f);    // FedNL-PP takes Lk after the update (k_pp_dir)
     }
 }
 
@@ -635,12 +653,12 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int ustr, int U, int k,
                                                         int lek, double delta, const double* __restrict__ F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
-                                                        double* pdraw, int* minidx, int* err)
+                                                        double* pdraw, int* minidx, int* err, const int* act)
 {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     __shared__ __align__(8) unsigned long long s_bar[2];
     __shared__ int s_keep, s_fail;
-    const int c = blockIdx.x;
+    const int c = act ? act[blockIdx.x] : blockIdx.x;
     const double* v = vals + (size_t)c * ustr;
     unsigned* sc = sel + (size_t)c * SW;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -985,9 +1003,9 @@ __device__ __forceinline__ void hmap_put(unsigned long long* m, int cap, unsigne
 }
 
 __global__ void k_randk(unsigned* states, int n_gen, int U, int k, unsigned long long* hmap, int hcap,
-                        unsigned* sel, int SW, int* cnt)
+                        unsigned* sel, int SW, int* cnt, const int* act)
 {
-    int c = blockIdx.x;
+    int c = act ? act[blockIdx.x] : blockIdx.x;
     unsigned long long* m = hmap + (size_t)c * hcap;
     unsigned* sc = sel + (size_t)c * SW;
     for (int t = threadIdx.x; t < hcap; t += blockDim.x) m[t] = ~0ull;
@@ -1018,9 +1036,10 @@ __global__ void k_randk(unsigned* states, int n_gen, int U, int k, unsigned long
 }
 
 // generateRandSeqKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:137-169)
-__global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq, unsigned* sel, int SW, int* cnt)
+__global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq, unsigned* sel, int SW, int* cnt,
+                           const int* act)
 {
-    int c = blockIdx.x;
+    int c = act ? act[blockIdx.x] : blockIdx.x;
     unsigned* sc = sel + (size_t)c * SW;
     for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
     __shared__ unsigned s_r;
@@ -1051,14 +1070,17 @@ __global__ void k_apply(Dev P)
     double h = P.H[p];
     const bool all = (P.comp == 0 || P.comp == 5);
     const unsigned bit = 1u << (p & 31);
-    for (int c0 = 0; c0 < P.nc; c0 += 16) {
+    for (int c0 = 0; c0 < P.n_act; c0 += 16) {
         unsigned wd[16];
+        int cl[16];
 #pragma unroll
-        for (int t = 0; t < 16; ++t)
-            wd[t] = (c0 + t < P.nc) ? (all ? bit : P.sel[(size_t)(c0 + t) * P.SW + (p >> 5)]) : 0u;
+        for (int t = 0; t < 16; ++t) {
+            cl[t] = (c0 + t < P.n_act) ? (P.act ? P.act[c0 + t] : c0 + t) : 0;
+            wd[t] = (c0 + t < P.n_act) ? (all ? bit : P.sel[(size_t)cl[t] * P.SW + (p >> 5)]) : 0u;
+        }
         for (int t = 0; t < 16; ++t) {
             if (!(wd[t] & bit)) continue;
-            const size_t q = (size_t)(c0 + t) * P.ustr + p;
+            const size_t q = (size_t)cl[t] * P.ustr + p;
             const double dv = P.diff[q];
             double item, sent;
             if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
@@ -1406,6 +1428,230 @@ __global__ void k_natural_pack(const double* in, long long n, unsigned char* pac
     packed[3 * q + 0] = (unsigned char)(v & 0xFF);
     packed[3 * q + 1] = (unsigned char)((v >> 8) & 0xFF);
     packed[3 * q + 2] = (unsigned char)((v >> 16) & 0xFF);
+}
+
+
+// ---- 9. FedNL-PP (dopt/bin_fednl_local_pp) ----------------------------------------------------
+// Client sampler (TrainLoop.h:1150-1157): a fresh 0..n-1 is shuffled for tau steps by the partial
+// Fisher-Yates of Shuffle.h:76-93 with the sampler's RandomGenIntegerLinear; its first tau entries
+// are this round's clients, processed and merged in ascending client order (forcesequpdate).  One
+// CTA; the permutation lives in shared memory when it fits (smem_perm), else in global scratch.
+// needs[] is cleared so that the TopLEK draw kernel skips clients that were not sampled.
+constexpr int kPPThreads = 256;
+
+__global__ void __launch_bounds__(kPPThreads) k_pp_sample(int n, int tau, unsigned* sampler, int* gperm, int* act,
+                                                          int* is_sel, int* needs, int smem_perm)
+{
+    extern __shared__ int s_perm[];
+    __shared__ int s_wsum[kPPThreads / 32];
+    int* perm = smem_perm ? s_perm : gperm;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < n; i += blockDim.x) {
+        perm[i] = i;
+        is_sel[i] = 0;
+        if (needs) needs[i] = 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        unsigned st = *sampler;
+        unsigned long long n_minus_i_minus_one = (unsigned long long)n - 1;
+        for (int i = 0; i < tau; ++i, --n_minus_i_minus_one) {
+            const double u = lcg_int_unit(st);
+            const unsigned long long r_off = round_to_nearest(__dmul_rn(u, (double)n_minus_i_minus_one));
+            if (r_off != 0) {
+                const int r = i + (int)r_off;
+                const int a = perm[i], b = perm[r];
+                perm[i] = b;
+                perm[r] = a;
+            }
+        }
+        *sampler = st;
+    }
+    __syncthreads();
+    for (int t = tid; t < tau; t += blockDim.x) is_sel[perm[t]] = 1;
+    __syncthreads();
+    // ascending compaction: thread t owns clients [t * per, (t + 1) * per)
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, tid * per), hi = min(n, lo + per);
+    int cnt = 0;
+    for (int c = lo; c < hi; ++c) cnt += is_sel[c];
+    int incl = cnt;
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += s_wsum[w];
+    int pos = base + incl - cnt;
+    for (int c = lo; c < hi; ++c)
+        if (is_sel[c]) act[pos++] = c;
+}
+
+// True gradient at the round's starting iterate (computeFullGradient, TrainLoop.h:117-129), in
+// the fixed blocked order of the CPU oracle: in-order sums over blocks of 32 consecutive clients,
+// block sums in order, then / n.  One warp per coordinate; lane l owns blocks l, l + 32, ...
+// The last CTA also records ||true gradient|| (sequential sum of squares) as the round's norm.
+__global__ void k_pp_truegrad(Dev P)
+{
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i < P.d) {
+        const int nb = (P.nc + 31) / 32;
+        double acc = 0.0;
+        for (int b0 = 0; b0 < nb; b0 += 32) {
+            const int b = b0 + lane;
+            double bs = 0.0;
+            if (b < nb) {
+                const int c0 = b * 32, c1 = min(P.nc, c0 + 32);
+                bs = P.gc[(size_t)c0 * P.d + i];
+                for (int c = c0 + 1; c < c1; ++c) bs = __dadd_rn(bs, P.gc[(size_t)c * P.d + i]);
+            }
+            const int cntb = min(32, nb - b0);
+            for (int t = 0; t < cntb; ++t) {
+                const double v = __shfl_sync(0xffffffffu, bs, t);
+                acc = (b0 + t == 0) ? v : __dadd_rn(acc, v);
+            }
+        }
+        if (lane == 0) P.tg[i] = __ddiv_rn(acc, (double)P.nc);
+    }
+}
+
+__global__ void k_pp_norm(Dev P)
+{
+    if (threadIdx.x != 0) return;
+    double gs = 0.0;
+    for (int i = 0; i < P.d; ++i) gs = __dadd_rn(gs, __dmul_rn(P.tg[i], P.tg[i]));
+    const double gn = sqrt(gs);
+    P.stats[0] = gn;
+    const int r = *P.round_ctr;
+    if (r < P.hist_cap) P.hist[r] = gn;
+    *P.round_ctr = r + 1;
+}
+
+// ||shift - H_i||_F^2 after the shift update (the PP workers' "Put Lk", e.g. RandSeqK.h:166-173) in
+// the segment order of k_hess_binary: warp per 512 upper positions, diagonal and off-diagonal
+// accumulators apart, halving tree.
+__global__ void __launch_bounds__(kHessThreads) k_pp_lkpart(Dev P)
+{
+    const int c = P.act[blockIdx.y];
+    const size_t base = (size_t)c * P.ustr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = blockIdx.x * (kHessThreads / 32) + warp;
+    const int p_seg = seg * 512;
+    double fa = 0.0, fb2 = 0.0;
+    for (int q = 0; q < 16; ++q) {
+        const int p = p_seg + 32 * q + lane;
+        if (p >= P.U) break;
+        const double df = __dsub_rn(P.shift[base + p], P.hbuf[base + p]);
+        const double t = __dmul_rn(df, df);
+        if (upper_is_diag(p)) fa = __dadd_rn(fa, t);
+        else fb2 = __dadd_rn(fb2, t);
+    }
+    if (p_seg < P.U) {
+        const double cs = chunk_tree(segment_value(fa, fb2));
+        if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
+    }
+}
+
+// Per processed client: Lk = ||shift - H_i||_F (segment sums in order), its difference, and the
+// direction dir = x Lk + shift x - grad with shift x swept column by column
+// (MatrixNMD::matrixVectorMultiply, MatrixNMD.h:1299-1325); the difference to the previous
+// direction is what the client sends.
+__global__ void k_pp_dir(Dev P)
+{
+    __shared__ double s_lk;
+    const int c = P.act[blockIdx.x];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const double* fp = P.Fpart + (size_t)c * P.nseg;
+        double f = 0.0;
+        for (int q0 = 0; q0 < P.nseg; q0 += 32) {
+            const double v = (q0 + lane < P.nseg) ? fp[q0 + lane] : 0.0;
+            const int cnt = min(32, P.nseg - q0);
+            for (int t = 0; t < cnt; ++t) f = __dadd_rn(f, __shfl_sync(0xffffffffu, v, t));
+        }
+        if (lane == 0) {
+            const double lk = sqrt(f);
+            P.dlk[c] = __dsub_rn(lk, P.lk[c]);
+            P.lk[c] = lk;
+            s_lk = lk;
+        }
+    }
+    __syncthreads();
+    const double lk = s_lk;
+    const double* sh = P.shift + (size_t)c * P.ustr;
+    for (int i = threadIdx.x; i < P.d; i += blockDim.x) {
+        double y = 0.0;
+        for (int j = 0; j < P.d; ++j) {
+            const int a = min(i, j), b = max(i, j);
+            y = __dadd_rn(y, __dmul_rn(sh[(size_t)b * (b + 1) / 2 + a], P.x[j]));
+        }
+        const size_t q = (size_t)c * P.d + i;
+        const double dv = __dsub_rn(__dadd_rn(__dmul_rn(P.x[i], lk), y), P.gc[q]);
+        P.ddir[q] = __dsub_rn(dv, P.dir[q]);
+        P.dir[q] = dv;
+    }
+}
+
+// Master (TrainLoop.h:1168-1450): g = (sum of the sent direction differences) / n + g_prev and
+// l = (sum of the Lk differences) / n + l_prev, processed clients in ascending order.
+__global__ void k_pp_aggregate(Dev P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.d) {
+        double g = 0.0;
+        for (int s = 0; s < P.n_act; ++s) g = __dadd_rn(g, P.ddir[(size_t)P.act[s] * P.d + i]);
+        g = __dadd_rn(__dmul_rn(g, P.inv_n), P.gprev[i]);
+        P.gprev[i] = g;
+        P.g[i] = g;
+    }
+    if (i == 0) {
+        double l = 0.0;
+        for (int s = 0; s < P.n_act; ++s) l = __dadd_rn(l, P.dlk[P.act[s]]);
+        l = __dadd_rn(__dmul_rn(l, P.inv_n), *P.lprev);
+        *P.lprev = l;
+        P.stats[1] = l;
+    }
+}
+
+// FedNL-PP initial state (LocalWorkerForFedNL_RandSeqK.h:22-31 and TrainLoop.h:1064-1080):
+// Lk = 0, dir = shift x0 - grad(x0) per client; g_prev = mean dir (clients in order), l_prev = 0.
+__global__ void k_pp_init_dir(Dev P)
+{
+    const int c = blockIdx.x;
+    const double* sh = P.shift + (size_t)c * P.ustr;
+    for (int i = threadIdx.x; i < P.d; i += blockDim.x) {
+        double y = 0.0;
+        for (int j = 0; j < P.d; ++j) {
+            const int a = min(i, j), b = max(i, j);
+            y = __dadd_rn(y, __dmul_rn(sh[(size_t)b * (b + 1) / 2 + a], P.x[j]));
+        }
+        const size_t q = (size_t)c * P.d + i;
+        P.dir[q] = __dsub_rn(y, P.gc[q]);
+        P.ddir[q] = 0.0;
+    }
+    if (threadIdx.x == 0) {
+        P.lk[c] = 0.0;
+        P.dlk[c] = 0.0;
+    }
+}
+
+__global__ void k_pp_init_mean(Dev P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.d) {
+        double g = 0.0;
+        for (int c = 0; c < P.nc; ++c) g = __dadd_rn(g, P.dir[(size_t)c * P.d + i]);
+        P.gprev[i] = __dmul_rn(g, P.inv_n);
+    }
+    if (i == 0) {
+        double l = 0.0;
+        for (int c = 0; c < P.nc; ++c) l = __dadd_rn(l, P.lk[c]);
+        *P.lprev = __dmul_rn(l, P.inv_n);
+    }
 }
 
 }  // namespace fednl

@@ -36,7 +36,8 @@ class ProblemDesc(C.Structure):
                 ("n_samples", C.POINTER(C.c_int32)), ("lambda_", C.c_double),
                 ("compressor", C.c_int32), ("k", C.c_int32), ("alpha", C.c_double),
                 ("workers", C.c_int32), ("seed_base", C.c_uint32), ("toplek_seed", C.c_uint32),
-                ("feature_format", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("feature_format", C.c_int32), ("clients_per_round", C.c_int32),
+                ("client_seed", C.c_uint32), ("reserved", C.c_int32 * 2)]
 
 
 class RoundStats(C.Structure):
@@ -47,7 +48,8 @@ class RoundStats(C.Structure):
 EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_data", "fednl_gpu_init_shifts",
            "fednl_gpu_round", "fednl_gpu_run", "fednl_gpu_get_x", "fednl_gpu_set_x", "fednl_gpu_get_grad",
            "fednl_gpu_get_H", "fednl_gpu_get_shift", "fednl_gpu_get_l", "fednl_gpu_get_lk",
-           "fednl_gpu_get_message", "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
+           "fednl_gpu_get_message", "fednl_gpu_get_selected", "fednl_gpu_get_true_grad", "fednl_gpu_get_dir",
+           "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
            "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
            "fednl_gpu_last_error"]
@@ -80,6 +82,9 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_get_x": [vp, dp], "fednl_gpu_set_x": [vp, dp], "fednl_gpu_get_grad": [vp, dp],
         "fednl_gpu_get_H": [vp, dp], "fednl_gpu_get_shift": [vp, C.c_int32, dp],
         "fednl_gpu_get_message": [vp, C.c_int32, up, dp, ip],
+        "fednl_gpu_get_selected": [vp, ip, ip],
+        "fednl_gpu_get_true_grad": [vp, dp],
+        "fednl_gpu_get_dir": [vp, C.c_int32, dp, dp],
         "fednl_gpu_topk": [dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
         "fednl_gpu_toplek": [dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, up, up, ip],
         "fednl_gpu_randk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
@@ -199,10 +204,12 @@ def cholesky_option_b_solve(H: np.ndarray, d: int, lda: int, l: float, g: np.nda
 # ---- whole runs ------------------------------------------------------------------------------
 
 class FedNL:
-    """One FedNL problem resident on the GPU (reference: bin_fednl_local train())."""
+    """One FedNL problem resident on the GPU (reference: bin_fednl_local train()); with
+    clients_per_round set, FedNL-PP (bin_fednl_local_pp train()) with that many sampled clients."""
 
     def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
-                 seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0):
+                 seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0,
+                 clients_per_round: int = 0, client_seed: int = 1234):
         self.d = prob.d
         self.lda = lda or reference_lda(prob.d)
         self.n_clients = prob.n_clients
@@ -211,7 +218,8 @@ class FedNL:
         self.compressor = comp
         desc = ProblemDesc(self.d, self.lda, self.n_clients, _ip(self._ns), float(prob.lam), comp, int(k),
                            float(alpha), int(workers), int(seed_base), int(toplek_seed), int(feature_format),
-                           (C.c_int32 * 4)(0, 0, 0, 0))
+                           int(clients_per_round or 0), int(client_seed), (C.c_int32 * 2)(0, 0))
+        self.pp = bool(clients_per_round)
         h = C.c_void_p()
         _check(load().fednl_gpu_create(C.byref(desc), C.byref(h)))
         self._h = h
@@ -291,6 +299,23 @@ class FedNL:
 
     def lk(self, c: int) -> float:
         return load().fednl_gpu_get_lk(self._h, c)
+
+    def selected(self) -> np.ndarray:
+        """FedNL-PP: the last round's sampled clients, ascending."""
+        out = np.empty(self.n_clients, dtype=np.int32)
+        cnt = np.zeros(1, dtype=np.int32)
+        _check(load().fednl_gpu_get_selected(self._h, _ip(out), _ip(cnt)))
+        return out[:int(cnt[0])].copy()
+
+    def true_grad(self) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_gpu_get_true_grad(self._h, _dp(out)))
+        return out
+
+    def dir(self, c: int):
+        dr, dd = np.empty(self.d), np.empty(self.d)
+        _check(load().fednl_gpu_get_dir(self._h, c, _dp(dr), _dp(dd)))
+        return dr, dd
 
     def message(self, c: int):
         U = self.d * (self.d + 1) // 2
