@@ -16,6 +16,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -73,7 +74,7 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"fednl_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
@@ -215,6 +216,44 @@ def run_reference(args, ws, rank, td):
     return 0
 
 
+def extra_workloads(fednl, threads: int, steps: int):
+    """The other configurations of the reference's benchmark set, device-timed the same way (cold L2
+    before every round) beside a bounded sample of the CPU port: the a9a-like FedNL TopK run and the
+    phishing-like FedNL-PP runs (2048 clients x 6 samples, tau = 128; RandSeqK and Natural)."""
+    from ufednl_gb300 import datagen
+    from oracle import pyoracle
+    out = {}
+    U69 = 69 * 70 // 2
+    cases = [("a9a-like d124 80x407 TopK k=8d", datagen.workload_a9a_like(), "topk", 8 * 124, 1.0, 0),
+             ("phishing-like d69 2048x6 FedNL-PP tau=128 RandSeqK k=d", datagen.workload_phishing_pp(),
+              "randseqk", 69, 69 / U69, 128),
+             ("phishing-like d69 2048x6 FedNL-PP tau=128 Natural", datagen.workload_phishing_pp(),
+              "natural", U69, 1.0 / (1.0 + 1.0 / 8.0), 128)]
+    n = max(20, min(steps, 200))
+    for name, prob, comp, k, alpha, tau in cases:
+        fed = fednl.FedNL(prob, comp, k, alpha, workers=threads, clients_per_round=tau)
+        fed.run(3)
+        tot, per = fed.time_rounds(n, L2_FLUSH_BYTES)
+        prof = fed.profile_kernels(min(n, 20), L2_FLUSH_BYTES)
+        fed.close()
+        orc = pyoracle.FedNL(prob, comp, k, alpha, workers=threads, threads=threads,
+                             clients_per_round=tau or None)
+        orc.round()
+        t0 = time.perf_counter()
+        m = 0
+        while m < 200 and time.perf_counter() - t0 < 3.0:
+            orc.round()
+            m += 1
+        cpu = m / (time.perf_counter() - t0)
+        orc.close()
+        top = max(prof, key=lambda t: t[1])
+        out[name] = {"rounds_per_s": n / (tot / 1000.0), "round_ms_p50": float(np.percentile(per, 50)),
+                     "round_ms_p99": float(np.percentile(per, 99)), "rounds_timed": n,
+                     "top_kernel": {"name": top[0], "ms": top[1]}, "gpu_launches_per_round": len(prof),
+                     "cpu_port_rounds_per_s": cpu, "cpu_port_sample": f"{m} rounds, {threads} threads"}
+    return out
+
+
 def config_dict(prob, comp, k, workers):
     return {"workload": prob.name, "d": prob.d, "clients": prob.n_clients, "samples": prob.total_samples,
             "compressor": comp, "k": k, "alpha": 1.0, "option": "B", "lambda": prob.lam, "workers": workers,
@@ -296,6 +335,8 @@ def run_ours(args, ws, rank, local, td):
                             "timed": "device time of rounds 1..R from x0 = 0"},
             "roofline": roof, "round_roofline": round_roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
             "clocks": clocks, "e2e": e2e}
+    if ws == 1 and rank == 0 and not args.no_extra:
+        line["extra_workloads"] = extra_workloads(fednl, os.cpu_count() or 1, args.steps)
     if ws == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, n, dt = cpu_port_rounds_per_s(prob, comp, k, threads, 20, 20.0)
@@ -315,6 +356,7 @@ def main():
     ap.add_argument("--workload", choices=["w8a", "a9a"], default="w8a")
     ap.add_argument("--workers", type=int, default=0, help="reference --workers (TopLEK streams); 0 = host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the a9a-like and FedNL-PP side measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -1138,10 +1138,12 @@ __device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j +
 // ---- 8b. Option-B solve across the whole GPU -------------------------------------------------
 // Blocked right-looking Cholesky in one cooperative launch.  For each panel of kCholNB rows:
 //   1. every CTA factors the kCholNB x kCholNB diagonal block redundantly in shared memory (no
-//      barrier needed; CTA 0 writes it back);
-//   2. the warps of all CTAs finish the panel's rows of R column by column (one column per warp:
-//      lane t holds a_{c0+t,j}; r_kj = a_kj (1 / r_kk), then a_ij = fma(-r_ki, r_kj, a_ij));
-//   3. grid barrier, then all threads apply the panel to the trailing triangle entry by entry
+//      barrier needed; CTA 0 writes it back) and, in the same column loop, the panel rows of its
+//      own share of the columns right of the block (r_kj = a_kj (1 / r_kk), then
+//      a_ij = fma(-r_ki, r_kj, a_ij)); on GB300 a warp's FP64 instructions issue about once per
+//      64 cycles and sqrt + reciprocal take ~1000 cycles, so the loop keeps the pivot chain short
+//      (two CTA barriers per column) and spreads the updates over all warps;
+//   2. grid barrier, then all threads apply the panel to the trailing triangle entry by entry
 //      (a_ij = fma(-r_ki, r_kj, a_ij), k over the panel in order); grid barrier.
 // Every entry undergoes exactly the operation sequence of the unblocked right-looking algorithm,
 // so the factor equals the CPU oracle's factor bit for bit.  g is appended as column d of the
@@ -1150,6 +1152,7 @@ __device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j +
 // up in column d.  The backward substitution runs in CTA 0, blocked by 32 rows, same order as the
 // oracle's.
 constexpr int kCholNB = 32;
+constexpr int kCholSlab = 8;                          // panel columns per CTA kept in shared memory
 constexpr int kCoopThreads = 256;
 constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIMEOUT
 
@@ -1197,7 +1200,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                                                             double* xupd, int record)
 {
     __shared__ double Db[kCholNB][kCholNB + 1];
+    __shared__ double Sb[kCholNB][kCholSlab + 1];
     __shared__ double s_inv[kCholNB];
+    __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
     const double l = lptr ? *lptr : lval;
     const int d = P.d;
@@ -1220,32 +1225,71 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     if (!grid_barrier(P.bar, G)) goto timeout;
     for (int c0 = 0; c0 < d; c0 += kCholNB) {
         const int nb = min(kCholNB, d - c0), c1 = c0 + nb;
+        // this CTA's panel columns right of the block: j = c1 + blockIdx.x + s G, s < ns (kept in
+        // shared memory, at most kCholSlab; any further ones are finished after the column loop)
+        const int ntot = D > c1 ? (D - c1 - (int)blockIdx.x + (int)G - 1) / (int)G : 0;
+        const int ns = max(0, min(ntot, kCholSlab));
         for (int t = tid; t < nb * nb; t += blockDim.x) {
             int i = t % nb, j = t / nb;
             if (i <= j) Db[i][j] = A[up_pos(c0 + i, c0 + j)];
         }
+        for (int t = tid; t < nb * ns; t += blockDim.x) {
+            const int i = t % nb, sl = t / nb;
+            Sb[i][sl] = A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)];
+        }
+        // block entries (i, j), i <= j, listed by descending i: those with i > k are a prefix
+        for (int e = tid; e < nb * (nb + 1) / 2; e += blockDim.x) {
+            int i = nb - 1, rem = e;
+            while (rem >= nb - i) {
+                rem -= nb - i;
+                --i;
+            }
+            s_ent[e] = (unsigned short)((i << 8) | (i + rem));
+        }
         if (tid == 0) s_fail = 0;
         __syncthreads();
+        // column loop (the unblocked right-looking steps restricted to the panel's rows): warps 0
+        // and 1 both form the pivot from the broadcast diagonal entry (no barrier between them);
+        // warp 0 scales the block's row k, warp 1 the slab's; then all threads apply the rank-1
+        // update to the block and slab entries below row k.
         for (int k = 0; k < nb; ++k) {
-            if (tid == 0) {
+            double r_keep = 0.0;
+            if (tid < 64) {
                 double a = Db[k][k];
+                bool bad = false;
                 if (a < 0) {
                     if (a > -0.0) a = 0.0;
-                    else s_fail = 1;
+                    else bad = true;
                 }
-                double r = sqrt(a);
-                Db[k][k] = r;
-                s_inv[k] = 1.0 / r;
+                const double r = sqrt(a);
+                const double inv = 1.0 / r;
+                if (tid < 32) {
+                    const int j = k + 1 + lane;
+                    if (j < nb) Db[k][j] = __dmul_rn(Db[k][j], inv);
+                    if (lane == 0) {     // r_kk is stored after the barrier: warp 1 may still read a_kk
+                        r_keep = r;
+                        s_inv[k] = inv;
+                        if (bad) s_fail = 1;
+                    }
+                } else if (lane < ns) {
+                    Sb[k][lane] = __dmul_rn(Sb[k][lane], inv);
+                }
             }
             __syncthreads();
             if (s_fail) break;
-            const double inv = s_inv[k];
-            for (int j = k + 1 + tid; j < nb; j += blockDim.x) Db[k][j] = __dmul_rn(Db[k][j], inv);
-            __syncthreads();
-            const int m = nb - k - 1;
-            for (int t = tid; t < m * m; t += blockDim.x) {
-                int ii = k + 1 + t % m, jj = k + 1 + t / m;
-                if (ii <= jj) Db[ii][jj] = fma(-Db[k][ii], Db[k][jj], Db[ii][jj]);
+            if (tid == 0) Db[k][k] = r_keep;
+            const int nblk = (nb - 1 - k) * (nb - k) / 2;
+            const int nall = nblk + (nb - 1 - k) * ns;
+            for (int e = tid; e < nall; e += blockDim.x) {
+                if (e < nblk) {
+                    const unsigned v = s_ent[e];
+                    const int i = (int)(v >> 8), j = (int)(v & 0xffu);
+                    Db[i][j] = fma(-Db[k][i], Db[k][j], Db[i][j]);
+                } else {
+                    const int q = e - nblk;
+                    const int i = k + 1 + q / ns, sl = q - (q / ns) * ns;
+                    Sb[i][sl] = fma(-Db[k][i], Sb[k][sl], Sb[i][sl]);
+                }
             }
             __syncthreads();
         }
@@ -1263,16 +1307,23 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             }
             for (int t = tid; t < nb; t += blockDim.x) P.rinv[c0 + t] = s_inv[t];
         }
-        // panel rows of R for the columns right of the diagonal block (and of y in column d)
-        const int gw = gtid >> 5, nwarps = gthreads >> 5;
-        for (int j = c1 + gw; j < D; j += nwarps) {
-            double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
-            for (int k = 0; k < nb; ++k) {
-                if (lane == k) a = __dmul_rn(a, s_inv[k]);
-                double r = __shfl_sync(0xffffffffu, a, k);
-                if (lane > k && lane < nb) a = fma(-Db[k][lane], r, a);
+        for (int t = tid; t < nb * ns; t += blockDim.x) {
+            const int i = t % nb, sl = t / nb;
+            A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)] = Sb[i][sl];
+        }
+        // panel columns beyond the slab (very large d only): one column per warp, same steps
+        {
+            const int w = tid >> 5;
+            for (int sl = kCholSlab + w; sl < ntot; sl += kCoopThreads / 32) {
+                const int j = c1 + (int)blockIdx.x + sl * (int)G;
+                double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
+                for (int k = 0; k < nb; ++k) {
+                    if (lane == k) a = __dmul_rn(a, s_inv[k]);
+                    double r = __shfl_sync(0xffffffffu, a, k);
+                    if (lane > k && lane < nb) a = fma(-Db[k][lane], r, a);
+                }
+                if (lane < nb) A[up_pos(c0 + lane, j)] = a;
             }
-            if (lane < nb) A[up_pos(c0 + lane, j)] = a;
         }
         if (c1 >= d) break;
         if (!grid_barrier(P.bar, G)) goto timeout;
