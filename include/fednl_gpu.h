@@ -70,6 +70,12 @@ typedef struct fednl_problem_desc {
      * 0 = plain FedNL (bin_fednl_local) */
     int32_t clients_per_round;
     uint32_t client_seed;       /* FedNL-PP sampler seed (--client-selection-seed, reference: 1234) */
+    /* FedNL options of bin_fednl_local (TrainLoop.h:300-360, 1383-1640) */
+    int32_t option_a;           /* 1: Option A, Cholesky of H + lambda I (--fednl-option-a); 0: Option B */
+    int32_t line_search;        /* 1: FedNL-LS backtracking on the iterate (--line_search); not with PP */
+    double ls_c, ls_gamma;      /* --c_line_search, --gamma_line_search */
+    int32_t ls_max_steps;       /* --max_line_search_steps (reference default 5) */
+    int32_t track_f;            /* 1: form f(x) at every round's starting iterate (--tracking) */
     int32_t reserved[2];        /* must be zero */
 } fednl_problem_desc;
 
@@ -124,6 +130,12 @@ int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double*
  * x Lk + shift x - grad with its last sent difference (LocalWorkerForFedNL_*.h "gradient like
  * direction").  EINVAL on a handle without FedNL-PP. */
 int fednl_gpu_get_selected(fednl_handle h, int32_t* clients, int32_t* count);
+
+/* f(x) at the last round's starting iterate (function_aggregation, TrainLoop.h:1511-1541; needs
+ * line_search or track_f, else NAN) and the number of objective evaluations of the last round's
+ * line search (0 without FedNL-LS). */
+double fednl_gpu_get_f(fednl_handle h);
+int32_t fednl_gpu_get_ls_steps(fednl_handle h);
 int fednl_gpu_get_true_grad(fednl_handle h, double* g);                    /* [d] */
 int fednl_gpu_get_dir(fednl_handle h, int32_t client, double* dir, double* ddir);   /* [d] each */
 
@@ -191,12 +203,28 @@ int fednl_gpu_time_rounds(fednl_handle h, int32_t rounds, int64_t flush_bytes, d
                           double* per_round_ms);
 
 /* Per-kernel breakdown of the same rounds: launched kernel by kernel with CUDA events between the
- * launches on the handle's stream.  kernel_ms[t] (capacity 32) receives the mean time of the t-th
+ * launches on the handle's stream.  kernel_ms[t] (capacity 64) receives the mean time of the t-th
  * launch of a round; names receives the kernel names separated by ';'. */
 int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_bytes, int32_t* n_kernels,
                               double* kernel_ms, char* names, int32_t names_len);
 
 const char* fednl_gpu_last_error(void);
+
+/* ---- the reference's local driver ---------------------------------------------------------- */
+/* Callback of doptExecuteLocal (bin_fednl_local/include/TrainCallbaksShared.h:11-14): dimension,
+ * ||g|| of the last round, ||g||^2 / (2 mu) and 2 ||g||^2 / mu with mu = lambda
+ * (TrainLoop.h:1854-1860, ConvexOptimizationRoutines.h:13-27). */
+typedef void (*fednl_result_callback)(int x_dimension, double grad_norm, double f_gap_bound, double x_gap_bound);
+
+/* doptExecuteLocal (bin_fednl_local/src/mainShared.cpp:15-38) on the GB300 engine: the command is
+ * bin_fednl_local's command line (--train_dataset, --clients, --reshuffle_train, --add_intercept,
+ * --lambda, --rounds, --workers, --algorithm fednl1, --compressor identical|natural|randk|topk|
+ * toplek|seqk, --k_compressor_as_d_mult, --alpha_step_size or --theoretical_alpha with
+ * --use_theoretical_alpha_option_1|2, --fednl-option-a|b, --line_search with --c_line_search,
+ * --gamma_line_search, --max_line_search_steps, --tracking, --out, --debug).  Returns the
+ * reference's TrainReturnCodes (0 ok, -1 missing argument, -2 wrong argument, -3 dataset missing,
+ * -4 parse error, -5 split error, -6 saving failed, -7 internal error, -8 unknown debug mode). */
+int fednl_gpu_execute_local(const char* command, fednl_result_callback callback);
 
 #ifdef __cplusplus
 }

@@ -516,6 +516,74 @@ double orc_exp(double x)
     return p * pow2i(k);
 }
 
+/* Natural logarithm, own implementation shared bit for bit with the GB300 kernels: x = 2^e m with
+ * m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s) with s = (m - 1)/(m + 1) (m - 1 exact by Sterbenz,
+ * m + 1 and s carried as double-doubles), the odd series 2 s^3 (1/3 + s^2/5 + ... + s^20/23) for
+ * the tail (|s| < 0.172, so 11 terms reach 2^-58 relative), and e ln 2 from the same two-part ln 2
+ * as orc_exp.  Errors stay below one ulp; results need not equal libm's. */
+double orc_log(double x)
+{
+    if (x != x)
+        return x;
+    if (x < 0.0)
+        return 0.0 / 0.0;
+    if (x == 0.0)
+        return -1.0 / 0.0;
+    if (x == 1.0 / 0.0)
+        return x;
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    int e = 0;
+    if ((b >> 52) == 0) {                     /* subnormal: scale into the normal range */
+        x = x * 18014398509481984.0;          /* 2^54 */
+        memcpy(&b, &x, 8);
+        e = -54;
+    }
+    e += (int)(b >> 52) - 1023;
+    uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+    double m;
+    memcpy(&m, &mb, 8);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        e += 1;
+    }
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    double f = m - 1.0;
+    double g_hi, g_lo;
+    two_sum(m, 1.0, &g_hi, &g_lo);
+    double s_hi = f / g_hi;
+    double r = fma(-s_hi, g_hi, f) - s_hi * g_lo;
+    double s_lo = r / g_hi;
+    double z = s_hi * s_hi;
+    double q = 1.0 / 23.0;
+    q = fma(q, z, 1.0 / 21.0);
+    q = fma(q, z, 1.0 / 19.0);
+    q = fma(q, z, 1.0 / 17.0);
+    q = fma(q, z, 1.0 / 15.0);
+    q = fma(q, z, 1.0 / 13.0);
+    q = fma(q, z, 1.0 / 11.0);
+    q = fma(q, z, 1.0 / 9.0);
+    q = fma(q, z, 1.0 / 7.0);
+    q = fma(q, z, 1.0 / 5.0);
+    q = fma(q, z, 1.0 / 3.0);
+    double tail = ((s_hi * z) * q) * 2.0;
+    double ed = (double)e;
+    double h, l;
+    two_sum(ed * ln2_hi, s_hi * 2.0, &h, &l);
+    l = l + ((s_lo * 2.0 + tail) + ed * ln2_lo);
+    return h + l;
+}
+
+double orc_client_function(const double* sig, int32_t n, const double* x, int32_t d, double lambda)
+{
+    double* t = (double*)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+    for (int32_t s = 0; s < n; ++s)
+        t[s] = -orc_log(sig[s]);
+    double loss = chunked_sum(t, (size_t)n) / (double)n;
+    free(t);
+    return loss + (lambda * 0.5) * orc_l2sq(x, (size_t)d);
+}
+
 /* elementwiseSigmoid, dopt/dopt/linalg_vectors/include_internal/VectorND_Raw_SIMD_double.h:1596-1650 */
 void orc_sigmoid(const double* m, int32_t n, double* sig)
 {
@@ -647,6 +715,7 @@ typedef struct {
     uint32_t* msg_idx;  /* flat indices */
     double* msg_val;    /* values exactly as the master adds them to H */
     int32_t msg_count;
+    double fi;          /* f_i at the round's starting iterate (tracking / line search) */
     double* dir;        /* FedNL-PP: localGradient = x Lk + shift x - grad (d) */
     double* ddir;       /* FedNL-PP: the difference last sent to the master (d) */
     double dlk;         /* FedNL-PP: the Lk difference last sent */
@@ -674,6 +743,8 @@ struct orc_state {
     uint8_t* is_sel;       /* [n] selected this round */
     int32_t* selected;     /* [tau] ascending */
     int32_t tau;
+    double f_k;            /* f at the round's starting iterate */
+    int32_t ls_steps;      /* function evaluations of the last line search */
 };
 
 /* Worker side of one client, first half: the compressor's index draw, margins, sigmoid, gradient,
@@ -697,6 +768,8 @@ static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff
     orc_margin(C->atr, d, lda, n, S->x, mtmp);
     orc_sigmoid(mtmp, n, stmp);
     orc_gradient(C->atr, d, lda, n, S->x, stmp, P->lambda, C->grad);
+    if (P->line_search || P->track_f)      /* "Put fi" (TopK.h:132-137) */
+        C->fi = orc_client_function(stmp, n, S->x, d, P->lambda);
     orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
     for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
         diff[t] = hbuf[t] - C->shift[t];
@@ -988,6 +1061,60 @@ void orc_destroy(orc_state* S)
 }
 
 static int orc_round_pp_master(orc_state* S, double* grad_norm);
+
+/* f(x) = mean of the clients' objectives at x (clients' sums in the fixed chunked order) */
+static double objective_at(orc_state* S, const double* x)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d, lda = P->lda, nc = P->n_clients;
+    int32_t nmax = 1;
+    for (int32_t c = 0; c < nc; ++c)
+        if (S->clients[c].n > nmax)
+            nmax = S->clients[c].n;
+    double* mtmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* stmp = (double*)malloc((size_t)nmax * sizeof(double));
+    double* fs = (double*)malloc((size_t)nc * sizeof(double));
+    for (int32_t c = 0; c < nc; ++c) {
+        orc_client* C = &S->clients[c];
+        orc_margin(C->atr, d, lda, C->n, x, mtmp);
+        orc_sigmoid(mtmp, C->n, stmp);
+        fs[c] = orc_client_function(stmp, C->n, x, d, P->lambda);
+    }
+    double f = chunked_sum(fs, (size_t)nc) * (1.0 / (double)nc);
+    free(mtmp);
+    free(stmp);
+    free(fs);
+    return f;
+}
+
+/* FedNL-LS backtracking (TrainLoop.h:1543-1640): t = 1; x = x_k - t dx until
+ * f(x) <= f(x_k) + (c t) (-(dx . g)), t *= gamma after each failure, at most ls_max_steps
+ * evaluations; the last trial point stays when none passes.  The dot product uses the chunked
+ * order. */
+static void orc_line_search(orc_state* S, const double* dx)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d;
+    double* t_dg = (double*)malloc((size_t)d * sizeof(double));
+    double* xprev = (double*)malloc((size_t)d * sizeof(double));
+    for (int32_t i = 0; i < d; ++i) {
+        t_dg[i] = dx[i] * S->g[i];
+        xprev[i] = S->x[i];
+    }
+    double dxg = -chunked_sum(t_dg, (size_t)d);
+    double t = 1.0;
+    for (int32_t it = 0; it < P->ls_max_steps; ++it) {
+        for (int32_t i = 0; i < d; ++i)
+            S->x[i] = xprev[i] - t * dx[i];
+        double fr = objective_at(S, S->x);
+        S->ls_steps = it + 1;
+        if (fr <= S->f_k + (P->ls_c * t) * dxg)
+            break;
+        t = t * P->ls_gamma;
+    }
+    free(t_dg);
+    free(xprev);
+}
 static void pp_select_and_track(orc_state* S);
 
 int orc_round(orc_state* S, double* grad_norm)
@@ -1037,13 +1164,26 @@ int orc_round(orc_state* S, double* grad_norm)
     l *= inv_n;
     S->l = l;
 
-    /* Option B: chol(H + l I), two triangular solves, x -= dx (TrainLoop.h:1431-1508) */
+    /* Option B: chol(H + l I), two triangular solves, x -= dx (TrainLoop.h:1431-1508); Option A
+     * regularises by mu = lambda instead (:1383-1430, computeMuStrongConvexity) */
     double* dx = (double*)malloc((size_t)d * sizeof(double));
-    int ok = orc_cholesky(S->H, d, lda, l, S->ltr);
+    int ok = orc_cholesky(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr);
+    S->ls_steps = 0;
+    if (P->line_search || P->track_f) {       /* function_aggregation (TrainLoop.h:1511-1541) */
+        double* fs = (double*)malloc((size_t)nc * sizeof(double));
+        for (int32_t c = 0; c < nc; ++c)
+            fs[c] = S->clients[c].fi;
+        S->f_k = chunked_sum(fs, (size_t)nc) * inv_n;
+        free(fs);
+    }
     if (ok) {
         orc_solve_chol(S->ltr, d, lda, S->g, dx);
-        for (int32_t i = 0; i < d; ++i)
-            S->x[i] -= dx[i];
+        if (!P->line_search) {
+            for (int32_t i = 0; i < d; ++i)
+                S->x[i] -= dx[i];
+        } else {
+            orc_line_search(S, dx);
+        }
     }
     free(dx);
     if (grad_norm) {
@@ -1142,6 +1282,9 @@ static int orc_round_pp_master(orc_state* S, double* grad_norm)
     }
     return ok ? 0 : -1;
 }
+
+double orc_get_f(const orc_state* S) { return S->f_k; }
+int32_t orc_get_ls_steps(const orc_state* S) { return S->ls_steps; }
 
 void orc_get_true_grad(const orc_state* S, double* g)
 {

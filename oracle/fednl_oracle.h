@@ -47,6 +47,11 @@ typedef struct orc_problem {
     int32_t pp;                /* 1: FedNL-PP (dopt/bin_fednl_local_pp), 0: FedNL */
     int32_t clients_per_round; /* FedNL-PP tau (--clients-per-round) */
     uint32_t client_seed;      /* FedNL-PP client sampler seed (--client-selection-seed, reference: 1234) */
+    int32_t option_a;          /* 1: FedNL Option A, Cholesky of H + lambda I (--fednl-option-a) */
+    int32_t line_search;       /* 1: FedNL-LS backtracking on the iterate (--line_search) */
+    double ls_c, ls_gamma;     /* --c_line_search, --gamma_line_search */
+    int32_t ls_max_steps;      /* --max_line_search_steps (reference default 5) */
+    int32_t track_f;           /* 1: form f(x) every round (--tracking) */
 } orc_problem;
 
 typedef struct orc_state orc_state;
@@ -73,6 +78,10 @@ uint32_t orc_pack2_natural(double a, double b);      /* pack2FP64NoMantissa, Flo
 double  orc_l2sq(const double* v, size_t n);          /* fixed chunked order, see the .c file */
 double  orc_frob_sym(const double* m, int32_t d, int32_t lda);
 double  orc_exp(double x);
+double  orc_log(double x);
+/* L2-logistic objective of one client from its sigmoid values (evaluateFunction(x, margin, sigmoid),
+ * logistic_regression.h:119-123): -mean log sigma_s + lambda/2 ||x||^2 */
+double  orc_client_function(const double* sig, int32_t n, const double* x, int32_t d, double lambda);
 
 /* ---- logistic-regression oracle (one client) ------------------------------------------ */
 /* atr: d x n col-major with leading dimension lda, column s = b_s * a_s */
@@ -110,6 +119,10 @@ double orc_get_lk(const orc_state* s, int32_t c);
 void   orc_get_true_grad(const orc_state* s, double* g);
 /* the round's sampled clients in ascending order; returns tau */
 int32_t orc_get_selected(const orc_state* s, int32_t* out);
+/* f(x) at the last round's starting iterate (tracking / line search) and the number of line-search
+ * evaluations the last round made */
+double  orc_get_f(const orc_state* s);
+int32_t orc_get_ls_steps(const orc_state* s);
 /* client c's running direction (x Lk + shift x - grad) and its last sent difference */
 void   orc_get_dir(const orc_state* s, int32_t c, double* dir, double* ddir);
 

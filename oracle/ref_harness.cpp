@@ -57,6 +57,7 @@ struct Client {
     dopt::RandomGenIntegerLinear rng;
     Vec dir, ddir;          // FedNL-PP: localGradient and the last sent difference
     double dlk = 0.0;       // FedNL-PP: the last sent Lk difference
+    double fi = 0.0;        // f_i at the round's iterate (tracking / line search)
 };
 
 // compression, message and shift update of one client (LocalWorkerForFedNL_{TopK,TopLEK,RandK,
@@ -119,7 +120,9 @@ static void compress_client(Client& C, const Mat& diff, int32_t comp, int32_t k,
 }
 
 // ---- run: whole FedNL (Option B) ---------------------------------------------------------
-static int cmd_run(const char* in_path, const char* out_path)
+// ext: the header carries Option A, FedNL-LS and tracking switches, and every round also reports
+// f(x_k) and the number of line-search evaluations (TrainLoop.h:1383-1430, 1511-1640)
+static int cmd_run(const char* in_path, const char* out_path, bool ext)
 {
     FILE* fi = fopen(in_path, "rb");
     FILE* fo = fopen(out_path, "wb");
@@ -129,6 +132,16 @@ static int cmd_run(const char* in_path, const char* out_path)
     int32_t d = R.get<int32_t>(), nc = R.get<int32_t>(), comp = R.get<int32_t>(), k = R.get<int32_t>();
     int32_t nworkers = R.get<int32_t>(), rounds = R.get<int32_t>(), dump_rounds = R.get<int32_t>();
     double lambda = R.get<double>(), alpha = R.get<double>();
+    int32_t option_a = 0, line_search = 0, ls_max = 5, track_f = 0;
+    double ls_c = 0.5, ls_gamma = 0.5;
+    if (ext) {
+        option_a = R.get<int32_t>();
+        line_search = R.get<int32_t>();
+        ls_max = R.get<int32_t>();
+        track_f = R.get<int32_t>();
+        ls_c = R.get<double>();
+        ls_gamma = R.get<double>();
+    }
     std::vector<int32_t> ns(nc);
     R.get(ns.data(), nc);
     size_t S = 0;
@@ -173,6 +186,7 @@ static int cmd_run(const char* in_path, const char* out_path)
         Vec margin = P->evaluateClassificationMargin(x);
         Vec sig = P->evaluateClassificationMarginSigmoid(margin);
         C.grad = P->evaluateGradient(x, margin, sig);
+        if (line_search || track_f) C.fi = P->evaluateFunction(x, margin, sig);
         Mat hess = P->evaluateHessian(x, margin, sig);
         Mat diff = hess - C.shift;
         C.lk = diff.frobeniusNormForSymmetricMatrixFromUpPart();
@@ -210,17 +224,46 @@ static int cmd_run(const char* in_path, const char* out_path)
         }
         g *= inv_n;
         l *= inv_n;
-        bool ok = dopt::cholFactorization::choleskyFactorization<Mat, true, true>(Ltr, H, l);
+        bool ok = dopt::cholFactorization::choleskyFactorization<Mat, true, true>(Ltr, H, option_a ? lambda : l);
         Vec dx(d);
         if (ok) {
             Vec y = dopt::forwardSubstitutionWithATranspose(Ltr, g);
             dx = dopt::backwardSubstitutionWithATranspose(Ltr, y);
         }
-        x -= dx;
+        double f_k = 0.0;
+        int32_t ls_steps = 0;
+        if (line_search || track_f) {
+            for (int32_t c = 0; c < nc; ++c) f_k += cl[c].fi;
+            f_k *= inv_n;
+        }
+        if (!line_search) {
+            x -= dx;
+        } else {
+            double t = 1.0;
+            double dxg = -(dx & g);
+            Vec xprev = x;
+            for (int32_t it = 0; it < ls_max; ++it) {
+                x = xprev - (t * dx);
+                double fr = 0.0;
+                for (int32_t c = 0; c < nc; ++c) {
+                    Vec mg = cl[c].prob->evaluateClassificationMargin(x);
+                    Vec sg = cl[c].prob->evaluateClassificationMarginSigmoid(mg);
+                    fr += cl[c].prob->evaluateFunction(x, mg, sg);
+                }
+                fr *= inv_n;
+                ls_steps = it + 1;
+                if (fr <= f_k + (ls_c * t) * dxg) break;
+                t *= ls_gamma;
+            }
+        }
         W.put<int32_t>(ok ? 1 : 0);
         W.put<double>(g.vectorL2Norm());
         W.put<double>(l);
         W.put(x.dataConst(), (size_t)d);
+        if (ext) {
+            W.put<double>(f_k);
+            W.put<int32_t>(ls_steps);
+        }
         if (r < dump_rounds) {
             for (int32_t c = 0; c < nc; ++c) {
                 W.put<int32_t>((int32_t)cl[c].idx.size());
@@ -462,7 +505,8 @@ int main(int argc, char** argv)
         fprintf(stderr, "usage: ref_harness run|topk|toplek|chol IN OUT | randk|randseqk OUT d k seed draws\n");
         return 2;
     }
-    if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3]);
+    if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3], false);
+    if (!strcmp(argv[1], "runx")) return cmd_run(argv[2], argv[3], true);
     if (!strcmp(argv[1], "pp")) return cmd_pp(argv[2], argv[3]);
     if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
     if (!strcmp(argv[1], "toplek")) return cmd_select(argv[2], argv[3], true);

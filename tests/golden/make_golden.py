@@ -40,8 +40,10 @@ def _skip(kind):
     return ONLY is not None and not kind.startswith(ONLY)
 
 
-def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
-    if _skip("run"):
+def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds, ext=None):
+    """ext = dict(option_a, line_search, ls_max, track_f, ls_c, ls_gamma): the extended run
+    (Option A / FedNL-LS / tracking), written as runx_<name>.npz with f(x_k) and line-search counts."""
+    if _skip("runx" if ext else "run"):
         return
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
@@ -49,10 +51,13 @@ def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
             np.array([prob.d, prob.n_clients, COMP[comp], k, workers, rounds, dump_rounds],
                      dtype="<i4").tofile(f)
             np.array([prob.lam, alpha], dtype="<f8").tofile(f)
+            if ext:
+                np.array([ext["option_a"], ext["line_search"], ext["ls_max"], ext["track_f"]], dtype="<i4").tofile(f)
+                np.array([ext["ls_c"], ext["ls_gamma"]], dtype="<f8").tofile(f)
             prob.n_samples.astype("<i4").tofile(f)
             prob.features.astype("<f8").tofile(f)
             prob.labels.astype("<f8").tofile(f)
-        subprocess.run([HARNESS, "run", fin, fout], check=True)
+        subprocess.run([HARNESS, "runx" if ext else "run", fin, fout], check=True)
         raw = open(fout, "rb").read()
     pos = 0
 
@@ -64,13 +69,16 @@ def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
 
     lda = int(take("<i4", 1)[0])
     d, nc = prob.d, prob.n_clients
-    ok, gnorm, lval, xs = [], [], [], []
+    ok, gnorm, lval, xs, fks, lss = [], [], [], [], [], []
     msg_idx, msg_val, lks, msg_cnt = [], [], [], []
     for r in range(rounds):
         ok.append(int(take("<i4", 1)[0]))
         gnorm.append(float(take("<f8", 1)[0]))
         lval.append(float(take("<f8", 1)[0]))
         xs.append(take("<f8", d))
+        if ext:
+            fks.append(float(take("<f8", 1)[0]))
+            lss.append(int(take("<i4", 1)[0]))
         if r < dump_rounds:
             for c in range(nc):
                 cnt = int(take("<i4", 1)[0])
@@ -79,14 +87,17 @@ def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds):
                 msg_val.append(take("<f8", cnt))
                 lks.append(float(take("<f8", 1)[0]))
     assert pos == len(raw)
+    extra = {}
+    if ext:
+        extra = dict(f=np.array(fks), ls_steps=np.array(lss, dtype=np.int32), **{k_: v for k_, v in ext.items()})
     np.savez_compressed(
-        os.path.join(HERE, f"run_{name}.npz"),
+        os.path.join(HERE, f"{'runx' if ext else 'run'}_{name}.npz"),
         d=d, lda=lda, n_samples=prob.n_samples, features=prob.features, labels=prob.labels,
         lam=prob.lam, compressor=comp, k=k, alpha=alpha, workers=workers, rounds=rounds,
         dump_rounds=dump_rounds, ok=np.array(ok), gnorm=np.array(gnorm), l=np.array(lval),
         x=np.array(xs), msg_count=np.array(msg_cnt, dtype=np.int32),
         msg_idx=np.concatenate(msg_idx).astype(np.uint32), msg_val=np.concatenate(msg_val),
-        lk=np.array(lks))
+        lk=np.array(lks), **extra)
 
 
 def pp_case(name, prob, comp, k, alpha, tau, rounds, dump_rounds, sel_seed=1234):
@@ -241,6 +252,17 @@ def main():
     run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 60, 3)
     dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
     run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
+
+    # Option A, FedNL-LS and tracked objective values
+    ls = dict(option_a=0, line_search=1, ls_max=5, track_f=1, ls_c=0.5, ls_gamma=0.5)
+    run_case("ls_randk_d13", small, "randk", 26, 26 / U, 2, 12, 2, ext=ls)
+    run_case("ls_natural_d13", small, "natural", U, 1.0 / (1.0 + 1.0 / 8.0), 2, 10, 2,
+             ext=dict(ls, ls_c=0.25, ls_gamma=0.7, ls_max=3))
+    run_case("ls_topk_d40", mid, "topk", 320, 1.0, 3, 40, 2, ext=ls)
+    run_case("opta_randseqk_d13", small, "randseqk", 13, 13 / U, 2, 12, 2,
+             ext=dict(option_a=1, line_search=0, ls_max=5, track_f=1, ls_c=0.5, ls_gamma=0.5))
+    run_case("track_toplek_d13", small, "toplek", 39, 1.0, 2, 10, 2,
+             ext=dict(option_a=0, line_search=0, ls_max=5, track_f=1, ls_c=0.5, ls_gamma=0.5))
 
     # FedNL-PP runs: uneven-free small federation (the reference's PP binary splits evenly), every
     # compressor; a phishing-shaped case (d = 69, n_i = 6)

@@ -190,30 +190,36 @@ def test_logreg_oracle_vs_cpu(gpu, oracle, kind):
 
 # ---- whole runs -------------------------------------------------------------------------------
 
-@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("run_*.npz"))), ids=os.path.basename)
+@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz"))),
+                         ids=os.path.basename)
 def test_run_golden(gpu, path):
-    """Whole runs against the reference's golden runs, same contract as the CPU oracle's."""
-    from test_oracle_golden import check_run_against_reference
+    """Whole runs against the reference's golden runs, same contract as the CPU oracle's (Option A,
+    FedNL-LS and tracked objective values included)."""
+    from test_oracle_golden import check_run_against_reference, run_kwargs
     z = np.load(path)
     prob = _problem(z)
     fed = gpu.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
-                    workers=int(z["workers"]))
+                    workers=int(z["workers"]), **run_kwargs(z))
     check_run_against_reference(fed, z, prob)
     fed.close()
 
 
-def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None):
+def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None, **opts):
     """GPU and CPU oracle perform the same IEEE operations in the same order: every round's
-    iterate, aggregated gradient, l and every client's message must agree bit for bit."""
+    iterate, aggregated gradient, l and every client's message must agree bit for bit (and f(x_k)
+    and the line-search evaluation count when those options are on)."""
     threads = threads or min(workers, os.cpu_count() or 1)
-    orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads)
-    fed = gpu.FedNL(prob, comp, k, alpha, workers=workers)
+    orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads, **opts)
+    fed = gpu.FedNL(prob, comp, k, alpha, workers=workers, **opts)
     for r in range(rounds):
         go = orc.round()
         gg = fed.round()
         np.testing.assert_array_equal(fed.x(), orc.x(), err_msg=f"round {r}: iterate")
         np.testing.assert_array_equal(fed.grad(), orc.grad(), err_msg=f"round {r}: gradient")
         assert fed.l() == orc.l(), f"round {r}: l"
+        if opts.get("line_search") or opts.get("track_f"):
+            assert fed.f() == orc.f(), f"round {r}: f(x_k)"
+            assert fed.ls_steps() == orc.ls_steps(), f"round {r}: line-search evaluations"
         assert abs(gg - go) <= 1e-14 * go + 1e-300
         for c in range(0, prob.n_clients, max(1, prob.n_clients // 7)):
             io, vo = orc.message(c)
@@ -233,6 +239,28 @@ def test_run_vs_oracle_small(gpu, oracle, comp):
     k = {"topk": 120, "toplek": 150, "randk": 60, "randseqk": 30, "natural": U, "identity": U}[comp]
     alpha = {"randk": k / U, "randseqk": k / U, "natural": 8 / 9}.get(comp, 1.0)
     _compare_runs(gpu, oracle, prob, comp, k, alpha, 8, workers=4)
+
+
+@pytest.mark.parametrize("opts", [dict(line_search=(0.5, 0.5, 5), track_f=True),
+                                  dict(line_search=(0.3, 0.6, 3)),
+                                  dict(option_a=True, track_f=True)], ids=["ls", "ls-short", "option-a"])
+@pytest.mark.parametrize("comp", ["topk", "randk", "natural"])
+def test_run_options_vs_oracle(gpu, oracle, comp, opts):
+    """FedNL-LS (trial points, objective, Armijo test on the device), Option A and tracked
+    objective values, bit for bit against the oracle."""
+    prob = datagen.binary_problem(23, 30, [37, 52, 29, 61, 44, 33], 0.15, 1e-3)
+    U = 30 * 31 // 2
+    k = {"topk": 120, "randk": 60, "natural": U}[comp]
+    alpha = {"randk": k / U, "natural": 8 / 9}.get(comp, 1.0)
+    _compare_runs(gpu, oracle, prob, comp, k, alpha, 12, workers=4, **opts)
+
+
+def test_run_options_vs_oracle_dense_and_w8a(gpu, oracle):
+    prob = datagen.dense_problem(24, 18, [31, 27, 40], 1e-2)
+    _compare_runs(gpu, oracle, prob, "topk", 36, 1.0, 6, workers=2, line_search=(0.5, 0.5, 5), track_f=True)
+    prob = datagen.workload_w8a_like()
+    _compare_runs(gpu, oracle, prob, "toplek", 8 * 301, 1.0, 3, workers=8, threads=os.cpu_count(),
+                  line_search=(0.5, 0.5, 5))
 
 
 def test_run_vs_oracle_dense(gpu, oracle):

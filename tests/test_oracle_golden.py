@@ -11,7 +11,7 @@ import pytest
 from conftest import golden_path
 from ufednl_gb300 import datagen
 
-RUNS = sorted(glob.glob(golden_path("run_*.npz")))
+RUNS = sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz")))
 SELECTS = sorted(glob.glob(golden_path("select_*.npz")))
 RANDS = sorted(glob.glob(golden_path("rand_*.npz")))
 PPS = sorted(glob.glob(golden_path("pp_*.npz")))
@@ -25,6 +25,14 @@ def _full(m, d, lda):
     full = np.zeros((d, lda))
     full[:, :d] = m.T          # full[j] = column j (column-major storage)
     return full.reshape(-1)
+
+
+def run_kwargs(z):
+    """Option A / FedNL-LS / tracking switches of an extended golden run (runx_*.npz)."""
+    if "f" not in z:
+        return {}
+    ls = (float(z["ls_c"]), float(z["ls_gamma"]), int(z["ls_max"])) if int(z["line_search"]) else None
+    return dict(option_a=bool(int(z["option_a"])), line_search=ls, track_f=bool(int(z["track_f"])))
 
 
 def check_run_against_reference(fed, z, prob):
@@ -69,6 +77,9 @@ def check_run_against_reference(fed, z, prob):
         if diverged_at is None and (r < dump or not chaotic):
             assert abs(g - z["gnorm"][r]) <= 1e-8 * z["gnorm"][r] + 1e-14 * z["gnorm"][0]
             assert abs(fed.l() - z["l"][r]) <= 1e-10 * z["l"][r] + 1e-12 * np.max(z["l"])
+        if diverged_at is None and "f" in z:       # objective at x_k and line-search evaluations
+            assert abs(fed.f() - z["f"][r]) <= 1e-12 * abs(z["f"][r]), (r, fed.f(), z["f"][r])
+            assert fed.ls_steps() == int(z["ls_steps"][r])
     if diverged_at is not None:
         assert diverged_at >= 1                 # round 0 never diverges
         gref = z["gnorm"][-1]
@@ -83,7 +94,7 @@ def test_run_matches_reference(oracle, path):
     z = np.load(path)
     prob = _problem(z)
     fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
-                       workers=int(z["workers"]))
+                       workers=int(z["workers"]), **run_kwargs(z))
     check_run_against_reference(fed, z, prob)
     fed.close()
 
@@ -128,6 +139,20 @@ def test_pp_run_matches_reference(oracle, path):
                        workers=1, clients_per_round=int(z["tau"]), client_seed=int(z["sel_seed"]))
     check_pp_against_reference(fed, z, prob)
     fed.close()
+
+
+def test_log_is_faithful(oracle):
+    """The oracle's own logarithm (shared bit for bit with the kernels) is within one ulp of the
+    correctly rounded libm log over the sigmoid range, wide magnitudes and subnormals."""
+    import math
+    L = oracle.lib()
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.random(20000), np.exp(rng.uniform(-700, 700, 20000)),
+                         1 + rng.uniform(-1e-6, 1e-6, 5000), [5e-324, 1e-310, 1.0, 2.0, 0.5, 1e308]])
+    for x in xs:
+        a, b = L.orc_log(float(x)), math.log(float(x))
+        assert abs(a - b) <= math.ulp(b), (x, a, b)
+    assert L.orc_log(1.0) == 0.0 and L.orc_log(0.0) == -np.inf and np.isnan(L.orc_log(-1.0))
 
 
 @pytest.mark.parametrize("path", SELECTS, ids=lambda p: os.path.basename(p))

@@ -2,7 +2,8 @@
 
     python -m ufednl_gb300.build
 
-One nvcc invocation, one -gencode; the output goes to ufednl_gb300/_build/.
+One nvcc invocation (the CUDA round engine and the host-side local driver), one -gencode; the
+output goes to ufednl_gb300/_build/.
 """
 from __future__ import annotations
 
@@ -15,7 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libfednl_gpu.so")
-SOURCES = [os.path.join(PKG, "csrc", "fednl_gpu.cu")]
+SOURCES = [os.path.join(PKG, "csrc", "fednl_gpu.cu"), os.path.join(PKG, "csrc", "fednl_local.cpp")]
 DEPS = SOURCES + [os.path.join(PKG, "csrc", f) for f in os.listdir(os.path.join(PKG, "csrc"))] + \
     [os.path.join(REPO, "include", "fednl_gpu.h")]
 

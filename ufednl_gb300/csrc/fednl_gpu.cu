@@ -152,7 +152,7 @@ struct Marks {
 
 int mark(fednl_handle h, Marks* m, const char* name)
 {
-    if (!m) return FEDNL_OK;
+    if (!m || m->next >= m->ev->size()) return FEDNL_OK;
     if (m->names && m->names->size() <= m->next) m->names->push_back(name);
     CK(cudaEventRecord((*m->ev)[m->next], h->stream));
     m->next += 1;
@@ -251,8 +251,37 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
     MARK("k_aggregate");
     k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads, kAggThreads, 0, st>>>(P);
     CKL();
+    if (P.fmode) {       // f(x_k) from the round's sigmoid values
+        MARK("k_fclient");
+        k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, nullptr);
+        CKL();
+        MARK("k_fmaster");
+        k_fmaster<<<1, 32, 0, st>>>(P, P.stats + 2);
+        CKL();
+    }
+    const fednl_problem_desc& D = h->desc;
+    const double* lptr = D.option_a ? nullptr : P.stats + 1;      // Option A: H + lambda I
     MARK("k_chol_coop");
-    CK(launch_chol(P, h->chol_grid, st, P.H, 0, P.stats + 1, 0.0, P.g, P.dx, P.x, 1));
+    CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1));
+    if (D.line_search) {
+        MARK("k_ls_init");
+        k_ls_init<<<1, 256, 0, st>>>(P);
+        CKL();
+        for (int it = 0; it < D.ls_max_steps; ++it) {
+            MARK("k_ls_trial");
+            k_ls_trial<<<(h->d + 255) / 256, 256, 0, st>>>(P);
+            CKL();
+            MARK("k_ls_margin");
+            k_ls_margin<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+            CKL();
+            MARK("k_fclient");
+            k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, P.ls);
+            CKL();
+            MARK("k_ls_check");
+            k_ls_check<<<1, 32, 0, st>>>(P, D.ls_c, D.ls_gamma);
+            CKL();
+        }
+    }
     MARK("end");
     return FEDNL_OK;
 }
@@ -294,6 +323,9 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
         if (D.reserved[i]) return fail(FEDNL_EINVAL, "reserved fields must be zero");
     if (D.clients_per_round < 0 || D.clients_per_round > D.n_clients)
         return fail(FEDNL_EINVAL, "clients_per_round %d outside [0, n_clients]", D.clients_per_round);
+    if (D.line_search && (D.clients_per_round > 0 || D.ls_max_steps < 1 || !(D.ls_c > 0.0) || !(D.ls_gamma > 0.0) ||
+                          !(D.ls_gamma < 1.0)))
+        return fail(FEDNL_EINVAL, "line search needs plain FedNL, max steps >= 1, c > 0 and 0 < gamma < 1");
     int lda = D.lda ? D.lda : (D.d + 3) / 4 * 4;
     if (lda < D.d) return fail(FEDNL_EINVAL, "lda %d < d %d", lda, D.d);
     long long U = (long long)D.d * (D.d + 1) / 2;
@@ -362,6 +394,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     P.hist_cap = 1 << 16;
     P.pp = h->pp;
     P.n_act = h->tau;
+    P.fmode = (D.line_search || D.track_f) && !h->pp;
     size_t ncU = (size_t)h->nc * h->ustr;
     Arena& A = h->state;
     A.want((int**)&P.ns, h->nc);
@@ -395,8 +428,14 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     A.want(&P.hist, P.hist_cap);
     A.want(&P.round_ctr, 1);
     A.want(&P.status, 1);
-    A.want(&P.stats, 2);
+    A.want(&P.stats, 4);
     A.want(&P.bar, 4);
+    if (P.fmode) {
+        A.want(&P.fterm, h->S);
+        A.want(&P.fi, h->nc);
+        A.want(&P.xprev, h->d);
+        A.want(&P.ls, 5);
+    }
     if (h->pp) {
         A.want((int**)&P.act, h->nc);
         A.want(&P.is_sel, h->nc);
@@ -650,6 +689,24 @@ int fednl_gpu_round(fednl_handle h, fednl_round_stats* stats)
         stats->l = st[1];
     }
     return rc;
+}
+
+double fednl_gpu_get_f(fednl_handle h)
+{
+    if (!h || !h->dev.fmode) return NAN;
+    double v = NAN;
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(&v, h->dev.stats + 2, 8, cudaMemcpyDeviceToHost);
+    return v;
+}
+
+int32_t fednl_gpu_get_ls_steps(fednl_handle h)
+{
+    if (!h || !h->desc.line_search) return 0;
+    double v = 0.0;
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(&v, h->dev.ls + 3, 8, cudaMemcpyDeviceToHost);
+    return (int32_t)v;
 }
 
 int fednl_gpu_get_selected(fednl_handle h, int32_t* clients, int32_t* count)
@@ -1127,7 +1184,7 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
 {
     if (!h || rounds < 1 || !n_kernels || !kernel_ms) return fail(FEDNL_EINVAL, "bad argument");
     if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
-    const int kMaxMarks = 33;
+    const int kMaxMarks = 65;
     std::vector<std::vector<cudaEvent_t>> ev(rounds, std::vector<cudaEvent_t>(kMaxMarks, nullptr));
     for (auto& v : ev)
         for (auto& e : v) CK(cudaEventCreate(&e));
@@ -1146,7 +1203,7 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
     cudaError_t e = cudaStreamSynchronize(h->stream);
     int nk = (int)nmarks - 1;
     if (rc == FEDNL_OK && e == cudaSuccess) {
-        for (int t = 0; t < nk && t < 32; ++t) {
+        for (int t = 0; t < nk && t < 64; ++t) {
             double acc = 0.0;
             for (int r = 0; r < rounds; ++r) {
                 float ms = 0.f;
@@ -1155,10 +1212,10 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
             }
             kernel_ms[t] = acc / rounds;
         }
-        *n_kernels = std::min(nk, 32);
+        *n_kernels = std::min(nk, 64);
         if (names && names_len > 0) {
             std::string all;
-            for (int t = 0; t < nk && t < 32; ++t) {
+            for (int t = 0; t < nk && t < 64; ++t) {
                 if (t) all += ";";
                 all += nm[t];
             }

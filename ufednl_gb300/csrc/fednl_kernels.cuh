@@ -86,6 +86,12 @@ struct Dev {
     double* gprev;          // [d] running mean of the directions
     double* lprev;          // [1] running mean of Lk
     double* tg;             // [d] true gradient at the round's starting iterate
+    // objective values (tracking) and FedNL-LS
+    int fmode;              // 1: form -log sigma_s per sample and f_i per client every round
+    double* fterm;          // [S] -log sigma_s at the last evaluated point
+    double* fi;             // [nc] f_i at the last evaluated point
+    double* xprev;          // [d] x_k during the line search
+    double* ls;             // [5] line search: t, -(dx . g), done, evaluations, solve succeeded
 };
 
 // ---- helpers -------------------------------------------------------------------------------
@@ -201,6 +207,55 @@ __device__ __forceinline__ double fednl_exp(double x)
     return __dmul_rn(p, pow2i(k));
 }
 
+// Natural logarithm (the CPU oracle's orc_log, operation for operation): x = 2^e m, m in
+// [sqrt(1/2), sqrt(2)), log m = 2 atanh((m - 1)/(m + 1)) with the quotient as a double-double, the
+// odd series to s^23/23 for the tail, e ln 2 in two parts.  Below one ulp of error.
+__device__ __forceinline__ double fednl_log(double x)
+{
+    if (x != x) return x;
+    if (x < 0.0) return __longlong_as_double(0x7ff8000000000000ll);
+    if (x == 0.0) return __longlong_as_double((long long)0xfff0000000000000ull);
+    if (x == __longlong_as_double(0x7ff0000000000000ll)) return x;
+    long long b = __double_as_longlong(x);
+    int e = 0;
+    if ((b >> 52) == 0) {
+        x = __dmul_rn(x, 18014398509481984.0);
+        b = __double_as_longlong(x);
+        e = -54;
+    }
+    e += (int)(b >> 52) - 1023;
+    double m = __longlong_as_double((b & 0x000fffffffffffffll) | 0x3ff0000000000000ll);
+    if (m > 1.4142135623730951) {
+        m = __dmul_rn(m, 0.5);
+        e += 1;
+    }
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    const double f = __dsub_rn(m, 1.0);
+    double g_hi, g_lo;
+    two_sum(m, 1.0, g_hi, g_lo);
+    const double s_hi = __ddiv_rn(f, g_hi);
+    const double r = __dsub_rn(fma(-s_hi, g_hi, f), __dmul_rn(s_hi, g_lo));
+    const double s_lo = __ddiv_rn(r, g_hi);
+    const double z = __dmul_rn(s_hi, s_hi);
+    double q = 1.0 / 23.0;
+    q = fma(q, z, 1.0 / 21.0);
+    q = fma(q, z, 1.0 / 19.0);
+    q = fma(q, z, 1.0 / 17.0);
+    q = fma(q, z, 1.0 / 15.0);
+    q = fma(q, z, 1.0 / 13.0);
+    q = fma(q, z, 1.0 / 11.0);
+    q = fma(q, z, 1.0 / 9.0);
+    q = fma(q, z, 1.0 / 7.0);
+    q = fma(q, z, 1.0 / 5.0);
+    q = fma(q, z, 1.0 / 3.0);
+    const double tail = __dmul_rn(__dmul_rn(__dmul_rn(s_hi, z), q), 2.0);
+    const double ed = (double)e;
+    double h, l;
+    two_sum(__dmul_rn(ed, ln2_hi), __dmul_rn(s_hi, 2.0), h, l);
+    l = __dadd_rn(l, __dadd_rn(__dadd_rn(__dmul_rn(s_lo, 2.0), tail), __dmul_rn(ed, ln2_lo)));
+    return __dadd_rn(h, l);
+}
+
 __device__ __forceinline__ double fednl_sigmoid(double m)
 {
     return __ddiv_rn(1.0, __dadd_rn(1.0, fednl_exp(-m)));
@@ -249,6 +304,7 @@ __global__ void k_margin_binary(Dev P, int S)
     P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
     double q = __dmul_rn(z1, -inv_m);
     P.qb[s] = (b == 1.0) ? q : __dmul_rn(-1.0, q);
+    if (P.fmode) P.fterm[s] = -fednl_log(sig);
 }
 
 // dense features: column s of Atr is b_s * a_s (logistic_regression.h:45-75)
@@ -269,6 +325,7 @@ __global__ void k_margin_dense(Dev P, int S)
     double z1 = __dsub_rn(1.0, sig);
     P.Dv[s] = __dmul_rn(inv_m, __dmul_rn(z1, sig));
     P.qb[s] = __dmul_rn(z1, -inv_m);   // dense: the label enters through u
+    if (P.fmode) P.fterm[s] = -fednl_log(sig);
 }
 
 // ---- 2. client gradients g_c = lambda x + sum_s Atr[:, s] q_s (samples in order) ----------
@@ -1204,13 +1261,16 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     __shared__ double s_inv[kCholNB];
     __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
+    __shared__ double s_yb[32];
+    int ent_nb = -1;
     const double l = lptr ? *lptr : lval;
     const int d = P.d;
     const int D = d + 1;                       // augmented by the right-hand side
     const int UA = D * (D + 1) / 2;
     double* A = P.work;                        // [UA]
     const unsigned G = gridDim.x;
-    const int tid = threadIdx.x, lane = tid & 31;
+    if (P.ls && blockIdx.x == 0 && threadIdx.x == 0) P.ls[4] = 0.0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int gtid = blockIdx.x * blockDim.x + tid, gthreads = G * blockDim.x;
     for (int p = gtid; p < UA; p += gthreads) {
         int i, j;
@@ -1238,57 +1298,82 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             Sb[i][sl] = A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)];
         }
         // block entries (i, j), i <= j, listed by descending i: those with i > k are a prefix
-        for (int e = tid; e < nb * (nb + 1) / 2; e += blockDim.x) {
-            int i = nb - 1, rem = e;
-            while (rem >= nb - i) {
-                rem -= nb - i;
-                --i;
+        if (nb != ent_nb) {
+            for (int e = tid; e < nb * (nb + 1) / 2; e += blockDim.x) {
+                int i = nb - 1, rem = e;
+                while (rem >= nb - i) {
+                    rem -= nb - i;
+                    --i;
+                }
+                s_ent[e] = (unsigned short)((i << 8) | (i + rem));
             }
-            s_ent[e] = (unsigned short)((i << 8) | (i + rem));
+            ent_nb = nb;
         }
         if (tid == 0) s_fail = 0;
         __syncthreads();
-        // column loop (the unblocked right-looking steps restricted to the panel's rows): warps 0
-        // and 1 both form the pivot from the broadcast diagonal entry (no barrier between them);
-        // warp 0 scales the block's row k, warp 1 the slab's; then all threads apply the rank-1
-        // update to the block and slab entries below row k.
-        for (int k = 0; k < nb; ++k) {
-            double r_keep = 0.0;
-            if (tid < 64) {
-                double a = Db[k][k];
-                bool bad = false;
-                if (a < 0) {
-                    if (a > -0.0) a = 0.0;
-                    else bad = true;
-                }
-                const double r = sqrt(a);
-                const double inv = 1.0 / r;
-                if (tid < 32) {
-                    const int j = k + 1 + lane;
-                    if (j < nb) Db[k][j] = __dmul_rn(Db[k][j], inv);
-                    if (lane == 0) {     // r_kk is stored after the barrier: warp 1 may still read a_kk
-                        r_keep = r;
-                        s_inv[k] = inv;
-                        if (bad) s_fail = 1;
-                    }
-                } else if (lane < ns) {
-                    Sb[k][lane] = __dmul_rn(Sb[k][lane], inv);
+        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Warp 0
+        // owns the pivot chain: at step k it applies step k to row k+1 (block and slab), forms the
+        // pivot of row k+1 (every lane, from the broadcast entry) and scales that row, while warps
+        // 1..7 apply step k to rows k+2 and below; one CTA barrier per column.
+        auto pivot_row = [&](int kk) {
+            const double a0 = Db[kk][kk];
+            const long long ab = __double_as_longlong(a0);
+            const long long mag = ab & 0x7fffffffffffffffll;
+            const bool bad = ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll;   // a < 0 (not NaN, not -0)
+            const double r = sqrt(a0);
+            const double inv = 1.0 / r;
+            const int nd = nb - 1 - kk;
+            for (int it = lane; it < nd + ns; it += 32) {
+                if (it < nd) {
+                    const int j = kk + 1 + it;
+                    Db[kk][j] = __dmul_rn(Db[kk][j], inv);
+                } else {
+                    Sb[kk][it - nd] = __dmul_rn(Sb[kk][it - nd], inv);
                 }
             }
-            __syncthreads();
+            __syncwarp();
+            if (lane == 0) {
+                Db[kk][kk] = r;
+                s_inv[kk] = inv;
+                if (bad) s_fail = 1;
+            }
+        };
+        if (warp == 0) pivot_row(0);
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
             if (s_fail) break;
-            if (tid == 0) Db[k][k] = r_keep;
-            const int nblk = (nb - 1 - k) * (nb - k) / 2;
-            const int nall = nblk + (nb - 1 - k) * ns;
-            for (int e = tid; e < nall; e += blockDim.x) {
-                if (e < nblk) {
-                    const unsigned v = s_ent[e];
-                    const int i = (int)(v >> 8), j = (int)(v & 0xffu);
-                    Db[i][j] = fma(-Db[k][i], Db[k][j], Db[i][j]);
-                } else {
-                    const int q = e - nblk;
-                    const int i = k + 1 + q / ns, sl = q - (q / ns) * ns;
-                    Sb[i][sl] = fma(-Db[k][i], Sb[k][sl], Sb[i][sl]);
+            if (warp == 0) {
+                if (k + 1 < nb) {
+                    const int nd = nb - 1 - k;              // row k+1: j = k+1 .. nb-1, then the slab
+                    const double rk = Db[k][k + 1];
+                    for (int it = lane; it < nd + ns; it += 32) {
+                        if (it < nd) {
+                            const int j = k + 1 + it;
+                            Db[k + 1][j] = fma(-rk, Db[k][j], Db[k + 1][j]);
+                        } else {
+                            const int sl = it - nd;
+                            Sb[k + 1][sl] = fma(-rk, Sb[k][sl], Sb[k + 1][sl]);
+                        }
+                    }
+                    __syncwarp();
+                    pivot_row(k + 1);
+                }
+            } else {
+                const int rows = nb - 2 - k;               // rows k+2 .. nb-1
+                if (rows > 0) {
+                    const int nblk = rows * (rows + 1) / 2;
+                    const int nall = nblk + rows * ns;
+                    for (int e = tid - 32; e < nall; e += kCoopThreads - 32) {
+                        if (e < nblk) {
+                            const unsigned v = s_ent[e];
+                            const int i = (int)(v >> 8), j = (int)(v & 0xffu);
+                            Db[i][j] = fma(-Db[k][i], Db[k][j], Db[i][j]);
+                        } else {
+                            const int q = e - nblk;
+                            const int i = k + 2 + q / ns, sl = q - (q / ns) * ns;
+                            Sb[i][sl] = fma(-Db[k][i], Sb[k][sl], Sb[i][sl]);
+                        }
+                    }
                 }
             }
             __syncthreads();
@@ -1337,8 +1422,16 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                 const int i = c1 + ii, j = c1 + jj;
                 const double* ci = A + up_pos(0, i);
                 const double* cj = A + up_pos(0, j);
+                double u[kCholNB], w[kCholNB];     // panel rows of columns i and j, loaded ahead
+#pragma unroll
+                for (int k = 0; k < kCholNB; ++k) {
+                    u[k] = k < nb ? ci[c0 + k] : 0.0;
+                    w[k] = k < nb ? cj[c0 + k] : 0.0;
+                }
                 double a = cj[i];
-                for (int k = c0; k < c1; ++k) a = fma(-ci[k], cj[k], a);
+#pragma unroll
+                for (int k = 0; k < kCholNB; ++k)
+                    if (k < nb) a = fma(-u[k], w[k], a);
                 A[up_pos(i, j)] = a;
             }
         }
@@ -1368,21 +1461,35 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         __syncthreads();
         for (int b1 = d; b1 > 0; b1 -= 32) {
             const int b0 = max(0, b1 - 32);
-            if (tid < 32) {
-                const int nbk = b1 - b0;
+            const int nbk = b1 - b0;
+            if (tid < 32) {           // the block's triangle and 1/r_tt in registers, then the chain
+                double ar[32];
+#pragma unroll
+                for (int s = 0; s < 32; ++s) ar[s] = (lane < s && s < nbk) ? A[up_pos(b0 + lane, b0 + s)] : 0.0;
+                const double myinv = (lane < nbk) ? P.rinv[b0 + lane] : 0.0;
                 double v = (lane < nbk) ? y[b0 + lane] : 0.0;
-                for (int s = nbk - 1; s >= 0; --s) {
-                    const int t = b0 + s;
-                    if (lane == s) v = __dmul_rn(v, P.rinv[t]);
-                    double yt = __shfl_sync(0xffffffffu, v, s);
-                    if (lane < s) v = fma(-A[up_pos(b0 + lane, t)], yt, v);
+#pragma unroll
+                for (int s = 31; s >= 0; --s) {
+                    if (s < nbk) {
+                        if (lane == s) v = __dmul_rn(v, myinv);
+                        const double yt = __shfl_sync(0xffffffffu, v, s);
+                        if (lane < s) v = fma(-ar[s], yt, v);
+                    }
                 }
-                if (lane < nbk) y[b0 + lane] = v;
+                if (lane < nbk) {
+                    y[b0 + lane] = v;
+                    s_yb[lane] = v;
+                }
             }
             __syncthreads();
             for (int i = tid; i < b0; i += blockDim.x) {
+                double av[32];
+#pragma unroll
+                for (int s = 0; s < 32; ++s) av[s] = (s < nbk) ? A[up_pos(i, b0 + s)] : 0.0;
                 double v = y[i];
-                for (int t = b1 - 1; t >= b0; --t) v = fma(-A[up_pos(i, t)], y[t], v);
+#pragma unroll
+                for (int s = 31; s >= 0; --s)
+                    if (s < nbk) v = fma(-av[s], s_yb[s], v);
                 y[i] = v;
             }
             __syncthreads();
@@ -1397,6 +1504,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             if (r < P.hist_cap) P.hist[r] = P.stats[0];
             *P.round_ctr = r + 1;
         }
+        if (P.ls && tid == 0) P.ls[4] = 1.0;
     }
     return;
 timeout:
@@ -1481,6 +1589,126 @@ __global__ void k_natural_pack(const double* in, long long n, unsigned char* pac
     packed[3 * q + 2] = (unsigned char)((v >> 16) & 0xFF);
 }
 
+
+// ---- 8c. objective values and FedNL-LS --------------------------------------------------------
+// f_i = -mean_s log sigma_s + (lambda / 2) ||x||^2 (evaluateFunction(x, margin, sigmoid),
+// logistic_regression.h:119-123); the per-sample terms come from the margin kernels.  Sums in the
+// CPU oracle's chunked order (halving tree over 32 terms, chunks in order).
+__device__ __forceinline__ double warp_chunked_sum(const double* v, int n)
+{
+    const int lane = threadIdx.x & 31;
+    double total = 0.0;
+    for (int base = 0; base < n; base += 32) {
+        const double cs = chunk_tree(base + lane < n ? v[base + lane] : 0.0);
+        total = __dadd_rn(total, __shfl_sync(0xffffffffu, cs, 0));
+    }
+    return total;
+}
+
+__device__ __forceinline__ double warp_chunked_sumsq(const double* v, int n)
+{
+    const int lane = threadIdx.x & 31;
+    double total = 0.0;
+    for (int base = 0; base < n; base += 32) {
+        const double t = base + lane < n ? v[base + lane] : 0.0;
+        const double cs = chunk_tree(__dmul_rn(t, t));
+        total = __dadd_rn(total, __shfl_sync(0xffffffffu, cs, 0));
+    }
+    return total;
+}
+
+// one warp per client; skipped once the line search has finished (gate = P.ls)
+__global__ void k_fclient(Dev P, const double* x, const double* gate)
+{
+    if (gate && gate[2] != 0.0) return;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= P.nc) return;
+    const int n = P.ns[c];
+    const double loss = __ddiv_rn(warp_chunked_sum(P.fterm + P.soff[c], n), (double)n);
+    const double xs = warp_chunked_sumsq(x, P.d);
+    if ((threadIdx.x & 31) == 0) P.fi[c] = __dadd_rn(loss, __dmul_rn(__dmul_rn(P.lambda, 0.5), xs));
+}
+
+// master: f = (chunked sum of f_i) / n into out (function_aggregation, TrainLoop.h:1511-1541)
+__global__ void k_fmaster(Dev P, double* out)
+{
+    const double f = __dmul_rn(warp_chunked_sum(P.fi, P.nc), P.inv_n);
+    if (threadIdx.x == 0) *out = f;
+}
+
+// FedNL-LS (TrainLoop.h:1543-1640): t = 1, -(dx . g) in the chunked order, x_k kept; nothing to
+// search when the solve failed
+__global__ void k_ls_init(Dev P)
+{
+    __shared__ double s_dg[1024];
+    for (int i = threadIdx.x; i < P.d && i < 1024; i += blockDim.x) s_dg[i] = __dmul_rn(P.dx[i], P.g[i]);
+    for (int i = threadIdx.x; i < P.d; i += blockDim.x) P.xprev[i] = P.x[i];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double dg = 0.0;
+        if (P.d <= 1024) {
+            dg = warp_chunked_sum(s_dg, P.d);
+        } else {       // larger d: the same chunked order, terms formed on the fly
+            const int lane = threadIdx.x;
+            for (int base = 0; base < P.d; base += 32) {
+                const int i = base + lane;
+                const double cs = chunk_tree(i < P.d ? __dmul_rn(P.dx[i], P.g[i]) : 0.0);
+                dg = __dadd_rn(dg, __shfl_sync(0xffffffffu, cs, 0));
+            }
+        }
+        if (threadIdx.x == 0) {
+            P.ls[0] = 1.0;
+            P.ls[1] = -dg;
+            P.ls[2] = P.ls[4] != 0.0 ? 0.0 : 1.0;
+            P.ls[3] = 0.0;
+        }
+    }
+}
+
+// trial point x = x_k - t dx
+__global__ void k_ls_trial(Dev P)
+{
+    if (P.ls[2] != 0.0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.d) P.x[i] = __dsub_rn(P.xprev[i], __dmul_rn(P.ls[0], P.dx[i]));
+}
+
+// -log sigma_s at the trial point
+__global__ void k_ls_margin(Dev P, int S)
+{
+    if (P.ls[2] != 0.0) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    double m;
+    const double b = P.lab[s];
+    if (P.A == nullptr) {
+        double acc = 0.0;
+        for (int t = P.rowptr[s]; t < P.rowptr[s + 1]; ++t) acc = __dadd_rn(acc, P.x[P.colidx[t]]);
+        m = (b == 1.0) ? acc : -acc;
+    } else {
+        const double* a = P.A + (size_t)s * P.d;
+        double acc = 0.0;
+        for (int i = 0; i < P.d; ++i) {
+            const double u = (b == 1.0) ? a[i] : __dmul_rn(a[i], -1.0);
+            acc = __dadd_rn(acc, __dmul_rn(u, P.x[i]));
+        }
+        m = acc;
+    }
+    P.fterm[s] = -fednl_log(fednl_sigmoid(m));
+}
+
+// Armijo test f(x) <= f(x_k) + (c t)(-(dx . g)); t *= gamma after a failure
+__global__ void k_ls_check(Dev P, double c, double gamma)
+{
+    if (P.ls[2] != 0.0) return;
+    const double fr = __dmul_rn(warp_chunked_sum(P.fi, P.nc), P.inv_n);
+    if (threadIdx.x == 0) {
+        P.ls[3] = __dadd_rn(P.ls[3], 1.0);
+        const double t = P.ls[0];
+        if (fr <= __dadd_rn(P.stats[2], __dmul_rn(__dmul_rn(c, t), P.ls[1]))) P.ls[2] = 1.0;
+        else P.ls[0] = __dmul_rn(t, gamma);
+    }
+}
 
 // ---- 9. FedNL-PP (dopt/bin_fednl_local_pp) ----------------------------------------------------
 // Client sampler (TrainLoop.h:1150-1157): a fresh 0..n-1 is shuffled for tau steps by the partial

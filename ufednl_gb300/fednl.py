@@ -37,22 +37,27 @@ class ProblemDesc(C.Structure):
                 ("compressor", C.c_int32), ("k", C.c_int32), ("alpha", C.c_double),
                 ("workers", C.c_int32), ("seed_base", C.c_uint32), ("toplek_seed", C.c_uint32),
                 ("feature_format", C.c_int32), ("clients_per_round", C.c_int32),
-                ("client_seed", C.c_uint32), ("reserved", C.c_int32 * 2)]
+                ("client_seed", C.c_uint32), ("option_a", C.c_int32), ("line_search", C.c_int32),
+                ("ls_c", C.c_double), ("ls_gamma", C.c_double), ("ls_max_steps", C.c_int32), ("track_f", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class RoundStats(C.Structure):
     _fields_ = [("round", C.c_int32), ("status", C.c_int32), ("grad_norm", C.c_double), ("l", C.c_double)]
 
 
+# fednl_result_callback: (dimension, ||g||, ||g||^2/(2 mu), 2||g||^2/mu)
+RESULT_CALLBACK = C.CFUNCTYPE(None, C.c_int, C.c_double, C.c_double, C.c_double)
+
 # every symbol declared in include/fednl_gpu.h
 EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_data", "fednl_gpu_init_shifts",
            "fednl_gpu_round", "fednl_gpu_run", "fednl_gpu_get_x", "fednl_gpu_set_x", "fednl_gpu_get_grad",
            "fednl_gpu_get_H", "fednl_gpu_get_shift", "fednl_gpu_get_l", "fednl_gpu_get_lk",
-           "fednl_gpu_get_message", "fednl_gpu_get_selected", "fednl_gpu_get_true_grad", "fednl_gpu_get_dir",
+           "fednl_gpu_get_message", "fednl_gpu_get_f", "fednl_gpu_get_ls_steps", "fednl_gpu_get_selected", "fednl_gpu_get_true_grad", "fednl_gpu_get_dir",
            "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
            "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
-           "fednl_gpu_last_error"]
+           "fednl_gpu_last_error", "fednl_gpu_execute_local"]
 
 _lib = None
 
@@ -104,6 +109,12 @@ def load(build_if_missing: bool = True):
     L.fednl_gpu_get_l.restype = C.c_double
     L.fednl_gpu_get_lk.argtypes = [vp, C.c_int32]
     L.fednl_gpu_get_lk.restype = C.c_double
+    L.fednl_gpu_get_f.argtypes = [vp]
+    L.fednl_gpu_get_f.restype = C.c_double
+    L.fednl_gpu_get_ls_steps.argtypes = [vp]
+    L.fednl_gpu_get_ls_steps.restype = C.c_int32
+    L.fednl_gpu_execute_local.argtypes = [C.c_char_p, RESULT_CALLBACK]
+    L.fednl_gpu_execute_local.restype = C.c_int
     L.fednl_gpu_last_error.argtypes = []
     L.fednl_gpu_last_error.restype = C.c_char_p
     _lib = L
@@ -209,7 +220,8 @@ class FedNL:
 
     def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
                  seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0,
-                 clients_per_round: int = 0, client_seed: int = 1234):
+                 clients_per_round: int = 0, client_seed: int = 1234, option_a: bool = False,
+                 line_search=None, track_f: bool = False):
         self.d = prob.d
         self.lda = lda or reference_lda(prob.d)
         self.n_clients = prob.n_clients
@@ -218,7 +230,10 @@ class FedNL:
         self.compressor = comp
         desc = ProblemDesc(self.d, self.lda, self.n_clients, _ip(self._ns), float(prob.lam), comp, int(k),
                            float(alpha), int(workers), int(seed_base), int(toplek_seed), int(feature_format),
-                           int(clients_per_round or 0), int(client_seed), (C.c_int32 * 2)(0, 0))
+                           int(clients_per_round or 0), int(client_seed), 1 if option_a else 0,
+                           1 if line_search else 0, float(line_search[0]) if line_search else 0.5,
+                           float(line_search[1]) if line_search else 0.5, int(line_search[2]) if line_search else 5,
+                           1 if track_f else 0, (C.c_int32 * 2)(0, 0))
         self.pp = bool(clients_per_round)
         h = C.c_void_p()
         _check(load().fednl_gpu_create(C.byref(desc), C.byref(h)))
@@ -264,9 +279,9 @@ class FedNL:
     def profile_kernels(self, rounds: int, flush_bytes: int = 0):
         """Mean per-launch time of every kernel of a round: {name: ms}, in launch order."""
         n = np.zeros(1, dtype=np.int32)
-        ms = np.zeros(32)
-        buf = C.create_string_buffer(2048)
-        _check(load().fednl_gpu_profile_kernels(self._h, rounds, flush_bytes, _ip(n), _dp(ms), buf, 2048))
+        ms = np.zeros(64)
+        buf = C.create_string_buffer(4096)
+        _check(load().fednl_gpu_profile_kernels(self._h, rounds, flush_bytes, _ip(n), _dp(ms), buf, 4096))
         names = buf.value.decode().split(";")
         return [(names[t], float(ms[t])) for t in range(int(n[0]))]
 
@@ -300,6 +315,13 @@ class FedNL:
     def lk(self, c: int) -> float:
         return load().fednl_gpu_get_lk(self._h, c)
 
+    def f(self) -> float:
+        """f(x) at the last round's starting iterate (line search or track_f)."""
+        return load().fednl_gpu_get_f(self._h)
+
+    def ls_steps(self) -> int:
+        return load().fednl_gpu_get_ls_steps(self._h)
+
     def selected(self) -> np.ndarray:
         """FedNL-PP: the last round's sampled clients, ascending."""
         out = np.empty(self.n_clients, dtype=np.int32)
@@ -325,3 +347,18 @@ class FedNL:
         _check(load().fednl_gpu_get_message(self._h, c, _up(idx), _dp(val), _ip(cnt)))
         n = int(cnt[0])
         return idx[:n].copy(), val[:n].copy()
+
+
+# ---- the reference's local driver ---------------------------------------------------------------
+
+def execute_local(command: str):
+    """doptExecuteLocal (bin_fednl_local/src/mainShared.cpp:15-38) on the GPU engine: runs the
+    bin_fednl_local command line and returns (return code, callback values or None)."""
+    got = []
+
+    @RESULT_CALLBACK
+    def cb(d, gnorm, fgap, xgap):
+        got.append((int(d), float(gnorm), float(fgap), float(xgap)))
+
+    rc = load().fednl_gpu_execute_local(command.encode(), cb)
+    return rc, (got[0] if got else None)
