@@ -226,6 +226,15 @@ typedef void (*fednl_result_callback)(int x_dimension, double grad_norm, double 
  * -4 parse error, -5 split error, -6 saving failed, -7 internal error, -8 unknown debug mode). */
 int fednl_gpu_execute_local(const char* command, fednl_result_callback callback);
 
+/* The reference's LIBSVM text loader (dataset_loader_fs.h:380-885 as TrainLoop.h:124-180 drives
+ * it): labels remapped to +-1 around the mean of the smallest and largest label, attribute
+ * indices shifted by the smallest index found, optional intercept attribute (= 1) last.  Host only,
+ * no device needed.  Call with features = labels = NULL to get n_samples and d, then again with
+ * buffers of n_samples * d (row-major) and n_samples doubles.  Returns 0, -3 (file missing) or -4
+ * (parse error, or not exactly two label values). */
+int fednl_gpu_load_libsvm(const char* path, int32_t add_intercept, int32_t* n_samples, int32_t* d,
+                          double* features, double* labels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,8 @@
 #include "dopt/random/include/RandomGenIntegerLinear.h"
 #include "dopt/random/include/Shuffle.h"
 #include "dopt/system/include/FloatUtils.h"
+#include "dopt/optimization_problems/include/ml/dataset_loader_fs.h"
+#include "dopt/copylocal/include/Data.h"
 
 #include <barrier>
 #include <cstdio>
@@ -418,6 +420,48 @@ static int cmd_pp(const char* in_path, const char* out_path)
     return 0;
 }
 
+// ---- libsvm: the reference's text loader (dataset_loader_fs.h) as bin_fednl_local drives it
+// (TrainLoop.h:124-180): statistics pass, then createDataset with label remapping and optional
+// intercept.  Output: status, d, n, then features [n][d] and labels [n].
+static int cmd_libsvm(const char* in_path, const char* out_path, int add_intercept)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    std::string text;
+    char buf[65536];
+    size_t got;
+    while ((got = fread(buf, 1, sizeof(buf), fi)) > 0) text.append(buf, got);
+    fclose(fi);
+    Writer W{fo};
+    auto line_sep = [](char c) { return c == '\n' || c == '\r'; };
+    auto field_sep = [](char c) { return c == '\t' || c == ' '; };
+    auto attr_sep = [](char c) { return c == ':'; };
+    auto skip = [](char c) { return false; };
+    dopt::Data raw(text.data(), text.size(), dopt::Data::MemInitializedType::eGiftWholeMemoryPleaseNotFree);
+    dopt::TextFileDataSetLoader loader(raw, line_sep, field_sep, attr_sep, skip);
+    auto stats = loader.computeStatisticsWithOneDataPass<false, true, int32_t, int32_t>();
+    if (!stats.ok) {
+        W.put<int32_t>(0);
+        fclose(fo);
+        return 0;
+    }
+    typedef dopt::DataSet<Mat, Vec, dopt::VectorNDRaw_b, Vec> DS;
+    DS ds;
+    int flags = (add_intercept ? dopt::CreateDatasetFlags::eAddInterceptTerm : dopt::CreateDatasetFlags::eNone) |
+                dopt::CreateDatasetFlags::eMakeRemappingForBinaryLogisticLoss;
+    size_t n = loader.createDataset<true, true>(ds, stats, flags);
+    int32_t d = (int32_t)ds.train_samples_tr.rows();
+    W.put<int32_t>(1);
+    W.put<int32_t>(d);
+    W.put<int32_t>((int32_t)n);
+    for (size_t s = 0; s < n; ++s)
+        for (int32_t i = 0; i < d; ++i) W.put<double>(ds.train_samples_tr.get(i, s));
+    for (size_t s = 0; s < n; ++s) W.put<double>(ds.train_outputs.get(s));
+    fclose(fo);
+    return 0;
+}
+
 // ---- topk / toplek on given matrices (one OS thread => one TopLEK stream) ------------------
 static int cmd_select(const char* in_path, const char* out_path, bool lek)
 {
@@ -508,6 +552,7 @@ int main(int argc, char** argv)
     if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3], false);
     if (!strcmp(argv[1], "runx")) return cmd_run(argv[2], argv[3], true);
     if (!strcmp(argv[1], "pp")) return cmd_pp(argv[2], argv[3]);
+    if (!strcmp(argv[1], "libsvm") && argc >= 5) return cmd_libsvm(argv[2], argv[3], atoi(argv[4]));
     if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
     if (!strcmp(argv[1], "toplek")) return cmd_select(argv[2], argv[3], true);
     if (!strcmp(argv[1], "chol")) return cmd_chol(argv[2], argv[3]);

@@ -151,6 +151,36 @@ def pp_case(name, prob, comp, k, alpha, tau, rounds, dump_rounds, sel_seed=1234)
         lk=np.array(lks), dir=np.array(dirs))
 
 
+LIBSVM_TEXTS = {
+    # tabs, CR/LF endings, an empty line, exponents, signs, repeated separators; the first line's
+    # smallest index reappears later (the reference's statistics pass resets min/max per entry of
+    # line 1)
+    "mixed": "+1 1:0.5 3:1 7:2.25e-1\r\n-1 2:1\t4:0.125 7:1\n\n+1 1:1 2:3E2 5:-0.75\n"
+             "-1   3:1e-2  6:1.5\r+1 4:0.1234567 7:10.0\n-1 1:2 5:+3.5e+1\n",
+    # 0/1 labels and binary features (a9a-style)
+    "binary01": "0 1:1 4:1 9:1\n1 2:1 3:1 9:1\n1 1:1 5:1 7:1 8:1\n0 4:1 6:1 9:1\n1 3:1 9:1\n",
+}
+
+
+def libsvm_case(name, text, add_intercept):
+    if _skip("libsvm"):
+        return
+    src = os.path.join(HERE, f"libsvm_{name}.txt")
+    with open(src, "w", newline="") as f:
+        f.write(text)
+    with tempfile.TemporaryDirectory() as td:
+        fout = os.path.join(td, "out.bin")
+        subprocess.run([HARNESS, "libsvm", src, fout, str(int(add_intercept))], check=True)
+        raw = open(fout, "rb").read()
+    ok = int(np.frombuffer(raw, "<i4", 1, 0)[0])
+    assert ok == 1
+    d, n = (int(v) for v in np.frombuffer(raw, "<i4", 2, 4))
+    x = np.frombuffer(raw, "<f8", n * d, 12).reshape(n, d).copy()
+    y = np.frombuffer(raw, "<f8", n, 12 + 8 * n * d).copy()
+    np.savez_compressed(os.path.join(HERE, f"libsvm_{name}_{int(add_intercept)}.npz"), x=x, y=y,
+                        add_intercept=int(add_intercept))
+
+
 def select_case(name, mats, d, k, lek):
     if _skip("select"):
         return
@@ -252,6 +282,11 @@ def main():
     run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 60, 3)
     dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
     run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
+
+    # the reference's LIBSVM loader on tricky text
+    for nm, txt in LIBSVM_TEXTS.items():
+        libsvm_case(nm, txt, False)
+        libsvm_case(nm, txt, True)
 
     # Option A, FedNL-LS and tracked objective values
     ls = dict(option_a=0, line_search=1, ls_max=5, track_f=1, ls_c=0.5, ls_gamma=0.5)

@@ -1,0 +1,140 @@
+"""The reference's local driver on the engine: fednl_gpu_execute_local (doptExecuteLocal's command
+line) and the LIBSVM loader it uses.
+
+The loader is pinned bit for bit by fixtures made with the reference's own TextFileDataSetLoader
+(tests/golden/make_golden.py, "libsvm"); argument handling returns the reference's
+TrainReturnCodes before any device work, so it is tested without a GPU.  The GPU test runs a whole
+command and compares the callback and the tracking records with the same run made through the
+Python API."""
+import glob
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import golden_path
+from ufednl_gb300 import datagen
+
+LIBSVM = sorted(glob.glob(golden_path("libsvm_*.npz")))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ufednl_gb300 import build, fednl
+    build.build()
+    return fednl
+
+
+@pytest.mark.parametrize("path", LIBSVM, ids=os.path.basename)
+def test_libsvm_loader_matches_reference(lib, path):
+    z = np.load(path)
+    txt = path.rsplit("_", 1)[0] + ".txt"
+    x, y = lib.load_libsvm(txt, bool(int(z["add_intercept"])))
+    np.testing.assert_array_equal(x, z["x"])
+    np.testing.assert_array_equal(y, z["y"])
+
+
+def test_libsvm_loader_errors(lib, tmp_path):
+    with pytest.raises(lib.FedNLError):
+        lib.load_libsvm(str(tmp_path / "missing.txt"))
+    three = tmp_path / "three.txt"
+    three.write_text("1 1:1\n2 1:1\n3 2:1\n")
+    with pytest.raises(lib.FedNLError):
+        lib.load_libsvm(str(three))
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1 x:1\n-1 2:1\n")
+    with pytest.raises(lib.FedNLError):
+        lib.load_libsvm(str(bad))
+
+
+def test_execute_local_argument_errors(lib, tmp_path):
+    data = golden_path("libsvm_binary01.txt")
+    base = (f"--train_dataset {data} --clients 2 --lambda 0.001 --rounds 3 --algorithm fednl1 "
+            f"--k_compressor_as_d_mult 1 --alpha_step_size 1 --fednl-option-b --out {tmp_path}/t.bin")
+    assert lib.execute_local("--lambda 0.1")[0] == -1                                   # no --out
+    assert lib.execute_local(f"--out {tmp_path}/t.bin --train_dataset {tmp_path}/none.txt")[0] == -3
+    assert lib.execute_local(base + " --compressor topk --debug forcesequpdate,bogus")[0] == -8
+    assert lib.execute_local(base + " --compressor fancy")[0] == -2                     # unknown compressor
+    assert lib.execute_local(base.replace("fednl1", "gd") + " --compressor topk")[0] == -2
+    assert lib.execute_local(base.replace("--fednl-option-b", "") + " --compressor topk")[0] == -1
+    assert lib.execute_local(base.replace("--rounds 3", "") + " --compressor topk")[0] == -1
+    assert lib.execute_local(base.replace("--clients 2", "--clients 99") + " --compressor topk")[0] == -5
+
+
+def _write_libsvm(path, prob):
+    with open(path, "w") as f:
+        for s in range(prob.total_samples):
+            a = prob.features[s]
+            items = " ".join(f"{i + 1}:{int(a[i])}" for i in range(prob.d) if a[i] != 0.0)
+            f.write(f"{'+1' if prob.labels[s] > 0 else '-1'} {items}\n")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("extra,comp,k", [("--use_theoretical_alpha_option_2 --theoretical_alpha", "topk", 2),
+                                          ("--alpha_step_size 1 --line_search --c_line_search 0.5 "
+                                           "--gamma_line_search 0.5", "toplek", 2),
+                                          ("--theoretical_alpha", "seqk", 1)])
+def test_execute_local_matches_api_run(lib, tmp_path, extra, comp, k):
+    """A whole bin_fednl_local command line: even split of the file's samples over 6 clients with
+    the reference's reshuffle, intercept added by the loader, tracking file written; the callback
+    and the tracked ||g|| / f must equal the same run made through the Python API."""
+    prob = datagen.binary_problem(41, 16, [30] * 6, 0.3, 1e-3)       # last attribute = intercept
+    body = datagen.Problem(prob.d - 1, prob.n_samples, prob.features[:, :-1], prob.labels, prob.lam)
+    data = tmp_path / "data.txt"
+    _write_libsvm(data, body)
+    out = tmp_path / "track_{algorithm}_{dataset}.bin"
+    cmd = (f"--train_dataset {data} --clients 6 --reshuffle_train --add_intercept --lambda 0.001 --rounds 12 "
+           f"--workers 3 --algorithm fednl1 --compressor {comp} --k_compressor_as_d_mult {k} --fednl-option-b "
+           f"--tracking --out {out} --debug forcesequpdate {extra}")
+    rc, cbv = lib.execute_local(cmd)
+    assert rc == 0 and cbv is not None
+    # the same run through the Python API
+    x, y = lib.load_libsvm(str(data), True)
+    n = len(y)
+    order = np.arange(n)
+    st = np.uint32(123)
+    nm = n - 1
+    for i in range(n):                               # Shuffle.h:133-160 with RandomGenIntegerLinear
+        st = np.uint32((int(st) * 214013 + 2531011) & 0xffffffff)
+        u = float(st) * (1.0 / 4294967295.0)
+        v = u * nm
+        r = int(v) + (1 if v - int(v) > 0.5 else 0)
+        if r:
+            order[i], order[i + r] = order[i + r], order[i]
+        nm -= 1
+    per = n // 6
+    sel = order[:per * 6]
+    p2 = datagen.Problem(x.shape[1], np.full(6, per, dtype=np.int32), x[sel], y[sel], 1e-3)
+    d = x.shape[1]
+    U = d * (d + 1) // 2
+    comp_api = {"topk": "topk", "toplek": "toplek", "seqk": "randseqk"}[comp]
+    kk = int(k * d)
+    alpha = 1.0 if comp != "seqk" else 1.0 / (U / kk - 1.0 + 1.0)
+    opts = dict(track_f=True)
+    if "line_search" in extra:
+        opts["line_search"] = (0.5, 0.5, 5)
+    fed = lib.FedNL(p2, comp_api, kk, alpha, workers=3, **opts)
+    gn, fs = [], []
+    for _ in range(12):
+        gn.append(fed.round())
+        fs.append(fed.f())
+    g = fed.grad()
+    fed.close()
+    g2 = float(np.dot(g, g))
+    assert cbv[0] == d
+    assert cbv[1] == pytest.approx(np.sqrt(g2), rel=1e-12, abs=1e-300)
+    # tracking file: header then one record per round (TrainLoop.h:753-792, 1679-1691)
+    raw = open(str(tmp_path / f"track_fednl1_data.bin"), "rb").read()
+    parts = raw.split(b"\0", 3)
+    assert parts[0] == b"data" and parts[1].startswith(b"FedNL") and parts[2] == comp.encode()
+    rest = parts[3]
+    hdr = struct.unpack("<6i4d", rest[:56])
+    assert hdr[0] == per and hdr[2] == 12 and hdr[3] == 6 and hdr[4] == d and hdr[5] == kk
+    recs = rest[56:]
+    assert len(recs) == 12 * (4 + 6 * 8)
+    for r in range(12):
+        rec = struct.unpack("<i6d", recs[r * 52:(r + 1) * 52])
+        assert rec[0] == r
+        assert rec[1] == gn[r]
+        assert rec[2] == fs[r]

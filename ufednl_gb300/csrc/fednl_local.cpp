@@ -322,6 +322,21 @@ struct Tracker {
 
 }  // namespace
 
+extern "C" int fednl_gpu_load_libsvm(const char* path, int32_t add_intercept, int32_t* n_samples, int32_t* d,
+                                     double* features, double* labels)
+{
+    if (!path || !n_samples || !d) return -1;
+    Dataset ds;
+    std::string err;
+    const int rc = load_libsvm(path, add_intercept != 0, ds, err);
+    if (rc) return rc;
+    *n_samples = ds.n;
+    *d = ds.d;
+    if (features) std::memcpy(features, ds.x.data(), ds.x.size() * sizeof(double));
+    if (labels) std::memcpy(labels, ds.y.data(), ds.y.size() * sizeof(double));
+    return 0;
+}
+
 extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callback cb)
 {
     if (!command) return -1;

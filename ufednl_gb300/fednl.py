@@ -57,7 +57,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
            "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
-           "fednl_gpu_last_error", "fednl_gpu_execute_local"]
+           "fednl_gpu_last_error", "fednl_gpu_execute_local", "fednl_gpu_load_libsvm"]
 
 _lib = None
 
@@ -113,6 +113,8 @@ def load(build_if_missing: bool = True):
     L.fednl_gpu_get_f.restype = C.c_double
     L.fednl_gpu_get_ls_steps.argtypes = [vp]
     L.fednl_gpu_get_ls_steps.restype = C.c_int32
+    L.fednl_gpu_load_libsvm.argtypes = [C.c_char_p, C.c_int32, ip, ip, dp, dp]
+    L.fednl_gpu_load_libsvm.restype = C.c_int
     L.fednl_gpu_execute_local.argtypes = [C.c_char_p, RESULT_CALLBACK]
     L.fednl_gpu_execute_local.restype = C.c_int
     L.fednl_gpu_last_error.argtypes = []
@@ -362,3 +364,15 @@ def execute_local(command: str):
 
     rc = load().fednl_gpu_execute_local(command.encode(), cb)
     return rc, (got[0] if got else None)
+
+
+def load_libsvm(path: str, add_intercept: bool = False):
+    """The reference's LIBSVM loader semantics: returns (features [n, d] row-major, labels +-1)."""
+    L = load()
+    n = np.zeros(1, dtype=np.int32)
+    d = np.zeros(1, dtype=np.int32)
+    _check(L.fednl_gpu_load_libsvm(path.encode(), int(add_intercept), _ip(n), _ip(d), None, None))
+    feats = np.empty((int(n[0]), int(d[0])))
+    labs = np.empty(int(n[0]))
+    _check(L.fednl_gpu_load_libsvm(path.encode(), int(add_intercept), _ip(n), _ip(d), _dp(feats), _dp(labs)))
+    return feats, labs
