@@ -1261,7 +1261,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     __shared__ double s_inv[kCholNB];
     __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
-    __shared__ double s_yb[32];
+    __shared__ double s_yb[2][32];
     int ent_nb = -1;
     const double l = lptr ? *lptr : lval;
     const int d = P.d;
@@ -1313,8 +1313,8 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         __syncthreads();
         // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Warp 0
         // owns the pivot chain: at step k it applies step k to row k+1 (block and slab), forms the
-        // pivot of row k+1 (every lane, from the broadcast entry) and scales that row, while warps
-        // 1..7 apply step k to rows k+2 and below; one CTA barrier per column.
+        // pivot of row k+1 (every lane, from the broadcast entry) and scales that row, while six
+        // other warps apply step k to rows k+2 and below; one CTA barrier per column.
         auto pivot_row = [&](int kk) {
             const double a0 = Db[kk][kk];
             const long long ab = __double_as_longlong(a0);
@@ -1358,12 +1358,15 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                     __syncwarp();
                     pivot_row(k + 1);
                 }
-            } else {
+            } else if (warp != 4) {
+                // warps 1-3 and 5-7: warp 4 shares warp 0's SM sub-partition (warp id mod 4), whose
+                // FP64 pipe must stay free for the pivot chain
                 const int rows = nb - 2 - k;               // rows k+2 .. nb-1
                 if (rows > 0) {
                     const int nblk = rows * (rows + 1) / 2;
                     const int nall = nblk + rows * ns;
-                    for (int e = tid - 32; e < nall; e += kCoopThreads - 32) {
+                    const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
+                    for (int e = ut; e < nall; e += kCoopThreads - 64) {
                         if (e < nblk) {
                             const unsigned v = s_ent[e];
                             const int i = (int)(v >> 8), j = (int)(v & 0xffu);
@@ -1459,15 +1462,23 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             }
         }
         __syncthreads();
-        for (int b1 = d; b1 > 0; b1 -= 32) {
-            const int b0 = max(0, b1 - 32);
-            const int nbk = b1 - b0;
-            if (tid < 32) {           // the block's triangle and 1/r_tt in registers, then the chain
+        // Blocks of 32 rows from the bottom.  Warp 0 solves a block (lane = row, the block's
+        // triangle and 1/r_tt in registers), then applies the block's solution to the next block's
+        // rows, which it keeps in registers; meanwhile warps 1-7 apply it to all rows above.  A row
+        // receives its updates in descending t order whichever warp applies them.
+        const int nblocks = (d + 31) / 32;
+        double v = 0.0;
+        if (tid < 32) {
+            const int b1 = d, b0 = max(0, d - 32);
+            v = (lane < b1 - b0) ? y[b0 + lane] : 0.0;
+        }
+        for (int blk = 0; blk < nblocks; ++blk) {
+            const int b1 = d - 32 * blk, b0 = max(0, b1 - 32), nbk = b1 - b0;
+            if (tid < 32) {
                 double ar[32];
 #pragma unroll
                 for (int s = 0; s < 32; ++s) ar[s] = (lane < s && s < nbk) ? A[up_pos(b0 + lane, b0 + s)] : 0.0;
                 const double myinv = (lane < nbk) ? P.rinv[b0 + lane] : 0.0;
-                double v = (lane < nbk) ? y[b0 + lane] : 0.0;
 #pragma unroll
                 for (int s = 31; s >= 0; --s) {
                     if (s < nbk) {
@@ -1478,22 +1489,37 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                 }
                 if (lane < nbk) {
                     y[b0 + lane] = v;
-                    s_yb[lane] = v;
+                    s_yb[blk & 1][lane] = v;
                 }
             }
             __syncthreads();
-            for (int i = tid; i < b0; i += blockDim.x) {
-                double av[32];
+            const int n0 = max(0, b0 - 32);                 // next block: rows [n0, b0)
+            if (tid < 32) {
+                if (b0 > 0) {
+                    const int i = n0 + lane;
+                    double av[32];
 #pragma unroll
-                for (int s = 0; s < 32; ++s) av[s] = (s < nbk) ? A[up_pos(i, b0 + s)] : 0.0;
-                double v = y[i];
+                    for (int s = 0; s < 32; ++s) av[s] = (s < nbk && i < b0) ? A[up_pos(i, b0 + s)] : 0.0;
+                    double w = (i < b0) ? y[i] : 0.0;
 #pragma unroll
-                for (int s = 31; s >= 0; --s)
-                    if (s < nbk) v = fma(-av[s], s_yb[s], v);
-                y[i] = v;
+                    for (int s = 31; s >= 0; --s)
+                        if (s < nbk) w = fma(-av[s], s_yb[blk & 1][s], w);
+                    v = w;
+                }
+            } else {
+                for (int i = tid - 32; i < n0; i += blockDim.x - 32) {
+                    double av[32];
+#pragma unroll
+                    for (int s = 0; s < 32; ++s) av[s] = (s < nbk) ? A[up_pos(i, b0 + s)] : 0.0;
+                    double w = y[i];
+#pragma unroll
+                    for (int s = 31; s >= 0; --s)
+                        if (s < nbk) w = fma(-av[s], s_yb[blk & 1][s], w);
+                    y[i] = w;
+                }
             }
-            __syncthreads();
         }
+        __syncthreads();
         for (int i = tid; i < d; i += blockDim.x) {
             const double dxi = y[i];
             if (dxout) dxout[i] = dxi;
