@@ -210,6 +210,16 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
 
 const char* fednl_gpu_last_error(void);
 
+/* ---- tensor-core (tcgen05) operators of the mixed-precision form ---------------------------- */
+/* Weighted Gram matrices H_c = X_c^T diag(w) X_c + lambda I of dense FP32 client blocks on the
+ * tensor cores (TF32 inputs, FP32 accumulation in tensor memory): the Hessian sum of
+ * evaluateHessian (logistic_regression.h:365-547) with w = D_s.  features: host [sum n][d]
+ * row-major FP32 (clients in order), weights: host [sum n] FP32, out: host [n_clients][d][d]
+ * row-major FP32 of which the upper 128 x 128 tiles (row tile <= column tile) are written.
+ * d must be a multiple of 128. */
+int fednl_gpu_weighted_gram_tf32(const float* features, const float* weights, const int32_t* n_samples,
+                                 int32_t n_clients, int32_t d, float lambda, float* out);
+
 /* ---- the reference's local driver ---------------------------------------------------------- */
 /* Callback of doptExecuteLocal (bin_fednl_local/include/TrainCallbaksShared.h:11-14): dimension,
  * ||g|| of the last round, ||g||^2 / (2 mu) and 2 ||g||^2 / mu with mu = lambda

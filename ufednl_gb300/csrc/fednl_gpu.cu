@@ -122,6 +122,9 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
 
 }  // namespace
 
+// error reporting shared with the tensor-core translation unit (fednl_mixed.cu)
+int fednl_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 struct fednl_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;

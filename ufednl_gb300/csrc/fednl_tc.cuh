@@ -1,0 +1,306 @@
+// fednl_tc.cuh -- tensor-core (tcgen05) kernels of the mixed-precision round, sm_103a.
+//
+// The client Hessian of the L2-logistic objective is H_i = sum_s D_s a_s a_s^T + lambda I
+// (logistic_regression.h:163-547).  In the mixed-precision form the sum is a weighted Gram matrix
+// X_i diag(D) X_i^T of the client's feature-major FP32 block X_i (d x n_i), computed on the 5th
+// generation tensor cores in TF32 with FP32 accumulation in tensor memory:
+//
+//   * one CTA per 128 x 128 tile of the upper triangle of H_i (tiles of one client are scheduled
+//     together so that the client's block stays in L2);
+//   * warp 0 streams 128 x 32 FP32 slabs of the two tile rows with TMA (3-D tensor map over
+//     [client][feature][sample], 128-byte swizzle) into a 4-stage ring guarded by mbarriers;
+//   * warps 2-5 scale the B slab by the per-sample weights D_s in shared memory (the swizzle is
+//     undone to find each element's sample) and release it to the tensor cores;
+//   * warp 1 (one lane) issues tcgen05.mma.kind::tf32 (M = N = 128, K = 8, four per slab) into a
+//     128-column TMEM accumulator and frees each slab with tcgen05.commit;
+//   * warps 2-5 read the accumulator back with tcgen05.ld (warp w owns TMEM lanes 32 (w mod 4) ..)
+//     and hand each 16-column chunk to the epilogue functor.
+//
+// Every wait is bounded; a wait that runs out raises the CTA's abort flag, sets *err, lets the
+// copies and MMAs already issued drain (bounded again), frees the TMEM and returns.
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace fednl_tc {
+
+constexpr int kBM = 128, kBN = 128, kBK = 32;     // tile rows, tile columns, FP32 samples per slab
+constexpr int kStages = 4;
+constexpr int kSlabBytes = kBM * kBK * 4;         // 16 KB (128 rows x 128 bytes)
+constexpr int kThreads = 192;
+constexpr long long kWaitCycles = 2000000000ll;   // ~1 s
+constexpr uint32_t kTmemCols = 128;
+
+// dynamic shared memory: 1024-byte alignment slack + A and B rings + barriers
+constexpr size_t smem_bytes() { return 1024 + 2 * kStages * kSlabBytes + 256; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; false when it ran out or another role aborted
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag)
+{
+    const long long t0 = clock64();
+    while (!mbar_try(b, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// UMMA shared-memory descriptor, K-major operand in the 128-byte swizzle layout TMA writes:
+// rows of 128 bytes, 8-row atoms 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;                   // leading byte offset (unused by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// instruction descriptor of kind::tf32: D = F32, A = B = TF32, both K-major, N = M = 128
+constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                                ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(kIdescTf32), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GramJob {
+    int d;                 // features (multiple of 128)
+    int nc;                // clients
+    int L;                 // padded samples per client (multiple of 32)
+    int nbk;               // tile rows per client (d / 128)
+    int tiles;             // upper tiles per client, nbk (nbk + 1) / 2
+    const int* ns;         // [nc] samples per client
+    const int* act;        // [n_jobs / tiles] processed clients, or nullptr (all)
+    const float* w;        // [nc][L] per-sample weights D_s (0 beyond n_i)
+    int* err;              // set to 1 when a bounded wait ran out
+};
+
+// upper tile t of an nb x nb tile grid, row-major over the upper triangle
+__device__ __forceinline__ void upper_tile(int t, int nb, int& mi, int& ni)
+{
+    int i = 0, rem = t;
+    while (rem >= nb - i) {
+        rem -= nb - i;
+        ++i;
+    }
+    mi = i;
+    ni = i + rem;
+}
+
+// Epilogue functor: operator()(client, row m, first column n0, 16 FP32 values) for every row of
+// the tile (called by the 128 epilogue threads, 8 times each).
+template <class Epi>
+__global__ void __launch_bounds__(kThreads) k_gram_tf32(const __grid_constant__ CUtensorMap tmX, GramJob J, Epi epi)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* ringA = smem;
+    unsigned char* ringB = smem + kStages * kSlabBytes;
+    uint64_t* full = (uint64_t*)(smem + 2 * kStages * kSlabBytes);
+    uint64_t* scaled = full + kStages;
+    uint64_t* empty = scaled + kStages;
+    uint64_t* done = empty + kStages;
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int slot = blockIdx.x / J.tiles, t = blockIdx.x % J.tiles;
+    const int c = J.act ? J.act[slot] : slot;
+    int mi, ni;
+    upper_tile(t, J.nbk, mi, ni);
+    const int n = J.ns[c];
+    const int nk = (n + kBK - 1) / kBK;
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&scaled[s], 128);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmX)) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {                      // TMA producer
+            int issued = 0;
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % kStages;
+                if (kb >= kStages && !mbar_wait(&empty[s], (uint32_t)((kb / kStages) - 1) & 1u, abort_flag)) break;
+                mbar_expect_tx(&full[s], 2 * kSlabBytes);
+                tma_load_3d(ringA + s * kSlabBytes, &tmX, kb * kBK, mi * kBM, c, &full[s]);
+                tma_load_3d(ringB + s * kSlabBytes, &tmX, kb * kBK, ni * kBN, c, &full[s]);
+                ++issued;
+            }
+            if (*abort_flag) {                // let the copies in flight land before leaving
+                for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb) {
+                    const int s = kb % kStages;
+                    const long long t0 = clock64();
+                    while (!mbar_try(&full[s], (uint32_t)(kb / kStages) & 1u) && clock64() - t0 < kWaitCycles) {
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {                      // MMA issuer
+            int kb = 0;
+            for (; kb < nk; ++kb) {
+                const int s = kb % kStages;
+                if (!mbar_wait(&scaled[s], (uint32_t)(kb / kStages) & 1u, abort_flag)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = smem_u32(ringA + s * kSlabBytes), b0 = smem_u32(ringB + s * kSlabBytes);
+#pragma unroll
+                for (int kk = 0; kk < kBK / 8; ++kk)
+                    mma_tf32(tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), (kb > 0 || kk > 0) ? 1u : 0u);
+                mma_commit(&empty[s]);
+            }
+            mma_commit(done);                 // arrives once every MMA issued so far has completed
+        }
+    } else {
+        const int et = tid - 64;              // 0..127
+        for (int kb = 0; kb < nk; ++kb) {     // weight the B slab: column k of the slab by D_(k0 + k)
+            const int s = kb % kStages;
+            if (!mbar_wait(&full[s], (uint32_t)(kb / kStages) & 1u, abort_flag)) break;
+            float4* slab = (float4*)(ringB + s * kSlabBytes);
+            const float* wrow = J.w + (size_t)c * J.L + kb * kBK;
+#pragma unroll
+            for (int q = et; q < kBN * 8; q += 128) {      // 16-byte chunks of the slab
+                const int r = q >> 3, pc = q & 7, lc = pc ^ (r & 7);
+                const float4 wv = *reinterpret_cast<const float4*>(wrow + lc * 4);
+                float4 x = slab[q];
+                x.x *= wv.x;
+                x.y *= wv.y;
+                x.z *= wv.z;
+                x.w *= wv.w;
+                slab[q] = x;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&scaled[s]);
+        }
+        // epilogue: the accumulator rows of this warp's TMEM lane quarter
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0u, abort_flag));   // warp-uniform for tcgen05.ld
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (ok) {
+            const int quarter = warp & 3;
+            const int m = mi * kBM + quarter * 32 + lane;
+#pragma unroll 1
+            for (int j = 0; j < kBN / 16; ++j) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(j * 16), v);
+                epi(c, m, ni * kBN + j * 16, v);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (*abort_flag) {
+        if (tid == 0) *J.err = 1;
+        if (warp == 1) {                      // MMAs issued before the abort must finish first
+            const long long t0 = clock64();
+            while (!mbar_try(done, 0u) && clock64() - t0 < kWaitCycles) {
+            }
+        }
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// Epilogue writing the raw tile (plus lambda on the diagonal) into a full row-major d x d FP32
+// matrix per client: out[c][m][n]
+struct EpiStore {
+    float* out;
+    int d;
+    float lambda;
+    __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v) const
+    {
+        float* row = out + ((size_t)c * d + m) * d + n0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) row[i] = v[i] + ((m == n0 + i) ? lambda : 0.0f);
+    }
+};
+
+}  // namespace fednl_tc

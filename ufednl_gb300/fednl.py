@@ -57,7 +57,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_topk", "fednl_gpu_toplek", "fednl_gpu_randk",
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
            "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
-           "fednl_gpu_last_error", "fednl_gpu_execute_local", "fednl_gpu_load_libsvm"]
+           "fednl_gpu_last_error", "fednl_gpu_execute_local", "fednl_gpu_load_libsvm",
+           "fednl_gpu_weighted_gram_tf32"]
 
 _lib = None
 
@@ -113,6 +114,9 @@ def load(build_if_missing: bool = True):
     L.fednl_gpu_get_f.restype = C.c_double
     L.fednl_gpu_get_ls_steps.argtypes = [vp]
     L.fednl_gpu_get_ls_steps.restype = C.c_int32
+    fp = C.POINTER(C.c_float)
+    L.fednl_gpu_weighted_gram_tf32.argtypes = [fp, fp, ip, C.c_int32, C.c_int32, C.c_float, fp]
+    L.fednl_gpu_weighted_gram_tf32.restype = C.c_int
     L.fednl_gpu_load_libsvm.argtypes = [C.c_char_p, C.c_int32, ip, ip, dp, dp]
     L.fednl_gpu_load_libsvm.restype = C.c_int
     L.fednl_gpu_execute_local.argtypes = [C.c_char_p, RESULT_CALLBACK]
@@ -376,3 +380,17 @@ def load_libsvm(path: str, add_intercept: bool = False):
     labs = np.empty(int(n[0]))
     _check(L.fednl_gpu_load_libsvm(path.encode(), int(add_intercept), _ip(n), _ip(d), _dp(feats), _dp(labs)))
     return feats, labs
+
+
+def weighted_gram_tf32(features, weights, n_samples, lam: float = 0.0) -> np.ndarray:
+    """Tensor-core weighted Gram X_c^T diag(w) X_c + lam I per client (upper 128-tiles filled);
+    features [sum n][d] FP32, weights [sum n] FP32."""
+    f = np.ascontiguousarray(features, dtype=np.float32)
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    ns = np.ascontiguousarray(n_samples, dtype=np.int32)
+    d = f.shape[1]
+    out = np.zeros((len(ns), d, d), dtype=np.float32)
+    fp = C.POINTER(C.c_float)
+    _check(load().fednl_gpu_weighted_gram_tf32(f.ctypes.data_as(fp), w.ctypes.data_as(fp), _ip(ns), len(ns), d,
+                                               float(lam), out.ctypes.data_as(fp)))
+    return out
