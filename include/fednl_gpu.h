@@ -41,7 +41,9 @@ typedef enum fednl_compressor {
     FEDNL_TOPK = 2,
     FEDNL_RANDSEQK = 3,
     FEDNL_TOPLEK = 4,
-    FEDNL_NATURAL = 5
+    FEDNL_NATURAL = 5,
+    FEDNL_RANDK_PHILOX = 6      /* project-defined RandK stream: k positions from a Philox4x32-10-keyed
+                                   Feistel permutation of the upper positions (no reference counterpart) */
 } fednl_compressor;
 
 typedef enum fednl_feature_format {

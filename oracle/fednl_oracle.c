@@ -70,6 +70,78 @@ void orc_upper_indices(int32_t d, int32_t lda, uint32_t* out)
             out[w++] = (uint32_t)j * (uint32_t)lda + (uint32_t)i;
 }
 
+/* Philox4x32-10: ten rounds of (hi0, lo0) = 0xD2511F53 c0, (hi1, lo1) = 0xCD9E8D57 c2,
+ * c = (hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0), the key bumped by the Weyl constants
+ * (0x9E3779B9, 0xBB67AE85) between rounds (Salmon et al., SC'11). */
+void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* Feistel permutation of [0, 2^(2h)) with six rounds whose round function is Philox keyed by
+ * (seed, client) on the counter (right half, round, draw, 'RAND') */
+static uint32_t feistel(uint32_t x, int h, uint32_t seed, uint32_t client, uint32_t draw)
+{
+    uint32_t mask = (1u << h) - 1u, L = x >> h, R = x & mask;
+    for (uint32_t r = 0; r < 6; ++r) {
+        uint32_t ctr[4] = {R, r, draw, 0x52414E44u}, key[2] = {seed, client}, o[4];
+        orc_philox4x32(ctr, key, o);
+        uint32_t nl = R, nr = L ^ (o[0] & mask);
+        L = nl;
+        R = nr;
+    }
+    return (L << h) | R;
+}
+
+static int philox_half_bits(size_t U)
+{
+    int b = 0;
+    while (((size_t)1 << b) < U)
+        ++b;
+    if (b < 2)
+        b = 2;
+    return (b + 1) / 2;
+}
+
+static uint32_t philox_position(uint32_t i, size_t U, int h, uint32_t seed, uint32_t client, uint32_t draw)
+{
+    uint32_t y = feistel(i, h, seed, client, draw);
+    while ((size_t)y >= U)                    /* cycle walking: a permutation of [0, U) */
+        y = feistel(y, h, seed, client, draw);
+    return y;
+}
+
+void orc_randk_philox(uint32_t seed, uint32_t client, uint32_t draw, int32_t k, size_t U, const uint32_t* upper,
+                      uint32_t* out)
+{
+    int h = philox_half_bits(U);
+    uint8_t* mark = (uint8_t*)calloc(U, 1);
+    for (int32_t i = 0; i < k; ++i)
+        mark[philox_position((uint32_t)i, U, h, seed, client, draw)] = 1;
+    int32_t w = 0;
+    for (size_t p = 0; p < U; ++p)
+        if (mark[p])
+            out[w++] = upper[p];
+    free(mark);
+}
+
 /* Partial Fisher-Yates with early stop, dopt/dopt/random/include/Shuffle.h:31-95 (active loop :76-93) */
 void orc_shuffle_partial(uint32_t* arr, size_t n, size_t k, uint32_t* state)
 {
@@ -712,6 +784,7 @@ typedef struct {
     double* grad;       /* d */
     double lk;
     uint32_t rng;       /* RandK / RandSeqK generator (seed_base + c) */
+    uint32_t draws;     /* RandK-Philox: draws made so far */
     uint32_t* msg_idx;  /* flat indices */
     double* msg_val;    /* values exactly as the master adds them to H */
     int32_t msg_count;
@@ -764,6 +837,8 @@ static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff
         orc_randk(&C->rng, S->k_eff, U, S->upper, C->msg_idx);
     else if (P->compressor == ORC_RANDSEQK)
         orc_randseqk(&C->rng, S->k_eff, U, S->upper, C->msg_idx);
+    else if (P->compressor == ORC_RANDK_PHILOX)
+        orc_randk_philox(P->seed_base, (uint32_t)c, C->draws++, S->k_eff, U, S->upper, C->msg_idx);
 
     orc_margin(C->atr, d, lda, n, S->x, mtmp);
     orc_sigmoid(mtmp, n, stmp);
@@ -805,7 +880,7 @@ static void client_compress(orc_state* S, int32_t c, uint32_t* toplek_rng, const
             if (ir != jc)
                 C->shift[(size_t)ir * lda + jc] += alpha * item;
         }
-    } else if (P->compressor == ORC_RANDK || P->compressor == ORC_RANDSEQK) {
+    } else if (P->compressor == ORC_RANDK || P->compressor == ORC_RANDSEQK || P->compressor == ORC_RANDK_PHILOX) {
         double mult = (double)U / (double)k;    /* RandK.h:90 */
         C->msg_count = k;
         for (int32_t t = 0; t < k; ++t) {       /* RandK.h:127-162 */

@@ -28,6 +28,7 @@ extern "C" {
 #define ORC_RANDSEQK 3
 #define ORC_TOPLEK   4
 #define ORC_NATURAL  5
+#define ORC_RANDK_PHILOX 6   /* project-defined RandK stream (Philox-keyed permutation), no reference counterpart */
 
 typedef struct orc_problem {
     int32_t d;                 /* dimension including the intercept column */
@@ -68,6 +69,12 @@ void   orc_upper_indices(int32_t d, int32_t lda, uint32_t* out);
 void   orc_shuffle_partial(uint32_t* arr, size_t n, size_t k, uint32_t* state);
 void   orc_randk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
 void   orc_randseqk(uint32_t* state, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) */
+void   orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* k distinct upper positions of draw number `draw` of client `client`: images of 0..k-1 under a
+ * Philox-keyed Feistel permutation of [0, 2^b) walked into [0, U); out = sorted flat indices */
+void   orc_randk_philox(uint32_t seed, uint32_t client, uint32_t draw, int32_t k, size_t U, const uint32_t* upper,
+                        uint32_t* out);
 /* TopK over |m[upper[..]]| of a full d x lda column-major matrix; writes k sorted flat indices */
 int32_t orc_topk(const double* m, int32_t k, size_t U, const uint32_t* upper, uint32_t* out);
 /* TopLEK; frob_sq = squared L2 norm of the whole d x lda buffer; returns the count written */

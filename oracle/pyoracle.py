@@ -14,9 +14,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL = 0, 1, 2, 3, 4, 5
+IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL, RANDK_PHILOX = 0, 1, 2, 3, 4, 5, 6
 COMPRESSORS = {"identity": IDENTITY, "randk": RANDK, "topk": TOPK, "randseqk": RANDSEQK,
-               "toplek": TOPLEK, "natural": NATURAL}
+               "toplek": TOPLEK, "natural": NATURAL, "randk_philox": RANDK_PHILOX}
 
 
 class Problem(C.Structure):
@@ -77,6 +77,8 @@ def lib():
         L.orc_toplek.argtypes = [dp, C.c_int32, C.c_int32, C.c_size_t, up, C.c_double, C.c_double, up, up]
         L.orc_randk.argtypes = [up, C.c_int32, C.c_size_t, up, up]
         L.orc_randseqk.argtypes = [up, C.c_int32, C.c_size_t, up, up]
+        L.orc_randk_philox.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, C.c_size_t, up, up]
+        L.orc_philox4x32.argtypes = [up, up, up]
         L.orc_natural.restype = C.c_double
         L.orc_natural.argtypes = [C.c_double]
         L.orc_pack2_natural.restype = C.c_uint32

@@ -232,12 +232,13 @@ def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=No
     orc.close()
 
 
-@pytest.mark.parametrize("comp", ["topk", "toplek", "randk", "randseqk", "natural", "identity"])
+@pytest.mark.parametrize("comp", ["topk", "toplek", "randk", "randseqk", "natural", "identity", "randk_philox"])
 def test_run_vs_oracle_small(gpu, oracle, comp):
     prob = datagen.binary_problem(21, 30, [37, 52, 29, 61, 44, 33], 0.15, 1e-3)
     U = 30 * 31 // 2
-    k = {"topk": 120, "toplek": 150, "randk": 60, "randseqk": 30, "natural": U, "identity": U}[comp]
-    alpha = {"randk": k / U, "randseqk": k / U, "natural": 8 / 9}.get(comp, 1.0)
+    k = {"topk": 120, "toplek": 150, "randk": 60, "randseqk": 30, "natural": U, "identity": U,
+         "randk_philox": 60}[comp]
+    alpha = {"randk": k / U, "randseqk": k / U, "natural": 8 / 9, "randk_philox": k / U}.get(comp, 1.0)
     _compare_runs(gpu, oracle, prob, comp, k, alpha, 8, workers=4)
 
 

@@ -141,6 +141,38 @@ def test_pp_run_matches_reference(oracle, path):
     fed.close()
 
 
+def test_philox_known_answers_and_randk_stream(oracle):
+    """Philox4x32-10 against the published known-answer vectors of its authors' Random123 suite,
+    and the RandK-Philox stream's invariants (k distinct upper indices, ascending, deterministic,
+    a new set per draw)."""
+    import ctypes as C
+    L = oracle.lib()
+
+    def ph(c, k):
+        ctr, key, out = (C.c_uint32 * 4)(*c), (C.c_uint32 * 2)(*k), (C.c_uint32 * 4)()
+        L.orc_philox4x32(ctr, key, out)
+        return list(out)
+    assert ph([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert ph([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert ph([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+    d, lda, k = 40, 40, 160
+    U = d * (d + 1) // 2
+    upper = np.array([j * lda + i for j in range(d) for i in range(j + 1)], dtype=np.uint32)
+    up = upper.ctypes.data_as(C.POINTER(C.c_uint32))
+    sets = []
+    for draw in range(3):
+        out = np.empty(k, dtype=np.uint32)
+        L.orc_randk_philox(123, 7, draw, k, U, up, out.ctypes.data_as(C.POINTER(C.c_uint32)))
+        assert len(np.unique(out)) == k and np.all(np.diff(out.astype(np.int64)) > 0)
+        assert np.all(np.isin(out, upper))
+        sets.append(out)
+    again = np.empty(k, dtype=np.uint32)
+    L.orc_randk_philox(123, 7, 0, k, U, up, again.ctypes.data_as(C.POINTER(C.c_uint32)))
+    np.testing.assert_array_equal(again, sets[0])
+    assert not np.array_equal(sets[0], sets[1])
+
+
 def test_log_is_faithful(oracle):
     """The oracle's own logarithm (shared bit for bit with the kernels) is within one ulp of the
     correctly rounded libm log over the sigmoid range, wide magnitudes and subnormals."""

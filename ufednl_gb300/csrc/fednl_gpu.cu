@@ -228,6 +228,13 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
         MARK("k_randk");
         k_randk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.hmap, h->hcap, P.sel, h->SW, P.cnt, P.act);
         CKL();
+    } else if (comp == FEDNL_RANDK_PHILOX) {
+        MARK("k_randk_philox");
+        int hb = 2;
+        while ((1ll << hb) < h->U) ++hb;
+        k_randk_philox<<<na, 256, 0, st>>>(P.rstate, h->U, h->k, (hb + 1) / 2, h->desc.seed_base, P.sel, h->SW, P.cnt,
+                                           P.act);
+        CKL();
     } else if (comp == FEDNL_RANDSEQK) {
         MARK("k_randseqk");
         k_randseqk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt, P.act);
@@ -321,7 +328,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     if (rc) return rc;
     const fednl_problem_desc& D = *desc;
     if (D.d < 1 || D.n_clients < 1 || !D.n_samples) return fail(FEDNL_EINVAL, "d and n_clients must be >= 1");
-    if (D.compressor < 0 || D.compressor > 5) return fail(FEDNL_EINVAL, "unknown compressor %d", D.compressor);
+    if (D.compressor < 0 || D.compressor > 6) return fail(FEDNL_EINVAL, "unknown compressor %d", D.compressor);
     for (int i = 0; i < 2; ++i)
         if (D.reserved[i]) return fail(FEDNL_EINVAL, "reserved fields must be zero");
     if (D.clients_per_round < 0 || D.clients_per_round > D.n_clients)
@@ -336,7 +343,7 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
         return fail(FEDNL_EINVAL, "d too large for 32-bit flat indices");
     int k = (D.compressor == FEDNL_IDENTITY || D.compressor == FEDNL_NATURAL) ? (int)U : D.k;
     if (k < 1) return fail(FEDNL_EINVAL, "k must be >= 1");
-    if ((D.compressor == FEDNL_RANDK || D.compressor == FEDNL_RANDSEQK) && k > U)
+    if ((D.compressor == FEDNL_RANDK || D.compressor == FEDNL_RANDSEQK || D.compressor == FEDNL_RANDK_PHILOX) && k > U)
         return fail(FEDNL_EINVAL, "k %d larger than U %lld", k, U);
     if ((D.compressor == FEDNL_TOPK || D.compressor == FEDNL_TOPLEK) && k < U && k > kMaxK)
         return fail(FEDNL_EINVAL, "TopK/TopLEK k %d above the shared-memory heap limit %d", k, kMaxK);
@@ -644,7 +651,8 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
         CK(cudaMemsetAsync(P.stats, 0, 16, st));
     }
     std::vector<unsigned> ws(h->W, h->desc.toplek_seed), rs(h->nc);
-    for (int c = 0; c < h->nc; ++c) rs[c] = h->desc.seed_base + (unsigned)c;   // TrainLoop.h:632
+    for (int c = 0; c < h->nc; ++c)     // TrainLoop.h:632; the Philox stream counts draws instead
+        rs[c] = h->comp == FEDNL_RANDK_PHILOX ? 0u : h->desc.seed_base + (unsigned)c;
     CK(cudaMemcpyAsync(P.wstate, ws.data(), h->W * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(P.rstate, rs.data(), h->nc * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(P.round_ctr, 0, 4, st));
@@ -857,7 +865,7 @@ int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double*
                 memcpy(&item, &b, 8);
                 val[t] = P.prescale * item;
             } else {
-                if (comp == FEDNL_RANDK || comp == FEDNL_RANDSEQK) item = item * P.mult;
+                if (comp == FEDNL_RANDK || comp == FEDNL_RANDSEQK || comp == FEDNL_RANDK_PHILOX) item = item * P.mult;
                 val[t] = item * P.prescale;
             }
         }

@@ -1092,6 +1092,64 @@ __global__ void k_randk(unsigned* states, int n_gen, int U, int k, unsigned long
     if (threadIdx.x == 0) cnt[c] = k;
 }
 
+// Project-defined RandK stream (FEDNL_RANDK_PHILOX): the k positions of draw `draw` of client c are
+// the images of 0..k-1 under a six-round Feistel permutation of [0, 2^(2h)) whose round function is
+// Philox4x32-10 (Salmon et al., SC'11) keyed by (seed, c), walked back into [0, U).  Every position
+// is formed independently, one thread each; the CPU oracle computes the same stream.
+__device__ __forceinline__ void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                                           uint32_t& o0)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    o0 = c0;
+}
+
+__device__ __forceinline__ uint32_t philox_feistel(uint32_t x, int h, uint32_t seed, uint32_t client, uint32_t draw)
+{
+    const uint32_t mask = (1u << h) - 1u;
+    uint32_t L = x >> h, R = x & mask;
+    for (uint32_t r = 0; r < 6; ++r) {
+        uint32_t o;
+        philox4x32(R, r, draw, 0x52414E44u, seed, client, o);
+        const uint32_t nr = L ^ (o & mask);
+        L = R;
+        R = nr;
+    }
+    return (L << h) | R;
+}
+
+__global__ void k_randk_philox(unsigned* draws, int U, int k, int h, unsigned seed, unsigned* sel, int SW, int* cnt,
+                               const int* act)
+{
+    const int c = act ? act[blockIdx.x] : blockIdx.x;
+    unsigned* sc = sel + (size_t)c * SW;
+    for (int w = threadIdx.x; w < SW; w += blockDim.x) sc[w] = 0u;
+    const unsigned draw = draws[c];
+    __syncthreads();
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        uint32_t y = philox_feistel((uint32_t)i, h, seed, (uint32_t)c, draw);
+        while (y >= (uint32_t)U) y = philox_feistel(y, h, seed, (uint32_t)c, draw);   // ends: a cycle holds i < U
+        atomicOr(&sc[y >> 5], 1u << (y & 31));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        draws[c] = draw + 1;
+        cnt[c] = k;
+    }
+}
+
 // generateRandSeqKItemsInUpperTriangularPart (SpecialMathRoutinesForMatrix.h:137-169)
 __global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq, unsigned* sel, int SW, int* cnt,
                            const int* act)
@@ -1144,7 +1202,7 @@ __global__ void k_apply(Dev P)
                 item = natural_trunc(dv);
                 sent = __dmul_rn(P.prescale, item);
             } else {
-                item = (P.comp == 1 || P.comp == 3) ? __dmul_rn(dv, P.mult) : dv;
+                item = (P.comp == 1 || P.comp == 3 || P.comp == 6) ? __dmul_rn(dv, P.mult) : dv;
                 sent = __dmul_rn(item, P.prescale);
             }
             P.shift[q] = __dadd_rn(P.shift[q], __dmul_rn(P.alpha, item));
@@ -1257,7 +1315,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                                                             double* xupd, int record)
 {
     __shared__ double Db[kCholNB][kCholNB + 1];
+    __shared__ double Rb[kCholNB][kCholNB + 1];
     __shared__ double Sb[kCholNB][kCholSlab + 1];
+    __shared__ double SR[kCholNB][kCholSlab + 1];
     __shared__ double s_inv[kCholNB];
     __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
@@ -1311,70 +1371,64 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         }
         if (tid == 0) s_fail = 0;
         __syncthreads();
-        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Warp 0
-        // owns the pivot chain: at step k it applies step k to row k+1 (block and slab), forms the
-        // pivot of row k+1 (every lane, from the broadcast entry) and scales that row, while six
-        // other warps apply step k to rows k+2 and below; one CTA barrier per column.
-        auto pivot_row = [&](int kk) {
-            const double a0 = Db[kk][kk];
-            const long long ab = __double_as_longlong(a0);
-            const long long mag = ab & 0x7fffffffffffffffll;
-            const bool bad = ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll;   // a < 0 (not NaN, not -0)
+        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Db and Sb
+        // hold the working entries, Rb and SR the finished rows of R.  Warp 0 runs only the pivot
+        // chain: at step k it forms r_{k,k+1} = a_{k,k+1} (1 / r_kk), applies step k to the next
+        // diagonal entry itself and takes its square root and reciprocal.  Meanwhile six other
+        // warps scale row k (into Rb / SR) and apply step k to every other entry below row k.
+        // Warp 4 stays idle: it shares warp 0's SM sub-partition, whose FP64 pipe the chain needs.
+        double inv_k = 0.0;
+        if (warp == 0) {
+            const double a0 = Db[0][0];
+            const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
             const double r = sqrt(a0);
-            const double inv = 1.0 / r;
-            const int nd = nb - 1 - kk;
-            for (int it = lane; it < nd + ns; it += 32) {
-                if (it < nd) {
-                    const int j = kk + 1 + it;
-                    Db[kk][j] = __dmul_rn(Db[kk][j], inv);
-                } else {
-                    Sb[kk][it - nd] = __dmul_rn(Sb[kk][it - nd], inv);
-                }
-            }
-            __syncwarp();
+            inv_k = 1.0 / r;
             if (lane == 0) {
-                Db[kk][kk] = r;
-                s_inv[kk] = inv;
-                if (bad) s_fail = 1;
+                Rb[0][0] = r;
+                s_inv[0] = inv_k;
+                if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;   // a < 0 (not NaN, not -0)
             }
-        };
-        if (warp == 0) pivot_row(0);
+        }
         __syncthreads();
         for (int k = 0; k < nb; ++k) {
             if (s_fail) break;
             if (warp == 0) {
                 if (k + 1 < nb) {
-                    const int nd = nb - 1 - k;              // row k+1: j = k+1 .. nb-1, then the slab
-                    const double rk = Db[k][k + 1];
-                    for (int it = lane; it < nd + ns; it += 32) {
-                        if (it < nd) {
-                            const int j = k + 1 + it;
-                            Db[k + 1][j] = fma(-rk, Db[k][j], Db[k + 1][j]);
-                        } else {
-                            const int sl = it - nd;
-                            Sb[k + 1][sl] = fma(-rk, Sb[k][sl], Sb[k + 1][sl]);
-                        }
+                    const double rk = __dmul_rn(Db[k][k + 1], inv_k);
+                    const double a0 = fma(-rk, rk, Db[k + 1][k + 1]);
+                    const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
+                    const double r = sqrt(a0);
+                    inv_k = 1.0 / r;
+                    if (lane == 0) {
+                        Rb[k + 1][k + 1] = r;
+                        s_inv[k + 1] = inv_k;
+                        if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;
                     }
-                    __syncwarp();
-                    pivot_row(k + 1);
                 }
             } else if (warp != 4) {
-                // warps 1-3 and 5-7: warp 4 shares warp 0's SM sub-partition (warp id mod 4), whose
-                // FP64 pipe must stay free for the pivot chain
-                const int rows = nb - 2 - k;               // rows k+2 .. nb-1
+                const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;    // 0..191
+                const double inv = s_inv[k];
+                const int nd = nb - 1 - k;
+                for (int it = ut; it < nd + ns; it += kCoopThreads - 64) {
+                    if (it < nd) Rb[k][k + 1 + it] = __dmul_rn(Db[k][k + 1 + it], inv);
+                    else SR[k][it - nd] = __dmul_rn(Sb[k][it - nd], inv);
+                }
+                asm volatile("bar.sync 1, 192;" ::: "memory");
+                const int rows = nb - 1 - k;               // rows k+1 .. nb-1
                 if (rows > 0) {
                     const int nblk = rows * (rows + 1) / 2;
+                    const int skip = nblk - rows;          // entry (k+1, k+1): the pivot chain's own
                     const int nall = nblk + rows * ns;
-                    const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
                     for (int e = ut; e < nall; e += kCoopThreads - 64) {
                         if (e < nblk) {
+                            if (e == skip) continue;
                             const unsigned v = s_ent[e];
                             const int i = (int)(v >> 8), j = (int)(v & 0xffu);
-                            Db[i][j] = fma(-Db[k][i], Db[k][j], Db[i][j]);
+                            Db[i][j] = fma(-Rb[k][i], Rb[k][j], Db[i][j]);
                         } else {
                             const int q = e - nblk;
-                            const int i = k + 2 + q / ns, sl = q - (q / ns) * ns;
-                            Sb[i][sl] = fma(-Db[k][i], Sb[k][sl], Sb[i][sl]);
+                            const int i = k + 1 + q / ns, sl = q - (q / ns) * ns;
+                            Sb[i][sl] = fma(-Rb[k][i], SR[k][sl], Sb[i][sl]);
                         }
                     }
                 }
@@ -1391,13 +1445,13 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         if (blockIdx.x == 0) {
             for (int t = tid; t < nb * nb; t += blockDim.x) {
                 int i = t % nb, j = t / nb;
-                if (i <= j) A[up_pos(c0 + i, c0 + j)] = Db[i][j];
+                if (i <= j) A[up_pos(c0 + i, c0 + j)] = Rb[i][j];
             }
             for (int t = tid; t < nb; t += blockDim.x) P.rinv[c0 + t] = s_inv[t];
         }
         for (int t = tid; t < nb * ns; t += blockDim.x) {
             const int i = t % nb, sl = t / nb;
-            A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)] = Sb[i][sl];
+            A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)] = SR[i][sl];
         }
         // panel columns beyond the slab (very large d only): one column per warp, same steps
         {
@@ -1408,7 +1462,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                 for (int k = 0; k < nb; ++k) {
                     if (lane == k) a = __dmul_rn(a, s_inv[k]);
                     double r = __shfl_sync(0xffffffffu, a, k);
-                    if (lane > k && lane < nb) a = fma(-Db[k][lane], r, a);
+                    if (lane > k && lane < nb) a = fma(-Rb[k][lane], r, a);
                 }
                 if (lane < nb) A[up_pos(c0 + lane, j)] = a;
             }

@@ -19,9 +19,9 @@ import numpy as np
 
 from . import build as _build
 
-IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL = 0, 1, 2, 3, 4, 5
+IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL, RANDK_PHILOX = 0, 1, 2, 3, 4, 5, 6
 COMPRESSORS = {"identity": IDENTITY, "randk": RANDK, "topk": TOPK, "randseqk": RANDSEQK,
-               "seqk": RANDSEQK, "toplek": TOPLEK, "natural": NATURAL}
+               "seqk": RANDSEQK, "toplek": TOPLEK, "natural": NATURAL, "randk_philox": RANDK_PHILOX}
 STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTPD", -5: "ETIMEOUT", -6: "ENODEV"}
 
 
