@@ -254,6 +254,48 @@ def extra_workloads(fednl, threads: int, steps: int):
     return out
 
 
+def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
+    """The mixed-precision configuration: dense N(0,1) FP32 features, d=1024, 256 clients with
+    n_i ~ U{512..4096} (seed 2), lambda 1e-4, RandK-Philox k=4d.  The mixed round (TF32 tensor-core
+    Hessians) is device-timed; the FP64 GPU round (the same algorithm on the FP64 engine) and the
+    CPU port run a bounded sample on the same data; ||grad|| after the same rounds is compared."""
+    from ufednl_gb300 import datagen
+    from oracle import pyoracle
+    prob = datagen.workload_dense_fp32_1024()
+    d, k = prob.d, 4 * prob.d
+    U = d * (d + 1) // 2
+    alpha = k / U
+    R = 10
+    mx = fednl.MixedFedNL(prob, k, alpha)
+    g_mx = mx.run(R)
+    tot, per = mx.time_rounds(20)
+    prof = mx.profile_kernels(5)
+    mx.close()
+    gram_ms = dict(prof)["k_gram_tf32"]
+    flops = float(prob.total_samples) * d * (d + 1)          # upper triangle incl. diagonal, 2 flops per MAC
+    tf = flops / (gram_ms * 1e-3) / 1e12
+    p64 = datagen.Problem(d, prob.n_samples, prob.features.astype(np.float64), prob.labels, prob.lam)
+    f64 = fednl.FedNL(p64, "randk_philox", k, alpha, feature_format=2)
+    g_64 = f64.run(R)
+    tot64, _ = f64.time_rounds(2)
+    f64.close()
+    orc = pyoracle.FedNL(p64, "randk_philox", k, alpha, workers=threads, threads=threads)
+    t0 = time.perf_counter()
+    orc.round()
+    cpu_s = time.perf_counter() - t0
+    orc.close()
+    return {"rounds_per_s": 20 / (tot / 1000.0), "round_ms_p50": float(np.percentile(per, 50)),
+            "round_ms_p99": float(np.percentile(per, 99)), "kernels_ms": dict(prof),
+            "tensor": {"kernel": "k_gram_tf32", "precision": "tf32 x tf32 -> fp32 (tcgen05.mma kind::tf32)",
+                       "flops_per_launch": flops, "achieved_tflops": tf, "peak_tflops": tensor_peak_tflops,
+                       "frac": tf / tensor_peak_tflops,
+                       "peak_source": f"{src}: MEASURED_PEAKS.json bf16_tflops / 2 (tf32 rate)"},
+            "fp64_gpu_rounds_per_s": 2 / (tot64 / 1000.0), "cpu_port_rounds_per_s": 1.0 / cpu_s,
+            "cpu_port_sample": f"1 round, {threads} threads",
+            "grad_norm_after_rounds": {"rounds": R, "mixed": float(g_mx[-1]), "fp64": float(g_64[-1]),
+                                       "rel_diff": float(abs(g_mx[-1] - g_64[-1]) / g_64[-1])}}
+
+
 def config_dict(prob, comp, k, workers):
     return {"workload": prob.name, "d": prob.d, "clients": prob.n_clients, "samples": prob.total_samples,
             "compressor": comp, "k": k, "alpha": 1.0, "option": "B", "lambda": prob.lam, "workers": workers,
@@ -337,6 +379,8 @@ def run_ours(args, ws, rank, local, td):
             "clocks": clocks, "e2e": e2e}
     if ws == 1 and rank == 0 and not args.no_extra:
         line["extra_workloads"] = extra_workloads(fednl, os.cpu_count() or 1, args.steps)
+        line["extra_workloads"]["dense FP32 d1024 256x(512-4096) RandK-Philox k=4d, mixed precision"] = \
+            mixed_workload(fednl, os.cpu_count() or 1, bf16 / 2.0, src)
     if ws == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, n, dt = cpu_port_rounds_per_s(prob, comp, k, threads, 20, 20.0)

@@ -222,6 +222,26 @@ const char* fednl_gpu_last_error(void);
 int fednl_gpu_weighted_gram_tf32(const float* features, const float* weights, const int32_t* n_samples,
                                  int32_t n_clients, int32_t d, float lambda, float* out);
 
+/* ---- the mixed-precision round (dense FP32 features) --------------------------------------- */
+/* The FedNL round with client Hessians on the tensor cores: per client H_c = X_c^T diag(D) X_c +
+ * lambda I in TF32 with FP32 accumulation (tcgen05), fused with the FP32 shift difference, its
+ * Frobenius norm and the RandK-Philox selection; margins and gradients in FP32 pairs (about 2^-44
+ * relative); master H, aggregation and the Option-B Cholesky solve in FP64.  desc: d a multiple of
+ * 128, compressor FEDNL_RANDK_PHILOX, Option B, no PP / LS.  features: host [sum n][d] FP32.  The
+ * entry points mirror fednl_gpu_create / upload / init_shifts / run / get_*. */
+typedef struct fednl_mx_handle_s* fednl_mx_handle;
+int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out);
+int fednl_mx_destroy(fednl_mx_handle h);
+int fednl_mx_upload_client_data(fednl_mx_handle h, const float* features, const double* labels);
+int fednl_mx_init_shifts(fednl_mx_handle h, const double* x0);
+int fednl_mx_run(fednl_mx_handle h, int32_t rounds, double* grad_norms);
+int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, double* total_ms, double* per_round_ms);
+/* mean per-launch time of the round's 9 kernels (names ';'-separated), CUDA events between launches */
+int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_ms, char* names, int32_t names_len);
+int fednl_mx_get_x(fednl_mx_handle h, double* x);
+int fednl_mx_get_grad(fednl_mx_handle h, double* g);
+double fednl_mx_get_l(fednl_mx_handle h);
+
 /* ---- the reference's local driver ---------------------------------------------------------- */
 /* Callback of doptExecuteLocal (bin_fednl_local/include/TrainCallbaksShared.h:11-14): dimension,
  * ||g|| of the last round, ||g||^2 / (2 mu) and 2 ||g||^2 / mu with mu = lambda

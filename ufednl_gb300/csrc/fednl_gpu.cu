@@ -125,6 +125,35 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
 // error reporting shared with the tensor-core translation unit (fednl_mixed.cu)
 int fednl_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// The cooperative Option-B solve on caller-owned device buffers, for the mixed-precision
+// translation unit: H packed upper FP64 [d(d+1)/2], l from *lptr, dx = (H + l I)^-1 g, x -= dx
+// when xupd is given; with record, stats[0] = ||g|| and the history / round counter advance.
+// work: (d+1)(d+2)/2 doubles, ybuf and rinv: d doubles, bar: 4 x u32 (zero), status: 1 int.
+int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const double* g, double* dx, double* xupd,
+                               double* work, double* ybuf, double* rinv, unsigned* bar, int* status, double* stats,
+                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st)
+{
+    Dev P{};
+    P.d = d;
+    P.U = d * (d + 1) / 2;
+    P.work = work;
+    P.ybuf = ybuf;
+    P.rinv = rinv;
+    P.bar = bar;
+    P.status = status;
+    P.stats = stats;
+    P.hist = hist;
+    P.round_ctr = round_ctr;
+    P.hist_cap = hist_cap;
+    static int grid_cache_d = -1, grid_cache = 1;
+    if (grid_cache_d != d) {
+        grid_cache = chol_grid(d);
+        grid_cache_d = d;
+    }
+    CK(launch_chol(P, grid_cache, st, H, 0, lptr, 0.0, g, dx, xupd, record));
+    return FEDNL_OK;
+}
+
 struct fednl_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;
@@ -230,10 +259,8 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
         CKL();
     } else if (comp == FEDNL_RANDK_PHILOX) {
         MARK("k_randk_philox");
-        int hb = 2;
-        while ((1ll << hb) < h->U) ++hb;
-        k_randk_philox<<<na, 256, 0, st>>>(P.rstate, h->U, h->k, (hb + 1) / 2, h->desc.seed_base, P.sel, h->SW, P.cnt,
-                                           P.act);
+        k_randk_philox<<<na, 256, 0, st>>>(P.rstate, h->U, h->k, philox_half_bits(h->U), h->desc.seed_base, P.sel,
+                                           h->SW, P.cnt, P.act);
         CKL();
     } else if (comp == FEDNL_RANDSEQK) {
         MARK("k_randseqk");

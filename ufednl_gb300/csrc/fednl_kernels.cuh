@@ -19,6 +19,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fednl_philox.cuh"
+
 namespace fednl {
 
 constexpr int kMaxK = 9600;             // largest TopK/TopLEK k: heap, chain and staging fit in 227 KB of shared memory
@@ -1096,40 +1098,6 @@ __global__ void k_randk(unsigned* states, int n_gen, int U, int k, unsigned long
 // the images of 0..k-1 under a six-round Feistel permutation of [0, 2^(2h)) whose round function is
 // Philox4x32-10 (Salmon et al., SC'11) keyed by (seed, c), walked back into [0, U).  Every position
 // is formed independently, one thread each; the CPU oracle computes the same stream.
-__device__ __forceinline__ void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
-                                           uint32_t& o0)
-{
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r) {
-            k0 += 0x9E3779B9u;
-            k1 += 0xBB67AE85u;
-        }
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0;
-        c1 = lo1;
-        c2 = n2;
-        c3 = lo0;
-    }
-    o0 = c0;
-}
-
-__device__ __forceinline__ uint32_t philox_feistel(uint32_t x, int h, uint32_t seed, uint32_t client, uint32_t draw)
-{
-    const uint32_t mask = (1u << h) - 1u;
-    uint32_t L = x >> h, R = x & mask;
-    for (uint32_t r = 0; r < 6; ++r) {
-        uint32_t o;
-        philox4x32(R, r, draw, 0x52414E44u, seed, client, o);
-        const uint32_t nr = L ^ (o & mask);
-        L = R;
-        R = nr;
-    }
-    return (L << h) | R;
-}
-
 __global__ void k_randk_philox(unsigned* draws, int U, int k, int h, unsigned seed, unsigned* sel, int SW, int* cnt,
                                const int* act)
 {

@@ -184,3 +184,377 @@ extern "C" int fednl_gpu_weighted_gram_tf32(const float* features, const float* 
     cleanup();
     return rc;
 }
+
+// =================================================================================================
+// The mixed-precision FedNL round (dense FP32 features, RandK-Philox, Option B): client Hessians on
+// the tensor cores (TF32 x TF32 -> FP32 in TMEM) fused with the shift difference, FP32 shifts,
+// float-float margins and gradients, FP64 master H, aggregation and Cholesky solve.
+
+int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const double* g, double* dx, double* xupd,
+                               double* work, double* ybuf, double* rinv, unsigned* bar, int* status, double* stats,
+                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st);
+
+struct fednl_mx_handle_s {
+    fednl_problem_desc desc{};
+    std::vector<int32_t> ns, soff;
+    int d = 0, nc = 0, L = 0, U = 0, SW = 0, k = 0, S = 0, tiles = 0;
+    long long Up = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    fednl_tc::MxDev P{};
+    CUtensorMap map;
+    int* ns_dev = nullptr;
+    int* err = nullptr;
+    double *dx = nullptr, *work = nullptr, *ybuf = nullptr, *rinv = nullptr, *hist = nullptr;
+    unsigned* bar = nullptr;
+    int *status = nullptr, *round_ctr = nullptr;
+    int hist_cap = 1 << 16;
+    bool ready = false;
+    int rounds_done = 0;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    template <class T> int alloc(T** p, size_t n)
+    {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+            return fail_m(FEDNL_ENOMEM, "device allocation of %zu bytes failed", n * sizeof(T));
+        allocs.push_back(q);
+        *p = (T*)q;
+        return FEDNL_OK;
+    }
+};
+
+namespace {
+
+// the round's launches; with ev, an event is recorded before each kernel and after the last
+const char* const kMxKernelNames[] = {"k_mx_split_x", "k_mx_margin", "k_mx_grad", "k_mx_draw",
+                                      "k_gram_tf32", "k_mx_lk", "k_mx_apply", "k_mx_aggregate", "k_chol_coop"};
+constexpr int kMxKernels = 9;
+
+int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr)
+{
+    using namespace fednl_tc;
+    MxDev& P = h->P;
+    cudaStream_t st = h->stream;
+    int e = 0;
+    auto mark = [&]() {
+        if (ev) cudaEventRecord(ev[e++], st);
+    };
+    mark();
+    k_mx_split_x<<<(h->d + 255) / 256, 256, 0, st>>>(P);
+    mark();
+    k_mx_margin<<<dim3((h->L + 255) / 256, h->nc), 256, 0, st>>>(P);
+    mark();
+    k_mx_grad<<<(h->nc * h->d + 7) / 8, 256, 0, st>>>(P);
+    mark();
+    k_mx_draw<<<h->nc, 256, 0, st>>>(P, h->k, fednl::philox_half_bits(h->U), h->desc.seed_base);
+    mark();
+    GramJob J{h->d, h->nc, h->L, h->d / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
+    EpiDiff epi{P.shift, P.dsel, P.sel, P.fpart, h->Up, h->SW, h->tiles, (float)P.lambda};
+    k_gram_tf32<EpiDiff><<<h->nc * h->tiles, kThreads, smem_bytes(), st>>>(h->map, J, epi);
+    mark();
+    k_mx_lk<<<h->nc, 256, 0, st>>>(P);
+    mark();
+    k_mx_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
+    mark();
+    k_mx_aggregate<<<(h->d + 255) / 256, 256, 0, st>>>(P);
+    mark();
+    CKM(cudaGetLastError());
+    int rc = fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, h->dx, P.x, h->work, h->ybuf, h->rinv, h->bar,
+                                        h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st);
+    mark();
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
+{
+    if (!desc || !out) return fail_m(FEDNL_EINVAL, "null argument");
+    *out = nullptr;
+    const fednl_problem_desc& D = *desc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail_m(FEDNL_ENODEV, "no CUDA device available");
+    if (D.d < fednl_tc::kBM || D.d % fednl_tc::kBM)
+        return fail_m(FEDNL_EINVAL, "the mixed-precision form needs d a multiple of %d", fednl_tc::kBM);
+    if (D.n_clients < 1 || !D.n_samples) return fail_m(FEDNL_EINVAL, "no clients");
+    if (D.compressor != FEDNL_RANDK_PHILOX) return fail_m(FEDNL_EINVAL, "the mixed-precision form runs RandK-Philox");
+    if (D.option_a || D.line_search || D.clients_per_round)
+        return fail_m(FEDNL_EINVAL, "the mixed-precision form runs plain FedNL with Option B");
+    const long long U = (long long)D.d * (D.d + 1) / 2;
+    if (D.k < 1 || D.k > U) return fail_m(FEDNL_EINVAL, "k outside [1, U]");
+    fednl_mx_handle h = new fednl_mx_handle_s();
+    h->desc = D;
+    h->d = D.d;
+    h->nc = D.n_clients;
+    h->U = (int)U;
+    h->Up = (U + 31) / 32 * 32;
+    h->SW = (int)((U + 31) / 32);
+    h->k = D.k;
+    h->tiles = (D.d / fednl_tc::kBM) * (D.d / fednl_tc::kBM + 1) / 2;
+    h->ns.assign(D.n_samples, D.n_samples + D.n_clients);
+    h->soff.assign(h->nc + 1, 0);
+    int maxn = 0;
+    for (int c = 0; c < h->nc; ++c) {
+        if (h->ns[c] < 1) {
+            delete h;
+            return fail_m(FEDNL_EINVAL, "client %d has no samples", c);
+        }
+        h->soff[c + 1] = h->soff[c] + h->ns[c];
+        maxn = std::max(maxn, h->ns[c]);
+    }
+    h->S = h->soff[h->nc];
+    h->L = (maxn + 31) / 32 * 32;
+    fednl_tc::MxDev& P = h->P;
+    P.d = h->d;
+    P.nc = h->nc;
+    P.L = h->L;
+    P.U = h->U;
+    P.Up = h->Up;
+    P.SW = h->SW;
+    P.tiles = h->tiles;
+    P.lambda = D.lambda;
+    P.alpha = D.alpha;
+    P.inv_n = 1.0 / (double)h->nc;
+    P.prescale = P.inv_n * D.alpha;
+    P.mult = (double)U / (double)h->k;
+    const size_t ncL = (size_t)h->nc * h->L, ncUp = (size_t)h->nc * h->Up;
+    int rc = 0;
+    float* X;
+    double* lab;
+    rc |= h->alloc(&h->ns_dev, h->nc);
+    rc |= h->alloc(&X, (size_t)h->nc * h->d * h->L);
+    rc |= h->alloc(&lab, ncL);
+    rc |= h->alloc(&P.x, h->d);
+    rc |= h->alloc(&P.xh, h->d);
+    rc |= h->alloc(&P.xl, h->d);
+    rc |= h->alloc(&P.Dw, ncL);
+    rc |= h->alloc(&P.qh, ncL);
+    rc |= h->alloc(&P.ql, ncL);
+    rc |= h->alloc(&P.gc, (size_t)h->nc * h->d);
+    rc |= h->alloc(&P.g, h->d);
+    rc |= h->alloc(&P.H, h->U);
+    rc |= h->alloc(&P.shift, ncUp);
+    rc |= h->alloc(&P.dsel, ncUp);
+    rc |= h->alloc(&P.sel, (size_t)h->nc * h->SW);
+    rc |= h->alloc(&P.draws, h->nc);
+    rc |= h->alloc(&P.fpart, (size_t)h->nc * h->tiles * 128);
+    rc |= h->alloc(&P.lk, h->nc);
+    rc |= h->alloc(&P.stats, 4);
+    rc |= h->alloc(&h->err, 1);
+    rc |= h->alloc(&h->dx, h->d);
+    rc |= h->alloc(&h->work, (size_t)(h->d + 1) * (h->d + 2) / 2);
+    rc |= h->alloc(&h->ybuf, h->d);
+    rc |= h->alloc(&h->rinv, h->d);
+    rc |= h->alloc(&h->hist, h->hist_cap);
+    rc |= h->alloc(&h->bar, 4);
+    rc |= h->alloc(&h->status, 1);
+    rc |= h->alloc(&h->round_ctr, 1);
+    if (rc || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        fednl_mx_destroy(h);
+        return rc ? rc : fail_m(FEDNL_ECUDA, "stream creation failed");
+    }
+    P.X = X;
+    P.lab = lab;
+    P.ns = h->ns_dev;
+    if (cudaMemcpy(h->ns_dev, h->ns.data(), h->nc * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(X, 0, (size_t)h->nc * h->d * h->L * 4) != cudaSuccess || cudaMemset(lab, 0, ncL * 8) != cudaSuccess ||
+        cudaMemset(P.Dw, 0, ncL * 4) != cudaSuccess || cudaMemset(P.qh, 0, ncL * 4) != cudaSuccess ||
+        cudaMemset(P.ql, 0, ncL * 4) != cudaSuccess || cudaMemset(P.dsel, 0, ncUp * 4) != cudaSuccess ||
+        cudaMemset(P.draws, 0, h->nc * 4) != cudaSuccess || cudaMemset(h->err, 0, 4) != cudaSuccess ||
+        cudaMemset(h->bar, 0, 16) != cudaSuccess || cudaMemset(h->status, 0, 4) != cudaSuccess ||
+        cudaMemset(h->round_ctr, 0, 4) != cudaSuccess || cudaMemset(P.stats, 0, 32) != cudaSuccess) {
+        fednl_mx_destroy(h);
+        return fail_m(FEDNL_ECUDA, "initial copies failed");
+    }
+    rc = make_feature_map(&h->map, X, h->L, h->d, h->nc);
+    if (rc || cudaFuncSetAttribute(fednl_tc::k_gram_tf32<fednl_tc::EpiDiff>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)fednl_tc::smem_bytes()) != cudaSuccess ||
+        cudaFuncSetAttribute(fednl_tc::k_gram_tf32<fednl_tc::EpiInitShift>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fednl_tc::smem_bytes()) != cudaSuccess) {
+        fednl_mx_destroy(h);
+        return rc ? rc : fail_m(FEDNL_ECUDA, "shared-memory attribute refused");
+    }
+    *out = h;
+    return FEDNL_OK;
+}
+
+int fednl_mx_destroy(fednl_mx_handle h)
+{
+    if (!h) return FEDNL_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return FEDNL_OK;
+}
+
+int fednl_mx_upload_client_data(fednl_mx_handle h, const float* features, const double* labels)
+{
+    if (!h || !features || !labels) return fail_m(FEDNL_EINVAL, "null argument");
+    for (int s = 0; s < h->S; ++s)
+        if (labels[s] != 1.0 && labels[s] != -1.0) return fail_m(FEDNL_EINVAL, "label %d is not +-1", s);
+    float* dA = nullptr;
+    int* dsoff = nullptr;
+    if (cudaMalloc(&dA, (size_t)h->S * h->d * 4) != cudaSuccess || cudaMalloc(&dsoff, (h->nc + 1) * 4) != cudaSuccess) {
+        cudaFree(dA);
+        return fail_m(FEDNL_ENOMEM, "staging allocation failed");
+    }
+    std::vector<double> labp((size_t)h->nc * h->L, 0.0);
+    for (int c = 0; c < h->nc; ++c)
+        for (int s = 0; s < h->ns[c]; ++s) labp[(size_t)c * h->L + s] = labels[h->soff[c] + s];
+    int rc = FEDNL_OK;
+    if (cudaMemcpy(dA, features, (size_t)h->S * h->d * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dsoff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((void*)h->P.lab, labp.data(), labp.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = fail_m(FEDNL_ECUDA, "upload failed");
+    } else {
+        k_to_feature_major<<<dim3(h->L / 32, (h->d + 31) / 32, h->nc), dim3(32, 8)>>>(dA, dsoff, h->d, h->L, h->nc,
+                                                                                      (float*)h->P.X);
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "layout kernel failed");
+    }
+    cudaFree(dA);
+    cudaFree(dsoff);
+    return rc;
+}
+
+int fednl_mx_init_shifts(fednl_mx_handle h, const double* x0)
+{
+    using namespace fednl_tc;
+    if (!h) return fail_m(FEDNL_EINVAL, "null handle");
+    MxDev& P = h->P;
+    cudaStream_t st = h->stream;
+    if (x0) CKM(cudaMemcpyAsync(P.x, x0, h->d * 8, cudaMemcpyHostToDevice, st));
+    else CKM(cudaMemsetAsync(P.x, 0, h->d * 8, st));
+    k_mx_split_x<<<(h->d + 255) / 256, 256, 0, st>>>(P);
+    k_mx_margin<<<dim3((h->L + 255) / 256, h->nc), 256, 0, st>>>(P);
+    GramJob J{h->d, h->nc, h->L, h->d / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
+    EpiInitShift epi{P.shift, h->Up, (float)P.lambda};
+    k_gram_tf32<EpiInitShift><<<h->nc * h->tiles, kThreads, smem_bytes(), st>>>(h->map, J, epi);
+    k_mx_hinit<<<(h->U + 255) / 256, 256, 0, st>>>(P);
+    CKM(cudaGetLastError());
+    CKM(cudaStreamSynchronize(st));
+    int err = 0;
+    CKM(cudaMemcpy(&err, h->err, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail_m(FEDNL_ETIMEOUT, "a bounded wait of the Gram kernel ran out");
+    h->ready = true;
+    h->rounds_done = 0;
+    return FEDNL_OK;
+}
+
+int fednl_mx_run(fednl_mx_handle h, int32_t rounds, double* grad_norms)
+{
+    if (!h || !h->ready) return fail_m(FEDNL_EINVAL, "call fednl_mx_init_shifts first");
+    if (!h->gexec) {
+        CKM(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = mx_launch_round(h);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail_m(FEDNL_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        h->graph = g;
+        CKM(cudaGraphInstantiate(&h->gexec, g, 0));
+    }
+    for (int r = 0; r < rounds; ++r) CKM(cudaGraphLaunch(h->gexec, h->stream));
+    CKM(cudaStreamSynchronize(h->stream));
+    const int first = h->rounds_done;
+    h->rounds_done += rounds;
+    if (grad_norms && rounds > 0) {
+        const int have = std::max(0, std::min(rounds, h->hist_cap - first));
+        if (have) CKM(cudaMemcpy(grad_norms, h->hist + first, (size_t)have * 8, cudaMemcpyDeviceToHost));
+    }
+    int err = 0, status = 0;
+    CKM(cudaMemcpy(&err, h->err, 4, cudaMemcpyDeviceToHost));
+    CKM(cudaMemcpy(&status, h->status, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail_m(FEDNL_ETIMEOUT, "a bounded wait of the Gram kernel ran out");
+    if (status == FEDNL_ETIMEOUT) return fail_m(status, "grid barrier of the Cholesky timed out");
+    if (status) return fail_m(status, "Option-B matrix not positive definite in one of the rounds");
+    return FEDNL_OK;
+}
+
+int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, double* total_ms, double* per_round_ms)
+{
+    if (!h || rounds < 1 || !total_ms) return fail_m(FEDNL_EINVAL, "bad argument");
+    int rc = fednl_mx_run(h, 0, nullptr);      // builds the graph
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev(rounds + 1);
+    for (auto& e : ev) CKM(cudaEventCreate(&e));
+    CKM(cudaEventRecord(ev[0], h->stream));
+    for (int r = 0; r < rounds; ++r) {
+        CKM(cudaGraphLaunch(h->gexec, h->stream));
+        CKM(cudaEventRecord(ev[r + 1], h->stream));
+    }
+    CKM(cudaStreamSynchronize(h->stream));
+    float tot = 0.f;
+    cudaEventElapsedTime(&tot, ev[0], ev[rounds]);
+    *total_ms = tot;
+    for (int r = 0; r < rounds && per_round_ms; ++r) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[r], ev[r + 1]);
+        per_round_ms[r] = ms;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    h->rounds_done += rounds;
+    return FEDNL_OK;
+}
+
+int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_ms, char* names, int32_t names_len)
+{
+    if (!h || !h->ready || rounds < 1 || !kernel_ms) return fail_m(FEDNL_EINVAL, "bad argument");
+    std::vector<cudaEvent_t> ev((size_t)rounds * (kMxKernels + 1));
+    for (auto& e : ev) CKM(cudaEventCreate(&e));
+    int rc = FEDNL_OK;
+    for (int r = 0; r < rounds && !rc; ++r) rc = mx_launch_round(h, &ev[(size_t)r * (kMxKernels + 1)]);
+    CKM(cudaStreamSynchronize(h->stream));
+    for (int t = 0; t < kMxKernels; ++t) {
+        double acc = 0.0;
+        for (int r = 0; r < rounds; ++r) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[(size_t)r * (kMxKernels + 1) + t], ev[(size_t)r * (kMxKernels + 1) + t + 1]);
+            acc += ms;
+        }
+        kernel_ms[t] = acc / rounds;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (names && names_len > 0) {
+        std::string all;
+        for (int t = 0; t < kMxKernels; ++t) all += std::string(t ? ";" : "") + kMxKernelNames[t];
+        snprintf(names, (size_t)names_len, "%s", all.c_str());
+    }
+    h->rounds_done += rounds;
+    return rc;
+}
+
+int fednl_mx_get_x(fednl_mx_handle h, double* x)
+{
+    if (!h || !x) return fail_m(FEDNL_EINVAL, "null argument");
+    CKM(cudaStreamSynchronize(h->stream));
+    CKM(cudaMemcpy(x, h->P.x, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_mx_get_grad(fednl_mx_handle h, double* g)
+{
+    if (!h || !g) return fail_m(FEDNL_EINVAL, "null argument");
+    CKM(cudaStreamSynchronize(h->stream));
+    CKM(cudaMemcpy(g, h->P.g, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+double fednl_mx_get_l(fednl_mx_handle h)
+{
+    if (!h) return NAN;
+    double st[2] = {NAN, NAN};
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(st, h->P.stats, 16, cudaMemcpyDeviceToHost);
+    return st[1];
+}
+
+}  // extern "C"

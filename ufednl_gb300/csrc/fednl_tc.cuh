@@ -24,6 +24,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include "fednl_philox.cuh"
+
 namespace fednl_tc {
 
 constexpr int kBM = 128, kBN = 128, kBK = 32;     // tile rows, tile columns, FP32 samples per slab
@@ -157,8 +159,9 @@ __device__ __forceinline__ void upper_tile(int t, int nb, int& mi, int& ni)
     ni = i + rem;
 }
 
-// Epilogue functor: operator()(client, row m, first column n0, 16 FP32 values) for every row of
-// the tile (called by the 128 epilogue threads, 8 times each).
+// Epilogue functor: operator()(client, row m, first column n0, 16 FP32 values, acc) for every row
+// of the tile (called by the 128 epilogue threads, 8 times each, acc a per-thread Epi::Acc), then
+// finish(client, tile, thread 0..127, acc).
 template <class Epi>
 __global__ void __launch_bounds__(kThreads) k_gram_tf32(const __grid_constant__ CUtensorMap tmX, GramJob J, Epi epi)
 {
@@ -265,12 +268,14 @@ __global__ void __launch_bounds__(kThreads) k_gram_tf32(const __grid_constant__ 
         if (ok) {
             const int quarter = warp & 3;
             const int m = mi * kBM + quarter * 32 + lane;
+            typename Epi::Acc acc{};
 #pragma unroll 1
             for (int j = 0; j < kBN / 16; ++j) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(j * 16), v);
-                epi(c, m, ni * kBN + j * 16, v);
+                epi(c, m, ni * kBN + j * 16, v, acc);
             }
+            epi.finish(c, t, quarter * 32 + lane, acc);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -292,15 +297,257 @@ __global__ void __launch_bounds__(kThreads) k_gram_tf32(const __grid_constant__ 
 // Epilogue writing the raw tile (plus lambda on the diagonal) into a full row-major d x d FP32
 // matrix per client: out[c][m][n]
 struct EpiStore {
+    struct Acc {};
     float* out;
     int d;
     float lambda;
-    __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v) const
+    __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v, Acc&) const
     {
         float* row = out + ((size_t)c * d + m) * d + n0;
 #pragma unroll
         for (int i = 0; i < 16; ++i) row[i] = v[i] + ((m == n0 + i) ? lambda : 0.0f);
     }
+    __device__ __forceinline__ void finish(int, int, int, const Acc&) const {}
 };
+
+// packed upper position of (m, n), m <= n
+__device__ __forceinline__ long long upos(int m, int n) { return (long long)n * (n + 1) / 2 + m; }
+
+// Initial shifts: shift_c = H_c(x0) in FP32, packed upper (the lanes of a warp hold consecutive
+// rows m, so for each column n they touch consecutive packed positions)
+struct EpiInitShift {
+    struct Acc {};
+    float* shift;          // [nc][Up]
+    long long Up;
+    float lambda;
+    __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v, Acc&) const
+    {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int n = n0 + i;
+            if (m <= n) shift[(size_t)c * Up + upos(m, n)] = v[i] + (m == n ? lambda : 0.0f);
+        }
+    }
+    __device__ __forceinline__ void finish(int, int, int, const Acc&) const {}
+};
+
+// Round epilogue: diff = H_c - shift_c on the upper triangle; per-thread weighted sum of squares
+// (diagonal once, off-diagonal twice: the full symmetric matrix) into fpart[c][tile][thread]; the
+// differences at the client's selected positions into dsel[c][p]
+struct EpiDiff {
+    struct Acc {
+        float sq = 0.0f;
+    };
+    const float* shift;    // [nc][Up]
+    float* dsel;           // [nc][Up]
+    const unsigned* sel;   // [nc][SW]
+    float* fpart;          // [nc][tiles][128]
+    long long Up;
+    int SW, tiles;
+    float lambda;
+    __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v, Acc& a) const
+    {
+        const unsigned* sc = sel + (size_t)c * SW;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int n = n0 + i;
+            if (m <= n) {
+                const long long p = upos(m, n);
+                const float df = (v[i] + (m == n ? lambda : 0.0f)) - shift[(size_t)c * Up + p];
+                a.sq = fmaf(m == n ? df : 2.0f * df, df, a.sq);
+                if ((sc[p >> 5] >> (p & 31)) & 1u) dsel[(size_t)c * Up + p] = df;
+            }
+        }
+    }
+    __device__ __forceinline__ void finish(int c, int t, int th, const Acc& a) const
+    {
+        fpart[((size_t)c * tiles + t) * 128 + th] = a.sq;
+    }
+};
+
+
+// ---- mixed-precision round kernels (dense FP32 features, feature-major [nc][d][L]) ------------
+// Margins and gradients need FP64-grade sums (the final ||grad|| is ~1e-9 of terms of order 1), and
+// GB300 issues a warp's FP64 instruction about once per 64 cycles; both are therefore formed with
+// FP32 pairs ("float-float"): each product x * (y_hi + y_lo) as an exact two-product plus the small
+// cross term, accumulated with two-sum (Dekker / Knuth) -- roughly 2^-44 relative, at the FP32 rate.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float p, float e)
+{
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+
+__device__ __forceinline__ void ff_mac(float& hi, float& lo, float x, float yh, float yl)
+{
+    const float p = __fmul_rn(x, yh);
+    const float e = __fadd_rn(fmaf(x, yh, -p), __fmul_rn(x, yl));
+    ff_add(hi, lo, p, e);
+}
+
+__device__ __forceinline__ void split_ff(double v, float& h, float& l)
+{
+    h = __double2float_rn(v);
+    l = __double2float_rn(v - (double)h);
+}
+
+struct MxDev {
+    int d, nc, L, U, SW, tiles;
+    long long Up;
+    double lambda, alpha, prescale, inv_n, mult;
+    const int* ns;          // [nc]
+    const float* X;         // [nc][d][L]
+    const double* lab;      // [nc][L] labels (+-1, 0 beyond n)
+    double* x;              // [d]
+    float* xh;              // [d] split iterate
+    float* xl;
+    float* Dw;              // [nc][L] Gram weights D_s
+    float* qh;              // [nc][L] gradient weights b_s q_s as FP32 pairs
+    float* ql;
+    double* gc;             // [nc][d]
+    double* g;              // [d]
+    double* H;              // [U] master, packed upper
+    float* shift;           // [nc][Up]
+    float* dsel;            // [nc][Up]
+    unsigned* sel;          // [nc][SW]
+    unsigned* draws;        // [nc]
+    float* fpart;           // [nc][tiles][128]
+    double* lk;             // [nc]
+    double* stats;          // [4]: ||g||, l
+};
+
+__global__ void k_mx_split_x(MxDev P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.d) split_ff(P.x[i], P.xh[i], P.xl[i]);
+}
+
+// margin m_s = b_s a_s^T x, sigmoid (FP64), D_s (Gram weight, FP32) and b_s q_s (FP32 pair)
+__device__ __forceinline__ double mx_sigmoid(double m) { return 1.0 / (1.0 + exp(-m)); }
+
+__global__ void __launch_bounds__(256) k_mx_margin(MxDev P)
+{
+    __shared__ float s_xh[1024], s_xl[1024];
+    const int c = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = threadIdx.x; i < P.d && i < 1024; i += blockDim.x) {
+        s_xh[i] = P.xh[i];
+        s_xl[i] = P.xl[i];
+    }
+    __syncthreads();
+    const int n = P.ns[c];
+    if (s >= n) return;
+    const float* col = P.X + (size_t)c * P.d * P.L + s;
+    float hi = 0.0f, lo = 0.0f;
+    for (int i = 0; i < P.d; ++i) {
+        const float xv = col[(size_t)i * P.L];
+        const float yh = i < 1024 ? s_xh[i] : P.xh[i], yl = i < 1024 ? s_xl[i] : P.xl[i];
+        ff_mac(hi, lo, xv, yh, yl);
+    }
+    const double b = P.lab[(size_t)c * P.L + s];
+    const double m = b * ((double)hi + (double)lo);
+    const double sig = mx_sigmoid(m);
+    const double inv_n = 1.0 / (double)n;
+    const double z1 = 1.0 - sig;
+    P.Dw[(size_t)c * P.L + s] = (float)(inv_n * (z1 * sig));
+    const double q = b * (z1 * -inv_n);
+    split_ff(q, P.qh[(size_t)c * P.L + s], P.ql[(size_t)c * P.L + s]);
+}
+
+// client gradients: one warp per (client, feature), lanes over the samples
+__global__ void __launch_bounds__(256) k_mx_grad(MxDev P)
+{
+    const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (wid >= P.nc * P.d) return;
+    const int c = wid / P.d, i = wid - c * P.d;
+    const int n = P.ns[c];
+    const float* row = P.X + ((size_t)c * P.d + i) * P.L;
+    const float* qh = P.qh + (size_t)c * P.L;
+    const float* ql = P.ql + (size_t)c * P.L;
+    float hi = 0.0f, lo = 0.0f;
+    for (int s = lane; s < n; s += 32) ff_mac(hi, lo, row[s], qh[s], ql[s]);
+    double v = (double)hi + (double)lo;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) P.gc[(size_t)c * P.d + i] = v + P.lambda * P.x[i];
+}
+
+// RandK-Philox draw of every client (the FP64 engine's stream)
+__global__ void k_mx_draw(MxDev P, int k, int h, unsigned seed)
+{
+    const int c = blockIdx.x;
+    unsigned* sc = P.sel + (size_t)c * P.SW;
+    for (int w = threadIdx.x; w < P.SW; w += blockDim.x) sc[w] = 0u;
+    const unsigned draw = P.draws[c];
+    __syncthreads();
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        uint32_t y = fednl::philox_feistel((uint32_t)i, h, seed, (uint32_t)c, draw);
+        while (y >= (uint32_t)P.U) y = fednl::philox_feistel(y, h, seed, (uint32_t)c, draw);
+        atomicOr(&sc[y >> 5], 1u << (y & 31));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) P.draws[c] = draw + 1;
+}
+
+// Lk = ||H_c - shift_c||_F from the Gram epilogue's partial sums
+__global__ void k_mx_lk(MxDev P)
+{
+    const int c = blockIdx.x;
+    const float* fp = P.fpart + (size_t)c * P.tiles * 128;
+    double v = 0.0;
+    for (int t = threadIdx.x; t < P.tiles * 128; t += blockDim.x) v += (double)fp[t];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ double s_w[32];
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
+        P.lk[c] = sqrt(t);
+    }
+}
+
+// worker shift update (FP32) and master merge (FP64), clients in order per position
+__global__ void k_mx_apply(MxDev P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.U) return;
+    double h = P.H[p];
+    const unsigned bit = 1u << (p & 31);
+    for (int c = 0; c < P.nc; ++c) {
+        if (!(P.sel[(size_t)c * P.SW + (p >> 5)] & bit)) continue;
+        const size_t q = (size_t)c * P.Up + p;
+        const double item = (double)P.dsel[q] * P.mult;
+        P.shift[q] = (float)((double)P.shift[q] + P.alpha * item);
+        h += item * P.prescale;
+    }
+    P.H[p] = h;
+}
+
+// g = mean g_c, l = mean Lk
+__global__ void k_mx_aggregate(MxDev P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.d) {
+        double v = 0.0;
+        for (int c = 0; c < P.nc; ++c) v += P.gc[(size_t)c * P.d + i];
+        P.g[i] = v * P.inv_n;
+    }
+    if (i == 0) {
+        double l = 0.0;
+        for (int c = 0; c < P.nc; ++c) l += P.lk[c];
+        P.stats[1] = l * P.inv_n;
+    }
+}
+
+// H = mean of the initial shifts (FP64 sum of the FP32 shifts, clients in order)
+__global__ void k_mx_hinit(MxDev P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.U) return;
+    double h = 0.0;
+    for (int c = 0; c < P.nc; ++c) h += (double)P.shift[(size_t)c * P.Up + p];
+    P.H[p] = h * P.inv_n;
+}
 
 }  // namespace fednl_tc

@@ -96,6 +96,28 @@ def workload_dense_1024() -> Problem:
     return dense_problem(1002, 1024, ns, 1e-4, name="dense d1024 256 clients n_i 512-4096")
 
 
+def dense_problem_fp32(seed: int, d: int, n_samples, lam: float, name: str = "") -> Problem:
+    """Dense N(0,1) features kept as FP32 (no intercept column), labels from a planted
+    w* ~ N(0, I/d): the mixed-precision configuration.  features has dtype float32."""
+    rng = np.random.default_rng(seed)
+    ns = np.asarray(n_samples, dtype=np.int32)
+    s = int(ns.sum())
+    a = rng.standard_normal((s, d), dtype=np.float32)
+    w = rng.normal(0.0, 1.0 / np.sqrt(d), size=d).astype(np.float32)
+    z = a @ w
+    p = 1.0 / (1.0 + np.exp(-z.astype(np.float64)))
+    y = np.where(rng.random(s) < p, 1.0, -1.0)
+    return Problem(d=d, n_samples=ns, features=a, labels=y, lam=lam, name=name)
+
+
+def workload_dense_fp32_1024() -> Problem:
+    """The mixed-precision workload: d=1024 dense N(0,1) FP32 features, 256 clients,
+    n_i ~ U{512..4096} (seed 2), lambda 1e-4, planted labels."""
+    rng = np.random.default_rng(2)
+    ns = rng.integers(512, 4097, size=256)
+    return dense_problem_fp32(1002, 1024, ns, 1e-4, name="dense FP32 d1024 256 clients n_i 512-4096")
+
+
 def workload_phishing_pp() -> Problem:
     """d=69 (68 Bernoulli(0.45) + intercept), 2048 clients x 6 samples, lambda 1e-3, seed 3."""
     return binary_problem(3, 69, [6] * 2048, 0.45, 1e-3, name="phishing-like d69 2048x6")

@@ -58,7 +58,9 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_randseqk", "fednl_gpu_natural", "fednl_gpu_logreg_oracle", "fednl_gpu_optionb_solve",
            "fednl_gpu_optionb_solve_noalloc", "fednl_gpu_time_rounds", "fednl_gpu_profile_kernels",
            "fednl_gpu_last_error", "fednl_gpu_execute_local", "fednl_gpu_load_libsvm",
-           "fednl_gpu_weighted_gram_tf32"]
+           "fednl_gpu_weighted_gram_tf32", "fednl_mx_create", "fednl_mx_destroy", "fednl_mx_upload_client_data",
+           "fednl_mx_init_shifts", "fednl_mx_run", "fednl_mx_time_rounds", "fednl_mx_get_x", "fednl_mx_get_grad",
+           "fednl_mx_get_l", "fednl_mx_profile_kernels"]
 
 _lib = None
 
@@ -117,6 +119,15 @@ def load(build_if_missing: bool = True):
     fp = C.POINTER(C.c_float)
     L.fednl_gpu_weighted_gram_tf32.argtypes = [fp, fp, ip, C.c_int32, C.c_int32, C.c_float, fp]
     L.fednl_gpu_weighted_gram_tf32.restype = C.c_int
+    for name, args in {"fednl_mx_create": [C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)], "fednl_mx_destroy": [vp],
+                       "fednl_mx_upload_client_data": [vp, fp, dp], "fednl_mx_init_shifts": [vp, dp],
+                       "fednl_mx_run": [vp, C.c_int32, dp], "fednl_mx_time_rounds": [vp, C.c_int32, dp, dp],
+                       "fednl_mx_get_x": [vp, dp], "fednl_mx_get_grad": [vp, dp],
+                       "fednl_mx_profile_kernels": [vp, C.c_int32, dp, C.c_char_p, C.c_int32]}.items():
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = C.c_int
+    L.fednl_mx_get_l.argtypes = [vp]
+    L.fednl_mx_get_l.restype = C.c_double
     L.fednl_gpu_load_libsvm.argtypes = [C.c_char_p, C.c_int32, ip, ip, dp, dp]
     L.fednl_gpu_load_libsvm.restype = C.c_int
     L.fednl_gpu_execute_local.argtypes = [C.c_char_p, RESULT_CALLBACK]
@@ -394,3 +405,70 @@ def weighted_gram_tf32(features, weights, n_samples, lam: float = 0.0) -> np.nda
     _check(load().fednl_gpu_weighted_gram_tf32(f.ctypes.data_as(fp), w.ctypes.data_as(fp), _ip(ns), len(ns), d,
                                                float(lam), out.ctypes.data_as(fp)))
     return out
+
+
+class MixedFedNL:
+    """The mixed-precision FedNL round (dense FP32 features, RandK-Philox, Option B): client
+    Hessians on the tensor cores, FP64 master and solve."""
+
+    def __init__(self, prob, k: int, alpha: float, seed_base: int = 123, x0=None):
+        self.d = prob.d
+        self.n_clients = prob.n_clients
+        self._ns = np.ascontiguousarray(prob.n_samples, dtype=np.int32)
+        desc = ProblemDesc(self.d, 0, self.n_clients, _ip(self._ns), float(prob.lam), RANDK_PHILOX, int(k),
+                           float(alpha), 1, int(seed_base), 1234, 2, 0, 1234, 0, 0, 0.5, 0.5, 5, 0,
+                           (C.c_int32 * 2)(0, 0))
+        h = C.c_void_p()
+        _check(load().fednl_mx_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        try:
+            f = np.ascontiguousarray(prob.features, dtype=np.float32)
+            b = np.ascontiguousarray(prob.labels, dtype=np.float64)
+            _check(load().fednl_mx_upload_client_data(self._h, f.ctypes.data_as(C.POINTER(C.c_float)), _dp(b)))
+            xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+            _check(load().fednl_mx_init_shifts(self._h, _dp(xx) if xx is not None else None))
+        except Exception:
+            self.close()
+            raise
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().fednl_mx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, rounds: int) -> np.ndarray:
+        out = np.empty(rounds)
+        _check(load().fednl_mx_run(self._h, rounds, _dp(out)))
+        return out
+
+    def time_rounds(self, rounds: int):
+        tot = C.c_double(0.0)
+        per = np.empty(rounds)
+        _check(load().fednl_mx_time_rounds(self._h, rounds, C.byref(tot), _dp(per)))
+        return tot.value, per
+
+    def profile_kernels(self, rounds: int):
+        ms = np.zeros(16)
+        buf = C.create_string_buffer(1024)
+        _check(load().fednl_mx_profile_kernels(self._h, rounds, _dp(ms), buf, 1024))
+        names = buf.value.decode().split(";")
+        return [(names[t], float(ms[t])) for t in range(len(names))]
+
+    def x(self) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_mx_get_x(self._h, _dp(out)))
+        return out
+
+    def grad(self) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_mx_get_grad(self._h, _dp(out)))
+        return out
+
+    def l(self) -> float:
+        return load().fednl_mx_get_l(self._h)
