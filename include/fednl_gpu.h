@@ -222,13 +222,16 @@ const char* fednl_gpu_last_error(void);
 int fednl_gpu_weighted_gram_tf32(const float* features, const float* weights, const int32_t* n_samples,
                                  int32_t n_clients, int32_t d, float lambda, float* out);
 
-/* ---- the mixed-precision round (dense FP32 features) --------------------------------------- */
+/* ---- the mixed-precision round (FP32 features) --------------------------------------------- */
 /* The FedNL round with client Hessians on the tensor cores: per client H_c = X_c^T diag(D) X_c +
- * lambda I in TF32 with FP32 accumulation (tcgen05), fused with the FP32 shift difference, its
- * Frobenius norm and the RandK-Philox selection; margins and gradients in FP32 pairs (about 2^-44
- * relative); master H, aggregation and the Option-B Cholesky solve in FP64.  desc: d a multiple of
- * 128, compressor FEDNL_RANDK_PHILOX, Option B, no PP / LS.  features: host [sum n][d] FP32.  The
- * entry points mirror fednl_gpu_create / upload / init_shifts / run / get_*. */
+ * lambda I in TF32 with FP32 accumulation (tcgen05; d padded to a multiple of 128 with zero
+ * features), fused with the FP32 shift difference and its Frobenius norm; margins and gradients in
+ * FP32 pairs (about 2^-44 relative); master H, aggregation and the Option-B Cholesky solve in FP64.
+ * Compressors: FEDNL_RANDK_PHILOX (selection fused into the Gram epilogue), FEDNL_TOPK and
+ * FEDNL_TOPLEK on the FP32 differences (radix select of the k largest magnitudes, ties to the lower
+ * packed position; TopLEK's window rule on that set with a Philox draw for the boundary entry).
+ * desc: Option B, no PP / LS.  features: host [sum n][d] FP32.  The entry points mirror
+ * fednl_gpu_create / upload / init_shifts / run / get_*. */
 typedef struct fednl_mx_handle_s* fednl_mx_handle;
 int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out);
 int fednl_mx_destroy(fednl_mx_handle h);
@@ -241,6 +244,77 @@ int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_m
 int fednl_mx_get_x(fednl_mx_handle h, double* x);
 int fednl_mx_get_grad(fednl_mx_handle h, double* g);
 double fednl_mx_get_l(fednl_mx_handle h);
+/* the last round's FP32 differences H_c - shift_c (packed upper, [U]; RandK-Philox: only the
+ * selected positions are current), selected packed positions, and the FP32 shift of a client */
+int fednl_mx_get_diff(fednl_mx_handle h, int32_t client, float* diff);
+int fednl_mx_get_selection(fednl_mx_handle h, int32_t client, uint32_t* pos, int32_t* count);
+int fednl_mx_get_shift(fednl_mx_handle h, int32_t client, float* shift);
+
+/* ---- serving: a round split into its client phase and a batched solve ------------------------ */
+/* Everything of one round up to the master's aggregation, on the handle's stream (plain FedNL). */
+int fednl_gpu_client_phase(fednl_handle h);
+int fednl_mx_client_phase(fednl_mx_handle h);
+/* The Option-B solves that end the rounds of every listed handle in one cooperative launch (each
+ * problem gets a group of CTAs and its own barrier words; more problems than resident CTAs take
+ * successive launches).  Results equal those of fednl_gpu_round bit for bit. */
+int fednl_gpu_solve_batch(fednl_handle* handles, int32_t n, fednl_mx_handle* mixed, int32_t n_mixed);
+/* waits for the handle's last round and reports it as fednl_gpu_round does */
+int fednl_gpu_round_result(fednl_handle h, fednl_round_stats* stats);
+int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats);
+/* free and total device memory (admission by free memory) */
+int fednl_gpu_mem_info(int64_t* free_bytes, int64_t* total_bytes);
+/* device bytes a handle of this desc holds: its state plus (FP64) a dense bound on the client data
+ * or (mixed) the padded feature-major copy and the upload's staging buffer */
+int fednl_gpu_footprint(const fednl_problem_desc* desc, int64_t* bytes);
+int fednl_mx_footprint(const fednl_problem_desc* desc, int64_t* bytes);
+
+/* ---- the serving loop ------------------------------------------------------------------------
+ * Independent problems are submitted at any time (the client data is copied), admitted in arrival
+ * order as device memory (footprint + reserve <= free, held footprints <= budget) and live slots
+ * allow, and advance one round per fednl_server_tick: every live problem's client phase on its own
+ * stream, then one batched Option-B solve launch for all of them.  A problem retires when its ||g||
+ * is at most its tolerance or it has run max_rounds rounds; its iterate stays readable. */
+typedef enum fednl_precision {
+    FEDNL_PRECISION_FP64 = 0,   /* the FP64 engine (features: double, S x d row-major) */
+    FEDNL_PRECISION_MIXED = 1   /* the mixed-precision engine (features: float, S x d row-major) */
+} fednl_precision;
+
+typedef enum fednl_problem_state {
+    FEDNL_PROBLEM_QUEUED = 0,
+    FEDNL_PROBLEM_LIVE = 1,
+    FEDNL_PROBLEM_DONE = 2,
+    FEDNL_PROBLEM_FAILED = 3
+} fednl_problem_state;
+
+typedef struct fednl_problem_status {
+    int32_t state;              /* fednl_problem_state */
+    int32_t rounds;             /* rounds run */
+    int32_t error;              /* status code of a failed problem */
+    int32_t d;
+    double grad_norm;           /* ||g|| of the last round (-1 before the first) */
+    double t_submit_ms, t_admit_ms, t_done_ms;   /* since fednl_server_create; -1 until reached */
+    int64_t bytes;              /* admission footprint */
+} fednl_problem_status;
+
+typedef struct fednl_tick_stats {
+    int32_t live;               /* problems that ran a round in this tick */
+    int32_t admitted, retired, pending;
+    double tick_ms;             /* host wall time of the round phase */
+    int64_t held_bytes;         /* footprints of the problems live after the tick */
+    int64_t device_free, device_total;
+} fednl_tick_stats;
+
+typedef struct fednl_server_s* fednl_server;
+/* budget_bytes: cap on the live problems' footprints (0: none); reserve_bytes: device memory left
+ * free; max_live: live-slot limit (0: none) */
+int fednl_server_create(int64_t budget_bytes, int64_t reserve_bytes, int32_t max_live, fednl_server* out);
+int fednl_server_destroy(fednl_server s);
+int fednl_server_submit(fednl_server s, const fednl_problem_desc* desc, int32_t precision, const void* features,
+                        const double* labels, double tol, int32_t max_rounds, int64_t* id);
+int fednl_server_tick(fednl_server s, fednl_tick_stats* stats);
+int fednl_server_status(fednl_server s, int64_t id, fednl_problem_status* status, double* x /* [d] or NULL */);
+/* per (problem, round) latencies in ms, in completion order; count = how many were recorded */
+int fednl_server_latencies(fednl_server s, double* out, int64_t cap, int64_t* count);
 
 /* ---- the reference's local driver ---------------------------------------------------------- */
 /* Callback of doptExecuteLocal (bin_fednl_local/include/TrainCallbaksShared.h:11-14): dimension,

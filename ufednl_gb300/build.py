@@ -17,7 +17,7 @@ REPO = os.path.dirname(PKG)
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libfednl_gpu.so")
 SOURCES = [os.path.join(PKG, "csrc", "fednl_gpu.cu"), os.path.join(PKG, "csrc", "fednl_mixed.cu"),
-           os.path.join(PKG, "csrc", "fednl_local.cpp")]
+           os.path.join(PKG, "csrc", "fednl_local.cpp"), os.path.join(PKG, "csrc", "fednl_serve.cpp")]
 DEPS = SOURCES + [os.path.join(PKG, "csrc", f) for f in os.listdir(os.path.join(PKG, "csrc"))] + \
     [os.path.join(REPO, "include", "fednl_gpu.h")]
 

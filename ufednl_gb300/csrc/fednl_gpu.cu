@@ -8,6 +8,8 @@
 
 #include "fednl_gpu.h"
 #include "fednl_kernels.cuh"
+#include "fednl_solve.h"
+#include "fednl_smem.h"
 
 #include <algorithm>
 #include <cmath>
@@ -56,10 +58,15 @@ struct Arena {
     size_t cap = 0, used = 0;
     std::vector<std::pair<void**, size_t>> plan;
     template <class T> void want(T** p, size_t count) { plan.push_back({(void**)p, count * sizeof(T)}); }
-    int commit()
+    size_t planned() const
     {
         size_t total = 0;
         for (auto& q : plan) total += (q.second + 255) / 256 * 256;
+        return total;
+    }
+    int commit()
+    {
+        size_t total = planned();
         if (total == 0) total = 256;
         cudaError_t e = cudaMalloc((void**)&base, total);
         if (e != cudaSuccess) return fail(FEDNL_ENOMEM, "cudaMalloc(%zu) failed: %s", total, cudaGetErrorString(e));
@@ -121,6 +128,82 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
 }
 
 }  // namespace
+
+// One cooperative launch solving several problems' systems: job j gets a contiguous group of CTAs
+// (its share of the SMs, at least one) and its own barrier words.  More jobs than resident CTAs
+// are solved in successive launches.
+int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream)
+{
+    if (n <= 0) return FEDNL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_batched, kCoopThreads, 0);
+    const int cap = std::max(1, sms * std::max(1, bps));
+    static CholJob* djobs = nullptr;
+    static int djobs_cap = 0;
+    for (int first = 0; first < n; first += cap) {
+        const int m = std::min(cap, n - first);
+        std::vector<CholJob> jobs(m);
+        std::vector<long long> want(m);
+        long long tot = 0;
+        for (int j = 0; j < m; ++j) {
+            want[j] = chol_grid(descs[first + j].d);
+            tot += want[j];
+        }
+        int cta = 0;
+        for (int j = 0; j < m; ++j) {
+            const FednlSolveDesc& S = descs[first + j];
+            int g = tot <= cap ? (int)want[j] : (int)std::max<long long>(1, want[j] * (cap - m) / tot + 1);
+            g = std::min(g, cap - cta - (m - 1 - j));
+            CholJob& J = jobs[j];
+            J = CholJob{};
+            J.P.d = S.d;
+            J.P.U = S.d * (S.d + 1) / 2;
+            J.P.work = S.work;
+            J.P.ybuf = S.ybuf;
+            J.P.rinv = S.rinv;
+            J.P.bar = S.bar;
+            J.P.status = S.status;
+            J.P.stats = S.stats;
+            J.P.hist = S.hist;
+            J.P.ls = S.ls;
+            J.P.round_ctr = S.round_ctr;
+            J.P.hist_cap = S.hist_cap;
+            J.Hin = S.H;
+            J.hin_lda = 0;
+            J.lptr = S.lptr;
+            J.lval = S.lval;
+            J.gin = S.g;
+            J.dxout = S.dx;
+            J.xupd = S.xupd;
+            J.record = S.record;
+            J.cta0 = cta;
+            J.ncta = g;
+            cta += g;
+        }
+        if (djobs_cap < m) {
+            if (djobs) cudaFree(djobs);
+            djobs = nullptr;
+            CK(cudaMalloc(&djobs, sizeof(CholJob) * cap));
+            djobs_cap = cap;
+        }
+        CK(cudaMemcpyAsync(djobs, jobs.data(), sizeof(CholJob) * m, cudaMemcpyHostToDevice, st));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cta);
+        cfg.blockDim = dim3(kCoopThreads);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CK(cudaLaunchKernelEx(&cfg, k_chol_batched, (const CholJob*)djobs, m));
+        CK(cudaStreamSynchronize(st));       // the job table is reused by the next launch
+    }
+    return FEDNL_OK;
+}
 
 // error reporting shared with the tensor-core translation unit (fednl_mixed.cu)
 int fednl_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
@@ -197,7 +280,7 @@ int mark(fednl_handle h, Marks* m, const char* name)
         if (rc_) return rc_;                                                                       \
     } while (0)
 
-int launch_round(fednl_handle h, Marks* M = nullptr)
+int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = false)
 {
     Dev& P = h->dev;
     cudaStream_t st = h->stream;
@@ -296,6 +379,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr)
         k_fmaster<<<1, 32, 0, st>>>(P, P.stats + 2);
         CKL();
     }
+    if (client_phase_only) return FEDNL_OK;
     const fednl_problem_desc& D = h->desc;
     const double* lptr = D.option_a ? nullptr : P.stats + 1;      // Option A: H + lambda I
     MARK("k_chol_coop");
@@ -347,11 +431,15 @@ extern "C" {
 
 const char* fednl_gpu_last_error(void) { return g_last_error.c_str(); }
 
-int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
+}  // extern "C"
+
+// create, or with footprint set only the device bytes a handle of this desc would hold (its state
+// arena plus a dense FP64 bound on the client data)
+static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_t* footprint)
 {
-    if (!desc || !out) return fail(FEDNL_EINVAL, "null argument");
-    *out = nullptr;
-    int rc = ensure_device();
+    if (!desc || (!out && !footprint)) return fail(FEDNL_EINVAL, "null argument");
+    if (out) *out = nullptr;
+    int rc = footprint ? FEDNL_OK : ensure_device();
     if (rc) return rc;
     const fednl_problem_desc& D = *desc;
     if (D.d < 1 || D.n_clients < 1 || !D.n_samples) return fail(FEDNL_EINVAL, "d and n_clients must be >= 1");
@@ -406,10 +494,6 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
     if (h->comp == FEDNL_RANDK)
         while (h->hcap < 4 * k) h->hcap <<= 1;
 
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete h;
-        return fail(FEDNL_ECUDA, "cudaStreamCreate failed");
-    }
     Dev& P = h->dev;
     P.d = h->d;
     P.lda = h->lda;
@@ -486,6 +570,15 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
         A.want(&P.lprev, 1);
         A.want(&P.tg, h->d);
     }
+    if (footprint) {
+        *footprint = (int64_t)A.planned() + (int64_t)h->S * (h->d + 1) * 8 + (int64_t)(h->S + 1) * 4 + 4096;
+        delete h;
+        return FEDNL_OK;
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(FEDNL_ECUDA, "cudaStreamCreate failed");
+    }
     rc = A.commit();
     if (rc) {
         cudaStreamDestroy(h->stream);
@@ -504,10 +597,24 @@ int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
         return fail(FEDNL_ECUDA, "initial copies failed");
     }
     if (select_smem(h->k) > 48 * 1024 && h->k < h->U)
-        cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(h->k));
+        fednl_raise_dyn_smem((const void*)k_select, select_smem(h->k));
     h->chol_grid = chol_grid(h->d);
     *out = h;
     return FEDNL_OK;
+}
+
+extern "C" {
+
+int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
+{
+    if (!out) return fail(FEDNL_EINVAL, "null argument");
+    return create_impl(desc, out, nullptr);
+}
+
+int fednl_gpu_footprint(const fednl_problem_desc* desc, int64_t* bytes)
+{
+    if (!bytes) return fail(FEDNL_EINVAL, "null argument");
+    return create_impl(desc, nullptr, bytes);
 }
 
 int fednl_gpu_destroy(fednl_handle h)
@@ -606,11 +713,11 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         h->hess_smem = h->hess_smem_bits ? need : (size_t)h->maxn * 8;
         if (h->hess_smem > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
         if (h->hess_smem_bits)
-            CK(cudaFuncSetAttribute(k_hess_binary<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
+            CK(fednl_raise_dyn_smem((const void*)k_hess_binary<true>, h->hess_smem));
         else
-            CK(cudaFuncSetAttribute(k_hess_binary<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hess_smem));
+            CK(fednl_raise_dyn_smem((const void*)k_hess_binary<false>, h->hess_smem));
         if ((size_t)h->maxn * 16 > 48 * 1024)
-            CK(cudaFuncSetAttribute(k_grad_binary, cudaFuncAttributeMaxDynamicSharedMemorySize, h->maxn * 16));
+            CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
         h->binary = 1;
     } else {
         double* dA;
@@ -773,6 +880,97 @@ int fednl_gpu_get_dir(fednl_handle h, int32_t client, double* dir, double* ddir)
     CK(cudaStreamSynchronize(h->stream));
     if (dir) CK(cudaMemcpy(dir, h->dev.dir + (size_t)client * h->d, h->d * 8, cudaMemcpyDeviceToHost));
     if (ddir) CK(cudaMemcpy(ddir, h->dev.ddir + (size_t)client * h->d, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_client_phase(fednl_handle h)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    if (h->desc.line_search || h->pp) return fail(FEDNL_EINVAL, "the split round serves plain FedNL");
+    CK(cudaMemsetAsync(h->dev.status, 0, 4, h->stream));
+    return launch_round(h, nullptr, true);
+}
+
+int fednl_gpu_round_result(fednl_handle h, fednl_round_stats* stats)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    CK(cudaStreamSynchronize(h->stream));
+    double st[2] = {0, 0};
+    int status = 0;
+    CK(cudaMemcpy(st, h->dev.stats, 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&status, h->dev.status, 4, cudaMemcpyDeviceToHost));
+    if (stats) {
+        stats->round = h->rounds_done - 1;
+        stats->status = status == FEDNL_ENOTPD ? FEDNL_ENOTPD : FEDNL_OK;
+        stats->grad_norm = st[0];
+        stats->l = st[1];
+    }
+    if (status == FEDNL_ETIMEOUT) return fail(status, "grid barrier of the Cholesky timed out");
+    if (status) return fail(status, "Option-B matrix not positive definite");
+    return FEDNL_OK;
+}
+
+int fednl_gpu_solve_batch(fednl_handle* hs, int32_t n, fednl_mx_handle* mxs, int32_t nmx)
+{
+    if (n < 0 || nmx < 0 || (n && !hs) || (nmx && !mxs)) return fail(FEDNL_EINVAL, "bad argument");
+    static cudaStream_t bst = nullptr;
+    if (!bst) CK(cudaStreamCreateWithFlags(&bst, cudaStreamNonBlocking));
+    std::vector<FednlSolveDesc> descs;
+    std::vector<cudaStream_t> streams;
+    for (int i = 0; i < n; ++i) {
+        fednl_handle h = hs[i];
+        if (!h || !h->shifts_ready) return fail(FEDNL_EINVAL, "handle %d not initialised", i);
+        Dev& P = h->dev;
+        FednlSolveDesc S{};
+        S.H = P.H;
+        S.d = h->d;
+        S.lptr = h->desc.option_a ? nullptr : P.stats + 1;
+        S.lval = P.lambda;
+        S.ls = P.ls;
+        S.g = P.g;
+        S.dx = P.dx;
+        S.xupd = P.x;
+        S.work = P.work;
+        S.ybuf = P.ybuf;
+        S.rinv = P.rinv;
+        S.bar = P.bar;
+        S.status = P.status;
+        S.stats = P.stats;
+        S.hist = P.hist;
+        S.round_ctr = P.round_ctr;
+        S.hist_cap = P.hist_cap;
+        S.record = 1;
+        descs.push_back(S);
+        streams.push_back(h->stream);
+    }
+    for (int i = 0; i < nmx; ++i) {
+        FednlSolveDesc S{};
+        cudaStream_t s2 = nullptr;
+        if (fednl_mx_solve_desc(mxs[i], &S, (void**)&s2)) return fail(FEDNL_EINVAL, "mixed handle %d not initialised", i);
+        descs.push_back(S);
+        streams.push_back(s2);
+    }
+    // the batch stream waits for every client phase, the problems' streams wait for the solve
+    for (cudaStream_t s2 : streams) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventRecord(e, s2));
+        CK(cudaStreamWaitEvent(bst, e, 0));
+        cudaEventDestroy(e);
+    }
+    int rc = fednl_solve_batch_launch(descs.data(), (int)descs.size(), bst);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) hs[i]->rounds_done += 1;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_mem_info(int64_t* free_bytes, int64_t* total_bytes)
+{
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = (int64_t)f;
+    if (total_bytes) *total_bytes = (int64_t)t;
     return FEDNL_OK;
 }
 
@@ -954,7 +1152,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
     k_l2sq_full<<<n_mat, 256, 0, s.st>>>(dfull, (long long)full, dcs, dF);
     CKL();
     if (select_smem(k) > 48 * 1024 && k < U)
-        CK(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem(k)));
+        CK(fednl_raise_dyn_smem((const void*)k_select, select_smem(k)));
     double delta = (double)k * (1.0 / (double)U);
     k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)ustr, (int)U, k, lek ? 1 : 0, delta,
                                                                       dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr);

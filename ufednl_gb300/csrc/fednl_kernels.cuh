@@ -1277,10 +1277,11 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblk)
 
 // Hin is the packed upper triangle, or (hin_lda > 0) a column-major matrix with that leading
 // dimension of which the upper triangle is read.
-__global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin, int hin_lda,
-                                                            const double* lptr, double lval,
-                                                            const double* __restrict__ gin, double* dxout,
-                                                            double* xupd, int record)
+// The solve of one problem by a group of G cooperating CTAs (this CTA is number bid of the group);
+// the grid barrier counts the group's CTAs on P.bar.
+__device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict__ Hin, int hin_lda, const double* lptr,
+                                          double lval, const double* __restrict__ gin, double* dxout, double* xupd,
+                                          int record, unsigned G, unsigned bid)
 {
     __shared__ double Db[kCholNB][kCholNB + 1];
     __shared__ double Rb[kCholNB][kCholNB + 1];
@@ -1296,10 +1297,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     const int D = d + 1;                       // augmented by the right-hand side
     const int UA = D * (D + 1) / 2;
     double* A = P.work;                        // [UA]
-    const unsigned G = gridDim.x;
-    if (P.ls && blockIdx.x == 0 && threadIdx.x == 0) P.ls[4] = 0.0;
+    if (P.ls && bid == 0 && threadIdx.x == 0) P.ls[4] = 0.0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int gtid = blockIdx.x * blockDim.x + tid, gthreads = G * blockDim.x;
+    const int gtid = bid * blockDim.x + tid, gthreads = G * blockDim.x;
     for (int p = gtid; p < UA; p += gthreads) {
         int i, j;
         upper_ij(p, i, j);
@@ -1313,9 +1313,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     if (!grid_barrier(P.bar, G)) goto timeout;
     for (int c0 = 0; c0 < d; c0 += kCholNB) {
         const int nb = min(kCholNB, d - c0), c1 = c0 + nb;
-        // this CTA's panel columns right of the block: j = c1 + blockIdx.x + s G, s < ns (kept in
+        // this CTA's panel columns right of the block: j = c1 + bid + s G, s < ns (kept in
         // shared memory, at most kCholSlab; any further ones are finished after the column loop)
-        const int ntot = D > c1 ? (D - c1 - (int)blockIdx.x + (int)G - 1) / (int)G : 0;
+        const int ntot = D > c1 ? (D - c1 - (int)bid + (int)G - 1) / (int)G : 0;
         const int ns = max(0, min(ntot, kCholSlab));
         for (int t = tid; t < nb * nb; t += blockDim.x) {
             int i = t % nb, j = t / nb;
@@ -1323,7 +1323,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         }
         for (int t = tid; t < nb * ns; t += blockDim.x) {
             const int i = t % nb, sl = t / nb;
-            Sb[i][sl] = A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)];
+            Sb[i][sl] = A[up_pos(c0 + i, c1 + (int)bid + sl * (int)G)];
         }
         // block entries (i, j), i <= j, listed by descending i: those with i > k are a prefix
         if (nb != ent_nb) {
@@ -1404,13 +1404,13 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
             __syncthreads();
         }
         if (s_fail) {   // identical decision in every CTA: all leave together
-            if (blockIdx.x == 0 && tid == 0) {
+            if (bid == 0 && tid == 0) {
                 *P.status = -4;
                 if (record) *P.round_ctr += 1;
             }
             return;
         }
-        if (blockIdx.x == 0) {
+        if (bid == 0) {
             for (int t = tid; t < nb * nb; t += blockDim.x) {
                 int i = t % nb, j = t / nb;
                 if (i <= j) A[up_pos(c0 + i, c0 + j)] = Rb[i][j];
@@ -1419,13 +1419,13 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         }
         for (int t = tid; t < nb * ns; t += blockDim.x) {
             const int i = t % nb, sl = t / nb;
-            A[up_pos(c0 + i, c1 + (int)blockIdx.x + sl * (int)G)] = SR[i][sl];
+            A[up_pos(c0 + i, c1 + (int)bid + sl * (int)G)] = SR[i][sl];
         }
         // panel columns beyond the slab (very large d only): one column per warp, same steps
         {
             const int w = tid >> 5;
             for (int sl = kCholSlab + w; sl < ntot; sl += kCoopThreads / 32) {
-                const int j = c1 + (int)blockIdx.x + sl * (int)G;
+                const int j = c1 + (int)bid + sl * (int)G;
                 double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
                 for (int k = 0; k < nb; ++k) {
                     if (lane == k) a = __dmul_rn(a, s_inv[k]);
@@ -1463,7 +1463,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
         if (!grid_barrier(P.bar, G)) goto timeout;
     }
     if (!grid_barrier(P.bar, G)) goto timeout;
-    if (blockIdx.x != 0) return;
+    if (bid != 0) return;
     {
         // R dx = y (y in column d), blocked by 32 rows (CTA 0)
         double* y = P.ybuf;
@@ -1556,10 +1556,43 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
     }
     return;
 timeout:
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bid == 0 && threadIdx.x == 0) {
         *P.status = -5;
         if (record) *P.round_ctr += 1;
     }
+}
+
+__global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin, int hin_lda,
+                                                            const double* lptr, double lval,
+                                                            const double* __restrict__ gin, double* dxout,
+                                                            double* xupd, int record)
+{
+    chol_body(P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, gridDim.x, blockIdx.x);
+}
+
+// Several independent Option-B solves in one cooperative launch (the serving loop's tick): job j
+// owns CTAs [cta0, cta0 + ncta) and its own barrier words, so problems of different d proceed
+// side by side.
+struct CholJob {
+    Dev P;
+    const double* Hin;
+    int hin_lda;
+    const double* lptr;
+    double lval;
+    const double* gin;
+    double* dxout;
+    double* xupd;
+    int record, cta0, ncta;
+};
+
+__global__ void __launch_bounds__(kCoopThreads) k_chol_batched(const CholJob* __restrict__ jobs, int njobs)
+{
+    int j = 0;
+    while (j + 1 < njobs && (int)blockIdx.x >= jobs[j + 1].cta0) ++j;
+    const CholJob& J = jobs[j];
+    if ((int)blockIdx.x >= J.cta0 + J.ncta) return;
+    chol_body(J.P, J.Hin, J.hin_lda, J.lptr, J.lval, J.gin, J.dxout, J.xupd, J.record, (unsigned)J.ncta,
+              blockIdx.x - (unsigned)J.cta0);
 }
 
 // ---- operator-level helpers -----------------------------------------------------------------

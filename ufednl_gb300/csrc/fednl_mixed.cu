@@ -8,6 +8,8 @@
 
 #include "fednl_gpu.h"
 #include "fednl_tc.cuh"
+#include "fednl_solve.h"
+#include "fednl_smem.h"
 
 #include <cudaTypedefs.h>
 
@@ -70,8 +72,8 @@ int make_feature_map(CUtensorMap* map, const float* X, int L, int d, int nc)
 }
 
 // sample-major [sum n][d] (clients in order) -> feature-major [nc][d][L], zero padding
-__global__ void k_to_feature_major(const float* __restrict__ A, const int* __restrict__ soff, int d, int L, int nc,
-                                   float* __restrict__ X)
+__global__ void k_to_feature_major(const float* __restrict__ A, const int* __restrict__ soff, int d, int dp, int L,
+                                   int nc, float* __restrict__ X)
 {
     __shared__ float tile[32][33];
     const int c = blockIdx.z;
@@ -84,7 +86,7 @@ __global__ void k_to_feature_major(const float* __restrict__ A, const int* __res
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int i = i0 + r, s = s0 + threadIdx.x;
-        if (i < d && s < L) X[((size_t)c * d + i) * L + s] = tile[threadIdx.x][r];
+        if (i < d && s < L) X[((size_t)c * dp + i) * L + s] = tile[threadIdx.x][r];
     }
 }
 
@@ -145,7 +147,7 @@ extern "C" int fednl_gpu_weighted_gram_tf32(const float* features, const float* 
             rc = fail_m(FEDNL_ECUDA, "copies failed");
             break;
         }
-        k_to_feature_major<<<dim3(L / 32, (d + 31) / 32, n_clients), dim3(32, 8)>>>(dA, dsoff, d, L, n_clients, dX);
+        k_to_feature_major<<<dim3(L / 32, (d + 31) / 32, n_clients), dim3(32, 8)>>>(dA, dsoff, d, d, L, n_clients, dX);
         k_pad_weights<<<dim3((L + 255) / 256, n_clients), 256>>>(dw, dsoff, L, n_clients, dW);
         CUtensorMap map;
         rc = make_feature_map(&map, dX, L, d, n_clients);
@@ -197,7 +199,7 @@ int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const
 struct fednl_mx_handle_s {
     fednl_problem_desc desc{};
     std::vector<int32_t> ns, soff;
-    int d = 0, nc = 0, L = 0, U = 0, SW = 0, k = 0, S = 0, tiles = 0;
+    int d = 0, dp = 0, nc = 0, L = 0, U = 0, SW = 0, k = 0, S = 0, tiles = 0, comp = 0;
     long long Up = 0;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
@@ -211,10 +213,18 @@ struct fednl_mx_handle_s {
     int hist_cap = 1 << 16;
     bool ready = false;
     int rounds_done = 0;
+    size_t select_smem = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
+    size_t dry = 0;            // footprint only: bytes the allocations would take
+    bool dry_run = false;
     template <class T> int alloc(T** p, size_t n)
     {
+        if (dry_run) {
+            dry += (std::max<size_t>(n, 1) * sizeof(T) + 511) / 512 * 512;
+            *p = nullptr;
+            return FEDNL_OK;
+        }
         void* q = nullptr;
         if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
             return fail_m(FEDNL_ENOMEM, "device allocation of %zu bytes failed", n * sizeof(T));
@@ -229,9 +239,11 @@ namespace {
 // the round's launches; with ev, an event is recorded before each kernel and after the last
 const char* const kMxKernelNames[] = {"k_mx_split_x", "k_mx_margin", "k_mx_grad", "k_mx_draw",
                                       "k_gram_tf32", "k_mx_lk", "k_mx_apply", "k_mx_aggregate", "k_chol_coop"};
+const char* const kMxKernelNamesTop[] = {"k_mx_split_x", "k_mx_margin", "k_mx_grad", "k_gram_tf32",
+                                         "k_mx_lk", "k_mx_select", "k_mx_apply", "k_mx_aggregate", "k_chol_coop"};
 constexpr int kMxKernels = 9;
 
-int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr)
+int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_phase_only = false)
 {
     using namespace fednl_tc;
     MxDev& P = h->P;
@@ -247,19 +259,28 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr)
     mark();
     k_mx_grad<<<(h->nc * h->d + 7) / 8, 256, 0, st>>>(P);
     mark();
-    k_mx_draw<<<h->nc, 256, 0, st>>>(P, h->k, fednl::philox_half_bits(h->U), h->desc.seed_base);
-    mark();
-    GramJob J{h->d, h->nc, h->L, h->d / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
-    EpiDiff epi{P.shift, P.dsel, P.sel, P.fpart, h->Up, h->SW, h->tiles, (float)P.lambda};
+    const bool randk = h->comp == FEDNL_RANDK_PHILOX;
+    if (randk) {
+        k_mx_draw<<<h->nc, 256, 0, st>>>(P, h->k, fednl::philox_half_bits(h->U), h->desc.seed_base);
+        mark();
+    }
+    GramJob J{h->dp, h->nc, h->L, h->dp / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
+    EpiDiff epi{P.shift, P.dsel, randk ? P.sel : nullptr, P.fpart, h->Up, h->SW, h->tiles, (float)P.lambda, h->d};
     k_gram_tf32<EpiDiff><<<h->nc * h->tiles, kThreads, smem_bytes(), st>>>(h->map, J, epi);
     mark();
     k_mx_lk<<<h->nc, 256, 0, st>>>(P);
     mark();
+    if (!randk) {
+        const int toplek = h->comp == FEDNL_TOPLEK;
+        k_mx_select<<<h->nc, kSelThreads, toplek ? h->select_smem : 0, st>>>(P, h->k, toplek, h->desc.toplek_seed);
+        mark();
+    }
     k_mx_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     mark();
     k_mx_aggregate<<<(h->d + 255) / 256, 256, 0, st>>>(P);
     mark();
     CKM(cudaGetLastError());
+    if (client_phase_only) return FEDNL_OK;
     int rc = fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, h->dx, P.x, h->work, h->ybuf, h->rinv, h->bar,
                                         h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st);
     mark();
@@ -270,30 +291,40 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr)
 
 extern "C" {
 
-int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
+}  // extern "C"
+
+static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, int64_t* footprint)
 {
-    if (!desc || !out) return fail_m(FEDNL_EINVAL, "null argument");
-    *out = nullptr;
+    if (!desc || (!out && !footprint)) return fail_m(FEDNL_EINVAL, "null argument");
+    if (out) *out = nullptr;
     const fednl_problem_desc& D = *desc;
     int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail_m(FEDNL_ENODEV, "no CUDA device available");
-    if (D.d < fednl_tc::kBM || D.d % fednl_tc::kBM)
-        return fail_m(FEDNL_EINVAL, "the mixed-precision form needs d a multiple of %d", fednl_tc::kBM);
+    if (!footprint && (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0))
+        return fail_m(FEDNL_ENODEV, "no CUDA device available");
+    if (D.d < 1) return fail_m(FEDNL_EINVAL, "d must be >= 1");
     if (D.n_clients < 1 || !D.n_samples) return fail_m(FEDNL_EINVAL, "no clients");
-    if (D.compressor != FEDNL_RANDK_PHILOX) return fail_m(FEDNL_EINVAL, "the mixed-precision form runs RandK-Philox");
+    if (D.compressor != FEDNL_RANDK_PHILOX && D.compressor != FEDNL_TOPK && D.compressor != FEDNL_TOPLEK)
+        return fail_m(FEDNL_EINVAL, "the mixed-precision form runs TopK, TopLEK or RandK-Philox");
+    for (int i = 0; i < 2; ++i)
+        if (D.reserved[i]) return fail_m(FEDNL_EINVAL, "reserved fields must be zero");
     if (D.option_a || D.line_search || D.clients_per_round)
         return fail_m(FEDNL_EINVAL, "the mixed-precision form runs plain FedNL with Option B");
     const long long U = (long long)D.d * (D.d + 1) / 2;
-    if (D.k < 1 || D.k > U) return fail_m(FEDNL_EINVAL, "k outside [1, U]");
+    if (D.k < 1 || (D.compressor == FEDNL_RANDK_PHILOX && D.k > U)) return fail_m(FEDNL_EINVAL, "k outside [1, U]");
+    if (D.compressor == FEDNL_TOPLEK && D.k < U && D.k > fednl_tc::kMxMaxLek)
+        return fail_m(FEDNL_EINVAL, "TopLEK k %d above the shared-memory limit %d", D.k, fednl_tc::kMxMaxLek);
     fednl_mx_handle h = new fednl_mx_handle_s();
+    h->dry_run = footprint != nullptr;
     h->desc = D;
     h->d = D.d;
+    h->dp = (D.d + fednl_tc::kBM - 1) / fednl_tc::kBM * fednl_tc::kBM;
+    h->comp = D.compressor;
     h->nc = D.n_clients;
     h->U = (int)U;
     h->Up = (U + 31) / 32 * 32;
     h->SW = (int)((U + 31) / 32);
     h->k = D.k;
-    h->tiles = (D.d / fednl_tc::kBM) * (D.d / fednl_tc::kBM + 1) / 2;
+    h->tiles = (h->dp / fednl_tc::kBM) * (h->dp / fednl_tc::kBM + 1) / 2;
     h->ns.assign(D.n_samples, D.n_samples + D.n_clients);
     h->soff.assign(h->nc + 1, 0);
     int maxn = 0;
@@ -309,6 +340,7 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
     h->L = (maxn + 31) / 32 * 32;
     fednl_tc::MxDev& P = h->P;
     P.d = h->d;
+    P.dp = h->dp;
     P.nc = h->nc;
     P.L = h->L;
     P.U = h->U;
@@ -319,13 +351,13 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
     P.alpha = D.alpha;
     P.inv_n = 1.0 / (double)h->nc;
     P.prescale = P.inv_n * D.alpha;
-    P.mult = (double)U / (double)h->k;
+    P.mult = D.compressor == FEDNL_RANDK_PHILOX ? (double)U / (double)h->k : 1.0;     // RandK.h:90 / TopK
     const size_t ncL = (size_t)h->nc * h->L, ncUp = (size_t)h->nc * h->Up;
     int rc = 0;
     float* X;
     double* lab;
     rc |= h->alloc(&h->ns_dev, h->nc);
-    rc |= h->alloc(&X, (size_t)h->nc * h->d * h->L);
+    rc |= h->alloc(&X, (size_t)h->nc * h->dp * h->L);
     rc |= h->alloc(&lab, ncL);
     rc |= h->alloc(&P.x, h->d);
     rc |= h->alloc(&P.xh, h->d);
@@ -342,6 +374,7 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
     rc |= h->alloc(&P.draws, h->nc);
     rc |= h->alloc(&P.fpart, (size_t)h->nc * h->tiles * 128);
     rc |= h->alloc(&P.lk, h->nc);
+    rc |= h->alloc(&P.cnt, h->nc);
     rc |= h->alloc(&P.stats, 4);
     rc |= h->alloc(&h->err, 1);
     rc |= h->alloc(&h->dx, h->d);
@@ -352,6 +385,11 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
     rc |= h->alloc(&h->bar, 4);
     rc |= h->alloc(&h->status, 1);
     rc |= h->alloc(&h->round_ctr, 1);
+    if (footprint) {     // plus the upload's staging copy of the sample-major features
+        *footprint = (int64_t)h->dry + (int64_t)h->S * h->d * 4 + (int64_t)(h->nc + 1) * 4 + 4096;
+        delete h;
+        return FEDNL_OK;
+    }
     if (rc || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         fednl_mx_destroy(h);
         return rc ? rc : fail_m(FEDNL_ECUDA, "stream creation failed");
@@ -360,7 +398,7 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
     P.lab = lab;
     P.ns = h->ns_dev;
     if (cudaMemcpy(h->ns_dev, h->ns.data(), h->nc * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(X, 0, (size_t)h->nc * h->d * h->L * 4) != cudaSuccess || cudaMemset(lab, 0, ncL * 8) != cudaSuccess ||
+        cudaMemset(X, 0, (size_t)h->nc * h->dp * h->L * 4) != cudaSuccess || cudaMemset(lab, 0, ncL * 8) != cudaSuccess ||
         cudaMemset(P.Dw, 0, ncL * 4) != cudaSuccess || cudaMemset(P.qh, 0, ncL * 4) != cudaSuccess ||
         cudaMemset(P.ql, 0, ncL * 4) != cudaSuccess || cudaMemset(P.dsel, 0, ncUp * 4) != cudaSuccess ||
         cudaMemset(P.draws, 0, h->nc * 4) != cudaSuccess || cudaMemset(h->err, 0, 4) != cudaSuccess ||
@@ -369,7 +407,7 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
         fednl_mx_destroy(h);
         return fail_m(FEDNL_ECUDA, "initial copies failed");
     }
-    rc = make_feature_map(&h->map, X, h->L, h->d, h->nc);
+    rc = make_feature_map(&h->map, X, h->L, h->dp, h->nc);
     if (rc || cudaFuncSetAttribute(fednl_tc::k_gram_tf32<fednl_tc::EpiDiff>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)fednl_tc::smem_bytes()) != cudaSuccess ||
         cudaFuncSetAttribute(fednl_tc::k_gram_tf32<fednl_tc::EpiInitShift>,
@@ -377,8 +415,31 @@ int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
         fednl_mx_destroy(h);
         return rc ? rc : fail_m(FEDNL_ECUDA, "shared-memory attribute refused");
     }
+    if (h->comp == FEDNL_TOPLEK && h->k < h->U) {
+        int kp = 1;
+        while (kp < h->k) kp <<= 1;
+        h->select_smem = (size_t)kp * 8;
+        if (fednl_raise_dyn_smem((const void*)fednl_tc::k_mx_select, h->select_smem) != cudaSuccess) {
+            fednl_mx_destroy(h);
+            return fail_m(FEDNL_ECUDA, "shared-memory attribute refused");
+        }
+    }
     *out = h;
     return FEDNL_OK;
+}
+
+extern "C" {
+
+int fednl_mx_create(const fednl_problem_desc* desc, fednl_mx_handle* out)
+{
+    if (!out) return fail_m(FEDNL_EINVAL, "null argument");
+    return mx_create_impl(desc, out, nullptr);
+}
+
+int fednl_mx_footprint(const fednl_problem_desc* desc, int64_t* bytes)
+{
+    if (!bytes) return fail_m(FEDNL_EINVAL, "null argument");
+    return mx_create_impl(desc, nullptr, bytes);
 }
 
 int fednl_mx_destroy(fednl_mx_handle h)
@@ -413,7 +474,7 @@ int fednl_mx_upload_client_data(fednl_mx_handle h, const float* features, const 
         cudaMemcpy((void*)h->P.lab, labp.data(), labp.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
         rc = fail_m(FEDNL_ECUDA, "upload failed");
     } else {
-        k_to_feature_major<<<dim3(h->L / 32, (h->d + 31) / 32, h->nc), dim3(32, 8)>>>(dA, dsoff, h->d, h->L, h->nc,
+        k_to_feature_major<<<dim3(h->L / 32, (h->d + 31) / 32, h->nc), dim3(32, 8)>>>(dA, dsoff, h->d, h->dp, h->L, h->nc,
                                                                                       (float*)h->P.X);
         if (cudaDeviceSynchronize() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "layout kernel failed");
     }
@@ -432,8 +493,8 @@ int fednl_mx_init_shifts(fednl_mx_handle h, const double* x0)
     else CKM(cudaMemsetAsync(P.x, 0, h->d * 8, st));
     k_mx_split_x<<<(h->d + 255) / 256, 256, 0, st>>>(P);
     k_mx_margin<<<dim3((h->L + 255) / 256, h->nc), 256, 0, st>>>(P);
-    GramJob J{h->d, h->nc, h->L, h->d / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
-    EpiInitShift epi{P.shift, h->Up, (float)P.lambda};
+    GramJob J{h->dp, h->nc, h->L, h->dp / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
+    EpiInitShift epi{P.shift, h->Up, (float)P.lambda, h->d};
     k_gram_tf32<EpiInitShift><<<h->nc * h->tiles, kThreads, smem_bytes(), st>>>(h->map, J, epi);
     k_mx_hinit<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     CKM(cudaGetLastError());
@@ -525,11 +586,66 @@ int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_m
     for (auto& e : ev) cudaEventDestroy(e);
     if (names && names_len > 0) {
         std::string all;
-        for (int t = 0; t < kMxKernels; ++t) all += std::string(t ? ";" : "") + kMxKernelNames[t];
+        const char* const* nm = h->comp == FEDNL_RANDK_PHILOX ? kMxKernelNames : kMxKernelNamesTop;
+        for (int t = 0; t < kMxKernels; ++t) all += std::string(t ? ";" : "") + nm[t];
         snprintf(names, (size_t)names_len, "%s", all.c_str());
     }
     h->rounds_done += rounds;
     return rc;
+}
+
+int fednl_mx_client_phase(fednl_mx_handle h)
+{
+    if (!h || !h->ready) return fail_m(FEDNL_EINVAL, "call fednl_mx_init_shifts first");
+    CKM(cudaMemsetAsync(h->status, 0, 4, h->stream));
+    return mx_launch_round(h, nullptr, true);
+}
+
+int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats)
+{
+    if (!h || !h->ready) return fail_m(FEDNL_EINVAL, "call fednl_mx_init_shifts first");
+    CKM(cudaStreamSynchronize(h->stream));
+    double st[2] = {0, 0};
+    int err = 0, status = 0;
+    CKM(cudaMemcpy(st, h->P.stats, 16, cudaMemcpyDeviceToHost));
+    CKM(cudaMemcpy(&err, h->err, 4, cudaMemcpyDeviceToHost));
+    CKM(cudaMemcpy(&status, h->status, 4, cudaMemcpyDeviceToHost));
+    if (stats) {
+        stats->round = h->rounds_done - 1;
+        stats->status = status == FEDNL_ENOTPD ? FEDNL_ENOTPD : FEDNL_OK;
+        stats->grad_norm = st[0];
+        stats->l = st[1];
+    }
+    if (err) return fail_m(FEDNL_ETIMEOUT, "a bounded wait of the Gram kernel ran out");
+    if (status == FEDNL_ETIMEOUT) return fail_m(status, "grid barrier of the Cholesky timed out");
+    if (status) return fail_m(status, "Option-B matrix not positive definite");
+    return FEDNL_OK;
+}
+
+int fednl_mx_solve_desc(fednl_mx_handle h, FednlSolveDesc* S, void** stream)
+{
+    if (!h || !h->ready || !S) return FEDNL_EINVAL;
+    const fednl_tc::MxDev& P = h->P;
+    *S = FednlSolveDesc{};
+    S->H = P.H;
+    S->d = h->d;
+    S->lptr = P.stats + 1;
+    S->g = P.g;
+    S->dx = h->dx;
+    S->xupd = P.x;
+    S->work = h->work;
+    S->ybuf = h->ybuf;
+    S->rinv = h->rinv;
+    S->bar = h->bar;
+    S->status = h->status;
+    S->stats = P.stats;
+    S->hist = h->hist;
+    S->round_ctr = h->round_ctr;
+    S->hist_cap = h->hist_cap;
+    S->record = 1;
+    if (stream) *stream = (void*)h->stream;
+    h->rounds_done += 1;
+    return FEDNL_OK;
 }
 
 int fednl_mx_get_x(fednl_mx_handle h, double* x)
@@ -537,6 +653,38 @@ int fednl_mx_get_x(fednl_mx_handle h, double* x)
     if (!h || !x) return fail_m(FEDNL_EINVAL, "null argument");
     CKM(cudaStreamSynchronize(h->stream));
     CKM(cudaMemcpy(x, h->P.x, h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_mx_get_diff(fednl_mx_handle h, int32_t client, float* diff)
+{
+    if (!h || !diff || client < 0 || client >= h->nc) return fail_m(FEDNL_EINVAL, "bad argument");
+    CKM(cudaStreamSynchronize(h->stream));
+    CKM(cudaMemcpy(diff, h->P.dsel + (size_t)client * h->Up, (size_t)h->U * 4, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_mx_get_selection(fednl_mx_handle h, int32_t client, uint32_t* pos, int32_t* count)
+{
+    if (!h || !count || client < 0 || client >= h->nc) return fail_m(FEDNL_EINVAL, "bad argument");
+    CKM(cudaStreamSynchronize(h->stream));
+    std::vector<unsigned> w(h->SW);
+    CKM(cudaMemcpy(w.data(), h->P.sel + (size_t)client * h->SW, (size_t)h->SW * 4, cudaMemcpyDeviceToHost));
+    int n = 0;
+    for (int q = 0; q < h->U; ++q)
+        if ((w[q >> 5] >> (q & 31)) & 1u) {
+            if (pos) pos[n] = (uint32_t)q;
+            ++n;
+        }
+    *count = n;
+    return FEDNL_OK;
+}
+
+int fednl_mx_get_shift(fednl_mx_handle h, int32_t client, float* shift)
+{
+    if (!h || !shift || client < 0 || client >= h->nc) return fail_m(FEDNL_EINVAL, "bad argument");
+    CKM(cudaStreamSynchronize(h->stream));
+    CKM(cudaMemcpy(shift, h->P.shift + (size_t)client * h->Up, (size_t)h->U * 4, cudaMemcpyDeviceToHost));
     return FEDNL_OK;
 }
 

@@ -8,7 +8,7 @@
 //   * one CTA per 128 x 128 tile of the upper triangle of H_i (tiles of one client are scheduled
 //     together so that the client's block stays in L2);
 //   * warp 0 streams 128 x 32 FP32 slabs of the two tile rows with TMA (3-D tensor map over
-//     [client][feature][sample], 128-byte swizzle) into a 4-stage ring guarded by mbarriers;
+//     [client][feature][sample], 128-byte swizzle) into a 6-stage ring guarded by mbarriers;
 //   * warps 2-5 scale the B slab by the per-sample weights D_s in shared memory (the swizzle is
 //     undone to find each element's sample) and release it to the tensor cores;
 //   * warp 1 (one lane) issues tcgen05.mma.kind::tf32 (M = N = 128, K = 8, four per slab) into a
@@ -29,7 +29,7 @@
 namespace fednl_tc {
 
 constexpr int kBM = 128, kBN = 128, kBK = 32;     // tile rows, tile columns, FP32 samples per slab
-constexpr int kStages = 4;
+constexpr int kStages = 6;
 constexpr int kSlabBytes = kBM * kBK * 4;         // 16 KB (128 rows x 128 bytes)
 constexpr int kThreads = 192;
 constexpr long long kWaitCycles = 2000000000ll;   // ~1 s
@@ -136,7 +136,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 }
 
 struct GramJob {
-    int d;                 // features (multiple of 128)
+    int d;                 // padded features (multiple of 128)
     int nc;                // clients
     int L;                 // padded samples per client (multiple of 32)
     int nbk;               // tile rows per client (d / 128)
@@ -243,24 +243,30 @@ __global__ void __launch_bounds__(kThreads) k_gram_tf32(const __grid_constant__ 
         }
     } else {
         const int et = tid - 64;              // 0..127
-        for (int kb = 0; kb < nk; ++kb) {     // weight the B slab: column k of the slab by D_(k0 + k)
+        // Weight the B slab: sample column k of the slab by D_(k0 + k).  Thread et owns the 16-byte
+        // chunks q = et + 128 i (rows r0 + 16 i, physical chunk et & 7); the 128-byte swizzle puts
+        // logical sample group lc = (et & 7) ^ (r0 & 7) there for every i, so one float4 of weights
+        // per slab serves all eight chunks; the next slab's is loaded before this slab is waited for.
+        const int r0 = et >> 3, lc = (et & 7) ^ (r0 & 7);
+        const float* wbase = J.w + (size_t)c * J.L + lc * 4;
+        float4 wv = nk > 0 ? *reinterpret_cast<const float4*>(wbase) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int kb = 0; kb < nk; ++kb) {
             const int s = kb % kStages;
+            const float4 wn = kb + 1 < nk ? *reinterpret_cast<const float4*>(wbase + (kb + 1) * kBK) : wv;
             if (!mbar_wait(&full[s], (uint32_t)(kb / kStages) & 1u, abort_flag)) break;
             float4* slab = (float4*)(ringB + s * kSlabBytes);
-            const float* wrow = J.w + (size_t)c * J.L + kb * kBK;
 #pragma unroll
-            for (int q = et; q < kBN * 8; q += 128) {      // 16-byte chunks of the slab
-                const int r = q >> 3, pc = q & 7, lc = pc ^ (r & 7);
-                const float4 wv = *reinterpret_cast<const float4*>(wrow + lc * 4);
-                float4 x = slab[q];
+            for (int i = 0; i < kBN / 16; ++i) {
+                float4 x = slab[et + 128 * i];
                 x.x *= wv.x;
                 x.y *= wv.y;
                 x.z *= wv.z;
                 x.w *= wv.w;
-                slab[q] = x;
+                slab[et + 128 * i] = x;
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&scaled[s]);
+            wv = wn;
         }
         // epilogue: the accumulator rows of this warp's TMEM lane quarter
         const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0u, abort_flag));   // warp-uniform for tcgen05.ld
@@ -320,12 +326,13 @@ struct EpiInitShift {
     float* shift;          // [nc][Up]
     long long Up;
     float lambda;
+    int d;                 // true dimension (rows and columns from d on are padding)
     __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v, Acc&) const
     {
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             const int n = n0 + i;
-            if (m <= n) shift[(size_t)c * Up + upos(m, n)] = v[i] + (m == n ? lambda : 0.0f);
+            if (m <= n && n < d) shift[(size_t)c * Up + upos(m, n)] = v[i] + (m == n ? lambda : 0.0f);
         }
     }
     __device__ __forceinline__ void finish(int, int, int, const Acc&) const {}
@@ -333,29 +340,44 @@ struct EpiInitShift {
 
 // Round epilogue: diff = H_c - shift_c on the upper triangle; per-thread weighted sum of squares
 // (diagonal once, off-diagonal twice: the full symmetric matrix) into fpart[c][tile][thread]; the
-// differences at the client's selected positions into dsel[c][p]
+// differences at the client's selected positions into dsel[c][p] (every difference when sel is
+// null: TopK / TopLEK select afterwards)
 struct EpiDiff {
     struct Acc {
         float sq = 0.0f;
     };
     const float* shift;    // [nc][Up]
     float* dsel;           // [nc][Up]
-    const unsigned* sel;   // [nc][SW]
+    const unsigned* sel;   // [nc][SW] or nullptr
     float* fpart;          // [nc][tiles][128]
     long long Up;
     int SW, tiles;
     float lambda;
+    int d;
     __device__ __forceinline__ void operator()(int c, int m, int n0, const float* v, Acc& a) const
     {
-        const unsigned* sc = sel + (size_t)c * SW;
+        // all 16 shift values and selection words are loaded before the first store, so that the
+        // loads overlap instead of waiting one by one behind the stores to dsel
+        const unsigned* sc = sel ? sel + (size_t)c * SW : nullptr;
+        const float* shc = shift + (size_t)c * Up;
+        float sh[16];
+        unsigned sw[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             const int n = n0 + i;
-            if (m <= n) {
+            const bool ok = m <= n && n < d;
+            const long long p = ok ? upos(m, n) : 0;
+            sh[i] = ok ? __ldg(shc + p) : 0.0f;
+            sw[i] = (ok && sc) ? __ldg(sc + (p >> 5)) : 0xffffffffu;
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int n = n0 + i;
+            if (m <= n && n < d) {
                 const long long p = upos(m, n);
-                const float df = (v[i] + (m == n ? lambda : 0.0f)) - shift[(size_t)c * Up + p];
+                const float df = (v[i] + (m == n ? lambda : 0.0f)) - sh[i];
                 a.sq = fmaf(m == n ? df : 2.0f * df, df, a.sq);
-                if ((sc[p >> 5] >> (p & 31)) & 1u) dsel[(size_t)c * Up + p] = df;
+                if ((sw[i] >> (p & 31)) & 1u) dsel[(size_t)c * Up + p] = df;
             }
         }
     }
@@ -394,11 +416,11 @@ __device__ __forceinline__ void split_ff(double v, float& h, float& l)
 }
 
 struct MxDev {
-    int d, nc, L, U, SW, tiles;
+    int d, dp, nc, L, U, SW, tiles;     // dp: d padded to the Gram tile (feature rows of X)
     long long Up;
     double lambda, alpha, prescale, inv_n, mult;
     const int* ns;          // [nc]
-    const float* X;         // [nc][d][L]
+    const float* X;         // [nc][dp][L]
     const double* lab;      // [nc][L] labels (+-1, 0 beyond n)
     double* x;              // [d]
     float* xh;              // [d] split iterate
@@ -412,7 +434,8 @@ struct MxDev {
     float* shift;           // [nc][Up]
     float* dsel;            // [nc][Up]
     unsigned* sel;          // [nc][SW]
-    unsigned* draws;        // [nc]
+    unsigned* draws;        // [nc] per-client draw counters (RandK-Philox, TopLEK rounding)
+    int* cnt;               // [nc] selected entries of the round (TopK / TopLEK)
     float* fpart;           // [nc][tiles][128]
     double* lk;             // [nc]
     double* stats;          // [4]: ||g||, l
@@ -438,7 +461,7 @@ __global__ void __launch_bounds__(256) k_mx_margin(MxDev P)
     __syncthreads();
     const int n = P.ns[c];
     if (s >= n) return;
-    const float* col = P.X + (size_t)c * P.d * P.L + s;
+    const float* col = P.X + (size_t)c * P.dp * P.L + s;
     float hi = 0.0f, lo = 0.0f;
     for (int i = 0; i < P.d; ++i) {
         const float xv = col[(size_t)i * P.L];
@@ -462,7 +485,7 @@ __global__ void __launch_bounds__(256) k_mx_grad(MxDev P)
     if (wid >= P.nc * P.d) return;
     const int c = wid / P.d, i = wid - c * P.d;
     const int n = P.ns[c];
-    const float* row = P.X + ((size_t)c * P.d + i) * P.L;
+    const float* row = P.X + ((size_t)c * P.dp + i) * P.L;
     const float* qh = P.qh + (size_t)c * P.L;
     const float* ql = P.ql + (size_t)c * P.L;
     float hi = 0.0f, lo = 0.0f;
@@ -487,6 +510,257 @@ __global__ void k_mx_draw(MxDev P, int k, int h, unsigned seed)
     }
     __syncthreads();
     if (threadIdx.x == 0) P.draws[c] = draw + 1;
+}
+
+// ---- TopK / TopLEK of the mixed-precision form -----------------------------------------------
+// On the FP32 differences every entry is a candidate; the key of an entry is the magnitude bits of
+// its FP32 value (ordered like |v| for finite values).  TopK keeps the k largest keys, ties at the
+// threshold going to the lower packed positions.  TopLEK then applies the reference's rule
+// (SpecialMathRoutinesForMatrix.h:377-511) to that set: with F = ||H_c - shift_c||_F^2 (diagonal
+// once, off-diagonal twice), delta = k / U and eps = F / 10, the kept entries are removed smallest
+// first (ties: higher position first) while the removed mass plus the mass outside the set stays
+// below the window; the boundary entry stays with probability 1 - p, p the window fraction, drawn
+// from Philox4x32-10 keyed by (seed, client) at the client's draw counter.
+constexpr int kSelThreads = 1024;
+constexpr int kMxMaxLek = 16384;          // TopLEK: the kept set is sorted in shared memory
+
+__device__ __forceinline__ unsigned mag_key(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+
+// inclusive scan of one unsigned per thread over the block (1024 threads); total in *tot
+__device__ __forceinline__ unsigned block_scan_u32(unsigned v, unsigned* s_w, unsigned* tot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) s_w[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = s_w[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        s_w[lane] = w;
+    }
+    __syncthreads();
+    const unsigned r = v + (warp ? s_w[warp - 1] : 0u);
+    if (tot) *tot = s_w[31];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ double block_scan_f64(double v, double* s_w, double* tot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) s_w[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double w = s_w[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        s_w[lane] = w;
+    }
+    __syncthreads();
+    const double r = v + (warp ? s_w[warp - 1] : 0.0);
+    if (tot) *tot = s_w[31];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ bool packed_is_diag(long long p)
+{
+    long long j = (long long)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    while (j > 0 && j * (j + 1) / 2 > p) --j;
+    while ((j + 1) * (j + 2) / 2 <= p) ++j;
+    return p - j * (j + 1) / 2 == j;
+}
+
+// one CTA (1024 threads) per client: selection bitmap sel[c] from the differences dsel[c]
+__global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int toplek, unsigned seed)
+{
+    extern __shared__ unsigned long long s_set[];       // TopLEK: [Kp]
+    __shared__ unsigned hist[2048];
+    __shared__ unsigned s_wu[32];
+    __shared__ double s_wd[32];
+    __shared__ unsigned s_bin, s_need, s_cnt[32], s_nk;
+    __shared__ int s_hit;
+    const int c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float* v = P.dsel + (size_t)c * P.Up;
+    unsigned* sc = P.sel + (size_t)c * P.SW;
+    const int U = P.U;
+    const int K = k < U ? k : U;
+    unsigned T = 0, need = 0;
+    if (K < U) {
+        // radix select of the K-th largest key: 11 + 11 + 9 bits from the top
+        unsigned prefix = 0, mask = 0;
+        need = (unsigned)K;
+        const int shs[3] = {20, 9, 0}, nbits[3] = {11, 11, 9};
+        for (int pass = 0; pass < 3; ++pass) {
+            const int sh = shs[pass], nb = 1 << nbits[pass];
+            for (int b = tid; b < 2048; b += kSelThreads) hist[b] = 0u;
+            __syncthreads();
+            for (int q = tid; q < U; q += kSelThreads) {
+                const unsigned key = mag_key(v[q]);
+                if ((key & mask) == prefix) atomicAdd(&hist[(key >> sh) & (unsigned)(nb - 1)], 1u);
+            }
+            __syncthreads();
+            // thread t owns bins nb-1-2t and nb-2-2t (descending keys)
+            const int b0 = nb - 1 - 2 * tid, b1 = b0 - 1;
+            const unsigned h0 = b0 >= 0 ? hist[b0] : 0u, h1 = b1 >= 0 ? hist[b1] : 0u;
+            const unsigned incl = block_scan_u32(h0 + h1, s_wu, nullptr);
+            const unsigned excl = incl - h0 - h1;
+            if (excl < need && need <= incl) {
+                if (excl + h0 >= need) {
+                    s_bin = (unsigned)b0;
+                    s_need = need - excl;
+                } else {
+                    s_bin = (unsigned)b1;
+                    s_need = need - excl - h0;
+                }
+            }
+            __syncthreads();
+            prefix |= s_bin << sh;
+            mask |= (unsigned)(nb - 1) << sh;
+            need = s_need;
+            __syncthreads();
+        }
+        T = prefix;
+    }
+    // bitmap in position order: keys above T, and the first `need` keys equal to T
+    unsigned carry = 0;
+    for (int base = 0; base < U; base += kSelThreads) {
+        const int q = base + tid;
+        const bool in = q < U;
+        const unsigned key = in ? mag_key(v[q]) : 0u;
+        const bool gt = in && (K >= U || key > T), eq = in && K < U && key == T;
+        const unsigned be = __ballot_sync(0xffffffffu, eq);
+        if (lane == 0) s_cnt[warp] = __popc(be);
+        __syncthreads();
+        unsigned off = 0, tot = 0;
+        for (int w = 0; w < 32; ++w) {
+            const unsigned cw = s_cnt[w];
+            if (w < warp) off += cw;
+            tot += cw;
+        }
+        const unsigned rank = carry + off + __popc(be & ((1u << lane) - 1u));
+        const bool take = gt || (eq && rank < need);
+        const unsigned word = __ballot_sync(0xffffffffu, take);
+        if (lane == 0 && base + warp * 32 < U) sc[(base >> 5) + warp] = word;
+        carry += tot;
+        __syncthreads();
+    }
+    if (!toplek || K >= U) {
+        if (tid == 0) P.cnt[c] = K;
+        return;
+    }
+    // ---- TopLEK on the kept set ----
+    int Kp = 1;
+    while (Kp < K) Kp <<= 1;
+    if (tid == 0) s_nk = 0;
+    for (int t = tid; t < Kp; t += kSelThreads) s_set[t] = ~0ull;
+    __syncthreads();
+    for (int q = tid; q < U; q += kSelThreads)
+        if ((sc[q >> 5] >> (q & 31)) & 1u) {
+            const unsigned slot = atomicAdd(&s_nk, 1u);
+            if (slot < (unsigned)Kp)
+                s_set[slot] = ((unsigned long long)mag_key(v[q]) << 32) | (unsigned long long)(0xffffffffu - (unsigned)q);
+        }
+    __syncthreads();
+    for (int size = 2; size <= Kp; size <<= 1) {         // bitonic sort, ascending
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = tid; t < Kp / 2; t += kSelThreads) {
+                const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+                const bool asc = (i & size) == 0;
+                const unsigned long long a = s_set[i], b = s_set[j];
+                if ((a > b) == asc) {
+                    s_set[i] = b;
+                    s_set[j] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // F from the Gram epilogue's partial sums; terms c v^2 of the sorted set
+    double f = 0.0;
+    for (int t = tid; t < P.tiles * 128; t += kSelThreads) f += (double)P.fpart[(size_t)c * P.tiles * 128 + t];
+    double F;
+    block_scan_f64(f, s_wd, &F);
+    const int per = (Kp + kSelThreads - 1) / kSelThreads;    // a run of consecutive sorted entries
+    const int m0 = tid * per;
+    double run = 0.0;
+    for (int m = m0; m < m0 + per && m < K; ++m) {
+        const unsigned long long e = s_set[m];
+        const double a = (double)__uint_as_float((unsigned)(e >> 32));
+        const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
+        run += packed_is_diag(q) ? a * a : (a * a) * 2.0;
+    }
+    double all;
+    const double incl = block_scan_f64(run, s_wd, &all);
+    const double delta = (double)k / (double)U;
+    const double omd_f = (1.0 - delta) * F, eps = 1e-1 * F, hi = omd_f + eps;
+    const double num0 = F - all;
+    if (tid == 0) s_hit = K;
+    __syncthreads();
+    if (hi > num0) {
+        double nx = num0 + (incl - run);
+        for (int m = m0; m < m0 + per && m < K; ++m) {
+            const unsigned long long e = s_set[m];
+            const double a = (double)__uint_as_float((unsigned)(e >> 32));
+            const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
+            nx += packed_is_diag(q) ? a * a : (a * a) * 2.0;
+            if (omd_f < nx + eps) {
+                atomicMin(&s_hit, m);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    const int hit = s_hit;                 // hit == K: no window (nothing kept)
+    int keep = 0;
+    if (hi > num0 && hit < K) {
+        // prev and next numerators at the hit, recomputed in sorted order by the thread that owns it
+        double pv = 0.0, nv = 0.0;
+        if (tid == hit / per) {
+            double acc = num0 + (incl - run);
+            for (int m = m0; m <= hit; ++m) {
+                const unsigned long long e = s_set[m];
+                const double a = (double)__uint_as_float((unsigned)(e >> 32));
+                const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
+                pv = acc;
+                acc += packed_is_diag(q) ? a * a : (a * a) * 2.0;
+            }
+            nv = acc;
+            const double pr = (omd_f - pv + eps) / (nv - pv + eps);
+            uint32_t o;
+            fednl::philox4x32(P.draws[c], 0x544C454Bu, 0u, 0u, seed, (uint32_t)c, o);
+            const double u = ((double)o + 0.5) * (1.0 / 4294967296.0);
+            keep = K - 1 - hit + (u > pr ? 1 : 0);
+            s_nk = (unsigned)keep;
+        }
+        __syncthreads();
+        keep = (int)s_nk;
+    }
+    // drop the K - keep smallest
+    for (int m = tid; m < K - keep; m += kSelThreads) {
+        const unsigned q = 0xffffffffu - (unsigned)(s_set[m] & 0xffffffffu);
+        atomicAnd(&sc[q >> 5], ~(1u << (q & 31)));
+    }
+    if (tid == 0) {
+        P.cnt[c] = keep;
+        P.draws[c] = P.draws[c] + 1;
+    }
 }
 
 // Lk = ||H_c - shift_c||_F from the Gram epilogue's partial sums

@@ -60,7 +60,11 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_last_error", "fednl_gpu_execute_local", "fednl_gpu_load_libsvm",
            "fednl_gpu_weighted_gram_tf32", "fednl_mx_create", "fednl_mx_destroy", "fednl_mx_upload_client_data",
            "fednl_mx_init_shifts", "fednl_mx_run", "fednl_mx_time_rounds", "fednl_mx_get_x", "fednl_mx_get_grad",
-           "fednl_mx_get_l", "fednl_mx_profile_kernels"]
+           "fednl_mx_get_l", "fednl_mx_profile_kernels", "fednl_gpu_client_phase", "fednl_mx_client_phase",
+           "fednl_gpu_solve_batch", "fednl_gpu_round_result", "fednl_mx_round_result", "fednl_gpu_mem_info",
+           "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
+           "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
+           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies"]
 
 _lib = None
 
@@ -124,6 +128,15 @@ def load(build_if_missing: bool = True):
                        "fednl_mx_run": [vp, C.c_int32, dp], "fednl_mx_time_rounds": [vp, C.c_int32, dp, dp],
                        "fednl_mx_get_x": [vp, dp], "fednl_mx_get_grad": [vp, dp],
                        "fednl_mx_profile_kernels": [vp, C.c_int32, dp, C.c_char_p, C.c_int32]}.items():
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = C.c_int
+    for name, args in {"fednl_gpu_client_phase": [vp], "fednl_mx_client_phase": [vp],
+                       "fednl_gpu_solve_batch": [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p), C.c_int32],
+                       "fednl_gpu_round_result": [vp, C.POINTER(RoundStats)],
+                       "fednl_mx_round_result": [vp, C.POINTER(RoundStats)],
+                       "fednl_gpu_mem_info": [C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+                       "fednl_mx_get_diff": [vp, C.c_int32, fp], "fednl_mx_get_shift": [vp, C.c_int32, fp],
+                       "fednl_mx_get_selection": [vp, C.c_int32, up, ip]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -286,6 +299,16 @@ class FedNL:
         _check(load().fednl_gpu_run(self._h, rounds, _dp(out)))
         return out
 
+    def client_phase(self):
+        """Launches the round up to the master's aggregation (no wait); solve_batch ends it."""
+        _check(load().fednl_gpu_client_phase(self._h))
+
+    def round_result(self) -> float:
+        """||g|| of the round that solve_batch just ended (waits for it)."""
+        st = RoundStats()
+        _check(load().fednl_gpu_round_result(self._h, C.byref(st)))
+        return st.grad_norm
+
     def time_rounds(self, rounds: int, flush_bytes: int = 0):
         """Device-timed rounds (CUDA events on the library's stream); returns (total_ms, per_round_ms)."""
         tot = C.c_double(0.0)
@@ -408,15 +431,18 @@ def weighted_gram_tf32(features, weights, n_samples, lam: float = 0.0) -> np.nda
 
 
 class MixedFedNL:
-    """The mixed-precision FedNL round (dense FP32 features, RandK-Philox, Option B): client
-    Hessians on the tensor cores, FP64 master and solve."""
+    """The mixed-precision FedNL round (FP32 features; RandK-Philox, TopK or TopLEK; Option B):
+    client Hessians on the tensor cores, FP64 master and solve."""
 
-    def __init__(self, prob, k: int, alpha: float, seed_base: int = 123, x0=None):
+    def __init__(self, prob, k: int, alpha: float, seed_base: int = 123, x0=None, compressor="randk_philox",
+                 toplek_seed: int = 1234):
         self.d = prob.d
+        self.U = prob.d * (prob.d + 1) // 2
         self.n_clients = prob.n_clients
         self._ns = np.ascontiguousarray(prob.n_samples, dtype=np.int32)
-        desc = ProblemDesc(self.d, 0, self.n_clients, _ip(self._ns), float(prob.lam), RANDK_PHILOX, int(k),
-                           float(alpha), 1, int(seed_base), 1234, 2, 0, 1234, 0, 0, 0.5, 0.5, 5, 0,
+        comp = COMPRESSORS[compressor] if isinstance(compressor, str) else int(compressor)
+        desc = ProblemDesc(self.d, 0, self.n_clients, _ip(self._ns), float(prob.lam), comp, int(k),
+                           float(alpha), 1, int(seed_base), int(toplek_seed), 2, 0, 1234, 0, 0, 0.5, 0.5, 5, 0,
                            (C.c_int32 * 2)(0, 0))
         h = C.c_void_p()
         _check(load().fednl_mx_create(C.byref(desc), C.byref(h)))
@@ -447,6 +473,14 @@ class MixedFedNL:
         _check(load().fednl_mx_run(self._h, rounds, _dp(out)))
         return out
 
+    def client_phase(self):
+        _check(load().fednl_mx_client_phase(self._h))
+
+    def round_result(self) -> float:
+        st = RoundStats()
+        _check(load().fednl_mx_round_result(self._h, C.byref(st)))
+        return st.grad_norm
+
     def time_rounds(self, rounds: int):
         tot = C.c_double(0.0)
         per = np.empty(rounds)
@@ -472,3 +506,38 @@ class MixedFedNL:
 
     def l(self) -> float:
         return load().fednl_mx_get_l(self._h)
+
+    def diff(self, c: int) -> np.ndarray:
+        """The last round's FP32 H_c - shift_c, packed upper [U]."""
+        out = np.empty(self.U, dtype=np.float32)
+        _check(load().fednl_mx_get_diff(self._h, c, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def shift(self, c: int) -> np.ndarray:
+        out = np.empty(self.U, dtype=np.float32)
+        _check(load().fednl_mx_get_shift(self._h, c, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def selection(self, c: int) -> np.ndarray:
+        """Packed upper positions the last round selected for client c."""
+        n = np.zeros(1, dtype=np.int32)
+        out = np.empty(self.U, dtype=np.uint32)
+        _check(load().fednl_mx_get_selection(self._h, c, _up(out), _ip(n)))
+        return out[: int(n[0])].copy()
+
+
+def solve_batch(problems):
+    """Ends the current round of every problem (FedNL or MixedFedNL after client_phase) with one
+    cooperative launch that solves all their Option-B systems."""
+    f64 = [p._h for p in problems if isinstance(p, FedNL)]
+    mx = [p._h for p in problems if isinstance(p, MixedFedNL)]
+    a = (C.c_void_p * max(1, len(f64)))(*f64)
+    b = (C.c_void_p * max(1, len(mx)))(*mx)
+    _check(load().fednl_gpu_solve_batch(a, len(f64), b, len(mx)))
+
+
+def mem_info():
+    """(free, total) device memory in bytes."""
+    f, t = C.c_int64(0), C.c_int64(0)
+    _check(load().fednl_gpu_mem_info(C.byref(f), C.byref(t)))
+    return f.value, t.value
