@@ -268,7 +268,7 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
     R = 10
     mx = fednl.MixedFedNL(prob, k, alpha)
     g_mx = mx.run(R)
-    tot, per = mx.time_rounds(20)
+    tot, per = mx.time_rounds(20, L2_FLUSH_BYTES)
     prof = mx.profile_kernels(5)
     mx.close()
     gram_ms = dict(prof)["k_gram_tf32"]
@@ -294,6 +294,69 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
             "cpu_port_sample": f"1 round, {threads} threads",
             "grad_norm_after_rounds": {"rounds": R, "mixed": float(g_mx[-1]), "fp64": float(g_64[-1]),
                                        "rel_diff": float(abs(g_mx[-1] - g_64[-1]) / g_64[-1])}}
+
+
+def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, fp64_tol_s):
+    """The mixed-precision form on the headline workload (w8a-like, d = 301 padded to 384 on the
+    tensor cores, TopLEK k = 8d): device-timed rounds with a cold L2 before each, the rounds and
+    device time to ||g|| <= 1e-9 from x0 = 0, and the speed-up over the FP64 GPU form."""
+    mx = fednl.MixedFedNL(prob, k, 1.0, compressor=comp)
+    g = mx.run(200)
+    mx.close()
+    hit = np.nonzero(g <= TOL)[0]
+    rounds_to_tol = int(hit[0]) + 1 if hit.size else None
+    mx = fednl.MixedFedNL(prob, k, 1.0, compressor=comp)
+    tol_ms = mx.time_rounds(rounds_to_tol, L2_FLUSH_BYTES)[0] if rounds_to_tol else None
+    mx.close()
+    mx = fednl.MixedFedNL(prob, k, 1.0, compressor=comp)
+    mx.run(3)
+    n = max(20, min(steps, 300))
+    tot, per = mx.time_rounds(n, L2_FLUSH_BYTES)
+    prof = mx.profile_kernels(10)
+    mx.close()
+    rps = n / (tot / 1000.0)
+    return {"rounds_per_s": rps, "round_ms_p50": float(np.percentile(per, 50)),
+            "round_ms_p99": float(np.percentile(per, 99)), "rounds_timed": n, "kernels_ms": dict(prof),
+            "gpu_launches_per_round": len(prof),
+            "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
+                            "seconds": tol_ms / 1000.0 if tol_ms is not None else None},
+            "speedup_vs_fp64_gpu_rounds_per_s": rps / fp64_rounds_per_s,
+            "speedup_vs_fp64_gpu_time_to_tol": (fp64_tol_s / (tol_ms / 1000.0))
+            if (fp64_tol_s and tol_ms) else None,
+            "precision": "TF32 tensor-core client Hessians (FP32 accumulate), FP32 shifts and selection, "
+                         "float-float margins/gradients, FP64 master, Cholesky and solve"}
+
+
+def serving_workload(fednl, count: int = 24, max_rounds: int = 20):
+    """The serving loop on a bounded sample of the request stream (Poisson arrivals at 200/s, seed
+    4; d in {69, 124, 301, 1024}, 16-512 clients, n_i 50-2000, Bernoulli or N(0,1) features, TopK /
+    RandK / TopLEK with k = 8d), every problem on the mixed-precision engine, retired at
+    ||g|| <= 1e-9 or after max_rounds rounds.  Request payloads are generated before the clock
+    starts; the clock covers submission (payload copy), admission (create, upload, initial shifts),
+    every tick and retirement."""
+    from ufednl_gb300 import serving
+    reqs = serving.draw_stream(count, rate=200.0, seed=4)
+    payloads = {r.pid: serving.make_data(r) for r in reqs}
+    srv = serving.Server(reserve_bytes=4 << 30)
+    ids, ticks, wall = serving.serve(reqs, payloads, srv, tol=TOL, max_rounds=max_rounds, realtime=True)
+    lat = srv.latencies()
+    sts = [srv.status(ids[r.pid])[0] for r in reqs]
+    srv.close()
+    done = [s for s in sts if s.state == serving.DONE]
+    resp = [s.t_done_ms - s.t_submit_ms for s in done]
+    held = [t[6] for t in ticks]
+    total = ticks[-1][8] if ticks else 0
+    return {"problems": count, "done": len(done), "failed": sum(s.state == serving.FAILED for s in sts),
+            "converged": sum(1 for s in done if s.grad_norm <= TOL),
+            "problems_per_s": len(done) / wall, "wall_s": wall, "ticks": len(ticks),
+            "round_latency_ms": {"p50": float(np.percentile(lat, 50)) if len(lat) else None,
+                                 "p99": float(np.percentile(lat, 99)) if len(lat) else None},
+            "problem_latency_ms": {"p50": float(np.percentile(resp, 50)) if resp else None,
+                                   "p99": float(np.percentile(resp, 99)) if resp else None},
+            "rounds_total": int(len(lat)), "max_live": int(max(t[1] for t in ticks)) if ticks else 0,
+            "hbm_held_gb": {"max": max(held) / 1e9 if held else 0.0, "mean": float(np.mean(held)) / 1e9 if held else 0.0},
+            "hbm_total_gb": total / 1e9,
+            "max_rounds": max_rounds, "arrivals": "Poisson 200/s (seed 4), realtime submission"}
 
 
 def config_dict(prob, comp, k, workers):
@@ -378,6 +441,9 @@ def run_ours(args, ws, rank, local, td):
             "roofline": roof, "round_roofline": round_roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
             "clocks": clocks, "e2e": e2e}
     if ws == 1 and rank == 0 and not args.no_extra:
+        line["mixed_precision"] = mixed_headline(fednl, prob, comp, k, args.steps, value,
+                                                 tol_ms / 1000.0 if tol_ms is not None else None)
+        line["serving"] = serving_workload(fednl)
         line["extra_workloads"] = extra_workloads(fednl, os.cpu_count() or 1, args.steps)
         line["extra_workloads"]["dense FP32 d1024 256x(512-4096) RandK-Philox k=4d, mixed precision"] = \
             mixed_workload(fednl, os.cpu_count() or 1, bf16 / 2.0, src)

@@ -191,6 +191,10 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
  * d returns FEDNL_EINVAL).  The first call on a device looks up that array's address, so make it
  * before any stream capture.  All calls share the array: calls that overlap on the GPU (different
  * streams or threads at the same time) race and must be serialised by the caller. */
+/* The mixed-precision form's solve of (H + l I) dx = g: FP32 Cholesky factor in one CTA's shared
+ * memory (d up to about 300), one step of iterative refinement on a float-float residual of H held
+ * as an FP32 pair, dx in FP64.  Host buffers, H column-major upper (lda >= d). */
+int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
 int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g,
                                     double* dx, void* stream);
 
@@ -238,12 +242,18 @@ int fednl_mx_destroy(fednl_mx_handle h);
 int fednl_mx_upload_client_data(fednl_mx_handle h, const float* features, const double* labels);
 int fednl_mx_init_shifts(fednl_mx_handle h, const double* x0);
 int fednl_mx_run(fednl_mx_handle h, int32_t rounds, double* grad_norms);
-int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, double* total_ms, double* per_round_ms);
+/* device-timed rounds (CUDA events around each graph replay; flush_bytes > 0 writes a buffer of that
+ * size before every round so that each starts with a cold L2) */
+int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, int64_t flush_bytes, double* total_ms,
+                         double* per_round_ms);
 /* mean per-launch time of the round's 9 kernels (names ';'-separated), CUDA events between launches */
 int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_ms, char* names, int32_t names_len);
 int fednl_mx_get_x(fednl_mx_handle h, double* x);
 int fednl_mx_get_grad(fednl_mx_handle h, double* g);
 double fednl_mx_get_l(fednl_mx_handle h);
+/* Newton solve of the round: 0 = FP64 cooperative Cholesky (default), 1 = FP32 Cholesky in one CTA's
+ * shared memory with one refinement step on a float-float residual (d up to about 300) */
+int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver);
 /* the last round's FP32 differences H_c - shift_c (packed upper, [U]; RandK-Philox: only the
  * selected positions are current), selected packed positions, and the FP32 shift of a client */
 int fednl_mx_get_diff(fednl_mx_handle h, int32_t client, float* diff);

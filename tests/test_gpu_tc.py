@@ -172,3 +172,57 @@ def test_mixed_padded_randk_tracks_fp64(gpu):
     f64.close()
     assert abs(g_mx[0] - g_64[0]) <= 1e-10 * g_64[0]
     assert np.all(np.abs(g_mx - g_64) / g_64 < 0.02)
+
+
+def _spd(rng, d, cond):
+    q, _ = np.linalg.qr(rng.standard_normal((d, d)))
+    ev = np.geomspace(1.0, 1.0 / cond, d)
+    return (q * ev) @ q.T
+
+
+@pytest.mark.parametrize("d", [1, 5, 31, 32, 33, 64, 65, 100, 257, 301, 304])
+def test_mixed_solve_matches_fp64(gpu, d):
+    """The mixed form's Newton solve (FP32 shared-memory Cholesky, one refinement step on a
+    float-float residual): relative error against an FP64 solve below 2e-8 for condition numbers
+    up to 1e3 and below 2e-4 at 1e5 (one refinement step squares the FP32 solve's error, about
+    cond x 2^-24)."""
+    rng = np.random.default_rng(d)
+    for cond, tol in ((1e3, 2e-8), (1e5, 2e-4)):
+        H = _spd(rng, d, cond)
+        lda = d + 3
+        Hc = np.zeros((d, lda))
+        Hc[:, :d] = H.T                                   # column-major with leading dimension lda
+        g = rng.standard_normal(d)
+        l = 1e-3
+        dx = gpu.cholesky_option_b_solve_mixed(Hc.ravel(), d, lda, l, g)
+        ref = np.linalg.solve(H + l * np.eye(d), g)
+        err = np.linalg.norm(dx - ref) / np.linalg.norm(ref)
+        assert err < tol, (d, cond, err)
+
+
+def test_mixed_solve_not_pd(gpu):
+    H = np.array([[1.0, 2.0], [2.0, 1.0]])
+    with pytest.raises(gpu.FedNLError) as e:
+        gpu.cholesky_option_b_solve_mixed(H.ravel(), 2, 2, 0.0, np.ones(2))
+    assert e.value.code == -4
+
+
+@pytest.mark.parametrize("comp", ["randk_philox", "toplek"])
+def test_mixed_round_with_refined_fp32_solve_tracks_fp64_solve(gpu, comp):
+    """The same mixed round solved by the FP32 shared-memory Cholesky with one refinement step
+    instead of the FP64 cooperative Cholesky: the ||g|| trajectories agree to 1e-6 relative while
+    ||g|| falls by decades (the refined solve is accurate to about 1e-8 relative)."""
+    from ufednl_gb300 import datagen
+    d = 200
+    prob = datagen.dense_problem_fp32(71, d, [240, 300, 180, 260], 1e-3)
+    k = 4 * d if comp == "randk_philox" else 8 * d
+    alpha = k / (d * (d + 1) // 2) if comp == "randk_philox" else 1.0
+    a = gpu.MixedFedNL(prob, k, alpha, compressor=comp)
+    ga = a.run(15)
+    a.close()
+    b = gpu.MixedFedNL(prob, k, alpha, compressor=comp, solver="fp32_refined")
+    gb = b.run(15)
+    b.close()
+    assert ga[0] == gb[0]
+    n = int(np.sum(ga > 1e-8))
+    assert np.all(np.abs(ga[:n] - gb[:n]) <= 1e-6 * ga[:n]), (ga, gb)

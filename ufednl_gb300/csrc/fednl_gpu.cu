@@ -944,12 +944,16 @@ int fednl_gpu_solve_batch(fednl_handle* hs, int32_t n, fednl_mx_handle* mxs, int
         descs.push_back(S);
         streams.push_back(h->stream);
     }
+    std::vector<fednl_mx_handle> small;       // mixed handles with the FP32 shared-memory solve
     for (int i = 0; i < nmx; ++i) {
         FednlSolveDesc S{};
         cudaStream_t s2 = nullptr;
         if (fednl_mx_solve_desc(mxs[i], &S, (void**)&s2)) return fail(FEDNL_EINVAL, "mixed handle %d not initialised", i);
-        descs.push_back(S);
         streams.push_back(s2);
+        if (fednl_mx_uses_chol32(mxs[i]))
+            small.push_back(mxs[i]);
+        else
+            descs.push_back(S);
     }
     // the batch stream waits for every client phase, the problems' streams wait for the solve
     for (cudaStream_t s2 : streams) {
@@ -960,6 +964,8 @@ int fednl_gpu_solve_batch(fednl_handle* hs, int32_t n, fednl_mx_handle* mxs, int
         cudaEventDestroy(e);
     }
     int rc = fednl_solve_batch_launch(descs.data(), (int)descs.size(), bst);
+    if (rc) return rc;
+    rc = fednl_mx_solve32_batch(small.data(), (int)small.size(), bst);
     if (rc) return rc;
     for (int i = 0; i < n; ++i) hs[i]->rounds_done += 1;
     return FEDNL_OK;

@@ -10,6 +10,7 @@
 #include "fednl_tc.cuh"
 #include "fednl_solve.h"
 #include "fednl_smem.h"
+#include "fednl_chol32.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -214,6 +215,11 @@ struct fednl_mx_handle_s {
     bool ready = false;
     int rounds_done = 0;
     size_t select_smem = 0;
+    bool chol32 = false;               // the round solves with the FP32 factor + refinement
+    bool chol32_ok = false;            // the system fits one CTA's shared memory
+    fednl_c32::Job* cjob = nullptr;    // device copy of the solve's job
+    void* flush_buf = nullptr;
+    int64_t flush_bytes = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
     size_t dry = 0;            // footprint only: bytes the allocations would take
@@ -281,6 +287,12 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     mark();
     CKM(cudaGetLastError());
     if (client_phase_only) return FEDNL_OK;
+    if (h->chol32) {
+        fednl_c32::k_chol32<<<1, fednl_c32::kT, fednl_c32::smem_bytes(h->d), st>>>(h->cjob);
+        mark();
+        CKM(cudaGetLastError());
+        return FEDNL_OK;
+    }
     int rc = fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, h->dx, P.x, h->work, h->ybuf, h->rinv, h->bar,
                                         h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st);
     mark();
@@ -368,6 +380,11 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     rc |= h->alloc(&P.gc, (size_t)h->nc * h->d);
     rc |= h->alloc(&P.g, h->d);
     rc |= h->alloc(&P.H, h->U);
+    rc |= h->alloc(&P.Hh, h->U);
+    rc |= h->alloc(&P.Hl, h->U);
+    rc |= h->alloc(&P.Hrh, h->U);
+    rc |= h->alloc(&P.Hrl, h->U);
+    rc |= h->alloc(&h->cjob, 1);
     rc |= h->alloc(&P.shift, ncUp);
     rc |= h->alloc(&P.dsel, ncUp);
     rc |= h->alloc(&P.sel, (size_t)h->nc * h->SW);
@@ -415,6 +432,35 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
         fednl_mx_destroy(h);
         return rc ? rc : fail_m(FEDNL_ECUDA, "shared-memory attribute refused");
     }
+    {   // the FP32 solve when the augmented system fits in one CTA's shared memory
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const size_t need = fednl_c32::smem_bytes(h->d);
+        if (need + 1024 <= (size_t)optin &&
+            fednl_raise_dyn_smem((const void*)fednl_c32::k_chol32, need) == cudaSuccess) {
+            fednl_c32::Job J{};
+            J.d = h->d;
+            J.Hh = P.Hh;
+            J.Hl = P.Hl;
+            J.Hrh = P.Hrh;
+            J.Hrl = P.Hrl;
+            J.lptr = P.stats + 1;
+            J.g = P.g;
+            J.dx = h->dx;
+            J.x = P.x;
+            J.stats = P.stats;
+            J.hist = h->hist;
+            J.round_ctr = h->round_ctr;
+            J.hist_cap = h->hist_cap;
+            J.status = h->status;
+            if (cudaMemcpy(h->cjob, &J, sizeof(J), cudaMemcpyHostToDevice) != cudaSuccess) {
+                fednl_mx_destroy(h);
+                return fail_m(FEDNL_ECUDA, "initial copies failed");
+            }
+            h->chol32_ok = true;
+        }
+    }
     if (h->comp == FEDNL_TOPLEK && h->k < h->U) {
         int kp = 1;
         while (kp < h->k) kp <<= 1;
@@ -449,6 +495,7 @@ int fednl_mx_destroy(fednl_mx_handle h)
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->graph) cudaGraphDestroy(h->graph);
     for (void* p : h->allocs) cudaFree(p);
+    if (h->flush_buf) cudaFree(h->flush_buf);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return FEDNL_OK;
@@ -540,29 +587,43 @@ int fednl_mx_run(fednl_mx_handle h, int32_t rounds, double* grad_norms)
     return FEDNL_OK;
 }
 
-int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, double* total_ms, double* per_round_ms)
+int fednl_mx_time_rounds(fednl_mx_handle h, int32_t rounds, int64_t flush_bytes, double* total_ms,
+                         double* per_round_ms)
 {
-    if (!h || rounds < 1 || !total_ms) return fail_m(FEDNL_EINVAL, "bad argument");
+    if (!h || rounds < 1 || !total_ms || flush_bytes < 0) return fail_m(FEDNL_EINVAL, "bad argument");
     int rc = fednl_mx_run(h, 0, nullptr);      // builds the graph
     if (rc) return rc;
-    std::vector<cudaEvent_t> ev(rounds + 1);
+    if (flush_bytes > h->flush_bytes) {        // a buffer larger than L2, written before every round
+        if (h->flush_buf) cudaFree(h->flush_buf);
+        h->flush_buf = nullptr;
+        h->flush_bytes = 0;
+        CKM(cudaMalloc(&h->flush_buf, (size_t)flush_bytes));
+        h->flush_bytes = flush_bytes;
+    }
+    std::vector<cudaEvent_t> ev(2 * (size_t)rounds);
     for (auto& e : ev) CKM(cudaEventCreate(&e));
-    CKM(cudaEventRecord(ev[0], h->stream));
     for (int r = 0; r < rounds; ++r) {
+        if (flush_bytes) CKM(cudaMemsetAsync(h->flush_buf, r & 0xFF, (size_t)flush_bytes, h->stream));
+        CKM(cudaEventRecord(ev[2 * r], h->stream));
         CKM(cudaGraphLaunch(h->gexec, h->stream));
-        CKM(cudaEventRecord(ev[r + 1], h->stream));
+        CKM(cudaEventRecord(ev[2 * r + 1], h->stream));
     }
     CKM(cudaStreamSynchronize(h->stream));
-    float tot = 0.f;
-    cudaEventElapsedTime(&tot, ev[0], ev[rounds]);
-    *total_ms = tot;
-    for (int r = 0; r < rounds && per_round_ms; ++r) {
+    double tot = 0.0;
+    for (int r = 0; r < rounds; ++r) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev[r], ev[r + 1]);
-        per_round_ms[r] = ms;
+        cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]);
+        tot += ms;
+        if (per_round_ms) per_round_ms[r] = ms;
     }
+    *total_ms = tot;
     for (auto& e : ev) cudaEventDestroy(e);
     h->rounds_done += rounds;
+    int err = 0, status = 0;
+    CKM(cudaMemcpy(&err, h->err, 4, cudaMemcpyDeviceToHost));
+    CKM(cudaMemcpy(&status, h->status, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail_m(FEDNL_ETIMEOUT, "a bounded wait of the Gram kernel ran out");
+    if (status) return fail_m(status, "Option-B solve failed in one of the timed rounds");
     return FEDNL_OK;
 }
 
@@ -587,11 +648,27 @@ int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_m
     if (names && names_len > 0) {
         std::string all;
         const char* const* nm = h->comp == FEDNL_RANDK_PHILOX ? kMxKernelNames : kMxKernelNamesTop;
-        for (int t = 0; t < kMxKernels; ++t) all += std::string(t ? ";" : "") + nm[t];
+        for (int t = 0; t < kMxKernels; ++t)
+            all += std::string(t ? ";" : "") + (t == kMxKernels - 1 && h->chol32 ? "k_chol32" : nm[t]);
         snprintf(names, (size_t)names_len, "%s", all.c_str());
     }
     h->rounds_done += rounds;
     return rc;
+}
+
+int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver)
+{
+    if (!h || solver < 0 || solver > 1) return fail_m(FEDNL_EINVAL, "bad argument");
+    if (solver == 1 && !h->chol32_ok) return fail_m(FEDNL_EINVAL, "d %d too large for the shared-memory solve", h->d);
+    const bool want = solver == 1;
+    if (want != h->chol32 && h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
+    }
+    h->chol32 = want;
+    return FEDNL_OK;
 }
 
 int fednl_mx_client_phase(fednl_mx_handle h)
@@ -621,6 +698,122 @@ int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats)
     if (status) return fail_m(status, "Option-B matrix not positive definite");
     return FEDNL_OK;
 }
+
+}  // extern "C"
+
+int fednl_mx_uses_chol32(fednl_mx_handle h) { return h && h->chol32 ? 1 : 0; }
+
+extern "C" int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, double l, const double* g,
+                                             double* dx)
+{
+    if (!H || !g || !dx || d < 1 || lda < d) return fail_m(FEDNL_EINVAL, "bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail_m(FEDNL_ENODEV, "no CUDA device available");
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t need = fednl_c32::smem_bytes(d);
+    if (need + 1024 > (size_t)optin) return fail_m(FEDNL_EINVAL, "d %d too large for the shared-memory solve", d);
+    CKM(fednl_raise_dyn_smem((const void*)fednl_c32::k_chol32, need));
+    const size_t U = (size_t)d * (d + 1) / 2;
+    std::vector<float> hh(U), hl(U), rh(U), rl(U);
+    for (int j = 0; j < d; ++j)
+        for (int i = 0; i <= j; ++i) {
+            const double v = H[(size_t)j * lda + i];
+            const float a = (float)v, b = (float)(v - (double)a);
+            hh[(size_t)j * (j + 1) / 2 + i] = a;
+            hl[(size_t)j * (j + 1) / 2 + i] = b;
+            const size_t r = (size_t)i * d - (size_t)i * (i - 1) / 2 + j - i;
+            rh[r] = a;
+            rl[r] = b;
+        }
+    float *dHh = nullptr, *dHl = nullptr, *dRh = nullptr, *dRl = nullptr;
+    double *dl = nullptr, *dg = nullptr, *ddx = nullptr, *dst = nullptr, *dhist = nullptr;
+    int *dctr = nullptr, *dstatus = nullptr;
+    fednl_c32::Job* dj = nullptr;
+    int rc = FEDNL_OK;
+    if (cudaMalloc(&dHh, U * 4) || cudaMalloc(&dHl, U * 4) || cudaMalloc(&dRh, U * 4) || cudaMalloc(&dRl, U * 4) ||
+        cudaMalloc(&dl, 8) || cudaMalloc(&dg, d * 8) ||
+        cudaMalloc(&ddx, d * 8) || cudaMalloc(&dst, 32) || cudaMalloc(&dhist, 8) || cudaMalloc(&dctr, 4) ||
+        cudaMalloc(&dstatus, 4) || cudaMalloc(&dj, sizeof(fednl_c32::Job))) {
+        rc = fail_m(FEDNL_ENOMEM, "device allocation failed");
+    } else {
+        fednl_c32::Job J{};
+        J.d = d;
+        J.Hh = dHh;
+        J.Hl = dHl;
+        J.Hrh = dRh;
+        J.Hrl = dRl;
+        J.lptr = dl;
+        J.g = dg;
+        J.dx = ddx;
+        J.x = nullptr;
+        J.stats = dst;
+        J.hist = dhist;
+        J.round_ctr = dctr;
+        J.hist_cap = 1;
+        J.status = dstatus;
+        if (cudaMemcpy(dHh, hh.data(), U * 4, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(dHl, hl.data(), U * 4, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(dRh, rh.data(), U * 4, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(dRl, rl.data(), U * 4, cudaMemcpyHostToDevice) || cudaMemcpy(dl, &l, 8, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(dg, g, d * 8, cudaMemcpyHostToDevice) || cudaMemset(dctr, 0, 4) || cudaMemset(dstatus, 0, 4) ||
+            cudaMemcpy(dj, &J, sizeof(J), cudaMemcpyHostToDevice)) {
+            rc = fail_m(FEDNL_ECUDA, "copies failed");
+        } else {
+            fednl_c32::k_chol32<<<1, fednl_c32::kT, need>>>(dj);
+            int status = 0;
+            if (cudaDeviceSynchronize() != cudaSuccess ||
+                cudaMemcpy(&status, dstatus, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = fail_m(FEDNL_ECUDA, "solve kernel failed");
+            else if (status)
+                rc = fail_m(status, "matrix not positive definite");
+            else if (cudaMemcpy(dx, ddx, d * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = fail_m(FEDNL_ECUDA, "copy back failed");
+        }
+    }
+    cudaFree(dHh);
+    cudaFree(dHl);
+    cudaFree(dRh);
+    cudaFree(dRl);
+    cudaFree(dl);
+    cudaFree(dg);
+    cudaFree(ddx);
+    cudaFree(dst);
+    cudaFree(dhist);
+    cudaFree(dctr);
+    cudaFree(dstatus);
+    cudaFree(dj);
+    return rc;
+}
+
+int fednl_mx_solve32_batch(fednl_mx_handle const* hs, int n, void* stream)
+{
+    if (n <= 0) return FEDNL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    static fednl_c32::Job* djobs = nullptr;
+    static int cap = 0;
+    std::vector<fednl_c32::Job> jobs(n);
+    size_t smem = 0;
+    for (int i = 0; i < n; ++i) {
+        CKM(cudaMemcpy(&jobs[i], hs[i]->cjob, sizeof(fednl_c32::Job), cudaMemcpyDeviceToHost));
+        smem = std::max(smem, fednl_c32::smem_bytes(hs[i]->d));
+    }
+    if (cap < n) {
+        if (djobs) cudaFree(djobs);
+        djobs = nullptr;
+        cap = 0;
+        CKM(cudaMalloc(&djobs, sizeof(fednl_c32::Job) * n));
+        cap = n;
+    }
+    CKM(cudaMemcpyAsync(djobs, jobs.data(), sizeof(fednl_c32::Job) * n, cudaMemcpyHostToDevice, st));
+    fednl_c32::k_chol32<<<n, fednl_c32::kT, smem, st>>>(djobs);
+    CKM(cudaGetLastError());
+    CKM(cudaStreamSynchronize(st));
+    return FEDNL_OK;
+}
+
+extern "C" {
 
 int fednl_mx_solve_desc(fednl_mx_handle h, FednlSolveDesc* S, void** stream)
 {

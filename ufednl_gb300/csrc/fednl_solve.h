@@ -30,3 +30,7 @@ int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream);
 // fednl_mixed.cu: a mixed-precision handle's solve as a descriptor (and its stream)
 struct fednl_mx_handle_s;
 extern "C" int fednl_mx_solve_desc(struct fednl_mx_handle_s* h, FednlSolveDesc* desc, void** stream);
+// 1 when the handle's solve is the FP32 shared-memory factor with refinement (fednl_chol32.cuh)
+int fednl_mx_uses_chol32(struct fednl_mx_handle_s* h);
+// those handles' solves in one launch, one CTA per system, on the given stream (host-synchronous)
+int fednl_mx_solve32_batch(struct fednl_mx_handle_s* const* hs, int n, void* stream);

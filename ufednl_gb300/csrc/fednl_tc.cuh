@@ -431,6 +431,10 @@ struct MxDev {
     double* gc;             // [nc][d]
     double* g;              // [d]
     double* H;              // [U] master, packed upper
+    float* Hh;              // [U] H as an FP32 pair (hi + lo) for the FP32 solve's residual
+    float* Hl;
+    float* Hrh;             // [U] the same pair in row-major packed order
+    float* Hrl;
     float* shift;           // [nc][Up]
     float* dsel;            // [nc][Up]
     unsigned* sel;          // [nc][SW]
@@ -781,6 +785,21 @@ __global__ void k_mx_lk(MxDev P)
     }
 }
 
+// H[p] as an FP32 pair at packed position p (column-major) and at its row-major position
+__device__ __forceinline__ void store_pair(const MxDev& P, int p, double h)
+{
+    int n = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+    while (n > 0 && n * (n + 1) / 2 > p) --n;
+    while ((n + 1) * (n + 2) / 2 <= p) ++n;
+    const int m = p - n * (n + 1) / 2;
+    const float hh = (float)h, hl = (float)(h - (double)hh);
+    P.Hh[p] = hh;
+    P.Hl[p] = hl;
+    const int r = m * P.d - (m * (m - 1)) / 2 + n - m;
+    P.Hrh[r] = hh;
+    P.Hrl[r] = hl;
+}
+
 // worker shift update (FP32) and master merge (FP64), clients in order per position
 __global__ void k_mx_apply(MxDev P)
 {
@@ -796,6 +815,7 @@ __global__ void k_mx_apply(MxDev P)
         h += item * P.prescale;
     }
     P.H[p] = h;
+    store_pair(P, p, h);
 }
 
 // g = mean g_c, l = mean Lk
@@ -821,7 +841,9 @@ __global__ void k_mx_hinit(MxDev P)
     if (p >= P.U) return;
     double h = 0.0;
     for (int c = 0; c < P.nc; ++c) h += (double)P.shift[(size_t)c * P.Up + p];
-    P.H[p] = h * P.inv_n;
+    h *= P.inv_n;
+    P.H[p] = h;
+    store_pair(P, p, h);
 }
 
 }  // namespace fednl_tc

@@ -64,7 +64,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_solve_batch", "fednl_gpu_round_result", "fednl_mx_round_result", "fednl_gpu_mem_info",
            "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
-           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies"]
+           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed",
+           "fednl_mx_set_solver"]
 
 _lib = None
 
@@ -104,6 +105,7 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_natural": [dp, C.c_int64, dp, C.POINTER(C.c_uint8)],
         "fednl_gpu_logreg_oracle": [dp, dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, dp, dp, dp],
         "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
+        "fednl_gpu_optionb_solve_mixed": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
         "fednl_gpu_optionb_solve_noalloc": [vp, C.c_int32, C.c_int32, C.c_double, vp, vp, vp],
         "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
         "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
@@ -125,7 +127,7 @@ def load(build_if_missing: bool = True):
     L.fednl_gpu_weighted_gram_tf32.restype = C.c_int
     for name, args in {"fednl_mx_create": [C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)], "fednl_mx_destroy": [vp],
                        "fednl_mx_upload_client_data": [vp, fp, dp], "fednl_mx_init_shifts": [vp, dp],
-                       "fednl_mx_run": [vp, C.c_int32, dp], "fednl_mx_time_rounds": [vp, C.c_int32, dp, dp],
+                       "fednl_mx_run": [vp, C.c_int32, dp], "fednl_mx_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
                        "fednl_mx_get_x": [vp, dp], "fednl_mx_get_grad": [vp, dp],
                        "fednl_mx_profile_kernels": [vp, C.c_int32, dp, C.c_char_p, C.c_int32]}.items():
         getattr(L, name).argtypes = args
@@ -136,7 +138,7 @@ def load(build_if_missing: bool = True):
                        "fednl_mx_round_result": [vp, C.POINTER(RoundStats)],
                        "fednl_gpu_mem_info": [C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
                        "fednl_mx_get_diff": [vp, C.c_int32, fp], "fednl_mx_get_shift": [vp, C.c_int32, fp],
-                       "fednl_mx_get_selection": [vp, C.c_int32, up, ip]}.items():
+                       "fednl_mx_get_selection": [vp, C.c_int32, up, ip], "fednl_mx_set_solver": [vp, C.c_int32]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -232,6 +234,15 @@ def evaluate_gradient_and_hessian(features, labels, lam: float, x, lda: int | No
     h = np.empty(d * lda)
     _check(load().fednl_gpu_logreg_oracle(_dp(f), _dp(b), n, d, lda, lam, _dp(xx), _dp(g), _dp(h)))
     return g, h
+
+
+def cholesky_option_b_solve_mixed(H: np.ndarray, d: int, lda: int, l: float, g: np.ndarray) -> np.ndarray:
+    """(H + l I) dx = g with the mixed-precision form's solve (FP32 factor, refined)."""
+    Hc = np.ascontiguousarray(H, dtype=np.float64)
+    gc = np.ascontiguousarray(g, dtype=np.float64)
+    dx = np.empty(d)
+    _check(load().fednl_gpu_optionb_solve_mixed(_dp(Hc), d, lda, float(l), _dp(gc), _dp(dx)))
+    return dx
 
 
 def cholesky_option_b_solve(H: np.ndarray, d: int, lda: int, l: float, g: np.ndarray) -> np.ndarray:
@@ -435,7 +446,7 @@ class MixedFedNL:
     client Hessians on the tensor cores, FP64 master and solve."""
 
     def __init__(self, prob, k: int, alpha: float, seed_base: int = 123, x0=None, compressor="randk_philox",
-                 toplek_seed: int = 1234):
+                 toplek_seed: int = 1234, solver: str = "fp64"):
         self.d = prob.d
         self.U = prob.d * (prob.d + 1) // 2
         self.n_clients = prob.n_clients
@@ -453,6 +464,7 @@ class MixedFedNL:
             _check(load().fednl_mx_upload_client_data(self._h, f.ctypes.data_as(C.POINTER(C.c_float)), _dp(b)))
             xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
             _check(load().fednl_mx_init_shifts(self._h, _dp(xx) if xx is not None else None))
+            _check(load().fednl_mx_set_solver(self._h, {"fp64": 0, "fp32_refined": 1}[solver]))
         except Exception:
             self.close()
             raise
@@ -481,10 +493,10 @@ class MixedFedNL:
         _check(load().fednl_mx_round_result(self._h, C.byref(st)))
         return st.grad_norm
 
-    def time_rounds(self, rounds: int):
+    def time_rounds(self, rounds: int, flush_bytes: int = 0):
         tot = C.c_double(0.0)
         per = np.empty(rounds)
-        _check(load().fednl_mx_time_rounds(self._h, rounds, C.byref(tot), _dp(per)))
+        _check(load().fednl_mx_time_rounds(self._h, rounds, flush_bytes, C.byref(tot), _dp(per)))
         return tot.value, per
 
     def profile_kernels(self, rounds: int):
