@@ -223,6 +223,6 @@ def test_mixed_round_with_refined_fp32_solve_tracks_fp64_solve(gpu, comp):
     b = gpu.MixedFedNL(prob, k, alpha, compressor=comp, solver="fp32_refined")
     gb = b.run(15)
     b.close()
-    assert ga[0] == gb[0]
+    assert abs(ga[0] - gb[0]) <= 1e-14 * ga[0]          # ||g|| summed in another order
     n = int(np.sum(ga > 1e-8))
     assert np.all(np.abs(ga[:n] - gb[:n]) <= 1e-6 * ga[:n]), (ga, gb)

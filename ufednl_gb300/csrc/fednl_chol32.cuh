@@ -205,73 +205,63 @@ __global__ void __launch_bounds__(kT, 1) k_chol32(const Job* __restrict__ jobs)
 
     for (int c0 = 0; c0 < d; c0 += kNB) {
         const int nb = d - c0 < kNB ? d - c0 : kNB, c1 = c0 + nb;
-        // 1. the diagonal block R_bb by warp 0 in registers: lane j holds column c0 + j
+        // 1. the diagonal block R_bb by warp 0 in registers: lane j holds column c0 + j, its rows
+        //    from the current pivot row down in a[0..]; after each step the rows move up one
+        //    register, so that one rolled loop body serves every step
         if (warp == 0) {
             float a[kNB];
 #pragma unroll
             for (int m = 0; m < kNB; ++m) a[m] = (m <= lane && lane < nb) ? A[rp(c0 + m, c0 + lane, D)] : 0.0f;
             bool bad = false;
-#pragma unroll
-            for (int k = 0; k < kNB; ++k) {
-                if (k < nb) {
-                    float inv = 0.0f;
-                    if (lane == k) {
-                        const float t = a[k];
-                        bad = !(t > 0.0f);
-                        inv = rsqrtf(t);
-                        a[k] = __fmul_rn(t, inv);
-                        rinv[c0 + k] = inv;
-                    }
-                    inv = __shfl_sync(0xffffffffu, inv, k);
-                    if (lane > k) a[k] = __fmul_rn(a[k], inv);          // r_{k, lane}
-                    s_row[lane] = a[k];                                 // row k of the block
-                    __syncwarp();
-                    float rv[kNB];
-#pragma unroll
-                    for (int q = 0; q < kNB / 4; ++q) {
-                        const float4 v4 = reinterpret_cast<const float4*>(s_row)[q];
-                        rv[4 * q] = v4.x;
-                        rv[4 * q + 1] = v4.y;
-                        rv[4 * q + 2] = v4.z;
-                        rv[4 * q + 3] = v4.w;
-                    }
-#pragma unroll
-                    for (int i = k + 1; i < kNB; ++i)
-                        if (i < nb && lane >= i) a[i] = fmaf(-rv[i], a[k], a[i]);
-                    __syncwarp();
+#pragma unroll 1
+            for (int k = 0; k < nb; ++k) {
+                float inv = 0.0f;
+                if (lane == k) {
+                    const float t = a[0];
+                    bad = !(t > 0.0f);
+                    inv = rsqrtf(t);
+                    a[0] = __fmul_rn(t, inv);
+                    rinv[c0 + k] = inv;
                 }
-            }
+                inv = __shfl_sync(0xffffffffu, inv, k);
+                if (lane > k) a[0] = __fmul_rn(a[0], inv);             // r_{k, lane}
+                s_row[lane] = a[0];
+                if (lane >= k && lane < nb) A[rp(c0 + k, c0 + lane, D)] = a[0];
+                __syncwarp();
 #pragma unroll
-            for (int m = 0; m < kNB; ++m)
-                if (m <= lane && lane < nb) A[rp(c0 + m, c0 + lane, D)] = a[m];
+                for (int m = 1; m < kNB; ++m) {
+                    const int i = k + m;                                 // row of a[m]
+                    const float rki = i < kNB ? s_row[i < kNB ? i : 0] : 0.0f;
+                    if (lane >= i && i < nb) a[m] = fmaf(-rki, a[0], a[m]);
+                }
+#pragma unroll
+                for (int m = 0; m + 1 < kNB; ++m) a[m] = a[m + 1];
+                a[kNB - 1] = 0.0f;
+                __syncwarp();
+            }
             if (__any_sync(0xffffffffu, bad) && lane == 0) s_fail = 1;
         }
         __syncthreads();
         if (s_fail) break;
         // 2. the panel rows right of the block: R_b,rest = R_bb^-T A_b,rest, one column per thread
+        //    (forward substitution with the same register rotation)
         for (int j = c1 + tid; j < D; j += kT) {
             float acc[kNB];
 #pragma unroll
             for (int m = 0; m < kNB; ++m) acc[m] = m < nb ? A[rp(c0 + m, j, D)] : 0.0f;
+#pragma unroll 1
+            for (int k = 0; k < nb; ++k) {
+                const float x = __fmul_rn(acc[0], rinv[c0 + k]);
+                A[rp(c0 + k, j, D)] = x;
+                Pk[k * S4 + j] = x;
+                const float* rowk = A + rp(c0 + k, c0 + k, D);         // row k of the block: rowk[m]
 #pragma unroll
-            for (int k = 0; k < kNB; ++k) {
-                if (k < nb) {
-                    const float* rowk = A + rp(c0 + k, c0 + k, D);     // row k of the block: rowk[m - k]
-                    float rv[kNB];
+                for (int m = 1; m < kNB; ++m)
+                    if (k + m < nb) acc[m] = fmaf(-rowk[m], x, acc[m]);
 #pragma unroll
-                    for (int m = k + 1; m < kNB; ++m) rv[m] = m < nb ? rowk[m - k] : 0.0f;
-                    const float x = __fmul_rn(acc[k], rinv[c0 + k]);
-                    acc[k] = x;
-#pragma unroll
-                    for (int m = k + 1; m < kNB; ++m) acc[m] = fmaf(-rv[m], x, acc[m]);
-                }
+                for (int m = 0; m + 1 < kNB; ++m) acc[m] = acc[m + 1];
+                acc[kNB - 1] = 0.0f;
             }
-#pragma unroll
-            for (int m = 0; m < kNB; ++m)
-                if (m < nb) {
-                    A[rp(c0 + m, j, D)] = acc[m];
-                    Pk[m * S4 + j] = acc[m];
-                }
         }
         __syncthreads();
         if (c1 >= d) break;

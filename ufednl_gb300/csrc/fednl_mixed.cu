@@ -278,12 +278,12 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     mark();
     if (!randk) {
         const int toplek = h->comp == FEDNL_TOPLEK;
-        k_mx_select<<<h->nc, kSelThreads, toplek ? h->select_smem : 0, st>>>(P, h->k, toplek, h->desc.toplek_seed);
+        k_mx_select<<<h->nc, kSelThreads, h->select_smem, st>>>(P, h->k, toplek, h->desc.toplek_seed);
         mark();
     }
     k_mx_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     mark();
-    k_mx_aggregate<<<(h->d + 255) / 256, 256, 0, st>>>(P);
+    k_mx_aggregate<<<(h->d + 7) / 8, 256, 0, st>>>(P);
     mark();
     CKM(cudaGetLastError());
     if (client_phase_only) return FEDNL_OK;
@@ -461,7 +461,7 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
             h->chol32_ok = true;
         }
     }
-    if (h->comp == FEDNL_TOPLEK && h->k < h->U) {
+    if (h->comp == FEDNL_TOPLEK && h->k < h->U) {     // TopLEK sorts its kept set in shared memory
         int kp = 1;
         while (kp < h->k) kp <<= 1;
         h->select_smem = (size_t)kp * 8;

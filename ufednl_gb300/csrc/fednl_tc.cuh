@@ -8,7 +8,8 @@
 //   * one CTA per 128 x 128 tile of the upper triangle of H_i (tiles of one client are scheduled
 //     together so that the client's block stays in L2);
 //   * warp 0 streams 128 x 32 FP32 slabs of the two tile rows with TMA (3-D tensor map over
-//     [client][feature][sample], 128-byte swizzle) into a 6-stage ring guarded by mbarriers;
+//     [client][feature][sample], 128-byte swizzle) into a 3-stage ring guarded by mbarriers (two CTAs
+//     fit an SM, so one CTA's epilogue overlaps the other's main loop);
 //   * warps 2-5 scale the B slab by the per-sample weights D_s in shared memory (the swizzle is
 //     undone to find each element's sample) and release it to the tensor cores;
 //   * warp 1 (one lane) issues tcgen05.mma.kind::tf32 (M = N = 128, K = 8, four per slab) into a
@@ -29,7 +30,7 @@
 namespace fednl_tc {
 
 constexpr int kBM = 128, kBN = 128, kBK = 32;     // tile rows, tile columns, FP32 samples per slab
-constexpr int kStages = 6;
+constexpr int kStages = 3;
 constexpr int kSlabBytes = kBM * kBK * 4;         // 16 KB (128 rows x 128 bytes)
 constexpr int kThreads = 192;
 constexpr long long kWaitCycles = 2000000000ll;   // ~1 s
@@ -466,12 +467,35 @@ __global__ void __launch_bounds__(256) k_mx_margin(MxDev P)
     const int n = P.ns[c];
     if (s >= n) return;
     const float* col = P.X + (size_t)c * P.dp * P.L + s;
-    float hi = 0.0f, lo = 0.0f;
-    for (int i = 0; i < P.d; ++i) {
-        const float xv = col[(size_t)i * P.L];
-        const float yh = i < 1024 ? s_xh[i] : P.xh[i], yl = i < 1024 ? s_xl[i] : P.xl[i];
-        ff_mac(hi, lo, xv, yh, yl);
+    // eight feature loads in flight, four independent float-float accumulators (feature i mod 4)
+    float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f, h2 = 0.0f, l2 = 0.0f, h3 = 0.0f, l3 = 0.0f;
+    int i = 0;
+    for (; i + 8 <= P.d; i += 8) {
+        float xv[8], yh[8], yl[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xv[u] = __ldg(col + (size_t)(i + u) * P.L);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            yh[u] = i + u < 1024 ? s_xh[i + u] : P.xh[i + u];
+            yl[u] = i + u < 1024 ? s_xl[i + u] : P.xl[i + u];
+        }
+        ff_mac(h0, l0, xv[0], yh[0], yl[0]);
+        ff_mac(h1, l1, xv[1], yh[1], yl[1]);
+        ff_mac(h2, l2, xv[2], yh[2], yl[2]);
+        ff_mac(h3, l3, xv[3], yh[3], yl[3]);
+        ff_mac(h0, l0, xv[4], yh[4], yl[4]);
+        ff_mac(h1, l1, xv[5], yh[5], yl[5]);
+        ff_mac(h2, l2, xv[6], yh[6], yl[6]);
+        ff_mac(h3, l3, xv[7], yh[7], yl[7]);
     }
+    for (; i < P.d; ++i) {
+        const float yh = i < 1024 ? s_xh[i] : P.xh[i], yl = i < 1024 ? s_xl[i] : P.xl[i];
+        ff_mac(h0, l0, __ldg(col + (size_t)i * P.L), yh, yl);
+    }
+    ff_add(h0, l0, h1, l1);
+    ff_add(h2, l2, h3, l3);
+    ff_add(h0, l0, h2, l2);
+    const float hi = h0, lo = l0;
     const double b = P.lab[(size_t)c * P.L + s];
     const double m = b * ((double)hi + (double)lo);
     const double sig = mx_sigmoid(m);
@@ -492,8 +516,16 @@ __global__ void __launch_bounds__(256) k_mx_grad(MxDev P)
     const float* row = P.X + ((size_t)c * P.dp + i) * P.L;
     const float* qh = P.qh + (size_t)c * P.L;
     const float* ql = P.ql + (size_t)c * P.L;
-    float hi = 0.0f, lo = 0.0f;
-    for (int s = lane; s < n; s += 32) ff_mac(hi, lo, row[s], qh[s], ql[s]);
+    float hi = 0.0f, lo = 0.0f, h1 = 0.0f, l1 = 0.0f;
+    int s = lane;
+    for (; s + 32 < n; s += 64) {
+        const float x0 = __ldg(row + s), x1 = __ldg(row + s + 32);
+        const float a0 = __ldg(qh + s), a1 = __ldg(qh + s + 32), b0 = __ldg(ql + s), b1 = __ldg(ql + s + 32);
+        ff_mac(hi, lo, x0, a0, b0);
+        ff_mac(h1, l1, x1, a1, b1);
+    }
+    if (s < n) ff_mac(hi, lo, row[s], qh[s], ql[s]);
+    ff_add(hi, lo, h1, l1);
     double v = (double)hi + (double)lo;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) P.gc[(size_t)c * P.d + i] = v + P.lambda * P.x[i];
@@ -585,7 +617,7 @@ __device__ __forceinline__ double block_scan_f64(double v, double* s_w, double* 
 
 __device__ __forceinline__ bool packed_is_diag(long long p)
 {
-    long long j = (long long)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    long long j = (long long)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
     while (j > 0 && j * (j + 1) / 2 > p) --j;
     while ((j + 1) * (j + 2) / 2 <= p) ++j;
     return p - j * (j + 1) / 2 == j;
@@ -601,9 +633,9 @@ __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int t
     __shared__ unsigned s_bin, s_need, s_cnt[32], s_nk;
     __shared__ int s_hit;
     const int c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int U = P.U;
     const float* v = P.dsel + (size_t)c * P.Up;
     unsigned* sc = P.sel + (size_t)c * P.SW;
-    const int U = P.U;
     const int K = k < U ? k : U;
     unsigned T = 0, need = 0;
     if (K < U) {
@@ -672,15 +704,29 @@ __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int t
     // ---- TopLEK on the kept set ----
     int Kp = 1;
     while (Kp < K) Kp <<= 1;
-    if (tid == 0) s_nk = 0;
     for (int t = tid; t < Kp; t += kSelThreads) s_set[t] = ~0ull;
     __syncthreads();
-    for (int q = tid; q < U; q += kSelThreads)
-        if ((sc[q >> 5] >> (q & 31)) & 1u) {
-            const unsigned slot = atomicAdd(&s_nk, 1u);
-            if (slot < (unsigned)Kp)
-                s_set[slot] = ((unsigned long long)mag_key(v[q]) << 32) | (unsigned long long)(0xffffffffu - (unsigned)q);
+    {   // the kept entries in position order: popcounts of the bitmap words, block-scanned
+        unsigned base_cnt = 0;
+        for (int w0 = 0; w0 < P.SW; w0 += kSelThreads) {
+            const int w = w0 + tid;
+            const unsigned word = w < P.SW ? sc[w] : 0u;
+            const unsigned pc = (unsigned)__popc(word);
+            unsigned tot;
+            const unsigned incl = block_scan_u32(pc, s_wu, &tot);
+            unsigned slot = base_cnt + incl - pc;
+            unsigned wd = word;
+            while (wd) {
+                const int b = __ffs(wd) - 1;
+                wd &= wd - 1u;
+                const unsigned q = (unsigned)w * 32u + (unsigned)b;
+                if (slot < (unsigned)Kp)
+                    s_set[slot] = ((unsigned long long)mag_key(v[q]) << 32) | (unsigned long long)(0xffffffffu - q);
+                ++slot;
+            }
+            base_cnt += tot;
         }
+    }
     __syncthreads();
     for (int size = 2; size <= Kp; size <<= 1) {         // bitonic sort, ascending
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -801,36 +847,66 @@ __device__ __forceinline__ void store_pair(const MxDev& P, int p, double h)
 }
 
 // worker shift update (FP32) and master merge (FP64), clients in order per position
+// A warp covers the 32 positions of one selection word: lane c of each batch of 32 clients loads
+// that client's word, and the clients with a selected position in the word are then visited in
+// increasing order, each lane updating its own position (the FP64 sum stays in client order).
 __global__ void k_mx_apply(MxDev P)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.U) return;
-    double h = P.H[p];
-    const unsigned bit = 1u << (p & 31);
-    for (int c = 0; c < P.nc; ++c) {
-        if (!(P.sel[(size_t)c * P.SW + (p >> 5)] & bit)) continue;
-        const size_t q = (size_t)c * P.Up + p;
-        const double item = (double)P.dsel[q] * P.mult;
-        P.shift[q] = (float)((double)P.shift[q] + P.alpha * item);
-        h += item * P.prescale;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const int word = p >> 5;                     // the same for the whole warp (blockDim % 32 == 0)
+    const bool in = p < P.U;
+    double h = in ? P.H[p] : 0.0;
+    for (int c0 = 0; c0 < P.nc; c0 += 32) {
+        const int cl = c0 + lane;
+        const unsigned wv = (cl < P.nc && word < P.SW) ? __ldg(P.sel + (size_t)cl * P.SW + word) : 0u;
+        if (!__any_sync(0xffffffffu, wv != 0u)) continue;
+        // transpose: bit t of mine = client c0 + t selected my position
+        unsigned mine = 0u;
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+            const unsigned b = __ballot_sync(0xffffffffu, (wv >> t) & 1u);
+            if (lane == t) mine = b;
+        }
+        if (!in) mine = 0u;
+        // loads of every selected client first, then the updates in client order
+        float dv[32], sv[32];
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if ((mine >> t) & 1u) {
+                const size_t q = (size_t)(c0 + t) * P.Up + p;
+                dv[t] = P.dsel[q];
+                sv[t] = P.shift[q];
+            }
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if ((mine >> t) & 1u) {
+                const size_t q = (size_t)(c0 + t) * P.Up + p;
+                const double item = (double)dv[t] * P.mult;
+                P.shift[q] = (float)((double)sv[t] + P.alpha * item);
+                h += item * P.prescale;
+            }
     }
-    P.H[p] = h;
-    store_pair(P, p, h);
+    if (in) {
+        P.H[p] = h;
+        store_pair(P, p, h);
+    }
 }
 
-// g = mean g_c, l = mean Lk
+// g = mean g_c (one warp per feature: lanes over clients, then a butterfly sum), l = mean Lk
 __global__ void k_mx_aggregate(MxDev P)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < P.d) {
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid < P.d) {
         double v = 0.0;
-        for (int c = 0; c < P.nc; ++c) v += P.gc[(size_t)c * P.d + i];
-        P.g[i] = v * P.inv_n;
+        for (int c = lane; c < P.nc; c += 32) v += P.gc[(size_t)c * P.d + wid];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) P.g[wid] = v * P.inv_n;
     }
-    if (i == 0) {
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
         double l = 0.0;
-        for (int c = 0; c < P.nc; ++c) l += P.lk[c];
-        P.stats[1] = l * P.inv_n;
+        for (int c = lane; c < P.nc; c += 32) l += P.lk[c];
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if (lane == 0) P.stats[1] = l * P.inv_n;
     }
 }
 
