@@ -260,6 +260,25 @@ int fednl_mx_get_diff(fednl_mx_handle h, int32_t client, float* diff);
 int fednl_mx_get_selection(fednl_mx_handle h, int32_t client, uint32_t* pos, int32_t* count);
 int fednl_mx_get_shift(fednl_mx_handle h, int32_t client, float* shift);
 
+/* ---- wire format of the distributed binaries -------------------------------------------------- */
+/* The bytes a u-FedNL distributed client (bin_fednl_distr_client) sends its master for one client's
+ * last round: the gradient packet, Lk (FEDNL_WIRE_LK, Option B), the Hessian message in chunks of
+ * 359 entries in the compressor's layout (TopK / TopLEK / RandK / RandSeqK: indices and scaled items;
+ * Natural: 3 bytes per pair of upper entries plus a trailing pair; Identity: all scaled items),
+ * f_i (FEDNL_WIRE_FI, tracking or line search) and the round-finished packet (FEDNL_WIRE_FINISH).
+ * Packet = signal byte, LEB128 length, payload (UsedTypes.h:1022-1125).  With out == NULL only
+ * *len is set (the size needed).  Plain FedNL handles only. */
+enum {
+    FEDNL_WIRE_LK = 1,
+    FEDNL_WIRE_FI = 2,
+    FEDNL_WIRE_FINISH = 4,
+    FEDNL_WIRE_RANDK_INDICES = 8   /* --transfer_indicies_for_randk */
+};
+int fednl_gpu_encode_client_round(fednl_handle h, int32_t client, int32_t flags, uint8_t* out, int64_t cap,
+                                  int64_t* len);
+int fednl_gpu_get_client_grad(fednl_handle h, int32_t client, double* g);     /* [d] the client's gradient */
+int fednl_gpu_get_diff(fednl_handle h, int32_t client, double* diff);         /* [U] H_c - shift_c, packed upper */
+
 /* ---- serving: a round split into its client phase and a batched solve ------------------------ */
 /* Everything of one round up to the master's aggregation, on the handle's stream (plain FedNL). */
 int fednl_gpu_client_phase(fednl_handle h);

@@ -23,6 +23,7 @@
 #include "dopt/system/include/FloatUtils.h"
 #include "dopt/optimization_problems/include/ml/dataset_loader_fs.h"
 #include "dopt/copylocal/include/Data.h"
+#include "dopt/copylocal/include/MutableData.h"
 
 #include <barrier>
 #include <cstdio>
@@ -543,6 +544,33 @@ static int cmd_chol(const char* in_path, const char* out_path)
     return 0;
 }
 
+// Packet framing of the distributed client's messages: for every record (u8 signal, u32 length,
+// payload) the bytes that WorkerContextForFedNL::prepareUpdate writes with dopt::MutableData
+// (dopt/bin_fednl_distr_client/include/UsedTypes.h:1022-1125): putByte(signal),
+// putUnsignedVaryingInteger(length), putBytes(payload).
+static int cmd_wire(const char* in_path, const char* out_path)
+{
+    FILE* fi = fopen(in_path, "rb");
+    FILE* fo = fopen(out_path, "wb");
+    if (!fi || !fo) return 1;
+    Reader R{fi};
+    int32_t n = R.get<int32_t>();
+    dopt::MutableData buf;
+    for (int32_t r = 0; r < n; ++r) {
+        uint8_t sig = (uint8_t)R.get<int32_t>();
+        uint32_t len = (uint32_t)R.get<int32_t>();
+        std::vector<uint8_t> payload(len);
+        if (len) R.get(payload.data(), len);
+        buf.putByte(sig);
+        buf.putUnsignedVaryingInteger(len);
+        if (len) buf.putBytes(payload.data(), len);
+    }
+    fwrite(buf.getPtr(), 1, buf.getFilledSize(), fo);
+    fclose(fi);
+    fclose(fo);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 3) {
@@ -556,6 +584,7 @@ int main(int argc, char** argv)
     if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
     if (!strcmp(argv[1], "toplek")) return cmd_select(argv[2], argv[3], true);
     if (!strcmp(argv[1], "chol")) return cmd_chol(argv[2], argv[3]);
+    if (!strcmp(argv[1], "wire")) return cmd_wire(argv[2], argv[3]);
     if ((!strcmp(argv[1], "randk") || !strcmp(argv[1], "randseqk")) && argc >= 7)
         return cmd_rand(argv[2], atoi(argv[3]), atoi(argv[4]), (uint32_t)strtoul(argv[5], 0, 10), atoi(argv[6]),
                         !strcmp(argv[1], "randseqk"));

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import os
+import struct
 import subprocess
 import sys
 import tempfile
@@ -257,6 +258,27 @@ def tie_matrices(rng, d, count, levels):
     return mats
 
 
+def wire_case(name, rng):
+    """The distributed client's packet framing (UsedTypes.h:1022-1125) through the reference's
+    own dopt::MutableData: signal byte, LEB128 length, payload."""
+    if _skip("wire"):
+        return
+    sizes = [0, 1, 8, 127, 128, 129, 2408 * 8, 16383, 16384, 300000, 2097152]
+    sigs = [41 + (t % 9) for t in range(len(sizes))]
+    payloads = [rng.integers(0, 256, n, dtype=np.uint8) if n <= 20000 else np.zeros(n, dtype=np.uint8) for n in sizes]
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(struct.pack("<i", len(sizes)))
+            for sg, pl in zip(sigs, payloads):
+                f.write(struct.pack("<ii", sg, len(pl)))
+                f.write(pl.tobytes())
+        subprocess.run([HARNESS, "wire", fin, fout], check=True)
+        framed = np.frombuffer(open(fout, "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, f"wire_{name}.npz"), sigs=np.array(sigs, dtype=np.int32),
+                        sizes=np.array(sizes, dtype=np.int64), payload=np.concatenate(payloads), framed=framed)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", default=os.environ.get("REF_ROOT", "/root/reference/dopt"))
@@ -267,6 +289,7 @@ def main():
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_ROOT={args.ref_root}"],
                    check=True)
     rng = np.random.default_rng(20241203)
+    wire_case("frames", np.random.default_rng(7))
 
     # whole runs: uneven clients, LDA padding (d=13 -> LDA 16), every compressor
     small = datagen.binary_problem(11, 13, [20, 31, 17, 25, 40], 0.3, 1e-3)

@@ -268,3 +268,18 @@ def test_topk_structure(oracle):
         true = np.sort(up[np.argsort(-np.abs(m[up]), kind="stable")[:min(k, U)]])
         not_exact += int(not np.array_equal(got, true))
     assert not_exact >= 1
+
+
+def test_wire_framing_matches_reference():
+    """The distributed client's packet framing restated in oracle/pywire.py equals the bytes the
+    reference's own dopt::MutableData writes (LEB128 lengths of 1 to 4 bytes, empty payloads)."""
+    from oracle import pywire
+    z = np.load(golden_path("wire_frames.npz"))
+    out = bytearray()
+    off = 0
+    for sg, n in zip(z["sigs"], z["sizes"]):
+        out += pywire.frame(int(sg), z["payload"][off:off + int(n)].tobytes())
+        off += int(n)
+    assert bytes(out) == z["framed"].tobytes()
+    recs = pywire.decode(bytes(out))
+    assert [r[0] for r in recs] == list(z["sigs"]) and [len(r[1]) for r in recs] == list(z["sizes"])

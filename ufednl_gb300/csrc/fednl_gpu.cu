@@ -1104,6 +1104,167 @@ int fednl_gpu_get_message(fednl_handle h, int32_t client, uint32_t* idx, double*
     return FEDNL_OK;
 }
 
+// ---- wire format of the distributed client ---------------------------------------------------
+// The bytes bin_fednl_distr_client sends its master for one client's round: each packet is a
+// signal byte, the payload length as unsigned LEB128 and the payload
+// (dopt/bin_fednl_distr_client/include/UsedTypes.h:1022-1125 with dopt::MutableData,
+// dopt/copylocal/include/MutableData.h:488-536); Hessian messages in chunks of
+// (1500 - 40 - 20 - 1 - 2) / 4 = 359 entries (LocalWorkerForFedNL_TopK.h:20-35).
+
+namespace {
+
+struct WireBuf {
+    std::vector<uint8_t> b;
+    void frame(uint8_t sig, const void* p, size_t n)
+    {
+        b.push_back(sig);
+        uint64_t v = n;
+        for (;;) {
+            const uint8_t low = (uint8_t)(v & 0x7F);
+            v >>= 7;
+            if (!v) {
+                b.push_back(low);
+                break;
+            }
+            b.push_back((uint8_t)(low | 0x80));
+        }
+        const uint8_t* q = (const uint8_t*)p;
+        b.insert(b.end(), q, q + n);
+    }
+};
+
+constexpr int kWireChunk = (1500 - 40 - 20 - 1 - 2) / 4;
+
+uint32_t natural_pack24(double a, double b)      // pack2FP64NoMantissa, FloatUtils.h:193-221
+{
+    uint64_t ba, bb;
+    memcpy(&ba, &a, 8);
+    memcpy(&bb, &b, 8);
+    return ((uint32_t)(ba >> 63) << 23) | ((uint32_t)((ba >> 52) & 0x7FF) << 12) | ((uint32_t)(bb >> 63) << 11) |
+           (uint32_t)((bb >> 52) & 0x7FF);
+}
+
+}  // namespace
+
+int fednl_gpu_encode_client_round(fednl_handle h, int32_t client, int32_t flags, uint8_t* out, int64_t cap,
+                                  int64_t* len)
+{
+    if (!h || client < 0 || client >= h->nc || !len || (flags & ~15)) return fail(FEDNL_EINVAL, "bad argument");
+    if (h->pp) return fail(FEDNL_EINVAL, "FedNL-PP clients use another protocol");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    const int comp = h->comp;
+    if (comp == FEDNL_RANDK_PHILOX && !(flags & FEDNL_WIRE_RANDK_INDICES))
+        return fail(FEDNL_EINVAL, "a reference master cannot re-derive RandK-Philox positions: send the indices");
+    if ((flags & FEDNL_WIRE_FI) && !h->dev.fmode) return fail(FEDNL_EINVAL, "f_i is formed only with track_f or line_search");
+    CK(cudaStreamSynchronize(h->stream));
+    const Dev& P = h->dev;
+    const int d = h->d, U = h->U;
+    WireBuf W;
+    std::vector<double> g(d);
+    CK(cudaMemcpy(g.data(), P.gc + (size_t)client * d, (size_t)d * 8, cudaMemcpyDeviceToHost));
+    W.frame(41, g.data(), (size_t)d * 8);                               // sig_messageGradient
+    if (flags & FEDNL_WIRE_LK) {
+        double lk = 0.0;
+        CK(cudaMemcpy(&lk, P.lk + client, 8, cudaMemcpyDeviceToHost));
+        W.frame(47, &lk, 8);                                             // sig_messageToSendLk
+    }
+    std::vector<double> dv(U);
+    CK(cudaMemcpy(dv.data(), P.diff + (size_t)client * h->ustr, (size_t)U * 8, cudaMemcpyDeviceToHost));
+    if (comp == FEDNL_NATURAL) {                                         // LocalWorkerForFedNL_Natural.h:143-201
+        double packs[2] = {0.0, 0.0};
+        int filled = 0, count = 0;
+        std::vector<uint8_t> chunk;
+        for (int p = 0; p < U; ++p) {
+            packs[filled++] = dv[p];
+            if (filled == 2) {
+                const uint32_t w = natural_pack24(packs[0], packs[1]);
+                chunk.push_back((uint8_t)w);
+                chunk.push_back((uint8_t)(w >> 8));
+                chunk.push_back((uint8_t)(w >> 16));
+                count += 2;
+                filled = 0;
+            }
+            if (count == kWireChunk || count == kWireChunk - 1) {
+                W.frame(42, nullptr, 0);
+                W.frame(44, chunk.data(), chunk.size());
+                chunk.clear();
+                count = 0;
+            }
+        }
+        const uint32_t w = natural_pack24(packs[0], packs[1]);          // the trailing pair
+        chunk.push_back((uint8_t)w);
+        chunk.push_back((uint8_t)(w >> 8));
+        chunk.push_back((uint8_t)(w >> 16));
+        W.frame(43, nullptr, 0);
+        W.frame(45, chunk.data(), chunk.size());
+    } else if (comp == FEDNL_IDENTITY) {                                 // LocalWorkerForFedNL_Identical.h:138-167
+        std::vector<double> chunk;
+        for (int p = 0; p < U; ++p) {
+            chunk.push_back(dv[p] * P.prescale);
+            if ((int)chunk.size() == kWireChunk) {
+                W.frame(42, nullptr, 0);
+                W.frame(44, chunk.data(), chunk.size() * 8);
+                chunk.clear();
+            }
+        }
+        W.frame(43, nullptr, 0);
+        W.frame(45, chunk.data(), chunk.size() * 8);
+    } else {                                                             // TopK.h:147-189, RandK.h:171-219, RandSeqK.h:172-236
+        int32_t n = 0;
+        int rc = fednl_gpu_get_message(h, client, nullptr, nullptr, &n);
+        if (rc) return rc;
+        std::vector<uint32_t> idx((size_t)std::max(n, 1));
+        rc = fednl_gpu_get_message(h, client, idx.data(), nullptr, &n);
+        if (rc) return rc;
+        const bool rk = comp == FEDNL_RANDK || comp == FEDNL_RANDSEQK || comp == FEDNL_RANDK_PHILOX;
+        const double scale = rk ? P.prescale * ((double)U / (double)h->k) : P.prescale;
+        const bool send_idx = !rk || (flags & FEDNL_WIRE_RANDK_INDICES);
+        std::vector<double> items;
+        for (int k = 0;;) {
+            const bool last = !(k + kWireChunk < n);
+            const int end = last ? n : k + kWireChunk;
+            W.frame(last ? 43 : 42, send_idx ? (const void*)(idx.data() + k) : nullptr,
+                    send_idx ? (size_t)(end - k) * 4 : 0);
+            items.clear();
+            for (int t = k; t < end; ++t) {
+                const uint32_t j = idx[t] / (uint32_t)h->lda, i = idx[t] - j * (uint32_t)h->lda;
+                items.push_back(dv[(size_t)j * (j + 1) / 2 + i] * scale);
+            }
+            W.frame(last ? 45 : 44, items.data(), items.size() * 8);
+            k = end;
+            if (last) break;
+        }
+    }
+    if (flags & FEDNL_WIRE_FI) {
+        double fi = 0.0;
+        CK(cudaMemcpy(&fi, P.fi + client, 8, cudaMemcpyDeviceToHost));
+        W.frame(48, &fi, 8);                                             // sig_messageToSendFi
+    }
+    if (flags & FEDNL_WIRE_FINISH) W.frame(49, nullptr, 0);              // sig_messageToSendRoundWorkHasBeenFinished
+    *len = (int64_t)W.b.size();
+    if (!out) return FEDNL_OK;
+    if (cap < (int64_t)W.b.size()) return fail(FEDNL_EINVAL, "output buffer of %lld bytes, %zu needed", (long long)cap,
+                                               W.b.size());
+    memcpy(out, W.b.data(), W.b.size());
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_client_grad(fednl_handle h, int32_t client, double* g)
+{
+    if (!h || client < 0 || client >= h->nc || !g) return fail(FEDNL_EINVAL, "bad argument");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(g, h->dev.gc + (size_t)client * h->d, (size_t)h->d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_get_diff(fednl_handle h, int32_t client, double* diff)
+{
+    if (!h || client < 0 || client >= h->nc || !diff) return fail(FEDNL_EINVAL, "bad argument");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(diff, h->dev.diff + (size_t)client * h->ustr, (size_t)h->U * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
 // ---- operator-level entry points -------------------------------------------------------------
 
 namespace {

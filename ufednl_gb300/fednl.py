@@ -65,7 +65,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed",
-           "fednl_mx_set_solver"]
+           "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff"]
 
 _lib = None
 
@@ -138,7 +138,10 @@ def load(build_if_missing: bool = True):
                        "fednl_mx_round_result": [vp, C.POINTER(RoundStats)],
                        "fednl_gpu_mem_info": [C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
                        "fednl_mx_get_diff": [vp, C.c_int32, fp], "fednl_mx_get_shift": [vp, C.c_int32, fp],
-                       "fednl_mx_get_selection": [vp, C.c_int32, up, ip], "fednl_mx_set_solver": [vp, C.c_int32]}.items():
+                       "fednl_mx_get_selection": [vp, C.c_int32, up, ip], "fednl_mx_set_solver": [vp, C.c_int32],
+                       "fednl_gpu_encode_client_round": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int64,
+                                                         C.POINTER(C.c_int64)],
+                       "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -389,6 +392,26 @@ class FedNL:
         dr, dd = np.empty(self.d), np.empty(self.d)
         _check(load().fednl_gpu_get_dir(self._h, c, _dp(dr), _dp(dd)))
         return dr, dd
+
+    def encode_round(self, c: int, flags: int) -> bytes:
+        """The bytes bin_fednl_distr_client sends its master for client c's last round."""
+        n = C.c_int64(0)
+        _check(load().fednl_gpu_encode_client_round(self._h, c, flags, None, 0, C.byref(n)))
+        buf = (C.c_uint8 * max(1, n.value))()
+        _check(load().fednl_gpu_encode_client_round(self._h, c, flags, buf, n.value, C.byref(n)))
+        return bytes(buf)[: n.value]
+
+    def client_grad(self, c: int) -> np.ndarray:
+        out = np.empty(self.d)
+        _check(load().fednl_gpu_get_client_grad(self._h, c, _dp(out)))
+        return out
+
+    def diff(self, c: int) -> np.ndarray:
+        """H_c - shift_c of the last round, packed upper (j (j + 1) / 2 + i)."""
+        U = self.d * (self.d + 1) // 2
+        out = np.empty(U)
+        _check(load().fednl_gpu_get_diff(self._h, c, _dp(out)))
+        return out
 
     def message(self, c: int):
         U = self.d * (self.d + 1) // 2
