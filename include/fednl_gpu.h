@@ -290,6 +290,15 @@ int fednl_gpu_solve_batch(fednl_handle* handles, int32_t n, fednl_mx_handle* mix
 /* waits for the handle's last round and reports it as fednl_gpu_round does */
 int fednl_gpu_round_result(fednl_handle h, fednl_round_stats* stats);
 int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats);
+/* ---- autotuning ------------------------------------------------------------------------------ */
+/* Measures the launch shapes of the round's Newton solve on the handle's current system (scratch
+ * outputs: the run's state does not change) and keeps the fastest; results are cached per d for the
+ * process.  FP64 handles: the cooperative Cholesky's CTA count (results are identical for every
+ * count).  Mixed handles: that count and the solver (FP64 cooperative or, d up to about 300, the FP32
+ * shared-memory factor with refinement). */
+int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid, double* solve_ms);
+int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver, int32_t* chol_grid, double* solve_ms);
+
 /* free and total device memory (admission by free memory) */
 int fednl_gpu_mem_info(int64_t* free_bytes, int64_t* total_bytes);
 /* device bytes a handle of this desc holds: its state plus (FP64) a dense bound on the client data

@@ -16,6 +16,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -214,7 +217,7 @@ int fednl_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 // work: (d+1)(d+2)/2 doubles, ybuf and rinv: d doubles, bar: 4 x u32 (zero), status: 1 int.
 int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const double* g, double* dx, double* xupd,
                                double* work, double* ybuf, double* rinv, unsigned* bar, int* status, double* stats,
-                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st)
+                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st, int grid)
 {
     Dev P{};
     P.d = d;
@@ -228,12 +231,74 @@ int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const
     P.hist = hist;
     P.round_ctr = round_ctr;
     P.hist_cap = hist_cap;
-    static int grid_cache_d = -1, grid_cache = 1;
-    if (grid_cache_d != d) {
-        grid_cache = chol_grid(d);
-        grid_cache_d = d;
+    if (grid <= 0) {
+        static int grid_cache_d = -1, grid_cache = 1;
+        if (grid_cache_d != d) {
+            grid_cache = chol_grid(d);
+            grid_cache_d = d;
+        }
+        grid = grid_cache;
     }
-    CK(launch_chol(P, grid_cache, st, H, 0, lptr, 0.0, g, dx, xupd, record));
+    CK(launch_chol(P, grid, st, H, 0, lptr, 0.0, g, dx, xupd, record));
+    return FEDNL_OK;
+}
+
+// ---- autotuning of the solve's launch shape ----------------------------------------------------
+// The cooperative Cholesky's CTA count is measured per dimension on the caller's own system (the
+// handle's current H, l and g into scratch outputs: nothing of the run changes) and cached
+// process-wide, so later handles of the same d reuse the choice.
+int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid, double* best_ms)
+{
+    static std::mutex mu;
+    static std::map<int, std::pair<int, double>> cache;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(d);
+        if (it != cache.end()) {
+            *best_grid = it->second.first;
+            *best_ms = it->second.second;
+            return FEDNL_OK;
+        }
+    }
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_coop, kCoopThreads, 0);
+    const int cap = std::min(sms, sms * std::max(1, bps));
+    std::vector<int> cand = {8, 16, 32, 48, 64, 96, 128, cap, chol_grid(d)};
+    std::sort(cand.begin(), cand.end());
+    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int bg = chol_grid(d);
+    double bm = 1e30;
+    for (int G : cand) {
+        if (G < 1 || G > cap) continue;
+        int rc = launch(G);                                   // warm
+        if (rc) return rc;
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            CK(cudaEventRecord(e0, st));
+            rc = launch(G);
+            if (rc) return rc;
+            CK(cudaEventRecord(e1, st));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = std::min(best, ms);
+        }
+        if (best < bm) {
+            bm = best;
+            bg = G;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> g(mu);
+    cache[d] = {bg, bm};
+    *best_grid = bg;
+    *best_ms = bm;
     return FEDNL_OK;
 }
 
@@ -968,6 +1033,44 @@ int fednl_gpu_solve_batch(fednl_handle* hs, int32_t n, fednl_mx_handle* mxs, int
     rc = fednl_mx_solve32_batch(small.data(), (int)small.size(), bst);
     if (rc) return rc;
     for (int i = 0; i < n; ++i) hs[i]->rounds_done += 1;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid_out, double* solve_ms)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    CK(cudaStreamSynchronize(h->stream));
+    Dev Q = h->dev;                        // scratch view: no statistics, no line-search state
+    Q.ls = nullptr;
+    double* scratch = nullptr;
+    int* sstatus = nullptr;
+    CK(cudaMalloc(&scratch, (size_t)h->d * 8));
+    CK(cudaMalloc(&sstatus, 4));
+    Q.status = sstatus;
+    const double* lptr = h->desc.option_a ? nullptr : h->dev.stats + 1;
+    const double lval = h->dev.lambda;
+    auto launch = [&](int G) -> int {
+        cudaError_t e = launch_chol(Q, G, h->stream, Q.H, 0, lptr, lval, Q.g, scratch, nullptr, 0);
+        return e == cudaSuccess ? FEDNL_OK : fail(FEDNL_ECUDA, "tuning launch failed: %s", cudaGetErrorString(e));
+    };
+    int grid = h->chol_grid;
+    double ms = 0.0;
+    int rc = fednl_tune_chol_grid(h->d, launch, h->stream, &grid, &ms);
+    cudaFree(scratch);
+    cudaFree(sstatus);
+    if (rc) return rc;
+    if (grid != h->chol_grid) {
+        h->chol_grid = grid;
+        if (h->gexec) {                    // the captured round holds the old launch shape
+            cudaGraphExecDestroy(h->gexec);
+            cudaGraphDestroy(h->graph);
+            h->gexec = nullptr;
+            h->graph = nullptr;
+        }
+    }
+    if (chol_grid_out) *chol_grid_out = grid;
+    if (solve_ms) *solve_ms = ms;
     return FEDNL_OK;
 }
 

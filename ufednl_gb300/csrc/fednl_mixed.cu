@@ -17,6 +17,8 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -195,7 +197,7 @@ extern "C" int fednl_gpu_weighted_gram_tf32(const float* features, const float* 
 
 int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const double* g, double* dx, double* xupd,
                                double* work, double* ybuf, double* rinv, unsigned* bar, int* status, double* stats,
-                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st);
+                               double* hist, int* round_ctr, int hist_cap, int record, cudaStream_t st, int grid);
 
 struct fednl_mx_handle_s {
     fednl_problem_desc desc{};
@@ -217,6 +219,7 @@ struct fednl_mx_handle_s {
     size_t select_smem = 0;
     bool chol32 = false;               // the round solves with the FP32 factor + refinement
     bool chol32_ok = false;            // the system fits one CTA's shared memory
+    int coop_grid = 0;                 // CTAs of the FP64 cooperative solve (0: the default heuristic)
     fednl_c32::Job* cjob = nullptr;    // device copy of the solve's job
     void* flush_buf = nullptr;
     int64_t flush_bytes = 0;
@@ -294,7 +297,7 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
         return FEDNL_OK;
     }
     int rc = fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, h->dx, P.x, h->work, h->ybuf, h->rinv, h->bar,
-                                        h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st);
+                                        h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st, h->coop_grid);
     mark();
     return rc;
 }
@@ -668,6 +671,109 @@ int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver)
         h->graph = nullptr;
     }
     h->chol32 = want;
+    return FEDNL_OK;
+}
+
+int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver_out, int32_t* grid_out, double* solve_ms)
+{
+    if (!h || !h->ready) return fail_m(FEDNL_EINVAL, "call fednl_mx_init_shifts first");
+    static std::mutex mu;
+    static std::map<int, std::pair<int, int>> cache;       // d -> (solver, CTAs)
+    static std::map<int, double> cache_ms;
+    CKM(cudaStreamSynchronize(h->stream));
+    int solver = 0, grid = 0;
+    double best = 0.0;
+    bool cached = false;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(h->d);
+        if (it != cache.end()) {
+            solver = it->second.first;
+            grid = it->second.second;
+            best = cache_ms[h->d];
+            cached = true;
+        }
+    }
+    if (!cached) {
+        // scratch outputs: the handle's iterate, statistics and history stay as they are
+        double *sdx = nullptr, *sstats = nullptr, *shist = nullptr;
+        int *sstatus = nullptr, *sctr = nullptr;
+        fednl_c32::Job* sjob = nullptr;
+        if (cudaMalloc(&sdx, (size_t)h->d * 8) || cudaMalloc(&sstats, 32) || cudaMalloc(&shist, 8) ||
+            cudaMalloc(&sstatus, 4) || cudaMalloc(&sctr, 4) || cudaMalloc(&sjob, sizeof(fednl_c32::Job))) {
+            cudaFree(sdx);
+            cudaFree(sstats);
+            cudaFree(shist);
+            cudaFree(sstatus);
+            cudaFree(sctr);
+            return fail_m(FEDNL_ENOMEM, "tuning scratch allocation failed");
+        }
+        cudaMemset(sctr, 0, 4);
+        const fednl_tc::MxDev& P = h->P;
+        cudaStream_t st = h->stream;
+        auto launch = [&](int G) -> int {
+            return fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, sdx, nullptr, h->work, h->ybuf, h->rinv,
+                                              h->bar, sstatus, sstats, shist, sctr, 1, 0, st, G);
+        };
+        double coop_ms = 0.0;
+        int rc = fednl_tune_chol_grid(h->d, launch, st, &grid, &coop_ms);
+        solver = 0;
+        best = coop_ms;
+        if (!rc && h->chol32_ok) {
+            fednl_c32::Job J{};
+            cudaMemcpy(&J, h->cjob, sizeof(J), cudaMemcpyDeviceToHost);
+            J.dx = sdx;
+            J.x = nullptr;
+            J.stats = sstats;
+            J.hist = shist;
+            J.round_ctr = sctr;
+            J.hist_cap = 1;
+            J.status = sstatus;
+            cudaMemcpy(sjob, &J, sizeof(J), cudaMemcpyHostToDevice);
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            float b32 = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {
+                cudaEventRecord(e0, st);
+                fednl_c32::k_chol32<<<1, fednl_c32::kT, fednl_c32::smem_bytes(h->d), st>>>(sjob);
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep) b32 = std::min(b32, ms);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (cudaGetLastError() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "tuning launch failed");
+            else if (b32 < coop_ms) {
+                solver = 1;
+                best = b32;
+            }
+        }
+        cudaFree(sdx);
+        cudaFree(sstats);
+        cudaFree(shist);
+        cudaFree(sstatus);
+        cudaFree(sctr);
+        cudaFree(sjob);
+        if (rc) return rc;
+        std::lock_guard<std::mutex> g(mu);
+        cache[h->d] = {solver, grid};
+        cache_ms[h->d] = best;
+    }
+    if (grid != h->coop_grid && h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
+    }
+    h->coop_grid = grid;
+    int rc = fednl_mx_set_solver(h, solver);
+    if (rc) return rc;
+    if (solver_out) *solver_out = solver;
+    if (grid_out) *grid_out = grid;
+    if (solve_ms) *solve_ms = best;
     return FEDNL_OK;
 }
 

@@ -3,6 +3,10 @@
 // of many live problems (the serving loop's batched solve).
 #pragma once
 
+#include <cuda_runtime.h>
+
+#include <functional>
+
 struct FednlSolveDesc {
     const double* H;       // packed upper FP64, d(d+1)/2
     int d;
@@ -26,6 +30,10 @@ struct FednlSolveDesc {
 
 // fednl_gpu.cu
 int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream);
+// the cooperative Cholesky's CTA count for dimension d, measured with launch(G) on the caller's
+// stream and cached per d for the process
+int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid,
+                         double* best_ms);
 
 // fednl_mixed.cu: a mixed-precision handle's solve as a descriptor (and its stream)
 struct fednl_mx_handle_s;

@@ -65,7 +65,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed",
-           "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff"]
+           "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
+           "fednl_gpu_autotune", "fednl_mx_autotune"]
 
 _lib = None
 
@@ -141,7 +142,8 @@ def load(build_if_missing: bool = True):
                        "fednl_mx_get_selection": [vp, C.c_int32, up, ip], "fednl_mx_set_solver": [vp, C.c_int32],
                        "fednl_gpu_encode_client_round": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int64,
                                                          C.POINTER(C.c_int64)],
-                       "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp]}.items():
+                       "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp],
+                       "fednl_gpu_autotune": [vp, ip, dp], "fednl_mx_autotune": [vp, ip, ip, dp]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -312,6 +314,13 @@ class FedNL:
         out = np.empty(rounds)
         _check(load().fednl_gpu_run(self._h, rounds, _dp(out)))
         return out
+
+    def autotune(self) -> dict:
+        """Measures the solve's CTA count on this problem and keeps the fastest (same results)."""
+        g = np.zeros(1, dtype=np.int32)
+        ms = np.zeros(1)
+        _check(load().fednl_gpu_autotune(self._h, _ip(g), _dp(ms)))
+        return {"chol_ctas": int(g[0]), "solve_ms": float(ms[0])}
 
     def client_phase(self):
         """Launches the round up to the master's aggregation (no wait); solve_batch ends it."""
@@ -507,6 +516,15 @@ class MixedFedNL:
         out = np.empty(rounds)
         _check(load().fednl_mx_run(self._h, rounds, _dp(out)))
         return out
+
+    def autotune(self) -> dict:
+        """Measures the solve (FP64 cooperative CTA count; FP32 shared-memory solver where it fits)
+        on this problem's current system and keeps the fastest."""
+        sv = np.zeros(1, dtype=np.int32)
+        g = np.zeros(1, dtype=np.int32)
+        ms = np.zeros(1)
+        _check(load().fednl_mx_autotune(self._h, _ip(sv), _ip(g), _dp(ms)))
+        return {"solver": ["fp64", "fp32_refined"][int(sv[0])], "chol_ctas": int(g[0]), "solve_ms": float(ms[0])}
 
     def client_phase(self):
         _check(load().fednl_mx_client_phase(self._h))
