@@ -322,7 +322,22 @@ def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, f
     prof = mx.profile_kernels(10)
     mx.close()
     rps = n / (tot / 1000.0)
+    # round-level bound: the slower of the tensor-core work (the padded client Gram matrices' upper
+    # tiles in TF32) and the FP32 shift stream (read, difference written, shift written back)
+    hbm, bf16, src = peaks()
+    dp = (prob.d + 127) // 128 * 128
+    tiles = (dp // 128) * (dp // 128 + 1) // 2
+    gram_flops = 2.0 * prob.total_samples * 128 * 128 * tiles
+    U = prob.d * (prob.d + 1) // 2
+    shift_bytes = 3.0 * prob.n_clients * U * 4
+    t_tensor = gram_flops / (bf16 / 2.0 * 1e12) * 1e3
+    t_hbm = shift_bytes / (hbm * 1e9) * 1e3
+    bound_ms = max(t_tensor, t_hbm)
     return {"rounds_per_s": rps, "round_ms_p50": float(np.percentile(per, 50)),
+            "round_roofline": {"bound": "tensor" if t_tensor >= t_hbm else "hbm", "gram_tf32_flops": gram_flops,
+                               "shift_stream_bytes": shift_bytes, "lower_bound_ms": bound_ms,
+                               "round_ms": tot / n, "frac": bound_ms / (tot / n),
+                               "peaks": f"{src}: tf32 = bf16_tflops / 2, hbm_gbs"},
             "round_ms_p99": float(np.percentile(per, 99)), "rounds_timed": n, "kernels_ms": dict(prof),
             "gpu_launches_per_round": len(prof),
             "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
