@@ -467,10 +467,12 @@ def run_ours(args, ws, rank, local, td):
             "roofline": roof, "round_roofline": round_roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
             "autotuned": tuned,
             "clocks": clocks, "e2e": e2e}
-    if ws == 1 and rank == 0 and not args.no_extra:
+    if ws == 1 and rank == 0:
         line["mixed_precision"] = mixed_headline(fednl, prob, comp, k, args.steps, value,
                                                  tol_ms / 1000.0 if tol_ms is not None else None)
-        line["serving"] = serving_workload(fednl)
+        if not args.no_serving:
+            line["serving"] = serving_workload(fednl)
+    if ws == 1 and rank == 0 and not args.no_extra:
         line["extra_workloads"] = extra_workloads(fednl, os.cpu_count() or 1, args.steps)
         line["extra_workloads"]["dense FP32 d1024 256x(512-4096) RandK-Philox k=4d, mixed precision"] = \
             mixed_workload(fednl, os.cpu_count() or 1, bf16 / 2.0, src)
@@ -493,6 +495,7 @@ def main():
     ap.add_argument("--workload", choices=["w8a", "a9a"], default="w8a")
     ap.add_argument("--workers", type=int, default=0, help="reference --workers (TopLEK streams); 0 = host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-extra", action="store_true", help="skip the a9a-like and FedNL-PP side measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

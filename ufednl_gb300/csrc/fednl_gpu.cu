@@ -416,7 +416,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         CKL();
     }
     MARK("k_apply");
-    k_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
+    k_apply<<<(h->U + 127) / 128, 128, 0, st>>>(P);
     CKL();
     if (h->pp) {
         MARK("k_pp_lkpart");
@@ -434,7 +434,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         return FEDNL_OK;
     }
     MARK("k_aggregate");
-    k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads, kAggThreads, 0, st>>>(P);
+    k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads + 1, kAggThreads, 0, st>>>(P);   // + the block for l
     CKL();
     if (P.fmode) {       // f(x_k) from the round's sigmoid values
         MARK("k_fclient");

@@ -1146,60 +1146,82 @@ __global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq,
 // whole symmetric difference).  Master: H[idx] += item * preScale in client order
 // (TrainLoop.h:1126-1276 with forcesequpdate).  One thread per upper position, looping over the
 // clients in order, so H receives exactly the reference's sequence of additions.
-__global__ void k_apply(Dev P)
+__global__ void __launch_bounds__(128) k_apply(Dev P)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.U) return;
-    double h = P.H[p];
+    // A warp covers the 32 positions of one selection word.  Per batch of 32 clients, lane t loads
+    // client t's word; 32 shuffles turn the words into each position's mask of selecting clients,
+    // the loads of all of them are issued together, and the FP64 updates follow in client order (the same operations as one position at a time; a warp no longer walks every client that
+    // any of its lanes selected with a load in each step).
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const bool in = p < P.U;
+    const int word = p >> 5;                      // the same for the whole warp (blockDim % 32 == 0)
     const bool all = (P.comp == 0 || P.comp == 5);
-    const unsigned bit = 1u << (p & 31);
-    for (int c0 = 0; c0 < P.n_act; c0 += 16) {
-        unsigned wd[16];
-        int cl[16];
+    double h = in ? P.H[p] : 0.0;
+    for (int c0 = 0; c0 < P.n_act; c0 += 32) {
+        const bool has = c0 + lane < P.n_act;
+        const int cl = has ? (P.act ? P.act[c0 + lane] : c0 + lane) : 0;
+        const unsigned wv = has ? (all ? 0xffffffffu : P.sel[(size_t)cl * P.SW + word]) : 0u;
+        unsigned mine = 0u;                       // bit t: client c0 + t selected my position
 #pragma unroll
-        for (int t = 0; t < 16; ++t) {
-            cl[t] = (c0 + t < P.n_act) ? (P.act ? P.act[c0 + t] : c0 + t) : 0;
-            wd[t] = (c0 + t < P.n_act) ? (all ? bit : P.sel[(size_t)cl[t] * P.SW + (p >> 5)]) : 0u;
+        for (int t = 0; t < 32; ++t) {
+            const unsigned w = __shfl_sync(0xffffffffu, wv, t);
+            mine |= ((w >> lane) & 1u) << t;
         }
-        for (int t = 0; t < 16; ++t) {
-            if (!(wd[t] & bit)) continue;
-            const size_t q = (size_t)cl[t] * P.ustr + p;
-            const double dv = P.diff[q];
-            double item, sent;
-            if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
-                item = natural_trunc(dv);
-                sent = __dmul_rn(P.prescale, item);
-            } else {
-                item = (P.comp == 1 || P.comp == 3 || P.comp == 6) ? __dmul_rn(dv, P.mult) : dv;
-                sent = __dmul_rn(item, P.prescale);
-            }
-            P.shift[q] = __dadd_rn(P.shift[q], __dmul_rn(P.alpha, item));
-            h = __dadd_rn(h, sent);
+        if (!in) mine = 0u;
+        if (!__any_sync(0xffffffffu, mine != 0u)) continue;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            int cls[16];
+#pragma unroll
+            for (int t = 0; t < 16; ++t) cls[t] = __shfl_sync(0xffffffffu, cl, half * 16 + t);
+            double dv[16], sv[16];
+#pragma unroll
+            for (int t = 0; t < 16; ++t)
+                if ((mine >> (half * 16 + t)) & 1u) {
+                    const size_t q = (size_t)cls[t] * P.ustr + p;
+                    dv[t] = P.diff[q];
+                    sv[t] = P.shift[q];
+                }
+#pragma unroll
+            for (int t = 0; t < 16; ++t)
+                if ((mine >> (half * 16 + t)) & 1u) {
+                    const size_t q = (size_t)cls[t] * P.ustr + p;
+                    double item, sent;
+                    if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
+                        item = natural_trunc(dv[t]);
+                        sent = __dmul_rn(P.prescale, item);
+                    } else {
+                        item = (P.comp == 1 || P.comp == 3 || P.comp == 6) ? __dmul_rn(dv[t], P.mult) : dv[t];
+                        sent = __dmul_rn(item, P.prescale);
+                    }
+                    P.shift[q] = __dadd_rn(sv[t], __dmul_rn(P.alpha, item));
+                    h = __dadd_rn(h, sent);
+                }
         }
     }
-    P.H[p] = h;
+    if (in) P.H[p] = h;
 }
 
 // ---- 7. master: g = (1/n) sum_c g_c, l = (1/n) sum_c Lk_c (TrainLoop.h:1100-1333) ------------
 // One thread per coordinate (32-thread blocks spread over SMs); clients added in order, loads
-// issued in batches ahead of the dependent additions.  Block 0's first warp forms l.
+// issued in batches of 32 ahead of the dependent additions.  The last block forms l.
 constexpr int kAggThreads = 32;
 __global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < P.d) {
         double g = 0.0;
-        for (int c0 = 0; c0 < P.nc; c0 += 8) {
-            double v[8];
+        for (int c0 = 0; c0 < P.nc; c0 += 32) {
+            double v[32];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) v[t] = (c0 + t < P.nc) ? P.gc[(size_t)(c0 + t) * P.d + j] : 0.0;
+            for (int t = 0; t < 32; ++t) v[t] = (c0 + t < P.nc) ? P.gc[(size_t)(c0 + t) * P.d + j] : 0.0;
 #pragma unroll
-            for (int t = 0; t < 8; ++t)
+            for (int t = 0; t < 32; ++t)
                 if (c0 + t < P.nc) g = __dadd_rn(g, v[t]);
         }
         P.g[j] = __dmul_rn(g, P.inv_n);
     }
-    if (blockIdx.x == 0) {
+    if (blockIdx.x == gridDim.x - 1) {     // l on a block of its own, the last
         const int lane = threadIdx.x & 31;
         double l = 0.0;
         for (int c0 = 0; c0 < P.nc; c0 += 32) {
