@@ -361,7 +361,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     CKL();
     MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
-    dim3 gg((h->d + 127) / 128, h->nc);
+    dim3 gg(h->binary ? (2 * h->d + 127) / 128 : (h->d + 127) / 128, h->nc);   // binary: a lane pair per attribute
     if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, st>>>(P);
     else k_grad_dense<<<gg, 128, 0, st>>>(P);
     CKL();
@@ -820,7 +820,7 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
     else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     CKL();
     if (h->binary) {    // gradient pass also forms the diagonal sums the Hessian kernel reuses
-        k_grad_binary<<<dim3((h->d + 127) / 128, h->nc), 128, (size_t)h->maxn * 16, st>>>(P);
+        k_grad_binary<<<dim3((2 * h->d + 127) / 128, h->nc), 128, (size_t)h->maxn * 16, st>>>(P);
         CKL();
     }
     dim3 hg(h->nfpart, h->nc);
@@ -1583,9 +1583,8 @@ int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_
     if (!rc) rc = fednl_gpu_init_shifts(h, x);      // shift_0 = H(x)
     if (!rc && grad) {
         Dev& P = h->dev;
-        dim3 gg((d + 127) / 128, 1);
-        if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, h->stream>>>(P);
-        else k_grad_dense<<<gg, 128, 0, h->stream>>>(P);
+        if (h->binary) k_grad_binary<<<dim3((2 * d + 127) / 128, 1), 128, (size_t)h->maxn * 16, h->stream>>>(P);
+        else k_grad_dense<<<dim3((d + 127) / 128, 1), 128, 0, h->stream>>>(P);
         cudaError_t e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) rc = fail(FEDNL_ECUDA, "gradient kernel failed: %s", cudaGetErrorString(e));
         else if (cudaMemcpy(grad, P.gc, d * 8, cudaMemcpyDeviceToHost) != cudaSuccess) rc = fail(FEDNL_ECUDA, "copy failed");

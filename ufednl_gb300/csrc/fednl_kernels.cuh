@@ -344,22 +344,24 @@ __global__ void k_grad_binary(Dev P)
         s_w[n + t] = P.Dv[off + t];
     }
     __syncthreads();
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    // lane pair (2j, 2j+1): the gradient sum and the diagonal sum of attribute j walk the same bits,
+    // one FP64 add each per bit (a warp issues one FP64 instruction per bit, not two)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = t >> 1, which = t & 1;
     if (j >= P.d) return;
     const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
-    double g = __dmul_rn(P.x[j], P.lambda);
-    double hs = 0.0;
+    const double* wv = s_w + (which ? n : 0);
+    double acc = which ? 0.0 : __dmul_rn(P.x[j], P.lambda);
     for (int w = 0; w < W; ++w) {
         unsigned long long m = fb[w];
         while (m) {
             const int b = w * 64 + __ffsll((long long)m) - 1;
             m &= m - 1;
-            g = __dadd_rn(g, s_w[b]);
-            hs = __dadd_rn(hs, s_w[n + b]);
+            acc = __dadd_rn(acc, wv[b]);
         }
     }
-    P.gc[(size_t)c * P.d + j] = g;
-    P.dsum[(size_t)c * P.d + j] = hs;
+    if (which) P.dsum[(size_t)c * P.d + j] = acc;
+    else P.gc[(size_t)c * P.d + j] = acc;
 }
 
 __global__ void k_grad_dense(Dev P)
@@ -1018,14 +1020,40 @@ __global__ void k_toplek_rng(int n_mat, int W, const int* worker_of, unsigned* w
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
     unsigned st = wstate[w];
-    for (int c = 0; c < n_mat; ++c) {
-        int owner = worker_of ? worker_of[c] : (c % W);
-        if (owner != w || !needs[c]) continue;
-        double u = lcg_real_unit(st);
-        if (u > pdraw[c]) {     // w.p. 1 - p keep the element (insertInMinHeap)
-            unsigned p = (unsigned)minidx[c];
-            sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
-            cnt[c] += 1;
+    if (worker_of) {
+        for (int c = 0; c < n_mat; ++c) {
+            int owner = worker_of[c];
+            if (owner != w || !needs[c]) continue;
+            double u = lcg_real_unit(st);
+            if (u > pdraw[c]) {     // w.p. 1 - p keep the element (insertInMinHeap)
+                unsigned p = (unsigned)minidx[c];
+                sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
+                cnt[c] += 1;
+            }
+        }
+    } else {
+        // clients w, w + W, ... in order; their flags loaded eight at a time ahead of the draws
+        for (int c0 = w; c0 < n_mat; c0 += 8 * W) {
+            int nd[8], mi[8];
+            double pd[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = c0 + t * W;
+                nd[t] = c < n_mat ? needs[c] : 0;
+                pd[t] = c < n_mat ? pdraw[c] : 0.0;
+                mi[t] = c < n_mat ? minidx[c] : 0;
+            }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = c0 + t * W;
+                if (c >= n_mat || !nd[t]) continue;
+                double u = lcg_real_unit(st);
+                if (u > pd[t]) {
+                    unsigned p = (unsigned)mi[t];
+                    sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
+                    cnt[c] += 1;
+                }
+            }
         }
     }
     wstate[w] = st;
