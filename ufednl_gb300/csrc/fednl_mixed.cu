@@ -367,6 +367,8 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     P.inv_n = 1.0 / (double)h->nc;
     P.prescale = P.inv_n * D.alpha;
     P.mult = D.compressor == FEDNL_RANDK_PHILOX ? (double)U / (double)h->k : 1.0;     // RandK.h:90 / TopK
+    P.multf = (float)P.mult;
+    P.alphaf = (float)D.alpha;
     const size_t ncL = (size_t)h->nc * h->L, ncUp = (size_t)h->nc * h->Up;
     int rc = 0;
     float* X;

@@ -420,6 +420,7 @@ struct MxDev {
     int d, dp, nc, L, U, SW, tiles;     // dp: d padded to the Gram tile (feature rows of X)
     long long Up;
     double lambda, alpha, prescale, inv_n, mult;
+    float alphaf, multf;    // the shift update runs in FP32 (the shifts are FP32)
     const int* ns;          // [nc]
     const float* X;         // [nc][dp][L]
     const double* lab;      // [nc][L] labels (+-1, 0 beyond n)
@@ -881,9 +882,9 @@ __global__ void k_mx_apply(MxDev P)
         for (int t = 0; t < 32; ++t)
             if ((mine >> t) & 1u) {
                 const size_t q = (size_t)(c0 + t) * P.Up + p;
-                const double item = (double)dv[t] * P.mult;
-                P.shift[q] = (float)((double)sv[t] + P.alpha * item);
-                h += item * P.prescale;
+                const float item = dv[t] * P.multf;
+                P.shift[q] = fmaf(P.alphaf, item, sv[t]);         // FP32 shift update
+                h = fma((double)item, P.prescale, h);              // FP64 master, clients in order
             }
     }
     if (in) {
