@@ -519,13 +519,21 @@ __global__ void __launch_bounds__(256) k_mx_grad(MxDev P)
     const float* ql = P.ql + (size_t)c * P.L;
     float hi = 0.0f, lo = 0.0f, h1 = 0.0f, l1 = 0.0f;
     int s = lane;
-    for (; s + 32 < n; s += 64) {
-        const float x0 = __ldg(row + s), x1 = __ldg(row + s + 32);
-        const float a0 = __ldg(qh + s), a1 = __ldg(qh + s + 32), b0 = __ldg(ql + s), b1 = __ldg(ql + s + 32);
-        ff_mac(hi, lo, x0, a0, b0);
-        ff_mac(h1, l1, x1, a1, b1);
+    for (; s + 224 < n; s += 256) {                    // eight samples a lane in flight
+        float x[8], a[8], b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            x[u] = __ldg(row + s + 32 * u);
+            a[u] = __ldg(qh + s + 32 * u);
+            b[u] = __ldg(ql + s + 32 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+            ff_mac(hi, lo, x[u], a[u], b[u]);
+            ff_mac(h1, l1, x[u + 1], a[u + 1], b[u + 1]);
+        }
     }
-    if (s < n) ff_mac(hi, lo, row[s], qh[s], ql[s]);
+    for (; s < n; s += 32) ff_mac(hi, lo, row[s], qh[s], ql[s]);
     ff_add(hi, lo, h1, l1);
     double v = (double)hi + (double)lo;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
