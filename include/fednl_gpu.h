@@ -195,6 +195,13 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
  * memory (d up to about 300), one step of iterative refinement on a float-float residual of H held
  * as an FP32 pair, dx in FP64.  Host buffers, H column-major upper (lda >= d). */
 int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
+/* The same system by the FP32 Cholesky on a cooperative grid (fednl_mx_set_solver 2): at most
+ * `refine` FP64-residual refinement steps (0..8; they stop once a correction is at most 2^-30 of the
+ * solution), `grid` CTAs (0: one per tile of the first trailing update),
+ * d up to 1344.  A pivot that loses more than 18 bits in FP32 hands the system to the FP64 solve,
+ * which returns FEDNL_ENOTPD for a matrix that is not positive definite.  Host buffers. */
+int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
+                              int32_t refine, int32_t grid);
 int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g,
                                     double* dx, void* stream);
 
@@ -252,7 +259,10 @@ int fednl_mx_get_x(fednl_mx_handle h, double* x);
 int fednl_mx_get_grad(fednl_mx_handle h, double* g);
 double fednl_mx_get_l(fednl_mx_handle h);
 /* Newton solve of the round: 0 = FP64 cooperative Cholesky (default), 1 = FP32 Cholesky in one CTA's
- * shared memory with one refinement step on a float-float residual (d up to about 300) */
+ * shared memory with one refinement step on a float-float residual (d up to about 300), 2 = FP32
+ * Cholesky on a cooperative grid with FP64-residual refinement until the correction is at most 2^-30
+ * of the solution, six steps at most (d up to 1344; a pivot that loses more than 18 bits in FP32
+ * hands the system to the FP64 solve in the same launch) */
 int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver);
 /* the last round's FP32 differences H_c - shift_c (packed upper, [U]; RandK-Philox: only the
  * selected positions are current), selected packed positions, and the FP32 shift of a client */
@@ -294,8 +304,8 @@ int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats);
 /* Measures the launch shapes of the round's Newton solve on the handle's current system (scratch
  * outputs: the run's state does not change) and keeps the fastest; results are cached per d for the
  * process.  FP64 handles: the cooperative Cholesky's CTA count (results are identical for every
- * count).  Mixed handles: that count and the solver (FP64 cooperative or, d up to about 300, the FP32
- * shared-memory factor with refinement). */
+ * count).  Mixed handles: the solver (FP64 cooperative, FP32 cooperative with refinement, or, d up
+ * to about 300, the FP32 shared-memory factor with refinement) and the chosen one's CTA count. */
 int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid, double* solve_ms);
 int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver, int32_t* chol_grid, double* solve_ms);
 

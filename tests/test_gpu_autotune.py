@@ -45,9 +45,9 @@ def test_mixed_autotune_choice_tracks(gpu, d):
     gb = b.run(2)
     x_before = b.x()
     t = b.autotune()
-    assert t["solver"] in ("fp64", "fp32_refined") and t["solve_ms"] > 0
+    assert t["solver"] in ("fp64", "fp32_refined", "fp32_coop") and t["solve_ms"] > 0
     if d > 304:
-        assert t["solver"] == "fp64"
+        assert t["solver"] != "fp32_refined"
     np.testing.assert_array_equal(b.x(), x_before)
     ga = np.concatenate([ga, a.run(6)])
     gb = np.concatenate([gb, b.run(6)])

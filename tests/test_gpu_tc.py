@@ -207,6 +207,77 @@ def test_mixed_solve_not_pd(gpu):
     assert e.value.code == -4
 
 
+@pytest.mark.parametrize("d", [1, 5, 31, 32, 33, 64, 65, 100, 257, 301, 640, 1024, 1344])
+def test_mixed_coop32_solve_matches_fp64(gpu, d):
+    """The FP32 Cholesky on a cooperative grid with FP64-residual refinement (to 2^-30, six steps at
+    most): relative error against an FP64 solve below 5e-9 at condition 1e3; at 1e5 each step gains
+    only a factor of about cond x 2^-24 x a growth factor in d, and the bar is 1e-3."""
+    rng = np.random.default_rng(1000 + d)
+    for cond, tol in ((1e3, 5e-9), (1e5, 1e-3)):
+        H = _spd(rng, d, cond)
+        lda = d + 3
+        Hc = np.zeros((d, lda))
+        Hc[:, :d] = H.T
+        g = rng.standard_normal(d)
+        l = 1e-3
+        dx = gpu.cholesky_option_b_solve32(Hc.ravel(), d, lda, l, g)
+        ref = np.linalg.solve(H + l * np.eye(d), g)
+        err = np.linalg.norm(dx - ref) / np.linalg.norm(ref)
+        assert err < tol, (d, cond, err)
+
+
+def test_mixed_coop32_solve_same_for_every_grid(gpu):
+    """Every element of the factor, the residual and the solves is computed by the same arithmetic
+    whichever CTA owns it: the result is bit-identical across CTA counts."""
+    rng = np.random.default_rng(7)
+    d = 300
+    H = _spd(rng, d, 1e4)
+    g = rng.standard_normal(d)
+    ref = gpu.cholesky_option_b_solve32(H, d, d, 1e-3, g, grid=1)
+    for G in (2, 3, 7, 45, 64):
+        np.testing.assert_array_equal(gpu.cholesky_option_b_solve32(H, d, d, 1e-3, g, grid=G), ref)
+    exact = np.linalg.solve(H + 1e-3 * np.eye(d), g)
+    e = [np.linalg.norm(gpu.cholesky_option_b_solve32(H, d, d, 1e-3, g, refine=r) - exact) / np.linalg.norm(exact)
+         for r in (0, 1, 2, 6)]
+    assert e[0] < 0.05 and e[3] < 1e-8 and e[3] <= e[2] <= e[1] <= e[0], e
+
+
+def test_mixed_coop32_solve_hands_ill_conditioned_and_indefinite_systems_to_fp64(gpu):
+    """A pivot that keeps fewer than six bits in FP32 (condition 1e9 here) sends the system to the
+    FP64 cooperative solve in the same launch: the answer has FP64 accuracy.  A matrix that is not
+    positive definite is reported by that solve (FEDNL_ENOTPD)."""
+    rng = np.random.default_rng(11)
+    d = 96
+    H = _spd(rng, d, 1e9)
+    g = rng.standard_normal(d)
+    dx = gpu.cholesky_option_b_solve32(H, d, d, 0.0, g)
+    ref = np.linalg.solve(H, g)
+    assert np.linalg.norm(dx - ref) / np.linalg.norm(ref) < 1e-5
+    with pytest.raises(gpu.FedNLError) as e:
+        gpu.cholesky_option_b_solve32(np.array([[1.0, 2.0], [2.0, 1.0]]), 2, 2, 0.0, np.ones(2))
+    assert e.value.code == -4
+
+
+@pytest.mark.parametrize("comp", ["randk_philox", "toplek"])
+def test_mixed_round_with_coop32_solve_tracks_fp64_solve(gpu, comp):
+    """The mixed round solved by the FP32 cooperative Cholesky with two refinement steps: the ||g||
+    trajectory agrees with the FP64-solve trajectory to 1e-8 relative while ||g|| falls by decades."""
+    from ufednl_gb300 import datagen
+    d = 200
+    prob = datagen.dense_problem_fp32(71, d, [240, 300, 180, 260], 1e-3)
+    k = 4 * d if comp == "randk_philox" else 8 * d
+    alpha = k / (d * (d + 1) // 2) if comp == "randk_philox" else 1.0
+    a = gpu.MixedFedNL(prob, k, alpha, compressor=comp)
+    ga = a.run(15)
+    a.close()
+    b = gpu.MixedFedNL(prob, k, alpha, compressor=comp, solver="fp32_coop")
+    gb = b.run(15)
+    b.close()
+    assert abs(ga[0] - gb[0]) <= 1e-14 * ga[0]
+    n = int(np.sum(ga > 1e-8))
+    assert n >= 4 and np.all(np.abs(ga[:n] - gb[:n]) <= 1e-8 * ga[:n]), (ga, gb)
+
+
 @pytest.mark.parametrize("comp", ["randk_philox", "toplek"])
 def test_mixed_round_with_refined_fp32_solve_tracks_fp64_solve(gpu, comp):
     """The same mixed round solved by the FP32 shared-memory Cholesky with one refinement step

@@ -8,6 +8,7 @@
 
 #include "fednl_gpu.h"
 #include "fednl_kernels.cuh"
+#include "fednl_chol32c.cuh"
 #include "fednl_solve.h"
 #include "fednl_smem.h"
 
@@ -243,35 +244,121 @@ int fednl_device_optionb_solve(const double* H, int d, const double* lptr, const
     return FEDNL_OK;
 }
 
+// ---- the FP32 cooperative solve of the mixed-precision form (fednl_chol32c.cuh) ---------------
+namespace {
+
+// dynamic shared memory of k_chol32c for dimension d, and whether CTA 0 keeps the factor resident
+// (when it fits beside the kernel's static shared memory)
+size_t chol32c_smem(int d, int* resident)
+{
+    static int optin = -1;
+    static size_t stat = 0;
+    if (optin < 0) {
+        int dev = 0, o = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, k_chol32c);
+        stat = fa.sharedSizeBytes;
+        optin = o;
+    }
+    const size_t rb = c32c_smem_bytes(d, true);
+    *resident = (d + 31) / 32 <= kC32ResBlocks && rb + stat + 1024 <= (size_t)optin ? 1 : 0;
+    return *resident ? rb : c32c_smem_bytes(d, false);
+}
+
+// resident CTAs of k_chol32c for dimension d (the cooperative launch's upper bound)
+int chol32c_cap(int d)
+{
+    int dev = 0, sms = 1, bps = 0, res = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t smem = chol32c_smem(d, &res);
+    if (fednl_raise_dyn_smem((const void*)k_chol32c, smem) != cudaSuccess) return 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol32c, kCoopThreads, smem);
+    return std::min(sms, sms * bps);
+}
+
+// default CTA count: one per 32 x 32 tile of the first trailing update, within the resident limit
+int chol32c_grid(int d)
+{
+    const long long nt = d > 32 ? (d - 32 + 31) / 32 : 1;
+    return (int)std::max<long long>(1, std::min<long long>(nt * (nt + 1) / 2, chol32c_cap(d)));
+}
+
+}  // namespace
+
+int fednl_solve32_max_d() { return kC32MaxD; }
+
+size_t fednl_solve32_bytes(int d)
+{
+    const size_t ld = (size_t)c32c_ld(d);
+    return ld * ld * 4 + (size_t)d * 4 + ld * 32 * 4 + 2 * (size_t)d * 8 + 4;
+}
+
+int fednl_device_optionb_solve32(const FednlSolveDesc& S, const FednlSolve32& E, cudaStream_t st, int grid)
+{
+    if (S.d < 1 || S.d > kC32MaxD || !S.lptr) return FEDNL_EINVAL;
+    Dev P{};
+    P.d = S.d;
+    P.U = S.d * (S.d + 1) / 2;
+    P.work = S.work;
+    P.ybuf = S.ybuf;
+    P.rinv = S.rinv;
+    P.bar = S.bar;
+    P.status = S.status;
+    P.stats = S.stats;
+    P.hist = S.hist;
+    P.ls = S.ls;
+    P.round_ctr = S.round_ctr;
+    P.hist_cap = S.hist_cap;
+    int res = 0;
+    const size_t smem = chol32c_smem(S.d, &res);
+    Chol32c C{E.a, E.diag0, E.linv, E.r, E.acc, E.flag, c32c_ld(S.d), E.refine, E.tol, res, (int)(smem / 4)};
+    const int cap = chol32c_cap(S.d);
+    if (cap < 1) return FEDNL_ECUDA;
+    if (grid <= 0) grid = chol32c_grid(S.d);
+    grid = std::min(grid, cap);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kCoopThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, k_chol32c, P, C, S.H, S.lptr, S.g, S.dx, S.xupd, S.record));
+    return FEDNL_OK;
+}
+
 // ---- autotuning of the solve's launch shape ----------------------------------------------------
-// The cooperative Cholesky's CTA count is measured per dimension on the caller's own system (the
+// A cooperative solve's CTA count is measured per dimension on the caller's own system (the
 // handle's current H, l and g into scratch outputs: nothing of the run changes) and cached
-// process-wide, so later handles of the same d reuse the choice.
-int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid, double* best_ms)
+// process-wide per solver kind, so later handles of the same d reuse the choice.
+static int tune_grid(int kind, int d, int cap, int dflt, const std::function<int(int)>& launch, cudaStream_t st,
+                     int* best_grid, double* best_ms)
 {
     static std::mutex mu;
-    static std::map<int, std::pair<int, double>> cache;
+    static std::map<std::pair<int, int>, std::pair<int, double>> cache;
     {
         std::lock_guard<std::mutex> g(mu);
-        auto it = cache.find(d);
+        auto it = cache.find({kind, d});
         if (it != cache.end()) {
             *best_grid = it->second.first;
             *best_ms = it->second.second;
             return FEDNL_OK;
         }
     }
-    int dev = 0, sms = 1, bps = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_coop, kCoopThreads, 0);
-    const int cap = std::min(sms, sms * std::max(1, bps));
-    std::vector<int> cand = {8, 16, 32, 48, 64, 96, 128, cap, chol_grid(d)};
+    if (cap < 1) return FEDNL_ECUDA;
+    std::vector<int> cand = {8, 16, 24, 32, 48, 64, 96, 128, cap, dflt};
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int bg = chol_grid(d);
+    int bg = std::min(dflt, cap);
     double bm = 1e30;
     for (int G : cand) {
         if (G < 1 || G > cap) continue;
@@ -296,10 +383,25 @@ int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStrea
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> g(mu);
-    cache[d] = {bg, bm};
+    cache[{kind, d}] = {bg, bm};
     *best_grid = bg;
     *best_ms = bm;
     return FEDNL_OK;
+}
+
+int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid, double* best_ms)
+{
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_coop, kCoopThreads, 0);
+    return tune_grid(0, d, std::min(sms, sms * std::max(1, bps)), chol_grid(d), launch, st, best_grid, best_ms);
+}
+
+int fednl_tune_chol32_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid,
+                           double* best_ms)
+{
+    return tune_grid(1, d, chol32c_cap(d), chol32c_grid(d), launch, st, best_grid, best_ms);
 }
 
 struct fednl_handle_s {
@@ -1631,6 +1733,74 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     if (status == FEDNL_ETIMEOUT) return fail(FEDNL_ETIMEOUT, "grid barrier of the Cholesky timed out");
     if (status) return fail(FEDNL_ENOTPD, "H + l I is not positive definite");
     CK(cudaMemcpy(dx, P.dx, d * 8, cudaMemcpyDeviceToHost));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
+                              int32_t refine, int32_t grid)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!H || !g || !dx || d < 1 || lda < d || refine < 0 || refine > 8 || grid < 0) return fail(FEDNL_EINVAL, "bad argument");
+    if (d > kC32MaxD) return fail(FEDNL_EINVAL, "d %d above the FP32 cooperative solve's limit %d", d, kC32MaxD);
+    long long U = (long long)d * (d + 1) / 2;
+    const size_t ld = (size_t)c32c_ld(d);
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *dfull, *dpack, *dg, *dl, *ddx, *work, *ybuf, *rinv, *stats;
+    unsigned* bar;
+    int* status;
+    FednlSolve32 E{};
+    s.a.want(&dfull, (size_t)d * lda);
+    s.a.want(&dpack, U);
+    s.a.want(&dg, d);
+    s.a.want(&dl, 1);
+    s.a.want(&ddx, d);
+    s.a.want(&work, (size_t)(d + 1) * (d + 2) / 2);
+    s.a.want(&ybuf, d);
+    s.a.want(&rinv, d);
+    s.a.want(&stats, 4);
+    s.a.want(&status, 1);
+    s.a.want(&bar, 4);
+    s.a.want(&E.a, ld * ld);
+    s.a.want(&E.diag0, d);
+    s.a.want(&E.linv, ld * 32);
+    s.a.want(&E.r, d);
+    s.a.want(&E.acc, d);
+    s.a.want(&E.flag, 1);
+    rc = s.a.commit();
+    if (rc) return rc;
+    E.refine = refine;
+    E.tol = 0x1p-30f;
+    CK(cudaMemsetAsync(bar, 0, 16, s.st));
+    CK(cudaMemsetAsync(status, 0, 4, s.st));
+    CK(cudaMemcpyAsync(dfull, H, (size_t)d * lda * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dg, g, d * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dl, &l, 8, cudaMemcpyHostToDevice, s.st));
+    k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U,
+                                                                                                (int)U, dpack);
+    CKL();
+    FednlSolveDesc S{};
+    S.H = dpack;
+    S.d = d;
+    S.lptr = dl;
+    S.g = dg;
+    S.dx = ddx;
+    S.work = work;
+    S.ybuf = ybuf;
+    S.rinv = rinv;
+    S.bar = bar;
+    S.status = status;
+    S.stats = stats;
+    S.record = 0;
+    rc = fednl_device_optionb_solve32(S, E, s.st, grid);
+    if (rc) return fail(rc, "FP32 cooperative solve launch failed");
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    if (st == FEDNL_ETIMEOUT) return fail(FEDNL_ETIMEOUT, "grid barrier of the Cholesky timed out");
+    if (st) return fail(FEDNL_ENOTPD, "H + l I is not positive definite");
+    CK(cudaMemcpy(dx, ddx, d * 8, cudaMemcpyDeviceToHost));
     return FEDNL_OK;
 }
 

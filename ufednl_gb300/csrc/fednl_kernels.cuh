@@ -1289,41 +1289,62 @@ constexpr int kCholSlab = 8;                          // panel columns per CTA k
 constexpr int kCoopThreads = 256;
 constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIMEOUT
 
-// bounded grid barrier; returns false (error flag set) if the other CTAs did not arrive in time
-__device__ bool grid_barrier(unsigned* bar, unsigned nblk)
-{
-    __syncthreads();
-    __shared__ int s_ok;
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = bar + 1;
-        volatile unsigned* verr = bar + 2;
-        unsigned gen = *vgen;
-        __threadfence();
-        unsigned arrived = atomicAdd(bar, 1u) + 1u;
-        int ok = 1;
-        if (arrived == nblk) {
-            atomicExch(bar, 0u);
+// Bounded grid barrier of n cooperating CTAs on three words: bar[0] counts arrivals since the
+// launch began (the e-th barrier completes when it reaches e n), bar[1] counts CTAs that have
+// finished, bar[2] is the error flag.  One fence and one reduction per CTA, then a poll with acquire
+// loads: no counter is reset between barriers.  Every CTA calls finish() once after its last
+// barrier; the last one to do so returns both counters to zero for the next launch.  sync() returns
+// false (error flag set) when the other CTAs did not arrive in time.
+struct GridSync {
+    unsigned* bar;
+    unsigned n;
+    unsigned epoch = 0;        // barriers this CTA has passed (kept by thread 0)
+
+    __device__ GridSync(unsigned* b, unsigned nblk) : bar(b), n(nblk) {}
+
+    __device__ bool sync()
+    {
+        __shared__ int s_ok;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            epoch += 1;
+            const unsigned target = epoch * n;
             __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long long t0 = clock64();
-            while (*vgen == gen) {
-                if (*verr) { ok = 0; break; }
+            atomicAdd(bar, 1u);
+            volatile unsigned* verr = bar + 2;
+            int ok = 1;
+            const long long t0 = clock64();
+            for (;;) {
+                unsigned v;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+                if ((int)(v - target) >= 0) break;
+                if (*verr) {
+                    ok = 0;
+                    break;
+                }
                 if (clock64() - t0 > kBarrierCycles) {
                     atomicExch(bar + 2, 1u);
                     ok = 0;
                     break;
                 }
-                __nanosleep(64);
             }
+            __threadfence();
+            if (*verr) ok = 0;
+            s_ok = ok;
         }
-        __threadfence();
-        if (*verr) ok = 0;
-        s_ok = ok;
+        __syncthreads();
+        return s_ok != 0;
     }
-    __syncthreads();
-    return s_ok != 0;
-}
+
+    __device__ void finish()
+    {
+        __syncthreads();
+        if (threadIdx.x == 0 && atomicAdd(bar + 1, 1u) == n - 1) {
+            atomicExch(bar, 0u);
+            atomicExch(bar + 1, 0u);
+        }
+    }
+};
 
 // Hin is the packed upper triangle, or (hin_lda > 0) a column-major matrix with that leading
 // dimension of which the upper triangle is read.
@@ -1331,7 +1352,7 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblk)
 // the grid barrier counts the group's CTAs on P.bar.
 __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict__ Hin, int hin_lda, const double* lptr,
                                           double lval, const double* __restrict__ gin, double* dxout, double* xupd,
-                                          int record, unsigned G, unsigned bid)
+                                          int record, unsigned G, unsigned bid, GridSync& gs)
 {
     __shared__ double Db[kCholNB][kCholNB + 1];
     __shared__ double Rb[kCholNB][kCholNB + 1];
@@ -1360,7 +1381,7 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             A[p] = (i < d) ? gin[i] : 0.0;
         }
     }
-    if (!grid_barrier(P.bar, G)) goto timeout;
+    if (!gs.sync()) goto timeout;
     for (int c0 = 0; c0 < d; c0 += kCholNB) {
         const int nb = min(kCholNB, d - c0), c1 = c0 + nb;
         // this CTA's panel columns right of the block: j = c1 + bid + s G, s < ns (kept in
@@ -1486,7 +1507,7 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             }
         }
         if (c1 >= d) break;
-        if (!grid_barrier(P.bar, G)) goto timeout;
+        if (!gs.sync()) goto timeout;
         // trailing update, entries (i, j) with c1 <= i <= j < D (column d carries y)
         {
             const int m = D - c1;
@@ -1510,9 +1531,9 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 A[up_pos(i, j)] = a;
             }
         }
-        if (!grid_barrier(P.bar, G)) goto timeout;
+        if (!gs.sync()) goto timeout;
     }
-    if (!grid_barrier(P.bar, G)) goto timeout;
+    if (!gs.sync()) goto timeout;
     if (bid != 0) return;
     {
         // R dx = y (y in column d), blocked by 32 rows (CTA 0)
@@ -1617,7 +1638,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double*
                                                             const double* __restrict__ gin, double* dxout,
                                                             double* xupd, int record)
 {
-    chol_body(P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, gridDim.x, blockIdx.x);
+    GridSync gs(P.bar, gridDim.x);
+    chol_body(P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, gridDim.x, blockIdx.x, gs);
+    gs.finish();
 }
 
 // Several independent Option-B solves in one cooperative launch (the serving loop's tick): job j
@@ -1641,8 +1664,10 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_batched(const CholJob* __
     while (j + 1 < njobs && (int)blockIdx.x >= jobs[j + 1].cta0) ++j;
     const CholJob& J = jobs[j];
     if ((int)blockIdx.x >= J.cta0 + J.ncta) return;
+    GridSync gs(J.P.bar, (unsigned)J.ncta);
     chol_body(J.P, J.Hin, J.hin_lda, J.lptr, J.lval, J.gin, J.dxout, J.xupd, J.record, (unsigned)J.ncta,
-              blockIdx.x - (unsigned)J.cta0);
+              blockIdx.x - (unsigned)J.cta0, gs);
+    gs.finish();
 }
 
 // ---- operator-level helpers -----------------------------------------------------------------

@@ -219,6 +219,10 @@ struct fednl_mx_handle_s {
     size_t select_smem = 0;
     bool chol32 = false;               // the round solves with the FP32 factor + refinement
     bool chol32_ok = false;            // the system fits one CTA's shared memory
+    bool coop32 = false;               // the round solves with the FP32 cooperative factor (fednl_chol32c.cuh)
+    bool coop32_ok = false;            // d within that solve's shared-memory limit
+    int coop32_grid = 0;               // its CTAs (0: default)
+    FednlSolve32 s32{};                // its buffers
     int coop_grid = 0;                 // CTAs of the FP64 cooperative solve (0: the default heuristic)
     fednl_c32::Job* cjob = nullptr;    // device copy of the solve's job
     void* flush_buf = nullptr;
@@ -252,6 +256,30 @@ const char* const kMxKernelNamesTop[] = {"k_mx_split_x", "k_mx_margin", "k_mx_gr
                                          "k_mx_lk", "k_mx_select", "k_mx_apply", "k_mx_aggregate", "k_chol_coop"};
 constexpr int kMxKernels = 9;
 
+// the handle's Option-B system as a solve descriptor (dx, x -= dx, statistics of the round)
+FednlSolveDesc mx_solve_desc(fednl_mx_handle h)
+{
+    const fednl_tc::MxDev& P = h->P;
+    FednlSolveDesc S{};
+    S.H = P.H;
+    S.d = h->d;
+    S.lptr = P.stats + 1;
+    S.g = P.g;
+    S.dx = h->dx;
+    S.xupd = P.x;
+    S.work = h->work;
+    S.ybuf = h->ybuf;
+    S.rinv = h->rinv;
+    S.bar = h->bar;
+    S.status = h->status;
+    S.stats = P.stats;
+    S.hist = h->hist;
+    S.round_ctr = h->round_ctr;
+    S.hist_cap = h->hist_cap;
+    S.record = 1;
+    return S;
+}
+
 int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_phase_only = false)
 {
     using namespace fednl_tc;
@@ -264,7 +292,7 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     mark();
     k_mx_split_x<<<(h->d + 255) / 256, 256, 0, st>>>(P);
     mark();
-    k_mx_margin<<<dim3((h->L + 255) / 256, h->nc), 256, 0, st>>>(P);
+    k_mx_margin<<<dim3((h->L + 63) / 64, h->nc), dim3(64, 4), 0, st>>>(P);
     mark();
     k_mx_grad<<<(h->nc * h->d + 7) / 8, 256, 0, st>>>(P);
     mark();
@@ -295,6 +323,11 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
         mark();
         CKM(cudaGetLastError());
         return FEDNL_OK;
+    }
+    if (h->coop32) {
+        int rc = fednl_device_optionb_solve32(mx_solve_desc(h), h->s32, st, h->coop32_grid);
+        mark();
+        return rc;
     }
     int rc = fednl_device_optionb_solve(P.H, h->d, P.stats + 1, P.g, h->dx, P.x, h->work, h->ybuf, h->rinv, h->bar,
                                         h->status, P.stats, h->hist, h->round_ctr, h->hist_cap, 1, st, h->coop_grid);
@@ -407,6 +440,18 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     rc |= h->alloc(&h->bar, 4);
     rc |= h->alloc(&h->status, 1);
     rc |= h->alloc(&h->round_ctr, 1);
+    h->coop32_ok = h->d <= fednl_solve32_max_d();
+    if (h->coop32_ok) {
+        const size_t ld = (size_t)((h->d + 31) & ~31);
+        rc |= h->alloc(&h->s32.a, ld * ld);
+        rc |= h->alloc(&h->s32.diag0, h->d);
+        rc |= h->alloc(&h->s32.linv, ld * 32);
+        rc |= h->alloc(&h->s32.r, h->d);
+        rc |= h->alloc(&h->s32.acc, h->d);
+        rc |= h->alloc(&h->s32.flag, 1);
+        h->s32.refine = 6;
+        h->s32.tol = 0x1p-30f;
+    }
     if (footprint) {     // plus the upload's staging copy of the sample-major features
         *footprint = (int64_t)h->dry + (int64_t)h->S * h->d * 4 + (int64_t)(h->nc + 1) * 4 + 4096;
         delete h;
@@ -544,7 +589,7 @@ int fednl_mx_init_shifts(fednl_mx_handle h, const double* x0)
     if (x0) CKM(cudaMemcpyAsync(P.x, x0, h->d * 8, cudaMemcpyHostToDevice, st));
     else CKM(cudaMemsetAsync(P.x, 0, h->d * 8, st));
     k_mx_split_x<<<(h->d + 255) / 256, 256, 0, st>>>(P);
-    k_mx_margin<<<dim3((h->L + 255) / 256, h->nc), 256, 0, st>>>(P);
+    k_mx_margin<<<dim3((h->L + 63) / 64, h->nc), dim3(64, 4), 0, st>>>(P);
     GramJob J{h->dp, h->nc, h->L, h->dp / kBM, h->tiles, h->ns_dev, nullptr, P.Dw, h->err};
     EpiInitShift epi{P.shift, h->Up, (float)P.lambda, h->d};
     k_gram_tf32<EpiInitShift><<<h->nc * h->tiles, kThreads, smem_bytes(), st>>>(h->map, J, epi);
@@ -654,7 +699,8 @@ int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_m
         std::string all;
         const char* const* nm = h->comp == FEDNL_RANDK_PHILOX ? kMxKernelNames : kMxKernelNamesTop;
         for (int t = 0; t < kMxKernels; ++t)
-            all += std::string(t ? ";" : "") + (t == kMxKernels - 1 && h->chol32 ? "k_chol32" : nm[t]);
+            all += std::string(t ? ";" : "") +
+                   (t == kMxKernels - 1 && h->chol32 ? "k_chol32" : t == kMxKernels - 1 && h->coop32 ? "k_chol32c" : nm[t]);
         snprintf(names, (size_t)names_len, "%s", all.c_str());
     }
     h->rounds_done += rounds;
@@ -663,16 +709,20 @@ int fednl_mx_profile_kernels(fednl_mx_handle h, int32_t rounds, double* kernel_m
 
 int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver)
 {
-    if (!h || solver < 0 || solver > 1) return fail_m(FEDNL_EINVAL, "bad argument");
+    if (!h || solver < 0 || solver > 2) return fail_m(FEDNL_EINVAL, "bad argument");
     if (solver == 1 && !h->chol32_ok) return fail_m(FEDNL_EINVAL, "d %d too large for the shared-memory solve", h->d);
-    const bool want = solver == 1;
-    if (want != h->chol32 && h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        cudaGraphDestroy(h->graph);
-        h->gexec = nullptr;
-        h->graph = nullptr;
+    if (solver == 2 && !h->coop32_ok)
+        return fail_m(FEDNL_EINVAL, "d %d above the FP32 cooperative solve's limit %d", h->d, fednl_solve32_max_d());
+    if ((solver == 1) != h->chol32 || (solver == 2) != h->coop32) {
+        if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            cudaGraphDestroy(h->graph);
+            h->gexec = nullptr;
+            h->graph = nullptr;
+        }
     }
-    h->chol32 = want;
+    h->chol32 = solver == 1;
+    h->coop32 = solver == 2;
     return FEDNL_OK;
 }
 
@@ -680,19 +730,23 @@ int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver_out, int32_t* grid_out,
 {
     if (!h || !h->ready) return fail_m(FEDNL_EINVAL, "call fednl_mx_init_shifts first");
     static std::mutex mu;
-    static std::map<int, std::pair<int, int>> cache;       // d -> (solver, CTAs)
-    static std::map<int, double> cache_ms;
+    struct Choice {
+        int solver, grid, grid32;
+        double ms;
+    };
+    static std::map<int, Choice> cache;                    // per d
     CKM(cudaStreamSynchronize(h->stream));
-    int solver = 0, grid = 0;
+    int solver = 0, grid = 0, grid32 = 0;
     double best = 0.0;
     bool cached = false;
     {
         std::lock_guard<std::mutex> g(mu);
         auto it = cache.find(h->d);
         if (it != cache.end()) {
-            solver = it->second.first;
-            grid = it->second.second;
-            best = cache_ms[h->d];
+            solver = it->second.solver;
+            grid = it->second.grid;
+            grid32 = it->second.grid32;
+            best = it->second.ms;
             cached = true;
         }
     }
@@ -748,9 +802,27 @@ int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver_out, int32_t* grid_out,
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             if (cudaGetLastError() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "tuning launch failed");
-            else if (b32 < coop_ms) {
+            else if (b32 < best) {
                 solver = 1;
                 best = b32;
+            }
+        }
+        if (!rc && h->coop32_ok) {
+            FednlSolveDesc S = mx_solve_desc(h);
+            S.dx = sdx;
+            S.xupd = nullptr;
+            S.stats = sstats;
+            S.hist = shist;
+            S.round_ctr = sctr;
+            S.hist_cap = 1;
+            S.status = sstatus;
+            auto launch32 = [&](int G) -> int { return fednl_device_optionb_solve32(S, h->s32, st, G); };
+            double ms32 = 0.0;
+            rc = fednl_tune_chol32_grid(h->d, launch32, st, &grid32, &ms32);
+            if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "tuning launch failed");
+            if (!rc && ms32 < best) {
+                solver = 2;
+                best = ms32;
             }
         }
         cudaFree(sdx);
@@ -761,9 +833,9 @@ int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver_out, int32_t* grid_out,
         cudaFree(sjob);
         if (rc) return rc;
         std::lock_guard<std::mutex> g(mu);
-        cache[h->d] = {solver, grid};
-        cache_ms[h->d] = best;
+        cache[h->d] = {solver, grid, grid32, best};
     }
+    h->coop32_grid = grid32;
     if (grid != h->coop_grid && h->gexec) {
         cudaGraphExecDestroy(h->gexec);
         cudaGraphDestroy(h->graph);
@@ -774,7 +846,7 @@ int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver_out, int32_t* grid_out,
     int rc = fednl_mx_set_solver(h, solver);
     if (rc) return rc;
     if (solver_out) *solver_out = solver;
-    if (grid_out) *grid_out = grid;
+    if (grid_out) *grid_out = solver == 2 ? grid32 : grid;
     if (solve_ms) *solve_ms = best;
     return FEDNL_OK;
 }
@@ -926,24 +998,7 @@ extern "C" {
 int fednl_mx_solve_desc(fednl_mx_handle h, FednlSolveDesc* S, void** stream)
 {
     if (!h || !h->ready || !S) return FEDNL_EINVAL;
-    const fednl_tc::MxDev& P = h->P;
-    *S = FednlSolveDesc{};
-    S->H = P.H;
-    S->d = h->d;
-    S->lptr = P.stats + 1;
-    S->g = P.g;
-    S->dx = h->dx;
-    S->xupd = P.x;
-    S->work = h->work;
-    S->ybuf = h->ybuf;
-    S->rinv = h->rinv;
-    S->bar = h->bar;
-    S->status = h->status;
-    S->stats = P.stats;
-    S->hist = h->hist;
-    S->round_ctr = h->round_ctr;
-    S->hist_cap = h->hist_cap;
-    S->record = 1;
+    *S = mx_solve_desc(h);
     if (stream) *stream = (void*)h->stream;
     h->rounds_done += 1;
     return FEDNL_OK;

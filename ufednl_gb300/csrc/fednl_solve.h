@@ -35,6 +35,27 @@ int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream);
 int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid,
                          double* best_ms);
 
+// The FP32 cooperative solve of the mixed-precision form (fednl_chol32c.cuh): its buffers, of
+// fednl_solve32_bytes(d) device bytes in all, for d up to fednl_solve32_max_d().
+struct FednlSolve32 {
+    float* a;              // [ld][ld], ld = d rounded up to 32
+    float* diag0;          // [d]
+    float* linv;           // [ld][32]
+    double* r;             // [d]
+    double* acc;           // [d]
+    int* flag;             // [1]
+    int refine;            // at most this many refinement steps after the first solve
+    float tol;             // stop refining when the correction is at most tol of the solution
+};
+int fednl_solve32_max_d();
+size_t fednl_solve32_bytes(int d);
+// (H + l I) dx = g, x -= dx with the FP32 factor and FP64 refinement on `grid` CTAs (0: default);
+// S.lptr is required.  An FP32 pivot that loses more than 18 bits hands the system to the FP64
+// cooperative solve in the same launch (S.work, S.ybuf, S.rinv).
+int fednl_device_optionb_solve32(const FednlSolveDesc& S, const FednlSolve32& E, cudaStream_t st, int grid);
+int fednl_tune_chol32_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid,
+                           double* best_ms);
+
 // fednl_mixed.cu: a mixed-precision handle's solve as a descriptor (and its stream)
 struct fednl_mx_handle_s;
 extern "C" int fednl_mx_solve_desc(struct fednl_mx_handle_s* h, FednlSolveDesc* desc, void** stream);

@@ -456,55 +456,61 @@ __global__ void k_mx_split_x(MxDev P)
 // margin m_s = b_s a_s^T x, sigmoid (FP64), D_s (Gram weight, FP32) and b_s q_s (FP32 pair)
 __device__ __forceinline__ double mx_sigmoid(double m) { return 1.0 / (1.0 + exp(-m)); }
 
+// A block covers 64 samples; its four warp rows split each sample's features in quarters (eight
+// loads in flight each, two float-float accumulators), and the quarters are added in order.
 __global__ void __launch_bounds__(256) k_mx_margin(MxDev P)
 {
     __shared__ float s_xh[1024], s_xl[1024];
-    const int c = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int i = threadIdx.x; i < P.d && i < 1024; i += blockDim.x) {
+    __shared__ float s_ph[4][64], s_pl[4][64];
+    const int c = blockIdx.y, sx = threadIdx.x, q = threadIdx.y;
+    const int tid = q * 64 + sx;
+    for (int i = tid; i < P.d && i < 1024; i += 256) {
         s_xh[i] = P.xh[i];
         s_xl[i] = P.xl[i];
     }
     __syncthreads();
     const int n = P.ns[c];
-    if (s >= n) return;
-    const float* col = P.X + (size_t)c * P.dp * P.L + s;
-    // eight feature loads in flight, four independent float-float accumulators (feature i mod 4)
-    float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f, h2 = 0.0f, l2 = 0.0f, h3 = 0.0f, l3 = 0.0f;
-    int i = 0;
-    for (; i + 8 <= P.d; i += 8) {
-        float xv[8], yh[8], yl[8];
+    const int s = blockIdx.x * 64 + sx;
+    const int per = (P.d + 3) / 4, i0 = q * per, i1 = min(P.d, i0 + per);
+    float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+    if (s < n) {
+        const float* col = P.X + (size_t)c * P.dp * P.L + s;
+        int i = i0;
+        for (; i + 8 <= i1; i += 8) {
+            float xv[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) xv[u] = __ldg(col + (size_t)(i + u) * P.L);
+            for (int u = 0; u < 8; ++u) xv[u] = __ldg(col + (size_t)(i + u) * P.L);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            yh[u] = i + u < 1024 ? s_xh[i + u] : P.xh[i + u];
-            yl[u] = i + u < 1024 ? s_xl[i + u] : P.xl[i + u];
+            for (int u = 0; u < 8; u += 2) {
+                const float yh0 = i + u < 1024 ? s_xh[i + u] : P.xh[i + u];
+                const float yl0 = i + u < 1024 ? s_xl[i + u] : P.xl[i + u];
+                const float yh1 = i + u + 1 < 1024 ? s_xh[i + u + 1] : P.xh[i + u + 1];
+                const float yl1 = i + u + 1 < 1024 ? s_xl[i + u + 1] : P.xl[i + u + 1];
+                ff_mac(h0, l0, xv[u], yh0, yl0);
+                ff_mac(h1, l1, xv[u + 1], yh1, yl1);
+            }
         }
-        ff_mac(h0, l0, xv[0], yh[0], yl[0]);
-        ff_mac(h1, l1, xv[1], yh[1], yl[1]);
-        ff_mac(h2, l2, xv[2], yh[2], yl[2]);
-        ff_mac(h3, l3, xv[3], yh[3], yl[3]);
-        ff_mac(h0, l0, xv[4], yh[4], yl[4]);
-        ff_mac(h1, l1, xv[5], yh[5], yl[5]);
-        ff_mac(h2, l2, xv[6], yh[6], yl[6]);
-        ff_mac(h3, l3, xv[7], yh[7], yl[7]);
+        for (; i < i1; ++i) {
+            const float yh = i < 1024 ? s_xh[i] : P.xh[i], yl = i < 1024 ? s_xl[i] : P.xl[i];
+            ff_mac(h0, l0, __ldg(col + (size_t)i * P.L), yh, yl);
+        }
+        ff_add(h0, l0, h1, l1);
     }
-    for (; i < P.d; ++i) {
-        const float yh = i < 1024 ? s_xh[i] : P.xh[i], yl = i < 1024 ? s_xl[i] : P.xl[i];
-        ff_mac(h0, l0, __ldg(col + (size_t)i * P.L), yh, yl);
-    }
-    ff_add(h0, l0, h1, l1);
-    ff_add(h2, l2, h3, l3);
-    ff_add(h0, l0, h2, l2);
-    const float hi = h0, lo = l0;
+    s_ph[q][sx] = h0;
+    s_pl[q][sx] = l0;
+    __syncthreads();
+    if (q != 0 || s >= n) return;
+    float hi = s_ph[0][sx], lo = s_pl[0][sx];
+#pragma unroll
+    for (int t = 1; t < 4; ++t) ff_add(hi, lo, s_ph[t][sx], s_pl[t][sx]);
     const double b = P.lab[(size_t)c * P.L + s];
     const double m = b * ((double)hi + (double)lo);
     const double sig = mx_sigmoid(m);
     const double inv_n = 1.0 / (double)n;
     const double z1 = 1.0 - sig;
     P.Dw[(size_t)c * P.L + s] = (float)(inv_n * (z1 * sig));
-    const double q = b * (z1 * -inv_n);
-    split_ff(q, P.qh[(size_t)c * P.L + s], P.ql[(size_t)c * P.L + s]);
+    const double qv = b * (z1 * -inv_n);
+    split_ff(qv, P.qh[(size_t)c * P.L + s], P.ql[(size_t)c * P.L + s]);
 }
 
 // client gradients: one warp per (client, feature), lanes over the samples

@@ -23,6 +23,10 @@ IDENTITY, RANDK, TOPK, RANDSEQK, TOPLEK, NATURAL, RANDK_PHILOX = 0, 1, 2, 3, 4, 
 COMPRESSORS = {"identity": IDENTITY, "randk": RANDK, "topk": TOPK, "randseqk": RANDSEQK,
                "seqk": RANDSEQK, "toplek": TOPLEK, "natural": NATURAL, "randk_philox": RANDK_PHILOX}
 STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTPD", -5: "ETIMEOUT", -6: "ENODEV"}
+# Newton solves of the mixed-precision form: FP64 cooperative Cholesky; FP32 Cholesky in one CTA's
+# shared memory with one refinement step (d up to about 300); FP32 Cholesky on a cooperative grid
+# with FP64-residual refinement to 2^-30 relative, six steps at most (d up to 1344)
+SOLVERS = {"fp64": 0, "fp32_refined": 1, "fp32_coop": 2}
 
 
 class FedNLError(RuntimeError):
@@ -64,7 +68,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_solve_batch", "fednl_gpu_round_result", "fednl_mx_round_result", "fednl_gpu_mem_info",
            "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
-           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed",
+           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
            "fednl_gpu_autotune", "fednl_mx_autotune"]
 
@@ -107,6 +111,7 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_logreg_oracle": [dp, dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, dp, dp, dp],
         "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
         "fednl_gpu_optionb_solve_mixed": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
+        "fednl_gpu_optionb_solve32": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp, C.c_int32, C.c_int32],
         "fednl_gpu_optionb_solve_noalloc": [vp, C.c_int32, C.c_int32, C.c_double, vp, vp, vp],
         "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
         "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
@@ -247,6 +252,16 @@ def cholesky_option_b_solve_mixed(H: np.ndarray, d: int, lda: int, l: float, g: 
     gc = np.ascontiguousarray(g, dtype=np.float64)
     dx = np.empty(d)
     _check(load().fednl_gpu_optionb_solve_mixed(_dp(Hc), d, lda, float(l), _dp(gc), _dp(dx)))
+    return dx
+
+
+def cholesky_option_b_solve32(H: np.ndarray, d: int, lda: int, l: float, g: np.ndarray, refine: int = 6,
+                              grid: int = 0) -> np.ndarray:
+    """(H + l I) dx = g with the FP32 cooperative factor and FP64 refinement (mixed solver 2)."""
+    Hc = np.ascontiguousarray(H, dtype=np.float64)
+    gc = np.ascontiguousarray(g, dtype=np.float64)
+    dx = np.empty(d)
+    _check(load().fednl_gpu_optionb_solve32(_dp(Hc), d, lda, float(l), _dp(gc), _dp(dx), int(refine), int(grid)))
     return dx
 
 
@@ -496,7 +511,7 @@ class MixedFedNL:
             _check(load().fednl_mx_upload_client_data(self._h, f.ctypes.data_as(C.POINTER(C.c_float)), _dp(b)))
             xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
             _check(load().fednl_mx_init_shifts(self._h, _dp(xx) if xx is not None else None))
-            _check(load().fednl_mx_set_solver(self._h, {"fp64": 0, "fp32_refined": 1}[solver]))
+            _check(load().fednl_mx_set_solver(self._h, SOLVERS[solver]))
         except Exception:
             self.close()
             raise
@@ -518,13 +533,13 @@ class MixedFedNL:
         return out
 
     def autotune(self) -> dict:
-        """Measures the solve (FP64 cooperative CTA count; FP32 shared-memory solver where it fits)
-        on this problem's current system and keeps the fastest."""
+        """Measures the solves (the FP64 and FP32 cooperative solves over CTA counts; the FP32
+        shared-memory solve where it fits) on this problem's current system and keeps the fastest."""
         sv = np.zeros(1, dtype=np.int32)
         g = np.zeros(1, dtype=np.int32)
         ms = np.zeros(1)
         _check(load().fednl_mx_autotune(self._h, _ip(sv), _ip(g), _dp(ms)))
-        return {"solver": ["fp64", "fp32_refined"][int(sv[0])], "chol_ctas": int(g[0]), "solve_ms": float(ms[0])}
+        return {"solver": list(SOLVERS)[int(sv[0])], "chol_ctas": int(g[0]), "solve_ms": float(ms[0])}
 
     def client_phase(self):
         _check(load().fednl_mx_client_phase(self._h))
