@@ -197,8 +197,10 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
 int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
 /* The same system by the FP32 Cholesky on a cooperative grid (fednl_mx_set_solver 2): at most
  * `refine` FP64-residual refinement steps (0..8; they stop once a correction is at most 2^-30 of the
- * solution), `grid` CTAs (0: one per tile of the first trailing update),
- * d up to 1344.  A pivot that loses more than 18 bits in FP32 hands the system to the FP64 solve,
+ * solution), `grid` CTAs of a cooperative launch, or -n for one thread-block cluster of n <= 16 CTAs
+ * synchronised by the cluster barrier (0: a cluster of 16 up to d = 512, else one CTA per tile of the
+ * first trailing update),
+ * d up to 1312.  A pivot that loses more than 18 bits in FP32 hands the system to the FP64 solve,
  * which returns FEDNL_ENOTPD for a matrix that is not positive definite.  Host buffers. */
 int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
                               int32_t refine, int32_t grid);
@@ -261,7 +263,7 @@ double fednl_mx_get_l(fednl_mx_handle h);
 /* Newton solve of the round: 0 = FP64 cooperative Cholesky (default), 1 = FP32 Cholesky in one CTA's
  * shared memory with one refinement step on a float-float residual (d up to about 300), 2 = FP32
  * Cholesky on a cooperative grid with FP64-residual refinement until the correction is at most 2^-30
- * of the solution, six steps at most (d up to 1344; a pivot that loses more than 18 bits in FP32
+ * of the solution, six steps at most (d up to 1312; a pivot that loses more than 18 bits in FP32
  * hands the system to the FP64 solve in the same launch) */
 int fednl_mx_set_solver(fednl_mx_handle h, int32_t solver);
 /* the last round's FP32 differences H_c - shift_c (packed upper, [U]; RandK-Philox: only the

@@ -13,7 +13,8 @@
 //      A22 -= L21 L21^T is split over the CTAs in 32 x 32 tiles; one grid barrier per panel.  The
 //      CTA that owns the panel also writes the inverse of the diagonal block (for the solves).
 //   3. L L^T e = r in FP32 by CTA 0 (blocks of 32: a GEMV over the finished part, then the
-//      block's inverse), dx += e in FP64, r = g - (H + l I) dx in FP64 by all CTAs, repeated until
+//      block's inverse), dx += e in FP64, r = g - (H + l I) dx by all CTAs (float-float on H held
+//      as FP32 pairs, about 2^-44 relative), repeated until
 //      ||e|| <= tol ||dx||, or the next correction is predicted below that (||e||^2 / ||e_prev||),
 //      or after `refine` corrections; x -= dx.
 // Every CTA makes the same pivot decisions (same data, same arithmetic), so a failed FP32 pivot
@@ -25,7 +26,7 @@ namespace fednl {
 
 constexpr int kC32Stride = 36;      // floats per panel row in shared memory: 16-byte rows, and the
                                     // float4 reads of 8 consecutive rows fall in distinct banks
-constexpr int kC32MaxD = 1344;      // panel rows beside the FP64 solve's static shared memory
+constexpr int kC32MaxD = 1312;      // panel rows beside the FP64 solve's static shared memory
 
 struct Chol32c {
     float* A;          // [ld][ld] row-major; the lower triangle ends as the factor L (A = L L^T)
@@ -33,21 +34,28 @@ struct Chol32c {
     float* linv;       // [ld / 32][32][32] inverses of the diagonal blocks, row-major
     double* r;         // [d] residual (FP64)
     double* acc;       // [d] solution being accumulated (FP64)
+    float* accp;       // [2][d] the same as FP32 pairs (hi, lo), for the float-float residual
+    const float* hh;   // H as FP32 pairs (about 2^-48 relative), packed upper column-major (hh + hl)
+    const float* hl;   // and row-major (rh + rl)
+    const float* rh;
+    const float* rl;
     int* flag;         // CTA 0's stop decision, read by every CTA after a grid barrier
     int ld;            // d rounded up to 32
     int refine;        // at most this many refinement steps after the first solve
     float tol;         // stop when the correction is at most tol of the solution (2-norms)
     int resident;      // CTA 0 keeps the factor in shared memory for the solves
     int smem_floats;   // dynamic shared memory of the launch, in floats
+    int cluster;       // the launch is one thread-block cluster (cluster barriers)
 };
 
 __host__ __device__ inline int c32c_ld(int d) { return (d + 31) & ~31; }
 
 // Dynamic shared memory, in floats: a fixed head (the factored diagonal block [32][36], the solve
-// vector [ld], reduction scratch [8][32] and [32]); in resident mode the factor's rows below the
+// vector [ld], reduction scratch [8][32] and [32], the first trailing-update tile's entries of A
+// [256][4], fetched while the panel is factored); in resident mode the factor's rows below the
 // diagonal blocks, column block after column block ([rows][32], filled by CTA 0 as the panels are
 // factored); and at the very end the current panel ([32 + rows below rounded up to 32][36]).
-__host__ __device__ inline int c32c_head_floats(int d) { return 32 * kC32Stride + c32c_ld(d) + 8 * 32 + 32; }
+__host__ __device__ inline int c32c_head_floats(int d) { return 32 * kC32Stride + c32c_ld(d) + 8 * 32 + 32 + 1024; }
 constexpr int kC32ResBlocks = 10;   // resident mode: at most 10 column blocks (d <= 320), whose
                                     // diagonal-block inverses the solves hold in registers
 __host__ __device__ inline int c32c_rows_below(int d, int b)
@@ -76,45 +84,62 @@ __host__ __device__ inline size_t c32c_smem_bytes(int d, bool resident)
     return ((size_t)c32c_head_floats(d) + need) * 4;
 }
 
-// Warp: lane i holds row i of the diagonal block (a[j] = A_ij for j <= i, zero above and on lanes
-// >= nb), dref its diagonal before the factorisation.  On return column k of the factor is in
+// Warp: lane i holds row i of the diagonal block (a[j] = A_ij for j <= i, zero above; a block of
+// nb < 32 rows is padded with rows of the identity, which factor to themselves and leave the others
+// alone), dref its diagonal before the factorisation.  On return column k of the factor is in
 // Lbt[k * kC32Stride + i] (i >= k) and 1 / L_kk in s_rinv[k]; false if a pivot fell to 2^-18 of its
 // original value or below (or is NaN): fewer than six bits of it would be left in FP32, and the
 // FP64 solve takes over.
-// Step k: every lane scales its entry of column k by 1 / sqrt(pivot) and stores it; the entry of
-// row k + 1 (needed first) comes by a shuffle and the rest of the column is read back as float4
-// broadcasts for the rank-1 update.  The next pivot is formed on its own (each lane as if it were
-// row k + 1) and shuffled from lane k + 1, so the chain from one pivot to the next is one multiply,
-// one fma, one shuffle and one rsqrt.
-__device__ __forceinline__ bool c32c_factor_diag(float (&a)[32], int nb, float dref, float* Lbt, float* s_rinv)
+// Step k: 1 / sqrt(pivot), every lane scales its entry of column k; the entries of rows k + 1 and
+// k + 2 of the column come by shuffles (the next pivot, formed by each lane as if it were row k + 1,
+// is shuffled from lane k + 1), so the chain from one pivot to the next is a multiply, an fma, a
+// shuffle and an rsqrt.  The column is also stored, and its update of rows k + 3 .. 31 is applied
+// one step later from shared memory (loaded at the start of that step), off the chain.
+__device__ __forceinline__ float c32c_rsqrt(float x)
+{
+    float r;   // the MUFU approximation; pivots reaching it are above 2^-100 (never subnormal)
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ bool c32c_factor_diag(float (&a)[32], float dref, float* Lbt, float* s_rinv)
 {
     const int lane = threadIdx.x & 31;
-    const float thr = 0x1p-18f * dref;
+    const float thr = fmaxf(0x1p-18f * dref, 0x1p-100f);
     bool bad = false;
     float piv = __shfl_sync(0xffffffffu, a[0], 0);
+    float lprev = 0.0f;                               // this lane's entry of column k - 1
 #pragma unroll
     for (int k = 0; k < 32; ++k) {
-        if (k < nb) {
+        {
+            float4 cp[8];                             // column k - 1, rows 4 q .. 4 q + 3
+            if (k >= 1) {
+#pragma unroll
+                for (int q = (k + 2) / 4; q < 8; ++q)
+                    cp[q] = reinterpret_cast<const float4*>(Lbt + (k - 1) * kC32Stride)[q];
+            }
             bad |= lane == k && !(a[k] > thr);
-            const float rk = rsqrtf(piv);
+            const float rk = c32c_rsqrt(piv);
             const float lik = a[k] * rk;          // lane k: sqrt(pivot); lanes below: L_ik
             a[k] = lik;
             if (k + 1 < 32) {
                 piv = __shfl_sync(0xffffffffu, fmaf(-lik, lik, a[k + 1]), k + 1);
                 a[k + 1] = fmaf(-lik, __shfl_sync(0xffffffffu, lik, k + 1), a[k + 1]);
             }
+            if (k + 2 < 32) a[k + 2] = fmaf(-lik, __shfl_sync(0xffffffffu, lik, k + 2), a[k + 2]);
+            if (k >= 1) {                         // column k - 1 on rows k + 2 .. 31
+#pragma unroll
+                for (int q = (k + 2) / 4; q < 8; ++q) {
+                    if (4 * q + 0 >= k + 2) a[4 * q + 0] = fmaf(-lprev, cp[q].x, a[4 * q + 0]);
+                    if (4 * q + 1 >= k + 2) a[4 * q + 1] = fmaf(-lprev, cp[q].y, a[4 * q + 1]);
+                    if (4 * q + 2 >= k + 2) a[4 * q + 2] = fmaf(-lprev, cp[q].z, a[4 * q + 2]);
+                    if (4 * q + 3 >= k + 2) a[4 * q + 3] = fmaf(-lprev, cp[q].w, a[4 * q + 3]);
+                }
+            }
             Lbt[k * kC32Stride + lane] = lik;
             if (lane == k) s_rinv[k] = rk;
+            lprev = lik;
             __syncwarp();
-            const float4* col = reinterpret_cast<const float4*>(Lbt + k * kC32Stride);
-#pragma unroll
-            for (int q = (k + 2) / 4; q < 8; ++q) {
-                const float4 c = col[q];
-                if (4 * q + 0 > k + 1) a[4 * q + 0] = fmaf(-lik, c.x, a[4 * q + 0]);
-                if (4 * q + 1 > k + 1) a[4 * q + 1] = fmaf(-lik, c.y, a[4 * q + 1]);
-                if (4 * q + 2 > k + 1) a[4 * q + 2] = fmaf(-lik, c.z, a[4 * q + 2]);
-                if (4 * q + 3 > k + 1) a[4 * q + 3] = fmaf(-lik, c.w, a[4 * q + 3]);
-            }
         }
     }
     return !__any_sync(0xffffffffu, bad);
@@ -309,6 +334,24 @@ __device__ __forceinline__ void c32c_backward_res(const float* st, const float4 
     }
 }
 
+// float-float accumulation (Dekker / Knuth two-sum, unnormalised low part): hi + lo += p + e
+__device__ __forceinline__ void c32c_ff_add(float& hi, float& lo, float p, float e)
+{
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+
+// hi + lo += (ah + al) (bh + bl): the exact product of the high parts plus the cross terms
+__device__ __forceinline__ void c32c_ff_mac(float& hi, float& lo, float ah, float al, float bh, float bl)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float e = __fadd_rn(fmaf(ah, bh, -p), fmaf(ah, bl, __fmul_rn(al, bh)));
+    c32c_ff_add(hi, lo, p, e);
+}
+
 __device__ __forceinline__ void c32c_timeout(const Dev& P, unsigned bid, int record)
 {
     if (bid == 0 && threadIdx.x == 0) {
@@ -329,19 +372,21 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
     float* v = Lbt + 32 * kC32Stride;
     float* s_part = v + ld;
     float* s_t = s_part + 8 * 32;
-    float* st = s_t + 32;                       // resident factor (CTA 0, resident mode)
+    float* s_pre = s_t + 32;                    // [256][4]
+    float* st = s_pre + 1024;                   // resident factor (CTA 0, resident mode)
     float* const top = sm + C.smem_floats;
     __shared__ float s_rinv[32];
     __shared__ int s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const double l = *lptr;
 
-    // 1. A = lower(H) + l I, one warp per row over the grid
+    // 1. A = lower(H) + l I, one warp per row over the grid (from the FP32 high parts)
+    const float lf = (float)l;
     for (int i = (int)bid * 8 + warp; i < d; i += (int)G * 8) {
-        const double* col = H + (size_t)i * (i + 1) / 2;
+        const size_t c0i = (size_t)i * (i + 1) / 2;
         float* row = C.A + (size_t)i * ld;
         for (int j = lane; j <= i; j += 32) {
-            const float a = (float)(j == i ? col[j] + l : col[j]);
+            const float a = j == i ? C.hh[c0i + j] + lf : C.hh[c0i + j];
             row[j] = a;
             if (j == i) C.diag0[i] = a;
         }
@@ -366,6 +411,23 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
             *reinterpret_cast<float4*>(Ls + r * kC32Stride + 4 * q) = val;
         }
         const float dref = (warp == 0 && lane < nb) ? C.diag0[c0 + lane] : 1.0f;
+        // this CTA's first tile of the trailing update: its four entries of A per thread, fetched
+        // now (asynchronously) so that the update itself only computes and stores
+        const int nt = mp / 32, ntiles = nt * (nt + 1) / 2, ty = tid >> 3, tx = tid & 7;
+        int ti = 0, tj = (int)bid;
+        while (ti < nt && tj > ti) {
+            tj -= ti + 1;
+            ++ti;
+        }
+        if ((int)bid < ntiles) {
+            const float* arow = C.A + (size_t)(c1 + ti * 32 + ty) * ld + c1 + tj * 32 + tx;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t sa = (uint32_t)__cvta_generic_to_shared(s_pre + tid * 4 + u);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(arow + 8 * u) : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        }
         __syncthreads();
         if (warp == 0) {
             float a[32];
@@ -380,12 +442,9 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
             }
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-                if (j > lane || lane >= nb) a[j] = 0.0f;
-            if (nb < 32) {        // the last block: zero columns and pivots beyond it
-                for (int k = nb; k < 32; ++k) Lbt[k * kC32Stride + lane] = 0.0f;
-                if (lane >= nb) s_rinv[lane] = 0.0f;
-            }
-            const bool ok = c32c_factor_diag(a, nb, dref, Lbt, s_rinv);
+                if (lane >= nb) a[j] = j == lane ? 1.0f : 0.0f;
+                else if (j > lane) a[j] = 0.0f;
+            const bool ok = c32c_factor_diag(a, dref, Lbt, s_rinv);
             if (lane == 0 && !ok) s_fail = 1;
         }
         __syncthreads();
@@ -434,12 +493,7 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
         // trailing update A22 -= L21 L21^T over lower 32 x 32 tiles (ti, tj), tj <= ti; thread
         // (row ty, columns tx + 8 q)
         {
-            const int nt = mp / 32, ntiles = nt * (nt + 1) / 2, ty = tid >> 3, tx = tid & 7;
-            int ti = 0, tj = (int)bid;
-            while (ti < nt && tj > ti) {
-                tj -= ti + 1;
-                ++ti;
-            }
+            asm volatile("cp.async.wait_all;" ::: "memory");
             for (int t = (int)bid; t < ntiles; t += (int)G) {
                 const float4* ri = reinterpret_cast<const float4*>(Lp + (ti * 32 + ty) * kC32Stride);
                 float xr[32];
@@ -467,8 +521,13 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
                     acc[u] = s;
                 }
                 float* arow = C.A + (size_t)(c1 + ti * 32 + ty) * ld + c1 + tj * 32 + tx;
+                if (t == (int)bid) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) arow[8 * u] -= acc[u];
+                    for (int u = 0; u < 4; ++u) arow[8 * u] = s_pre[tid * 4 + u] - acc[u];
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) arow[8 * u] -= acc[u];
+                }
                 // next tile of this CTA
                 tj += (int)G;
                 while (ti < nt && tj > ti) {
@@ -481,6 +540,7 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
     }
     __syncthreads();
     if (s_fail) {                 // an FP32 pivot was not positive: the FP64 solve decides
+        asm volatile("cp.async.wait_all;" ::: "memory");
         chol_body(P, H, 0, lptr, 0.0, g, dxout, xupd, record, G, bid, gs);
         return;
     }
@@ -512,6 +572,9 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
             for (int i = tid; i < d; i += kCoopThreads) {
                 const double e = (double)v[i], a = (it == 0 ? 0.0 : C.acc[i]) + e;
                 C.acc[i] = a;
+                const float ah = (float)a;
+                C.accp[i] = ah;
+                C.accp[d + i] = (float)(a - (double)ah);
                 en = fma(e, e, en);
                 an = fma(a, a, an);
             }
@@ -540,13 +603,18 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
         if (it >= C.refine) break;
         if (!gs.sync()) return c32c_timeout(P, bid, record);
         if (*(volatile int*)C.flag) break;
+        // residual in float-float on the FP32 pairs (the FP32 pipes run 64x the FP64 one)
         for (int i = (int)bid * 8 + warp; i < d; i += (int)G * 8) {
-            const double* col = H + (size_t)i * (i + 1) / 2;
-            double s = 0.0;
-            for (int j = lane; j <= i; j += 32) s = fma(col[j], C.acc[j], s);
-            for (int j = i + 1 + lane; j < d; j += 32) s = fma(H[(size_t)j * (j + 1) / 2 + i], C.acc[j], s);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) C.r[i] = g[i] - fma(l, C.acc[i], s);
+            const size_t c0i = (size_t)i * (i + 1) / 2, r0i = (size_t)i * d - (size_t)i * (i - 1) / 2;
+            float sh = 0.0f, sl = 0.0f;
+            for (int j = lane; j <= i; j += 32) c32c_ff_mac(sh, sl, C.hh[c0i + j], C.hl[c0i + j], C.accp[j], C.accp[d + j]);
+            for (int j = i + 1 + lane; j < d; j += 32)
+                c32c_ff_mac(sh, sl, C.rh[r0i + j - i], C.rl[r0i + j - i], C.accp[j], C.accp[d + j]);
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, sh, o), ol = __shfl_xor_sync(0xffffffffu, sl, o);
+                c32c_ff_add(sh, sl, oh, ol);
+            }
+            if (lane == 0) C.r[i] = g[i] - fma(l, C.acc[i], (double)sh + (double)sl);
         }
         if (!gs.sync()) return c32c_timeout(P, bid, record);
     }
@@ -575,11 +643,27 @@ __device__ __forceinline__ void chol32c_body(const Dev& P, const Chol32c& C, con
     }
 }
 
+// H (packed upper, column-major) as FP32 pairs in column-major and row-major packed order
+__global__ void k_split_pairs(const double* __restrict__ H, int d, float* hh, float* hl, float* rh, float* rl)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long long)d * (d + 1) / 2) return;
+    int i, j;
+    upper_ij((int)p, i, j);
+    const double h = H[p];
+    const float a = (float)h, b = (float)(h - (double)a);
+    hh[p] = a;
+    hl[p] = b;
+    const size_t r = (size_t)i * d - (size_t)i * (i - 1) / 2 + j - i;
+    rh[r] = a;
+    rl[r] = b;
+}
+
 __global__ void __launch_bounds__(kCoopThreads, 1) k_chol32c(Dev P, Chol32c C, const double* __restrict__ H,
                                                           const double* lptr, const double* __restrict__ g,
                                                           double* dxout, double* xupd, int record)
 {
-    GridSync gs(P.bar, gridDim.x);
+    GridSync gs(P.bar, gridDim.x, C.cluster != 0);
     chol32c_body(P, C, H, lptr, g, dxout, xupd, record, gridDim.x, blockIdx.x, gs);
     gs.finish();
 }

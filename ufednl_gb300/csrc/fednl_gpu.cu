@@ -279,9 +279,47 @@ int chol32c_cap(int d)
     return std::min(sms, sms * bps);
 }
 
-// default CTA count: one per 32 x 32 tile of the first trailing update, within the resident limit
+// whether one cluster of n CTAs of k_chol32c can be resident for dimension d
+bool chol32c_cluster_ok(int d, int n)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, bool> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find({d, n});
+    if (it != cache.end()) return it->second;
+    bool ok = false;
+    int res = 0;
+    const size_t smem = chol32c_smem(d, &res);
+    if (fednl_raise_dyn_smem((const void*)k_chol32c, smem) == cudaSuccess &&
+        (n <= 8 || cudaFuncSetAttribute(k_chol32c, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(n);
+        cfg.blockDim = dim3(kCoopThreads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = n;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        ok = cudaOccupancyMaxActiveClusters(&clusters, k_chol32c, &cfg) == cudaSuccess && clusters >= 1;
+    }
+    cudaGetLastError();
+    cache[{d, n}] = ok;
+    return ok;
+}
+
+// default launch: one cluster of 16 CTAs while the trailing updates are small (d up to 512), else
+// one CTA per 32 x 32 tile of the first trailing update within the resident limit (a negative
+// value -n stands for one cluster of n CTAs)
 int chol32c_grid(int d)
 {
+    if (d <= 512) {
+        if (chol32c_cluster_ok(d, 16)) return -16;
+        if (chol32c_cluster_ok(d, 8)) return -8;
+    }
     const long long nt = d > 32 ? (d - 32 + 31) / 32 : 1;
     return (int)std::max<long long>(1, std::min<long long>(nt * (nt + 1) / 2, chol32c_cap(d)));
 }
@@ -293,7 +331,7 @@ int fednl_solve32_max_d() { return kC32MaxD; }
 size_t fednl_solve32_bytes(int d)
 {
     const size_t ld = (size_t)c32c_ld(d);
-    return ld * ld * 4 + (size_t)d * 4 + ld * 32 * 4 + 2 * (size_t)d * 8 + 4;
+    return ld * ld * 4 + (size_t)d * 4 + ld * 32 * 4 + 2 * (size_t)d * 8 + 2 * (size_t)d * 4 + 4;
 }
 
 int fednl_device_optionb_solve32(const FednlSolveDesc& S, const FednlSolve32& E, cudaStream_t st, int grid)
@@ -314,19 +352,29 @@ int fednl_device_optionb_solve32(const FednlSolveDesc& S, const FednlSolve32& E,
     P.hist_cap = S.hist_cap;
     int res = 0;
     const size_t smem = chol32c_smem(S.d, &res);
-    Chol32c C{E.a, E.diag0, E.linv, E.r, E.acc, E.flag, c32c_ld(S.d), E.refine, E.tol, res, (int)(smem / 4)};
     const int cap = chol32c_cap(S.d);
     if (cap < 1) return FEDNL_ECUDA;
-    if (grid <= 0) grid = chol32c_grid(S.d);
-    grid = std::min(grid, cap);
+    if (grid == 0) grid = chol32c_grid(S.d);
+    const bool cl = grid < 0;
+    if (cl && !chol32c_cluster_ok(S.d, -grid)) return FEDNL_EINVAL;
+    grid = cl ? -grid : std::min(grid, cap);
+    Chol32c C{E.a,  E.diag0, E.linv, E.r,     E.acc,   E.accp, E.hh, E.hl,         E.rh,
+              E.rl, E.flag,  c32c_ld(S.d), E.refine, E.tol, res,    (int)(smem / 4), cl ? 1 : 0};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kCoopThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
+    if (cl) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = grid;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+    } else {
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+    }
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     CK(cudaLaunchKernelEx(&cfg, k_chol32c, P, C, S.H, S.lptr, S.g, S.dx, S.xupd, S.record));
@@ -338,7 +386,7 @@ int fednl_device_optionb_solve32(const FednlSolveDesc& S, const FednlSolve32& E,
 // handle's current H, l and g into scratch outputs: nothing of the run changes) and cached
 // process-wide per solver kind, so later handles of the same d reuse the choice.
 static int tune_grid(int kind, int d, int cap, int dflt, const std::function<int(int)>& launch, cudaStream_t st,
-                     int* best_grid, double* best_ms)
+                     int* best_grid, double* best_ms, const std::vector<int>& extra = {})
 {
     static std::mutex mu;
     static std::map<std::pair<int, int>, std::pair<int, double>> cache;
@@ -353,15 +401,16 @@ static int tune_grid(int kind, int d, int cap, int dflt, const std::function<int
     }
     if (cap < 1) return FEDNL_ECUDA;
     std::vector<int> cand = {8, 16, 24, 32, 48, 64, 96, 128, cap, dflt};
+    cand.insert(cand.end(), extra.begin(), extra.end());
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int bg = std::min(dflt, cap);
+    int bg = dflt > 0 ? std::min(dflt, cap) : dflt;
     double bm = 1e30;
     for (int G : cand) {
-        if (G < 1 || G > cap) continue;
+        if (G == 0 || G > cap || (G < 0 && std::find(extra.begin(), extra.end(), G) == extra.end())) continue;
         int rc = launch(G);                                   // warm
         if (rc) return rc;
         float best = 1e30f;
@@ -401,7 +450,10 @@ int fednl_tune_chol_grid(int d, const std::function<int(int)>& launch, cudaStrea
 int fednl_tune_chol32_grid(int d, const std::function<int(int)>& launch, cudaStream_t st, int* best_grid,
                            double* best_ms)
 {
-    return tune_grid(1, d, chol32c_cap(d), chol32c_grid(d), launch, st, best_grid, best_ms);
+    std::vector<int> extra;
+    for (int n : {8, 16})
+        if (chol32c_cluster_ok(d, n)) extra.push_back(-n);
+    return tune_grid(1, d, chol32c_cap(d), chol32c_grid(d), launch, st, best_grid, best_ms, extra);
 }
 
 struct fednl_handle_s {
@@ -1741,7 +1793,7 @@ int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l,
 {
     int rc = ensure_device();
     if (rc) return rc;
-    if (!H || !g || !dx || d < 1 || lda < d || refine < 0 || refine > 8 || grid < 0) return fail(FEDNL_EINVAL, "bad argument");
+    if (!H || !g || !dx || d < 1 || lda < d || refine < 0 || refine > 8 || grid < -16) return fail(FEDNL_EINVAL, "bad argument");
     if (d > kC32MaxD) return fail(FEDNL_EINVAL, "d %d above the FP32 cooperative solve's limit %d", d, kC32MaxD);
     long long U = (long long)d * (d + 1) / 2;
     const size_t ld = (size_t)c32c_ld(d);
@@ -1767,7 +1819,13 @@ int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l,
     s.a.want(&E.linv, ld * 32);
     s.a.want(&E.r, d);
     s.a.want(&E.acc, d);
+    s.a.want(&E.accp, 2 * (size_t)d);
     s.a.want(&E.flag, 1);
+    float *phh, *phl, *prh, *prl;
+    s.a.want(&phh, U);
+    s.a.want(&phl, U);
+    s.a.want(&prh, U);
+    s.a.want(&prl, U);
     rc = s.a.commit();
     if (rc) return rc;
     E.refine = refine;
@@ -1779,7 +1837,12 @@ int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l,
     CK(cudaMemcpyAsync(dl, &l, 8, cudaMemcpyHostToDevice, s.st));
     k_pack_upper<<<dim3((unsigned)std::min<long long>(1024, (U + 255) / 256), 1), 256, 0, s.st>>>(dfull, d, lda, (int)U,
                                                                                                 (int)U, dpack);
+    k_split_pairs<<<(unsigned)((U + 255) / 256), 256, 0, s.st>>>(dpack, d, phh, phl, prh, prl);
     CKL();
+    E.hh = phh;
+    E.hl = phl;
+    E.rh = prh;
+    E.rl = prl;
     FednlSolveDesc S{};
     S.H = dpack;
     S.d = d;

@@ -1295,15 +1295,23 @@ constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIM
 // loads: no counter is reset between barriers.  Every CTA calls finish() once after its last
 // barrier; the last one to do so returns both counters to zero for the next launch.  sync() returns
 // false (error flag set) when the other CTAs did not arrive in time.
+// A launch that is one thread-block cluster uses the cluster's hardware barrier instead (every
+// thread of every CTA arrives with release and waits with acquire semantics; the callers' control
+// flow is the same in every CTA, so every barrier is reached by all of them).
 struct GridSync {
     unsigned* bar;
     unsigned n;
+    bool cluster;
     unsigned epoch = 0;        // barriers this CTA has passed (kept by thread 0)
 
-    __device__ GridSync(unsigned* b, unsigned nblk) : bar(b), n(nblk) {}
+    __device__ GridSync(unsigned* b, unsigned nblk, bool in_cluster = false) : bar(b), n(nblk), cluster(in_cluster) {}
 
     __device__ bool sync()
     {
+        if (cluster) {
+            asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+            return true;
+        }
         __shared__ int s_ok;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1338,6 +1346,7 @@ struct GridSync {
 
     __device__ void finish()
     {
+        if (cluster) return;
         __syncthreads();
         if (threadIdx.x == 0 && atomicAdd(bar + 1, 1u) == n - 1) {
             atomicExch(bar, 0u);

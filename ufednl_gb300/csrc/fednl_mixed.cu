@@ -448,6 +448,11 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
         rc |= h->alloc(&h->s32.linv, ld * 32);
         rc |= h->alloc(&h->s32.r, h->d);
         rc |= h->alloc(&h->s32.acc, h->d);
+        rc |= h->alloc(&h->s32.accp, 2 * (size_t)h->d);
+        h->s32.hh = P.Hh;
+        h->s32.hl = P.Hl;
+        h->s32.rh = P.Hrh;
+        h->s32.rl = P.Hrl;
         rc |= h->alloc(&h->s32.flag, 1);
         h->s32.refine = 6;
         h->s32.tol = 0x1p-30f;

@@ -43,6 +43,11 @@ struct FednlSolve32 {
     float* linv;           // [ld][32]
     double* r;             // [d]
     double* acc;           // [d]
+    float* accp;           // [2 d]
+    const float* hh;       // H as FP32 pairs, packed upper column-major (hh, hl) and row-major
+    const float* hl;       // (rh, rl): the FP32 load of the system and the float-float residual
+    const float* rh;
+    const float* rl;
     int* flag;             // [1]
     int refine;            // at most this many refinement steps after the first solve
     float tol;             // stop refining when the correction is at most tol of the solution

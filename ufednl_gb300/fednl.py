@@ -25,7 +25,7 @@ COMPRESSORS = {"identity": IDENTITY, "randk": RANDK, "topk": TOPK, "randseqk": R
 STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTPD", -5: "ETIMEOUT", -6: "ENODEV"}
 # Newton solves of the mixed-precision form: FP64 cooperative Cholesky; FP32 Cholesky in one CTA's
 # shared memory with one refinement step (d up to about 300); FP32 Cholesky on a cooperative grid
-# with FP64-residual refinement to 2^-30 relative, six steps at most (d up to 1344)
+# with FP64-residual refinement to 2^-30 relative, six steps at most (d up to 1312)
 SOLVERS = {"fp64": 0, "fp32_refined": 1, "fp32_coop": 2}
 
 
