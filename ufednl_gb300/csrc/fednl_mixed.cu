@@ -519,7 +519,7 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     if (h->comp == FEDNL_TOPLEK && h->k < h->U) {     // TopLEK sorts its kept set in shared memory
         int kp = 1;
         while (kp < h->k) kp <<= 1;
-        h->select_smem = (size_t)kp * 8;
+        h->select_smem = ((size_t)std::max(kp, fednl_tc::kSelThreads) + 2048) * 8;
         if (fednl_raise_dyn_smem((const void*)fednl_tc::k_mx_select, h->select_smem) != cudaSuccess) {
             fednl_mx_destroy(h);
             return fail_m(FEDNL_ECUDA, "shared-memory attribute refused");

@@ -604,30 +604,33 @@ __device__ __forceinline__ unsigned block_scan_u32(unsigned v, unsigned* s_w, un
     return r;
 }
 
-__device__ __forceinline__ double block_scan_f64(double v, double* s_w, double* tot)
+// inclusive float-float scan over the block (1024 threads); total in (*th, *tl)
+__device__ __forceinline__ void block_scan_ff(float& h, float& l, float2* s_w, float* th, float* tl)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += t;
+        const float uh = __shfl_up_sync(0xffffffffu, h, o), ul = __shfl_up_sync(0xffffffffu, l, o);
+        if (lane >= o) ff_add(h, l, uh, ul);
     }
-    if (lane == 31) s_w[warp] = v;
+    if (lane == 31) s_w[warp] = make_float2(h, l);
     __syncthreads();
     if (warp == 0) {
-        double w = s_w[lane];
+        float wh = s_w[lane].x, wl = s_w[lane].y;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const double t = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += t;
+            const float uh = __shfl_up_sync(0xffffffffu, wh, o), ul = __shfl_up_sync(0xffffffffu, wl, o);
+            if (lane >= o) ff_add(wh, wl, uh, ul);
         }
-        s_w[lane] = w;
+        s_w[lane] = make_float2(wh, wl);
     }
     __syncthreads();
-    const double r = v + (warp ? s_w[warp - 1] : 0.0);
-    if (tot) *tot = s_w[31];
+    if (warp) ff_add(h, l, s_w[warp - 1].x, s_w[warp - 1].y);
+    if (th) {
+        *th = s_w[31].x;
+        *tl = s_w[31].y;
+    }
     __syncthreads();
-    return r;
 }
 
 __device__ __forceinline__ bool packed_is_diag(long long p)
@@ -638,15 +641,60 @@ __device__ __forceinline__ bool packed_is_diag(long long p)
     return p - j * (j + 1) / 2 == j;
 }
 
+// TopLEK's term of a kept-set entry (key << 32 | ~position) in fixed point: c v^2 2^sh (c = 1 on the
+// diagonal, 2 off it) for the FP32 magnitude v = m 2^(eb - 150) (biased exponent eb, significand m),
+// i.e. m^2 2^(2 eb - 300 + sh), exact where the shift is not negative
+__device__ __forceinline__ unsigned long long lek_fixed(unsigned long long e, int sh)
+{
+    const unsigned key = (unsigned)(e >> 32);
+    const int eb = (int)(key >> 23);
+    const unsigned long long m = eb ? (unsigned long long)((key & 0x7fffffu) | 0x800000u) : (unsigned long long)(key & 0x7fffffu);
+    const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
+    const int s = 2 * (eb ? eb : 1) - 300 + sh + (packed_is_diag(q) ? 0 : 1);
+    const unsigned long long m2 = m * m;
+    return s >= 0 ? m2 << s : (s > -64 ? m2 >> -s : 0ull);
+}
+
+// inclusive scan of one u64 per thread over the block (1024 threads); total in *tot
+__device__ __forceinline__ unsigned long long block_scan_u64(unsigned long long v, unsigned long long* s_w,
+                                                             unsigned long long* tot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) s_w[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = s_w[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        s_w[lane] = w;
+    }
+    __syncthreads();
+    const unsigned long long r = v + (warp ? s_w[warp - 1] : 0ull);
+    if (tot) *tot = s_w[31];
+    __syncthreads();
+    return r;
+}
+
 // one CTA (1024 threads) per client: selection bitmap sel[c] from the differences dsel[c]
 __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int toplek, unsigned seed)
 {
-    extern __shared__ unsigned long long s_set[];       // TopLEK: [Kp]
+    extern __shared__ unsigned long long s_set[];       // TopLEK: [max(Kp, 1024)] entries, [2048] masses
     __shared__ unsigned hist[2048];
     __shared__ unsigned s_wu[32];
-    __shared__ double s_wd[32];
-    __shared__ unsigned s_bin, s_need, s_cnt[32], s_nk;
-    __shared__ int s_hit;
+    __shared__ unsigned long long s_wl[32];
+    __shared__ float2 s_wf[32];
+    __shared__ double s_win[3];                 // TopLEK: F, (1 - k/U) F, F/10
+    __shared__ unsigned long long s_rx, s_above;
+    __shared__ unsigned s_bin, s_need, s_cnt[32], s_nk, s_kmax, s_qstar;
+    __shared__ int s_istar;
     const int c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int U = P.U;
     const float* v = P.dsel + (size_t)c * P.Up;
@@ -689,27 +737,46 @@ __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int t
         }
         T = prefix;
     }
-    // bitmap in position order: keys above T, and the first `need` keys equal to T
-    unsigned carry = 0;
-    for (int base = 0; base < U; base += kSelThreads) {
-        const int q = base + tid;
-        const bool in = q < U;
-        const unsigned key = in ? mag_key(v[q]) : 0u;
-        const bool gt = in && (K >= U || key > T), eq = in && K < U && key == T;
-        const unsigned be = __ballot_sync(0xffffffffu, eq);
-        if (lane == 0) s_cnt[warp] = __popc(be);
-        __syncthreads();
-        unsigned off = 0, tot = 0;
-        for (int w = 0; w < 32; ++w) {
-            const unsigned cw = s_cnt[w];
-            if (w < warp) off += cw;
-            tot += cw;
+    // bitmap in position order: keys above T, and the first `need` keys equal to T.  Warp w owns a
+    // contiguous range of selection words (lane = bit); pass 1 counts its keys equal to T, one block
+    // scan orders the warps, pass 2 forms the words (loads of eight words in flight in each pass).
+    {
+        const int SWn = (U + 31) >> 5, wpw = (SWn + 31) >> 5;
+        const int w0 = warp * wpw, w1 = min(SWn, w0 + wpw);
+        unsigned neq = 0;
+        for (int wd = w0; wd < w1; wd += 8) {
+            unsigned key[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int q = (wd + u) * 32 + lane;
+                key[u] = (wd + u < w1 && q < U) ? mag_key(v[q]) : 0xffffffffu;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) neq += __popc(__ballot_sync(0xffffffffu, K < U && key[u] == T));
         }
-        const unsigned rank = carry + off + __popc(be & ((1u << lane) - 1u));
-        const bool take = gt || (eq && rank < need);
-        const unsigned word = __ballot_sync(0xffffffffu, take);
-        if (lane == 0 && base + warp * 32 < U) sc[(base >> 5) + warp] = word;
-        carry += tot;
+        if (lane == 0) s_cnt[warp] = neq;
+        __syncthreads();
+        unsigned carry = 0;
+        for (int w = 0; w < warp; ++w) carry += s_cnt[w];
+        for (int wd = w0; wd < w1; wd += 8) {
+            unsigned key[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int q = (wd + u) * 32 + lane;
+                key[u] = (wd + u < w1 && q < U) ? mag_key(v[q]) : 0xffffffffu;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int q = (wd + u) * 32 + lane;
+                const bool in = wd + u < w1 && q < U;
+                const bool gt = in && (K >= U || key[u] > T), eq = in && K < U && key[u] == T;
+                const unsigned be = __ballot_sync(0xffffffffu, eq);
+                const unsigned rank = carry + __popc(be & ((1u << lane) - 1u));
+                const unsigned word = __ballot_sync(0xffffffffu, gt || (eq && rank < need));
+                if (lane == 0 && wd + u < w1) sc[wd + u] = word;
+                carry += __popc(be);
+            }
+        }
         __syncthreads();
     }
     if (!toplek || K >= U) {
@@ -717,10 +784,18 @@ __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int t
         return;
     }
     // ---- TopLEK on the kept set ----
+    // The reference's rule (SpecialMathRoutinesForMatrix.h:377-511) removes kept entries smallest
+    // first (ascending key, ties: higher position first) while the mass outside plus the removed
+    // mass stays below the window.  In descending order (key desc, position asc) with Top(j) the
+    // mass of the first j entries (terms v^2 on the diagonal, 2 v^2 off it), the boundary entry is
+    // the j*-th, Top(j*) < R <= Top(j* + 1), R = F + F/10 - (1 - k/U) F.  It is found without
+    // sorting: the masses are 64-bit fixed point (exact integer products of the FP32 significands,
+    // so sums are exact in any order), weighted histograms walk the key bits (11 + 11 + 9) from
+    // the top, then the entries tied at the boundary key are walked in position order.
     int Kp = 1;
     while (Kp < K) Kp <<= 1;
-    for (int t = tid; t < Kp; t += kSelThreads) s_set[t] = ~0ull;
-    __syncthreads();
+    unsigned long long* s_mass = s_set + (Kp > kSelThreads ? Kp : kSelThreads);     // [2048]
+    if (tid == 0) s_kmax = 0u;
     {   // the kept entries in position order: popcounts of the bitmap words, block-scanned
         unsigned base_cnt = 0;
         for (int w0 = 0; w0 < P.SW; w0 += kSelThreads) {
@@ -743,87 +818,147 @@ __global__ void __launch_bounds__(kSelThreads) k_mx_select(MxDev P, int k, int t
         }
     }
     __syncthreads();
-    for (int size = 2; size <= Kp; size <<= 1) {         // bitonic sort, ascending
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = tid; t < Kp / 2; t += kSelThreads) {
-                const int i = 2 * t - (t & (stride - 1)), j = i + stride;
-                const bool asc = (i & size) == 0;
-                const unsigned long long a = s_set[i], b = s_set[j];
-                if ((a > b) == asc) {
-                    s_set[i] = b;
-                    s_set[j] = a;
+    // the fixed-point scale from the largest key; F from the Gram epilogue's partial sums
+    {
+        unsigned km = 0u;
+        for (int m = tid; m < K; m += kSelThreads) km = max(km, (unsigned)(s_set[m] >> 32));
+        km = __reduce_max_sync(0xffffffffu, km);
+        if (lane == 0) atomicMax(&s_kmax, km);
+    }
+    float fh = 0.0f, fl = 0.0f;
+    for (int t = tid; t < P.tiles * 128; t += kSelThreads) ff_add(fh, fl, P.fpart[(size_t)c * P.tiles * 128 + t], 0.0f);
+    float Fh, Fl;
+    block_scan_ff(fh, fl, s_wf, &Fh, &Fl);
+    int lgK = 0;
+    while ((1 << lgK) < K) ++lgK;
+    const int ebmax = max(1, (int)(s_kmax >> 23));
+    const int sh = 314 - 2 * ebmax - lgK;              // K terms of at most 2^(2 ebmax - 251 + sh) < 2^63
+    unsigned long long mk = 0ull;
+    for (int m = tid; m < K; m += kSelThreads) mk += lek_fixed(s_set[m], sh);
+    unsigned long long total;
+    block_scan_u64(mk, s_wl, &total);
+    if (tid == 0) {
+        const double F = (double)Fh + (double)Fl, scale = ldexp(1.0, -sh);
+        const double all = (double)total * scale;
+        const double delta = (double)k / (double)U;
+        const double omd_f = (1.0 - delta) * F, eps = 1e-1 * F;
+        s_win[0] = F;
+        s_win[1] = omd_f;
+        s_win[2] = eps;
+        const double rr = (F + eps - omd_f) * ldexp(1.0, sh);
+        unsigned long long rx = rr >= 9.2e18 ? ~0ull >> 1 : (rr > 0.0 ? (unsigned long long)rr : 0ull);
+        if (rx > total) rx = total;                   // past the smallest entry: it is the boundary
+        s_rx = (omd_f + eps > F - all) ? rx : 0ull;   // 0: no window (nothing kept)
+        s_nk = 0u;
+        s_qstar = 0u;
+        s_istar = 0;
+    }
+    __syncthreads();
+    unsigned long long rrem = s_rx;
+    unsigned keep = 0u;
+    if (rrem > 0ull) {
+        unsigned prefix = 0u, mask = 0u;
+        unsigned long long above = 0ull;               // mass of the entries above the current range
+        unsigned above_n = 0u;
+        const int shs[3] = {20, 9, 0}, nbits[3] = {11, 11, 9};
+        for (int pass = 0; pass < 3; ++pass) {
+            const int sb = shs[pass], nb = 1 << nbits[pass];
+            for (int b = tid; b < 2048; b += kSelThreads) {
+                hist[b] = 0u;
+                s_mass[b] = 0ull;
+            }
+            __syncthreads();
+            for (int m = tid; m < K; m += kSelThreads) {
+                const unsigned long long e = s_set[m];
+                const unsigned key = (unsigned)(e >> 32);
+                if ((key & mask) == prefix) {
+                    const unsigned b = (key >> sb) & (unsigned)(nb - 1);
+                    atomicAdd(&hist[b], 1u);
+                    atomicAdd(&s_mass[b], lek_fixed(e, sh));
                 }
             }
             __syncthreads();
+            // descending bins: thread t owns nb-1-2t and nb-2-2t
+            const int b0 = nb - 1 - 2 * tid, b1 = b0 - 1;
+            const unsigned long long m0 = b0 >= 0 ? s_mass[b0] : 0ull, m1 = b1 >= 0 ? s_mass[b1] : 0ull;
+            const unsigned n0 = b0 >= 0 ? hist[b0] : 0u, n1 = b1 >= 0 ? hist[b1] : 0u;
+            unsigned long long mtot;
+            const unsigned long long mi = block_scan_u64(m0 + m1, s_wl, &mtot);
+            const unsigned ni = block_scan_u32(n0 + n1, s_wu, nullptr);
+            const unsigned long long me = mi - m0 - m1;
+            const unsigned ne = ni - n0 - n1;
+            if (me < rrem && rrem <= mi) {
+                if (rrem <= me + m0) {
+                    s_bin = (unsigned)b0;
+                    s_above = me;
+                    s_need = ne;
+                } else {
+                    s_bin = (unsigned)b1;
+                    s_above = me + m0;
+                    s_need = ne + n0;
+                }
+            }
+            __syncthreads();
+            prefix |= s_bin << sb;
+            mask |= (unsigned)(nb - 1) << sb;
+            above += s_above;
+            above_n += s_need;
+            rrem -= s_above;
+            __syncthreads();
         }
-    }
-    // F from the Gram epilogue's partial sums; terms c v^2 of the sorted set
-    double f = 0.0;
-    for (int t = tid; t < P.tiles * 128; t += kSelThreads) f += (double)P.fpart[(size_t)c * P.tiles * 128 + t];
-    double F;
-    block_scan_f64(f, s_wd, &F);
-    const int per = (Kp + kSelThreads - 1) / kSelThreads;    // a run of consecutive sorted entries
-    const int m0 = tid * per;
-    double run = 0.0;
-    for (int m = m0; m < m0 + per && m < K; ++m) {
-        const unsigned long long e = s_set[m];
-        const double a = (double)__uint_as_float((unsigned)(e >> 32));
-        const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
-        run += packed_is_diag(q) ? a * a : (a * a) * 2.0;
-    }
-    double all;
-    const double incl = block_scan_f64(run, s_wd, &all);
-    const double delta = (double)k / (double)U;
-    const double omd_f = (1.0 - delta) * F, eps = 1e-1 * F, hi = omd_f + eps;
-    const double num0 = F - all;
-    if (tid == 0) s_hit = K;
-    __syncthreads();
-    if (hi > num0) {
-        double nx = num0 + (incl - run);
+        // entries tied at the boundary key, in position order (= descending order among them)
+        const int per = (K + kSelThreads - 1) / kSelThreads, m0 = tid * per;
+        unsigned long long tm = 0ull;
+        unsigned tn = 0u;
         for (int m = m0; m < m0 + per && m < K; ++m) {
             const unsigned long long e = s_set[m];
-            const double a = (double)__uint_as_float((unsigned)(e >> 32));
-            const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
-            nx += packed_is_diag(q) ? a * a : (a * a) * 2.0;
-            if (omd_f < nx + eps) {
-                atomicMin(&s_hit, m);
-                break;
+            if ((unsigned)(e >> 32) == prefix) {
+                tm += lek_fixed(e, sh);
+                ++tn;
             }
         }
-    }
-    __syncthreads();
-    const int hit = s_hit;                 // hit == K: no window (nothing kept)
-    int keep = 0;
-    if (hi > num0 && hit < K) {
-        // prev and next numerators at the hit, recomputed in sorted order by the thread that owns it
-        double pv = 0.0, nv = 0.0;
-        if (tid == hit / per) {
-            double acc = num0 + (incl - run);
-            for (int m = m0; m <= hit; ++m) {
-                const unsigned long long e = s_set[m];
-                const double a = (double)__uint_as_float((unsigned)(e >> 32));
-                const long long q = (long long)(0xffffffffu - (unsigned)(e & 0xffffffffu));
-                pv = acc;
-                acc += packed_is_diag(q) ? a * a : (a * a) * 2.0;
+        const unsigned long long tmi = block_scan_u64(tm, s_wl, nullptr);
+        const unsigned tni = block_scan_u32(tn, s_wu, nullptr);
+        unsigned long long cum = tmi - tm;
+        unsigned idx = tni - tn;
+        for (int m = m0; m < m0 + per && m < K; ++m) {
+            const unsigned long long e = s_set[m];
+            if ((unsigned)(e >> 32) != prefix) continue;
+            const unsigned long long w = lek_fixed(e, sh);
+            if (cum < rrem && rrem <= cum + w) {      // the boundary entry: j* = above_n + idx
+                const double scale = ldexp(1.0, -sh);
+                const double F = s_win[0], omd_f = s_win[1], eps = s_win[2];
+                const double pv = F - (double)(above + cum + w) * scale, nv = F - (double)(above + cum) * scale;
+                const double pr = (omd_f - pv + eps) / (nv - pv + eps);
+                uint32_t o;
+                fednl::philox4x32(P.draws[c], 0x544C454Bu, 0u, 0u, seed, (uint32_t)c, o);
+                const double u = ((double)o + 0.5) * (1.0 / 4294967296.0);
+                const unsigned js = above_n + idx;
+                s_nk = js + (u > pr ? 1u : 0u);
+                s_qstar = 0xffffffffu - (unsigned)(e & 0xffffffffu);
+                s_istar = (u > pr) ? 1 : 0;
             }
-            nv = acc;
-            const double pr = (omd_f - pv + eps) / (nv - pv + eps);
-            uint32_t o;
-            fednl::philox4x32(P.draws[c], 0x544C454Bu, 0u, 0u, seed, (uint32_t)c, o);
-            const double u = ((double)o + 0.5) * (1.0 / 4294967296.0);
-            keep = K - 1 - hit + (u > pr ? 1 : 0);
-            s_nk = (unsigned)keep;
+            cum += w;
+            ++idx;
         }
         __syncthreads();
-        keep = (int)s_nk;
-    }
-    // drop the K - keep smallest
-    for (int m = tid; m < K - keep; m += kSelThreads) {
-        const unsigned q = 0xffffffffu - (unsigned)(s_set[m] & 0xffffffffu);
-        atomicAnd(&sc[q >> 5], ~(1u << (q & 31)));
+        keep = s_nk;
+        // the kept set: keys above the boundary key, tied entries before the boundary entry, and
+        // the boundary entry itself when the draw keeps it
+        const unsigned kap = prefix, qs = s_qstar;
+        const int inc = s_istar;
+        for (int w = tid; w < P.SW; w += kSelThreads) sc[w] = 0u;
+        __syncthreads();
+        for (int m = tid; m < K; m += kSelThreads) {
+            const unsigned long long e = s_set[m];
+            const unsigned key = (unsigned)(e >> 32), q = 0xffffffffu - (unsigned)(e & 0xffffffffu);
+            if (key > kap || (key == kap && (q < qs || (inc && q == qs)))) atomicOr(&sc[q >> 5], 1u << (q & 31));
+        }
+    } else {
+        for (int w = tid; w < P.SW; w += kSelThreads) sc[w] = 0u;
     }
     if (tid == 0) {
-        P.cnt[c] = keep;
+        P.cnt[c] = (int)keep;
         P.draws[c] = P.draws[c] + 1;
     }
 }
