@@ -268,6 +268,7 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
     R = 10
     mx = fednl.MixedFedNL(prob, k, alpha)
     g_mx = mx.run(R)
+    tuned = mx.autotune()
     tot, per = mx.time_rounds(20, L2_FLUSH_BYTES)
     prof = mx.profile_kernels(5)
     mx.close()
@@ -290,6 +291,7 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
                        "flops_per_launch": flops, "achieved_tflops": tf, "peak_tflops": tensor_peak_tflops,
                        "frac": tf / tensor_peak_tflops,
                        "peak_source": f"{src}: MEASURED_PEAKS.json bf16_tflops / 2 (tf32 rate)"},
+            "autotuned": tuned,
             "fp64_gpu_rounds_per_s": 2 / (tot64 / 1000.0), "cpu_port_rounds_per_s": 1.0 / cpu_s,
             "cpu_port_sample": f"1 round, {threads} threads",
             "grad_norm_after_rounds": {"rounds": R, "mixed": float(g_mx[-1]), "fp64": float(g_64[-1]),
@@ -347,8 +349,9 @@ def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, f
             if (fp64_tol_s and tol_ms) else None,
             "autotuned": tuned,
             "precision": "TF32 tensor-core client Hessians (FP32 accumulate), FP32 shifts and selection, "
-                         "float-float margins/gradients, FP64 master; solve as autotuned (FP64 Cholesky, or "
-                         "FP32 Cholesky with one float-float refinement step)"}
+                         "float-float margins/gradients, FP64 master; solve as autotuned (FP64 Cholesky; FP32 "
+                         "Cholesky on a cooperative grid or cluster with FP64-residual refinement to 2^-30; or "
+                         "FP32 one-CTA Cholesky with one float-float refinement step)"}
 
 
 def serving_workload(fednl, count: int = 24, max_rounds: int = 20):
