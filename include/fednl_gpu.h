@@ -202,6 +202,11 @@ int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, doubl
  * first trailing update),
  * d up to 1312.  A pivot that loses more than 18 bits in FP32 hands the system to the FP64 solve,
  * which returns FEDNL_ENOTPD for a matrix that is not positive definite.  Host buffers. */
+/* Self-test of the FP64 Cholesky's square root and reciprocal (integer arithmetic, correctly
+ * rounded): n inputs from a seeded generator (random bit patterns of every exponent and sign,
+ * significands near 0 and 1, squares and their neighbours); counts of results that differ bit for bit
+ * from the hardware sqrt and 1.0 / x. */
+int fednl_gpu_selftest_rn(int64_t n, uint64_t seed, int64_t* sqrt_mismatches, int64_t* rcp_mismatches);
 int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
                               int32_t refine, int32_t grid);
 int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g,

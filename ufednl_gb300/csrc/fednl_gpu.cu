@@ -1867,6 +1867,60 @@ int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l,
     return FEDNL_OK;
 }
 
+// ---- self-test of the integer square root and reciprocal --------------------------------------
+namespace {
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// inputs: random bit patterns (every exponent, both signs), significands near 0 and near 1, and
+// squares of random doubles and their neighbours
+__global__ void k_selftest_rn(unsigned long long seed, long long n, unsigned long long* bad)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long z = splitmix64(seed ^ (unsigned long long)i), w = splitmix64(z);
+        unsigned long long u;
+        switch (i & 3) {
+        case 0: u = z; break;
+        case 1: u = (z & 0x7FF0000000000000ull) | (w & 0xFFFFull); break;
+        case 2: u = (z & 0x7FF0000000000000ull) | (0xFFFFFFFFFFFFFull - (w & 0xFFFFull)); break;
+        default: {
+            const double x = __longlong_as_double((long long)((z & 0x000FFFFFFFFFFFFFull) | (0x3FF0000000000000ull + ((w & 0x3FFull) << 52) - (0x200ull << 52))));
+            u = (unsigned long long)__double_as_longlong(x * x) + (w >> 62) - 1ull;
+        }
+        }
+        const double a = __longlong_as_double((long long)u);
+        if (__double_as_longlong(sqrt_rn_int(a)) != __double_as_longlong(sqrt(a))) atomicAdd(&bad[0], 1ull);
+        if (__double_as_longlong(rcp_rn_int(a)) != __double_as_longlong(1.0 / a)) atomicAdd(&bad[1], 1ull);
+    }
+}
+}  // namespace
+
+int fednl_gpu_selftest_rn(int64_t n, uint64_t seed, int64_t* sqrt_mismatches, int64_t* rcp_mismatches)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (n < 1 || !sqrt_mismatches || !rcp_mismatches) return fail(FEDNL_EINVAL, "bad argument");
+    unsigned long long* d = nullptr;
+    CK(cudaMalloc(&d, 16));
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemset(d, 0, 16);
+    if (e == cudaSuccess) {
+        k_selftest_rn<<<1216, 256>>>(seed, n, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(FEDNL_ECUDA, "self-test kernel failed: %s", cudaGetErrorString(e));
+    *sqrt_mismatches = (int64_t)h[0];
+    *rcp_mismatches = (int64_t)h[1];
+    return FEDNL_OK;
+}
+
 // ---- instrumentation ---------------------------------------------------------------------------
 
 static int flush_l2(fednl_handle h, int64_t bytes)

@@ -1289,6 +1289,71 @@ constexpr int kCholSlab = 8;                          // panel columns per CTA k
 constexpr int kCoopThreads = 256;
 constexpr long long kBarrierCycles = 4000000000ll;   // ~2 s at 2 GHz, then ETIMEOUT
 
+// ---- correctly rounded square root and reciprocal without the FP64 pipe ----------------------
+// On this part a warp's FP64 instructions (and 64-bit integer <-> float conversions) issue about once
+// per 64 cycles, and the hardware sequences for sqrt and 1/x cost about 720 and 355 cycles on the
+// Cholesky's pivot chain.  These give the same correctly rounded results from integer arithmetic:
+// an FP32 estimate, Newton steps whose residuals are computed exactly in 64-bit integers (converted
+// to FP32 through 32-bit integers only), and a final exact remainder test that decides the rounding.
+// Outside their domain (sqrt: a not a positive normal; 1/x: the result not normal) they defer to
+// the hardware operation.
+
+// sqrt(a) = S 2^(e/2 - 52), S = the integer nearest sqrt(N), N = M 2^52, a = M 2^(e - 52) with e even
+// and M in [2^52, 2^54).  The FP32 square root of M gives S within 2^29; the Newton step from
+// s0 = r 2^26 uses the exact residual N - s0^2 = (M - r^2) 2^52 (|M - r^2| < 2^34) and lands within
+// 53; the next one's residual N - T^2 fits in 64 bits (|.| < 2^61) and lands within 1/2; then
+// (T + 1/2)^2 = T^2 + T + 1/4 decides: S = T + 1 when N - T^2 > T, T - 1 when N - T^2 <= -T.
+__device__ __forceinline__ double sqrt_rn_int(double a)
+{
+    const unsigned long long ia = (unsigned long long)__double_as_longlong(a);
+    const unsigned E = (unsigned)(ia >> 52);                       // sign bit included: 0 for a > 0
+    if (E - 1u >= 2046u) return sqrt(a);                          // zero, negative, subnormal, inf, nan
+    const int odd = (E & 1u) == 0u;                               // e = E - 1023 odd
+    const unsigned long long M = ((ia & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << odd;
+    const int eh = ((int)E - 1023 - odd) / 2;
+    const float fm = __fmul_rn(__uint2float_rn((unsigned)(M >> 22)), 4194304.0f);          // M (24 bits)
+    const unsigned ri = __float2uint_rn(__fsqrt_rn(fm));
+    const long long D0 = (long long)(M - (unsigned long long)ri * ri);
+    const float d1 = __fdiv_rn(__fmul_rn(__int2float_rn((int)(D0 >> 3)), 268435456.0f),   // D0 2^25 / r
+                               __uint2float_rn(ri));
+    unsigned long long T = ((unsigned long long)ri << 26) + (unsigned long long)(long long)__float2int_rn(d1);
+    const unsigned long long Nlo = M << 52;                      // N mod 2^64
+    long long Rm = (long long)(Nlo - T * T);
+    const float rf = __fmul_rn(__int2float_rn((int)(Rm >> 32)), 4294967296.0f);
+    const float tf = __fmul_rn(__uint2float_rn((unsigned)(T >> 29)), 536870912.0f);
+    T += (unsigned long long)(long long)__float2int_rn(__fdiv_rn(rf, __fmul_rn(tf, 2.0f)));
+    Rm = (long long)(Nlo - T * T);
+    if (Rm > (long long)T) ++T;
+    else if (Rm <= -(long long)T) --T;
+    return __longlong_as_double((long long)(((unsigned long long)(eh + 1023) << 52) + (T - (1ull << 52))));
+}
+
+// 1/r = Q 2^(970 - E), Q = the integer nearest 2^105 / M, r = M 2^(E - 1075), M in [2^52, 2^53).
+// A float-float Newton step from the FP32 reciprocal of M (held as its top 24 bits plus the rest)
+// gives Q within 361; the residual 2^105 - M Q is then exact in 64 bits (2^105 = 0 mod 2^64), one
+// more step lands within 1/2 and 2|2^105 - M Q| < M decides the rounding (no ties: 2^106 / M is an
+// odd integer for no M in range).
+__device__ __forceinline__ double rcp_rn_int(double r)
+{
+    const unsigned long long ir = (unsigned long long)__double_as_longlong(r);
+    const unsigned E = (unsigned)(ir >> 52);
+    if (E - 1u >= 2044u) return 1.0 / r;                          // the result would not be normal
+    const unsigned long long M = (ir & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const float mh = __fmul_rn(__uint2float_rn((unsigned)(M >> 29)), 536870912.0f);       // exact
+    const float ml = __uint2float_rn((unsigned)(M & 0x1FFFFFFFull));
+    const float y0 = __frcp_rn(mh);
+    const float e = __fsub_rn(fmaf(-mh, y0, 1.0f), __fmul_rn(ml, y0));                   // 1 - M y0
+    unsigned long long Q = ((unsigned long long)__float2uint_rn(__fmul_rn(y0, 0x1p76f)) << 29) +
+                           (unsigned long long)(long long)__float2int_rn(__fmul_rn(__fmul_rn(y0, e), 0x1p105f));
+    long long Rm = (long long)(0ull - M * Q);
+    Q += (unsigned long long)(long long)__float2int_rn(
+        __fmul_rn(__fmul_rn(__int2float_rn((int)(Rm >> 32)), 4294967296.0f), y0));
+    Rm = (long long)(0ull - M * Q);
+    if (2 * Rm > (long long)M) ++Q;
+    else if (2 * Rm < -(long long)M) --Q;
+    return __longlong_as_double((long long)(((unsigned long long)(2045u - E) << 52) + (Q - (1ull << 52))));
+}
+
 // Bounded grid barrier of n cooperating CTAs on three words: bar[0] counts arrivals since the
 // launch began (the e-th barrier completes when it reaches e n), bar[1] counts CTAs that have
 // finished, bar[2] is the error flag.  One fence and one reduction per CTA, then a poll with acquire
@@ -1429,8 +1494,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
         if (warp == 0) {
             const double a0 = Db[0][0];
             const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-            const double r = sqrt(a0);
-            inv_k = 1.0 / r;
+            const double r = sqrt_rn_int(a0);
+            inv_k = rcp_rn_int(r);
             if (lane == 0) {
                 Rb[0][0] = r;
                 s_inv[0] = inv_k;
@@ -1445,8 +1510,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                     const double rk = __dmul_rn(Db[k][k + 1], inv_k);
                     const double a0 = fma(-rk, rk, Db[k + 1][k + 1]);
                     const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-                    const double r = sqrt(a0);
-                    inv_k = 1.0 / r;
+                    const double r = sqrt_rn_int(a0);
+                    inv_k = rcp_rn_int(r);
                     if (lane == 0) {
                         Rb[k + 1][k + 1] = r;
                         s_inv[k + 1] = inv_k;

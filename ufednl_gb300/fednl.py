@@ -68,7 +68,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_solve_batch", "fednl_gpu_round_result", "fednl_mx_round_result", "fednl_gpu_mem_info",
            "fednl_mx_get_diff", "fednl_mx_get_selection", "fednl_mx_get_shift", "fednl_gpu_footprint",
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
-           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32",
+           "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32", "fednl_gpu_selftest_rn",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
            "fednl_gpu_autotune", "fednl_mx_autotune"]
 
@@ -112,6 +112,7 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
         "fednl_gpu_optionb_solve_mixed": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
         "fednl_gpu_optionb_solve32": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp, C.c_int32, C.c_int32],
+        "fednl_gpu_selftest_rn": [C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
         "fednl_gpu_optionb_solve_noalloc": [vp, C.c_int32, C.c_int32, C.c_double, vp, vp, vp],
         "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
         "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
@@ -253,6 +254,15 @@ def cholesky_option_b_solve_mixed(H: np.ndarray, d: int, lda: int, l: float, g: 
     dx = np.empty(d)
     _check(load().fednl_gpu_optionb_solve_mixed(_dp(Hc), d, lda, float(l), _dp(gc), _dp(dx)))
     return dx
+
+
+def selftest_rn(n: int, seed: int = 1) -> tuple:
+    """Mismatch counts (sqrt, reciprocal) of the Cholesky's integer square root and reciprocal against
+    the hardware operations over n generated inputs."""
+    a = C.c_int64(0)
+    b = C.c_int64(0)
+    _check(load().fednl_gpu_selftest_rn(int(n), int(seed), C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def cholesky_option_b_solve32(H: np.ndarray, d: int, lda: int, l: float, g: np.ndarray, refine: int = 6,
