@@ -513,37 +513,54 @@ __global__ void __launch_bounds__(256) k_mx_margin(MxDev P)
     split_ff(qv, P.qh[(size_t)c * P.L + s], P.ql[(size_t)c * P.L + s]);
 }
 
-// client gradients: one warp per (client, feature), lanes over the samples
+// client gradients: one warp per (client, feature), lanes over the samples (eight in flight, the
+// last pass masked).  The warp reduces in float-float; eight lanes of the block then form the FP64
+// sums of its eight features, so the FP64 pipe sees one conversion and add per block, not per warp.
 __global__ void __launch_bounds__(256) k_mx_grad(MxDev P)
 {
-    const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (wid >= P.nc * P.d) return;
-    const int c = wid / P.d, i = wid - c * P.d;
-    const int n = P.ns[c];
-    const float* row = P.X + ((size_t)c * P.dp + i) * P.L;
-    const float* qh = P.qh + (size_t)c * P.L;
-    const float* ql = P.ql + (size_t)c * P.L;
-    float hi = 0.0f, lo = 0.0f, h1 = 0.0f, l1 = 0.0f;
-    int s = lane;
-    for (; s + 224 < n; s += 256) {                    // eight samples a lane in flight
-        float x[8], a[8], b[8];
+    __shared__ float s_h[8], s_l[8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 8 + w, total = P.nc * P.d;
+    float hi = 0.0f, lo = 0.0f;
+    if (wid < total) {
+        const int c = wid / P.d, i = wid - c * P.d;
+        const int n = P.ns[c];
+        const float* row = P.X + ((size_t)c * P.dp + i) * P.L;
+        const float* qh = P.qh + (size_t)c * P.L;
+        const float* ql = P.ql + (size_t)c * P.L;
+        float h1 = 0.0f, l1 = 0.0f;
+        for (int s = lane; s < n; s += 256) {
+            float x[8], a[8], b[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            x[u] = __ldg(row + s + 32 * u);
-            a[u] = __ldg(qh + s + 32 * u);
-            b[u] = __ldg(ql + s + 32 * u);
+            for (int u = 0; u < 8; ++u) {
+                const int t = s + 32 * u;
+                const bool in = t < n;
+                x[u] = in ? __ldg(row + t) : 0.0f;
+                a[u] = in ? __ldg(qh + t) : 0.0f;
+                b[u] = in ? __ldg(ql + t) : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u += 2) {
+                ff_mac(hi, lo, x[u], a[u], b[u]);
+                ff_mac(h1, l1, x[u + 1], a[u + 1], b[u + 1]);
+            }
         }
-#pragma unroll
-        for (int u = 0; u < 8; u += 2) {
-            ff_mac(hi, lo, x[u], a[u], b[u]);
-            ff_mac(h1, l1, x[u + 1], a[u + 1], b[u + 1]);
+        ff_add(hi, lo, h1, l1);
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, oh, ol);
         }
     }
-    for (; s < n; s += 32) ff_mac(hi, lo, row[s], qh[s], ql[s]);
-    ff_add(hi, lo, h1, l1);
-    double v = (double)hi + (double)lo;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) P.gc[(size_t)c * P.d + i] = v + P.lambda * P.x[i];
+    if (lane == 0) {
+        s_h[w] = hi;
+        s_l[w] = lo;
+    }
+    __syncthreads();
+    const int t = blockIdx.x * 8 + threadIdx.x;
+    if (threadIdx.x < 8 && t < total) {
+        const int c = t / P.d, i = t - c * P.d;
+        P.gc[(size_t)c * P.d + i] = ((double)s_h[threadIdx.x] + (double)s_l[threadIdx.x]) + P.lambda * P.x[i];
+    }
 }
 
 // RandK-Philox draw of every client (the FP64 engine's stream)
