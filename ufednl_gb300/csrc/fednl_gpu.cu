@@ -21,6 +21,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace fednl;
@@ -850,6 +851,25 @@ int fednl_gpu_destroy(fednl_handle h)
     return FEDNL_OK;
 }
 
+// Host threads for the conversion of the uploaded rows: clients are split into contiguous ranges
+// (each client's CSR range and bitmap block are disjoint, so the ranges need no locking).
+static void for_client_ranges(int nc, const std::function<void(int, int, int)>& f)
+{
+    const unsigned hc = std::thread::hardware_concurrency();
+    const int nth = std::max(1, std::min<int>({(int)(hc ? hc : 1), 32, nc}));
+    if (nth == 1) {
+        f(0, 0, nc);
+        return;
+    }
+    std::vector<std::thread> ts;
+    const int per = (nc + nth - 1) / nth;
+    for (int t = 0; t < nth; ++t) {
+        const int c0 = t * per, c1 = std::min(nc, c0 + per);
+        if (c0 < c1) ts.emplace_back(f, t, c0, c1);
+    }
+    for (auto& th : ts) th.join();
+}
+
 int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
 {
     if (!h || !features || !labels) return fail(FEDNL_EINVAL, "null argument");
@@ -857,14 +877,32 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     for (int s = 0; s < S; ++s)
         if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
     int fmt = h->desc.feature_format;
-    if (fmt == FEDNL_FEATURES_AUTO) {
-        fmt = FEDNL_FEATURES_BINARY;
-        for (size_t t = 0; t < (size_t)S * d; ++t)
-            if (features[t] != 0.0 && features[t] != 1.0) {
-                fmt = FEDNL_FEATURES_DENSE;
-                break;
+    // first pass, per client range: ones per sample, and the first value that is neither 0 nor 1
+    // (samples in order, so the earliest range holding one has the first of the whole upload)
+    const int nc = h->nc;
+    std::vector<int> ones(S, 0);
+    std::vector<long long> first_bad(nc, -1);
+    if (fmt != FEDNL_FEATURES_DENSE) {
+        for_client_ranges(nc, [&](int, int c0, int c1) {
+            for (int s = h->soff[c0]; s < h->soff[c1]; ++s) {
+                const double* a = features + (size_t)s * d;
+                int n1 = 0;
+                for (int i = 0; i < d; ++i) {
+                    if (a[i] == 1.0) ++n1;
+                    else if (a[i] != 0.0) {
+                        first_bad[c0] = (long long)s * d + i;
+                        return;
+                    }
+                }
+                ones[s] = n1;
             }
+        });
     }
+    long long bad = -1;
+    for (int c = 0; c < nc && bad < 0; ++c) bad = first_bad[c];
+    if (fmt == FEDNL_FEATURES_AUTO) fmt = bad < 0 ? FEDNL_FEATURES_BINARY : FEDNL_FEATURES_DENSE;
+    if (fmt == FEDNL_FEATURES_BINARY && bad >= 0)
+        return fail(FEDNL_EINVAL, "feature (%d,%d) is not 0/1 in binary format", (int)(bad / d), (int)(bad % d));
     h->feat.release();
     Dev& P = h->dev;
     P.rowptr = nullptr;
@@ -874,30 +912,32 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     P.A = nullptr;
     double* lab = nullptr;
     if (fmt == FEDNL_FEATURES_BINARY) {
-        std::vector<int> rowptr(S + 1, 0), colidx;
-        std::vector<long long> fboff(h->nc);
+        std::vector<int> rowptr(S + 1, 0);
+        for (int s = 0; s < S; ++s) rowptr[s + 1] = rowptr[s] + ones[s];
+        std::vector<int> colidx(rowptr[S]);
+        std::vector<long long> fboff(nc);
         long long words = 0;
-        for (int c = 0; c < h->nc; ++c) {
+        for (int c = 0; c < nc; ++c) {
             fboff[c] = words;
             words += (long long)d * ((h->ns[c] + 63) / 64);
         }
         std::vector<unsigned long long> fbits(words, 0ull);
-        for (int c = 0; c < h->nc; ++c) {
-            int W = (h->ns[c] + 63) / 64;
-            for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
-                const double* a = features + (size_t)s * d;
-                int ls = s - h->soff[c];
-                for (int i = 0; i < d; ++i) {
-                    if (a[i] == 1.0) {
-                        colidx.push_back(i);
-                        fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
-                    } else if (a[i] != 0.0) {
-                        return fail(FEDNL_EINVAL, "feature (%d,%d) is not 0/1 in binary format", s, i);
-                    }
+        // second pass: the CSR columns and the per-client bitmaps (feature-major, 64 samples a word)
+        for_client_ranges(nc, [&](int, int c0, int c1) {
+            for (int c = c0; c < c1; ++c) {
+                const int W = (h->ns[c] + 63) / 64;
+                for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+                    const double* a = features + (size_t)s * d;
+                    const int ls = s - h->soff[c];
+                    int p = rowptr[s];
+                    for (int i = 0; i < d; ++i)
+                        if (a[i] == 1.0) {
+                            colidx[p++] = i;
+                            fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
+                        }
                 }
-                rowptr[s + 1] = (int)colidx.size();
             }
-        }
+        });
         std::vector<int> icpt(h->nc, 1);
         for (int c = 0; c < h->nc; ++c)
             for (int s = h->soff[c]; s < h->soff[c + 1]; ++s)
