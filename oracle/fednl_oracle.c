@@ -299,8 +299,11 @@ int32_t orc_topk(const double* m, int32_t k, size_t U, const uint32_t* upper, ui
 
 /* getTopLEKFromUpperDiagonalPart<ignoreSign=true>, SpecialMathRoutinesForMatrix.h:377-511.
  * rng_state is the calling worker thread's RandomGenRealLinear state (thread_local, :383). */
-int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
-                   double delta, double frob_sq, uint32_t* rng_state, uint32_t* out)
+static int32_t toplek_ref_window(orc_heap* h, const double* m, int32_t lda, size_t K, double frob_sq,
+                                 double one_minus_delta_xf, double eps, uint32_t* rng_state);
+
+static int32_t toplek_impl(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                           double delta, double frob_sq, uint32_t* rng_state, uint32_t* out, int ref_order)
 {
     double one_minus_delta = 1.0 - delta;
     double one_minus_delta_xf = one_minus_delta * frob_sq;
@@ -315,6 +318,11 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
     h.data = out;
     h.m = m;
     topk_heap_scan(&h, k, U, upper);
+    if (ref_order) {
+        int32_t keep = toplek_ref_window(&h, m, lda, (size_t)k, frob_sq, one_minus_delta_xf, eps, rng_state);
+        qsort(out, (size_t)keep, sizeof(uint32_t), cmp_u32);
+        return keep;
+    }
 
     /* Numerator of the rounding window (:435-503).  The reference subtracts the heap's terms from
      * ||M||^2 one by one in heap-array order and then adds back the extracted terms one by one in
@@ -393,6 +401,57 @@ int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint
     free(terms);
     qsort(out, keep, sizeof(uint32_t), cmp_u32);
     return (int32_t)keep;
+}
+
+int32_t orc_toplek(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                   double delta, double frob_sq, uint32_t* rng_state, uint32_t* out)
+{
+    return toplek_impl(m, lda, k, U, upper, delta, frob_sq, rng_state, out, 0);
+}
+
+int32_t orc_toplek_ref(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                       double delta, double frob_sq, uint32_t* rng_state, uint32_t* out)
+{
+    return toplek_impl(m, lda, k, U, upper, delta, frob_sq, rng_state, out, 1);
+}
+
+/* The rounding window in the reference's own order (SpecialMathRoutinesForMatrix.h:435-503): the
+ * numerator starts at ||M||^2 and loses c v^2 (c = 1 on the diagonal, 2.0 * v * v off it) for every
+ * heap entry in heap-array order; then the heap is extracted one minimum at a time (MinHeap.h:133-140
+ * extraction, the extracted element lands at the array's end) and the numerator gains the extracted
+ * entry's term; the first step with (1-delta)||M||^2 + eps > prev and (1-delta)||M||^2 < next + eps
+ * draws u from the worker's generator and re-inserts the extracted entry when u > p.  Returns the
+ * number of kept entries, which are the array prefix (plus the re-inserted one at its end). */
+static int32_t toplek_ref_window(orc_heap* h, const double* m, int32_t lda, size_t K, double frob_sq,
+                                 double one_minus_delta_xf, double eps, uint32_t* rng_state)
+{
+    double numerator = frob_sq;
+    for (size_t i = 0; i < K; ++i) {
+        uint32_t index = h->data[i];
+        double item = m[index];
+        uint32_t jc = index / (uint32_t)lda, ir = index - jc * (uint32_t)lda;
+        numerator = (ir == jc) ? numerator - item * item : numerator - (2.0 * item) * item;
+    }
+    size_t size = K;
+    while (size > 0) {
+        double prev = numerator;
+        uint32_t t = h->data[0];
+        h->data[0] = h->data[size - 1];
+        h->data[size - 1] = t;
+        heap_sift(h, 0, size - 1);
+        size -= 1;
+        double item = m[t];
+        uint32_t jc = t / (uint32_t)lda, ir = t - jc * (uint32_t)lda;
+        numerator = (ir == jc) ? numerator + item * item : numerator + (2.0 * item) * item;
+        double next = numerator;
+        if (one_minus_delta_xf + eps > prev && one_minus_delta_xf < next + eps) {
+            double p = (one_minus_delta_xf - prev + eps) / (next - prev + eps);
+            if (orc_lcg_real_unit(rng_state) > p)
+                size += 1;     /* insertInMinHeap: the extracted entry still sits at position size */
+            break;
+        }
+    }
+    return (int32_t)size;
 }
 
 /* applyNaturalCompressorNaive: sign and exponent kept, mantissa zeroed, MatrixNMD.h:2013-2031 */
@@ -646,6 +705,314 @@ double orc_log(double x)
     return h + l;
 }
 
+/* ================================================================================== */
+/* Reference arithmetic order (orc_problem.ref_order = 1)                             */
+/* The operation sequence of the reference's AVX2 build without FMA (the reference's   */
+/* SUPPORT_CPU_AVX_256_bits=1, SUPPORT_CPU_FMA_EXT=0 with -mno-fma -ffp-contract=off). */
+/* ================================================================================== */
+
+/* Dot product in the reference's lane order (LightVectorND::operator& and
+ * dotProductForAlignedMemory, dopt/dopt/linalg_vectors/include_internal/LightVector_SIMD_double.h:233-313,
+ * :316-380; VectorNDRaw::operator&, VectorND_Raw_SIMD_double.h:253): two Vec4d accumulators, element
+ * e < 8 floor(n/8) goes to lane e mod 8 (products rounded, then added); each Vec4d is reduced as
+ * (c0 + c2) + (c1 + c3) (horizontal_add, vectorclass/vectorf256.h:1967); the two results are added
+ * to 0 in order; the tail e >= 8 floor(n/8) is summed in order from 0 and added last. */
+double orc_ref_dot(const double* a, const double* b, size_t n)
+{
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    size_t items = n & ~(size_t)7;
+    size_t i = 0;
+    for (; i < items; i += 8)
+        for (int l = 0; l < 8; ++l)
+            c[l] = c[l] + a[i + (size_t)l] * b[i + (size_t)l];
+    double r0 = (c[0] + c[2]) + (c[1] + c[3]);
+    double r1 = (c[4] + c[6]) + (c[5] + c[7]);
+    double fin = 0.0;
+    fin = fin + r0;
+    fin = fin + r1;
+    double rest = 0.0;
+    for (; i < n; ++i)
+        rest = rest + a[i] * b[i];
+    return fin + rest;
+}
+
+/* Squared L2 norm in the same lane order (vectorL2NormSquare, VectorND_Raw_SIMD_double.h:749-800;
+ * LightVectorND::vectorL2NormSquareForAlignedMemory, LightVector_SIMD_double.h:772-830) */
+double orc_ref_norm2(const double* a, size_t n)
+{
+    return orc_ref_dot(a, a, n);
+}
+
+/* The vectorclass exp of one SIMD lane (exp_d<Vec4d, 0, 0>, dopt/dopt/3rdparty/vectorclass/
+ * vectormath_exp.h:141-230, without FMA: mul_add(a, b, c) = a*b + c, nmul_add(a, b, c) = c - a*b,
+ * vectorf256.h:2148-2179): r = round(x log2e) (nearest even), x - r ln2_hi - r ln2_lo, the Taylor
+ * polynomial 1/2! .. 1/13! in the grouping of polynomial_13m (vectormath_common.h:311-321), then
+ * (z + 1) 2^r.  Lanes outside |x| < 708.39 give 0 / +inf, NaN passes through. */
+double orc_exp_vcl(double x0)
+{
+    if (x0 != x0)
+        return x0;
+    if (!(fabs(x0) < 708.39))
+        return (x0 < 0) ? 0.0 : 1.0 / 0.0;
+    const double p2 = 1. / 2., p3 = 1. / 6., p4 = 1. / 24., p5 = 1. / 120., p6 = 1. / 720., p7 = 1. / 5040.;
+    const double p8 = 1. / 40320., p9 = 1. / 362880., p10 = 1. / 3628800., p11 = 1. / 39916800.;
+    const double p12 = 1. / 479001600., p13 = 1. / 6227020800.;
+    const double ln2d_hi = 0.693145751953125, ln2d_lo = 1.42860682030941723212E-6;
+    const double log2e = 1.44269504088896340736;
+    double r = rint(x0 * log2e);
+    double x = x0 - r * ln2d_hi;
+    x = x - r * ln2d_lo;
+    double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
+    double hi = (p13 * x + p12) * x4 + ((p11 * x + p10) * x2 + (p9 * x + p8));
+    double lo = ((p7 * x + p6) * x2 + (p5 * x + p4)) * x4 + ((p3 * x + p2) * x2 + x);
+    double z = hi * x8 + lo;
+    return (z + 1.0) * pow2i((int)r);
+}
+
+/* Correctly rounded exp (own method, used for the reference's scalar tail, which calls libm exp):
+ * x = k ln2 + r with ln2 in three parts (30-bit head, so k*L1 and x - k*L1 are exact), r kept as a
+ * double-double; exp(r 2^-10) by its Taylor series to degree 9 in double-double arithmetic, squared
+ * ten times; one rounding of hi + lo, then the exact scaling by 2^k.  The double-double error is
+ * below 2^-90 relative, so the result is the correctly rounded one for every result in the normal
+ * range except inputs within 2^-90 of a rounding boundary.  libm's exp is within 0.51 ulp and equals
+ * the correctly rounded value for all but a few inputs in ten thousand (measured on glibc 2.39). */
+typedef struct { double hi, lo; } orc_dd;
+
+static inline orc_dd dd_norm(double s, double e)
+{
+    double t = s + e;
+    orc_dd r = {t, e - (t - s)};
+    return r;
+}
+
+static inline orc_dd dd_add(orc_dd a, orc_dd b)
+{
+    double s, e;
+    two_sum(a.hi, b.hi, &s, &e);
+    e = e + (a.lo + b.lo);
+    return dd_norm(s, e);
+}
+
+static inline orc_dd dd_mul(orc_dd a, orc_dd b)
+{
+    double p = a.hi * b.hi;
+    double e = fma(a.hi, b.hi, -p);
+    e = e + (a.hi * b.lo + a.lo * b.hi);
+    return dd_norm(p, e);
+}
+
+double orc_exp_cr(double x)
+{
+    if (x != x)
+        return x;
+    if (x > 709.782712893384)
+        return 1.0 / 0.0;
+    if (x < -745.1332191019412)
+        return 0.0;
+    static const double L1 = 0x1.62e42fe8p-1, L2 = 0x1.e8e7bcd5e4f1ep-31, L3 = -0x1.8cff81a12a17ep-85;
+    static const double inv_fact[10][2] = {
+        {1.0, 0.0}, {1.0, 0.0}, {0x1p-1, 0.0}, {0x1.5555555555555p-3, 0x1.5555555555555p-57},
+        {0x1.5555555555555p-5, 0x1.5555555555555p-59}, {0x1.1111111111111p-7, 0x1.1111111111111p-63},
+        {0x1.6c16c16c16c17p-10, -0x1.f49f49f49f49fp-65}, {0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-73},
+        {0x1.a01a01a01a01ap-16, 0x1.a01a01a01a01ap-76}, {0x1.71de3a556c734p-19, -0x1.c154f8ddc6c00p-73}};
+    double kd = rint(x * 0x1.71547652b82fep+0);
+    double r1 = x - kd * L1;                      /* exact */
+    double p2 = kd * L2;
+    double p2e = fma(kd, L2, -p2);
+    double s, e;
+    two_sum(r1, -p2, &s, &e);
+    e = (e - p2e) - kd * L3;
+    orc_dd y = dd_norm(s, e);
+    y.hi = y.hi * 0x1p-10;
+    y.lo = y.lo * 0x1p-10;
+    orc_dd t = {inv_fact[9][0], inv_fact[9][1]};
+    for (int n = 8; n >= 0; --n) {
+        orc_dd c = {inv_fact[n][0], inv_fact[n][1]};
+        t = dd_add(dd_mul(t, y), c);
+    }
+    for (int q = 0; q < 10; ++q)
+        t = dd_mul(t, t);
+    double p = t.hi + t.lo;
+    int k = (int)kd;
+    if (k > 1000)
+        return (p * pow2i(k - 1000)) * pow2i(1000);
+    if (k < -1000)
+        return (p * pow2i(k + 1000)) * pow2i(-1000);
+    return p * pow2i(k);
+}
+
+/* The vectorclass log of one SIMD lane (log_d<Vec4d, 0>, vectormath_exp.h:947-1003, without FMA):
+ * x = fraction_2(x1) in [0.5, 1), fe = exponent_f(x1); x <= sqrt(2)/2 is doubled, otherwise fe + 1;
+ * x - 1; res = P5(x) x^3 / Q5n(x) (polynomial_5 / polynomial_5n groupings, vectormath_common.h:206-223);
+ * res += fe ln2_lo; res += x - 0.5 x^2; res += fe ln2_hi.  Zero gives -inf, +inf itself, negative
+ * and NaN inputs NaN; subnormal inputs are outside the reference's use (sigmoid values). */
+double orc_log_vcl(double x1)
+{
+    if (x1 != x1 || x1 < 0.0)
+        return 0.0 / 0.0;
+    if (x1 == 0.0)
+        return -1.0 / 0.0;
+    if (x1 == 1.0 / 0.0)
+        return x1;
+    const double ln2_hi = 0.693359375, ln2_lo = -2.121944400546905827679E-4;
+    const double P0 = 7.70838733755885391666E0, P1 = 1.79368678507819816313E1, P2 = 1.44989225341610930846E1;
+    const double P3 = 4.70579119878881725854E0, P4 = 4.97494994976747001425E-1, P5 = 1.01875663804580931796E-4;
+    const double Q0 = 2.31251620126765340583E1, Q1 = 7.11544750618563894466E1, Q2 = 8.29875266912776603211E1;
+    const double Q3 = 4.52279145837532221105E1, Q4 = 1.12873587189167450590E1;
+    const double sqrt2_half = 1.41421356237309504880 * 0.5;
+    uint64_t b;
+    memcpy(&b, &x1, 8);
+    uint64_t fb = (b & 0x000FFFFFFFFFFFFFull) | 0x3FE0000000000000ull;
+    double x;
+    memcpy(&x, &fb, 8);
+    double fe = (double)(int64_t)(b >> 52) - 1023.0;
+    if (x > sqrt2_half)
+        fe = fe + 1.0;
+    else
+        x = x + x;
+    x = x - 1.0;
+    double xx2 = x * x, xx4 = xx2 * xx2;
+    double px = (P3 * x + P2) * xx2 + ((P5 * x + P4) * xx4 + (P1 * x + P0));
+    double x2 = x * x;
+    px = px * (x * x2);
+    double qx = (Q3 * x + Q2) * xx2 + ((Q4 + x) * xx4 + (Q1 * x + Q0));
+    double res = px / qx;
+    res = fe * ln2_lo + res;
+    res = res + (x - x2 * 0.5);
+    res = fe * ln2_hi + res;
+    return res;
+}
+
+/* margins in the reference's order (the AVX2 specialisation of matrixVectorMultiplyWithPreTranspose,
+ * dopt/dopt/linalg_matrices/include/include_internal/MatrixNMD_SIMD_double.h:1256-1430): one Vec4d
+ * accumulator, attribute j < 4 floor(d/4) to lane j mod 4 (a_j x_j rounded, then added), reduced as
+ * (c0 + c2) + (c1 + c3), then the remaining attributes added one by one in order. */
+void orc_margin_ref(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x, double* m)
+{
+    int32_t cb = d & ~3;
+    for (int32_t s = 0; s < n; ++s) {
+        const double* a = atr + (size_t)s * lda;
+        double c[4] = {0, 0, 0, 0};
+        int32_t j = 0;
+        for (; j < cb; j += 4)
+            for (int l = 0; l < 4; ++l)
+                c[l] = c[l] + a[j + l] * x[j + l];
+        double acc = (c[0] + c[2]) + (c[1] + c[3]);
+        for (; j < d; ++j)
+            acc = acc + a[j] * x[j];
+        m[s] = acc;
+    }
+}
+
+/* ||M||_F^2 of a symmetric matrix from its upper part in the reference's order (the AVX2
+ * specialisation of frobeniusNormSquareForSymmetricMatrixFromUpPart / frobeniusNormFor...,
+ * MatrixNMD_SIMD_double.h:1068-1253): eight lane accumulators shared by all columns; in column j the
+ * strictly upper rows i < 8 floor(j/8) go to lane i mod 8, the rows 8 floor(j/8) <= i < j to one
+ * running scalar, the diagonal to another; at the end out = (0 + h(c0..c3)) + h(c4..c7) with
+ * h(c) = (c0 + c2) + (c1 + c3), out += rest, and the result is (out + out) + diagonal. */
+double orc_frob_ref(const double* m, int32_t d, int32_t lda)
+{
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double rest = 0.0, diag = 0.0;
+    for (int32_t j = 0; j < d; ++j) {
+        const double* col = m + (size_t)j * lda;
+        int32_t items = j & ~7;
+        int32_t i = 0;
+        for (; i < items; i += 8)
+            for (int l = 0; l < 8; ++l)
+                c[l] = c[l] + col[i + l] * col[i + l];
+        for (; i < j; ++i)
+            rest = rest + col[i] * col[i];
+        diag = diag + col[j] * col[j];
+    }
+    double out = 0.0;
+    out = out + ((c[0] + c[2]) + (c[1] + c[3]));
+    out = out + ((c[4] + c[6]) + (c[5] + c[7]));
+    out = out + rest;
+    return (out + out) + diag;
+}
+
+/* elementwiseSigmoid (VectorND_Raw_SIMD_double.h:1596-1650): the SIMD lanes s < 8 floor(n/8) use the
+ * vectorclass exp, the tail libm's exp (here: the correctly rounded one) */
+void orc_sigmoid_ref(const double* m, int32_t n, double* sig)
+{
+    int32_t items = n & ~7;
+    for (int32_t s = 0; s < n; ++s)
+        sig[s] = 1.0 / (1.0 + (s < items ? orc_exp_vcl(-m[s]) : orc_exp_cr(-m[s])));
+}
+
+/* logisticUnweightedLossFromMarginSigmoid (VectorND_Raw_SIMD_double.h:1464-1532): lanes c_l -= log
+ * (vectorclass log), the two Vec4d reduced and added as in orc_ref_dot, the tail rest -= log (libm;
+ * here the own log), (fin + rest) / n; plus lambda/2 ||x||^2 in lane order
+ * (evaluateFunction(x, margin, sigmoid), logistic_regression.h:119-123) */
+double orc_client_function_ref(const double* sig, int32_t n, const double* x, int32_t d, double lambda)
+{
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int32_t items = n & ~7;
+    int32_t i = 0;
+    for (; i < items; i += 8)
+        for (int l = 0; l < 8; ++l)
+            c[l] = c[l] - orc_log_vcl(sig[i + l]);
+    double r0 = (c[0] + c[2]) + (c[1] + c[3]);
+    double r1 = (c[4] + c[6]) + (c[5] + c[7]);
+    double fin = 0.0;
+    fin = fin + r0;
+    fin = fin + r1;
+    double rest = 0.0;
+    for (; i < n; ++i)
+        rest = rest - orc_log(sig[i]);
+    double loss = (fin + rest) / (double)n;
+    return loss + (lambda * 0.5) * orc_ref_norm2(x, (size_t)d);
+}
+
+/* choleskyFactorization<Mat, fill_L_factor_in_lower_part=true, in_input_symmetric=true>
+ * (CholeskyFactorization.h:153-272) in its own order: column i, rows j < i:
+ * R_ji = (1 / R_jj) (H_ji - R[0:j, i] . R[0:j, j]) with the lane-ordered dot product, mirrored into
+ * the lower part; then R_ii = sqrt((H_ii + l) - ||R[0:i, i]||^2) (a negative radicand fails). */
+int orc_cholesky_ref(const double* h, int32_t d, int32_t lda, double l, double* ltr)
+{
+    memset(ltr, 0, (size_t)d * (size_t)lda * sizeof(double));
+    for (int32_t i = 0; i < d; ++i) {
+        double* ci = ltr + (size_t)i * lda;
+        for (int32_t j = 0; j < i; ++j) {
+            const double* cj = ltr + (size_t)j * lda;
+            double squares = orc_ref_dot(ci, cj, (size_t)j);
+            double ljj = cj[j];
+            double res = (1.0 / ljj) * (h[(size_t)i * lda + j] - squares);
+            ci[j] = res;
+            ltr[(size_t)j * lda + i] = res;
+        }
+        double squares = orc_ref_norm2(ci, (size_t)i);
+        double res = (h[(size_t)i * lda + i] + l) - squares;
+        if (res < 0) {
+            if (res > -0.0)
+                res = 0.0;
+            else
+                return 0;
+        }
+        ci[i] = sqrt(res);
+    }
+    return 1;
+}
+
+/* forwardSubstitutionWithATranspose then backwardSubstitutionWithATranspose
+ * (ElementarySolvers.h:186-224, :71-128) in their own order: y_0 = b_0 / R_00,
+ * y_i = (b_i - R[0:i, i] . y[0:i]) / R_ii; x_i = (y_i - L[i+1:d, i] . x[i+1:d]) / R_ii with the
+ * lane-ordered dot product over the stored lower column (the mirror of row i of R). */
+void orc_solve_chol_ref(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
+{
+    double* y = (double*)malloc((size_t)d * sizeof(double));
+    y[0] = b[0] / ltr[0];
+    for (int32_t i = 1; i < d; ++i)
+        y[i] = (b[i] - orc_ref_dot(ltr + (size_t)i * lda, y, (size_t)i)) / ltr[(size_t)i * lda + i];
+    for (int32_t i = d - 1; i >= 0; --i) {
+        size_t len = (size_t)(d - 1 - i);
+        double acc = y[i] - orc_ref_dot(ltr + (size_t)i * lda + i + 1, x + i + 1, len);
+        x[i] = acc / ltr[(size_t)i * lda + i];
+    }
+    free(y);
+}
+
 double orc_client_function(const double* sig, int32_t n, const double* x, int32_t d, double lambda)
 {
     double* t = (double*)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
@@ -823,6 +1190,32 @@ struct orc_state {
 /* Worker side of one client, first half: the compressor's index draw, margins, sigmoid, gradient,
  * Hessian and difference (LocalWorkerForFedNL_*.h, bodies of the per-context loops).  Returns
  * ||diff||_F^2. */
+/* margins and sigmoid of one client at x in the selected arithmetic order */
+static void margin_sigmoid(const orc_problem* P, const double* atr, int32_t n, const double* x, double* m,
+                           double* sig)
+{
+    if (P->ref_order) {
+        orc_margin_ref(atr, P->d, P->lda, n, x, m);
+        orc_sigmoid_ref(m, n, sig);
+    } else {
+        orc_margin(atr, P->d, P->lda, n, x, m);
+        orc_sigmoid(m, n, sig);
+    }
+}
+
+/* mean of per-client scalars: the fixed chunked order, or the reference's running sum in client
+ * order times 1/n (function_aggregation, TrainLoop.h:1511-1541) */
+static double client_mean(const orc_problem* P, const double* v, int32_t nc)
+{
+    double inv_n = 1.0 / (double)nc;
+    if (!P->ref_order)
+        return chunked_sum(v, (size_t)nc) * inv_n;
+    double s = 0.0;
+    for (int32_t c = 0; c < nc; ++c)
+        s = s + v[c];
+    return s * inv_n;
+}
+
 static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff, double* mtmp, double* stmp)
 {
     const orc_problem* P = &S->p;
@@ -840,15 +1233,15 @@ static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff
     else if (P->compressor == ORC_RANDK_PHILOX)
         orc_randk_philox(P->seed_base, (uint32_t)c, C->draws++, S->k_eff, U, S->upper, C->msg_idx);
 
-    orc_margin(C->atr, d, lda, n, S->x, mtmp);
-    orc_sigmoid(mtmp, n, stmp);
+    margin_sigmoid(P, C->atr, n, S->x, mtmp, stmp);
     orc_gradient(C->atr, d, lda, n, S->x, stmp, P->lambda, C->grad);
     if (P->line_search || P->track_f)      /* "Put fi" (TopK.h:132-137) */
-        C->fi = orc_client_function(stmp, n, S->x, d, P->lambda);
+        C->fi = P->ref_order ? orc_client_function_ref(stmp, n, S->x, d, P->lambda)
+                             : orc_client_function(stmp, n, S->x, d, P->lambda);
     orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
     for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
         diff[t] = hbuf[t] - C->shift[t];
-    return orc_frob_sym(diff, d, lda);
+    return P->ref_order ? orc_frob_ref(diff, d, lda) : orc_frob_sym(diff, d, lda);
 }
 
 /* Worker side, second half: compression, message and shift update (TopK.h:80-129, TopLEK.h,
@@ -868,7 +1261,8 @@ static void client_compress(orc_state* S, int32_t c, uint32_t* toplek_rng, const
             cnt = orc_topk(diff, k, U, S->upper, C->msg_idx);
         } else {
             double delta = (double)k * (1.0 / (double)U);   /* TopLEK.h:205, :244 */
-            cnt = orc_toplek(diff, lda, k, U, S->upper, delta, frob_sq, toplek_rng, C->msg_idx);
+            cnt = P->ref_order ? orc_toplek_ref(diff, lda, k, U, S->upper, delta, frob_sq, toplek_rng, C->msg_idx)
+                               : orc_toplek(diff, lda, k, U, S->upper, delta, frob_sq, toplek_rng, C->msg_idx);
         }
         C->msg_count = cnt;
         for (int32_t t = 0; t < cnt; ++t) {     /* TopK.h:94-129 */
@@ -958,7 +1352,7 @@ static void client_round_pp(orc_state* S, int32_t c, uint32_t* toplek_rng, doubl
     client_compress(S, c, toplek_rng, diff, frob_sq);
     for (size_t t = 0; t < full; ++t)
         diff[t] = C->shift[t] - hbuf[t];
-    double lk_new = sqrt(orc_frob_sym(diff, d, lda));
+    double lk_new = sqrt(P->ref_order ? orc_frob_ref(diff, d, lda) : orc_frob_sym(diff, d, lda));
     C->dlk = lk_new - C->lk;
     C->lk = lk_new;
     matvec_cols(C->shift, d, lda, S->x, mtmp);
@@ -1060,8 +1454,7 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
         C->msg_val = (double*)malloc(msg_cap * sizeof(double));
         C->rng = p->seed_base + (uint32_t)c;    /* TrainLoop.h:632 */
         /* learningHessian = H_i(x0); H += learningHessian (TrainLoop.h:639-643) */
-        orc_margin(C->atr, d, lda, n, S->x, mtmp);
-        orc_sigmoid(mtmp, n, stmp);
+        margin_sigmoid(p, C->atr, n, S->x, mtmp, stmp);
         orc_hessian(C->atr, d, lda, n, stmp, p->lambda, C->shift);
         for (size_t t = 0; t < full; ++t)
             S->H[t] += C->shift[t];
@@ -1151,11 +1544,11 @@ static double objective_at(orc_state* S, const double* x)
     double* fs = (double*)malloc((size_t)nc * sizeof(double));
     for (int32_t c = 0; c < nc; ++c) {
         orc_client* C = &S->clients[c];
-        orc_margin(C->atr, d, lda, C->n, x, mtmp);
-        orc_sigmoid(mtmp, C->n, stmp);
-        fs[c] = orc_client_function(stmp, C->n, x, d, P->lambda);
+        margin_sigmoid(P, C->atr, C->n, x, mtmp, stmp);
+        fs[c] = P->ref_order ? orc_client_function_ref(stmp, C->n, x, d, P->lambda)
+                             : orc_client_function(stmp, C->n, x, d, P->lambda);
     }
-    double f = chunked_sum(fs, (size_t)nc) * (1.0 / (double)nc);
+    double f = client_mean(P, fs, nc);
     free(mtmp);
     free(stmp);
     free(fs);
@@ -1176,7 +1569,7 @@ static void orc_line_search(orc_state* S, const double* dx)
         t_dg[i] = dx[i] * S->g[i];
         xprev[i] = S->x[i];
     }
-    double dxg = -chunked_sum(t_dg, (size_t)d);
+    double dxg = P->ref_order ? -orc_ref_dot(dx, S->g, (size_t)d) : -chunked_sum(t_dg, (size_t)d);
     double t = 1.0;
     for (int32_t it = 0; it < P->ls_max_steps; ++it) {
         for (int32_t i = 0; i < d; ++i)
@@ -1242,17 +1635,21 @@ int orc_round(orc_state* S, double* grad_norm)
     /* Option B: chol(H + l I), two triangular solves, x -= dx (TrainLoop.h:1431-1508); Option A
      * regularises by mu = lambda instead (:1383-1430, computeMuStrongConvexity) */
     double* dx = (double*)malloc((size_t)d * sizeof(double));
-    int ok = orc_cholesky(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr);
+    int ok = P->ref_order ? orc_cholesky_ref(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr)
+                          : orc_cholesky(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr);
     S->ls_steps = 0;
     if (P->line_search || P->track_f) {       /* function_aggregation (TrainLoop.h:1511-1541) */
         double* fs = (double*)malloc((size_t)nc * sizeof(double));
         for (int32_t c = 0; c < nc; ++c)
             fs[c] = S->clients[c].fi;
-        S->f_k = chunked_sum(fs, (size_t)nc) * inv_n;
+        S->f_k = client_mean(P, fs, nc);
         free(fs);
     }
     if (ok) {
-        orc_solve_chol(S->ltr, d, lda, S->g, dx);
+        if (P->ref_order)
+            orc_solve_chol_ref(S->ltr, d, lda, S->g, dx);
+        else
+            orc_solve_chol(S->ltr, d, lda, S->g, dx);
         if (!P->line_search) {
             for (int32_t i = 0; i < d; ++i)
                 S->x[i] -= dx[i];
@@ -1263,8 +1660,12 @@ int orc_round(orc_state* S, double* grad_norm)
     free(dx);
     if (grad_norm) {
         double gs = 0.0;
-        for (int32_t i = 0; i < d; ++i)
-            gs += S->g[i] * S->g[i];
+        if (P->ref_order) {
+            gs = orc_ref_norm2(S->g, (size_t)d);
+        } else {
+            for (int32_t i = 0; i < d; ++i)
+                gs += S->g[i] * S->g[i];
+        }
         *grad_norm = sqrt(gs);
     }
     return ok ? 0 : -1;

@@ -53,6 +53,8 @@ typedef struct orc_problem {
     double ls_c, ls_gamma;     /* --c_line_search, --gamma_line_search */
     int32_t ls_max_steps;      /* --max_line_search_steps (reference default 5) */
     int32_t track_f;           /* 1: form f(x) every round (--tracking) */
+    int32_t ref_order;         /* 1: the reference's own operation order (lane-ordered dot products,
+                                  vectorclass exp/log, up-looking Cholesky, sequential TopLEK window) */
 } orc_problem;
 
 typedef struct orc_state orc_state;
@@ -86,6 +88,20 @@ double  orc_l2sq(const double* v, size_t n);          /* fixed chunked order, se
 double  orc_frob_sym(const double* m, int32_t d, int32_t lda);
 double  orc_exp(double x);
 double  orc_log(double x);
+/* reference-order arithmetic (ref_order = 1) */
+double  orc_ref_dot(const double* a, const double* b, size_t n);
+double  orc_ref_norm2(const double* a, size_t n);
+double  orc_exp_vcl(double x);
+double  orc_exp_cr(double x);
+double  orc_log_vcl(double x);
+double  orc_frob_ref(const double* m, int32_t d, int32_t lda);
+void    orc_margin_ref(const double* atr, int32_t d, int32_t lda, int32_t n, const double* x, double* m);
+void    orc_sigmoid_ref(const double* m, int32_t n, double* sig);
+double  orc_client_function_ref(const double* sig, int32_t n, const double* x, int32_t d, double lambda);
+int     orc_cholesky_ref(const double* h, int32_t d, int32_t lda, double l, double* ltr);
+void    orc_solve_chol_ref(const double* ltr, int32_t d, int32_t lda, const double* b, double* x);
+int32_t orc_toplek_ref(const double* m, int32_t lda, int32_t k, size_t U, const uint32_t* upper,
+                       double delta, double frob_sq, uint32_t* rng_state, uint32_t* out);
 /* L2-logistic objective of one client from its sigmoid values (evaluateFunction(x, margin, sigmoid),
  * logistic_regression.h:119-123): -mean log sigma_s + lambda/2 ||x||^2 */
 double  orc_client_function(const double* sig, int32_t n, const double* x, int32_t d, double lambda);

@@ -28,7 +28,7 @@ class Problem(C.Structure):
                 ("toplek_seed", C.c_uint32), ("pp", C.c_int32), ("clients_per_round", C.c_int32),
                 ("client_seed", C.c_uint32), ("option_a", C.c_int32), ("line_search", C.c_int32),
                 ("ls_c", C.c_double), ("ls_gamma", C.c_double), ("ls_max_steps", C.c_int32),
-                ("track_f", C.c_int32)]
+                ("track_f", C.c_int32), ("ref_order", C.c_int32)]
 
 
 def build() -> str:
@@ -66,8 +66,9 @@ def lib():
         L.orc_get_f.argtypes = [C.c_void_p]
         L.orc_get_ls_steps.restype = C.c_int32
         L.orc_get_ls_steps.argtypes = [C.c_void_p]
-        L.orc_log.restype = C.c_double
-        L.orc_log.argtypes = [C.c_double]
+        for f in ("orc_log", "orc_exp", "orc_exp_vcl", "orc_exp_cr", "orc_log_vcl"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.c_double]
         L.orc_get_message.restype = C.c_int32
         L.orc_get_message.argtypes = [C.c_void_p, C.c_int32, up, dp]
         L.orc_upper_indices.argtypes = [C.c_int32, C.c_int32, up]
@@ -160,10 +161,11 @@ class FedNL:
 
     def __init__(self, prob, compressor, k, alpha, lda=None, workers=1, threads=None,
                  seed_base=123, toplek_seed=1234, x0=None, clients_per_round=None, client_seed=1234,
-                 option_a=False, line_search=None, track_f=False):
+                 option_a=False, line_search=None, track_f=False, ref_order=False):
         """clients_per_round set: FedNL-PP (bin_fednl_local_pp) with that many clients per round.
         option_a: Cholesky of H + lambda I (--fednl-option-a).  line_search = (c, gamma, max_steps):
-        FedNL-LS (--line_search).  track_f: form f(x) every round (--tracking)."""
+        FedNL-LS (--line_search).  track_f: form f(x) every round (--tracking).  ref_order: the
+        reference's own operation order (bit-exact with the reference's no-FMA AVX2 build)."""
         self.d = prob.d
         self.lda = lda if lda is not None else (prob.d + 3) // 4 * 4
         self._keep = [np.ascontiguousarray(prob.n_samples, dtype=np.int32),
@@ -177,7 +179,7 @@ class FedNL:
                     1 if clients_per_round else 0, int(clients_per_round or 0), client_seed,
                     1 if option_a else 0, 1 if line_search else 0,
                     float(line_search[0]) if line_search else 0.5, float(line_search[1]) if line_search else 0.5,
-                    int(line_search[2]) if line_search else 5, 1 if track_f else 0)
+                    int(line_search[2]) if line_search else 5, 1 if track_f else 0, 1 if ref_order else 0)
         self.pp = bool(clients_per_round)
         x0 = np.zeros(self.d) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
         self._h = lib().orc_create(C.byref(p), _dp(x0))

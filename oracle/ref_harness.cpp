@@ -25,13 +25,39 @@
 #include "dopt/copylocal/include/Data.h"
 #include "dopt/copylocal/include/MutableData.h"
 
+#include <atomic>
 #include <barrier>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <cstdint>
 #include <functional>
 #include <thread>
 #include <vector>
+
+// the oracle's correctly rounded exp (oracle/fednl_oracle.c), linked in to check the reference's
+// scalar libm exp calls
+extern "C" double orc_exp_cr(double x);
+
+// The reference's sigmoid evaluates its scalar tail (samples 8 floor(n/8) .. n-1) with libm's exp
+// (VectorND_Raw_SIMD_double.h:1596-1650).  glibc's exp is within 0.51 ulp but not correctly rounded:
+// for a few inputs in ten thousand it returns the other neighbour, and sometimes that changes the
+// sigmoid value 1 / (1 + exp(-m)).  This records the first round in which a tail sigmoid differs
+// from the one formed with the correctly rounded exp, so a checker that uses a correctly rounded exp
+// knows from which round on it cannot reproduce the reference's bits.
+static std::atomic<int32_t> g_first_misround{-1};
+
+static void note_tail_sigmoid(const dopt::VectorNDRaw_d& margin, const dopt::VectorNDRaw_d& sig, int32_t round)
+{
+    size_t n = margin.size();
+    for (size_t s = n & ~size_t(7); s < n; ++s) {
+        if (1.0 / (1.0 + orc_exp_cr(-margin.get(s))) != sig.get(s)) {
+            int32_t cur = g_first_misround.load();
+            while ((cur < 0 || round < cur) && !g_first_misround.compare_exchange_weak(cur, round)) {
+            }
+        }
+    }
+}
 
 typedef dopt::VectorNDRaw_d Vec;
 typedef dopt::MatrixNMD<Vec> Mat;
@@ -180,6 +206,8 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
     std::vector<uint32_t> upper = dopt::indiciesForUpperTriangularPart(H);
     W.put<int32_t>((int32_t)H.LDA);
 
+    int32_t cur_round = 0;
+    g_first_misround = -1;
     auto client_step = [&](Client& C) {
         Problem* P = C.prob;
         if (comp == kRandK)
@@ -188,6 +216,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
             C.idx = dopt::generateRandSeqKItemsInUpperTriangularPart(C.rng, k, C.shift, upper);
         Vec margin = P->evaluateClassificationMargin(x);
         Vec sig = P->evaluateClassificationMarginSigmoid(margin);
+        note_tail_sigmoid(margin, sig, cur_round);
         C.grad = P->evaluateGradient(x, margin, sig);
         if (line_search || track_f) C.fi = P->evaluateFunction(x, margin, sig);
         Mat hess = P->evaluateHessian(x, margin, sig);
@@ -216,6 +245,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
 
     Mat Ltr;
     for (int32_t r = 0; r < rounds; ++r) {
+        cur_round = r;
         start_bar.arrive_and_wait();
         done_bar.arrive_and_wait();
         Vec g(d);
@@ -251,6 +281,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
                 for (int32_t c = 0; c < nc; ++c) {
                     Vec mg = cl[c].prob->evaluateClassificationMargin(x);
                     Vec sg = cl[c].prob->evaluateClassificationMarginSigmoid(mg);
+                    note_tail_sigmoid(mg, sg, cur_round);
                     fr += cl[c].prob->evaluateFunction(x, mg, sg);
                 }
                 fr *= inv_n;
@@ -280,6 +311,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
     start_bar.arrive_and_wait();
     for (auto& t : th) t.join();
     for (auto& c : cl) delete c.prob;
+    W.put<int32_t>(g_first_misround.load());   // trailer: first round whose sigmoid a libm misrounding changed
     fclose(fi);
     fclose(fo);
     return 0;

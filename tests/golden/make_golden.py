@@ -30,7 +30,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
+sys.path.insert(0, os.path.dirname(HERE))
+
 from ufednl_gb300 import datagen  # noqa: E402
+from golden_runs import message_digest, problem_digest  # noqa: E402
 
 COMP = {"identity": 0, "randk": 1, "topk": 2, "randseqk": 3, "toplek": 4, "natural": 5}
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
@@ -41,9 +44,12 @@ def _skip(kind):
     return ONLY is not None and not kind.startswith(ONLY)
 
 
-def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds, ext=None):
+def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds, ext=None, workload=None):
     """ext = dict(option_a, line_search, ls_max, track_f, ls_c, ls_gamma): the extended run
-    (Option A / FedNL-LS / tracking), written as runx_<name>.npz with f(x_k) and line-search counts."""
+    (Option A / FedNL-LS / tracking), written as runx_<name>.npz with f(x_k) and line-search counts.
+    workload = the datagen workload function's name: the fixture stores that name and a digest of
+    the generated inputs instead of the inputs, and per-client message digests instead of the
+    messages (the workload-sized runs)."""
     if _skip("runx" if ext else "run"):
         return
     with tempfile.TemporaryDirectory() as td:
@@ -87,18 +93,23 @@ def run_case(name, prob, comp, k, alpha, workers, rounds, dump_rounds, ext=None)
                 msg_idx.append(take("<u4", cnt))
                 msg_val.append(take("<f8", cnt))
                 lks.append(float(take("<f8", 1)[0]))
+    misround = int(take("<i4", 1)[0])
     assert pos == len(raw)
     extra = {}
     if ext:
         extra = dict(f=np.array(fks), ls_steps=np.array(lss, dtype=np.int32), **{k_: v for k_, v in ext.items()})
+    if workload:
+        inputs = dict(workload=workload, inputs_sha256=problem_digest(prob), n_samples=prob.n_samples)
+        msgs = dict(msg_digest=np.array([message_digest(i, v, lk) for i, v, lk in zip(msg_idx, msg_val, lks)]))
+    else:
+        inputs = dict(n_samples=prob.n_samples, features=prob.features, labels=prob.labels)
+        msgs = dict(msg_idx=np.concatenate(msg_idx).astype(np.uint32), msg_val=np.concatenate(msg_val))
     np.savez_compressed(
         os.path.join(HERE, f"{'runx' if ext else 'run'}_{name}.npz"),
-        d=d, lda=lda, n_samples=prob.n_samples, features=prob.features, labels=prob.labels,
-        lam=prob.lam, compressor=comp, k=k, alpha=alpha, workers=workers, rounds=rounds,
+        d=d, lda=lda, lam=prob.lam, compressor=comp, k=k, alpha=alpha, workers=workers, rounds=rounds,
         dump_rounds=dump_rounds, ok=np.array(ok), gnorm=np.array(gnorm), l=np.array(lval),
-        x=np.array(xs), msg_count=np.array(msg_cnt, dtype=np.int32),
-        msg_idx=np.concatenate(msg_idx).astype(np.uint32), msg_val=np.concatenate(msg_val),
-        lk=np.array(lks), **extra)
+        x=np.array(xs), msg_count=np.array(msg_cnt, dtype=np.int32), lk=np.array(lks),
+        libm_first_misround=misround, **inputs, **msgs, **extra)
 
 
 def pp_case(name, prob, comp, k, alpha, tau, rounds, dump_rounds, sel_seed=1234):
@@ -281,9 +292,12 @@ def wire_case(name, rng):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default=os.environ.get("REF_ROOT", "/root/reference/dopt"))
+    ap.add_argument("--ref-root", default=os.environ.get("REF_ROOT"),
+                    help="the reference's dopt source folder (or set REF_ROOT)")
     ap.add_argument("--only", default=None, help="regenerate only fixtures whose kind starts with this (run, pp, ...)")
     args = ap.parse_args()
+    if not args.ref_root:
+        ap.error("the reference source folder is needed: --ref-root PATH or REF_ROOT=PATH")
     global ONLY
     ONLY = args.only
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_ROOT={args.ref_root}"],
@@ -305,6 +319,13 @@ def main():
     run_case("toplek_d40", mid, "toplek", 320, 1.0, 3, 60, 3)
     dense = datagen.dense_problem(13, 10, [30, 22, 41], 1e-2)
     run_case("topk_dense_d10", dense, "topk", 20, 1.0, 1, 8, 3)
+
+    # the benchmark workloads at full size: a9a-like (d=124, 80 x 407, TopK k=8d) and w8a-like
+    # (d=301, 142 clients n_i 200-600, TopLEK k=8d, 16 reference workers)
+    run_case("topk_a9a_d124", datagen.workload_a9a_like(), "topk", 8 * 124, 1.0, 8, 12, 12,
+             workload="workload_a9a_like")
+    run_case("toplek_w8a_d301", datagen.workload_w8a_like(), "toplek", 8 * 301, 1.0, 16, 8, 8,
+             workload="workload_w8a_like")
 
     # the reference's LIBSVM loader on tricky text
     for nm, txt in LIBSVM_TEXTS.items():

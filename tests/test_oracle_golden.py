@@ -8,17 +8,20 @@ import os
 import numpy as np
 import pytest
 
+import golden_runs
 from conftest import golden_path
-from ufednl_gb300 import datagen
 
-RUNS = sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz")))
+ALL_RUNS = sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz")))
+# the oracle's default (fixed-order) arithmetic is held to the converged-minimiser contract, which
+# the short workload-sized runs do not reach
+RUNS = [p for p in ALL_RUNS if "_a9a_" not in p and "_w8a_" not in p]
 SELECTS = sorted(glob.glob(golden_path("select_*.npz")))
 RANDS = sorted(glob.glob(golden_path("rand_*.npz")))
 PPS = sorted(glob.glob(golden_path("pp_*.npz")))
 
 
 def _problem(z):
-    return datagen.Problem(int(z["d"]), z["n_samples"], z["features"], z["labels"], float(z["lam"]))
+    return golden_runs.problem_of(z)
 
 
 def _full(m, d, lda):
@@ -27,12 +30,7 @@ def _full(m, d, lda):
     return full.reshape(-1)
 
 
-def run_kwargs(z):
-    """Option A / FedNL-LS / tracking switches of an extended golden run (runx_*.npz)."""
-    if "f" not in z:
-        return {}
-    ls = (float(z["ls_c"]), float(z["ls_gamma"]), int(z["ls_max"])) if int(z["line_search"]) else None
-    return dict(option_a=bool(int(z["option_a"])), line_search=ls, track_f=bool(int(z["track_f"])))
+run_kwargs = golden_runs.run_kwargs
 
 
 def check_run_against_reference(fed, z, prob):
@@ -97,6 +95,50 @@ def test_run_matches_reference(oracle, path):
                        workers=int(z["workers"]), **run_kwargs(z))
     check_run_against_reference(fed, z, prob)
     fed.close()
+
+
+@pytest.mark.parametrize("path", ALL_RUNS, ids=lambda p: os.path.basename(p))
+def test_run_bitexact_reference_order(oracle, path):
+    """The oracle in the reference's own operation order reproduces the reference's golden runs bit
+    for bit (iterates, ||g||, l, every message and Lk) up to the first round in which glibc's exp
+    misrounded a sigmoid tail value, and within 1e-10 after it; the workload-sized runs (a9a-like
+    d=124 TopK, w8a-like d=301 TopLEK with 16 workers) included."""
+    z = np.load(path)
+    prob = _problem(z)
+    fed = oracle.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
+                       workers=int(z["workers"]), threads=min(8, int(z["workers"])), ref_order=True,
+                       **run_kwargs(z))
+    exact = golden_runs.check_run_bitexact(fed, z, prob.n_clients)
+    fed.close()
+    assert exact >= 1
+
+
+def test_reference_order_primitives(oracle):
+    """The vectorclass exp restatement against its published definition on edge inputs, the
+    correctly rounded exp against 200-bit arithmetic, and the lane-ordered dot product against the
+    order written out by hand."""
+    import math
+    import mpmath
+    L = oracle.lib()
+    mpmath.mp.prec = 200
+    rng = np.random.default_rng(7)
+    for x in np.concatenate([rng.uniform(-40, 40, 3000), rng.uniform(-745, 709, 500)]):
+        cr = float(mpmath.exp(mpmath.mpf(float(x))))
+        assert L.orc_exp_cr(float(x)) == cr, x
+    assert L.orc_exp_vcl(0.0) == 1.0 and L.orc_exp_vcl(-800.0) == 0.0 and L.orc_exp_vcl(800.0) == math.inf
+    a, b = rng.standard_normal(21), rng.standard_normal(21)
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    L.orc_ref_dot.restype = C.c_double
+    L.orc_ref_dot.argtypes = [dp, dp, C.c_size_t]
+    c = [0.0] * 8
+    for i in range(16):
+        c[i % 8] = c[i % 8] + a[i] * b[i]
+    fin = (0.0 + ((c[0] + c[2]) + (c[1] + c[3]))) + ((c[4] + c[6]) + (c[5] + c[7]))
+    rest = 0.0
+    for i in range(16, 21):
+        rest = rest + a[i] * b[i]
+    assert L.orc_ref_dot(a.ctypes.data_as(dp), b.ctypes.data_as(dp), 21) == fin + rest
 
 
 def check_pp_against_reference(fed, z, prob):
