@@ -78,8 +78,17 @@ typedef struct fednl_problem_desc {
     double ls_c, ls_gamma;      /* --c_line_search, --gamma_line_search */
     int32_t ls_max_steps;       /* --max_line_search_steps (reference default 5) */
     int32_t track_f;            /* 1: form f(x) at every round's starting iterate (--tracking) */
-    int32_t reserved[2];        /* must be zero */
+    /* Arithmetic order (plain FedNL only): FEDNL_ORDER_FIXED (0) is the engine's own fixed order,
+     * reproducible on every GPU and equal to the test oracle bit for bit; FEDNL_ORDER_REFERENCE (1)
+     * performs the IEEE operations of the reference's AVX2 build without FMA in its order
+     * (two-Vec4d dot products and norms, vectorclass exp/log in SIMD lanes, up-looking Cholesky,
+     * TopLEK window numerators one by one), which reproduces the reference's rounds bit for bit;
+     * the reference's scalar libm exp tail is replaced by the correctly rounded exp. */
+    int32_t arith_order;
+    int32_t reserved;           /* must be zero */
 } fednl_problem_desc;
+
+enum { FEDNL_ORDER_FIXED = 0, FEDNL_ORDER_REFERENCE = 1 };
 
 typedef struct fednl_round_stats {
     int32_t round;              /* index of the round just completed */

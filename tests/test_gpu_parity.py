@@ -10,6 +10,7 @@ import os
 import numpy as np
 import pytest
 
+import golden_runs
 from conftest import golden_path
 from ufednl_gb300 import datagen
 
@@ -31,7 +32,7 @@ def _full(m, d, lda):
 
 
 def _problem(z):
-    return datagen.Problem(int(z["d"]), z["n_samples"], z["features"], z["labels"], float(z["lam"]))
+    return golden_runs.problem_of(z)
 
 
 # ---- compressors against the reference's golden vectors -----------------------------------
@@ -190,27 +191,46 @@ def test_logreg_oracle_vs_cpu(gpu, oracle, kind):
 
 # ---- whole runs -------------------------------------------------------------------------------
 
-@pytest.mark.parametrize("path", sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz"))),
-                         ids=os.path.basename)
+ALL_RUNS = sorted(glob.glob(golden_path("run_*.npz")) + glob.glob(golden_path("runx_*.npz")))
+
+
+@pytest.mark.parametrize("path", [p for p in ALL_RUNS if "_a9a_" not in p and "_w8a_" not in p], ids=os.path.basename)
 def test_run_golden(gpu, path):
-    """Whole runs against the reference's golden runs, same contract as the CPU oracle's (Option A,
-    FedNL-LS and tracked objective values included)."""
-    from test_oracle_golden import check_run_against_reference, run_kwargs
+    """Whole runs in the engine's fixed order against the reference's golden runs, same contract as
+    the CPU oracle's (Option A, FedNL-LS and tracked objective values included)."""
+    from test_oracle_golden import check_run_against_reference
     z = np.load(path)
     prob = _problem(z)
     fed = gpu.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
-                    workers=int(z["workers"]), **run_kwargs(z))
+                    workers=int(z["workers"]), **golden_runs.run_kwargs(z))
     check_run_against_reference(fed, z, prob)
     fed.close()
 
 
-def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None, **opts):
+@pytest.mark.parametrize("path", ALL_RUNS, ids=os.path.basename)
+def test_run_golden_reference_order(gpu, path):
+    """Whole runs in the reference's arithmetic order reproduce the reference's golden runs bit for
+    bit (iterates, ||g||, l, every client's message and Lk) up to the first round whose sigmoid
+    glibc's exp misrounded, and within 1e-10 after it; the a9a-like (d=124, 80 x 407, TopK) and
+    w8a-like (d=301, 142 clients, TopLEK with 16 reference workers) workloads at full size."""
+    z = np.load(path)
+    prob = _problem(z)
+    fed = gpu.FedNL(prob, str(z["compressor"]), int(z["k"]), float(z["alpha"]), lda=int(z["lda"]),
+                    workers=int(z["workers"]), order="reference", **golden_runs.run_kwargs(z))
+    exact = golden_runs.check_run_bitexact(fed, z, prob.n_clients)
+    fed.close()
+    assert exact >= 1
+
+
+def _compare_runs(gpu, oracle, prob, comp, k, alpha, rounds, workers, threads=None, order="fixed", **opts):
     """GPU and CPU oracle perform the same IEEE operations in the same order: every round's
     iterate, aggregated gradient, l and every client's message must agree bit for bit (and f(x_k)
-    and the line-search evaluation count when those options are on)."""
+    and the line-search evaluation count when those options are on).  order: the engine's fixed
+    order or the reference's."""
     threads = threads or min(workers, os.cpu_count() or 1)
-    orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads, **opts)
-    fed = gpu.FedNL(prob, comp, k, alpha, workers=workers, **opts)
+    orc = oracle.FedNL(prob, comp, k, alpha, workers=workers, threads=threads, ref_order=order == "reference",
+                       **opts)
+    fed = gpu.FedNL(prob, comp, k, alpha, workers=workers, order=order, **opts)
     for r in range(rounds):
         go = orc.round()
         gg = fed.round()
@@ -281,6 +301,31 @@ def test_run_vs_oracle_w8a_like_full_size(gpu, oracle):
     _compare_runs(gpu, oracle, prob, "toplek", 8 * 301, 1.0, 3, workers=8, threads=os.cpu_count())
 
 
+@pytest.mark.parametrize("comp", ["topk", "toplek", "randk", "randseqk", "natural", "identity"])
+def test_run_vs_oracle_reference_order(gpu, oracle, comp):
+    """The reference-order kernels against the oracle's reference-order restatement, bit for bit,
+    on uneven clients with tail samples (n_i not multiples of 8) and d not a multiple of 8."""
+    prob = datagen.binary_problem(25, 30, [37, 52, 29, 61, 44, 33], 0.15, 1e-3)
+    U = 30 * 31 // 2
+    k = {"topk": 120, "toplek": 150, "randk": 60, "randseqk": 30, "natural": U, "identity": U}[comp]
+    alpha = {"randk": k / U, "randseqk": k / U, "natural": 8 / 9}.get(comp, 1.0)
+    _compare_runs(gpu, oracle, prob, comp, k, alpha, 8, workers=4, order="reference")
+
+
+def test_run_options_vs_oracle_reference_order(gpu, oracle):
+    """FedNL-LS, tracked objective values and Option A in the reference's order; dense features;
+    the w8a-like workload at full size."""
+    prob = datagen.binary_problem(26, 30, [37, 52, 29, 61, 44, 33], 0.15, 1e-3)
+    _compare_runs(gpu, oracle, prob, "topk", 120, 1.0, 10, workers=4, order="reference",
+                  line_search=(0.5, 0.5, 5), track_f=True)
+    _compare_runs(gpu, oracle, prob, "randk", 60, 60 / 465, 6, workers=4, order="reference", option_a=True)
+    dense = datagen.dense_problem(27, 19, [31, 27, 40], 1e-2)
+    _compare_runs(gpu, oracle, dense, "topk", 38, 1.0, 6, workers=2, order="reference")
+    w8a = datagen.workload_w8a_like()
+    _compare_runs(gpu, oracle, w8a, "toplek", 8 * 301, 1.0, 3, workers=16, threads=os.cpu_count(),
+                  order="reference")
+
+
 def test_run_is_deterministic(gpu):
     prob = datagen.binary_problem(23, 40, [50, 61, 47, 55], 0.2, 1e-3)
     xs = []
@@ -311,3 +356,7 @@ def test_edge_cases(gpu, oracle):
     one = datagen.Problem(1, np.array([4, 2], dtype=np.int32), np.ones((6, 1)),
                           np.array([1.0, -1, 1, 1, -1, 1]), 1e-2)
     _compare_runs(gpu, oracle, one, "topk", 1, 1.0, 3, workers=1)
+    for order in ("reference",):
+        for comp, k in (("topk", U), ("toplek", U + 5), ("topk", 1), ("toplek", 1)):
+            _compare_runs(gpu, oracle, prob, comp, k, 1.0, 3, workers=2, order=order)
+        _compare_runs(gpu, oracle, one, "topk", 1, 1.0, 3, workers=1, order=order)

@@ -8,6 +8,7 @@
 
 #include "fednl_gpu.h"
 #include "fednl_kernels.cuh"
+#include "fednl_refmode.cuh"
 #include "fednl_chol32c.cuh"
 #include "fednl_solve.h"
 #include "fednl_smem.h"
@@ -130,6 +131,35 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record);
+}
+
+// the reference-order solve of the master's system (k_chol_ref, one cooperative launch)
+cudaError_t launch_chol_ref(const Dev& P, int grid, cudaStream_t st, const double* lptr, double lval, double* dxout,
+                            double* xupd, int record)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kRefCholThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_chol_ref, P, (const double*)P.H, lptr, lval, (const double*)P.g, dxout, xupd,
+                              record);
+}
+
+// CTAs of the reference-order solve: its trailing updates are light, its cost is the per-block
+// barriers and the pivot rows, so a modest grid
+int ref_grid()
+{
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_ref, kRefCholThreads, 0);
+    return std::max(1, std::min(32, sms * std::max(1, bps)));
 }
 
 }  // namespace
@@ -472,6 +502,7 @@ struct fednl_handle_s {
     size_t hess_smem = 0;
     bool hess_smem_bits = true;
     int chol_grid = 1;
+    int ref_grid = 1;          // CTAs of the reference-order solve
     int rounds_done = 0;
     void* flush_buf = nullptr;
     size_t flush_cap = 0;
@@ -511,9 +542,14 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
             h->nc, h->tau, P.sampler, P.perm, (int*)P.act, P.is_sel, P.needs, h->pp_smem_perm);
         CKL();
     }
-    MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
-    if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
-    else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    if (P.ref) {
+        MARK("k_margin_ref");
+        k_margin_ref<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    } else {
+        MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
+        if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+        else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    }
     CKL();
     MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
     dim3 gg(h->binary ? (2 * h->d + 127) / 128 : (h->d + 127) / 128, h->nc);   // binary: a lane pair per attribute
@@ -539,8 +575,13 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, hmode);
     }
     CKL();
-    MARK("k_fsum");
-    k_fsum<<<(na + 3) / 4, 128, 0, st>>>(P);
+    if (P.ref) {
+        MARK("k_frob_ref");
+        k_frob_ref<<<(na + 3) / 4, 128, 0, st>>>(P);
+    } else {
+        MARK("k_fsum");
+        k_fsum<<<(na + 3) / 4, 128, 0, st>>>(P);
+    }
     CKL();
     int comp = h->comp;
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
@@ -548,7 +589,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         double delta = (double)h->k * (1.0 / (double)h->U);
         k_select<<<na, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
             P.diff, h->ustr, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F, P.sel, h->SW, P.cnt, P.needs, P.pdraw,
-            P.minidx, P.status, P.act);
+            P.minidx, P.status, P.act, P.ref);
         CKL();
         if (comp == FEDNL_TOPLEK) {
             MARK("k_toplek_rng");
@@ -593,33 +634,44 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     CKL();
     if (P.fmode) {       // f(x_k) from the round's sigmoid values
         MARK("k_fclient");
-        k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, nullptr);
+        if (P.ref) k_fclient_ref<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, nullptr);
+        else k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, nullptr);
         CKL();
         MARK("k_fmaster");
-        k_fmaster<<<1, 32, 0, st>>>(P, P.stats + 2);
+        if (P.ref) k_fmaster_ref<<<1, 32, 0, st>>>(P, P.stats + 2);
+        else k_fmaster<<<1, 32, 0, st>>>(P, P.stats + 2);
         CKL();
     }
     if (client_phase_only) return FEDNL_OK;
     const fednl_problem_desc& D = h->desc;
     const double* lptr = D.option_a ? nullptr : P.stats + 1;      // Option A: H + lambda I
-    MARK("k_chol_coop");
-    CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1));
+    if (P.ref) {
+        MARK("k_chol_ref");
+        CK(launch_chol_ref(P, h->ref_grid, st, lptr, P.lambda, P.dx, D.line_search ? nullptr : P.x, 1));
+    } else {
+        MARK("k_chol_coop");
+        CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1));
+    }
     if (D.line_search) {
         MARK("k_ls_init");
-        k_ls_init<<<1, 256, 0, st>>>(P);
+        if (P.ref) k_ls_init_ref<<<1, 256, 0, st>>>(P);
+        else k_ls_init<<<1, 256, 0, st>>>(P);
         CKL();
         for (int it = 0; it < D.ls_max_steps; ++it) {
             MARK("k_ls_trial");
             k_ls_trial<<<(h->d + 255) / 256, 256, 0, st>>>(P);
             CKL();
             MARK("k_ls_margin");
-            k_ls_margin<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+            if (P.ref) k_ls_margin_ref<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+            else k_ls_margin<<<(S + 255) / 256, 256, 0, st>>>(P, S);
             CKL();
             MARK("k_fclient");
-            k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, P.ls);
+            if (P.ref) k_fclient_ref<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, P.ls);
+            else k_fclient<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, P.ls);
             CKL();
             MARK("k_ls_check");
-            k_ls_check<<<1, 32, 0, st>>>(P, D.ls_c, D.ls_gamma);
+            if (P.ref) k_ls_check_ref<<<1, 32, 0, st>>>(P, D.ls_c, D.ls_gamma);
+            else k_ls_check<<<1, 32, 0, st>>>(P, D.ls_c, D.ls_gamma);
             CKL();
         }
     }
@@ -664,8 +716,11 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     const fednl_problem_desc& D = *desc;
     if (D.d < 1 || D.n_clients < 1 || !D.n_samples) return fail(FEDNL_EINVAL, "d and n_clients must be >= 1");
     if (D.compressor < 0 || D.compressor > 6) return fail(FEDNL_EINVAL, "unknown compressor %d", D.compressor);
-    for (int i = 0; i < 2; ++i)
-        if (D.reserved[i]) return fail(FEDNL_EINVAL, "reserved fields must be zero");
+    if (D.reserved) return fail(FEDNL_EINVAL, "reserved fields must be zero");
+    if (D.arith_order != FEDNL_ORDER_FIXED && D.arith_order != FEDNL_ORDER_REFERENCE)
+        return fail(FEDNL_EINVAL, "unknown arith_order %d", D.arith_order);
+    if (D.arith_order == FEDNL_ORDER_REFERENCE && D.clients_per_round > 0)
+        return fail(FEDNL_EINVAL, "the reference arithmetic order is available for plain FedNL only");
     if (D.clients_per_round < 0 || D.clients_per_round > D.n_clients)
         return fail(FEDNL_EINVAL, "clients_per_round %d outside [0, n_clients]", D.clients_per_round);
     if (D.line_search && (D.clients_per_round > 0 || D.ls_max_steps < 1 || !(D.ls_c > 0.0) || !(D.ls_gamma > 0.0) ||
@@ -736,6 +791,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     P.pp = h->pp;
     P.n_act = h->tau;
     P.fmode = (D.line_search || D.track_f) && !h->pp;
+    P.ref = D.arith_order == FEDNL_ORDER_REFERENCE;
     size_t ncU = (size_t)h->nc * h->ustr;
     Arena& A = h->state;
     A.want((int**)&P.ns, h->nc);
@@ -771,6 +827,11 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     A.want(&P.status, 1);
     A.want(&P.stats, 4);
     A.want(&P.bar, 4);
+    if (P.ref) {
+        const size_t ua = (size_t)(h->d + 1) * (h->d + 2) / 2;
+        A.want(&P.rref, ua);
+        A.want(&P.racc, 9 * ua);
+    }
     if (P.fmode) {
         A.want(&P.fterm, h->S);
         A.want(&P.fi, h->nc);
@@ -819,6 +880,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     if (select_smem(h->k) > 48 * 1024 && h->k < h->U)
         fednl_raise_dyn_smem((const void*)k_select, select_smem(h->k));
     h->chol_grid = chol_grid(h->d);
+    if (P.ref) h->ref_grid = ref_grid();
     *out = h;
     return FEDNL_OK;
 }
@@ -1010,7 +1072,8 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
     if (x0) CK(cudaMemcpyAsync(P.x, x0, h->d * 8, cudaMemcpyHostToDevice, st));
     else CK(cudaMemsetAsync(P.x, 0, h->d * 8, st));
     int S = h->S;
-    if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    if (P.ref) k_margin_ref<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    else if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
     CKL();
     if (h->binary) {    // gradient pass also forms the diagonal sums the Hessian kernel reuses
@@ -1619,7 +1682,7 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
         CK(fednl_raise_dyn_smem((const void*)k_select, select_smem(k)));
     double delta = (double)k * (1.0 / (double)U);
     k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)ustr, (int)U, k, lek ? 1 : 0, delta,
-                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr);
+                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr, 0);
     CKL();
     if (lek) {
         int W = std::max(1, n_workers);

@@ -94,6 +94,10 @@ struct Dev {
     double* fi;             // [nc] f_i at the last evaluated point
     double* xprev;          // [d] x_k during the line search
     double* ls;             // [5] line search: t, -(dx . g), done, evaluations, solve succeeded
+    // the reference's arithmetic order (fednl_refmode.cuh)
+    int ref;                // 1: FEDNL_ORDER_REFERENCE
+    double* rref;           // [(d+1)(d+2)/2] Cholesky factor with y as column d
+    double* racc;           // [9][(d+1)(d+2)/2] lane and tail accumulators of its dot products
 };
 
 // ---- helpers -------------------------------------------------------------------------------
@@ -714,7 +718,8 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int ustr, int U, int k,
                                                         int lek, double delta, const double* __restrict__ F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
-                                                        double* pdraw, int* minidx, int* err, const int* act)
+                                                        double* pdraw, int* minidx, int* err, const int* act,
+                                                        int ref)
 {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     __shared__ __align__(8) unsigned long long s_bar[2];
@@ -854,18 +859,28 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
         // heap terms in heap-array order, chunk trees, then the chunk sums in order
         for (int t = tid; t < k; t += blockDim.x) terms[t] = term_of(h.key[t], h.hid[t]);
         __syncthreads();
-        for (int q = warp; q < nch; q += nwarps) {
-            const int t = q * 32 + lane;
-            const double cs = chunk_tree(t < k ? terms[t] : 0.0);
-            if (lane == 0) csum[q] = cs;
+        if (!ref) {
+            for (int q = warp; q < nch; q += nwarps) {
+                const int t = q * 32 + lane;
+                const double cs = chunk_tree(t < k ? terms[t] : 0.0);
+                if (lane == 0) csum[q] = cs;
+            }
         }
         __syncthreads();
         if (warp == 0) {
-            double sh = 0.0;
-            if (lane == 0)
-                for (int q = 0; q < nch; ++q) sh = __dadd_rn(sh, csum[q]);
             const double fr = F[c];
-            const double num0 = __dsub_rn(fr, __shfl_sync(0xffffffffu, sh, 0));
+            double num0;
+            if (ref) {   // the reference's order: ||M||^2 minus each heap term in heap-array order
+                double nm = fr;
+                if (lane == 0)
+                    for (int t = 0; t < k; ++t) nm = __dsub_rn(nm, terms[t]);
+                num0 = __shfl_sync(0xffffffffu, nm, 0);
+            } else {
+                double sh = 0.0;
+                if (lane == 0)
+                    for (int q = 0; q < nch; ++q) sh = __dadd_rn(sh, csum[q]);
+                num0 = __dsub_rn(fr, __shfl_sync(0xffffffffu, sh, 0));
+            }
             // window test of SpecialMathRoutinesForMatrix.h:475-476 on the numerators before (prev) and
             // after (next) extraction m: hi > prev and omd < next + eps
             const double omd = __dmul_rn(__dsub_rn(1.0, delta), fr);
@@ -962,6 +977,30 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
                     __syncwarp();
                     const int m = q * 32 + lane;
                     double x = (m < k) ? term_of(h.key[k - 1 - m], h.hid[k - 1 - m]) : 0.0;
+                    if (ref) {   // numerators one extraction at a time (every lane walks the same chain)
+                        int hit = -1;
+                        double run = carry, ph = 0.0, nh = 0.0;
+                        const int nq = min(32, k - q * 32);
+                        for (int t = 0; t < nq; ++t) {
+                            const double tt = __shfl_sync(0xffffffffu, x, t);
+                            const double nx = __dadd_rn(run, tt);
+                            if (hi > run && omd < __dadd_rn(nx, eps)) {
+                                hit = t;
+                                ph = run;
+                                nh = nx;
+                                break;
+                            }
+                            run = nx;
+                        }
+                        if (hit >= 0) {
+                            first = q * 32 + hit;
+                            prev_hit = ph;
+                            next_hit = nh;
+                            break;
+                        }
+                        carry = run;
+                        continue;
+                    }
                     for (int hh = 1; hh < 32; hh <<= 1) {
                         const double y = __shfl_up_sync(0xffffffffu, x, hh);
                         if (lane >= hh) x = __dadd_rn(x, y);

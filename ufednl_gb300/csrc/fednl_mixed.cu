@@ -353,8 +353,9 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     if (D.n_clients < 1 || !D.n_samples) return fail_m(FEDNL_EINVAL, "no clients");
     if (D.compressor != FEDNL_RANDK_PHILOX && D.compressor != FEDNL_TOPK && D.compressor != FEDNL_TOPLEK)
         return fail_m(FEDNL_EINVAL, "the mixed-precision form runs TopK, TopLEK or RandK-Philox");
-    for (int i = 0; i < 2; ++i)
-        if (D.reserved[i]) return fail_m(FEDNL_EINVAL, "reserved fields must be zero");
+    if (D.reserved) return fail_m(FEDNL_EINVAL, "reserved fields must be zero");
+    if (D.arith_order != FEDNL_ORDER_FIXED)
+        return fail_m(FEDNL_EINVAL, "the mixed-precision form has no reference arithmetic order");
     if (D.option_a || D.line_search || D.clients_per_round)
         return fail_m(FEDNL_EINVAL, "the mixed-precision form runs plain FedNL with Option B");
     const long long U = (long long)D.d * (D.d + 1) / 2;

@@ -43,7 +43,11 @@ class ProblemDesc(C.Structure):
                 ("feature_format", C.c_int32), ("clients_per_round", C.c_int32),
                 ("client_seed", C.c_uint32), ("option_a", C.c_int32), ("line_search", C.c_int32),
                 ("ls_c", C.c_double), ("ls_gamma", C.c_double), ("ls_max_steps", C.c_int32), ("track_f", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("arith_order", C.c_int32), ("reserved", C.c_int32)]
+
+
+# arithmetic order of the FP64 engine: its own fixed order, or the reference's (bit for bit)
+ORDERS = {"fixed": 0, "reference": 1}
 
 
 class RoundStats(C.Structure):
@@ -292,7 +296,9 @@ class FedNL:
     def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
                  seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0,
                  clients_per_round: int = 0, client_seed: int = 1234, option_a: bool = False,
-                 line_search=None, track_f: bool = False):
+                 line_search=None, track_f: bool = False, order: str = "fixed"):
+        """order: "fixed" (the engine's own order, bit-identical to the test oracle) or "reference"
+        (the reference's operation order, bit-identical to the reference's rounds)."""
         self.d = prob.d
         self.lda = lda or reference_lda(prob.d)
         self.n_clients = prob.n_clients
@@ -304,7 +310,7 @@ class FedNL:
                            int(clients_per_round or 0), int(client_seed), 1 if option_a else 0,
                            1 if line_search else 0, float(line_search[0]) if line_search else 0.5,
                            float(line_search[1]) if line_search else 0.5, int(line_search[2]) if line_search else 5,
-                           1 if track_f else 0, (C.c_int32 * 2)(0, 0))
+                           1 if track_f else 0, ORDERS[order], 0)
         self.pp = bool(clients_per_round)
         h = C.c_void_p()
         _check(load().fednl_gpu_create(C.byref(desc), C.byref(h)))
@@ -510,8 +516,7 @@ class MixedFedNL:
         self._ns = np.ascontiguousarray(prob.n_samples, dtype=np.int32)
         comp = COMPRESSORS[compressor] if isinstance(compressor, str) else int(compressor)
         desc = ProblemDesc(self.d, 0, self.n_clients, _ip(self._ns), float(prob.lam), comp, int(k),
-                           float(alpha), 1, int(seed_base), int(toplek_seed), 2, 0, 1234, 0, 0, 0.5, 0.5, 5, 0,
-                           (C.c_int32 * 2)(0, 0))
+                           float(alpha), 1, int(seed_base), int(toplek_seed), 2, 0, 1234, 0, 0, 0.5, 0.5, 5, 0, 0, 0)
         h = C.c_void_p()
         _check(load().fednl_mx_create(C.byref(desc), C.byref(h)))
         self._h = h

@@ -127,7 +127,7 @@ def _desc(req: Request, ns: np.ndarray) -> ProblemDesc:
     if req.precision == PRECISION_MIXED:
         fmt = 2
     return ProblemDesc(d, 0, req.n_clients, _ip(ns), req.lam, comp, k, alpha, 1, 123 + req.pid, 1234, fmt,
-                       0, 1234, 0, 0, 0.5, 0.5, 5, 0, (C.c_int32 * 2)(0, 0))
+                       0, 1234, 0, 0, 0.5, 0.5, 5, 0, 0, 0)
 
 
 def footprint(req: Request) -> int:
@@ -178,7 +178,7 @@ class Server:
         comp = fednl.COMPRESSORS[compressor]
         fmt = 2 if precision == PRECISION_MIXED else 0
         desc = ProblemDesc(prob.d, 0, prob.n_clients, _ip(ns), float(prob.lam), comp, int(k), float(alpha), 1,
-                           int(seed_base), 1234, fmt, 0, 1234, 0, 0, 0.5, 0.5, 5, 0, (C.c_int32 * 2)(0, 0))
+                           int(seed_base), 1234, fmt, 0, 1234, 0, 0, 0.5, 0.5, 5, 0, 0, 0)
         want = np.float32 if precision == PRECISION_MIXED else np.float64
         f = np.ascontiguousarray(prob.features, dtype=want)
         y = np.ascontiguousarray(prob.labels, dtype=np.float64)
