@@ -177,6 +177,35 @@ int fednl_gpu_randseqk(uint32_t* states, int32_t n_gen, int32_t d, int32_t lda, 
  * 3 bytes per pair (pack2FP64NoMantissa, dopt/dopt/system/include/FloatUtils.h:193-221). */
 int fednl_gpu_natural(const double* in, int64_t n, double* out, uint8_t* packed);
 
+/* Shift update of the sparse compressors, batched over n_mat clients (LocalWorkerForFedNL_TopK.h:
+ * 103-129, RandK.h:136-162): for every selected flat index f = j * lda + i (i <= j) of client m,
+ * item = diffs[m][f] * value_mult, shifts[m][f] += alpha * item and, for i != j, the mirror
+ * shifts[m][i * lda + j] += alpha * item.  value_mult is 1 for TopK / TopLEK and U / k for RandK /
+ * RandSeqK (RandK.h:90).  shifts and diffs: n_mat column-major d x lda matrices; shifts is updated
+ * in place.  idx[m * k_stride + t], t < counts[m]: the client's selected flat indices (distinct
+ * upper entries; anything else returns FEDNL_EINVAL). */
+int fednl_gpu_shift_update(double* shifts, const double* diffs, int32_t n_mat, int32_t d, int32_t lda,
+                           const uint32_t* idx, const int32_t* counts, int32_t k_stride, double alpha,
+                           double value_mult);
+
+/* Master aggregation of one round (TrainLoop.h:1100-1333 with --debug forcesequpdate): the clients'
+ * gradients grads[n_clients][d] summed in client order then times 1/n into g[d]; their Lk summed in
+ * client order then times 1/n into *l; every client's message values added to H (column-major
+ * d x lda, upper entries updated in place) in client order: H[idx[c * k_stride + t]] +=
+ * vals[c * k_stride + t] for t < counts[c] (values as the master adds them: the worker's alpha / n
+ * pre-scaling included).  k_stride = 0: no Hessian messages (idx, vals, counts unused). */
+int fednl_gpu_aggregate(int32_t n_clients, int32_t d, int32_t lda, const double* grads, const double* lks,
+                        const uint32_t* idx, const double* vals, const int32_t* counts, int32_t k_stride,
+                        double* H, double* g, double* l);
+
+/* Identity compressor, batched over n_mat clients (LocalWorkerForFedNL_Identical.h:80-94): the
+ * message of client m is every upper entry of diffs[m] in the upper-index order (column j, rows
+ * 0..j): idx_out[m * U + p] its flat index, val_out[m * U + p] = diff * prescale (prescale = alpha / n,
+ * TrainLoop.h:531); shifts[m] += alpha * diffs[m] on both triangles (in place).  shifts, idx_out and
+ * val_out may each be NULL. */
+int fednl_gpu_compress_identity(const double* diffs, int32_t n_mat, int32_t d, int32_t lda, double alpha,
+                                double prescale, double* shifts, uint32_t* idx_out, double* val_out);
+
 /* Logistic oracle of one client: evaluateGradient and evaluateHessian<true, 4>
  * (dopt/dopt/optimization_problems/include/ml/logistic_regression.h:148-547).
  * features row-major [n][d], labels [n]; grad [d]; hess [d * lda] column-major symmetric. */
@@ -393,8 +422,25 @@ typedef void (*fednl_result_callback)(int x_dimension, double grad_norm, double 
  * --use_theoretical_alpha_option_1|2, --fednl-option-a|b, --line_search with --c_line_search,
  * --gamma_line_search, --max_line_search_steps, --tracking, --out, --debug).  Returns the
  * reference's TrainReturnCodes (0 ok, -1 missing argument, -2 wrong argument, -3 dataset missing,
- * -4 parse error, -5 split error, -6 saving failed, -7 internal error, -8 unknown debug mode). */
+ * -4 parse error, -5 split error, -6 saving failed, -7 internal error, -8 unknown debug mode).
+ * Engine option: --gpu-arith-order reference|fixed (default reference: the rounds reproduce the
+ * reference's values bit for bit; fixed: the engine's faster fixed order). */
 int fednl_gpu_execute_local(const char* command, fednl_result_callback callback);
+
+/* The reference's own exported symbols, so that a program linked against the reference's
+ * shared_bin_fednl_local / shared_bin_fednl_local_pp can load this library instead.
+ * doptExecuteLocal replaces bin_fednl_local/exported/FedNLLocalShared.h:8-17 (the same as
+ * fednl_gpu_execute_local).  doptExecuteLocalPP replaces
+ * bin_fednl_local_pp/exported/FedNLPPLocalShared.h:8-16: bin_fednl_local_pp's command line, i.e. the
+ * flags above without the line search plus --clients-per-round (required, 1..clients; the client
+ * sampler's seed is the reference's fixed 1234, Args.h:243-264); the rounds run in the engine's
+ * fixed order; the callback receives the dimension (TrainLoop.h:1870-1871); the tracking records
+ * carry NaN in place of f(x).  Same return codes. */
+typedef void (*ResultCallbackLocal)(int xDimension, double discrWithOptSolution, double discrWithOptValue,
+                                    double L2NormInLastIterate);
+typedef void (*ResultCallbackLocalPP)(int xDimension);
+int doptExecuteLocal(const char* command, ResultCallbackLocal resultCallback);
+int doptExecuteLocalPP(const char* command, ResultCallbackLocalPP resultCallback);
 
 /* The reference's LIBSVM text loader (dataset_loader_fs.h:380-885 as TrainLoop.h:124-180 drives
  * it): labels remapped to +-1 around the mean of the smallest and largest label, attribute

@@ -14,7 +14,8 @@ HEADER = os.path.join(REPO, "include", "fednl_gpu.h")
 
 def header_symbols():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|int32_t|double|const char\*)\s+(fednl_(?:gpu|mx|server)_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int32_t|double|const char\*)\s+(fednl_(?:gpu|mx|server)_\w+|doptExecute\w+)\s*\(",
+                                 txt, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -30,7 +31,7 @@ def test_header_declares_the_binding_table(lib):
 
 def test_library_exports_every_declared_symbol(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", lib.lib_path()], capture_output=True, text=True, check=True)
-    exported = set(re.findall(r"\bT (fednl_(?:gpu|mx|server)_\w+)", out.stdout))
+    exported = set(re.findall(r"\bT (fednl_(?:gpu|mx|server)_\w+|doptExecute\w+)", out.stdout))
     missing = [s for s in header_symbols() if s not in exported]
     assert not missing, missing
     L = lib.load()

@@ -360,3 +360,109 @@ def test_edge_cases(gpu, oracle):
         for comp, k in (("topk", U), ("toplek", U + 5), ("topk", 1), ("toplek", 1)):
             _compare_runs(gpu, oracle, prob, comp, k, 1.0, 3, workers=2, order=order)
         _compare_runs(gpu, oracle, one, "topk", 1, 1.0, 3, workers=1, order=order)
+
+
+# ---- the remaining operator entries of the reference's worker and master ----------------------
+
+def _sym_full(rng, n, d, lda):
+    out = np.zeros((n, d, lda))
+    for m in range(n):
+        a = rng.standard_normal((d, d))
+        out[m, :, :d] = np.triu(a) + np.triu(a, 1).T
+    return out.reshape(n, -1)
+
+
+@pytest.mark.parametrize("comp", ["topk", "randk"])
+def test_shift_update_operator(gpu, oracle, comp):
+    """fednl_gpu_shift_update against the worker's update written out in numpy
+    (LocalWorkerForFedNL_TopK.h:103-129 / RandK.h:136-162), bit for bit, on TopK and RandK selections."""
+    rng = np.random.default_rng(31)
+    d, lda, n = 37, 40, 5
+    U = d * (d + 1) // 2
+    k = 3 * d
+    diffs = _sym_full(rng, n, d, lda)
+    shifts = _sym_full(rng, n, d, lda)
+    if comp == "topk":
+        idx = np.stack([oracle.topk(diffs[m], d, lda, k) for m in range(n)])
+        mult = 1.0
+    else:
+        st = np.array([123], dtype=np.uint32)
+        idx = np.stack([oracle.randk(st, d, lda, k) for _ in range(n)])
+        mult = U / k
+    counts = np.full(n, k, dtype=np.int32)
+    counts[2] = k // 2                        # a shorter message (TopLEK keeps fewer than k)
+    alpha = 0.75
+    want = shifts.copy()
+    got = gpu.shift_update(shifts.copy(), diffs, d, lda, idx, counts, alpha, mult)
+    for m in range(n):
+        for f in idx[m, :counts[m]]:
+            f = int(f)
+            j, i = divmod(f, lda)
+            item = diffs[m, f] * mult if mult != 1.0 else diffs[m, f]
+            upd = alpha * item
+            want[m, f] = want[m, f] + upd
+            if i != j:
+                want[m, i * lda + j] = want[m, i * lda + j] + upd
+    np.testing.assert_array_equal(got, want)
+    bad = idx.copy()
+    bad[0, 0] = 1                             # row 1 of column 0: below the diagonal
+    with pytest.raises(gpu.FedNLError):
+        gpu.shift_update(shifts, diffs, d, lda, bad, counts, alpha, mult)
+
+
+def test_aggregate_operator(gpu):
+    """fednl_gpu_aggregate against the master's merge in client order (TrainLoop.h:1100-1333), bit for
+    bit: g and l as running sums times 1/n, H += each client's message in client order."""
+    rng = np.random.default_rng(32)
+    d, lda, nc, k = 29, 32, 9, 60
+    U = d * (d + 1) // 2
+    up = np.array([j * lda + i for j in range(d) for i in range(j + 1)], dtype=np.uint32)
+    grads = rng.standard_normal((nc, d))
+    lks = rng.random(nc)
+    H = _sym_full(rng, 1, d, lda)[0]
+    idx = np.stack([np.sort(rng.choice(up, k, replace=False)) for _ in range(nc)]).astype(np.uint32)
+    vals = rng.standard_normal((nc, k)) * 1e-3
+    counts = np.full(nc, k, dtype=np.int32)
+    counts[4] = 17
+    Hg, g, l = gpu.aggregate(grads, lks, d, lda, H, idx, vals, counts)
+    gw = np.zeros(d)
+    lw = 0.0
+    Hw = H.copy()
+    for c in range(nc):
+        gw = gw + grads[c]
+        lw = lw + lks[c]
+        Hw[idx[c, :counts[c]].astype(np.int64)] += vals[c, :counts[c]]
+    np.testing.assert_array_equal(g, gw * (1.0 / nc))
+    assert l == lw * (1.0 / nc)
+    np.testing.assert_array_equal(Hg, Hw)
+    H0, g0, l0 = gpu.aggregate(grads, lks, d, lda, H)             # no Hessian messages
+    np.testing.assert_array_equal(H0, H)
+    np.testing.assert_array_equal(g0, g)
+    dup = idx.copy()
+    dup[1, 1] = dup[1, 0]
+    with pytest.raises(gpu.FedNLError):
+        gpu.aggregate(grads, lks, d, lda, H, dup, vals, counts)
+    assert U > k
+
+
+def test_compress_identity_operator(gpu, oracle):
+    """fednl_gpu_compress_identity against LocalWorkerForFedNL_Identical.h:80-94 written out in numpy:
+    message = upper entries times alpha/n in the upper-index order, shift += alpha diff on both
+    triangles, bit for bit."""
+    rng = np.random.default_rng(33)
+    d, lda, n = 21, 24, 4
+    diffs = _sym_full(rng, n, d, lda)
+    shifts = _sym_full(rng, n, d, lda)
+    alpha, pre = 1.0, 1.0 / 7.0
+    idx, vals, sh = gpu.compress_identity(diffs, d, lda, alpha, pre, shifts)
+    up = oracle.upper_indices(d, lda)
+    for m in range(n):
+        np.testing.assert_array_equal(idx[m], up)
+        np.testing.assert_array_equal(vals[m], diffs[m][up.astype(np.int64)] * pre)
+        want = shifts[m].copy()
+        full = diffs[m].reshape(d, lda)
+        for j in range(d):
+            for i in range(d):
+                v = full[max(i, j), min(i, j)]
+                want[j * lda + i] = want[j * lda + i] + alpha * v
+        np.testing.assert_array_equal(sh[m], want)

@@ -60,6 +60,23 @@ def test_execute_local_argument_errors(lib, tmp_path):
     assert lib.execute_local(base.replace("--fednl-option-b", "") + " --compressor topk")[0] == -1
     assert lib.execute_local(base.replace("--rounds 3", "") + " --compressor topk")[0] == -1
     assert lib.execute_local(base.replace("--clients 2", "--clients 99") + " --compressor topk")[0] == -5
+    assert lib.execute_local(base + " --compressor topk --gpu-arith-order sideways")[0] == -1
+
+
+def test_reference_symbols_argument_errors(lib, tmp_path):
+    """doptExecuteLocal / doptExecuteLocalPP under the reference's names: the same return codes as the
+    reference's train() before any device work; the PP binary needs --clients-per-round in 1..clients."""
+    data = golden_path("libsvm_binary01.txt")
+    base = (f"--train_dataset {data} --clients 2 --lambda 0.001 --rounds 3 --algorithm fednl1 "
+            f"--k_compressor_as_d_mult 1 --alpha_step_size 1 --fednl-option-b --compressor topk "
+            f"--out {tmp_path}/t.bin")
+    assert lib.dopt_execute_local("--lambda 0.1")[0] == -1
+    assert lib.dopt_execute_local(base + " --debug bogus")[0] == -8
+    assert lib.dopt_execute_local_pp(base)[0] == -1                                   # no --clients-per-round
+    assert lib.dopt_execute_local_pp(base + " --clients-per-round 0")[0] == -1
+    assert lib.dopt_execute_local_pp(base + " --clients-per-round 3")[0] == -1         # more than --clients
+    assert lib.dopt_execute_local_pp(base + " --clients-per-round 1 --gpu-arith-order reference")[0] == -1
+    assert lib.dopt_execute_local_pp(base.replace("topk", "fancy") + " --clients-per-round 1")[0] == -2
 
 
 def _write_libsvm(path, prob):
@@ -114,7 +131,7 @@ def test_execute_local_matches_api_run(lib, tmp_path, extra, comp, k):
     opts = dict(track_f=True)
     if "line_search" in extra:
         opts["line_search"] = (0.5, 0.5, 5)
-    fed = lib.FedNL(p2, comp_api, kk, alpha, workers=3, **opts)
+    fed = lib.FedNL(p2, comp_api, kk, alpha, workers=3, order="reference", **opts)
     gn, fs = [], []
     for _ in range(12):
         gn.append(fed.round())
@@ -124,6 +141,9 @@ def test_execute_local_matches_api_run(lib, tmp_path, extra, comp, k):
     g2 = float(np.dot(g, g))
     assert cbv[0] == d
     assert cbv[1] == pytest.approx(np.sqrt(g2), rel=1e-12, abs=1e-300)
+    # the reference's own symbol gives the same callback values
+    rc2, cbv2 = lib.dopt_execute_local(cmd)
+    assert rc2 == 0 and cbv2 == cbv
     # tracking file: header then one record per round (TrainLoop.h:753-792, 1679-1691)
     raw = open(str(tmp_path / f"track_fednl1_data.bin"), "rb").read()
     parts = raw.split(b"\0", 3)
@@ -138,3 +158,38 @@ def test_execute_local_matches_api_run(lib, tmp_path, extra, comp, k):
         assert rec[0] == r
         assert rec[1] == gn[r]
         assert rec[2] == fs[r]
+
+
+@pytest.mark.gpu
+def test_execute_local_pp_matches_api_run(lib, tmp_path):
+    """doptExecuteLocalPP: bin_fednl_local_pp's command line (even split over 8 clients, 3 sampled per
+    round by the reference's fixed-seed sampler, RandSeqK with the theoretical alpha); the callback
+    receives the dimension and the tracked ||true gradient|| per round equals the same FedNL-PP run
+    made through the Python API."""
+    prob = datagen.binary_problem(43, 12, [20] * 8, 0.35, 1e-3)
+    body = datagen.Problem(prob.d - 1, prob.n_samples, prob.features[:, :-1], prob.labels, prob.lam)
+    data = tmp_path / "pp.txt"
+    _write_libsvm(data, body)
+    out = tmp_path / "pp_{algorithm}.bin"
+    cmd = (f"--train_dataset {data} --clients 8 --clients-per-round 3 --add_intercept --lambda 0.001 "
+           f"--rounds 10 --workers 2 --algorithm fednl1 --compressor seqk --k_compressor_as_d_mult 1 "
+           f"--theoretical_alpha --fednl-option-b --tracking --out {out}")
+    rc, d_cb = lib.dopt_execute_local_pp(cmd)
+    assert rc == 0
+    x, y = lib.load_libsvm(str(data), True)
+    d = x.shape[1]
+    assert d_cb == d
+    n = len(y) // 8
+    p2 = datagen.Problem(d, np.full(8, n, dtype=np.int32), x[:8 * n], y[:8 * n], 1e-3)
+    U = d * (d + 1) // 2
+    fed = lib.FedNL(p2, "randseqk", d, 1.0 / (U / d - 1.0 + 1.0), workers=2, clients_per_round=3)
+    gn = [fed.round() for _ in range(10)]
+    fed.close()
+    raw = open(str(tmp_path / "pp_fednl1.bin"), "rb").read()
+    parts = raw.split(b"\0", 3)
+    assert parts[0] == b"pp" and parts[1].startswith(b"FedNL-PP") and parts[2] == b"seqk"
+    recs = parts[3][56:]
+    assert len(recs) == 10 * 52
+    for r in range(10):
+        rec = struct.unpack("<i6d", recs[r * 52:(r + 1) * 52])
+        assert rec[0] == r and rec[1] == gn[r]

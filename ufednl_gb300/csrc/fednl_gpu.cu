@@ -1819,6 +1819,146 @@ int fednl_gpu_natural(const double* in, int64_t n, double* out, uint8_t* packed)
     return FEDNL_OK;
 }
 
+int fednl_gpu_shift_update(double* shifts, const double* diffs, int32_t n_mat, int32_t d, int32_t lda,
+                           const uint32_t* idx, const int32_t* counts, int32_t k_stride, double alpha,
+                           double value_mult)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!shifts || !diffs || !idx || !counts || n_mat < 1 || d < 1 || lda < d || k_stride < 1)
+        return fail(FEDNL_EINVAL, "bad argument");
+    const size_t full = (size_t)d * lda;
+    int kmax = 0;
+    for (int m = 0; m < n_mat; ++m) {
+        if (counts[m] < 0 || counts[m] > k_stride) return fail(FEDNL_EINVAL, "count %d outside [0, k_stride]", counts[m]);
+        for (int t = 0; t < counts[m]; ++t) {
+            const uint32_t f = idx[(size_t)m * k_stride + t];
+            const uint32_t jc = f / (uint32_t)lda, ir = f - jc * (uint32_t)lda;
+            if (jc >= (uint32_t)d || ir > jc) return fail(FEDNL_EINVAL, "index %u is not an upper entry", f);
+        }
+        kmax = std::max(kmax, counts[m]);
+    }
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *dsh, *ddf;
+    unsigned* didx;
+    int* dcnt;
+    s.a.want(&dsh, (size_t)n_mat * full);
+    s.a.want(&ddf, (size_t)n_mat * full);
+    s.a.want(&didx, (size_t)n_mat * k_stride);
+    s.a.want(&dcnt, n_mat);
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dsh, shifts, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(ddf, diffs, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(didx, idx, (size_t)n_mat * k_stride * 4, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dcnt, counts, (size_t)n_mat * 4, cudaMemcpyHostToDevice, s.st));
+    if (kmax > 0) {
+        k_op_shift_update<<<dim3((kmax + 255) / 256, n_mat), 256, 0, s.st>>>(dsh, ddf, n_mat, lda, full, didx, dcnt,
+                                                                          k_stride, alpha, value_mult);
+        CKL();
+    }
+    CK(cudaMemcpyAsync(shifts, dsh, (size_t)n_mat * full * 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_aggregate(int32_t n_clients, int32_t d, int32_t lda, const double* grads, const double* lks,
+                        const uint32_t* idx, const double* vals, const int32_t* counts, int32_t k_stride, double* H,
+                        double* g, double* l)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!grads || !lks || !H || !g || !l || n_clients < 1 || d < 1 || lda < d || k_stride < 0 ||
+        (k_stride > 0 && (!idx || !vals || !counts)))
+        return fail(FEDNL_EINVAL, "bad argument");
+    const long long U = (long long)d * (d + 1) / 2;
+    const size_t full = (size_t)d * lda;
+    for (int c = 0; c < n_clients && k_stride > 0; ++c) {
+        if (counts[c] < 0 || counts[c] > k_stride || counts[c] > U)
+            return fail(FEDNL_EINVAL, "count %d outside [0, min(k_stride, U)]", counts[c]);
+        std::vector<char> seen((size_t)U, 0);
+        for (int t = 0; t < counts[c]; ++t) {
+            const uint32_t f = idx[(size_t)c * k_stride + t];
+            const uint32_t jc = f / (uint32_t)lda, ir = f - jc * (uint32_t)lda;
+            if (jc >= (uint32_t)d || ir > jc) return fail(FEDNL_EINVAL, "index %u is not an upper entry", f);
+            const size_t p = (size_t)jc * (jc + 1) / 2 + ir;
+            if (seen[p]) return fail(FEDNL_EINVAL, "client %d sends entry %u twice", c, f);
+            seen[p] = 1;
+        }
+    }
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *dgr, *dlk, *dH, *dg, *dl, *dval = nullptr;
+    unsigned* didx = nullptr;
+    int *dcnt = nullptr, *dslot = nullptr;
+    s.a.want(&dgr, (size_t)n_clients * d);
+    s.a.want(&dlk, n_clients);
+    s.a.want(&dH, full);
+    s.a.want(&dg, d);
+    s.a.want(&dl, 1);
+    if (k_stride > 0) {
+        s.a.want(&didx, (size_t)n_clients * k_stride);
+        s.a.want(&dval, (size_t)n_clients * k_stride);
+        s.a.want(&dcnt, n_clients);
+        s.a.want(&dslot, (size_t)n_clients * U);
+    }
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dgr, grads, (size_t)n_clients * d * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dlk, lks, (size_t)n_clients * 8, cudaMemcpyHostToDevice, s.st));
+    CK(cudaMemcpyAsync(dH, H, full * 8, cudaMemcpyHostToDevice, s.st));
+    k_op_aggregate_g<<<(d + 127) / 128, 128, 0, s.st>>>(dgr, dlk, n_clients, d, 1.0 / (double)n_clients, dg, dl);
+    CKL();
+    if (k_stride > 0) {
+        CK(cudaMemcpyAsync(didx, idx, (size_t)n_clients * k_stride * 4, cudaMemcpyHostToDevice, s.st));
+        CK(cudaMemcpyAsync(dval, vals, (size_t)n_clients * k_stride * 8, cudaMemcpyHostToDevice, s.st));
+        CK(cudaMemcpyAsync(dcnt, counts, (size_t)n_clients * 4, cudaMemcpyHostToDevice, s.st));
+        CK(cudaMemsetAsync(dslot, 0xff, (size_t)n_clients * U * 4, s.st));
+        k_op_message_slots<<<dim3((k_stride + 255) / 256, n_clients), 256, 0, s.st>>>(didx, dcnt, k_stride, n_clients,
+                                                                                     lda, dslot, (int)U);
+        CKL();
+        k_op_aggregate_h<<<(unsigned)((U + 127) / 128), 128, 0, s.st>>>(dH, d, lda, (int)U, dval, dslot, k_stride,
+                                                                        n_clients);
+        CKL();
+    }
+    CK(cudaMemcpyAsync(H, dH, full * 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(g, dg, (size_t)d * 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(l, dl, 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return FEDNL_OK;
+}
+
+int fednl_gpu_compress_identity(const double* diffs, int32_t n_mat, int32_t d, int32_t lda, double alpha,
+                                double prescale, double* shifts, uint32_t* idx_out, double* val_out)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (!diffs || n_mat < 1 || d < 1 || lda < d) return fail(FEDNL_EINVAL, "bad argument");
+    const long long U = (long long)d * (d + 1) / 2;
+    const size_t full = (size_t)d * lda;
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double *ddf, *dsh = nullptr, *dval = nullptr;
+    unsigned* didx = nullptr;
+    s.a.want(&ddf, (size_t)n_mat * full);
+    if (shifts) s.a.want(&dsh, (size_t)n_mat * full);
+    if (idx_out) s.a.want(&didx, (size_t)n_mat * U);
+    if (val_out) s.a.want(&dval, (size_t)n_mat * U);
+    rc = s.a.commit();
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ddf, diffs, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
+    if (shifts) CK(cudaMemcpyAsync(dsh, shifts, (size_t)n_mat * full * 8, cudaMemcpyHostToDevice, s.st));
+    k_op_identity<<<dim3((unsigned)((U + 255) / 256), n_mat), 256, 0, s.st>>>(ddf, dsh, n_mat, lda, full, (int)U, alpha,
+                                                                             prescale, didx, dval);
+    CKL();
+    if (shifts) CK(cudaMemcpyAsync(shifts, dsh, (size_t)n_mat * full * 8, cudaMemcpyDeviceToHost, s.st));
+    if (idx_out) CK(cudaMemcpyAsync(idx_out, didx, (size_t)n_mat * U * 4, cudaMemcpyDeviceToHost, s.st));
+    if (val_out) CK(cudaMemcpyAsync(val_out, dval, (size_t)n_mat * U * 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return FEDNL_OK;
+}
+
 int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_t n, int32_t d, int32_t lda,
                             double lambda, const double* x, double* grad, double* hess)
 {

@@ -1784,6 +1784,103 @@ __global__ void __launch_bounds__(kCoopThreads) k_chol_batched(const CholJob* __
 }
 
 // ---- operator-level helpers -----------------------------------------------------------------
+// Shift update of the sparse compressors (LocalWorkerForFedNL_TopK.h:103-129; RandK.h:136-162):
+// for every selected flat index j*lda + i of matrix m, item = diff[idx] (times U/k for RandK and
+// RandSeqK, already part of the message), shift[idx] += alpha item and, off the diagonal, the mirror
+// shift[i*lda + j] += alpha item.  One thread per (matrix, selected entry); the entries of one matrix
+// are distinct upper positions, so no two threads touch the same element.
+__global__ void k_op_shift_update(double* shifts, const double* diffs, int n_mat, int lda, size_t full,
+                                  const unsigned* idx, const int* counts, int kstride, double alpha, double mult)
+{
+    const int m = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_mat || t >= counts[m]) return;
+    const unsigned f = idx[(size_t)m * kstride + t];
+    const unsigned jc = f / (unsigned)lda, ir = f - jc * (unsigned)lda;
+    const double item = (mult == 1.0) ? diffs[(size_t)m * full + f] : __dmul_rn(diffs[(size_t)m * full + f], mult);
+    const double upd = __dmul_rn(alpha, item);
+    double* sh = shifts + (size_t)m * full;
+    sh[f] = __dadd_rn(sh[f], upd);
+    if (ir != jc) {
+        const size_t g = (size_t)ir * lda + jc;
+        sh[g] = __dadd_rn(sh[g], upd);
+    }
+}
+
+// Master aggregation (TrainLoop.h:1100-1333 with forcesequpdate): g = (sum of the clients'
+// gradients in client order) * (1/n), l = (sum of Lk in client order) * (1/n); H[idx] += value for
+// every client message in client order.  One thread per H position of the upper triangle walks the
+// clients in order (each client's message holds a position at most once), one per coordinate of g.
+__global__ void k_op_aggregate_g(const double* grads, const double* lks, int nc, int d, double inv_n, double* g,
+                                 double* l)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < d) {
+        double s = 0.0;
+        for (int c = 0; c < nc; ++c) s = __dadd_rn(s, grads[(size_t)c * d + j]);
+        g[j] = __dmul_rn(s, inv_n);
+    }
+    if (j == 0) {
+        double s = 0.0;
+        for (int c = 0; c < nc; ++c) s = __dadd_rn(s, lks[c]);
+        *l = __dmul_rn(s, inv_n);
+    }
+}
+
+// per client: the message's upper positions scattered into a [nc][U] map of message slots (-1: none)
+__global__ void k_op_message_slots(const unsigned* idx, const int* counts, int kstride, int nc, int lda, int* slot,
+                                   int U)
+{
+    const int c = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc || t >= counts[c]) return;
+    const unsigned f = idx[(size_t)c * kstride + t];
+    const unsigned jc = f / (unsigned)lda, ir = f - jc * (unsigned)lda;
+    const size_t p = (size_t)jc * (jc + 1) / 2 + ir;
+    slot[(size_t)c * U + p] = t;
+}
+
+__global__ void k_op_aggregate_h(double* H, int d, int lda, int U, const double* vals, const int* slot, int kstride,
+                                 int nc)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= U) return;
+    int i, j;
+    upper_ij(p, i, j);
+    const size_t f = (size_t)j * lda + i;
+    double h = H[f];
+    for (int c = 0; c < nc; ++c) {
+        const int t = slot[(size_t)c * U + p];
+        if (t >= 0) h = __dadd_rn(h, vals[(size_t)c * kstride + t]);
+    }
+    H[f] = h;
+}
+
+// Identity compressor (LocalWorkerForFedNL_Identical.h:80-94): the message is every upper entry
+// times alpha / n in the upper-index order (column j, rows 0..j); the shift receives alpha diff on
+// both triangles.  One thread per (matrix, upper position).
+__global__ void k_op_identity(const double* diffs, double* shifts, int n_mat, int lda, size_t full, int U,
+                              double alpha, double prescale, unsigned* idx_out, double* val_out)
+{
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_mat || p >= U) return;
+    int i, j;
+    upper_ij(p, i, j);
+    const size_t f = (size_t)j * lda + i;
+    const double item = diffs[(size_t)m * full + f];
+    if (idx_out) idx_out[(size_t)m * U + p] = (unsigned)f;
+    if (val_out) val_out[(size_t)m * U + p] = __dmul_rn(item, prescale);
+    if (shifts) {
+        const double upd = __dmul_rn(alpha, item);
+        double* sh = shifts + (size_t)m * full;
+        sh[f] = __dadd_rn(sh[f], upd);
+        if (i != j) {
+            const size_t g = (size_t)i * lda + j;
+            sh[g] = __dadd_rn(sh[g], upd);
+        }
+    }
+}
 // pack the upper triangle of n column-major d x lda matrices and their full squared norms
 __global__ void k_pack_upper(const double* full, int d, int lda, int U, int ustr, double* packed)
 {

@@ -337,7 +337,27 @@ extern "C" int fednl_gpu_load_libsvm(const char* path, int32_t add_intercept, in
     return 0;
 }
 
-extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callback cb)
+// Squared L2 norm in the reference's two-Vec4d order (VectorNDRaw<double>::vectorL2NormSquare,
+// VectorND_Raw_SIMD_double.h:749-800): element i < 8 floor(n/8) into lane i mod 8, lanes reduced as
+// (0 + ((c0 + c2) + (c1 + c3))) + ((c4 + c6) + (c5 + c7)), the tail summed in order and added last.
+static double ref_norm2(const std::vector<double>& v)
+{
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const size_t n = v.size(), items = n & ~(size_t)7;
+    size_t i = 0;
+    for (; i < items; i += 8)
+        for (int l = 0; l < 8; ++l) c[l] = c[l] + v[i + l] * v[i + l];
+    double fin = 0.0;
+    fin = fin + ((c[0] + c[2]) + (c[1] + c[3]));
+    fin = fin + ((c[4] + c[6]) + (c[5] + c[7]));
+    double rest = 0.0;
+    for (; i < n; ++i) rest = rest + v[i] * v[i];
+    return fin + rest;
+}
+
+// bin_fednl_local's and bin_fednl_local_pp's train() on the engine.  pp: the partial-participation
+// binary (--clients-per-round, Option B/A, no line search; its callback receives the dimension only).
+static int execute_local_impl(const char* command, bool pp, fednl_result_callback cb, void (*cb_pp)(int))
 {
     if (!command) return -1;
     CmdLine cl;
@@ -403,9 +423,22 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
     const bool opt1 = cl.flag("use_theoretical_alpha_option_1"), opt2 = cl.flag("use_theoretical_alpha_option_2");
     double alpha = 0.0;
     if (!theo && !num("alpha_step_size", alpha)) return -1;
-    const bool ls = cl.flag("line_search");
+    const bool ls = !pp && cl.flag("line_search");          // the PP binary has no line search (its Args.h)
     double ls_c = 0.5, ls_gamma = 0.5;
     uint32_t ls_max = 5;
+    int32_t per_round = 0;
+    if (pp && (!i32("clients-per-round", per_round) || per_round < 1)) return -1;
+    // arithmetic order of the engine: the reference's own (default; bit-identical rounds) or the
+    // engine's fixed order (faster); FedNL-PP runs in the fixed order
+    int32_t arith = pp ? FEDNL_ORDER_FIXED : FEDNL_ORDER_REFERENCE;
+    {
+        std::string o;
+        if (cl.str("gpu-arith-order", o)) {
+            if (o == "fixed") arith = FEDNL_ORDER_FIXED;
+            else if (o == "reference" && !pp) arith = FEDNL_ORDER_REFERENCE;
+            else return -1;
+        }
+    }
     if (ls) {
         if (!num("c_line_search", ls_c) || !num("gamma_line_search", ls_gamma)) return -1;
         u32("max_line_search_steps", ls_max);
@@ -418,6 +451,7 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
     int rc = load_libsvm(path, add_intercept, ds, err);
     if (rc) return rc;
     if (n_clients < 1 || ds.n < n_clients) return -5;
+    if (pp && per_round > n_clients) return -1;
     const int d = ds.d;
     const long long U = (long long)d * (d + 1) / 2;
 
@@ -476,7 +510,10 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
     desc.ls_c = ls_c;
     desc.ls_gamma = ls_gamma;
     desc.ls_max_steps = (int32_t)ls_max;
-    desc.track_f = tracking ? 1 : 0;
+    desc.track_f = (tracking && !pp) ? 1 : 0;
+    desc.clients_per_round = pp ? per_round : 0;
+    desc.client_seed = 1234;    // bin_fednl_local_pp Args.h:244 (not taken from the command line)
+    desc.arith_order = arith;
     fednl_handle h = nullptr;
     if (fednl_gpu_create(&desc, &h) != 0) return -7;
     // x0 from RandomGenRealLinear(0, 0): every coordinate is 0 whatever the seed (Args.h:235)
@@ -489,7 +526,7 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
     Tracker tr;
     if (tracking) {
         tr.cstr(base_name(path), true);
-        std::string alg = "FedNL";
+        std::string alg = pp ? "FedNL-PP" : "FedNL";
         if (ls) alg += "-LS";
         if (opt_a) alg += " (a)";
         if (opt_b) alg += " (b)";
@@ -511,10 +548,13 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
     double sent_scalars = 0.0, sent_indices = 0.0;
     const auto t0 = std::chrono::steady_clock::now();
     int status = 0;
+    std::vector<int32_t> sel(n_clients);
     for (int r = 0; r < rounds; ++r) {
         fednl_gpu_get_x(h, x.data());
         double xn = 0.0;
-        for (double v : x) xn += v * v;
+        if (arith == FEDNL_ORDER_REFERENCE) xn = ref_norm2(x);
+        else
+            for (double v : x) xn += v * v;
         fednl_round_stats st{};
         const int rr = fednl_gpu_round(h, &st);
         if (rr != 0 && rr != FEDNL_ENOTPD) {
@@ -522,7 +562,10 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
             break;
         }
         double last_scalars = 0.0, last_idx = 0.0;
-        for (int c = 0; c < n_clients; ++c) {
+        int32_t nsel = n_clients;
+        if (pp) fednl_gpu_get_selected(h, sel.data(), &nsel);
+        for (int t = 0; t < nsel; ++t) {
+            const int c = pp ? sel[t] : t;
             int32_t cnt = 0;
             fednl_gpu_get_message(h, c, nullptr, nullptr, &cnt);
             if (comp == FEDNL_NATURAL) last_scalars += 3.0 * ((cnt + 2) / 2);
@@ -534,7 +577,7 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
             const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             tr.i32(r);
             tr.f64(st.grad_norm);
-            tr.f64(fednl_gpu_get_f(h));
+            tr.f64(pp ? NAN : fednl_gpu_get_f(h));       // FedNL-PP: f is not formed by the engine
             tr.f64(std::sqrt(xn));
             tr.f64(sent_scalars);
             tr.f64(sent_indices);
@@ -563,9 +606,32 @@ extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callbac
         if (!tr.bytes.empty()) fwrite(tr.bytes.data(), 1, tr.bytes.size(), f);
         fclose(f);
     }
+    if (pp) {
+        if (cb_pp) cb_pp(d);                                 // bin_fednl_local_pp TrainLoop.h:1870-1871
+        return 0;
+    }
     double g2 = 0.0;
-    for (double v : g) g2 += v * v;
+    if (arith == FEDNL_ORDER_REFERENCE) g2 = ref_norm2(g);
+    else
+        for (double v : g) g2 += v * v;
     const double mu = lambda;                                // computeMuStrongConvexity
     if (cb) cb(d, std::sqrt(g2), g2 / (mu + mu), (g2 + g2) / mu);
     return 0;
+}
+
+extern "C" int fednl_gpu_execute_local(const char* command, fednl_result_callback cb)
+{
+    return execute_local_impl(command, false, cb, nullptr);
+}
+
+// The reference's exported entry points (bin_fednl_local/exported/FedNLLocalShared.h:8-17 and
+// bin_fednl_local_pp/exported/FedNLPPLocalShared.h:8-16), same names, signatures and return codes.
+extern "C" int doptExecuteLocal(const char* command, ResultCallbackLocal resultCallback)
+{
+    return execute_local_impl(command, false, resultCallback, nullptr);
+}
+
+extern "C" int doptExecuteLocalPP(const char* command, ResultCallbackLocalPP resultCallback)
+{
+    return execute_local_impl(command, true, nullptr, resultCallback);
 }

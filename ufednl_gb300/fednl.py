@@ -74,7 +74,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32", "fednl_gpu_selftest_rn",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
-           "fednl_gpu_autotune", "fednl_mx_autotune"]
+           "fednl_gpu_autotune", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
+           "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity"]
 
 _lib = None
 
@@ -112,6 +113,10 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_randk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
         "fednl_gpu_randseqk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
         "fednl_gpu_natural": [dp, C.c_int64, dp, C.POINTER(C.c_uint8)],
+        "fednl_gpu_shift_update": [dp, dp, C.c_int32, C.c_int32, C.c_int32, up, ip, C.c_int32, C.c_double,
+                                   C.c_double],
+        "fednl_gpu_aggregate": [C.c_int32, C.c_int32, C.c_int32, dp, dp, up, dp, ip, C.c_int32, dp, dp, dp],
+        "fednl_gpu_compress_identity": [dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double, dp, up, dp],
         "fednl_gpu_logreg_oracle": [dp, dp, C.c_int32, C.c_int32, C.c_int32, C.c_double, dp, dp, dp],
         "fednl_gpu_optionb_solve": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
         "fednl_gpu_optionb_solve_mixed": [dp, C.c_int32, C.c_int32, C.c_double, dp, dp],
@@ -162,6 +167,10 @@ def load(build_if_missing: bool = True):
     L.fednl_gpu_load_libsvm.restype = C.c_int
     L.fednl_gpu_execute_local.argtypes = [C.c_char_p, RESULT_CALLBACK]
     L.fednl_gpu_execute_local.restype = C.c_int
+    L.doptExecuteLocal.argtypes = [C.c_char_p, RESULT_CALLBACK]
+    L.doptExecuteLocal.restype = C.c_int
+    L.doptExecuteLocalPP.argtypes = [C.c_char_p, C.CFUNCTYPE(None, C.c_int)]
+    L.doptExecuteLocalPP.restype = C.c_int
     L.fednl_gpu_last_error.argtypes = []
     L.fednl_gpu_last_error.restype = C.c_char_p
     _lib = L
@@ -475,6 +484,80 @@ def execute_local(command: str):
         got.append((int(d), float(gnorm), float(fgap), float(xgap)))
 
     rc = load().fednl_gpu_execute_local(command.encode(), cb)
+    return rc, (got[0] if got else None)
+
+
+def shift_update(shifts, diffs, d: int, lda: int, idx, counts, alpha: float, value_mult: float = 1.0):
+    """fednl_gpu_shift_update: shifts [n, d*lda] updated in place; idx [n, k_stride]; counts [n]."""
+    sh = np.ascontiguousarray(shifts, dtype=np.float64)
+    df = np.ascontiguousarray(diffs, dtype=np.float64)
+    ix = np.ascontiguousarray(idx, dtype=np.uint32)
+    ct = np.ascontiguousarray(counts, dtype=np.int32)
+    n = ct.size
+    _check(load().fednl_gpu_shift_update(_dp(sh), _dp(df), n, d, lda, _up(ix), _ip(ct), ix.shape[1], float(alpha),
+                                         float(value_mult)))
+    return sh
+
+
+def aggregate(grads, lks, d: int, lda: int, H, idx=None, vals=None, counts=None):
+    """fednl_gpu_aggregate: returns (H updated, g, l)."""
+    gr = np.ascontiguousarray(grads, dtype=np.float64)
+    lk = np.ascontiguousarray(lks, dtype=np.float64)
+    Hh = np.ascontiguousarray(H, dtype=np.float64).copy()
+    n = lk.size
+    g = np.empty(d)
+    l = np.zeros(1)
+    if idx is None:
+        _check(load().fednl_gpu_aggregate(n, d, lda, _dp(gr), _dp(lk), None, None, None, 0, _dp(Hh), _dp(g), _dp(l)))
+    else:
+        ix = np.ascontiguousarray(idx, dtype=np.uint32)
+        vv = np.ascontiguousarray(vals, dtype=np.float64)
+        ct = np.ascontiguousarray(counts, dtype=np.int32)
+        _check(load().fednl_gpu_aggregate(n, d, lda, _dp(gr), _dp(lk), _up(ix), _dp(vv), _ip(ct), ix.shape[1],
+                                          _dp(Hh), _dp(g), _dp(l)))
+    return Hh, g, float(l[0])
+
+
+def compress_identity(diffs, d: int, lda: int, alpha: float, prescale: float, shifts=None):
+    """fednl_gpu_compress_identity: returns (idx [n, U], vals [n, U], shifts updated or None)."""
+    df = np.ascontiguousarray(diffs, dtype=np.float64).reshape(-1, d * lda)
+    n = df.shape[0]
+    U = d * (d + 1) // 2
+    ix = np.empty((n, U), dtype=np.uint32)
+    vv = np.empty((n, U))
+    sh = None if shifts is None else np.ascontiguousarray(shifts, dtype=np.float64).reshape(n, d * lda).copy()
+    _check(load().fednl_gpu_compress_identity(_dp(df), n, d, lda, float(alpha), float(prescale),
+                                              _dp(sh) if sh is not None else None, _up(ix), _dp(vv)))
+    return ix, vv, sh
+
+
+# the reference's exported callback types (FedNLLocalShared.h:8-11, FedNLPPLocalShared.h:8)
+RESULT_CALLBACK_PP = C.CFUNCTYPE(None, C.c_int)
+
+
+def dopt_execute_local(command: str):
+    """The reference's own symbol doptExecuteLocal, exported by this library: returns (return code,
+    callback values or None)."""
+    got = []
+
+    @RESULT_CALLBACK
+    def cb(d, gnorm, fgap, xgap):
+        got.append((int(d), float(gnorm), float(fgap), float(xgap)))
+
+    rc = load().doptExecuteLocal(command.encode(), cb)
+    return rc, (got[0] if got else None)
+
+
+def dopt_execute_local_pp(command: str):
+    """The reference's own symbol doptExecuteLocalPP (bin_fednl_local_pp): returns (return code,
+    the dimension passed to the callback or None)."""
+    got = []
+
+    @RESULT_CALLBACK_PP
+    def cb(d):
+        got.append(int(d))
+
+    rc = load().doptExecuteLocalPP(command.encode(), cb)
     return rc, (got[0] if got else None)
 
 
