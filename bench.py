@@ -141,6 +141,30 @@ def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
     return 0.0, "n/a"
 
 
+def hess_fp64_ops(prob) -> float:
+    """FP64 operations of one k_hess_binary launch: for every client and upper entry (i, j) one add
+    per sample with both attributes set (the in-order sum of D_s), then the difference, its square
+    and the add into the entry's norm accumulator (3 more)."""
+    d = prob.d
+    U = d * (d + 1) // 2
+    tot = 0.0
+    for c in range(prob.n_clients):
+        a = prob.features[prob.client_slice(c)]
+        g = a.T @ a
+        tot += float(np.triu(g).sum())
+    return tot + 3.0 * prob.n_clients * U
+
+
+def kernel_roofline(name: str, ms: float, bound: str, work: float, peak: float, unit: str, what: str,
+                    peak_source: str) -> dict:
+    """achieved = algorithmic work per launch / mean launch time (CUDA events); frac = achieved / peak."""
+    scale = 1e9 if unit in ("GB/s", "Gop/s") else 1e12
+    ach = work / (ms * 1e-3) / scale if ms > 0 else 0.0
+    return {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+            "traffic": traffic_from_profiles(name), "work_per_launch": work, "work": what, "kernel_ms": ms,
+            "peak_source": peak_source}
+
+
 def traffic_from_profiles(kernel: str):
     """DRAM bytes per launch recorded from an ncu capture in profiles/<kernel>*.md, if any."""
     pdir = os.path.join(REPO, "profiles")
@@ -181,6 +205,72 @@ def cpu_port_rounds_per_s(prob, comp, k, threads: int, max_rounds: int, budget_s
     dt = time.perf_counter() - t0
     orc.close()
     return n / dt, n, dt
+
+
+def cpu_port_time_to_tol(prob, comp, k, threads: int, cap: int = 60):
+    """The CPU port from x0 = 0 until ||g|| <= TOL (or cap rounds): rounds and wall seconds."""
+    from oracle import pyoracle
+    pyoracle.build()
+    orc = pyoracle.FedNL(prob, comp, k, 1.0, workers=threads, threads=threads)
+    t0 = time.perf_counter()
+    rounds = None
+    for r in range(cap):
+        if orc.round() <= TOL:
+            rounds = r + 1
+            break
+    dt = time.perf_counter() - t0
+    orc.close()
+    return {"tol": TOL, "rounds": rounds, "seconds": dt if rounds else None, "cap": cap,
+            "timed": "wall clock of rounds 1..R from x0 = 0"}
+
+
+def reference_order_rounds(fednl, prob, comp, k, workers: int, n: int):
+    """The workload in the reference's arithmetic order (desc.arith_order = reference: rounds
+    bit-identical to the reference's own): device-timed rounds with a cold L2 before each, and the
+    per-kernel breakdown."""
+    fed = fednl.FedNL(prob, comp, k, 1.0, workers=workers, order="reference")
+    fed.run(3)
+    tot, per = fed.time_rounds(n, L2_FLUSH_BYTES)
+    prof = fed.profile_kernels(min(n, 20), L2_FLUSH_BYTES)
+    fed.close()
+    return {"rounds_per_s": n / (tot / 1000.0), "round_ms_p50": float(np.percentile(per, 50)),
+            "round_ms_p99": float(np.percentile(per, 99)), "rounds_timed": n, "kernels_ms": dict(prof)}
+
+
+def mixed_accuracy(fednl, prob_mx, prob64, comp, k, alpha, cap: int, fp64_to_tol: bool, feature_format: int = 0):
+    """The mixed-precision form run until its ||g|| <= TOL (or cap rounds), then the true FP64 gradient
+    at its final iterate from the FP64 engine (one round from that iterate reports ||grad f(x)||), and,
+    when fp64_to_tol, the FP64 GPU form run to TOL from x0 for the iterate comparison."""
+    mx = fednl.MixedFedNL(prob_mx, k, alpha, compressor=comp)
+    mx.autotune()
+    g_mx, rounds = None, None
+    for r in range(cap):
+        g_mx = float(mx.run(1)[0])
+        if g_mx <= TOL:
+            rounds = r + 1
+            break
+    x_mx = mx.x()
+    mx.close()
+    f64 = fednl.FedNL(prob64, comp, k, alpha, feature_format=feature_format)
+    f64.set_x(x_mx)
+    g_true = float(f64.round())
+    f64.close()
+    out = {"compressor": comp, "k": k, "tol": TOL, "round_cap": cap, "mixed_rounds_to_tol": rounds,
+           "mixed_grad_norm": g_mx, "fp64_grad_norm_at_mixed_iterate": g_true,
+           "grad_norm_error_vs_fp64": abs(g_mx - g_true) / g_true if g_true > 0 else None,
+           "meets_tol_in_fp64": g_true <= TOL}
+    if fp64_to_tol:
+        f64 = fednl.FedNL(prob64, comp, k, alpha, feature_format=feature_format)
+        r64 = None
+        for r in range(cap):
+            if f64.round() <= TOL:
+                r64 = r + 1
+                break
+        x64 = f64.x()
+        f64.close()
+        out["fp64_rounds_to_tol"] = r64
+        out["iterate_rel_diff_vs_fp64"] = float(np.linalg.norm(x_mx - x64) / np.linalg.norm(x64))
+    return out
 
 
 def run_reference(args, ws, rank, td):
@@ -257,17 +347,18 @@ def extra_workloads(fednl, threads: int, steps: int):
 def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
     """The mixed-precision configuration: dense N(0,1) FP32 features, d=1024, 256 clients with
     n_i ~ U{512..4096} (seed 2), lambda 1e-4, RandK-Philox k=4d.  The mixed round (TF32 tensor-core
-    Hessians) is device-timed; the FP64 GPU round (the same algorithm on the FP64 engine) and the
-    CPU port run a bounded sample on the same data; ||grad|| after the same rounds is compared."""
+    Hessians) is device-timed; the mixed form then runs to ||g|| <= 1e-9 (or 400 rounds) and the FP64
+    engine evaluates the true gradient at its final iterate; the FP64 GPU round and the CPU port are
+    timed on a bounded sample of the same data (the FP64 form is not run to tolerance here: about
+    3.6 s a round at this size)."""
     from ufednl_gb300 import datagen
     from oracle import pyoracle
     prob = datagen.workload_dense_fp32_1024()
     d, k = prob.d, 4 * prob.d
     U = d * (d + 1) // 2
     alpha = k / U
-    R = 10
     mx = fednl.MixedFedNL(prob, k, alpha)
-    g_mx = mx.run(R)
+    mx.run(2)
     tuned = mx.autotune()
     tot, per = mx.time_rounds(20, L2_FLUSH_BYTES)
     prof = mx.profile_kernels(5)
@@ -276,8 +367,8 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
     flops = float(prob.total_samples) * d * (d + 1)          # upper triangle incl. diagonal, 2 flops per MAC
     tf = flops / (gram_ms * 1e-3) / 1e12
     p64 = datagen.Problem(d, prob.n_samples, prob.features.astype(np.float64), prob.labels, prob.lam)
+    acc = mixed_accuracy(fednl, prob, p64, "randk_philox", k, alpha, 400, False, feature_format=2)
     f64 = fednl.FedNL(p64, "randk_philox", k, alpha, feature_format=2)
-    g_64 = f64.run(R)
     tot64, _ = f64.time_rounds(2)
     f64.close()
     orc = pyoracle.FedNL(p64, "randk_philox", k, alpha, workers=threads, threads=threads)
@@ -294,8 +385,7 @@ def mixed_workload(fednl, threads: int, tensor_peak_tflops: float, src: str):
             "autotuned": tuned,
             "fp64_gpu_rounds_per_s": 2 / (tot64 / 1000.0), "cpu_port_rounds_per_s": 1.0 / cpu_s,
             "cpu_port_sample": f"1 round, {threads} threads",
-            "grad_norm_after_rounds": {"rounds": R, "mixed": float(g_mx[-1]), "fp64": float(g_64[-1]),
-                                       "rel_diff": float(abs(g_mx[-1] - g_64[-1]) / g_64[-1])}}
+            "accuracy_vs_fp64": acc}
 
 
 def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, fp64_tol_s):
@@ -335,12 +425,23 @@ def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, f
     t_tensor = gram_flops / (bf16 / 2.0 * 1e12) * 1e3
     t_hbm = shift_bytes / (hbm * 1e9) * 1e3
     bound_ms = max(t_tensor, t_hbm)
+    km = dict(prof)
+    S = float(prob.total_samples)
+    hsrc = f"{src} (MEASURED_PEAKS.json hbm_gbs)"
+    mx_roof = [kernel_roofline("k_gram_tf32", km.get("k_gram_tf32", 0.0), "tensor", S * prob.d * (prob.d + 1),
+                               bf16 / 2.0, "TFLOP/s", "client Gram upper triangles incl. diagonal, 2 flops per MAC",
+                               f"{src}: MEASURED_PEAKS.json bf16_tflops / 2 (tf32 rate)"),
+               kernel_roofline("k_mx_select", km.get("k_mx_select", 0.0), "hbm", prob.n_clients * U * 4.0, hbm,
+                               "GB/s", "every client's FP32 difference read once", hsrc),
+               kernel_roofline("k_mx_margin", km.get("k_mx_margin", 0.0), "hbm", S * prob.d * 4.0, hbm, "GB/s",
+                               "the FP32 features read once", hsrc)]
     return {"rounds_per_s": rps, "round_ms_p50": float(np.percentile(per, 50)),
             "round_roofline": {"bound": "tensor" if t_tensor >= t_hbm else "hbm", "gram_tf32_flops": gram_flops,
                                "shift_stream_bytes": shift_bytes, "lower_bound_ms": bound_ms,
                                "round_ms": tot / n, "frac": bound_ms / (tot / n),
                                "peaks": f"{src}: tf32 = bf16_tflops / 2, hbm_gbs"},
             "round_ms_p99": float(np.percentile(per, 99)), "rounds_timed": n, "kernels_ms": dict(prof),
+            "roofline_kernels": mx_roof,
             "gpu_launches_per_round": len(prof),
             "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
                             "seconds": tol_ms / 1000.0 if tol_ms is not None else None},
@@ -348,6 +449,7 @@ def mixed_headline(fednl, prob, comp, k, steps: int, fp64_rounds_per_s: float, f
             "speedup_vs_fp64_gpu_time_to_tol": (fp64_tol_s / (tol_ms / 1000.0))
             if (fp64_tol_s and tol_ms) else None,
             "autotuned": tuned,
+            "accuracy_vs_fp64": [mixed_accuracy(fednl, prob, prob, c_, k, 1.0, 200, True) for c_ in (comp, "topk")],
             "precision": "TF32 tensor-core client Hessians (FP32 accumulate), FP32 shifts and selection, "
                          "float-float margins/gradients, FP64 master; solve as autotuned (FP64 Cholesky; FP32 "
                          "Cholesky on a cooperative grid or cluster with FP64-residual refinement to 2^-30; or "
@@ -414,13 +516,33 @@ def run_ours(args, ws, rank, local, td):
     # per-kernel breakdown with CUDA events on the library's stream
     prof = fed.profile_kernels(min(args.steps, 50), L2_FLUSH_BYTES)
     kernels = {n: ms for n, ms in prof}
-    dom, dom_ms = max(prof, key=lambda t: t[1])
     hbm, bf16, src = peaks()
-    abytes, what = algorithmic_bytes(dom, prob, k)
-    ach = abytes / (dom_ms / 1000.0) / 1e9 if abytes else 0.0
-    roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-            "traffic": traffic_from_profiles(dom), "algorithmic_bytes_per_launch": abytes,
-            "algorithmic_bytes": what, "kernel_ms": dom_ms, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)"}
+    fp64 = fednl.fp64_rate()              # this GPU's FP64 pipe, the FP64 kernels' denominator
+    hsrc = f"{src} (MEASURED_PEAKS.json hbm_gbs)"
+    fsrc = "measured by fednl_gpu_fp64_rate in this run (independent FP64 add chains, all SMs)"
+    # the kernels the round's bound is about, by name (the same set whatever --steps is): the shift
+    # stream (k_hess_binary reads every shift and writes every difference; k_select reads every
+    # difference once) against HBM, k_hess_binary's in-order sums against the FP64 pipe, and the
+    # Cholesky's latency chain in cycles per column
+    hb, hwhat = algorithmic_bytes("k_hess_binary", prob, k)
+    hops = hess_fp64_ops(prob)
+    sb, swhat = algorithmic_bytes("k_select", prob, k)
+    r_hess_hbm = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "hbm", hb, hbm, "GB/s", hwhat, hsrc)
+    r_hess_fp64 = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "fp64", hops, fp64["add_gops"],
+                                  "Gop/s", "in-order D_s sums (one add per sample with both attributes set) "
+                                  "+ difference, square and norm add per upper entry", fsrc)
+    r_select = kernel_roofline("k_select", kernels.get("k_select", 0.0), "hbm", sb, hbm, "GB/s", swhat, hsrc)
+    chol_ms = kernels.get("k_chol_coop", 0.0)
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    r_chol = {"kernel": "k_chol_coop", "bound": "latency (per-column FP64 dependency chain and grid barriers)",
+              "kernel_ms": chol_ms, "cycles_per_column": chol_ms * 1e-3 * sm_mhz * 1e6 / prob.d,
+              "sm_mhz": sm_mhz, "fp64_add_latency_cycles": fp64["add_latency_cycles"]}
+    roof = dict(r_hess_hbm)
+    roof["fp64"] = {k_: r_hess_fp64[k_] for k_ in ("achieved", "peak", "unit", "frac", "work_per_launch")}
+    roof["note"] = ("k_hess_binary streams the shift matrices (shift read, difference written); its in-order "
+                    "FP64 sums bind it to the FP64 pipe first (fp64.frac), HBM second (frac)")
+    roof_list = [r_hess_hbm, r_hess_fp64, r_select, r_chol]
+    slowest, slowest_ms = max(prof, key=lambda t: t[1])
     # round-level bound: the shift stream (every client's shift read and written once, packed
     # upper FP64) at the measured HBM bandwidth, against the measured time per round
     U = prob.d * (prob.d + 1) // 2
@@ -467,7 +589,12 @@ def run_ours(args, ws, rank, local, td):
             "time_to_tol": {"tol": TOL, "rounds": rounds_to_tol,
                             "seconds": tol_ms / 1000.0 if tol_ms is not None else None,
                             "timed": "device time of rounds 1..R from x0 = 0"},
-            "roofline": roof, "round_roofline": round_roof, "kernels_ms": kernels, "gpu_launches": args.steps * len(prof),
+            "roofline": roof, "roofline_kernels": roof_list,
+            "slowest_kernel": {"kernel": slowest, "ms": slowest_ms,
+                               "bound": next((r["bound"] for r in roof_list if r["kernel"] == slowest), "latency")},
+            "fp64_pipe": fp64, "round_roofline": round_roof, "kernels_ms": kernels,
+            "gpu_launches": args.steps * len(prof),
+            "reference_order": reference_order_rounds(fednl, prob, comp, k, W, min(args.steps, 60)),
             "autotuned": tuned,
             "clocks": clocks, "e2e": e2e}
     if ws == 1 and rank == 0:
@@ -483,9 +610,46 @@ def run_ours(args, ws, rank, local, td):
         threads = os.cpu_count() or 1
         v, n, dt = cpu_port_rounds_per_s(prob, comp, k, threads, 20, 20.0)
         line["cpu_baseline"] = {"value": v, "unit": "rounds/s", "cores": threads, "kind": "port",
-                                "sample": f"{n} full rounds of the workload after one warm-up round ({dt:.1f} s)"}
+                                "sample": f"{n} full rounds of the workload after one warm-up round ({dt:.1f} s)",
+                                "time_to_tol": cpu_port_time_to_tol(prob, comp, k, threads),
+                                "caveat": "the oracle's C port of the reference round (scalar, fixed operation "
+                                          "order, -O3 without -march) stands in for bin_fednl_local, whose "
+                                          "sources and x86 SIMD build are not available on this host"}
     if rank == 0:
         print(json.dumps(line))
+    return 0
+
+
+CASES = ("fp64-w8a", "fp64ref-w8a", "mixed-w8a", "mixed-dense1024")
+
+
+def run_case(case: str, rounds: int) -> int:
+    """A short fixed run of the round for profiling captures (no timing, no JSON line):
+    fp64-w8a        the FP64 engine on the w8a-like workload (d=301, 142 clients, TopLEK k=8d)
+    fp64ref-w8a     the same in the reference's arithmetic order
+    mixed-w8a       the mixed-precision engine on the same workload (solve autotuned)
+    mixed-dense1024 the mixed-precision engine, dense N(0,1) features, d=1024, 64 clients x 1024
+                    samples (268 MB of features, larger than L2), RandK-Philox k=4d"""
+    from ufednl_gb300 import build, datagen, fednl
+    build.build()
+    fednl.load()
+    if case in ("fp64-w8a", "fp64ref-w8a"):
+        prob = datagen.workload_w8a_like()
+        run = fednl.FedNL(prob, "toplek", 8 * prob.d, 1.0, workers=16,
+                          order="reference" if case == "fp64ref-w8a" else "fixed")
+    elif case == "mixed-w8a":
+        prob = datagen.workload_w8a_like()
+        run = fednl.MixedFedNL(prob, 8 * prob.d, 1.0, compressor="toplek")
+    else:
+        d = 1024
+        prob = datagen.dense_problem_fp32(7, d, [1024] * 64, 1e-4)
+        k = 4 * d
+        run = fednl.MixedFedNL(prob, k, k / (d * (d + 1) // 2))
+    if case.startswith("mixed"):
+        run.autotune()            # the solve and launch shape a benchmark run would use
+    g = run.run(rounds)
+    run.close()
+    print(case, "||g|| per round:", np.array2string(g, precision=6))
     return 0
 
 
@@ -500,7 +664,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-extra", action="store_true", help="skip the a9a-like and FedNL-PP side measurements")
+    ap.add_argument("--case", choices=CASES, default=None,
+                    help="run a short fixed case for a profiling capture instead of the benchmark")
+    ap.add_argument("--case-rounds", type=int, default=3)
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case, args.case_rounds)
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     if ws > 1:

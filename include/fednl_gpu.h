@@ -218,35 +218,53 @@ int fednl_gpu_logreg_oracle(const double* features, const double* labels, int32_
  * definite. */
 int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
 
-/* Allocation-free Option-B solve (no counterpart in the reference): the same factorisation and
- * solves as fednl_gpu_optionb_solve for callers that cannot allocate device memory -- code running
- * inside a stream capture whose memory pool forbids new allocations, latency-critical loops where a
- * cudaMalloc would stall the device, or hosts whose framework owns all device memory through its
- * own allocator.  H (column-major d x lda, upper triangle read), g and dx are DEVICE pointers the
- * caller owns; the call runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it
- * to read the status.  Scratch comes from one fixed device array of the library (about 1 MB, held
- * by every device that loads the library until the process exits), so d is limited to 512 (larger
- * d returns FEDNL_EINVAL).  The first call on a device looks up that array's address, so make it
- * before any stream capture.  All calls share the array: calls that overlap on the GPU (different
- * streams or threads at the same time) race and must be serialised by the caller. */
 /* The mixed-precision form's solve of (H + l I) dx = g: FP32 Cholesky factor in one CTA's shared
  * memory (d up to about 300), one step of iterative refinement on a float-float residual of H held
  * as an FP32 pair, dx in FP64.  Host buffers, H column-major upper (lda >= d). */
 int fednl_gpu_optionb_solve_mixed(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx);
+
 /* The same system by the FP32 Cholesky on a cooperative grid (fednl_mx_set_solver 2): at most
  * `refine` FP64-residual refinement steps (0..8; they stop once a correction is at most 2^-30 of the
  * solution), `grid` CTAs of a cooperative launch, or -n for one thread-block cluster of n <= 16 CTAs
  * synchronised by the cluster barrier (0: a cluster of 16 up to d = 512, else one CTA per tile of the
- * first trailing update),
- * d up to 1312.  A pivot that loses more than 18 bits in FP32 hands the system to the FP64 solve,
- * which returns FEDNL_ENOTPD for a matrix that is not positive definite.  Host buffers. */
+ * first trailing update), d up to 1312.  A pivot that loses more than 18 bits in FP32 hands the
+ * system to the FP64 solve, which returns FEDNL_ENOTPD for a matrix that is not positive definite.
+ * Host buffers. */
+int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
+                              int32_t refine, int32_t grid);
+
 /* Self-test of the FP64 Cholesky's square root and reciprocal (integer arithmetic, correctly
  * rounded): n inputs from a seeded generator (random bit patterns of every exponent and sign,
  * significands near 0 and 1, squares and their neighbours); counts of results that differ bit for bit
  * from the hardware sqrt and 1.0 / x. */
 int fednl_gpu_selftest_rn(int64_t n, uint64_t seed, int64_t* sqrt_mismatches, int64_t* rcp_mismatches);
-int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l, const double* g, double* dx,
-                              int32_t refine, int32_t grid);
+
+/* Measurement of this GPU's FP64 pipe (no counterpart in the reference; the denominator of the FP64
+ * kernels' roofline): lane operations per second of dependent FP64 fma and add chains with all SMs
+ * full of warps (8 chains a thread), in G op/s, and the clock cycles of one dependent FP64 add in a
+ * single warp.  `iters` operations per chain. */
+int fednl_gpu_fp64_rate(int64_t iters, double* fma_gops, double* add_gops, double* add_latency_cycles);
+
+/* Allocation-free Option-B solve.  It has no counterpart in the reference; it is for callers that
+ * cannot allocate device memory: a host framework that owns all device memory through its own
+ * allocator (a cudaMalloc beside it would fail or fragment its pool), a process running under a
+ * fixed device-memory budget, or a latency-critical loop in which cudaMalloc / cudaFree would
+ * synchronise the device.  It computes what fednl_gpu_optionb_solve computes (the same kernel and
+ * operation order, so the same bits) and allocates nothing:
+ *   - H (column-major d x lda, upper triangle read), g and dx are DEVICE pointers the caller owns;
+ *   - the call runs on `stream` (a cudaStream_t, NULL = the default stream) and waits for that
+ *     stream to finish the solve before it returns the status (FEDNL_OK, FEDNL_ENOTPD,
+ *     FEDNL_ETIMEOUT);
+ *   - its scratch is one fixed device array of the library, about 1 MB, which every device that
+ *     loads the library holds until the process exits; so d is at most 512, and a larger d returns
+ *     FEDNL_EINVAL with a message naming the limit;
+ *   - the first call on a device does a one-time set-up with that device current: it looks up the
+ *     array's device address, which can load the library's device code on that device (and so
+ *     reserve the array at that moment); make that first call before any stream capture, and before
+ *     measuring free device memory;
+ *   - every call uses the same array and finds the previous call's contents there; the call clears
+ *     what must start at zero.  Calls that overlap on the GPU (other streams or host threads at the
+ *     same time) race on the array: serialise them. */
 int fednl_gpu_optionb_solve_noalloc(const double* H, int32_t d, int32_t lda, double l, const double* g,
                                     double* dx, void* stream);
 

@@ -575,7 +575,8 @@ void orc_margin(const double* atr, int32_t d, int32_t lda, int32_t n, const doub
  * into a 32-bit head and a tail, r kept as a double-double (r_hi, r_lo); exp(r) = 1 + r + r^2/2 +
  * r^3/6 + r^4 P(r), the first four terms summed with exact two-sum / two-product error terms and
  * the Taylor tail P (1/24 ... 1/13!) in double; one final rounding; then scaling by 2^k.  The error
- * before the final rounding is about 1e-3 ulp, so results are correctly rounded except in rare
+ * before the final rounding is about 1e-3 ulp (the two-part ln2 is the split published with fdlibm's
+ * e_exp.c / e_log.c), so results are correctly rounded except in rare
  * near-halfway cases.  The reference's sigmoid uses the vectorclass exp in SIMD lanes and libm exp
  * for the tail (VectorND_Raw_SIMD_double.h:1596-1650), both within an ulp of this. */
 static double pow2i(int k)
@@ -1534,7 +1535,7 @@ static int orc_round_pp_master(orc_state* S, double* grad_norm);
 static double objective_at(orc_state* S, const double* x)
 {
     const orc_problem* P = &S->p;
-    int32_t d = P->d, lda = P->lda, nc = P->n_clients;
+    int32_t d = P->d, nc = P->n_clients;
     int32_t nmax = 1;
     for (int32_t c = 0; c < nc; ++c)
         if (S->clients[c].n > nmax)

@@ -176,8 +176,13 @@ int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_chol_batched, kCoopThreads, 0);
     const int cap = std::max(1, sms * std::max(1, bps));
-    static CholJob* djobs = nullptr;
-    static int djobs_cap = 0;
+    // the device job table is kept per device and reused launch after launch; one host thread at a
+    // time fills and launches it
+    static std::mutex tables_mu;
+    static std::map<int, std::pair<CholJob*, int>> tables;
+    std::lock_guard<std::mutex> lock(tables_mu);
+    CholJob*& djobs = tables[dev].first;
+    int& djobs_cap = tables[dev].second;
     for (int first = 0; first < n; first += cap) {
         const int m = std::min(cap, n - first);
         std::vector<CholJob> jobs(m);
@@ -225,6 +230,8 @@ int fednl_solve_batch_launch(const FednlSolveDesc* descs, int n, void* stream)
             djobs_cap = cap;
         }
         CK(cudaMemcpyAsync(djobs, jobs.data(), sizeof(CholJob) * m, cudaMemcpyHostToDevice, st));
+        for (int j = 0; j < m; ++j)     // barrier words start at zero (a timed-out launch leaves its flag set)
+            CK(cudaMemsetAsync(jobs[j].P.bar, 0, 4 * sizeof(unsigned), st));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cta);
         cfg.blockDim = dim3(kCoopThreads);
@@ -625,6 +632,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_pp_aggregate<<<(h->d + 127) / 128, 128, 0, st>>>(P);
         CKL();
         MARK("k_chol_coop");     // x = (H + l I)^-1 g (bin_fednl_local_pp TrainLoop.h:1560-1600)
+        CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(unsigned), st));   // barrier words and error flag start at zero
         CK(launch_chol(P, h->chol_grid, st, P.H, 0, P.stats + 1, 0.0, P.g, P.x, nullptr, 0));
         MARK("end");
         return FEDNL_OK;
@@ -645,6 +653,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     if (client_phase_only) return FEDNL_OK;
     const fednl_problem_desc& D = h->desc;
     const double* lptr = D.option_a ? nullptr : P.stats + 1;      // Option A: H + lambda I
+    CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(unsigned), st));      // barrier words and error flag start at zero
     if (P.ref) {
         MARK("k_chol_ref");
         CK(launch_chol_ref(P, h->ref_grid, st, lptr, P.lambda, P.dx, D.line_search ? nullptr : P.x, 1));
@@ -2164,6 +2173,87 @@ int fednl_gpu_selftest_rn(int64_t n, uint64_t seed, int64_t* sqrt_mismatches, in
     return FEDNL_OK;
 }
 
+// ---- FP64 pipe rate and latency ------------------------------------------------------------------
+// Throughput: every thread runs 8 independent chains of `iters` dependent FP64 operations (fma, or
+// add), all SMs full of warps; lane operations per second.  Latency: one warp, one dependent chain
+// of adds, clock64 cycles per add.  The values never leave registers except one store per thread,
+// so the kernels measure the FP64 pipe alone.
+__global__ void __launch_bounds__(256) k_fp64_rate(long long iters, int use_fma, double b, double* sink)
+{
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+    double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+    if (use_fma) {
+        for (long long t = 0; t < iters; ++t) {
+            a0 = __fma_rn(a0, b, 1e-12); a1 = __fma_rn(a1, b, 1e-12); a2 = __fma_rn(a2, b, 1e-12);
+            a3 = __fma_rn(a3, b, 1e-12); a4 = __fma_rn(a4, b, 1e-12); a5 = __fma_rn(a5, b, 1e-12);
+            a6 = __fma_rn(a6, b, 1e-12); a7 = __fma_rn(a7, b, 1e-12);
+        }
+    } else {
+        for (long long t = 0; t < iters; ++t) {
+            a0 = __dadd_rn(a0, b); a1 = __dadd_rn(a1, b); a2 = __dadd_rn(a2, b); a3 = __dadd_rn(a3, b);
+            a4 = __dadd_rn(a4, b); a5 = __dadd_rn(a5, b); a6 = __dadd_rn(a6, b); a7 = __dadd_rn(a7, b);
+        }
+    }
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+
+__global__ void k_fp64_latency(long long iters, double b, double* sink, long long* cycles)
+{
+    double a = threadIdx.x * 1e-9;
+    __syncwarp();
+    const long long t0 = clock64();
+    for (long long t = 0; t < iters; ++t) a = __dadd_rn(a, b);
+    const long long t1 = clock64();
+    sink[threadIdx.x] = a;
+    if (threadIdx.x == 0) *cycles = t1 - t0;
+}
+
+int fednl_gpu_fp64_rate(int64_t iters, double* fma_gops, double* add_gops, double* add_latency_cycles)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (iters < 1 || !fma_gops || !add_gops || !add_latency_cycles) return fail(FEDNL_EINVAL, "bad argument");
+    int dev = 0, sms = 1;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256;
+    Scratch s;
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    double* sink;
+    long long* cyc;
+    s.a.want(&sink, (size_t)blocks * threads);
+    s.a.want(&cyc, 1);
+    rc = s.a.commit();
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double out[2];
+    for (int f = 0; f < 2; ++f) {
+        k_fp64_rate<<<blocks, threads, 0, s.st>>>(iters / 16 + 1, 1 - f, 1.0000001, sink);   // warm-up
+        CKL();
+        CK(cudaEventRecord(e0, s.st));
+        k_fp64_rate<<<blocks, threads, 0, s.st>>>(iters, 1 - f, 1.0000001, sink);
+        CKL();
+        CK(cudaEventRecord(e1, s.st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        out[f] = (double)blocks * threads * 8.0 * (double)iters / (ms * 1e-3) / 1e9;
+    }
+    k_fp64_latency<<<1, 32, 0, s.st>>>(iters, 1e-7, sink, cyc);
+    CKL();
+    long long cycles = 0;
+    CK(cudaMemcpyAsync(&cycles, cyc, 8, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *fma_gops = out[0];
+    *add_gops = out[1];
+    *add_latency_cycles = (double)cycles / (double)iters;
+    return FEDNL_OK;
+}
+
 // ---- instrumentation ---------------------------------------------------------------------------
 
 static int flush_l2(fednl_handle h, int64_t bytes)
@@ -2266,14 +2356,17 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
 }
 
 // ---- allocation-free Option-B solve -------------------------------------------------------------
-// For callers that may not allocate device memory: code running while a CUDA graph is being
-// captured into a pool that forbids new allocations, real-time loops where a cudaMalloc would stall
-// the device, or hosts whose framework owns every byte of device memory through its own allocator.
-// The solve's scratch (the packed factor, two d-vectors, the grid-barrier counters and the status
-// word) lives in one fixed device array, allocated when the library's module is loaded on a device
-// and held by that device until the process exits.  Only host code needs the array's device
-// address: cudaGetSymbolAddress resolves it once per device, with that device current, on the
-// first call made on it.
+// For callers that may not allocate device memory: a host framework that owns every byte of device
+// memory through its own allocator (a cudaMalloc beside it fails or fragments its pool), a process
+// under a fixed device-memory budget, or a latency-critical loop in which cudaMalloc and cudaFree
+// would synchronise the device.  The solve's scratch (the packed factor, two d-vectors, the
+// grid-barrier counters and the status word) lives in one fixed device array of this file, which
+// every device that loads the library holds until the process exits.  In host code the array's
+// name is not a device address: the first call on a device, with that device current, looks the
+// address up with cudaGetSymbolAddress (which can load the library's device code on that device)
+// and keeps it; every call passes that address to the kernels.  Every call shares the array and
+// finds the previous call's contents there: the barrier counters and the status word are cleared
+// before each launch, the factor is overwritten.  Calls that overlap on the GPU race.
 namespace {
 constexpr int kNoAllocMaxD = 512;
 constexpr size_t kNoAllocMaxUA = (size_t)(kNoAllocMaxD + 1) * (kNoAllocMaxD + 2) / 2;   // factor with y column

@@ -155,7 +155,8 @@ __device__ __forceinline__ double natural_trunc(double v)
 }
 
 // exp(x), own implementation with the same IEEE operation sequence as the CPU oracle: Cody-Waite
-// reduction x = k ln2 + r (ln2 = 32-bit head + tail), r as a double-double, exp(r) = 1 + r + r^2/2
+// reduction x = k ln2 + r (ln2 = 32-bit head + tail: the two-part ln2 published with fdlibm's
+// e_exp.c / e_log.c, 6.93147180369123816490e-01 + 1.90821492927058770002e-10), r as a double-double, exp(r) = 1 + r + r^2/2
 // + r^3/6 + r^4 P(r) with the leading terms summed through exact two-sum / two-product errors and
 // the Taylor tail in double, one final rounding, scaling by 2^k.  Error before the last rounding
 // about 1e-3 ulp.

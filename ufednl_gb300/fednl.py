@@ -75,7 +75,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32", "fednl_gpu_selftest_rn",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
            "fednl_gpu_autotune", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
-           "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity"]
+           "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate"]
 
 _lib = None
 
@@ -113,6 +113,7 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_randk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
         "fednl_gpu_randseqk": [up, C.c_int32, C.c_int32, C.c_int32, C.c_int32, up],
         "fednl_gpu_natural": [dp, C.c_int64, dp, C.POINTER(C.c_uint8)],
+        "fednl_gpu_fp64_rate": [C.c_int64, dp, dp, dp],
         "fednl_gpu_shift_update": [dp, dp, C.c_int32, C.c_int32, C.c_int32, up, ip, C.c_int32, C.c_double,
                                    C.c_double],
         "fednl_gpu_aggregate": [C.c_int32, C.c_int32, C.c_int32, dp, dp, up, dp, ip, C.c_int32, dp, dp, dp],
@@ -529,6 +530,14 @@ def compress_identity(diffs, d: int, lda: int, alpha: float, prescale: float, sh
     _check(load().fednl_gpu_compress_identity(_dp(df), n, d, lda, float(alpha), float(prescale),
                                               _dp(sh) if sh is not None else None, _up(ix), _dp(vv)))
     return ix, vv, sh
+
+
+def fp64_rate(iters: int = 1 << 16) -> dict:
+    """This GPU's FP64 pipe: fma and add lane operations per second (G op/s, all SMs busy) and the
+    cycles of one dependent add in a single warp."""
+    a, b, c = np.zeros(1), np.zeros(1), np.zeros(1)
+    _check(load().fednl_gpu_fp64_rate(int(iters), _dp(a), _dp(b), _dp(c)))
+    return {"fma_gops": float(a[0]), "add_gops": float(b[0]), "add_latency_cycles": float(c[0])}
 
 
 # the reference's exported callback types (FedNLLocalShared.h:8-11, FedNLPPLocalShared.h:8)
