@@ -207,6 +207,16 @@ def cpu_port_rounds_per_s(prob, comp, k, threads: int, max_rounds: int, budget_s
     return n / dt, n, dt
 
 
+# The port against the reference's own operators on the same 8 x86 cores (Xeon @ 2.70 GHz), measured
+# with oracle/time_reference.py where the reference sources are available (reference built with its
+# Release options -O3 -march=native, AVX-512 and FMA): the reference's round is faster than the port,
+# so a GPU / port ratio overstates the GPU / reference ratio by the inverse of these factors.
+PORT_CALIBRATION = {"port_over_reference_native": {"w8a-like d301 TopLEK": 0.339, "a9a-like d124 TopK": 0.492},
+                    "measured": "8 threads each, x86 Xeon @ 2.70 GHz, oracle/time_reference.py, 16 rounds",
+                    "reference_rounds_per_s": {"w8a-like d301 TopLEK": 19.76, "a9a-like d124 TopK": 94.83},
+                    "port_rounds_per_s": {"w8a-like d301 TopLEK": 6.70, "a9a-like d124 TopK": 46.70}}
+
+
 def cpu_port_time_to_tol(prob, comp, k, threads: int, cap: int = 60):
     """The CPU port from x0 = 0 until ||g|| <= TOL (or cap rounds): rounds and wall seconds."""
     from oracle import pyoracle
@@ -300,7 +310,8 @@ def run_reference(args, ws, rank, td):
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": config_dict(prob, comp, k, threads),
-            "cpu_baseline": {"value": v, "unit": "rounds/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "rounds/s", "cores": threads, "kind": "port", "sample": sample,
+                             "calibration": PORT_CALIBRATION},
             "e2e": {"value": v, "unit": "rounds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -614,7 +625,8 @@ def run_ours(args, ws, rank, local, td):
                                 "time_to_tol": cpu_port_time_to_tol(prob, comp, k, threads),
                                 "caveat": "the oracle's C port of the reference round (scalar, fixed operation "
                                           "order, -O3 without -march) stands in for bin_fednl_local, whose "
-                                          "sources and x86 SIMD build are not available on this host"}
+                                          "sources and x86 SIMD build are not available on this host",
+                                "calibration": PORT_CALIBRATION}
     if rank == 0:
         print(json.dumps(line))
     return 0

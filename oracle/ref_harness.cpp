@@ -26,6 +26,7 @@
 #include "dopt/copylocal/include/MutableData.h"
 
 #include <atomic>
+#include <chrono>
 #include <barrier>
 #include <cmath>
 #include <cstdio>
@@ -151,7 +152,7 @@ static void compress_client(Client& C, const Mat& diff, int32_t comp, int32_t k,
 // ---- run: whole FedNL (Option B) ---------------------------------------------------------
 // ext: the header carries Option A, FedNL-LS and tracking switches, and every round also reports
 // f(x_k) and the number of line-search evaluations (TrainLoop.h:1383-1430, 1511-1640)
-static int cmd_run(const char* in_path, const char* out_path, bool ext)
+static int cmd_run(const char* in_path, const char* out_path, bool ext, bool timed = false)
 {
     FILE* fi = fopen(in_path, "rb");
     FILE* fo = fopen(out_path, "wb");
@@ -244,6 +245,8 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
         });
 
     Mat Ltr;
+    const auto t_start = std::chrono::steady_clock::now();
+    std::vector<double> round_end_s;
     for (int32_t r = 0; r < rounds; ++r) {
         cur_round = r;
         start_bar.arrive_and_wait();
@@ -290,6 +293,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
                 t *= ls_gamma;
             }
         }
+        round_end_s.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count());
         W.put<int32_t>(ok ? 1 : 0);
         W.put<double>(g.vectorL2Norm());
         W.put<double>(l);
@@ -312,6 +316,7 @@ static int cmd_run(const char* in_path, const char* out_path, bool ext)
     for (auto& t : th) t.join();
     for (auto& c : cl) delete c.prob;
     W.put<int32_t>(g_first_misround.load());   // trailer: first round whose sigmoid a libm misrounding changed
+    if (timed) W.put(round_end_s.data(), round_end_s.size());   // "time": wall seconds at the end of each round
     fclose(fi);
     fclose(fo);
     return 0;
@@ -611,6 +616,7 @@ int main(int argc, char** argv)
     }
     if (!strcmp(argv[1], "run")) return cmd_run(argv[2], argv[3], false);
     if (!strcmp(argv[1], "runx")) return cmd_run(argv[2], argv[3], true);
+    if (!strcmp(argv[1], "time")) return cmd_run(argv[2], argv[3], false, true);
     if (!strcmp(argv[1], "pp")) return cmd_pp(argv[2], argv[3]);
     if (!strcmp(argv[1], "libsvm") && argc >= 5) return cmd_libsvm(argv[2], argv[3], atoi(argv[4]));
     if (!strcmp(argv[1], "topk")) return cmd_select(argv[2], argv[3], false);
