@@ -584,7 +584,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     CKL();
     if (P.ref) {
         MARK("k_frob_ref");
-        k_frob_ref<<<(na + 3) / 4, 128, 0, st>>>(P);
+        k_frob_ref<<<na, kFrobRefThreads, (size_t)kFrobRing * h->d * 8, st>>>(P);
     } else {
         MARK("k_fsum");
         k_fsum<<<(na + 3) / 4, 128, 0, st>>>(P);
@@ -889,7 +889,11 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     if (select_smem(h->k) > 48 * 1024 && h->k < h->U)
         fednl_raise_dyn_smem((const void*)k_select, select_smem(h->k));
     h->chol_grid = chol_grid(h->d);
-    if (P.ref) h->ref_grid = ref_grid();
+    if (P.ref) {
+        h->ref_grid = ref_grid();
+        if ((size_t)kFrobRing * h->d * 8 > 48 * 1024)
+            fednl_raise_dyn_smem((const void*)k_frob_ref, (size_t)kFrobRing * h->d * 8);
+    }
     *out = h;
     return FEDNL_OK;
 }

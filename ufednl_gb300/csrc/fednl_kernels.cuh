@@ -440,9 +440,19 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
         } else {
             const unsigned long long* mi = fb + (size_t)i * W;
             const unsigned long long* mj = fb + (size_t)j * W;
+            // the in-order sum's first term is 0 + D_s = D_s exactly (D_s >= 0), so it costs no FP64
+            // add: on this part a warp's FP64 instruction takes the pipe for ~64 cycles however few
+            // lanes are active, and most entries have at most one sample with both attributes set
             h = 0.0;
+            bool first = true;
             for (int w = 0; w < W; ++w) {
                 unsigned long long m = mi[w] & mj[w];
+                if (m && first) {
+                    const int b = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    h = s_D[w * 64 + b];
+                    first = false;
+                }
                 while (m) {
                     const int b = __ffsll((long long)m) - 1;
                     m &= m - 1;

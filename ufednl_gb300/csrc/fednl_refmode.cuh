@@ -283,47 +283,57 @@ __global__ void k_ls_margin_ref(Dev P, int S)
 }
 
 // ---- 3r. ||diff||_F^2 from the packed upper part, per processed client ----------------------
-// One warp per client: lanes 0-7 are the eight lane accumulators (column j, rows i < 8 floor(j/8)
-// with i mod 8 = lane), lane 8 the tail scalar (rows 8 floor(j/8) .. j-1), lane 9 the diagonal;
-// each walks its entries column by column exactly as the reference's loop visits them.
-__global__ void k_frob_ref(Dev P)
+// One CTA per client.  The ten running sums of the reference's loop are chains of dependent FP64
+// adds (eight lane accumulators shared by all columns: column j, rows i < 8 floor(j/8) with
+// i mod 8 = lane; one scalar for rows 8 floor(j/8) .. j-1; one for the diagonal), and a dependent
+// FP64 add costs about 64 cycles on this part, so everything else is taken off those chains: warps
+// 1..7 stage the squares of the coming columns into a ring of shared-memory buffers while warp 0's
+// lanes 0..9 add one column's squares to their sums.
+constexpr int kFrobRefThreads = 256;
+constexpr int kFrobRing = 4;                       // ring buffers: a column is added 3 steps after staging
+
+__global__ void __launch_bounds__(kFrobRefThreads) k_frob_ref(Dev P)
 {
-    const int slot = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (slot >= P.n_act) return;
-    const int c = P.act ? P.act[slot] : slot;
+    extern __shared__ double s_sq[];               // [kFrobRing][d]
+    const int c = P.act ? P.act[blockIdx.x] : blockIdx.x;
     const double* v = P.diff + (size_t)c * P.ustr;
-    const int d = P.d;
+    const int d = P.d, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     double acc = 0.0;
-    if (lane < 8) {
-        for (int j = 8; j < d; ++j) {
-            const double* col = v + (size_t)j * (j + 1) / 2;
+    // step j0: warps 1..7 stage column j0 into buffer j0 % kFrobRing; warp 0 adds column
+    // j0 - (kFrobRing - 1), staged kFrobRing - 1 barriers earlier, from its buffer (a different one)
+    for (int j0 = 0; j0 < d + kFrobRing - 1; ++j0) {
+        if (warp > 0 && j0 < d) {
+            double* buf = s_sq + (size_t)(j0 % kFrobRing) * d;
+            const double* col = v + (size_t)j0 * (j0 + 1) / 2;
+            for (int i = tid - 32; i <= j0; i += kFrobRefThreads - 32) buf[i] = __dmul_rn(col[i], col[i]);
+        }
+        const int j = j0 - (kFrobRing - 1);
+        if (warp == 0 && j >= 0) {
+            const double* buf = s_sq + (size_t)(j % kFrobRing) * d;
             const int items = j & ~7;
-#pragma unroll 4
-            for (int i = lane; i < items; i += 8) acc = __dadd_rn(acc, __dmul_rn(col[i], col[i]));
+            if (lane < 8) {
+                for (int i = lane; i < items; i += 8) acc = __dadd_rn(acc, buf[i]);
+            } else if (lane == 8) {
+                for (int i = items; i < j; ++i) acc = __dadd_rn(acc, buf[i]);
+            } else if (lane == 9) {
+                acc = __dadd_rn(acc, buf[j]);
+            }
         }
-    } else if (lane == 8) {
-        for (int j = 1; j < d; ++j) {
-            const double* col = v + (size_t)j * (j + 1) / 2;
-            for (int i = j & ~7; i < j; ++i) acc = __dadd_rn(acc, __dmul_rn(col[i], col[i]));
-        }
-    } else if (lane == 9) {
-        for (int j = 0; j < d; ++j) {
-            const double t = v[(size_t)j * (j + 1) / 2 + j];
-            acc = __dadd_rn(acc, __dmul_rn(t, t));
-        }
+        __syncthreads();
     }
-    double c8[8];
+    if (warp == 0) {
+        double c8[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) c8[l] = __shfl_sync(0xffffffffu, acc, l);
-    const double rest = __shfl_sync(0xffffffffu, acc, 8);
-    const double diag = __shfl_sync(0xffffffffu, acc, 9);
-    if (lane == 0) {
-        double out = refo::lanes8(c8);
-        out = __dadd_rn(out, rest);
-        const double f = __dadd_rn(__dadd_rn(out, out), diag);
-        P.F[c] = f;
-        if (!P.pp) P.lk[c] = sqrt(f);
+        for (int l = 0; l < 8; ++l) c8[l] = __shfl_sync(0xffffffffu, acc, l);
+        const double rest = __shfl_sync(0xffffffffu, acc, 8);
+        const double diag = __shfl_sync(0xffffffffu, acc, 9);
+        if (lane == 0) {
+            double out = refo::lanes8(c8);
+            out = __dadd_rn(out, rest);
+            const double f = __dadd_rn(__dadd_rn(out, out), diag);
+            P.F[c] = f;
+            if (!P.pp) P.lk[c] = sqrt(f);
+        }
     }
 }
 
