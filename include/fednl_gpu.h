@@ -409,12 +409,19 @@ typedef struct fednl_problem_status {
 
 typedef struct fednl_tick_stats {
     int32_t live;               /* problems that ran a round in this tick */
-    int32_t admitted, retired, pending;
+    int32_t admitted, retired;  /* joined the live set at this tick; retired in it */
+    int32_t pending;            /* queued or being admitted after the tick */
     double tick_ms;             /* host wall time of the round phase */
+    double device_ms;           /* device time of the tick: first client phase to the batched solve's end */
     int64_t held_bytes;         /* footprints of the problems live after the tick */
     int64_t device_free, device_total;
 } fednl_tick_stats;
 
+/* The serving loop.  A server admits submitted problems on its own host thread (handle creation,
+ * client-data upload and initial shifts, in arrival order, while the queue head fits in free
+ * device memory less the reserve, the byte budget and the live-slot limit) and releases retired
+ * problems there too; each fednl_server_tick adds the problems admitted since the last tick and runs
+ * one round of every live problem (client phases on their own streams, one batched Newton solve). */
 typedef struct fednl_server_s* fednl_server;
 /* budget_bytes: cap on the live problems' footprints (0: none); reserve_bytes: device memory left
  * free; max_live: live-slot limit (0: none) */
@@ -422,10 +429,22 @@ int fednl_server_create(int64_t budget_bytes, int64_t reserve_bytes, int32_t max
 int fednl_server_destroy(fednl_server s);
 int fednl_server_submit(fednl_server s, const fednl_problem_desc* desc, int32_t precision, const void* features,
                         const double* labels, double tol, int32_t max_rounds, int64_t* id);
+/* The same without a copy: the server reads `features` and `labels` when it admits the problem, so
+ * the caller keeps them valid and unchanged until the problem's state leaves FEDNL_PROBLEM_QUEUED
+ * (for callers whose payloads are large or shared between problems). */
+int fednl_server_submit_ref(fednl_server s, const fednl_problem_desc* desc, int32_t precision, const void* features,
+                            const double* labels, double tol, int32_t max_rounds, int64_t* id);
 int fednl_server_tick(fednl_server s, fednl_tick_stats* stats);
 int fednl_server_status(fednl_server s, int64_t id, fednl_problem_status* status, double* x /* [d] or NULL */);
 /* per (problem, round) latencies in ms, in completion order; count = how many were recorded */
 int fednl_server_latencies(fednl_server s, double* out, int64_t cap, int64_t* count);
+/* per tick with live problems, the tick's device time in ms (no admission work is in it: problems
+ * are admitted on the server's own host thread); count = how many were recorded */
+int fednl_server_device_times(fednl_server s, double* out, int64_t cap, int64_t* count);
+/* the CUDA stream (a cudaStream_t) a handle's work runs on, for callers that order their own work
+ * around it; NULL for a NULL handle */
+void* fednl_gpu_stream(fednl_handle h);
+void* fednl_mx_stream(fednl_mx_handle h);
 
 /* ---- the reference's local driver ---------------------------------------------------------- */
 /* Callback of doptExecuteLocal (bin_fednl_local/include/TrainCallbaksShared.h:11-14): dimension,

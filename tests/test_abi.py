@@ -14,7 +14,7 @@ HEADER = os.path.join(REPO, "include", "fednl_gpu.h")
 
 def header_symbols():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|int32_t|double|const char\*)\s+(fednl_(?:gpu|mx|server)_\w+|doptExecute\w+)\s*\(",
+    return sorted(set(re.findall(r"^\s*(?:int|int32_t|double|const char\*|void\*)\s+(fednl_(?:gpu|mx|server)_\w+|doptExecute\w+)\s*\(",
                                  txt, re.M)))
 
 

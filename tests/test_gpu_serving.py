@@ -177,8 +177,8 @@ def test_server_refuses_what_never_fits(gpu):
     prob = datagen.binary_problem(5, 40, [30, 25, 33], 0.3, 1e-3)
     srv = serving.Server(budget_bytes=1 << 16)          # 64 KB: smaller than any problem's state
     pid = srv.submit_problem(prob, "topk", 320, 1.0)
+    s = srv.wait_settled(pid)                           # the admission thread refuses it
     st = srv.tick()
     assert st.live == 0 and st.pending == 0
-    s, _ = srv.status(pid)
     assert s.state == serving.FAILED and s.error == -2
     srv.close()

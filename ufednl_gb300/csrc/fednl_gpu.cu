@@ -1227,6 +1227,8 @@ int fednl_gpu_client_phase(fednl_handle h)
     return launch_round(h, nullptr, true);
 }
 
+void* fednl_gpu_stream(fednl_handle h) { return h ? (void*)h->stream : nullptr; }
+
 int fednl_gpu_round_result(fednl_handle h, fednl_round_stats* stats)
 {
     if (!h) return fail(FEDNL_EINVAL, "null handle");

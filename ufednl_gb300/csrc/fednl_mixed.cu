@@ -562,27 +562,33 @@ int fednl_mx_upload_client_data(fednl_mx_handle h, const float* features, const 
     if (!h || !features || !labels) return fail_m(FEDNL_EINVAL, "null argument");
     for (int s = 0; s < h->S; ++s)
         if (labels[s] != 1.0 && labels[s] != -1.0) return fail_m(FEDNL_EINVAL, "label %d is not +-1", s);
+    // stream-ordered staging on the handle's own stream: the upload neither waits for nor stalls
+    // other handles' work (a serving loop admits problems while others run)
+    cudaStream_t st = h->stream;
     float* dA = nullptr;
     int* dsoff = nullptr;
-    if (cudaMalloc(&dA, (size_t)h->S * h->d * 4) != cudaSuccess || cudaMalloc(&dsoff, (h->nc + 1) * 4) != cudaSuccess) {
-        cudaFree(dA);
+    if (cudaMallocAsync((void**)&dA, (size_t)h->S * h->d * 4, st) != cudaSuccess ||
+        cudaMallocAsync((void**)&dsoff, (h->nc + 1) * 4, st) != cudaSuccess) {
+        if (dA) cudaFreeAsync(dA, st);
+        cudaStreamSynchronize(st);
         return fail_m(FEDNL_ENOMEM, "staging allocation failed");
     }
     std::vector<double> labp((size_t)h->nc * h->L, 0.0);
     for (int c = 0; c < h->nc; ++c)
         for (int s = 0; s < h->ns[c]; ++s) labp[(size_t)c * h->L + s] = labels[h->soff[c] + s];
     int rc = FEDNL_OK;
-    if (cudaMemcpy(dA, features, (size_t)h->S * h->d * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(dsoff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy((void*)h->P.lab, labp.data(), labp.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpyAsync(dA, features, (size_t)h->S * h->d * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dsoff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync((void*)h->P.lab, labp.data(), labp.size() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         rc = fail_m(FEDNL_ECUDA, "upload failed");
     } else {
-        k_to_feature_major<<<dim3(h->L / 32, (h->d + 31) / 32, h->nc), dim3(32, 8)>>>(dA, dsoff, h->d, h->dp, h->L, h->nc,
-                                                                                      (float*)h->P.X);
-        if (cudaDeviceSynchronize() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "layout kernel failed");
+        k_to_feature_major<<<dim3(h->L / 32, (h->d + 31) / 32, h->nc), dim3(32, 8), 0, st>>>(
+            dA, dsoff, h->d, h->dp, h->L, h->nc, (float*)h->P.X);
+        if (cudaGetLastError() != cudaSuccess) rc = fail_m(FEDNL_ECUDA, "layout kernel failed");
     }
-    cudaFree(dA);
-    cudaFree(dsoff);
+    cudaFreeAsync(dA, st);
+    cudaFreeAsync(dsoff, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == FEDNL_OK) rc = fail_m(FEDNL_ECUDA, "upload failed");
     return rc;
 }
 
@@ -1000,6 +1006,8 @@ int fednl_mx_solve32_batch(fednl_mx_handle const* hs, int n, void* stream)
 }
 
 extern "C" {
+
+void* fednl_mx_stream(fednl_mx_handle h) { return h ? (void*)h->stream : nullptr; }
 
 int fednl_mx_solve_desc(fednl_mx_handle h, FednlSolveDesc* S, void** stream)
 {

@@ -75,7 +75,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32", "fednl_gpu_selftest_rn",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
            "fednl_gpu_autotune", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
-           "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate"]
+           "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate",
+           "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref"]
 
 _lib = None
 

@@ -26,8 +26,8 @@ QUEUED, LIVE, DONE, FAILED = 0, 1, 2, 3
 
 class TickStats(C.Structure):
     _fields_ = [("live", C.c_int32), ("admitted", C.c_int32), ("retired", C.c_int32), ("pending", C.c_int32),
-                ("tick_ms", C.c_double), ("held_bytes", C.c_int64), ("device_free", C.c_int64),
-                ("device_total", C.c_int64)]
+                ("tick_ms", C.c_double), ("device_ms", C.c_double), ("held_bytes", C.c_int64),
+                ("device_free", C.c_int64), ("device_total", C.c_int64)]
 
 
 class ProblemStatus(C.Structure):
@@ -47,6 +47,9 @@ def _lib():
                            "fednl_server_tick": [vp, C.POINTER(TickStats)],
                            "fednl_server_status": [vp, C.c_int64, C.POINTER(ProblemStatus), C.POINTER(C.c_double)],
                            "fednl_server_latencies": [vp, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)],
+                           "fednl_server_device_times": [vp, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)],
+                           "fednl_server_submit_ref": [vp, C.POINTER(ProblemDesc), C.c_int32, vp, C.POINTER(C.c_double),
+                                                       C.c_double, C.c_int32, C.POINTER(C.c_int64)],
                            "fednl_gpu_footprint": [C.POINTER(ProblemDesc), C.POINTER(C.c_int64)],
                            "fednl_mx_footprint": [C.POINTER(ProblemDesc), C.POINTER(C.c_int64)]}.items():
             getattr(L, name).argtypes = args
@@ -115,6 +118,39 @@ def make_data(req: Request):
     return np.ascontiguousarray(a), y
 
 
+def make_pool_payloads(reqs: list[Request], bernoulli_density: float = 0.275, chunk: int = 1 << 16):
+    """Payloads for a long request stream without one feature matrix per problem: the problems of one
+    (d, kind) take row prefixes of one shared FP32 pool (N(0,1), or Bernoulli {0,1} at
+    ``bernoulli_density`` -- the mean of the stream's U(0.05, 0.5) -- with the intercept column
+    last), each with its own labels from its own planted w*.  Returns {pid: (features, labels)};
+    the features are views into the pools, valid while the returned dict lives."""
+    need = {}
+    for r in reqs:
+        key = (r.d, r.kind)
+        need[key] = max(need.get(key, 0), int(r.n_samples.sum()))
+    pools = {}
+    for (d, kind), rows in sorted(need.items()):
+        rng = np.random.default_rng(1000003 * d + (1 if kind == "bernoulli" else 2))
+        a = np.empty((rows, d), dtype=np.float32)
+        for r0 in range(0, rows, chunk):
+            r1 = min(rows, r0 + chunk)
+            if kind == "bernoulli":
+                a[r0:r1, : d - 1] = rng.random((r1 - r0, d - 1), dtype=np.float32) < np.float32(bernoulli_density)
+                a[r0:r1, d - 1] = 1.0
+            else:
+                a[r0:r1] = rng.standard_normal((r1 - r0, d), dtype=np.float32)
+        pools[(d, kind)] = a
+    out = {}
+    for r in reqs:
+        S = int(r.n_samples.sum())
+        a = pools[(r.d, r.kind)][:S]
+        rng = np.random.default_rng(r.seed)
+        w = rng.normal(0.0, 1.0 / np.sqrt(r.d), size=r.d).astype(np.float32)
+        p = 1.0 / (1.0 + np.exp(-(a @ w).astype(np.float64)))
+        out[r.pid] = (a, np.where(rng.random(S) < p, 1.0, -1.0))
+    return out
+
+
 def _desc(req: Request, ns: np.ndarray) -> ProblemDesc:
     d = req.d
     U = d * (d + 1) // 2
@@ -146,6 +182,7 @@ class Server:
         _check(_lib().fednl_server_create(budget_bytes, reserve_bytes, max_live, C.byref(h)))
         self._h = h
         self.d = {}
+        self._refs = {}
 
     def close(self):
         if getattr(self, "_h", None):
@@ -169,6 +206,21 @@ class Server:
         _check(_lib().fednl_server_submit(self._h, C.byref(_desc(req, ns)), req.precision, f.ctypes.data_as(C.c_void_p),
                                           _dp(y), tol, max_rounds, C.byref(pid)))
         self.d[pid.value] = req.d
+        return pid.value
+
+    def submit_ref(self, req: Request, features, labels, tol: float = 1e-9, max_rounds: int = 30) -> int:
+        """Submission without a copy (fednl_server_submit_ref): the server reads features and labels
+        when it admits the problem; they must stay alive and unchanged until then (the server keeps a
+        reference to them here)."""
+        ns = np.ascontiguousarray(req.n_samples, dtype=np.int32)
+        want = np.float32 if req.precision == PRECISION_MIXED else np.float64
+        f = features if (features.dtype == want and features.flags.c_contiguous) else np.ascontiguousarray(features, dtype=want)
+        y = np.ascontiguousarray(labels, dtype=np.float64)
+        pid = C.c_int64(0)
+        _check(_lib().fednl_server_submit_ref(self._h, C.byref(_desc(req, ns)), req.precision,
+                                              f.ctypes.data_as(C.c_void_p), _dp(y), tol, max_rounds, C.byref(pid)))
+        self.d[pid.value] = req.d
+        self._refs[pid.value] = (f, y)
         return pid.value
 
     def submit_problem(self, prob, compressor: str, k: int, alpha: float, precision: int = PRECISION_FP64,
@@ -206,9 +258,27 @@ class Server:
         _check(_lib().fednl_server_latencies(self._h, _dp(out), n.value, C.byref(n)))
         return out
 
+    def device_times(self) -> np.ndarray:
+        """Device time in ms of every tick that had live problems."""
+        n = C.c_int64(0)
+        _check(_lib().fednl_server_device_times(self._h, None, 0, C.byref(n)))
+        out = np.empty(n.value)
+        _check(_lib().fednl_server_device_times(self._h, _dp(out), n.value, C.byref(n)))
+        return out
+
+    def wait_settled(self, pid: int, timeout_s: float = 10.0):
+        """Ticks until the problem has left the queue (admitted and run, or refused)."""
+        t0 = time.perf_counter()
+        while True:
+            self.tick()
+            st = self.status(pid)[0]
+            if st.state != QUEUED or time.perf_counter() - t0 > timeout_s:
+                return st
+            time.sleep(0.001)
+
 
 def serve(reqs: list[Request], payloads: dict, server: Server, tol: float = 1e-9, max_rounds: int = 30,
-          realtime: bool = True, max_ticks: int = 100000):
+          realtime: bool = True, max_ticks: int = 100000, borrow: bool = False):
     """Submits each request when its arrival time has passed (wall clock from the call, or all at
     once without ``realtime``) and ticks until every submitted problem has retired.  Returns the
     problem ids, the per-tick stats and the wall time in seconds."""
@@ -222,14 +292,19 @@ def serve(reqs: list[Request], payloads: dict, server: Server, tol: float = 1e-9
         while nxt < len(reqs) and (not realtime or reqs[nxt].arrival_s <= now):
             r = reqs[nxt]
             f, y = payloads[r.pid]
-            ids[r.pid] = server.submit(r, f, y, tol=tol, max_rounds=max_rounds)
+            if borrow:
+                ids[r.pid] = server.submit_ref(r, f, y, tol=tol, max_rounds=max_rounds)
+            else:
+                ids[r.pid] = server.submit(r, f, y, tol=tol, max_rounds=max_rounds)
             nxt += 1
         st = server.tick()
         ticks.append((time.perf_counter() - t0, st.live, st.admitted, st.retired, st.pending, st.tick_ms,
-                      st.held_bytes, st.device_free, st.device_total))
+                      st.held_bytes, st.device_free, st.device_total, st.device_ms))
         live_or_queued = st.live - st.retired + st.pending
         if nxt == len(reqs) and live_or_queued == 0 and st.admitted == 0:
             break
-        if st.live == 0 and st.admitted == 0 and nxt < len(reqs):
-            time.sleep(max(0.0, min(0.002, reqs[nxt].arrival_s - (time.perf_counter() - t0))))
+        if st.live == 0 and st.admitted == 0:
+            # nothing on the device: wait for the next arrival or for the admission thread
+            wait = 0.0005 if nxt >= len(reqs) else reqs[nxt].arrival_s - (time.perf_counter() - t0)
+            time.sleep(max(0.0, min(0.002, wait)))
     return ids, ticks, time.perf_counter() - t0
