@@ -137,10 +137,7 @@ def test_server_results_same_alone_and_in_the_mix(gpu):
                                        seed_base=123), t))
         if t % 3 == 2:               # later arrivals join a running mix
             srv.tick()
-    for _ in range(100):
-        st = srv.tick()
-        if st.live == st.retired and st.pending == 0:
-            break
+    srv.run_until_idle()
     for pid, t in ids:
         st, x = srv.status(pid)
         assert st.state == serving.DONE, (t, st.state, st.error)

@@ -502,6 +502,8 @@ struct fednl_handle_s {
     int pp = 0, tau = 0, pp_smem_perm = 0;   // FedNL-PP: clients per round, sampler in shared memory
     bool data_ready = false, shifts_ready = false;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;       // the round graph's second branch (k_aggregate)
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     Arena state, feat;
     Dev dev{};
     cudaGraph_t graph = nullptr;
@@ -585,11 +587,18 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     if (P.ref) {
         MARK("k_frob_ref");
         k_frob_ref<<<na, kFrobRefThreads, (size_t)kFrobRing * h->d * 8, st>>>(P);
-    } else {
-        MARK("k_fsum");
-        k_fsum<<<(na + 3) / 4, 128, 0, st>>>(P);
+        CKL();
+    }                             // otherwise the Hessian kernel's last block per client formed F
+    // k_aggregate needs only the gradients and Lk: in a graph it runs on a branch beside the
+    // selection and the shift update (kept in line when the round is profiled kernel by kernel)
+    const bool fork = !M && h->side && !h->pp;
+    if (fork) {
+        CK(cudaEventRecord(h->fork_ev, st));
+        CK(cudaStreamWaitEvent(h->side, h->fork_ev, 0));
+        k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads + 1, kAggThreads, 0, h->side>>>(P);
+        CKL();
+        CK(cudaEventRecord(h->join_ev, h->side));
     }
-    CKL();
     int comp = h->comp;
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
         MARK("k_select");
@@ -637,9 +646,13 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         MARK("end");
         return FEDNL_OK;
     }
-    MARK("k_aggregate");
-    k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads + 1, kAggThreads, 0, st>>>(P);   // + the block for l
-    CKL();
+    if (fork) {
+        CK(cudaStreamWaitEvent(st, h->join_ev, 0));
+    } else {
+        MARK("k_aggregate");
+        k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads + 1, kAggThreads, 0, st>>>(P);   // + the block for l
+        CKL();
+    }
     if (P.fmode) {       // f(x_k) from the round's sigmoid values
         MARK("k_fclient");
         if (P.ref) k_fclient_ref<<<(h->nc + 3) / 4, 128, 0, st>>>(P, P.x, nullptr);
@@ -817,6 +830,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     A.want(&P.Fpart, (size_t)h->nc * h->nseg);
     A.want(&P.dsum, (size_t)h->nc * h->d);
     A.want(&P.F, h->nc);
+    A.want(&P.hdone, h->nc);
     A.want(&P.lk, h->nc);
     A.want(&P.sel, (size_t)h->nc * h->SW);
     A.want(&P.cnt, h->nc);
@@ -865,7 +879,13 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
         delete h;
         return FEDNL_OK;
     }
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+        if (h->side) cudaStreamDestroy(h->side);
+        if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+        if (h->join_ev) cudaEventDestroy(h->join_ev);
         delete h;
         return fail(FEDNL_ECUDA, "cudaStreamCreate failed");
     }
@@ -882,7 +902,8 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
         cudaMemcpy((void*)P.soff, h->soff.data(), (h->nc + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy((void*)P.client_of, client_of.data(), (size_t)h->S * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(P.x, 0, h->d * 8) != cudaSuccess || cudaMemset(P.round_ctr, 0, 4) != cudaSuccess ||
-        cudaMemset(P.status, 0, 4) != cudaSuccess || cudaMemset(P.bar, 0, 16) != cudaSuccess) {
+        cudaMemset(P.status, 0, 4) != cudaSuccess || cudaMemset(P.bar, 0, 16) != cudaSuccess ||
+        cudaMemset(P.hdone, 0, (size_t)h->nc * 4) != cudaSuccess) {
         fednl_gpu_destroy(h);
         return fail(FEDNL_ECUDA, "initial copies failed");
     }
@@ -922,6 +943,9 @@ int fednl_gpu_destroy(fednl_handle h)
     h->feat.release();
     if (h->flush_buf) cudaFree(h->flush_buf);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
     delete h;
     return FEDNL_OK;
 }

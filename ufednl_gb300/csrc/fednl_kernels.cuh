@@ -94,6 +94,7 @@ struct Dev {
     double* fi;             // [nc] f_i at the last evaluated point
     double* xprev;          // [d] x_k during the line search
     double* ls;             // [5] line search: t, -(dx . g), done, evaluations, solve succeeded
+    unsigned* hdone;        // [nc] Hessian blocks of a client finished this round (the last one forms F)
     // the reference's arithmetic order (fednl_refmode.cuh)
     int ref;                // 1: FEDNL_ORDER_REFERENCE
     double* rref;           // [(d+1)(d+2)/2] Cholesky factor with y as column d
@@ -400,6 +401,39 @@ constexpr int kHessPerBlock = 4096;     // upper entries per block
 // contributes a + 2 b to the segment's halving tree.
 __device__ __forceinline__ double segment_value(double a, double b) { return __dadd_rn(a, __dmul_rn(b, 2.0)); }
 
+// F_c = ||diff_c||_F^2 as the in-order sum of the client's segment sums, and Lk = sqrt(F_c)
+// (TopK.h:74-78); one warp, 32 segment sums loaded at a time and added one by one
+__device__ __forceinline__ void client_fsum_warp(const Dev& P, int c, int lane)
+{
+    const double* fp = P.Fpart + (size_t)c * P.nseg;
+    double f = 0.0;
+    for (int q0 = 0; q0 < P.nseg; q0 += 32) {
+        const double v = (q0 + lane < P.nseg) ? __ldcg(fp + q0 + lane) : 0.0;
+        const int cnt = min(32, P.nseg - q0);
+        for (int t = 0; t < cnt; ++t) f = __dadd_rn(f, __shfl_sync(0xffffffffu, v, t));
+    }
+    if (lane == 0) {
+        P.F[c] = f;
+        if (!P.pp) P.lk[c] = sqrt(f);    // FedNL-PP takes Lk after the update (k_pp_dir)
+    }
+}
+
+// Called by every block of a Hessian launch after its Fpart stores: the last of a client's blocks
+// (gridDim.x of them) forms F_c and Lk, then re-arms the client's counter for the next round.
+__device__ __forceinline__ void client_fsum_last_block(const Dev& P, int c)
+{
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(P.hdone + c, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last && threadIdx.x < 32) {
+        __threadfence();
+        client_fsum_warp(P, c, threadIdx.x);
+        if (threadIdx.x == 0) P.hdone[c] = 0u;
+    }
+}
+
 template <bool SMEM_BITS>
 __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
 {
@@ -475,6 +509,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
+    if (mode != 1 && !P.ref) client_fsum_last_block(P, c);
 }
 
 // dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
@@ -516,26 +551,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
-}
-
-// per-client ||diff||_F^2 (segment sums in order) and Lk = ||diff||_F (TopK.h:74-78)
-__global__ void k_fsum(Dev P)
-{
-    const int slot = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (slot >= P.n_act) return;
-    const int c = P.act ? P.act[slot] : slot;
-    const double* fp = P.Fpart + (size_t)c * P.nseg;
-    double f = 0.0;
-    for (int q0 = 0; q0 < P.nseg; q0 += 32) {
-        const double v = (q0 + lane < P.nseg) ? fp[q0 + lane] : 0.0;
-        const int cnt = min(32, P.nseg - q0);
-        for (int t = 0; t < cnt; ++t) f = __dadd_rn(f, __shfl_sync(0xffffffffu, v, t));
-    }
-    if (lane == 0) {
-        P.F[c] = f;
-        if (!P.pp) P.lk[c] = sqrt(f);    // FedNL-PP takes Lk after the update (k_pp_dir)
-    }
+    if (mode != 1 && !P.ref) client_fsum_last_block(P, c);
 }
 
 // master H = mean_i shift_i after the initial shifts (TrainLoop.h:639-643, :732-735)

@@ -92,6 +92,7 @@ struct fednl_server_s {
     std::condition_variable cv;    // wakes the admission thread
     std::deque<Pending> queue;
     std::vector<Live> live;        // the tick thread's
+    int live_n = 0;                // live.size(), published under mu for the admission thread
     std::vector<Live> ready;       // admitted, joining at the next tick
     std::vector<Live> dead;        // retired, to be released by the admission thread
     int admitting = 0;             // taken from the queue, being admitted
@@ -137,7 +138,7 @@ static int admit_one(fednl_server_s* s)
     {
         std::lock_guard<std::mutex> g(s->mu);
         if (s->queue.empty()) return 0;
-        if (s->max_live > 0 && (int)s->live.size() >= s->max_live) return 0;
+        if (s->max_live > 0 && s->live_n + (int)s->ready.size() + s->admitting >= s->max_live) return 0;
         const Pending& head = s->queue.front();
         int64_t fr = 0, tot = 0;
         if (fednl_gpu_mem_info(&fr, &tot)) return 0;
@@ -340,6 +341,7 @@ int fednl_server_tick(fednl_server s, fednl_tick_stats* st)
         T.admitted = (int32_t)s->ready.size();
         for (Live& L : s->ready) s->live.push_back(L);
         s->ready.clear();
+        s->live_n = (int)s->live.size();
     }
     const double t_start = now_ms();
     T.live = (int32_t)s->live.size();
@@ -423,6 +425,7 @@ int fednl_server_tick(fednl_server s, fednl_tick_stats* st)
     T.tick_ms = now_ms() - t_start;
     {
         std::lock_guard<std::mutex> g(s->mu);
+        s->live_n = (int)s->live.size();
         T.pending = (int32_t)(s->queue.size() + s->ready.size()) + s->admitting;
         T.held_bytes = s->held;
     }

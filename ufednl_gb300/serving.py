@@ -266,6 +266,19 @@ class Server:
         _check(_lib().fednl_server_device_times(self._h, _dp(out), n.value, C.byref(n)))
         return out
 
+    def run_until_idle(self, timeout_s: float = 120.0) -> list[TickStats]:
+        """Ticks until nothing is queued, being admitted or live (sleeping 1 ms between ticks
+        that had nothing live, while the admission thread works), or until ``timeout_s``."""
+        t0 = time.perf_counter()
+        ticks = []
+        while True:
+            st = self.tick()
+            ticks.append(st)
+            if (st.live == st.retired and st.pending == 0) or time.perf_counter() - t0 > timeout_s:
+                return ticks
+            if st.live == 0:
+                time.sleep(0.001)
+
     def wait_settled(self, pid: int, timeout_s: float = 10.0):
         """Ticks until the problem has left the queue (admitted and run, or refused)."""
         t0 = time.perf_counter()
