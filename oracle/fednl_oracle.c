@@ -1079,64 +1079,64 @@ void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const dou
 /* Option-B solve                                                                     */
 /* ================================================================================== */
 
-/* choleskyFactorization<Mat, fill_L_factor=true, in_input_symmetric=true>
- * dopt/dopt/linalg_matrices/include/factorization/CholeskyFactorization.h:153-272:
- * H + l I = R^T R reading only the upper triangle; R is written to the upper triangle of ltr and
- * mirrored into the lower one.  Restated in right-looking order: a_ij starts at h_ij (+ l on the
- * diagonal) and receives a_ij = fma(-r_ki, r_kj, a_ij) for k = 0, 1, ... in order; then
- * r_ii = sqrt(a_ii) and r_ij = (1 / r_ii) a_ij.  The reference accumulates each dot product first
- * and subtracts it once, which differs by a few ulps; the GB300 kernel follows this order. */
-int orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr)
+/* The fixed-order Option-B solve (x = (H + l I)^{-1} b, the reference's choleskyFactorization and
+ * triangular solves, CholeskyFactorization.h:153-272 and ElementarySolvers.h:71-224, in an order
+ * with a short dependency chain per column): a square-root-free LDL^T factorization,
+ * H + l I = L D L^T with L unit lower triangular, right-looking.  a_ij starts at h_ij (+ l on the
+ * diagonal).  At step k the pivot d_k = a_kk is rejected when negative (as the reference rejects a
+ * negative radicand), inv_k = 1 / d_k, the row's multipliers are l_kj = a_kj inv_k, and every
+ * a_ij with k < i <= j receives a_ij = fma(-l_ki, a_kj, a_ij) (a_kj unscaled).  ltr's upper
+ * triangle receives the multipliers l_kj (row k of L^T) and d_k on the diagonal, mirrored into the
+ * lower triangle.  The GB300 kernel follows this order; the reference's own order is
+ * orc_cholesky_ref. */
+int orc_ldlt(const double* h, int32_t d, int32_t lda, double l, double* ltr)
 {
     memset(ltr, 0, (size_t)d * (size_t)lda * sizeof(double));
     for (int32_t j = 0; j < d; ++j)
         for (int32_t i = 0; i <= j; ++i)
             ltr[(size_t)j * lda + i] = (i == j) ? h[(size_t)j * lda + i] + l : h[(size_t)j * lda + i];
+    double* w = (double*)malloc((size_t)d * sizeof(double));
     for (int32_t k = 0; k < d; ++k) {
-        double a = ltr[(size_t)k * lda + k];
+        const double a = ltr[(size_t)k * lda + k];
         if (a < 0) {
-            if (a > -0.0)
-                a = 0.0;
-            else
-                return 0;
+            free(w);
+            return 0;
         }
-        double r = sqrt(a);
-        ltr[(size_t)k * lda + k] = r;
-        double inv = 1.0 / r;
-        for (int32_t j = k + 1; j < d; ++j)
-            ltr[(size_t)j * lda + k] *= inv;
+        const double inv = 1.0 / a;
         for (int32_t j = k + 1; j < d; ++j) {
-            double rkj = ltr[(size_t)j * lda + k];
+            w[j] = ltr[(size_t)j * lda + k];
+            ltr[(size_t)j * lda + k] = w[j] * inv;
+        }
+        for (int32_t j = k + 1; j < d; ++j) {
             double* col = ltr + (size_t)j * lda;
             for (int32_t i = k + 1; i <= j; ++i)
-                col[i] = fma(-ltr[(size_t)i * lda + k], rkj, col[i]);
+                col[i] = fma(-ltr[(size_t)i * lda + k], w[j], col[i]);
         }
     }
+    free(w);
     for (int32_t j = 0; j < d; ++j)
         for (int32_t i = 0; i < j; ++i)
             ltr[(size_t)i * lda + j] = ltr[(size_t)j * lda + i];
     return 1;
 }
 
-/* forwardSubstitutionWithATranspose then backwardSubstitutionWithATranspose
- * dopt/dopt/linalg_linsolvers/include/ElementarySolvers.h:186-224 and :71-128: R^T y = b, R x = y.
- * Restated column-oriented: y_t = y_t * (1 / r_tt) (the factorization's reciprocal; the reference
- * divides), then y_i = fma(-r_ti, y_t, y_i) for the remaining i. */
-void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
+/* L y = b, z = D^{-1} y, L^T x = z, column-oriented: y_i = fma(-l_ti, y_t, y_i) for t ascending,
+ * z_t = y_t (1 / d_t) (the factorization's reciprocal), then x_i = fma(-l_it, x_t, x_i) for t
+ * descending (unit diagonal: no division on the chain). */
+void orc_solve_ldlt(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
 {
     for (int32_t i = 0; i < d; ++i)
         x[i] = b[i];
     for (int32_t t = 0; t < d; ++t) {
-        x[t] = x[t] * (1.0 / ltr[(size_t)t * lda + t]);
-        double yt = x[t];
+        const double yt = x[t];
         for (int32_t i = t + 1; i < d; ++i)
             x[i] = fma(-ltr[(size_t)i * lda + t], yt, x[i]);
+        x[t] = yt * (1.0 / ltr[(size_t)t * lda + t]);
     }
     for (int32_t t = d - 1; t >= 0; --t) {
-        x[t] = x[t] * (1.0 / ltr[(size_t)t * lda + t]);
-        double yt = x[t];
+        const double xt = x[t];
         for (int32_t i = 0; i < t; ++i)
-            x[i] = fma(-ltr[(size_t)t * lda + i], yt, x[i]);
+            x[i] = fma(-ltr[(size_t)t * lda + i], xt, x[i]);
     }
 }
 
@@ -1637,7 +1637,7 @@ int orc_round(orc_state* S, double* grad_norm)
      * regularises by mu = lambda instead (:1383-1430, computeMuStrongConvexity) */
     double* dx = (double*)malloc((size_t)d * sizeof(double));
     int ok = P->ref_order ? orc_cholesky_ref(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr)
-                          : orc_cholesky(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr);
+                          : orc_ldlt(S->H, d, lda, P->option_a ? P->lambda : l, S->ltr);
     S->ls_steps = 0;
     if (P->line_search || P->track_f) {       /* function_aggregation (TrainLoop.h:1511-1541) */
         double* fs = (double*)malloc((size_t)nc * sizeof(double));
@@ -1650,7 +1650,7 @@ int orc_round(orc_state* S, double* grad_norm)
         if (P->ref_order)
             orc_solve_chol_ref(S->ltr, d, lda, S->g, dx);
         else
-            orc_solve_chol(S->ltr, d, lda, S->g, dx);
+            orc_solve_ldlt(S->ltr, d, lda, S->g, dx);
         if (!P->line_search) {
             for (int32_t i = 0; i < d; ++i)
                 S->x[i] -= dx[i];
@@ -1748,9 +1748,9 @@ static int orc_round_pp_master(orc_state* S, double* grad_norm)
     l = l * inv_n + S->l_prev;
     S->l_prev = l;
     S->l = l;
-    int ok = orc_cholesky(S->H, d, lda, l, S->ltr);
+    int ok = orc_ldlt(S->H, d, lda, l, S->ltr);
     if (ok)
-        orc_solve_chol(S->ltr, d, lda, S->g, S->x);
+        orc_solve_ldlt(S->ltr, d, lda, S->g, S->x);
     if (grad_norm) {
         double gs = 0.0;
         for (int32_t i = 0; i < d; ++i)

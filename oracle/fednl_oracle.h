@@ -117,9 +117,10 @@ void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const dou
                  double lambda, double* h);
 
 /* ---- Option-B solve -------------------------------------------------------------------- */
-/* Cholesky of (upper(h) + l I) into ltr (d x lda, upper = R, lower = R^T); 1 on success */
-int  orc_cholesky(const double* h, int32_t d, int32_t lda, double l, double* ltr);
-void orc_solve_chol(const double* ltr, int32_t d, int32_t lda, const double* b, double* x);
+/* LDL^T of (upper(h) + l I) into ltr (d x lda: upper = multipliers of L^T with D on the diagonal,
+ * mirrored into the lower part); 1 on success, 0 for a negative pivot */
+int  orc_ldlt(const double* h, int32_t d, int32_t lda, double l, double* ltr);
+void orc_solve_ldlt(const double* ltr, int32_t d, int32_t lda, const double* b, double* x);
 
 /* ---- whole FedNL run (forcesequpdate semantics: master merges clients in order) -------- */
 orc_state* orc_create(const orc_problem* p, const double* x0);

@@ -86,9 +86,12 @@ def lib():
         L.orc_pack2_natural.argtypes = [C.c_double, C.c_double]
         L.orc_l2sq.restype = C.c_double
         L.orc_l2sq.argtypes = [dp, C.c_size_t]
-        L.orc_cholesky.restype = C.c_int
-        L.orc_cholesky.argtypes = [dp, C.c_int32, C.c_int32, C.c_double, dp]
-        L.orc_solve_chol.argtypes = [dp, C.c_int32, C.c_int32, dp, dp]
+        L.orc_ldlt.restype = C.c_int
+        L.orc_ldlt.argtypes = [dp, C.c_int32, C.c_int32, C.c_double, dp]
+        L.orc_solve_ldlt.argtypes = [dp, C.c_int32, C.c_int32, dp, dp]
+        L.orc_cholesky_ref.restype = C.c_int
+        L.orc_cholesky_ref.argtypes = [dp, C.c_int32, C.c_int32, C.c_double, dp]
+        L.orc_solve_chol_ref.argtypes = [dp, C.c_int32, C.c_int32, dp, dp]
         L.orc_margin.argtypes = [dp, C.c_int32, C.c_int32, C.c_int32, dp, dp]
         L.orc_sigmoid.argtypes = [dp, C.c_int32, dp]
         L.orc_gradient.argtypes = [dp, C.c_int32, C.c_int32, C.c_int32, dp, dp, C.c_double, dp]
@@ -148,11 +151,11 @@ def randseqk(rng_state: np.ndarray, d: int, lda: int, k: int) -> np.ndarray:
 def cholesky_solve(h_full: np.ndarray, d: int, lda: int, l: float, b: np.ndarray):
     h = np.ascontiguousarray(h_full, dtype=np.float64)
     ltr = np.zeros(d * lda)
-    ok = lib().orc_cholesky(_dp(h), d, lda, l, _dp(ltr))
+    ok = lib().orc_ldlt(_dp(h), d, lda, l, _dp(ltr))
     x = np.zeros(d)
     if ok:
         bb = np.ascontiguousarray(b, dtype=np.float64)
-        lib().orc_solve_chol(_dp(ltr), d, lda, _dp(bb), _dp(x))
+        lib().orc_solve_ldlt(_dp(ltr), d, lda, _dp(bb), _dp(x))
     return bool(ok), x
 
 

@@ -265,19 +265,34 @@ def test_cholesky_matches_reference(oracle):
 
 def test_cholesky_known_answer(oracle):
     """Known-answer case of dopt/bin_tests/src/linalg_matrices/CholeskyFactorizationGTest.cpp:11-40:
-    L = [[1,0,0],[4,7,0],[1,2,5]], A = L L^T is factored back into L exactly; [[1,2],[2,1]] is
-    rejected as not positive definite."""
-    L = np.array([[1.0, 0, 0], [4, 7, 0], [1, 2, 5]])
-    A = L @ L.T
-    lib = oracle.lib()
-    ltr = np.zeros(9)
+    L = [[1,0,0],[4,7,0],[1,2,5]], A = L L^T is factored back into L exactly by the reference's
+    algorithm (orc_cholesky_ref); [[1,2],[2,1]] is rejected as not positive definite.  The fixed
+    order's LDL^T factors A = L1 D L1^T (L1 unit lower with integer entries, D powers of two) back
+    exactly and rejects the same matrix."""
     import ctypes as C
     dp = C.POINTER(C.c_double)
-    assert lib.orc_cholesky(A.T.copy().ctypes.data_as(dp), 3, 3, 0.0, ltr.ctypes.data_as(dp)) == 1
+    lib = oracle.lib()
+    L = np.array([[1.0, 0, 0], [4, 7, 0], [1, 2, 5]])
+    A = L @ L.T
+    ltr = np.zeros(9)
+    assert lib.orc_cholesky_ref(A.T.copy().ctypes.data_as(dp), 3, 3, 0.0, ltr.ctypes.data_as(dp)) == 1
     R = ltr.reshape(3, 3).T           # row-major view: R[i][j] = ltr[j*3+i]
     np.testing.assert_array_equal(np.triu(R), L.T)
     bad = np.array([[1.0, 2.0], [2.0, 1.0]])
-    assert lib.orc_cholesky(bad.T.copy().ctypes.data_as(dp), 2, 2, 0.0, np.zeros(4).ctypes.data_as(dp)) == 0
+    assert lib.orc_cholesky_ref(bad.T.copy().ctypes.data_as(dp), 2, 2, 0.0, np.zeros(4).ctypes.data_as(dp)) == 0
+    L1 = np.array([[1.0, 0, 0], [3, 1, 0], [-2, 5, 1]])
+    D = np.diag([1.0, 4.0, 2.0])
+    A1 = L1 @ D @ L1.T
+    ltr = np.zeros(9)
+    assert lib.orc_ldlt(A1.T.copy().ctypes.data_as(dp), 3, 3, 0.0, ltr.ctypes.data_as(dp)) == 1
+    F = ltr.reshape(3, 3).T
+    np.testing.assert_array_equal(np.triu(F, 1), np.triu(L1.T, 1))
+    np.testing.assert_array_equal(np.diag(F), np.diag(D))
+    b = np.array([1.0, -2.0, 3.0])
+    ok, x = oracle.cholesky_solve(A1, 3, 3, 0.0, b)
+    assert ok
+    np.testing.assert_allclose(x, np.linalg.solve(A1, b), rtol=1e-14)
+    assert lib.orc_ldlt(bad.T.copy().ctypes.data_as(dp), 2, 2, 0.0, np.zeros(4).ctypes.data_as(dp)) == 0
 
 
 def test_natural_pack_layout(oracle):

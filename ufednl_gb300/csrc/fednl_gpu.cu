@@ -26,6 +26,7 @@
 #include <vector>
 
 using namespace fednl;
+static_assert(kCholNB == 32, "fednl_chol_work_elems sizes the panel buffer for 32-row panels");
 
 namespace {
 
@@ -841,7 +842,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     A.want(&P.rstate, h->nc);
     A.want(&P.rseq, h->nc);
     A.want(&P.hmap, (size_t)h->nc * h->hcap);
-    A.want(&P.work, (size_t)(h->d + 1) * (h->d + 2) / 2);
+    A.want(&P.work, fednl_chol_work_elems(h->d));
     A.want(&P.dx, h->d);
     A.want(&P.ybuf, h->d);
     A.want(&P.rinv, h->d);
@@ -2043,7 +2044,7 @@ int fednl_gpu_optionb_solve(const double* H, int32_t d, int32_t lda, double l, c
     s.a.want(&dfull, (size_t)d * lda);
     s.a.want(&dpack, U);
     s.a.want(&dg, d);
-    s.a.want(&P.work, (size_t)(d + 1) * (d + 2) / 2);
+    s.a.want(&P.work, fednl_chol_work_elems(d));
     s.a.want(&P.dx, d);
     s.a.want(&P.ybuf, d);
     s.a.want(&P.rinv, d);
@@ -2090,7 +2091,7 @@ int fednl_gpu_optionb_solve32(const double* H, int32_t d, int32_t lda, double l,
     s.a.want(&dg, d);
     s.a.want(&dl, 1);
     s.a.want(&ddx, d);
-    s.a.want(&work, (size_t)(d + 1) * (d + 2) / 2);
+    s.a.want(&work, fednl_chol_work_elems(d));
     s.a.want(&ybuf, d);
     s.a.want(&rinv, d);
     s.a.want(&stats, 4);
@@ -2178,6 +2179,12 @@ __global__ void k_selftest_rn(unsigned long long seed, long long n, unsigned lon
         const double a = __longlong_as_double((long long)u);
         if (__double_as_longlong(sqrt_rn_int(a)) != __double_as_longlong(sqrt(a))) atomicAdd(&bad[0], 1ull);
         if (__double_as_longlong(rcp_rn_int(a)) != __double_as_longlong(1.0 / a)) atomicAdd(&bad[1], 1ull);
+        // the pivot's fused pair: r against sqrt(a), 1 / r against the division of 1 by sqrt(a)
+        double inv;
+        const double r = sqrt_rcp_rn_int(a, inv);
+        const double rh = sqrt(a);
+        if (__double_as_longlong(r) != __double_as_longlong(rh)) atomicAdd(&bad[0], 1ull);
+        if (rh > 0.0 && __double_as_longlong(inv) != __double_as_longlong(1.0 / rh)) atomicAdd(&bad[1], 1ull);
     }
 }
 }  // namespace
@@ -2399,7 +2406,8 @@ int fednl_gpu_profile_kernels(fednl_handle h, int32_t rounds, int64_t flush_byte
 // before each launch, the factor is overwritten.  Calls that overlap on the GPU race.
 namespace {
 constexpr int kNoAllocMaxD = 512;
-constexpr size_t kNoAllocMaxUA = (size_t)(kNoAllocMaxD + 1) * (kNoAllocMaxD + 2) / 2;   // factor with y column
+constexpr size_t kNoAllocMaxUA = (size_t)(kNoAllocMaxD + 1) * (kNoAllocMaxD + 2) / 2 +
+                                  (size_t)kCholNB * (kNoAllocMaxD + 1);   // factor with y column, panel rows
 constexpr size_t kNoAllocDoubles = kNoAllocMaxUA + 2 * kNoAllocMaxD + 4;   // factor, y, 1/r, barrier+status
 constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];

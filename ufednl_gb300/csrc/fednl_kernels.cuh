@@ -576,8 +576,11 @@ __global__ void k_h_init(Dev P)
 // * buildMinHeap runs level by level in parallel: sifts of nodes on one level touch disjoint
 //   subtrees, so the result equals the reference's descending-index order.
 // * The scanned entries stream into shared memory by bulk asynchronous copies (cp.async.bulk with
-//   an mbarrier per buffer, double-buffered); one warp tests them 256 at a time, one vote per
-//   256 when none exceeds the root, one ballot per 32 otherwise.
+//   an mbarrier per buffer, double-buffered); one warp tests them 256 at a time, each lane its
+//   first entry above the root, one warp-wide minimum per replacement.  The heap's top two levels
+//   live in registers during the scan, the same in every lane, and the warp replaces the root in
+//   step: most root replacements stop within the top three levels (the carried comparison value
+//   ends the walk early), so a replacement is a few compares and at most one shared-memory load.
 // * TopLEK extracts in chunks of 32 recording the order in place (extracFromMinHeap leaves the
 //   extracted element at the array's end, MinHeap.h:133-140) and stops after the chunk that opens
 //   the rounding window; the top two heap levels live in registers during the extraction.  The
@@ -690,6 +693,49 @@ __device__ __forceinline__ unsigned long long heap_replace_root(HeapS& h, int k,
     h.key[0] = m;
     h.hid[0] = h.hid[lo];
     heap_descend(h, lo, k, m, cand, p);
+    return m;
+}
+
+// heap_replace_root with the heap's levels 0 and 1 in registers (K0..K4, I0..I4; k >= 21, so levels
+// 0-2 are complete): the same comparisons and moves, level 2 and below in shared memory
+__device__ __forceinline__ unsigned long long heap_replace_root_r(HeapS& h, int k, unsigned long long cand, unsigned p,
+                                                                  unsigned long long& K0, unsigned long long& K1,
+                                                                  unsigned long long& K2, unsigned long long& K3,
+                                                                  unsigned long long& K4, unsigned& I0, unsigned& I1,
+                                                                  unsigned& I2, unsigned& I3, unsigned& I4)
+{
+    const bool r12 = K2 < K1, r34 = K4 < K3;
+    const unsigned long long m12 = r12 ? K2 : K1, m34 = r34 ? K4 : K3;
+    const bool r = m34 < m12;
+    const unsigned long long m = r ? m34 : m12;
+    if (!(cand > m)) {
+        K0 = cand;
+        I0 = p;
+        return cand;
+    }
+    const int lo = r ? (r34 ? 4 : 3) : (r12 ? 2 : 1);
+    K0 = m;
+    I0 = lo == 1 ? I1 : lo == 2 ? I2 : lo == 3 ? I3 : I4;
+    // the children of lo (level 2) against the value that moved up
+    const int f = 4 * lo + 1;
+    const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(h.key + f);
+    const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(h.key + f + 2);
+    const bool s01 = a.y < a.x, s23 = b.y < b.x;
+    const unsigned long long n01 = s01 ? a.y : a.x, n23 = s23 ? b.y : b.x;
+    const bool sr = n23 < n01;
+    const unsigned long long m2 = sr ? n23 : n01;
+    unsigned long long nk = cand;
+    unsigned ni = p;
+    if (m > m2) {
+        const int gp = f + (sr ? (s23 ? 3 : 2) : (s01 ? 1 : 0));
+        nk = m2;
+        ni = h.hid[gp];
+        heap_descend(h, gp, k, m2, cand, p);
+    }
+    if (lo == 1) { K1 = nk; I1 = ni; }
+    else if (lo == 2) { K2 = nk; I2 = ni; }
+    else if (lo == 3) { K3 = nk; I3 = ni; }
+    else { K4 = nk; I4 = ni; }
     return m;
 }
 
@@ -813,6 +859,15 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
     // scan, SpecialMathRoutinesForMatrix.h:300-318
     if (warp == 0) {
         unsigned long long root = h.key[0];
+        // levels 0 and 1 of the heap live in registers during the scan (k >= 21), the same in every
+        // lane: the warp replaces the root in step, without a divergent branch or a broadcast
+        const bool regs = k >= 21;
+        unsigned long long K0 = 0, K1 = 0, K2 = 0, K3 = 0, K4 = 0;
+        unsigned I0 = 0, I1 = 0, I2 = 0, I3 = 0, I4 = 0;
+        if (regs) {
+            K0 = h.key[0]; K1 = h.key[1]; K2 = h.key[2]; K3 = h.key[3]; K4 = h.key[4];
+            I0 = h.hid[0]; I1 = h.hid[1]; I2 = h.hid[2]; I3 = h.hid[3]; I4 = h.hid[4];
+        }
         for (int q = 0; q < n_chunks; ++q) {
             const int b = q & 1;
             if (!mbar_wait(&s_bar[b], (unsigned)(q >> 1) & 1u)) {
@@ -823,11 +878,11 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
             const int len = min(kSelStage, U - st);
             const double* buf = stage + b * kSelStage;
             // 256 entries per step, 8 per lane in lane-contiguous groups of 32 (entry e = 32 j + lane
-            // of the step).  Each pass votes all 8 groups against the root and takes the first entry
-            // above it that comes after the last one taken; lane 0 replaces the root and broadcasts
-            // the new root.  The root of this heap can also decrease (a deeper element may move up),
-            // so every remaining entry is voted again after each replacement.  Entries outside
-            // [k, U) read as 0, which never exceeds the root.
+            // of the step).  Each pass finds the first entry above the root that comes after the last
+            // one taken (each lane its own first, then the warp minimum) and replaces the root with
+            // it.  The root of this heap can also decrease (a deeper element may move up), so every
+            // remaining entry is tested again after each replacement.  Entries outside [k, U) read as
+            // 0, which never exceeds the root.
             for (int o = 0; o < len; o += 256) {
                 unsigned long long v[8];
 #pragma unroll
@@ -837,28 +892,27 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
                 }
                 int done = -1;                           // last entry taken in this step
                 for (;;) {
-                    unsigned m[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) m[j] = __ballot_sync(0xffffffffu, v[j] > root && j * 32 + lane > done);
-                    int jf = -1;
-                    unsigned mf = 0u;
+                    unsigned e = 0xffffffffu;
+                    unsigned long long mine = 0ull;
 #pragma unroll
                     for (int j = 7; j >= 0; --j)
-                        if (m[j]) {
-                            jf = j;
-                            mf = m[j];
+                        if (v[j] > root && j * 32 + lane > done) {
+                            e = (unsigned)(j * 32 + lane);
+                            mine = v[j];
                         }
-                    if (jf < 0) break;
-                    const int l = __ffs(mf) - 1;
-                    unsigned long long mine = v[0];
-#pragma unroll
-                    for (int j = 1; j < 8; ++j)
-                        if (jf == j) mine = v[j];
-                    const unsigned long long cand = __shfl_sync(0xffffffffu, mine, l);
-                    done = jf * 32 + l;
-                    unsigned long long nr = 0ull;
-                    if (lane == 0) nr = heap_replace_root(h, k, cand, (unsigned)(st + o + done));
-                    root = __shfl_sync(0xffffffffu, nr, 0);
+                    e = __reduce_min_sync(0xffffffffu, e);
+                    if (e == 0xffffffffu) break;
+                    const unsigned long long cand = __shfl_sync(0xffffffffu, mine, (int)(e & 31u));
+                    done = (int)e;
+                    if (regs) {
+                        root = heap_replace_root_r(h, k, cand, (unsigned)(st + o + done), K0, K1, K2, K3, K4, I0, I1,
+                                                   I2, I3, I4);
+                        __syncwarp();
+                    } else {
+                        unsigned long long nr = 0ull;
+                        if (lane == 0) nr = heap_replace_root(h, k, cand, (unsigned)(st + o + done));
+                        root = __shfl_sync(0xffffffffu, nr, 0);
+                    }
                 }
             }
             __syncwarp();
@@ -868,6 +922,10 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
                 const int nlen = min(kSelStage, ustr - nst);
                 tma_load_1d(stage + b * kSelStage, v + nst, (unsigned)nlen * 8u, &s_bar[b]);
             }
+        }
+        if (regs && lane == 0) {
+            h.key[0] = K0; h.key[1] = K1; h.key[2] = K2; h.key[3] = K3; h.key[4] = K4;
+            h.hid[0] = I0; h.hid[1] = I1; h.hid[2] = I2; h.hid[3] = I3; h.hid[4] = I4;
         }
     }
     __syncthreads();
@@ -1335,21 +1393,26 @@ __global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
 __device__ __forceinline__ size_t up_pos(int i, int j) { return (size_t)j * (j + 1) / 2 + i; }
 
 // ---- 8b. Option-B solve across the whole GPU -------------------------------------------------
-// Blocked right-looking Cholesky in one cooperative launch.  For each panel of kCholNB rows:
+// Blocked right-looking LDL^T (H + l I = L D L^T, L unit lower; the oracle's orc_ldlt order) in
+// one cooperative launch.  Square-root free: the pivot chain of a column is the reciprocal of the
+// pivot, one multiply and one fused multiply-add.  For each panel of kCholNB rows:
 //   1. every CTA factors the kCholNB x kCholNB diagonal block redundantly in shared memory (no
 //      barrier needed; CTA 0 writes it back) and, in the same column loop, the panel rows of its
-//      own share of the columns right of the block (r_kj = a_kj (1 / r_kk), then
-//      a_ij = fma(-r_ki, r_kj, a_ij)); on GB300 a warp's FP64 instructions issue about once per
-//      64 cycles and sqrt + reciprocal take ~1000 cycles, so the loop keeps the pivot chain short
-//      (two CTA barriers per column) and spreads the updates over all warps;
-//   2. grid barrier, then all threads apply the panel to the trailing triangle entry by entry
-//      (a_ij = fma(-r_ki, r_kj, a_ij), k over the panel in order); grid barrier.
+//      own share of the columns right of the block (l_kj = a_kj (1 / d_k), then
+//      a_ij = fma(-l_ki, a_kj, a_ij) with a_kj unscaled); on GB300 a warp's FP64 instructions
+//      issue about once per 64 cycles and the correctly rounded reciprocal takes ~300 cycles, so
+//      the loop keeps the pivot chain short (two CTA barriers per column) and spreads the updates
+//      over all warps;
+//   2. the panel's multipliers go to the packed factor and its unscaled rows right of the block to
+//      the work array's panel buffer; grid barrier, then all threads apply the panel to the
+//      trailing triangle entry by entry (a_ij = fma(-l_ki, a_kj, a_ij), k over the panel in
+//      order); grid barrier.
 // Every entry undergoes exactly the operation sequence of the unblocked right-looking algorithm,
 // so the factor equals the CPU oracle's factor bit for bit.  g is appended as column d of the
-// packed matrix: the strips and trailing updates then carry out the forward substitution
-// R^T y = g in the column-oriented order (y_t *= 1/r_tt, y_i = fma(-r_ti, y_t, y_i)), and y ends
-// up in column d.  The backward substitution runs in CTA 0, blocked by 32 rows, same order as the
-// oracle's.
+// packed matrix: the strips and trailing updates then carry out the forward substitution L y = g
+// (y_i = fma(-l_ti, y_t, y_i)), and the scaling of row t leaves z_t = y_t (1 / d_t) in column d.
+// The backward substitution L^T x = z (unit diagonal) runs in CTA 0, blocked by 32 rows, same
+// order as the oracle's.
 constexpr int kCholNB = 32;
 constexpr int kCholSlab = 8;                          // panel columns per CTA kept in shared memory
 constexpr int kCoopThreads = 256;
@@ -1418,6 +1481,65 @@ __device__ __forceinline__ double rcp_rn_int(double r)
     if (2 * Rm > (long long)M) ++Q;
     else if (2 * Rm < -(long long)M) --Q;
     return __longlong_as_double((long long)(((unsigned long long)(2045u - E) << 52) + (Q - (1ull << 52))));
+}
+
+// r = RN(sqrt(a)) and inv = RN(1 / r) together, as the Cholesky's pivot needs them.  The square root
+// runs as in sqrt_rn_int.  The reciprocal's float-float estimate Q0 ~ 2^105 / T1 is formed from the
+// square root's first Newton value T1 (within 53 of the root S), independently of the square root's
+// second step, so only its exact integer correction waits for S: Q0 is within 361 of 2^105 / T1 and
+// 2^105 / T1 within 2 |T1 - S| + 1 of 2^105 / S, so the residual 2^105 - S Q0 stays below 2^62 and
+// one correction step lands within 1/2 (the FP32 reciprocal of T1 differs from that of S by
+// 2^-46 relative); the remainder test then rounds as in rcp_rn_int.  S = 2^53 (the root rounds up
+// to the next power of two) gives r and 1 / r as exact powers of two.
+__device__ __forceinline__ double sqrt_rcp_rn_int(double a, double& inv)
+{
+    const unsigned long long ia = (unsigned long long)__double_as_longlong(a);
+    const unsigned E = (unsigned)(ia >> 52);
+    if (E - 1u >= 2046u) {                                         // zero, negative, subnormal, inf, nan
+        const double r = sqrt(a);
+        inv = rcp_rn_int(r);
+        return r;
+    }
+    const int odd = (E & 1u) == 0u;
+    const unsigned long long M = ((ia & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << odd;
+    const int eh = ((int)E - 1023 - odd) / 2;
+    const float fm = __fmul_rn(__uint2float_rn((unsigned)(M >> 22)), 4194304.0f);
+    const unsigned ri = __float2uint_rn(__fsqrt_rn(fm));
+    const long long D0 = (long long)(M - (unsigned long long)ri * ri);
+    const float d1 = __fdiv_rn(__fmul_rn(__int2float_rn((int)(D0 >> 3)), 268435456.0f), __uint2float_rn(ri));
+    unsigned long long T = ((unsigned long long)ri << 26) + (unsigned long long)(long long)__float2int_rn(d1);
+    // reciprocal estimate from T1 (= T here), clamped to [2^52, 2^53) so that mh is exact and
+    // y0 2^76 an integer; the clamp moves it no further from S < 2^53
+    const unsigned long long T1 = min(max(T, 1ull << 52), (1ull << 53) - 1ull);
+    const float mh = __fmul_rn(__uint2float_rn((unsigned)(T1 >> 29)), 536870912.0f);
+    const float ml = __uint2float_rn((unsigned)(T1 & 0x1FFFFFFFull));
+    const float y0 = __frcp_rn(mh);
+    const float e = __fsub_rn(fmaf(-mh, y0, 1.0f), __fmul_rn(ml, y0));
+    unsigned long long Q = ((unsigned long long)__float2uint_rn(__fmul_rn(y0, 0x1p76f)) << 29) +
+                           (unsigned long long)(long long)__float2int_rn(__fmul_rn(__fmul_rn(y0, e), 0x1p105f));
+    // square root, second step and rounding
+    const unsigned long long Nlo = M << 52;
+    long long Rm = (long long)(Nlo - T * T);
+    const float rf = __fmul_rn(__int2float_rn((int)(Rm >> 32)), 4294967296.0f);
+    const float tf = __fmul_rn(__uint2float_rn((unsigned)(T >> 29)), 536870912.0f);
+    T += (unsigned long long)(long long)__float2int_rn(__fdiv_rn(rf, __fmul_rn(tf, 2.0f)));
+    Rm = (long long)(Nlo - T * T);
+    if (Rm > (long long)T) ++T;
+    else if (Rm <= -(long long)T) --T;
+    const double r = __longlong_as_double((long long)(((unsigned long long)(eh + 1023) << 52) + (T - (1ull << 52))));
+    if (T == (1ull << 53)) {                                       // r = 2^(eh + 1)
+        inv = __longlong_as_double((long long)((unsigned long long)(1022 - eh) << 52));
+        return r;
+    }
+    // reciprocal of r = T 2^(eh - 52): Q = RN(2^105 / T), 1 / r = Q 2^(-53 - eh)
+    long long Rq = (long long)(0ull - T * Q);
+    Q += (unsigned long long)(long long)__float2int_rn(
+        __fmul_rn(__fmul_rn(__int2float_rn((int)(Rq >> 32)), 4294967296.0f), y0));
+    Rq = (long long)(0ull - T * Q);
+    if (2 * Rq > (long long)T) ++Q;
+    else if (2 * Rq < -(long long)T) --Q;
+    inv = __longlong_as_double((long long)(((unsigned long long)(1022 - eh) << 52) + (Q - (1ull << 52))));
+    return r;
 }
 
 // Bounded grid barrier of n cooperating CTAs on three words: bar[0] counts arrivals since the
@@ -1508,6 +1630,7 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     const int D = d + 1;                       // augmented by the right-hand side
     const int UA = D * (D + 1) / 2;
     double* A = P.work;                        // [UA]
+    double* W = P.work + UA;                   // [kCholNB][D]: the panel's unscaled rows
     if (P.ls && bid == 0 && threadIdx.x == 0) P.ls[4] = 0.0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int gtid = bid * blockDim.x + tid, gthreads = G * blockDim.x;
@@ -1550,20 +1673,57 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
         }
         if (tid == 0) s_fail = 0;
         __syncthreads();
-        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Db and Sb
-        // hold the working entries, Rb and SR the finished rows of R.  Warp 0 runs only the pivot
-        // chain: at step k it forms r_{k,k+1} = a_{k,k+1} (1 / r_kk), applies step k to the next
-        // diagonal entry itself and takes its square root and reciprocal.  Meanwhile six other
-        // warps scale row k (into Rb / SR) and apply step k to every other entry below row k.
-        // Warp 4 stays idle: it shares warp 0's SM sub-partition, whose FP64 pipe the chain needs.
+        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Warp 0
+        // runs only the pivot chain: at step k it forms l_{k,k+1} = a_{k,k+1} (1 / d_k), applies
+        // step k to the next diagonal entry itself and takes its reciprocal.  Six other warps scale
+        // row k (into Rb / SR) and apply step k to every other entry below row k.  Each of their
+        // threads owns fixed entries for the whole panel and keeps them in registers: block entries
+        // e = ut + 192 q of the descending-row list (rows 1..nb-1) and slab entries (row
+        // nb-1 - e / ns, slab column e mod ns) likewise, so the entries still active at step k
+        // (row > k) fill the lowest slots of consecutive threads.  An entry is written to Db / Sb
+        // when its row becomes the next pivot row (the diagonal entry one step earlier, for the
+        // chain).  Warp 4 stays idle: it shares warp 0's SM sub-partition, whose FP64 pipe the
+        // chain needs.
+        constexpr int kSlotsB = (kCholNB * (kCholNB - 1) / 2 + kCoopThreads - 65) / (kCoopThreads - 64);
+        constexpr int kSlotsS = ((kCholNB - 1) * kCholSlab + kCoopThreads - 65) / (kCoopThreads - 64);
+        const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;    // 0..191 for the update warps
+        double vb[kSlotsB], vs[kSlotsS];
+        int ib[kSlotsB], jb[kSlotsB], is_[kSlotsS], ss[kSlotsS];
+        if (warp != 0 && warp != 4) {
+            const int nbe = nb * (nb - 1) / 2;     // block entries below row 0
+#pragma unroll
+            for (int q = 0; q < kSlotsB; ++q) {
+                const int e = ut + q * (kCoopThreads - 64);
+                ib[q] = -1;
+                jb[q] = 0;
+                vb[q] = 0.0;
+                if (e < nbe) {
+                    const unsigned v = s_ent[e];
+                    ib[q] = (int)(v >> 8);
+                    jb[q] = (int)(v & 0xffu);
+                    vb[q] = Db[ib[q]][jb[q]];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kSlotsS; ++q) {
+                const int e = ut + q * (kCoopThreads - 64);
+                is_[q] = -1;
+                ss[q] = 0;
+                vs[q] = 0.0;
+                if (ns > 0 && e < (nb - 1) * ns) {
+                    is_[q] = nb - 1 - e / ns;
+                    ss[q] = e - (e / ns) * ns;
+                    vs[q] = Sb[is_[q]][ss[q]];
+                }
+            }
+        }
         double inv_k = 0.0;
         if (warp == 0) {
             const double a0 = Db[0][0];
             const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-            const double r = sqrt_rn_int(a0);
-            inv_k = rcp_rn_int(r);
+            inv_k = rcp_rn_int(a0);
             if (lane == 0) {
-                Rb[0][0] = r;
+                Rb[0][0] = a0;
                 s_inv[0] = inv_k;
                 if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;   // a < 0 (not NaN, not -0)
             }
@@ -1573,42 +1733,36 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             if (s_fail) break;
             if (warp == 0) {
                 if (k + 1 < nb) {
-                    const double rk = __dmul_rn(Db[k][k + 1], inv_k);
-                    const double a0 = fma(-rk, rk, Db[k + 1][k + 1]);
+                    const double w = Db[k][k + 1];
+                    const double a0 = fma(-__dmul_rn(w, inv_k), w, Db[k + 1][k + 1]);
                     const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-                    const double r = sqrt_rn_int(a0);
-                    inv_k = rcp_rn_int(r);
+                    inv_k = rcp_rn_int(a0);
                     if (lane == 0) {
-                        Rb[k + 1][k + 1] = r;
+                        Rb[k + 1][k + 1] = a0;
                         s_inv[k + 1] = inv_k;
                         if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;
                     }
                 }
             } else if (warp != 4) {
-                const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;    // 0..191
                 const double inv = s_inv[k];
-                const int nd = nb - 1 - k;
-                for (int it = ut; it < nd + ns; it += kCoopThreads - 64) {
-                    if (it < nd) Rb[k][k + 1 + it] = __dmul_rn(Db[k][k + 1 + it], inv);
-                    else SR[k][it - nd] = __dmul_rn(Sb[k][it - nd], inv);
-                }
+                const int nd = nb - 1 - k;                 // rows k+1 .. nb-1
+                if (ut < nd) Rb[k][k + 1 + ut] = __dmul_rn(Db[k][k + 1 + ut], inv);
+                else if (ut < nd + ns) SR[k][ut - nd] = __dmul_rn(Sb[k][ut - nd], inv);
                 asm volatile("bar.sync 1, 192;" ::: "memory");
-                const int rows = nb - 1 - k;               // rows k+1 .. nb-1
-                if (rows > 0) {
-                    const int nblk = rows * (rows + 1) / 2;
-                    const int skip = nblk - rows;          // entry (k+1, k+1): the pivot chain's own
-                    const int nall = nblk + rows * ns;
-                    for (int e = ut; e < nall; e += kCoopThreads - 64) {
-                        if (e < nblk) {
-                            if (e == skip) continue;
-                            const unsigned v = s_ent[e];
-                            const int i = (int)(v >> 8), j = (int)(v & 0xffu);
-                            Db[i][j] = fma(-Rb[k][i], Rb[k][j], Db[i][j]);
-                        } else {
-                            const int q = e - nblk;
-                            const int i = k + 1 + q / ns, sl = q - (q / ns) * ns;
-                            Sb[i][sl] = fma(-Rb[k][i], SR[k][sl], Sb[i][sl]);
-                        }
+#pragma unroll
+                for (int q = 0; q < kSlotsB; ++q) {
+                    const int i = ib[q], j = jb[q];
+                    if (i > k && !(j == k + 1)) {          // (k+1, k+1) is the chain's
+                        vb[q] = fma(-Rb[k][i], Db[k][j], vb[q]);
+                        if (i == k + 1 || (i == j && i == k + 2)) Db[i][j] = vb[q];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kSlotsS; ++q) {
+                    const int i = is_[q];
+                    if (i > k) {
+                        vs[q] = fma(-Rb[k][i], Sb[k][ss[q]], vs[q]);
+                        if (i == k + 1) Sb[i][ss[q]] = vs[q];
                     }
                 }
             }
@@ -1630,7 +1784,9 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
         }
         for (int t = tid; t < nb * ns; t += blockDim.x) {
             const int i = t % nb, sl = t / nb;
-            A[up_pos(c0 + i, c1 + (int)bid + sl * (int)G)] = SR[i][sl];
+            const int j = c1 + (int)bid + sl * (int)G;
+            A[up_pos(c0 + i, j)] = SR[i][sl];
+            W[(size_t)i * D + j] = Sb[i][sl];
         }
         // panel columns beyond the slab (very large d only): one column per warp, same steps
         {
@@ -1639,9 +1795,12 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 const int j = c1 + (int)bid + sl * (int)G;
                 double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
                 for (int k = 0; k < nb; ++k) {
-                    if (lane == k) a = __dmul_rn(a, s_inv[k]);
-                    double r = __shfl_sync(0xffffffffu, a, k);
-                    if (lane > k && lane < nb) a = fma(-Rb[k][lane], r, a);
+                    const double w = __shfl_sync(0xffffffffu, a, k);     // a_kj, final and unscaled
+                    if (lane == k) {
+                        W[(size_t)k * D + j] = w;
+                        a = __dmul_rn(a, s_inv[k]);
+                    }
+                    if (lane > k && lane < nb) a = fma(-Rb[k][lane], w, a);
                 }
                 if (lane < nb) A[up_pos(c0 + lane, j)] = a;
             }
@@ -1657,14 +1816,14 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 upper_ij(e, ii, jj);
                 const int i = c1 + ii, j = c1 + jj;
                 const double* ci = A + up_pos(0, i);
-                const double* cj = A + up_pos(0, j);
-                double u[kCholNB], w[kCholNB];     // panel rows of columns i and j, loaded ahead
+                const double* wj = W + j;
+                double u[kCholNB], w[kCholNB];     // multipliers l_ki, unscaled a_kj, loaded ahead
 #pragma unroll
                 for (int k = 0; k < kCholNB; ++k) {
                     u[k] = k < nb ? ci[c0 + k] : 0.0;
-                    w[k] = k < nb ? cj[c0 + k] : 0.0;
+                    w[k] = k < nb ? wj[(size_t)k * D] : 0.0;
                 }
-                double a = cj[i];
+                double a = A[up_pos(i, j)];
 #pragma unroll
                 for (int k = 0; k < kCholNB; ++k)
                     if (k < nb) a = fma(-u[k], w[k], a);
@@ -1676,7 +1835,7 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     if (!gs.sync()) goto timeout;
     if (bid != 0) return;
     {
-        // R dx = y (y in column d), blocked by 32 rows (CTA 0)
+        // L^T dx = z (z in column d), blocked by 32 rows (CTA 0)
         double* y = P.ybuf;
         double gs = 0.0;
         for (int i = tid; i < d; i += blockDim.x) {
@@ -1711,11 +1870,9 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 double ar[32];
 #pragma unroll
                 for (int s = 0; s < 32; ++s) ar[s] = (lane < s && s < nbk) ? A[up_pos(b0 + lane, b0 + s)] : 0.0;
-                const double myinv = (lane < nbk) ? P.rinv[b0 + lane] : 0.0;
 #pragma unroll
                 for (int s = 31; s >= 0; --s) {
                     if (s < nbk) {
-                        if (lane == s) v = __dmul_rn(v, myinv);
                         const double yt = __shfl_sync(0xffffffffu, v, s);
                         if (lane < s) v = fma(-ar[s], yt, v);
                     }

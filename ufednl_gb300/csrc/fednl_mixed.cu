@@ -434,7 +434,7 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
     rc |= h->alloc(&P.stats, 4);
     rc |= h->alloc(&h->err, 1);
     rc |= h->alloc(&h->dx, h->d);
-    rc |= h->alloc(&h->work, (size_t)(h->d + 1) * (h->d + 2) / 2);
+    rc |= h->alloc(&h->work, fednl_chol_work_elems(h->d));
     rc |= h->alloc(&h->ybuf, h->d);
     rc |= h->alloc(&h->rinv, h->d);
     rc |= h->alloc(&h->hist, h->hist_cap);

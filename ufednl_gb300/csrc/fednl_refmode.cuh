@@ -458,9 +458,10 @@ __global__ void __launch_bounds__(kRefCholThreads) k_chol_ref(Dev P, const doubl
                     const double sq = __dadd_rn(refo::lanes8(c8), acc[8 * Ua + apos(k, k)]);
                     const double a = __dsub_rn(__dadd_rn(Hin[up_pos(k, k)], l), sq);
                     s_bad = (a < 0.0) ? 1 : 0;
-                    const double r = sqrt_rn_int(a);
+                    double inv;
+                    const double r = sqrt_rcp_rn_int(a, inv);
                     s_r = r;
-                    s_inv = rcp_rn_int(r);
+                    s_inv = inv;
                     R[apos(k, k)] = r;
                 }
                 __syncthreads();

@@ -7,6 +7,11 @@
 
 #include <functional>
 
+// elements of the FP64 cooperative solve's work array: the packed factor of the system augmented by
+// the right-hand side as column d, then the current panel's unscaled rows (32 x (d + 1)) that the
+// trailing update of the LDL^T factorization reads
+inline size_t fednl_chol_work_elems(int d) { return (size_t)(d + 1) * (d + 2) / 2 + (size_t)32 * (d + 1); }
+
 struct FednlSolveDesc {
     const double* H;       // packed upper FP64, d(d+1)/2
     int d;
@@ -15,7 +20,7 @@ struct FednlSolveDesc {
     const double* g;       // device right-hand side
     double* dx;            // device solution
     double* xupd;          // device iterate (x -= dx) or nullptr
-    double* work;          // (d+1)(d+2)/2
+    double* work;          // fednl_chol_work_elems(d)
     double* ybuf;          // d
     double* rinv;          // d
     unsigned* bar;         // 4 x u32
