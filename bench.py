@@ -143,16 +143,21 @@ def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
 
 def hess_fp64_ops(prob) -> float:
     """FP64 operations of one k_hess_binary launch: for every client and upper entry (i, j) one add
-    per sample with both attributes set (the in-order sum of D_s), then the difference, its square
-    and the add into the entry's norm accumulator (3 more)."""
+    per sample after the first with both attributes set (the in-order sum of D_s; the first term is
+    exact and costs none), the diagonal's + lambda (the intercept column is the attribute's D_s sum,
+    already formed), then the difference and the fused square-add into the entry's norm
+    accumulator (2 more)."""
     d = prob.d
     U = d * (d + 1) // 2
     tot = 0.0
     for c in range(prob.n_clients):
         a = prob.features[prob.client_slice(c)]
         g = a.T @ a
-        tot += float(np.triu(g).sum())
-    return tot + 3.0 * prob.n_clients * U
+        off = np.triu(g, 1)
+        if a.shape[0] and np.all(a[:, -1] == 1.0):
+            off[:, -1] = 0.0
+        tot += float(np.maximum(off - 1.0, 0.0).sum()) + d
+    return tot + 2.0 * prob.n_clients * U
 
 
 def kernel_roofline(name: str, ms: float, bound: str, work: float, peak: float, unit: str, what: str,
@@ -555,7 +560,7 @@ def run_ours(args, ws, rank, local, td):
     sb, swhat = algorithmic_bytes("k_select", prob, k)
     r_hess_hbm = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "hbm", hb, hbm, "GB/s", hwhat, hsrc)
     r_hess_fp64 = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "fp64", hops, fp64["add_gops"],
-                                  "Gop/s", "in-order D_s sums (one add per sample with both attributes set) "
+                                  "Gop/s", "in-order D_s sums (one add per sample after the first with both attributes set) "
                                   "+ difference, square and norm add per upper entry", fsrc)
     r_select = kernel_roofline("k_select", kernels.get("k_select", 0.0), "hbm", sb, hbm, "GB/s", swhat, hsrc)
     chol_ms = kernels.get("k_chol_coop", 0.0)

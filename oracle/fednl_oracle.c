@@ -511,7 +511,8 @@ double orc_l2sq(const double* v, size_t n)
  * frobeniusNormForSymmetricMatrixFromUpPart over the full buffer, MatrixNMD.h:478-488), in a fixed
  * order that the GB300 kernel follows exactly: upper positions p (column j, rows 0..j) are cut into
  * segments of 512; inside a segment, lane l = p mod 32 accumulates m_p^2 over its 16 positions in
- * order, diagonal entries into a_l and off-diagonal ones into b_l; lane l contributes
+ * order with fused multiply-adds (a_l = fma(m_p, m_p, a_l)), diagonal entries into a_l and
+ * off-diagonal ones into b_l; lane l contributes
  * v_l = a_l + 2 b_l, the 32 lane values are reduced by the halving tree, and the segment sums are
  * added in order. */
 double orc_frob_sym(const double* m, int32_t d, int32_t lda)
@@ -535,11 +536,10 @@ double orc_frob_sym(const double* m, int32_t d, int32_t lda)
                 if (pp >= U)
                     continue;
                 double x = m[(size_t)col[pp] * lda + row[pp]];
-                double t = x * x;
                 if (row[pp] == col[pp])
-                    a = a + t;
+                    a = fma(x, x, a);
                 else
-                    b = b + t;
+                    b = fma(x, x, b);
             }
             v[l] = a + b * 2.0;
         }

@@ -1067,9 +1067,10 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         P.fboff = d_fboff;
         P.fbits = d_fbits;
         int maxW = (h->maxn + 63) / 64;
-        size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8;
+        // attribute masks (when they fit), D_s, and the diagonal values
+        size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8 + (size_t)d * 8;
         h->hess_smem_bits = need <= 200 * 1024;
-        h->hess_smem = h->hess_smem_bits ? need : (size_t)h->maxn * 8;
+        h->hess_smem = h->hess_smem_bits ? need : (size_t)h->maxn * 8 + (size_t)d * 8;
         if (h->hess_smem > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
         if (h->hess_smem_bits)
             CK(fednl_raise_dyn_smem((const void*)k_hess_binary<true>, h->hess_smem));

@@ -397,8 +397,8 @@ constexpr int kHessThreads = 256;
 constexpr int kHessPerBlock = 4096;     // upper entries per block
 
 // Fixed-order ||diff||_F^2 (the CPU oracle's orc_frob_sym): each warp owns one segment of 512
-// upper positions; lane l accumulates its 16 terms, diagonal (a) and off-diagonal (b) apart, then
-// contributes a + 2 b to the segment's halving tree.
+// upper positions; lane l accumulates its 16 squares with fused multiply-adds, diagonal (a) and
+// off-diagonal (b) apart, then contributes a + 2 b to the segment's halving tree.
 __device__ __forceinline__ double segment_value(double a, double b) { return __dadd_rn(a, __dmul_rn(b, 2.0)); }
 
 // F_c = ||diff_c||_F^2 as the in-order sum of the client's segment sums, and Lk = sqrt(F_c)
@@ -452,45 +452,65 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
         fb = gfb;
     }
     for (int t = threadIdx.x; t < n; t += blockDim.x) s_D[t] = P.Dv[off + t];
+    // the diagonal entries sum_s D_s a_si + lambda, formed once per block: in the entry loop a
+    // diagonal lane would cost its warp a whole FP64 instruction
+    double* s_dl = s_D + n;
+    const double* dsum = P.dsum + (size_t)c * P.d;
+    for (int t = threadIdx.x; t < P.d; t += blockDim.x) s_dl[t] = __dadd_rn(dsum[t], P.lambda);
     __syncthreads();
 
     const size_t base = (size_t)c * P.ustr;
-    const double* dsum = P.dsum + (size_t)c * P.d;
     const bool icpt = P.icpt[c] != 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int seg = blockIdx.x * (kHessThreads / 32) + warp;     // 512 positions per warp
     const int p_seg = seg * 512;
     double fa = 0.0, fb2 = 0.0;
+    int i, j;
+    upper_ij(p_seg + lane, i, j);
     for (int q = 0; q < 16; ++q) {
         const int p = p_seg + 32 * q + lane;
         if (p >= P.U) break;
-        int i, j;
-        upper_ij(p, i, j);
+        if (q > 0) {                   // advance (i, j) by 32 packed positions
+            i += 32;
+            while (i > j) {
+                i -= j + 1;
+                ++j;
+            }
+        }
         double h;
         if (i == j) {
-            h = __dadd_rn(dsum[i], P.lambda);
+            h = s_dl[i];
         } else if (icpt && j == P.d - 1) {
             h = dsum[i];               // samples with attribute i set, all of which have the intercept
         } else {
             const unsigned long long* mi = fb + (size_t)i * W;
             const unsigned long long* mj = fb + (size_t)j * W;
-            // the in-order sum's first term is 0 + D_s = D_s exactly (D_s >= 0), so it costs no FP64
-            // add: on this part a warp's FP64 instruction takes the pipe for ~64 cycles however few
-            // lanes are active, and most entries have at most one sample with both attributes set
+            // Per 32 mask words: pass 1, without branches, finds the words holding samples with
+            // both attributes set; pass 2 sums over those words only, in sample order.  The sum's
+            // first term is 0 + D_s = D_s exactly (D_s >= 0), so it costs no FP64 add: on this part
+            // a warp's FP64 instruction takes the pipe for ~64 cycles however few lanes are active,
+            // and most entries have at most one sample with both attributes set
             h = 0.0;
             bool first = true;
-            for (int w = 0; w < W; ++w) {
-                unsigned long long m = mi[w] & mj[w];
-                if (m && first) {
-                    const int b = __ffsll((long long)m) - 1;
-                    m &= m - 1;
-                    h = s_D[w * 64 + b];
-                    first = false;
-                }
-                while (m) {
-                    const int b = __ffsll((long long)m) - 1;
-                    m &= m - 1;
-                    h = __dadd_rn(h, s_D[w * 64 + b]);
+            for (int w0 = 0; w0 < W; w0 += 32) {
+                const int w1 = min(W, w0 + 32);
+                unsigned nz = 0u;
+                for (int w = w0; w < w1; ++w) nz |= (unsigned)((mi[w] & mj[w]) != 0ull) << (w - w0);
+                while (nz) {
+                    const int w = w0 + __ffs(nz) - 1;
+                    nz &= nz - 1u;
+                    unsigned long long m = mi[w] & mj[w];
+                    if (first) {
+                        const int b = __ffsll((long long)m) - 1;
+                        m &= m - 1;
+                        h = s_D[w * 64 + b];
+                        first = false;
+                    }
+                    while (m) {
+                        const int b = __ffsll((long long)m) - 1;
+                        m &= m - 1;
+                        h = __dadd_rn(h, s_D[w * 64 + b]);
+                    }
                 }
             }
         }
@@ -500,9 +520,9 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
             if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
-            const double t = __dmul_rn(df, df);
-            if (i == j) fa = __dadd_rn(fa, t);
-            else fb2 = __dadd_rn(fb2, t);
+            const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
+            if (i == j) fa = r;
+            else fb2 = r;
         }
     }
     if (mode != 1 && p_seg < P.U) {
@@ -542,9 +562,9 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
             if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
-            const double t = __dmul_rn(df, df);
-            if (i == j) fa = __dadd_rn(fa, t);
-            else fb2 = __dadd_rn(fb2, t);
+            const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
+            if (i == j) fa = r;
+            else fb2 = r;
         }
     }
     if (mode != 1 && p_seg < P.U) {
@@ -2375,9 +2395,10 @@ __global__ void __launch_bounds__(kHessThreads) k_pp_lkpart(Dev P)
         const int p = p_seg + 32 * q + lane;
         if (p >= P.U) break;
         const double df = __dsub_rn(P.shift[base + p], P.hbuf[base + p]);
-        const double t = __dmul_rn(df, df);
-        if (upper_is_diag(p)) fa = __dadd_rn(fa, t);
-        else fb2 = __dadd_rn(fb2, t);
+        const bool dg = upper_is_diag(p);
+        const double r = fma(df, df, dg ? fa : fb2);
+        if (dg) fa = r;
+        else fb2 = r;
     }
     if (p_seg < P.U) {
         const double cs = chunk_tree(segment_value(fa, fb2));
