@@ -505,6 +505,7 @@ struct fednl_handle_s {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;       // the round graph's second branch (k_aggregate)
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    unsigned* drawctr = nullptr;       // [1] k_select's finished CTAs (TopLEK draws in the last one)
     Arena state, feat;
     Dev dev{};
     cudaGraph_t graph = nullptr;
@@ -541,6 +542,9 @@ int mark(fednl_handle h, Marks* m, const char* name)
         if (rc_) return rc_;                                                                       \
     } while (0)
 
+// threads of k_client_binary: a lane pair per attribute when that fits one CTA
+int client_threads(int d) { return std::min(1024, std::max(128, (2 * d + 31) / 32 * 32)); }
+
 int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = false)
 {
     Dev& P = h->dev;
@@ -552,20 +556,26 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
             h->nc, h->tau, P.sampler, P.perm, (int*)P.act, P.is_sel, P.needs, h->pp_smem_perm);
         CKL();
     }
-    if (P.ref) {
-        MARK("k_margin_ref");
-        k_margin_ref<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+    if (h->binary && !P.ref) {       // the client oracle in one launch
+        MARK("k_client_binary");
+        k_client_binary<<<h->nc, client_threads(h->d), (size_t)h->maxn * 16, st>>>(P);
+        CKL();
     } else {
-        MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
-        if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
-        else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+        if (P.ref) {
+            MARK("k_margin_ref");
+            k_margin_ref<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+        } else {
+            MARK(h->binary ? "k_margin_binary" : "k_margin_dense");
+            if (h->binary) k_margin_binary<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+            else k_margin_dense<<<(S + 255) / 256, 256, 0, st>>>(P, S);
+        }
+        CKL();
+        MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
+        dim3 gg(h->binary ? (2 * h->d + 127) / 128 : (h->d + 127) / 128, h->nc);   // binary: a lane pair per attribute
+        if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, st>>>(P);
+        else k_grad_dense<<<gg, 128, 0, st>>>(P);
+        CKL();
     }
-    CKL();
-    MARK(h->binary ? "k_grad_binary" : "k_grad_dense");
-    dim3 gg(h->binary ? (2 * h->d + 127) / 128 : (h->d + 127) / 128, h->nc);   // binary: a lane pair per attribute
-    if (h->binary) k_grad_binary<<<gg, 128, (size_t)h->maxn * 16, st>>>(P);
-    else k_grad_dense<<<gg, 128, 0, st>>>(P);
-    CKL();
     const int na = P.n_act;
     if (h->pp) {
         MARK("k_pp_truegrad");
@@ -590,9 +600,12 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_frob_ref<<<na, kFrobRefThreads, (size_t)kFrobRing * h->d * 8, st>>>(P);
         CKL();
     }                             // otherwise the Hessian kernel's last block per client formed F
-    // k_aggregate needs only the gradients and Lk: in a graph it runs on a branch beside the
-    // selection and the shift update (kept in line when the round is profiled kernel by kernel)
-    const bool fork = !M && h->side && !h->pp;
+    int comp = h->comp;
+    // The master's aggregation needs only the gradients and Lk.  With TopK / TopLEK it runs in the
+    // selection kernel's idle warps; otherwise, in a graph, on a branch beside the compressor and the
+    // shift update (kept in line when the round is profiled kernel by kernel)
+    const bool agg_in_select = !h->pp && (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK);
+    const bool fork = !M && h->side && !h->pp && !agg_in_select;
     if (fork) {
         CK(cudaEventRecord(h->fork_ev, st));
         CK(cudaStreamWaitEvent(h->side, h->fork_ev, 0));
@@ -600,20 +613,16 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         CKL();
         CK(cudaEventRecord(h->join_ev, h->side));
     }
-    int comp = h->comp;
     if (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK) {
         MARK("k_select");
         double delta = (double)h->k * (1.0 / (double)h->U);
+        // TopLEK's rounding draws run in the launch's last CTA
+        SelectDraws dr{comp == FEDNL_TOPLEK ? h->drawctr : nullptr, h->nc, h->W, P.wstate, MasterAgg{}};
+        if (agg_in_select) dr.agg = MasterAgg{P.gc, P.lk, P.g, P.stats, h->d, h->nc, P.inv_n};
         k_select<<<na, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
             P.diff, h->ustr, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F, P.sel, h->SW, P.cnt, P.needs, P.pdraw,
-            P.minidx, P.status, P.act, P.ref);
+            P.minidx, P.status, P.act, P.ref, dr);
         CKL();
-        if (comp == FEDNL_TOPLEK) {
-            MARK("k_toplek_rng");
-            k_toplek_rng<<<(h->W + 31) / 32, 32, 0, st>>>(h->nc, h->W, nullptr, P.wstate, P.needs, P.pdraw, P.minidx,
-                                                         P.sel, h->SW, P.cnt);
-            CKL();
-        }
     } else if (comp == FEDNL_RANDK) {
         MARK("k_randk");
         k_randk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.hmap, h->hcap, P.sel, h->SW, P.cnt, P.act);
@@ -649,7 +658,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     }
     if (fork) {
         CK(cudaStreamWaitEvent(st, h->join_ev, 0));
-    } else {
+    } else if (!agg_in_select) {
         MARK("k_aggregate");
         k_aggregate<<<(h->d + kAggThreads - 1) / kAggThreads + 1, kAggThreads, 0, st>>>(P);   // + the block for l
         CKL();
@@ -832,6 +841,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     A.want(&P.dsum, (size_t)h->nc * h->d);
     A.want(&P.F, h->nc);
     A.want(&P.hdone, h->nc);
+    A.want(&h->drawctr, 1);
     A.want(&P.lk, h->nc);
     A.want(&P.sel, (size_t)h->nc * h->SW);
     A.want(&P.cnt, h->nc);
@@ -904,7 +914,7 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
         cudaMemcpy((void*)P.client_of, client_of.data(), (size_t)h->S * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(P.x, 0, h->d * 8) != cudaSuccess || cudaMemset(P.round_ctr, 0, 4) != cudaSuccess ||
         cudaMemset(P.status, 0, 4) != cudaSuccess || cudaMemset(P.bar, 0, 16) != cudaSuccess ||
-        cudaMemset(P.hdone, 0, (size_t)h->nc * 4) != cudaSuccess) {
+        cudaMemset(P.hdone, 0, (size_t)h->nc * 4) != cudaSuccess || cudaMemset(h->drawctr, 0, 4) != cudaSuccess) {
         fednl_gpu_destroy(h);
         return fail(FEDNL_ECUDA, "initial copies failed");
     }
@@ -1076,8 +1086,10 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
             CK(fednl_raise_dyn_smem((const void*)k_hess_binary<true>, h->hess_smem));
         else
             CK(fednl_raise_dyn_smem((const void*)k_hess_binary<false>, h->hess_smem));
-        if ((size_t)h->maxn * 16 > 48 * 1024)
+        if ((size_t)h->maxn * 16 > 48 * 1024) {
             CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
+            CK(fednl_raise_dyn_smem((const void*)k_client_binary, (size_t)h->maxn * 16));
+        }
         h->binary = 1;
     } else {
         double* dA;
@@ -1723,7 +1735,8 @@ int select_common(const double* mats, int n_mat, int d, int lda, int k, bool lek
         CK(fednl_raise_dyn_smem((const void*)k_select, select_smem(k)));
     double delta = (double)k * (1.0 / (double)U);
     k_select<<<n_mat, kSelThreads, k < U ? select_smem(k) : 0, s.st>>>(dpack, (int)ustr, (int)U, k, lek ? 1 : 0, delta,
-                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr, 0);
+                                                                      dF, dsel, SW, dcnt, dneeds, dp, dmi, derr, nullptr, 0,
+                                                                      SelectDraws{nullptr, 0, 0, nullptr, MasterAgg{}});
     CKL();
     if (lek) {
         int W = std::max(1, n_workers);

@@ -370,6 +370,53 @@ __global__ void k_grad_binary(Dev P)
     else P.gc[(size_t)c * P.d + j] = acc;
 }
 
+// ---- 1 + 2 fused for binary features: one CTA per client -----------------------------------
+// The client's margins, sigmoid values and weights (k_margin_binary's operations, one sample per
+// thread), then its gradient and attribute sums (k_grad_binary's, a lane pair per attribute) with
+// the weights already in shared memory: one launch for the client oracle.  blockDim.x is a
+// multiple of 32.
+__global__ void k_client_binary(Dev P)
+{
+    extern __shared__ double s_w[];    // [n] b_s q_s, then [n] D_s
+    const int c = blockIdx.x;
+    const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int s = off + t;
+        double acc = 0.0;
+        for (int u = P.rowptr[s]; u < P.rowptr[s + 1]; ++u) acc = __dadd_rn(acc, P.x[P.colidx[u]]);
+        const double b = P.lab[s];
+        const double m = (b == 1.0) ? acc : -acc;
+        const double sig = fednl_sigmoid(m);
+        const double inv_m = 1.0 / (double)n;
+        const double z1 = __dsub_rn(1.0, sig);
+        const double dv = __dmul_rn(inv_m, __dmul_rn(z1, sig));
+        const double q = __dmul_rn(z1, -inv_m);
+        const double qb = (b == 1.0) ? q : __dmul_rn(-1.0, q);
+        P.Dv[s] = dv;
+        P.qb[s] = qb;
+        if (P.fmode) P.fterm[s] = -fednl_log(sig);
+        s_w[t] = qb;
+        s_w[n + t] = dv;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 2 * P.d; t += blockDim.x) {
+        const int j = t >> 1, which = t & 1;
+        const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
+        const double* wv = s_w + (which ? n : 0);
+        double acc = which ? 0.0 : __dmul_rn(P.x[j], P.lambda);
+        for (int w = 0; w < W; ++w) {
+            unsigned long long m = fb[w];
+            while (m) {
+                const int b = w * 64 + __ffsll((long long)m) - 1;
+                m &= m - 1;
+                acc = __dadd_rn(acc, wv[b]);
+            }
+        }
+        if (which) P.dsum[(size_t)c * P.d + j] = acc;
+        else P.gc[(size_t)c * P.d + j] = acc;
+    }
+}
+
 __global__ void k_grad_dense(Dev P)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -805,6 +852,119 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     }
 }
 
+// Worker w's draws.  FRESH: the flags were written by other CTAs of the same launch (read through
+// L2, selection words and counts updated atomically).
+template <bool FRESH>
+__device__ __forceinline__ void toplek_draws(int w, int n_mat, int W, const int* worker_of, unsigned* wstate,
+                                             const int* needs, const double* pdraw, const int* minidx, unsigned* sel,
+                                             int SW, int* cnt)
+{
+    unsigned st = wstate[w];
+    auto keep = [&](int c, unsigned p) {     // w.p. 1 - p keep the element (insertInMinHeap)
+        if (FRESH) {
+            atomicOr(&sel[(size_t)c * SW + (p >> 5)], 1u << (p & 31));
+            atomicAdd(&cnt[c], 1);
+        } else {
+            sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
+            cnt[c] += 1;
+        }
+    };
+    if (worker_of) {
+        for (int c = 0; c < n_mat; ++c) {
+            int owner = worker_of[c];
+            if (owner != w || !(FRESH ? __ldcg(needs + c) : needs[c])) continue;
+            double u = lcg_real_unit(st);
+            if (u > (FRESH ? __ldcg(pdraw + c) : pdraw[c])) keep(c, (unsigned)(FRESH ? __ldcg(minidx + c) : minidx[c]));
+        }
+    } else {
+        // clients w, w + W, ... in order; their flags loaded eight at a time ahead of the draws
+        for (int c0 = w; c0 < n_mat; c0 += 8 * W) {
+            int nd[8], mi[8];
+            double pd[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = c0 + t * W;
+                nd[t] = c < n_mat ? (FRESH ? __ldcg(needs + c) : needs[c]) : 0;
+                pd[t] = c < n_mat ? (FRESH ? __ldcg(pdraw + c) : pdraw[c]) : 0.0;
+                mi[t] = c < n_mat ? (FRESH ? __ldcg(minidx + c) : minidx[c]) : 0;
+            }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = c0 + t * W;
+                if (c >= n_mat || !nd[t]) continue;
+                double u = lcg_real_unit(st);
+                if (u > pd[t]) keep(c, (unsigned)mi[t]);
+            }
+        }
+    }
+    wstate[w] = st;
+}
+
+// The master's aggregation: g = (1/n) sum_c g_c per coordinate, l = (1/n) sum_c Lk_c, clients in
+// order (TrainLoop.h:1100-1333).
+struct MasterAgg {
+    const double* gc;      // [nc][d]
+    const double* lk;      // [nc]
+    double* g;             // [d]
+    double* stats;         // stats[1] = l
+    int d, nc;
+    double inv_n;
+};
+
+// coordinate j: 32 clients' values loaded ahead of their in-order additions
+__device__ __forceinline__ void master_g(const MasterAgg& A, int j)
+{
+    double g = 0.0;
+    for (int c0 = 0; c0 < A.nc; c0 += 32) {
+        double v[32];
+#pragma unroll
+        for (int t = 0; t < 32; ++t) v[t] = (c0 + t < A.nc) ? A.gc[(size_t)(c0 + t) * A.d + j] : 0.0;
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if (c0 + t < A.nc) g = __dadd_rn(g, v[t]);
+    }
+    A.g[j] = __dmul_rn(g, A.inv_n);
+}
+
+// l by one warp: 32 values loaded at a time, added in client order
+__device__ __forceinline__ void master_l(const MasterAgg& A, int lane)
+{
+    double l = 0.0;
+    for (int c0 = 0; c0 < A.nc; c0 += 32) {
+        const double v = (c0 + lane < A.nc) ? A.lk[c0 + lane] : 0.0;
+        const int cnt = min(32, A.nc - c0);
+        for (int t = 0; t < cnt; ++t) l = __dadd_rn(l, __shfl_sync(0xffffffffu, v, t));
+    }
+    if (lane == 0) A.stats[1] = __dmul_rn(l, A.inv_n);
+}
+
+// Work fused into k_select.  TopLEK's rounding draws: the launch's last CTA to finish (counted on
+// ctr, which it returns to zero) makes every worker's draws (k_toplek_rng's work) once all clients'
+// window flags are written; ctr == nullptr: no draws in this launch.  The master's aggregation
+// (agg.gc != nullptr): CTA 0's three other warps form l and g while its first warp walks the heap.
+struct SelectDraws {
+    unsigned* ctr;
+    int n_mat, W;
+    unsigned* wstate;
+    MasterAgg agg;
+};
+
+__device__ __forceinline__ void select_finish(const SelectDraws& dr, const int* needs, const double* pdraw,
+                                              const int* minidx, unsigned* sel, int SW, int* cnt)
+{
+    if (!dr.ctr) return;
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(dr.ctr, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int w = threadIdx.x; w < dr.W; w += blockDim.x)
+        toplek_draws<true>(w, dr.n_mat, dr.W, nullptr, dr.wstate, needs, pdraw, minidx, sel, SW, cnt);
+    if (threadIdx.x == 0) *dr.ctr = 0u;
+}
+
 // vals: [n_mat][ustr] packed upper values (signed), rows 16-byte aligned (ustr even); F: [n_mat]
 // squared Frobenius norms.  Output: sel bitmap per matrix, cnt (entries kept before the rounding
 // draw), TopLEK draw request.  err: set to 1 if a bounded wait ran out.
@@ -812,7 +972,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
                                                         int lek, double delta, const double* __restrict__ F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
                                                         double* pdraw, int* minidx, int* err, const int* act,
-                                                        int ref)
+                                                        int ref, SelectDraws dr)
 {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     __shared__ __align__(8) unsigned long long s_bar[2];
@@ -833,6 +993,12 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
             cnt[c] = U;
             if (needs) needs[c] = 0;
         }
+        if (dr.agg.gc && blockIdx.x == 0 && warp != 0) {
+            if (warp == 1) master_l(dr.agg, lane);
+            else
+                for (int j = tid - 64; j < dr.agg.d; j += blockDim.x - 64) master_g(dr.agg, j);
+        }
+        select_finish(dr, needs, pdraw, minidx, sel, SW, cnt);
         return;
     }
     double* stage = (double*)s_dyn;                                          // [2][kSelStage]
@@ -877,7 +1043,13 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
         }
     }
     // scan, SpecialMathRoutinesForMatrix.h:300-318
-    if (warp == 0) {
+    if (warp != 0) {
+        if (dr.agg.gc && blockIdx.x == 0) {      // the master's aggregation beside the heap walk
+            if (warp == 1) master_l(dr.agg, lane);
+            else
+                for (int j = tid - 64; j < dr.agg.d; j += blockDim.x - 64) master_g(dr.agg, j);
+        }
+    } else {
         unsigned long long root = h.key[0];
         // levels 0 and 1 of the heap live in registers during the scan (k >= 21), the same in every
         // lane: the warp replaces the root in step, without a divergent branch or a broadcast
@@ -956,6 +1128,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
             cnt[c] = 0;
             if (needs) needs[c] = 0;
         }
+        select_finish(dr, needs, pdraw, minidx, sel, SW, cnt);
         return;
     }
     int keep = k;
@@ -1153,6 +1326,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
         atomicOr(&sc[p >> 5], 1u << (p & 31));
     }
     if (tid == 0) cnt[c] = keep;
+    select_finish(dr, needs, pdraw, minidx, sel, SW, cnt);
 }
 
 // TopLEK rounding draws: each reference worker w owns one thread_local RandomGenRealLinear
@@ -1163,44 +1337,7 @@ __global__ void k_toplek_rng(int n_mat, int W, const int* worker_of, unsigned* w
 {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
-    unsigned st = wstate[w];
-    if (worker_of) {
-        for (int c = 0; c < n_mat; ++c) {
-            int owner = worker_of[c];
-            if (owner != w || !needs[c]) continue;
-            double u = lcg_real_unit(st);
-            if (u > pdraw[c]) {     // w.p. 1 - p keep the element (insertInMinHeap)
-                unsigned p = (unsigned)minidx[c];
-                sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
-                cnt[c] += 1;
-            }
-        }
-    } else {
-        // clients w, w + W, ... in order; their flags loaded eight at a time ahead of the draws
-        for (int c0 = w; c0 < n_mat; c0 += 8 * W) {
-            int nd[8], mi[8];
-            double pd[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int c = c0 + t * W;
-                nd[t] = c < n_mat ? needs[c] : 0;
-                pd[t] = c < n_mat ? pdraw[c] : 0.0;
-                mi[t] = c < n_mat ? minidx[c] : 0;
-            }
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int c = c0 + t * W;
-                if (c >= n_mat || !nd[t]) continue;
-                double u = lcg_real_unit(st);
-                if (u > pd[t]) {
-                    unsigned p = (unsigned)mi[t];
-                    sel[(size_t)c * SW + (p >> 5)] |= 1u << (p & 31);
-                    cnt[c] += 1;
-                }
-            }
-        }
-    }
-    wstate[w] = st;
+    toplek_draws<false>(w, n_mat, W, worker_of, wstate, needs, pdraw, minidx, sel, SW, cnt);
 }
 
 // ---- 5. RandK / RandSeqK ---------------------------------------------------------------------
@@ -1376,33 +1513,15 @@ __global__ void __launch_bounds__(128) k_apply(Dev P)
 
 // ---- 7. master: g = (1/n) sum_c g_c, l = (1/n) sum_c Lk_c (TrainLoop.h:1100-1333) ------------
 // One thread per coordinate (32-thread blocks spread over SMs); clients added in order, loads
-// issued in batches of 32 ahead of the dependent additions.  The last block forms l.
+// issued in batches of 32 ahead of the dependent additions.  The last block forms l.  In the FP64
+// TopK / TopLEK round the same work runs in k_select's idle warps (MasterAgg).
 constexpr int kAggThreads = 32;
 __global__ void __launch_bounds__(kAggThreads) k_aggregate(Dev P)
 {
+    const MasterAgg A{P.gc, P.lk, P.g, P.stats, P.d, P.nc, P.inv_n};
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < P.d) {
-        double g = 0.0;
-        for (int c0 = 0; c0 < P.nc; c0 += 32) {
-            double v[32];
-#pragma unroll
-            for (int t = 0; t < 32; ++t) v[t] = (c0 + t < P.nc) ? P.gc[(size_t)(c0 + t) * P.d + j] : 0.0;
-#pragma unroll
-            for (int t = 0; t < 32; ++t)
-                if (c0 + t < P.nc) g = __dadd_rn(g, v[t]);
-        }
-        P.g[j] = __dmul_rn(g, P.inv_n);
-    }
-    if (blockIdx.x == gridDim.x - 1) {     // l on a block of its own, the last
-        const int lane = threadIdx.x & 31;
-        double l = 0.0;
-        for (int c0 = 0; c0 < P.nc; c0 += 32) {
-            const double v = (c0 + lane < P.nc) ? P.lk[c0 + lane] : 0.0;
-            const int cnt = min(32, P.nc - c0);
-            for (int t = 0; t < cnt; ++t) l = __dadd_rn(l, __shfl_sync(0xffffffffu, v, t));
-        }
-        if (lane == 0) P.stats[1] = __dmul_rn(l, P.inv_n);
-    }
+    if (j < P.d) master_g(A, j);
+    if (blockIdx.x == gridDim.x - 1) master_l(A, threadIdx.x & 31);     // l on a block of its own, the last
 }
 
 // ---- 8. Option-B solve: Cholesky of H + l I, two triangular solves, x -= dx ------------------
