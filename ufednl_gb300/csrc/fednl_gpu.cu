@@ -119,7 +119,7 @@ int chol_grid(int d)
 }
 
 cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* Hin, int hin_lda, const double* lptr,
-                        double lval, const double* gin, double* dxout, double* xupd, int record)
+                        double lval, const double* gin, double* dxout, double* xupd, int record, int apply_first = 0)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -131,7 +131,7 @@ cudaError_t launch_chol(const Dev& P, int grid, cudaStream_t st, const double* H
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record);
+    return cudaLaunchKernelEx(&cfg, k_chol_coop, P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, apply_first);
 }
 
 // the reference-order solve of the master's system (k_chol_ref, one cooperative launch)
@@ -637,9 +637,14 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_randseqk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt, P.act);
         CKL();
     }
-    MARK("k_apply");
-    k_apply<<<(h->U + 127) / 128, 128, 0, st>>>(P);
-    CKL();
+    // the master merge runs in the solve's first phase (FP64 order, not FedNL-PP, not when the
+    // solve is left to a batched launch)
+    const bool apply_in_solve = !h->pp && !P.ref && !client_phase_only;
+    if (!apply_in_solve) {
+        MARK("k_apply");
+        k_apply<<<(h->U + 127) / 128, 128, 0, st>>>(P);
+        CKL();
+    }
     if (h->pp) {
         MARK("k_pp_lkpart");
         k_pp_lkpart<<<dim3(h->nfpart, na), kHessThreads, 0, st>>>(P);
@@ -682,7 +687,8 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         CK(launch_chol_ref(P, h->ref_grid, st, lptr, P.lambda, P.dx, D.line_search ? nullptr : P.x, 1));
     } else {
         MARK("k_chol_coop");
-        CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1));
+        CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1,
+                       apply_in_solve ? 1 : 0));
     }
     if (D.line_search) {
         MARK("k_ls_init");

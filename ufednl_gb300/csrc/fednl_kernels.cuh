@@ -1455,21 +1455,30 @@ __global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq,
 // whole symmetric difference).  Master: H[idx] += item * preScale in client order
 // (TrainLoop.h:1126-1276 with forcesequpdate).  One thread per upper position, looping over the
 // clients in order, so H receives exactly the reference's sequence of additions.
-__global__ void __launch_bounds__(128) k_apply(Dev P)
+// Position p = 32 word + lane of one selection word, called by the 32 lanes of a converged warp
+// (lanes past U take part in the shuffles only).  Per batch of 32 clients, lane t loads client t's
+// word; 32 shuffles turn the words into each position's mask of selecting clients, the loads of
+// all of them are issued together, and the FP64 updates follow in client order (the same
+// operations as one position at a time).  Updates the selecting clients' shifts; returns the new
+// H[p].
+__device__ __forceinline__ double apply_word(const Dev& P, int p, int lane)
 {
-    // A warp covers the 32 positions of one selection word.  Per batch of 32 clients, lane t loads
-    // client t's word; 32 shuffles turn the words into each position's mask of selecting clients,
-    // the loads of all of them are issued together, and the FP64 updates follow in client order (the same operations as one position at a time; a warp no longer walks every client that
-    // any of its lanes selected with a load in each step).
-    const int p = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
     const bool in = p < P.U;
-    const int word = p >> 5;                      // the same for the whole warp (blockDim % 32 == 0)
+    const int word = p >> 5;                      // the same for the whole warp
     const bool all = (P.comp == 0 || P.comp == 5);
     double h = in ? P.H[p] : 0.0;
+    // each batch's client ids and selection words are loaded one batch ahead
+    auto client_of_lane = [&](int c0) { return (c0 + lane < P.n_act) ? (P.act ? P.act[c0 + lane] : c0 + lane) : -1; };
+    auto word_of = [&](int cl) { return cl < 0 ? 0u : (all ? 0xffffffffu : P.sel[(size_t)cl * P.SW + word]); };
+    int cl_next = client_of_lane(0);
+    unsigned wv_next = word_of(cl_next);
     for (int c0 = 0; c0 < P.n_act; c0 += 32) {
-        const bool has = c0 + lane < P.n_act;
-        const int cl = has ? (P.act ? P.act[c0 + lane] : c0 + lane) : 0;
-        const unsigned wv = has ? (all ? 0xffffffffu : P.sel[(size_t)cl * P.SW + word]) : 0u;
+        const int cl = cl_next < 0 ? 0 : cl_next;
+        const unsigned wv = wv_next;
+        if (c0 + 32 < P.n_act) {
+            cl_next = client_of_lane(c0 + 32);
+            wv_next = word_of(cl_next);
+        }
         unsigned mine = 0u;                       // bit t: client c0 + t selected my position
 #pragma unroll
         for (int t = 0; t < 32; ++t) {
@@ -1508,7 +1517,16 @@ __global__ void __launch_bounds__(128) k_apply(Dev P)
                 }
         }
     }
-    if (in) P.H[p] = h;
+    return h;
+}
+
+// A warp covers the 32 positions of one selection word.  In the FP64 round the same work runs in
+// the Option-B solve's first phase (chol_body, apply_first).
+__global__ void __launch_bounds__(128) k_apply(Dev P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const double h = apply_word(P, p, lane);      // blockDim % 32 == 0: the warp covers one word
+    if (p < P.U) P.H[p] = h;
 }
 
 // ---- 7. master: g = (1/n) sum_c g_c, l = (1/n) sum_c Lk_c (TrainLoop.h:1100-1333) ------------
@@ -1751,9 +1769,11 @@ struct GridSync {
 // dimension of which the upper triangle is read.
 // The solve of one problem by a group of G cooperating CTAs (this CTA is number bid of the group);
 // the grid barrier counts the group's CTAs on P.bar.
+// apply_first: the round's master merge (k_apply's work) runs first, each warp a selection word at
+// a time, and the system is formed from the merged H (Hin must be P.H, packed).
 __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict__ Hin, int hin_lda, const double* lptr,
                                           double lval, const double* __restrict__ gin, double* dxout, double* xupd,
-                                          int record, unsigned G, unsigned bid, GridSync& gs)
+                                          int record, unsigned G, unsigned bid, GridSync& gs, int apply_first = 0)
 {
     __shared__ double Db[kCholNB][kCholNB + 1];
     __shared__ double Rb[kCholNB][kCholNB + 1];
@@ -1773,14 +1793,29 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     if (P.ls && bid == 0 && threadIdx.x == 0) P.ls[4] = 0.0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int gtid = bid * blockDim.x + tid, gthreads = G * blockDim.x;
-    for (int p = gtid; p < UA; p += gthreads) {
-        int i, j;
-        upper_ij(p, i, j);
-        if (j < d) {
-            const double hv = hin_lda > 0 ? Hin[(size_t)j * hin_lda + i] : Hin[p];
-            A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
-        } else {
-            A[p] = (i < d) ? gin[i] : 0.0;
+    if (apply_first) {
+        const int U = d * (d + 1) / 2;
+        for (int wd = gtid >> 5; wd < (U + 31) >> 5; wd += gthreads >> 5) {
+            const int p = wd * 32 + lane;
+            const double hv = apply_word(P, p, lane);
+            if (p < U) {
+                P.H[p] = hv;
+                int i, j;
+                upper_ij(p, i, j);
+                A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
+            }
+        }
+        for (int p = U + gtid; p < UA; p += gthreads) A[p] = (p - U < d) ? gin[p - U] : 0.0;    // column d
+    } else {
+        for (int p = gtid; p < UA; p += gthreads) {
+            int i, j;
+            upper_ij(p, i, j);
+            if (j < d) {
+                const double hv = hin_lda > 0 ? Hin[(size_t)j * hin_lda + i] : Hin[p];
+                A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
+            } else {
+                A[p] = (i < d) ? gin[i] : 0.0;
+            }
         }
     }
     if (!gs.sync()) goto timeout;
@@ -2072,10 +2107,10 @@ timeout:
 __global__ void __launch_bounds__(kCoopThreads) k_chol_coop(Dev P, const double* __restrict__ Hin, int hin_lda,
                                                             const double* lptr, double lval,
                                                             const double* __restrict__ gin, double* dxout,
-                                                            double* xupd, int record)
+                                                            double* xupd, int record, int apply_first)
 {
     GridSync gs(P.bar, gridDim.x);
-    chol_body(P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, gridDim.x, blockIdx.x, gs);
+    chol_body(P, Hin, hin_lda, lptr, lval, gin, dxout, xupd, record, gridDim.x, blockIdx.x, gs, apply_first);
     gs.finish();
 }
 
