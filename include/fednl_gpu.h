@@ -370,6 +370,13 @@ int fednl_mx_round_result(fednl_mx_handle h, fednl_round_stats* stats);
  * count).  Mixed handles: the solver (FP64 cooperative, FP32 cooperative with refinement, or, d up
  * to about 300, the FP32 shared-memory factor with refinement) and the chosen one's CTA count. */
 int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid, double* solve_ms);
+/* the launch shape fednl_gpu_autotune chose for the binary-feature Hessian kernel, measured per
+ * (d, bucket of the clients' largest n_i: n_i in (2^(b-1), 2^b] is bucket b) and cached for the
+ * process: threads per block (128, 256, 512), whether the attribute masks are staged in shared
+ * memory, the bucket, and the chosen shape's launch time in ms (0 before tuning or for dense
+ * features); results do not depend on the shape */
+int fednl_gpu_autotune_shapes(fednl_handle h, int32_t* hess_threads, int32_t* hess_masks_in_smem, int32_t* ni_bucket,
+                              double* hess_ms);
 int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver, int32_t* chol_grid, double* solve_ms);
 
 /* free and total device memory (admission by free memory) */

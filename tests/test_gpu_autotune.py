@@ -1,6 +1,7 @@
-"""Autotuning of the round's Newton solve: the measurement leaves the run's state untouched, the
-FP64 engine's results do not depend on the chosen CTA count, and the mixed engine's choice keeps its
-trajectory (the FP32 solver agrees with the FP64 one to about 1e-6 relative)."""
+"""Autotuning of the round's Newton solve and of the binary Hessian's launch shape: the measurement
+leaves the run's state untouched, the FP64 engine's results do not depend on the chosen CTA count or
+shape, and the mixed engine's choice keeps its trajectory (the FP32 solver agrees with the FP64 one
+to about 1e-6 relative)."""
 import numpy as np
 import pytest
 
@@ -26,6 +27,8 @@ def test_fp64_autotune_keeps_results(gpu):
     x_before = b.x()
     t = b.autotune()
     assert 1 <= t["chol_ctas"] <= 152 and t["solve_ms"] > 0
+    # the Hessian's launch shape, tuned per (d, n_i bucket): n_i up to 81 is bucket 7
+    assert t["hess_threads"] in (128, 256, 512) and t["ni_bucket"] == 7 and t["hess_ms"] > 0
     np.testing.assert_array_equal(b.x(), x_before)            # tuning ran on scratch outputs
     ga = np.concatenate([ga, a.run(5)])
     gb = np.concatenate([gb, b.run(5)])

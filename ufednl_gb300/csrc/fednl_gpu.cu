@@ -510,8 +510,11 @@ struct fednl_handle_s {
     Dev dev{};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    size_t hess_smem = 0;
-    bool hess_smem_bits = true;
+    size_t hess_smem = 0;              // dynamic shared memory of the chosen binary-Hessian shape
+    bool hess_smem_bits = true;        // chosen: attribute masks staged in shared memory
+    int hess_nt = kHessThreads;        // chosen: threads per block
+    size_t hess_smem_sm = 0, hess_smem_gl = 0;   // bytes with the masks staged (0: they do not fit) / read from global
+    double hess_ms = 0.0;              // tuned shape's measured launch time (0: not tuned)
     int chol_grid = 1;
     int ref_grid = 1;          // CTAs of the reference-order solve
     int rounds_done = 0;
@@ -544,6 +547,40 @@ int mark(fednl_handle h, Marks* m, const char* name)
 
 // threads of k_client_binary: a lane pair per attribute when that fits one CTA
 int client_threads(int d) { return std::min(1024, std::max(128, (2 * d + 31) / 32 * 32)); }
+
+// The binary Hessian in one of its launch shapes (the results do not depend on the shape: every
+// warp owns the same 512 upper positions and the client's last block adds the segments in order).
+template <bool SM>
+cudaError_t launch_hess_binary_t(const Dev& Q, int nseg, size_t smem, int nclients, int mode, cudaStream_t st, int nt)
+{
+    const unsigned gx = (unsigned)((nseg + nt / 32 - 1) / (nt / 32));
+    switch (nt) {
+    case 128: k_hess_binary<SM, 128><<<dim3(gx, nclients), 128, smem, st>>>(Q, mode); break;
+    case 512: k_hess_binary<SM, 512><<<dim3(gx, nclients), 512, smem, st>>>(Q, mode); break;
+    default: k_hess_binary<SM, 256><<<dim3(gx, nclients), 256, smem, st>>>(Q, mode); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hess_binary(fednl_handle h, const Dev& Q, int nclients, int mode, cudaStream_t st, bool smem_bits,
+                               int nt)
+{
+    if (smem_bits) return launch_hess_binary_t<true>(Q, h->nseg, h->hess_smem_sm, nclients, mode, st, nt);
+    return launch_hess_binary_t<false>(Q, h->nseg, h->hess_smem_gl, nclients, mode, st, nt);
+}
+
+cudaError_t raise_hess_smem(fednl_handle h)
+{
+    cudaError_t e = cudaSuccess;
+    for (const void* k : {(const void*)k_hess_binary<false, 128>, (const void*)k_hess_binary<false, 256>,
+                          (const void*)k_hess_binary<false, 512>})
+        if (e == cudaSuccess) e = fednl_raise_dyn_smem(k, h->hess_smem_gl);
+    if (h->hess_smem_sm)
+        for (const void* k : {(const void*)k_hess_binary<true, 128>, (const void*)k_hess_binary<true, 256>,
+                              (const void*)k_hess_binary<true, 512>})
+            if (e == cudaSuccess) e = fednl_raise_dyn_smem(k, h->hess_smem_sm);
+    return e;
+}
 
 int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = false)
 {
@@ -586,15 +623,13 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         CKL();
     }
     MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
-    dim3 hg(h->nfpart, na);
     const int hmode = h->pp ? 2 : 0;
     if (h->binary) {
-        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(P, hmode);
-        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(P, hmode);
+        CK(launch_hess_binary(h, P, na, hmode, st, h->hess_smem_bits, h->hess_nt));
     } else {
-        k_hess_dense<<<hg, kHessThreads, 0, st>>>(P, hmode);
+        k_hess_dense<<<dim3(h->nfpart, na), kHessThreads, 0, st>>>(P, hmode);
+        CKL();
     }
-    CKL();
     if (P.ref) {
         MARK("k_frob_ref");
         k_frob_ref<<<na, kFrobRefThreads, (size_t)kFrobRing * h->d * 8, st>>>(P);
@@ -1085,13 +1120,12 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         int maxW = (h->maxn + 63) / 64;
         // attribute masks (when they fit), D_s, and the diagonal values
         size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8 + (size_t)d * 8;
-        h->hess_smem_bits = need <= 200 * 1024;
-        h->hess_smem = h->hess_smem_bits ? need : (size_t)h->maxn * 8 + (size_t)d * 8;
+        h->hess_smem_gl = (size_t)h->maxn * 8 + (size_t)d * 8;
+        h->hess_smem_sm = need <= 200 * 1024 ? need : 0;
+        h->hess_smem_bits = h->hess_smem_sm != 0;
+        h->hess_smem = h->hess_smem_bits ? h->hess_smem_sm : h->hess_smem_gl;
         if (h->hess_smem > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
-        if (h->hess_smem_bits)
-            CK(fednl_raise_dyn_smem((const void*)k_hess_binary<true>, h->hess_smem));
-        else
-            CK(fednl_raise_dyn_smem((const void*)k_hess_binary<false>, h->hess_smem));
+        CK(raise_hess_smem(h));
         if ((size_t)h->maxn * 16 > 48 * 1024) {
             CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
             CK(fednl_raise_dyn_smem((const void*)k_client_binary, (size_t)h->maxn * 16));
@@ -1137,17 +1171,15 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
         k_grad_binary<<<dim3((2 * h->d + 127) / 128, h->nc), 128, (size_t)h->maxn * 16, st>>>(P);
         CKL();
     }
-    dim3 hg(h->nfpart, h->nc);
     Dev Pall = P;             // every client's initial shift, whatever a round processes
     Pall.act = nullptr;
     Pall.n_act = h->nc;
     if (h->binary) {
-        if (h->hess_smem_bits) k_hess_binary<true><<<hg, kHessThreads, h->hess_smem, st>>>(Pall, 1);
-        else k_hess_binary<false><<<hg, kHessThreads, h->hess_smem, st>>>(Pall, 1);
+        CK(launch_hess_binary(h, Pall, h->nc, 1, st, h->hess_smem_bits, h->hess_nt));
     } else {
-        k_hess_dense<<<hg, kHessThreads, 0, st>>>(Pall, 1);
+        k_hess_dense<<<dim3(h->nfpart, h->nc), kHessThreads, 0, st>>>(Pall, 1);
+        CKL();
     }
-    CKL();
     k_h_init<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     CKL();
     if (h->pp) {
@@ -1352,6 +1384,79 @@ int fednl_gpu_solve_batch(fednl_handle* hs, int32_t n, fednl_mx_handle* mxs, int
     return FEDNL_OK;
 }
 
+namespace {
+// clients' sample counts bucketed by powers of two: n_i in (2^(b-1), 2^b] is bucket b
+int ni_bucket_of(int n)
+{
+    int b = 0;
+    while ((1 << b) < n && b < 30) ++b;
+    return b;
+}
+
+// The binary Hessian's launch shape (masks staged in shared memory or read from global memory;
+// 128, 256 or 512 threads per block) for this d and the clients' largest n_i bucket: measured once
+// per process and key on the handle's own data (round-mode launches between rounds: their outputs
+// are recomputed by the next round before any use), cached for later handles.  Returns 1 when the
+// handle's shape changed.
+int tune_hess_shape(fednl_handle h)
+{
+    struct Shape {
+        bool sm;
+        int nt;
+        double ms;
+    };
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, Shape> cache;
+    const std::pair<int, int> key(h->d, ni_bucket_of(h->maxn) + (h->hess_smem_sm ? 0 : 64));
+    Shape best{h->hess_smem_bits, h->hess_nt, 0.0};
+    bool hit = false;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            best = it->second;
+            hit = true;
+        }
+    }
+    if (!hit) {
+        cudaStream_t st = h->stream;
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        best.ms = 1e30;
+        const Dev& Q = h->dev;
+        for (int sm = h->hess_smem_sm ? 1 : 0; sm >= 0; --sm)
+            for (int nt : {128, 256, 512}) {
+                cudaError_t e = launch_hess_binary(h, Q, h->nc, 0, st, sm != 0, nt);   // warm-up
+                for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
+                    if (r == 1) e = cudaEventRecord(e0, st);
+                    if (e == cudaSuccess) e = launch_hess_binary(h, Q, h->nc, 0, st, sm != 0, nt);
+                }
+                if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float t = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+                if (e != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return fail(FEDNL_ECUDA, "Hessian tuning launch failed: %s", cudaGetErrorString(e));
+                }
+                if (t / 2.0 < best.ms) best = Shape{sm != 0, nt, t / 2.0};
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::lock_guard<std::mutex> g(mu);
+        cache[key] = best;
+    }
+    const bool changed = best.sm != h->hess_smem_bits || best.nt != h->hess_nt;
+    h->hess_smem_bits = best.sm;
+    h->hess_nt = best.nt;
+    h->hess_smem = best.sm ? h->hess_smem_sm : h->hess_smem_gl;
+    h->hess_ms = best.ms;
+    return changed ? 1 : 0;
+}
+}  // namespace
+
 int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid_out, double* solve_ms)
 {
     if (!h) return fail(FEDNL_EINVAL, "null handle");
@@ -1376,17 +1481,32 @@ int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid_out, double* solve_ms)
     cudaFree(scratch);
     cudaFree(sstatus);
     if (rc) return rc;
-    if (grid != h->chol_grid) {
-        h->chol_grid = grid;
-        if (h->gexec) {                    // the captured round holds the old launch shape
-            cudaGraphExecDestroy(h->gexec);
-            cudaGraphDestroy(h->graph);
-            h->gexec = nullptr;
-            h->graph = nullptr;
-        }
+    bool reshape = grid != h->chol_grid;
+    h->chol_grid = grid;
+    if (h->binary && !h->pp) {
+        rc = tune_hess_shape(h);
+        if (rc > 0) reshape = true;
+        else if (rc < 0) return rc;
+    }
+    if (reshape && h->gexec) {             // the captured round holds the old launch shapes
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
     }
     if (chol_grid_out) *chol_grid_out = grid;
     if (solve_ms) *solve_ms = ms;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_autotune_shapes(fednl_handle h, int32_t* hess_threads, int32_t* hess_masks_in_smem, int32_t* ni_bucket,
+                              double* hess_ms)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (hess_threads) *hess_threads = h->binary ? h->hess_nt : kHessThreads;
+    if (hess_masks_in_smem) *hess_masks_in_smem = h->binary && h->hess_smem_bits ? 1 : 0;
+    if (ni_bucket) *ni_bucket = ni_bucket_of(h->maxn);
+    if (hess_ms) *hess_ms = h->hess_ms;
     return FEDNL_OK;
 }
 

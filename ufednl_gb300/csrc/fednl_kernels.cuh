@@ -481,8 +481,8 @@ __device__ __forceinline__ void client_fsum_last_block(const Dev& P, int c)
     }
 }
 
-template <bool SMEM_BITS>
-__global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
+template <bool SMEM_BITS, int NT>
+__global__ void __launch_bounds__(NT) k_hess_binary(Dev P, int mode)
 {
     extern __shared__ unsigned long long s_fb[];
     const int c = P.act ? P.act[blockIdx.y] : blockIdx.y;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_binary(Dev P, int mode)
     const size_t base = (size_t)c * P.ustr;
     const bool icpt = P.icpt[c] != 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int seg = blockIdx.x * (kHessThreads / 32) + warp;     // 512 positions per warp
+    const int seg = blockIdx.x * (NT / 32) + warp;     // 512 positions per warp, NT / 32 warps per block
     const int p_seg = seg * 512;
     double fa = 0.0, fb2 = 0.0;
     int i, j;

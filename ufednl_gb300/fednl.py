@@ -74,7 +74,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_mx_footprint", "fednl_server_create", "fednl_server_destroy", "fednl_server_submit",
            "fednl_server_tick", "fednl_server_status", "fednl_server_latencies", "fednl_gpu_optionb_solve_mixed", "fednl_gpu_optionb_solve32", "fednl_gpu_selftest_rn",
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
-           "fednl_gpu_autotune", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
+           "fednl_gpu_autotune", "fednl_gpu_autotune_shapes", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
            "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate",
            "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref"]
 
@@ -160,7 +160,8 @@ def load(build_if_missing: bool = True):
                        "fednl_gpu_encode_client_round": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int64,
                                                          C.POINTER(C.c_int64)],
                        "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp],
-                       "fednl_gpu_autotune": [vp, ip, dp], "fednl_mx_autotune": [vp, ip, ip, dp]}.items():
+                       "fednl_gpu_autotune": [vp, ip, dp], "fednl_gpu_autotune_shapes": [vp, ip, ip, ip, dp],
+                       "fednl_mx_autotune": [vp, ip, ip, dp]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -358,11 +359,18 @@ class FedNL:
         return out
 
     def autotune(self) -> dict:
-        """Measures the solve's CTA count on this problem and keeps the fastest (same results)."""
+        """Measures the solve's CTA count and the binary Hessian's launch shape (per d and n_i
+        bucket) on this problem and keeps the fastest (same results)."""
         g = np.zeros(1, dtype=np.int32)
         ms = np.zeros(1)
         _check(load().fednl_gpu_autotune(self._h, _ip(g), _dp(ms)))
-        return {"chol_ctas": int(g[0]), "solve_ms": float(ms[0])}
+        nt = np.zeros(1, dtype=np.int32)
+        sm = np.zeros(1, dtype=np.int32)
+        b = np.zeros(1, dtype=np.int32)
+        hms = np.zeros(1)
+        _check(load().fednl_gpu_autotune_shapes(self._h, _ip(nt), _ip(sm), _ip(b), _dp(hms)))
+        return {"chol_ctas": int(g[0]), "solve_ms": float(ms[0]), "hess_threads": int(nt[0]),
+                "hess_masks_in_smem": bool(sm[0]), "ni_bucket": int(b[0]), "hess_ms": float(hms[0])}
 
     def client_phase(self):
         """Launches the round up to the master's aggregation (no wait); solve_batch ends it."""
