@@ -336,6 +336,28 @@ __global__ void k_margin_dense(Dev P, int S)
     if (P.fmode) P.fterm[s] = -fednl_log(sig);
 }
 
+// acc + the weights of the samples whose bits are set in the attribute's W mask words, added in
+// sample order.  A full word (every sample of 64, as the intercept column's) takes the 64 adds with
+// their loads issued ahead: the chain is then the FP64 add latency alone, not a bit walk per term.
+__device__ __forceinline__ double attr_sum(const unsigned long long* fb, int W, const double* wv, double acc)
+{
+    for (int w = 0; w < W; ++w) {
+        unsigned long long m = fb[w];
+        if (m == ~0ull) {
+            const double* v = wv + w * 64;
+#pragma unroll 16
+            for (int t = 0; t < 64; ++t) acc = __dadd_rn(acc, v[t]);
+            continue;
+        }
+        while (m) {
+            const int b = w * 64 + __ffsll((long long)m) - 1;
+            m &= m - 1;
+            acc = __dadd_rn(acc, wv[b]);
+        }
+    }
+    return acc;
+}
+
 // ---- 2. client gradients g_c = lambda x + sum_s Atr[:, s] q_s (samples in order) ----------
 // One block per (client, range of attributes); the client's weights are staged in shared memory.
 // The same bit loop also forms dsum_j = sum of D_s over the samples with attribute j set, which is
@@ -357,15 +379,7 @@ __global__ void k_grad_binary(Dev P)
     if (j >= P.d) return;
     const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
     const double* wv = s_w + (which ? n : 0);
-    double acc = which ? 0.0 : __dmul_rn(P.x[j], P.lambda);
-    for (int w = 0; w < W; ++w) {
-        unsigned long long m = fb[w];
-        while (m) {
-            const int b = w * 64 + __ffsll((long long)m) - 1;
-            m &= m - 1;
-            acc = __dadd_rn(acc, wv[b]);
-        }
-    }
+    const double acc = attr_sum(fb, W, wv, which ? 0.0 : __dmul_rn(P.x[j], P.lambda));
     if (which) P.dsum[(size_t)c * P.d + j] = acc;
     else P.gc[(size_t)c * P.d + j] = acc;
 }
@@ -403,15 +417,7 @@ __global__ void k_client_binary(Dev P)
         const int j = t >> 1, which = t & 1;
         const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
         const double* wv = s_w + (which ? n : 0);
-        double acc = which ? 0.0 : __dmul_rn(P.x[j], P.lambda);
-        for (int w = 0; w < W; ++w) {
-            unsigned long long m = fb[w];
-            while (m) {
-                const int b = w * 64 + __ffsll((long long)m) - 1;
-                m &= m - 1;
-                acc = __dadd_rn(acc, wv[b]);
-            }
-        }
+        const double acc = attr_sum(fb, W, wv, which ? 0.0 : __dmul_rn(P.x[j], P.lambda));
         if (which) P.dsum[(size_t)c * P.d + j] = acc;
         else P.gc[(size_t)c * P.d + j] = acc;
     }

@@ -205,6 +205,8 @@ struct fednl_mx_handle_s {
     int d = 0, dp = 0, nc = 0, L = 0, U = 0, SW = 0, k = 0, S = 0, tiles = 0, comp = 0;
     long long Up = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;       // the round graph's branch: client gradients and the aggregation
+    cudaEvent_t ev_margin = nullptr, ev_lk = nullptr, ev_join = nullptr;
     std::vector<void*> allocs;
     fednl_tc::MxDev P{};
     CUtensorMap map;
@@ -294,7 +296,15 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     mark();
     k_mx_margin<<<dim3((h->L + 63) / 64, h->nc), dim3(64, 4), 0, st>>>(P);
     mark();
-    k_mx_grad<<<(h->nc * h->d + 7) / 8, 256, 0, st>>>(P);
+    // The client gradients and the master's aggregation read only the margins' weights and Lk: in
+    // a graph they run on a branch beside the Gram tiles, the selection and the shift update (kept
+    // in line when the round is profiled kernel by kernel)
+    const bool fork = !ev && h->side;
+    if (fork) {
+        CKM(cudaEventRecord(h->ev_margin, st));
+        CKM(cudaStreamWaitEvent(h->side, h->ev_margin, 0));
+    }
+    k_mx_grad<<<(h->nc * h->d + 7) / 8, 256, 0, fork ? h->side : st>>>(P);
     mark();
     const bool randk = h->comp == FEDNL_RANDK_PHILOX;
     if (randk) {
@@ -307,6 +317,12 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     mark();
     k_mx_lk<<<h->nc, 256, 0, st>>>(P);
     mark();
+    if (fork) {
+        CKM(cudaEventRecord(h->ev_lk, st));
+        CKM(cudaStreamWaitEvent(h->side, h->ev_lk, 0));
+        k_mx_aggregate<<<(h->d + 7) / 8, 256, 0, h->side>>>(P);
+        CKM(cudaEventRecord(h->ev_join, h->side));
+    }
     if (!randk) {
         const int toplek = h->comp == FEDNL_TOPLEK;
         k_mx_select<<<h->nc, kSelThreads, h->select_smem, st>>>(P, h->k, toplek, h->desc.toplek_seed);
@@ -314,8 +330,12 @@ int mx_launch_round(fednl_mx_handle h, cudaEvent_t* ev = nullptr, bool client_ph
     }
     k_mx_apply<<<(h->U + 255) / 256, 256, 0, st>>>(P);
     mark();
-    k_mx_aggregate<<<(h->d + 7) / 8, 256, 0, st>>>(P);
-    mark();
+    if (fork) {
+        CKM(cudaStreamWaitEvent(st, h->ev_join, 0));
+    } else {
+        k_mx_aggregate<<<(h->d + 7) / 8, 256, 0, st>>>(P);
+        mark();
+    }
     CKM(cudaGetLastError());
     if (client_phase_only) return FEDNL_OK;
     if (h->chol32) {
@@ -463,7 +483,11 @@ static int mx_create_impl(const fednl_problem_desc* desc, fednl_mx_handle* out, 
         delete h;
         return FEDNL_OK;
     }
-    if (rc || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (rc || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_margin, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_lk, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         fednl_mx_destroy(h);
         return rc ? rc : fail_m(FEDNL_ECUDA, "stream creation failed");
     }
@@ -553,6 +577,9 @@ int fednl_mx_destroy(fednl_mx_handle h)
     for (void* p : h->allocs) cudaFree(p);
     if (h->flush_buf) cudaFree(h->flush_buf);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    for (cudaEvent_t e : {h->ev_margin, h->ev_lk, h->ev_join})
+        if (e) cudaEventDestroy(e);
     delete h;
     return FEDNL_OK;
 }
