@@ -193,3 +193,56 @@ def test_execute_local_pp_matches_api_run(lib, tmp_path):
     for r in range(10):
         rec = struct.unpack("<i6d", recs[r * 52:(r + 1) * 52])
         assert rec[0] == r and rec[1] == gn[r]
+
+
+def _read_tracking(raw: bytes):
+    """The tracking layout the engine writes (TrainLoop.h:753-792, 1679-1691): three NUL-terminated
+    strings, six int32 and four doubles, then per round an int32 and six doubles."""
+    parts = raw.split(b"\0", 3)
+    rest = parts[3]
+    ints = struct.unpack("<6i", rest[:24])
+    dbl = struct.unpack("<4d", rest[24:56])
+    recs = [struct.unpack("<i6d", rest[56 + 52 * r:56 + 52 * (r + 1)]) for r in range(ints[2])]
+    return [p.decode() for p in parts[:3]], ints, dbl, recs
+
+
+def test_tracking_file_read_by_reference_reader():
+    """tests/golden/tracking_show.npz holds a tracking file written by the engine's driver and what the
+    reference's own reader (experiments/show.py, run unchanged by make_tracking_golden.py) read from
+    it: every header field and per-round value agrees with the engine's layout, bit for bit."""
+    z = np.load(golden_path("tracking_show.npz"))
+    strs, ints, dbl, recs = _read_tracking(z["raw"].tobytes())
+    assert strs == [str(z["dataset"]), str(z["algorithm"]), str(z["compressor"])]
+    assert list(ints) == list(z["ints"])
+    np.testing.assert_array_equal(np.array(dbl), z["doubles"])
+    n = len(recs)
+    assert n == len(z["rounds"]) == ints[2]
+    got = np.array([r[1:] for r in recs])
+    np.testing.assert_array_equal([r[0] for r in recs], z["rounds"])
+    np.testing.assert_array_equal(got[:, 0], z["grad_norm"])
+    np.testing.assert_array_equal(got[:, 1], z["func_value"])          # show.py: f - f* with f* = 0
+    np.testing.assert_array_equal(got[:, 2], z["x_norm"])
+    nc = ints[3]
+    np.testing.assert_array_equal((got[:, 3] * 8 / nc) + (got[:, 4] * 8 / nc), z["send_bits_total"])
+    np.testing.assert_array_equal(got[:, 4] * 8 / nc, z["send_bits_indices"])
+    np.testing.assert_array_equal(got[:, 5], z["elapsed"])
+
+
+@pytest.mark.gpu
+def test_tracking_file_matches_reference_reader_fixture(lib, tmp_path):
+    """The driver run that made the fixture, again: the new file equals the fixture's bytes except the
+    per-round wall-clock times, so the reference's reader reads the same values from it."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_tracking_golden", golden_path("make_tracking_golden.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    data = tmp_path / "data.txt"
+    mk.write_libsvm(data, mk.tracking_problem())
+    out = tmp_path / "track_{algorithm}_{dataset}.bin"
+    rc, _ = lib.execute_local(mk.COMMAND.format(data=data, out=out))
+    assert rc == 0
+    new = _read_tracking(open(tmp_path / "track_fednl1_data.bin", "rb").read())
+    ref = _read_tracking(np.load(golden_path("tracking_show.npz"))["raw"].tobytes())
+    assert new[0] == ref[0] and new[1] == ref[1] and new[2] == ref[2]
+    for a, b in zip(new[3], ref[3]):
+        assert a[:6] == b[:6]                    # all but the elapsed time
