@@ -378,6 +378,14 @@ int fednl_gpu_autotune(fednl_handle h, int32_t* chol_grid, double* solve_ms);
 int fednl_gpu_autotune_shapes(fednl_handle h, int32_t* hess_threads, int32_t* hess_masks_in_smem, int32_t* ni_bucket,
                               double* hess_ms);
 int fednl_mx_autotune(fednl_mx_handle h, int32_t* solver, int32_t* chol_grid, double* solve_ms);
+/* the binary-feature Hessian's kernel: kind 0 intersects the attribute masks staged in shared
+ * memory, 1 the masks read from global memory, 2 reads the lists of common samples built at upload
+ * (built when no client has more than 16 U attribute pairs, n_i < 32767 and d < 8192;
+ * lists_built says whether they were); threads per block 128, 256 or 512.  The upload
+ * picks kind 2 when the lists exist, fednl_gpu_autotune measures every available pair; the set
+ * call overrides it.  Results are identical for every kind and shape. */
+int fednl_gpu_hess_schedule(fednl_handle h, int32_t* kind, int32_t* threads, int32_t* lists_built);
+int fednl_gpu_set_hess_schedule(fednl_handle h, int32_t kind, int32_t threads);
 
 /* free and total device memory (admission by free memory) */
 int fednl_gpu_mem_info(int64_t* free_bytes, int64_t* total_bytes);

@@ -7,7 +7,9 @@
  * repository root).  Floating-point formulas keep the reference's operation order where the
  * reference fixes it (per-entry sample order of the Hessian and gradient sums, products as
  * written); SIMD horizontal-sum orders of dot products and norms are restated as sequential
- * sums, which changes results by a few ulps only.  The file is compiled with
+ * sums, which changes results by a few ulps only.  In the fixed order (not ref_order), {0,1}
+ * features take their attribute sums (gradient, Hessian diagonal, intercept column) in 64-sample
+ * words (blocked_attr_sum), the GPU engine's order for them.  The file is compiled with
  * -ffp-contract=off so that no multiply-add is fused.
  */
 #include "fednl_oracle.h"
@@ -1160,10 +1162,12 @@ typedef struct {
     double* dir;        /* FedNL-PP: localGradient = x Lk + shift x - grad (d) */
     double* ddir;       /* FedNL-PP: the difference last sent to the master (d) */
     double dlk;         /* FedNL-PP: the Lk difference last sent */
+    int32_t icpt;       /* the last attribute is 1 in every sample (an intercept column) */
 } orc_client;
 
 struct orc_state {
     orc_problem p;
+    int32_t blocked;    /* {0,1} features in the fixed order: attribute sums in 64-sample words */
     size_t U;
     uint32_t* upper;
     orc_client* clients;
@@ -1187,6 +1191,71 @@ struct orc_state {
     double f_k;            /* f at the round's starting iterate */
     int32_t ls_steps;      /* function evaluations of the last line search */
 };
+
+/* The GPU engine's fixed order for the attribute sums of {0,1} features (its default feature format
+ * takes the bit-packed kernels for them): acc + the terms of the samples holding attribute i, taken
+ * in 64-sample words; a word's terms are summed in sample order (its first term exactly) and the
+ * word sums are added to acc in word order.  signed_terms: the term is column i of Atr (b_s = +-1)
+ * times v_s, else v_s. */
+static double blocked_attr_sum(const double* atr, int32_t lda, int32_t n, int32_t i, const double* v,
+                               int32_t signed_terms, double acc)
+{
+    for (int32_t w0 = 0; w0 < n; w0 += 64) {
+        int32_t w1 = w0 + 64 < n ? w0 + 64 : n;
+        int32_t have = 0;
+        double part = 0.0;
+        for (int32_t s = w0; s < w1; ++s) {
+            double a = atr[(size_t)s * lda + i];
+            if (a == 0.0)
+                continue;
+            double t = signed_terms ? a * v[s] : v[s];
+            part = have ? part + t : t;
+            have = 1;
+        }
+        if (have)
+            acc = acc + part;
+    }
+    return acc;
+}
+
+/* Gradient (grad) and Hessian (h) of one client at the sigmoid values sig: orc_gradient and
+ * orc_hessian, whose per-entry sample order the reference fixes; in the blocked order (S->blocked)
+ * the attribute sums -- the gradient, the Hessian diagonal and, when the client's last attribute
+ * is an intercept, the Hessian's last column -- are taken by blocked_attr_sum. */
+static void client_grad_hess(const orc_state* S, const orc_client* C, const double* sig, double* grad, double* h)
+{
+    const orc_problem* P = &S->p;
+    int32_t d = P->d, lda = P->lda, n = C->n;
+    if (grad)
+        orc_gradient(C->atr, d, lda, n, S->x, sig, P->lambda, grad);
+    if (h)
+        orc_hessian(C->atr, d, lda, n, sig, P->lambda, h);
+    if (!S->blocked)
+        return;
+    double inv_m = 1.0 / (double)n;
+    double minus_inv_m = -inv_m;
+    double* q = (double*)malloc((size_t)n * sizeof(double));
+    double* dv = (double*)malloc((size_t)n * sizeof(double));
+    for (int32_t s = 0; s < n; ++s) {
+        double z1 = 1.0 - sig[s];
+        q[s] = z1 * minus_inv_m;              /* orc_gradient's q_s */
+        dv[s] = inv_m * (z1 * sig[s]);        /* orc_hessian's D_s */
+    }
+    for (int32_t i = 0; i < d; ++i) {
+        if (grad)
+            grad[i] = blocked_attr_sum(C->atr, lda, n, i, q, 1, S->x[i] * P->lambda);
+        if (h) {
+            double ds = blocked_attr_sum(C->atr, lda, n, i, dv, 0, 0.0);
+            h[(size_t)i * lda + i] = ds + P->lambda;
+            if (C->icpt && i < d - 1) {
+                h[(size_t)(d - 1) * lda + i] = ds;
+                h[(size_t)i * lda + (d - 1)] = ds;
+            }
+        }
+    }
+    free(q);
+    free(dv);
+}
 
 /* Worker side of one client, first half: the compressor's index draw, margins, sigmoid, gradient,
  * Hessian and difference (LocalWorkerForFedNL_*.h, bodies of the per-context loops).  Returns
@@ -1235,11 +1304,10 @@ static double client_prepare(orc_state* S, int32_t c, double* hbuf, double* diff
         orc_randk_philox(P->seed_base, (uint32_t)c, C->draws++, S->k_eff, U, S->upper, C->msg_idx);
 
     margin_sigmoid(P, C->atr, n, S->x, mtmp, stmp);
-    orc_gradient(C->atr, d, lda, n, S->x, stmp, P->lambda, C->grad);
     if (P->line_search || P->track_f)      /* "Put fi" (TopK.h:132-137) */
         C->fi = P->ref_order ? orc_client_function_ref(stmp, n, S->x, d, P->lambda)
                              : orc_client_function(stmp, n, S->x, d, P->lambda);
-    orc_hessian(C->atr, d, lda, n, stmp, P->lambda, hbuf);
+    client_grad_hess(S, C, stmp, C->grad, hbuf);
     for (size_t t = 0; t < full; ++t)           /* difference = H_i - shift_i (TopK.h:70-71) */
         diff[t] = hbuf[t] - C->shift[t];
     return P->ref_order ? orc_frob_ref(diff, d, lda) : orc_frob_sym(diff, d, lda);
@@ -1416,6 +1484,15 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
     S->upper = (uint32_t*)malloc(S->U * sizeof(uint32_t));
     orc_upper_indices(d, lda, S->upper);
     S->k_eff = (p->compressor == ORC_IDENTITY || p->compressor == ORC_NATURAL) ? (int32_t)S->U : p->k;
+    {
+        size_t tot = 0;
+        for (int32_t c = 0; c < nc; ++c)
+            tot += (size_t)p->n_samples[c];
+        S->blocked = !p->ref_order;
+        for (size_t t = 0; S->blocked && t < tot * (size_t)d; ++t)
+            if (p->features[t] != 0.0 && p->features[t] != 1.0)
+                S->blocked = 0;
+    }
     S->prescale = (1.0 / (double)nc) * p->alpha;
     S->x = (double*)malloc((size_t)d * sizeof(double));
     memcpy(S->x, x0, (size_t)d * sizeof(double));
@@ -1448,6 +1525,10 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
             for (int32_t i = 0; i < d; ++i)
                 col[i] = (b == 1.0) ? a[i] : a[i] * -1.0;
         }
+        C->icpt = 1;
+        for (int32_t s = 0; s < n; ++s)
+            if (p->features[(off + (size_t)s) * (size_t)d + (size_t)(d - 1)] != 1.0)
+                C->icpt = 0;
         off += (size_t)n;
         C->shift = (double*)malloc(full * sizeof(double));
         C->grad = (double*)calloc((size_t)d, sizeof(double));
@@ -1456,7 +1537,7 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
         C->rng = p->seed_base + (uint32_t)c;    /* TrainLoop.h:632 */
         /* learningHessian = H_i(x0); H += learningHessian (TrainLoop.h:639-643) */
         margin_sigmoid(p, C->atr, n, S->x, mtmp, stmp);
-        orc_hessian(C->atr, d, lda, n, stmp, p->lambda, C->shift);
+        client_grad_hess(S, C, stmp, NULL, C->shift);
         for (size_t t = 0; t < full; ++t)
             S->H[t] += C->shift[t];
         if (p->pp) {
@@ -1464,7 +1545,7 @@ orc_state* orc_create(const orc_problem* p, const double* x0)
              * localGradient = shift x0 - grad(x0) */
             C->dir = (double*)calloc((size_t)d, sizeof(double));
             C->ddir = (double*)calloc((size_t)d, sizeof(double));
-            orc_gradient(C->atr, d, lda, n, S->x, stmp, p->lambda, C->grad);
+            client_grad_hess(S, C, stmp, C->grad, NULL);
             matvec_cols(C->shift, d, lda, S->x, mtmp);
             for (int32_t i = 0; i < d; ++i)
                 C->dir[i] = mtmp[i] - C->grad[i];
@@ -1707,7 +1788,7 @@ static void pp_select_and_track(orc_state* S)
         orc_client* C = &S->clients[c];
         orc_margin(C->atr, d, lda, C->n, S->x, mtmp);
         orc_sigmoid(mtmp, C->n, stmp);
-        orc_gradient(C->atr, d, lda, C->n, S->x, stmp, P->lambda, gtmp);
+        client_grad_hess(S, C, stmp, gtmp, NULL);
         for (int32_t i = 0; i < d; ++i)
             bsum[i] = (c % 32 == 0) ? gtmp[i] : bsum[i] + gtmp[i];
         if (c % 32 == 31 || c == nc - 1)

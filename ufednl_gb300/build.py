@@ -3,7 +3,9 @@
     python -m ufednl_gb300.build
 
 One nvcc invocation (the CUDA round engine and the host-side local driver), one -gencode; the
-output goes to ufednl_gb300/_build/.
+output goes to ufednl_gb300/_build/.  Host code is compiled with -ffp-contract=off: gcc contracts
+a*b+c into one FMA by default on aarch64 but not on x86-64, and the host parts (the LIBSVM number
+parser, the driver's norms) must round the same on both.
 """
 from __future__ import annotations
 
@@ -22,7 +24,8 @@ DEPS = SOURCES + [os.path.join(PKG, "csrc", f) for f in os.listdir(os.path.join(
     [os.path.join(REPO, "include", "fednl_gpu.h")]
 
 NVCC_FLAGS = ["-O3", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
-              "-Xcompiler", "-fPIC", "-shared", "-Xcompiler", "-fvisibility=default"]
+              "-Xcompiler", "-fPIC", "-shared", "-Xcompiler", "-fvisibility=default",
+              "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

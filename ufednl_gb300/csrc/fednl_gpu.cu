@@ -510,10 +510,11 @@ struct fednl_handle_s {
     Dev dev{};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    size_t hess_smem = 0;              // dynamic shared memory of the chosen binary-Hessian shape
-    bool hess_smem_bits = true;        // chosen: attribute masks staged in shared memory
+    int hess_kind = 0;                 // chosen binary-Hessian kernel (kHessMasksSmem, kHessMasksGlobal, kHessHits)
     int hess_nt = kHessThreads;        // chosen: threads per block
     size_t hess_smem_sm = 0, hess_smem_gl = 0;   // bytes with the masks staged (0: they do not fit) / read from global
+    bool hits_ready = false;           // common-sample lists built at upload (k_hess_hits)
+    int hits_maxrec = 0;               // most multi-sample records in one segment
     double hess_ms = 0.0;              // tuned shape's measured launch time (0: not tuned)
     int chol_grid = 1;
     int ref_grid = 1;          // CTAs of the reference-order solve
@@ -545,8 +546,16 @@ int mark(fednl_handle h, Marks* m, const char* name)
         if (rc_) return rc_;                                                                       \
     } while (0)
 
-// threads of k_client_binary: a lane pair per attribute when that fits one CTA
-int client_threads(int d) { return std::min(1024, std::max(128, (2 * d + 31) / 32 * 32)); }
+// threads of k_client_binary: a lane pair per attribute when that fits one CTA, and a warp for the
+// intercept's sums
+int client_threads(int d) { return std::min(1024, std::max(128, (2 * d + 31) / 32 * 32 + 32)); }
+
+// dynamic shared memory of k_client_binary: the weights and the intercept's word sums
+size_t client_smem(fednl_handle h) { return (size_t)h->maxn * 16 + (size_t)((h->maxn + 63) / 64) * 16; }
+
+// The binary Hessian's kernels: attribute masks intersected every round (staged in shared memory
+// or read from global memory), or the common-sample lists built at upload.
+enum { kHessMasksSmem = 0, kHessMasksGlobal = 1, kHessHits = 2 };
 
 // The binary Hessian in one of its launch shapes (the results do not depend on the shape: every
 // warp owns the same 512 upper positions and the client's last block adds the segments in order).
@@ -562,16 +571,35 @@ cudaError_t launch_hess_binary_t(const Dev& Q, int nseg, size_t smem, int nclien
     return cudaGetLastError();
 }
 
-cudaError_t launch_hess_binary(fednl_handle h, const Dev& Q, int nclients, int mode, cudaStream_t st, bool smem_bits,
-                               int nt)
+size_t hits_smem(fednl_handle h, int nt)
 {
-    if (smem_bits) return launch_hess_binary_t<true>(Q, h->nseg, h->hess_smem_sm, nclients, mode, st, nt);
+    return hits_stage_bytes(nt) + ((size_t)h->maxn + 2 * h->d + (size_t)(nt / 32) * h->hits_maxrec) * 8;
+}
+
+cudaError_t launch_hess_binary(fednl_handle h, const Dev& Q, int nclients, int mode, cudaStream_t st, int kind, int nt)
+{
+    if (kind == kHessHits) {
+        const unsigned gx = (unsigned)((h->nseg + nt / 32 - 1) / (nt / 32));
+        const size_t smem = hits_smem(h, nt);
+        switch (nt) {
+        case 128: k_hess_hits<128><<<dim3(gx, nclients), 128, smem, st>>>(Q, mode, h->hits_maxrec); break;
+        case 512: k_hess_hits<512><<<dim3(gx, nclients), 512, smem, st>>>(Q, mode, h->hits_maxrec); break;
+        default: k_hess_hits<256><<<dim3(gx, nclients), 256, smem, st>>>(Q, mode, h->hits_maxrec); break;
+        }
+        return cudaGetLastError();
+    }
+    if (kind == kHessMasksSmem) return launch_hess_binary_t<true>(Q, h->nseg, h->hess_smem_sm, nclients, mode, st, nt);
     return launch_hess_binary_t<false>(Q, h->nseg, h->hess_smem_gl, nclients, mode, st, nt);
 }
 
 cudaError_t raise_hess_smem(fednl_handle h)
 {
     cudaError_t e = cudaSuccess;
+    if (h->hits_ready) {
+        if (e == cudaSuccess) e = fednl_raise_dyn_smem((const void*)k_hess_hits<128>, hits_smem(h, 128));
+        if (e == cudaSuccess) e = fednl_raise_dyn_smem((const void*)k_hess_hits<256>, hits_smem(h, 256));
+        if (e == cudaSuccess) e = fednl_raise_dyn_smem((const void*)k_hess_hits<512>, hits_smem(h, 512));
+    }
     for (const void* k : {(const void*)k_hess_binary<false, 128>, (const void*)k_hess_binary<false, 256>,
                           (const void*)k_hess_binary<false, 512>})
         if (e == cudaSuccess) e = fednl_raise_dyn_smem(k, h->hess_smem_gl);
@@ -595,7 +623,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     }
     if (h->binary && !P.ref) {       // the client oracle in one launch
         MARK("k_client_binary");
-        k_client_binary<<<h->nc, client_threads(h->d), (size_t)h->maxn * 16, st>>>(P);
+        k_client_binary<<<h->nc, client_threads(h->d), client_smem(h), st>>>(P);
         CKL();
     } else {
         if (P.ref) {
@@ -622,10 +650,21 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_pp_norm<<<1, 32, 0, st>>>(P);
         CKL();
     }
+    int comp = h->comp;
+    // The master's aggregation needs only the gradients and Lk.  With TopK / TopLEK it runs in the
+    // selection kernel's idle warps; otherwise, in a graph, on a branch beside the compressor and the
+    // shift update (kept in line when the round is profiled kernel by kernel)
+    const bool agg_in_select = !h->pp && (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK);
+    // the master merge runs in the solve's first phase (FP64 order, not FedNL-PP, not when the
+    // solve is left to a batched launch)
+    const bool apply_in_solve = !h->pp && !P.ref && !client_phase_only;
+    // With TopK / TopLEK in the fixed order the selection kernel's idle warps also form ||diff||_F^2
+    // and Lk (the Hessian writes the difference only), and the solve forms l from Lk while it merges
+    const bool norms_in_select = agg_in_select && apply_in_solve && !h->desc.option_a;
     MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
-    const int hmode = h->pp ? 2 : 0;
+    const int hmode = h->pp ? 2 : norms_in_select ? 3 : 0;
     if (h->binary) {
-        CK(launch_hess_binary(h, P, na, hmode, st, h->hess_smem_bits, h->hess_nt));
+        CK(launch_hess_binary(h, P, na, hmode, st, h->hess_kind, h->hess_nt));
     } else {
         k_hess_dense<<<dim3(h->nfpart, na), kHessThreads, 0, st>>>(P, hmode);
         CKL();
@@ -635,11 +674,6 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_frob_ref<<<na, kFrobRefThreads, (size_t)kFrobRing * h->d * 8, st>>>(P);
         CKL();
     }                             // otherwise the Hessian kernel's last block per client formed F
-    int comp = h->comp;
-    // The master's aggregation needs only the gradients and Lk.  With TopK / TopLEK it runs in the
-    // selection kernel's idle warps; otherwise, in a graph, on a branch beside the compressor and the
-    // shift update (kept in line when the round is profiled kernel by kernel)
-    const bool agg_in_select = !h->pp && (comp == FEDNL_TOPK || comp == FEDNL_TOPLEK);
     const bool fork = !M && h->side && !h->pp && !agg_in_select;
     if (fork) {
         CK(cudaEventRecord(h->fork_ev, st));
@@ -654,6 +688,13 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         // TopLEK's rounding draws run in the launch's last CTA
         SelectDraws dr{comp == FEDNL_TOPLEK ? h->drawctr : nullptr, h->nc, h->W, P.wstate, MasterAgg{}};
         if (agg_in_select) dr.agg = MasterAgg{P.gc, P.lk, P.g, P.stats, h->d, h->nc, P.inv_n};
+        if (norms_in_select) {
+            dr.agg.lk = nullptr;          // l is formed by the solve
+            dr.norms = 1;
+            dr.nseg = h->nseg;
+            dr.fpart = P.Fpart;
+            dr.lk = P.lk;
+        }
         k_select<<<na, kSelThreads, h->k < h->U ? select_smem(h->k) : 0, st>>>(
             P.diff, h->ustr, h->U, h->k, comp == FEDNL_TOPLEK, delta, P.F, P.sel, h->SW, P.cnt, P.needs, P.pdraw,
             P.minidx, P.status, P.act, P.ref, dr);
@@ -672,9 +713,6 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
         k_randseqk<<<na, 256, 0, st>>>(P.rstate, h->nc, h->U, h->k, P.rseq, P.sel, h->SW, P.cnt, P.act);
         CKL();
     }
-    // the master merge runs in the solve's first phase (FP64 order, not FedNL-PP, not when the
-    // solve is left to a batched launch)
-    const bool apply_in_solve = !h->pp && !P.ref && !client_phase_only;
     if (!apply_in_solve) {
         MARK("k_apply");
         k_apply<<<(h->U + 127) / 128, 128, 0, st>>>(P);
@@ -723,7 +761,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     } else {
         MARK("k_chol_coop");
         CK(launch_chol(P, h->chol_grid, st, P.H, 0, lptr, P.lambda, P.g, P.dx, D.line_search ? nullptr : P.x, 1,
-                       apply_in_solve ? 1 : 0));
+                       norms_in_select ? 2 : apply_in_solve ? 1 : 0));
     }
     if (D.line_search) {
         MARK("k_ls_init");
@@ -1021,6 +1059,113 @@ static void for_client_ranges(int nc, const std::function<void(int, int, int)>& 
     for (auto& th : ts) th.join();
 }
 
+// Common-sample lists of the binary Hessian (k_hess_hits), from the CSR rows of the upload: each
+// client's samples in order, every pair a < b of a sample's attributes other than the intercept
+// adds the sample to upper position b (b + 1) / 2 + a.  Built only when the lists stay small (at
+// most 16 pairs per upper position in every client, 64 M in all) and the codes can hold the
+// sample and attribute indices.
+struct HitLists {
+    std::vector<uint16_t> code;    // [nc][ustr]
+    std::vector<uint32_t> seg;     // [nc][nseg + 1]
+    std::vector<uint32_t> rec;     // [records + 1]
+    std::vector<uint16_t> hits;
+    int maxrec = 0;
+};
+
+static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, const std::vector<int>& colidx,
+                            const std::vector<int>& icpt, HitLists& L)
+{
+    const int nc = h->nc, d = h->d, U = h->U, nseg = h->nseg;
+    if (h->maxn > 0x7ffe || d > 0x1fff) return false;
+    std::vector<long long> pairs(nc, 0);
+    long long total = 0;
+    for (int c = 0; c < nc; ++c) {
+        for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+            const long long m = rowptr[s + 1] - rowptr[s] - (icpt[c] ? 1 : 0);
+            pairs[c] += m * (m - 1) / 2;
+        }
+        if (pairs[c] > 16ll * U) return false;
+        total += pairs[c];
+    }
+    if (total > (64ll << 20)) return false;
+    auto for_pairs = [&](int c, auto&& f) {   // f(local sample, position)
+        const int last = icpt[c] ? d - 1 : d;
+        for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+            const int b0 = rowptr[s], b1 = rowptr[s + 1];
+            for (int y = b0; y < b1; ++y) {
+                const int b = colidx[y];
+                if (b >= last) break;
+                const int pb = b * (b + 1) / 2;
+                for (int x = b0; x < y; ++x) f(s - h->soff[c], pb + colidx[x]);
+            }
+        }
+    };
+    // pass 1: records and their samples per client and segment
+    std::vector<long long> nrec(nc, 0), nhit(nc, 0);
+    std::vector<int> segrec((size_t)nc * nseg, 0);
+    std::vector<int> maxrec(nc, 0);
+    for_client_ranges(nc, [&](int, int c0, int c1) {
+        std::vector<int> cnt(U);
+        for (int c = c0; c < c1; ++c) {
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for_pairs(c, [&](int, int p) { ++cnt[p]; });
+            for (int p = 0; p < U; ++p)
+                if (cnt[p] >= 2) {
+                    ++segrec[(size_t)c * nseg + p / 512];
+                    nrec[c] += 1;
+                    nhit[c] += cnt[p];
+                }
+            for (int g = 0; g < nseg; ++g) maxrec[c] = std::max(maxrec[c], segrec[(size_t)c * nseg + g]);
+        }
+    });
+    std::vector<long long> rbase(nc + 1, 0), hbase(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) {
+        rbase[c + 1] = rbase[c] + nrec[c];
+        hbase[c + 1] = hbase[c] + nhit[c];
+    }
+    if (hbase[nc] >= 0xffffffffll) return false;
+    L.code.assign((size_t)nc * h->ustr, (uint16_t)kHitNone);
+    L.seg.assign((size_t)nc * (nseg + 1), 0u);
+    L.rec.assign((size_t)rbase[nc] + 1, 0u);
+    L.hits.assign((size_t)hbase[nc], 0);
+    L.maxrec = std::max(1, *std::max_element(maxrec.begin(), maxrec.end()));
+    L.rec[rbase[nc]] = (uint32_t)hbase[nc];
+    // pass 2: codes, record starts, then the samples in order
+    for_client_ranges(nc, [&](int, int c0, int c1) {
+        std::vector<int> cnt(U), at(U);
+        for (int c = c0; c < c1; ++c) {
+            std::fill(cnt.begin(), cnt.end(), 0);
+            uint16_t* code = L.code.data() + (size_t)c * h->ustr;
+            for_pairs(c, [&](int ls, int p) {
+                if (cnt[p]++ == 0) code[p] = (uint16_t)ls;
+            });
+            long long r = rbase[c], e = hbase[c];
+            for (int g = 0; g < nseg; ++g) {
+                L.seg[(size_t)c * (nseg + 1) + g] = (uint32_t)r;
+                const long long rg = r;
+                for (int p = g * 512; p < std::min(U, g * 512 + 512); ++p)
+                    if (cnt[p] >= 2) {
+                        code[p] = (uint16_t)(0x8000u | (unsigned)(r - rg));
+                        L.rec[r++] = (uint32_t)e;
+                        at[p] = (int)(e - hbase[c]);
+                        e += cnt[p];
+                    }
+            }
+            L.seg[(size_t)c * (nseg + 1) + nseg] = (uint32_t)r;
+            uint16_t* hits = L.hits.data() + hbase[c];
+            for_pairs(c, [&](int ls, int p) {
+                if (cnt[p] >= 2) hits[at[p]++] = (uint16_t)ls;
+            });
+            for (int j = 0; j < d; ++j) {
+                code[j * (j + 1) / 2 + j] = (uint16_t)(0xc000u | (unsigned)j);
+                if (icpt[c] && j == d - 1)
+                    for (int i = 0; i < j; ++i) code[j * (j + 1) / 2 + i] = (uint16_t)(0xa000u | (unsigned)i);
+            }
+        }
+    });
+    return true;
+}
+
 int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
 {
     if (!h || !features || !labels) return fail(FEDNL_EINVAL, "null argument");
@@ -1061,6 +1206,11 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     P.fbits = nullptr;
     P.icpt = nullptr;
     P.A = nullptr;
+    P.hcode = nullptr;
+    P.hseg = nullptr;
+    P.hrec = nullptr;
+    P.hhits = nullptr;
+    h->hits_ready = false;
     double* lab = nullptr;
     if (fmt == FEDNL_FEATURES_BINARY) {
         std::vector<int> rowptr(S + 1, 0);
@@ -1096,6 +1246,17 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
                     icpt[c] = 0;
                     break;
                 }
+        HitLists hl;
+        h->hits_ready = build_hit_lists(h, rowptr, colidx, icpt, hl);
+        h->hits_maxrec = h->hits_ready ? hl.maxrec : 0;
+        uint16_t *d_hcode = nullptr, *d_hhits = nullptr;
+        uint32_t *d_hseg = nullptr, *d_hrec = nullptr;
+        if (h->hits_ready) {
+            h->feat.want(&d_hcode, hl.code.size());
+            h->feat.want(&d_hseg, hl.seg.size());
+            h->feat.want(&d_hrec, hl.rec.size());
+            h->feat.want(&d_hhits, std::max<size_t>(1, hl.hits.size()));
+        }
         int *d_rowptr, *d_colidx, *d_icpt;
         long long* d_fboff;
         unsigned long long* d_fbits;
@@ -1112,6 +1273,16 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         CK(cudaMemcpy(d_fboff, fboff.data(), h->nc * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_fbits, fbits.data(), words * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_icpt, icpt.data(), h->nc * 4, cudaMemcpyHostToDevice));
+        if (h->hits_ready) {
+            CK(cudaMemcpy(d_hcode, hl.code.data(), hl.code.size() * 2, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_hseg, hl.seg.data(), hl.seg.size() * 4, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_hrec, hl.rec.data(), hl.rec.size() * 4, cudaMemcpyHostToDevice));
+            if (!hl.hits.empty()) CK(cudaMemcpy(d_hhits, hl.hits.data(), hl.hits.size() * 2, cudaMemcpyHostToDevice));
+        }
+        P.hcode = d_hcode;
+        P.hseg = d_hseg;
+        P.hrec = d_hrec;
+        P.hhits = d_hhits;
         P.icpt = d_icpt;
         P.rowptr = d_rowptr;
         P.colidx = d_colidx;
@@ -1122,14 +1293,13 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8 + (size_t)d * 8;
         h->hess_smem_gl = (size_t)h->maxn * 8 + (size_t)d * 8;
         h->hess_smem_sm = need <= 200 * 1024 ? need : 0;
-        h->hess_smem_bits = h->hess_smem_sm != 0;
-        h->hess_smem = h->hess_smem_bits ? h->hess_smem_sm : h->hess_smem_gl;
-        if (h->hess_smem > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
+        if (h->hits_ready && hits_smem(h, 512) > 200 * 1024) h->hits_ready = false;
+        h->hess_kind = h->hits_ready ? kHessHits : h->hess_smem_sm ? kHessMasksSmem : kHessMasksGlobal;
+        h->hess_nt = kHessThreads;
+        if (h->hess_smem_gl > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
         CK(raise_hess_smem(h));
-        if ((size_t)h->maxn * 16 > 48 * 1024) {
-            CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
-            CK(fednl_raise_dyn_smem((const void*)k_client_binary, (size_t)h->maxn * 16));
-        }
+        if ((size_t)h->maxn * 16 > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
+        if (client_smem(h) > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_client_binary, client_smem(h)));
         h->binary = 1;
     } else {
         double* dA;
@@ -1175,7 +1345,7 @@ int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
     Pall.act = nullptr;
     Pall.n_act = h->nc;
     if (h->binary) {
-        CK(launch_hess_binary(h, Pall, h->nc, 1, st, h->hess_smem_bits, h->hess_nt));
+        CK(launch_hess_binary(h, Pall, h->nc, 1, st, h->hess_kind, h->hess_nt));
     } else {
         k_hess_dense<<<dim3(h->nfpart, h->nc), kHessThreads, 0, st>>>(Pall, 1);
         CKL();
@@ -1393,22 +1563,22 @@ int ni_bucket_of(int n)
     return b;
 }
 
-// The binary Hessian's launch shape (masks staged in shared memory or read from global memory;
-// 128, 256 or 512 threads per block) for this d and the clients' largest n_i bucket: measured once
-// per process and key on the handle's own data (round-mode launches between rounds: their outputs
-// are recomputed by the next round before any use), cached for later handles.  Returns 1 when the
-// handle's shape changed.
+// The binary Hessian's kernel and launch shape (common-sample lists, masks staged in shared memory
+// or masks read from global memory; 128, 256 or 512 threads per block) for this d and the clients'
+// largest n_i bucket: measured once per process and key on the handle's own data (round-mode
+// launches between rounds: their outputs are recomputed by the next round before any use), cached
+// for later handles.  Returns 1 when the handle's shape changed.
 int tune_hess_shape(fednl_handle h)
 {
     struct Shape {
-        bool sm;
+        int kind;
         int nt;
         double ms;
     };
     static std::mutex mu;
     static std::map<std::pair<int, int>, Shape> cache;
-    const std::pair<int, int> key(h->d, ni_bucket_of(h->maxn) + (h->hess_smem_sm ? 0 : 64));
-    Shape best{h->hess_smem_bits, h->hess_nt, 0.0};
+    const std::pair<int, int> key(h->d, ni_bucket_of(h->maxn) + (h->hess_smem_sm ? 0 : 64) + (h->hits_ready ? 0 : 128));
+    Shape best{h->hess_kind, h->hess_nt, 0.0};
     bool hit = false;
     {
         std::lock_guard<std::mutex> g(mu);
@@ -1425,12 +1595,13 @@ int tune_hess_shape(fednl_handle h)
         CK(cudaEventCreate(&e1));
         best.ms = 1e30;
         const Dev& Q = h->dev;
-        for (int sm = h->hess_smem_sm ? 1 : 0; sm >= 0; --sm)
+        for (int kind : {kHessHits, kHessMasksSmem, kHessMasksGlobal}) {
+            if ((kind == kHessHits && !h->hits_ready) || (kind == kHessMasksSmem && !h->hess_smem_sm)) continue;
             for (int nt : {128, 256, 512}) {
-                cudaError_t e = launch_hess_binary(h, Q, h->nc, 0, st, sm != 0, nt);   // warm-up
+                cudaError_t e = launch_hess_binary(h, Q, h->nc, 0, st, kind, nt);   // warm-up
                 for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
                     if (r == 1) e = cudaEventRecord(e0, st);
-                    if (e == cudaSuccess) e = launch_hess_binary(h, Q, h->nc, 0, st, sm != 0, nt);
+                    if (e == cudaSuccess) e = launch_hess_binary(h, Q, h->nc, 0, st, kind, nt);
                 }
                 if (e == cudaSuccess) e = cudaEventRecord(e1, st);
                 if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -1441,17 +1612,17 @@ int tune_hess_shape(fednl_handle h)
                     cudaEventDestroy(e1);
                     return fail(FEDNL_ECUDA, "Hessian tuning launch failed: %s", cudaGetErrorString(e));
                 }
-                if (t / 2.0 < best.ms) best = Shape{sm != 0, nt, t / 2.0};
+                if (t / 2.0 < best.ms) best = Shape{kind, nt, t / 2.0};
             }
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         std::lock_guard<std::mutex> g(mu);
         cache[key] = best;
     }
-    const bool changed = best.sm != h->hess_smem_bits || best.nt != h->hess_nt;
-    h->hess_smem_bits = best.sm;
+    const bool changed = best.kind != h->hess_kind || best.nt != h->hess_nt;
+    h->hess_kind = best.kind;
     h->hess_nt = best.nt;
-    h->hess_smem = best.sm ? h->hess_smem_sm : h->hess_smem_gl;
     h->hess_ms = best.ms;
     return changed ? 1 : 0;
 }
@@ -1504,9 +1675,38 @@ int fednl_gpu_autotune_shapes(fednl_handle h, int32_t* hess_threads, int32_t* he
 {
     if (!h) return fail(FEDNL_EINVAL, "null handle");
     if (hess_threads) *hess_threads = h->binary ? h->hess_nt : kHessThreads;
-    if (hess_masks_in_smem) *hess_masks_in_smem = h->binary && h->hess_smem_bits ? 1 : 0;
+    if (hess_masks_in_smem) *hess_masks_in_smem = h->binary && h->hess_kind == kHessMasksSmem ? 1 : 0;
     if (ni_bucket) *ni_bucket = ni_bucket_of(h->maxn);
     if (hess_ms) *hess_ms = h->hess_ms;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_hess_schedule(fednl_handle h, int32_t* kind, int32_t* threads, int32_t* lists_built)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (kind) *kind = h->binary ? h->hess_kind : -1;
+    if (threads) *threads = h->binary ? h->hess_nt : kHessThreads;
+    if (lists_built) *lists_built = h->binary && h->hits_ready ? 1 : 0;
+    return FEDNL_OK;
+}
+
+int fednl_gpu_set_hess_schedule(fednl_handle h, int32_t kind, int32_t threads)
+{
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->binary) return fail(FEDNL_EINVAL, "the Hessian schedule applies to binary features only");
+    if (threads != 128 && threads != 256 && threads != 512) return fail(FEDNL_EINVAL, "threads must be 128, 256 or 512");
+    if (kind == kHessHits && !h->hits_ready) return fail(FEDNL_EINVAL, "no common-sample lists for this data");
+    if (kind == kHessMasksSmem && !h->hess_smem_sm) return fail(FEDNL_EINVAL, "the masks do not fit in shared memory");
+    if (kind < kHessMasksSmem || kind > kHessHits) return fail(FEDNL_EINVAL, "unknown Hessian kernel %d", kind);
+    CK(cudaStreamSynchronize(h->stream));
+    h->hess_kind = kind;
+    h->hess_nt = threads;
+    if (h->gexec) {                        // the captured round holds the old launch shape
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
+    }
     return FEDNL_OK;
 }
 

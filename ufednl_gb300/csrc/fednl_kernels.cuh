@@ -95,6 +95,11 @@ struct Dev {
     double* xprev;          // [d] x_k during the line search
     double* ls;             // [5] line search: t, -(dx . g), done, evaluations, solve succeeded
     unsigned* hdone;        // [nc] Hessian blocks of a client finished this round (the last one forms F)
+    // binary Hessian from the clients' static common-sample lists (k_hess_hits)
+    const unsigned short* hcode; // [nc][ustr] per upper position (see k_hess_hits)
+    const unsigned* hseg;        // [nc][nseg + 1] first multi-sample record of each segment
+    const unsigned* hrec;        // [records + 1] first common sample of each record in hhits
+    const unsigned short* hhits; // common samples of the multi-sample records, in sample order
     // the reference's arithmetic order (fednl_refmode.cuh)
     int ref;                // 1: FEDNL_ORDER_REFERENCE
     double* rref;           // [(d+1)(d+2)/2] Cholesky factor with y as column d
@@ -358,6 +363,36 @@ __device__ __forceinline__ double attr_sum(const unsigned long long* fb, int W, 
     return acc;
 }
 
+// The engine's fixed order for the attribute sums of {0,1} features (gradient and dsum): the
+// samples holding the attribute are taken in 64-sample words; a word's terms are summed in sample
+// order (its first term exactly), and the word sums are added to acc in word order (the CPU
+// oracle's blocked_attr_sum).  One FP64 add per set bit, in a single loop over the bits whose
+// adds are branch-free: a bit that opens a new word adds the finished word sum into acc, any other
+// bit adds its term into the open word sum.  The lanes of a warp then issue one FP64 instruction
+// per step of the longest bit list, not per word of it.
+__device__ __forceinline__ double attr_sum_blocked(const unsigned long long* fb, int W, const double* wv, double acc)
+{
+    int w = 0;
+    unsigned long long m = fb[0];
+    while (!m && ++w < W) m = fb[w];
+    if (!m) return acc;
+    int pw = w;
+    double part = wv[w * 64 + __ffsll((long long)m) - 1];
+    m &= m - 1;
+    for (;;) {
+        while (!m && ++w < W) m = fb[w];
+        if (!m) break;
+        const double v = wv[w * 64 + __ffsll((long long)m) - 1];
+        m &= m - 1;
+        const bool nw = w != pw;
+        const double sum = __dadd_rn(nw ? acc : part, nw ? part : v);
+        acc = nw ? sum : acc;
+        part = nw ? v : sum;
+        pw = w;
+    }
+    return __dadd_rn(acc, part);
+}
+
 // ---- 2. client gradients g_c = lambda x + sum_s Atr[:, s] q_s (samples in order) ----------
 // One block per (client, range of attributes); the client's weights are staged in shared memory.
 // The same bit loop also forms dsum_j = sum of D_s over the samples with attribute j set, which is
@@ -379,21 +414,28 @@ __global__ void k_grad_binary(Dev P)
     if (j >= P.d) return;
     const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
     const double* wv = s_w + (which ? n : 0);
-    const double acc = attr_sum(fb, W, wv, which ? 0.0 : __dmul_rn(P.x[j], P.lambda));
+    const double a0 = which ? 0.0 : __dmul_rn(P.x[j], P.lambda);
+    const double acc = P.ref ? attr_sum(fb, W, wv, a0) : attr_sum_blocked(fb, W, wv, a0);
     if (which) P.dsum[(size_t)c * P.d + j] = acc;
     else P.gc[(size_t)c * P.d + j] = acc;
 }
 
 // ---- 1 + 2 fused for binary features: one CTA per client -----------------------------------
 // The client's margins, sigmoid values and weights (k_margin_binary's operations, one sample per
-// thread), then its gradient and attribute sums (k_grad_binary's, a lane pair per attribute) with
-// the weights already in shared memory: one launch for the client oracle.  blockDim.x is a
-// multiple of 32.
+// thread), then its gradient and attribute sums (k_grad_binary's, blocked order, a lane pair per
+// attribute) with the weights already in shared memory: one launch for the client oracle.  When the
+// client's last attribute is an intercept (set in every sample), the block's last warp forms its two
+// sums alone: the word sums in parallel, one lane per word, then added in word order, so that the
+// longest chain of dependent adds is 63 + W instead of n.  blockDim.x is a multiple of 32.
 __global__ void k_client_binary(Dev P)
 {
-    extern __shared__ double s_w[];    // [n] b_s q_s, then [n] D_s
+    extern __shared__ double s_w[];    // [n] b_s q_s, [n] D_s, [2][W] intercept word sums
+    __shared__ double s_inv;
     const int c = blockIdx.x;
     const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    if (threadIdx.x == 0) s_inv = 1.0 / (double)n;      // one FP64 division per client
+    __syncthreads();
+    const double inv_m = s_inv;
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const int s = off + t;
         double acc = 0.0;
@@ -401,7 +443,6 @@ __global__ void k_client_binary(Dev P)
         const double b = P.lab[s];
         const double m = (b == 1.0) ? acc : -acc;
         const double sig = fednl_sigmoid(m);
-        const double inv_m = 1.0 / (double)n;
         const double z1 = __dsub_rn(1.0, sig);
         const double dv = __dmul_rn(inv_m, __dmul_rn(z1, sig));
         const double q = __dmul_rn(z1, -inv_m);
@@ -413,11 +454,39 @@ __global__ void k_client_binary(Dev P)
         s_w[n + t] = dv;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < 2 * P.d; t += blockDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const bool icw = P.icpt[c] != 0;
+    if (icw && warp == nw - 1) {
+        double* part = s_w + 2 * n;
+        for (int t = lane; t < 2 * W; t += 32) {
+            const int which = t >= W ? 1 : 0, w = t - which * W;
+            const double* v = s_w + which * n + w * 64;
+            double a = v[0];
+            if (w * 64 + 64 <= n) {
+#pragma unroll 21
+                for (int k = 1; k < 64; ++k) a = __dadd_rn(a, v[k]);
+            } else {
+                for (int k = 1; k < n - w * 64; ++k) a = __dadd_rn(a, v[k]);
+            }
+            part[t] = a;
+        }
+        __syncwarp();
+        if (lane < 2) {
+            const int j = P.d - 1;
+            double acc = lane ? 0.0 : __dmul_rn(P.x[j], P.lambda);
+            for (int w = 0; w < W; ++w) acc = __dadd_rn(acc, part[lane * W + w]);
+            if (lane) P.dsum[(size_t)c * P.d + j] = acc;
+            else P.gc[(size_t)c * P.d + j] = acc;
+        }
+        return;
+    }
+    const int nt = icw ? blockDim.x - 32 : blockDim.x;
+    const int na = icw ? P.d - 1 : P.d;
+    for (int t = threadIdx.x; t < 2 * na; t += nt) {
         const int j = t >> 1, which = t & 1;
         const unsigned long long* fb = P.fbits + P.fboff[c] + (size_t)j * W;
         const double* wv = s_w + (which ? n : 0);
-        const double acc = attr_sum(fb, W, wv, which ? 0.0 : __dmul_rn(P.x[j], P.lambda));
+        const double acc = attr_sum_blocked(fb, W, wv, which ? 0.0 : __dmul_rn(P.x[j], P.lambda));
         if (which) P.dsum[(size_t)c * P.d + j] = acc;
         else P.gc[(size_t)c * P.d + j] = acc;
     }
@@ -444,8 +513,8 @@ __global__ void k_grad_dense(Dev P)
 // entry is the in-order sum of D_s over the samples where both attributes are set (bitmask
 // AND).  Then + lambda on the diagonal.  mode 0: diff = H_i - shift_i (TopK.h:70-71) and the
 // partial sums of ||diff||_F^2 over the full symmetric matrix; mode 1: shift_i = H_i(x0); mode 2
-// (FedNL-PP): mode 0 and H_i kept for the Lk taken after the shift update.  Grid y runs over the
-// processed clients (P.act).
+// (FedNL-PP): mode 0 and H_i kept for the Lk taken after the shift update; mode 3: the difference
+// only (the selection kernel forms the norms).  Grid y runs over the processed clients (P.act).
 constexpr int kHessThreads = 256;
 constexpr int kHessPerBlock = 4096;     // upper entries per block
 
@@ -573,16 +642,18 @@ __global__ void __launch_bounds__(NT) k_hess_binary(Dev P, int mode)
             if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
-            const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
-            if (i == j) fa = r;
-            else fb2 = r;
+            if (mode != 3) {
+                const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
+                if (i == j) fa = r;
+                else fb2 = r;
+            }
         }
     }
-    if (mode != 1 && p_seg < P.U) {
+    if ((mode == 0 || mode == 2) && p_seg < P.U) {
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
-    if (mode != 1 && !P.ref) client_fsum_last_block(P, c);
+    if ((mode == 0 || mode == 2) && !P.ref) client_fsum_last_block(P, c);
 }
 
 // dense FP64: the reference's per-entry order u_i (D_s u_j), samples in order
@@ -615,16 +686,18 @@ __global__ void __launch_bounds__(kHessThreads) k_hess_dense(Dev P, int mode)
             if (mode == 2) P.hbuf[base + p] = h;
             const double df = __dsub_rn(h, P.shift[base + p]);
             P.diff[base + p] = df;
-            const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
-            if (i == j) fa = r;
-            else fb2 = r;
+            if (mode != 3) {
+                const double r = fma(df, df, i == j ? fa : fb2);     // one FP64 instruction per warp
+                if (i == j) fa = r;
+                else fb2 = r;
+            }
         }
     }
-    if (mode != 1 && p_seg < P.U) {
+    if ((mode == 0 || mode == 2) && p_seg < P.U) {
         const double cs = chunk_tree(segment_value(fa, fb2));
         if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
     }
-    if (mode != 1 && !P.ref) client_fsum_last_block(P, c);
+    if ((mode == 0 || mode == 2) && !P.ref) client_fsum_last_block(P, c);
 }
 
 // master H = mean_i shift_i after the initial shifts (TrainLoop.h:639-643, :732-735)
@@ -858,6 +931,138 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     }
 }
 
+// The binary Hessian (k_hess_binary's sums: in-order over the samples holding both attributes,
+// the first term exact) from lists of common samples built once from the static features, so no
+// masks are intersected in the rounds.  hcode[p] describes upper position p:
+//   < 0x7fff           the one sample holding both attributes: the entry is D_s
+//   0x7fff             no such sample: 0
+//   0x8000 | m         the segment's m-th entry with several common samples (a record)
+//   0xa000 | i         intercept column (i, d-1): dsum_i
+//   0xc000 | i         diagonal (i, i): dsum_i + lambda
+// Each warp owns a segment of 512 positions.  Its lane 0 first starts bulk copies of the segment's
+// codes and shift values into shared memory (one mbarrier per warp); while they fly the block stages
+// D_s and dsum and the warp sums its segment's records, a lane per record (the warp's FP64
+// instructions then serve up to 32 multi-sample entries at once, not the few lanes of a 32-position
+// row that hold one).  Then the positions are formed from shared memory as k_hess_binary forms them.
+constexpr unsigned kHitNone = 0x7fffu;
+
+__host__ __device__ inline size_t hits_stage_bytes(int nt) { return (size_t)(nt / 32) * 512 * 10; }
+
+__device__ __forceinline__ void bulk_copy_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_hess_hits(Dev P, int mode, int maxrec)
+{
+    // [NT / 32][512] shift values, [NT / 32][512] codes, [n] D_s, [d] dsum, [d] diagonal values,
+    // [NT / 32][maxrec] record sums
+    extern __shared__ __align__(16) double s_hx[];
+    __shared__ __align__(8) unsigned long long s_bar[NT / 32];
+    const int c = P.act ? P.act[blockIdx.y] : blockIdx.y;
+    const int n = P.ns[c], off = P.soff[c];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = blockIdx.x * (NT / 32) + warp;
+    const int p_seg = seg * 512;
+    const bool live = p_seg < P.U;
+    const int cnt = live ? min(512, P.U - p_seg) : 0;
+    const size_t base = (size_t)c * P.ustr;
+    double* s_sh = s_hx + (size_t)warp * 512;
+    unsigned short* s_cd = reinterpret_cast<unsigned short*>(s_hx + (size_t)(NT / 32) * 512) + warp * 512;
+    if (live && lane == 0) {
+        // rows start 16-byte aligned (ustr is a multiple of 32, segments of 512); sizes rounded up to
+        // 16 bytes stay inside the client's row of ustr entries
+        const unsigned bc = (unsigned)((cnt * 2 + 15) & ~15), bs = mode != 1 ? (unsigned)((cnt * 8 + 15) & ~15) : 0u;
+        mbar_init(&s_bar[warp]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&s_bar[warp])),
+                     "r"(bc + bs)
+                     : "memory");
+        bulk_copy_1d(s_cd, P.hcode + base + p_seg, bc, &s_bar[warp]);
+        if (bs) bulk_copy_1d(s_sh, P.shift + base + p_seg, bs, &s_bar[warp]);
+    }
+    double* s_D = s_hx + (size_t)(NT / 32) * 640;
+    double* s_ds = s_D + n;
+    double* s_dl = s_ds + P.d;
+    const double* dsum = P.dsum + (size_t)c * P.d;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s_D[t] = P.Dv[off + t];
+    for (int t = threadIdx.x; t < P.d; t += blockDim.x) {
+        const double v = dsum[t];
+        s_ds[t] = v;
+        s_dl[t] = __dadd_rn(v, P.lambda);
+    }
+    __syncthreads();
+
+    double* s_r = s_dl + P.d + (size_t)warp * maxrec;
+    double fa = 0.0, fb2 = 0.0;
+    if (live) {
+        const unsigned* sg = P.hseg + (size_t)c * (P.nseg + 1) + seg;
+        const unsigned r0 = sg[0], r1 = sg[1];
+        for (unsigned b = r0; b < r1; b += 32) {
+            const unsigned r = b + lane;
+            if (r < r1) {
+                const unsigned e0 = P.hrec[r], e1 = P.hrec[r + 1];
+                double h = s_D[P.hhits[e0]];
+                unsigned e = e0 + 1;
+                for (; e + 4 <= e1; e += 4) {     // four indices and values loaded ahead of the adds
+                    const double v0 = s_D[P.hhits[e]], v1 = s_D[P.hhits[e + 1]];
+                    const double v2 = s_D[P.hhits[e + 2]], v3 = s_D[P.hhits[e + 3]];
+                    h = __dadd_rn(h, v0);
+                    h = __dadd_rn(h, v1);
+                    h = __dadd_rn(h, v2);
+                    h = __dadd_rn(h, v3);
+                }
+                for (; e < e1; ++e) h = __dadd_rn(h, s_D[P.hhits[e]]);
+                s_r[r - r0] = h;
+            }
+        }
+        __syncwarp();
+        if (!mbar_wait(&s_bar[warp], 0u)) {     // a copy never completed: report it, form nothing
+            if (lane == 0) {
+                mbar_wait(&s_bar[warp], 0u);
+                atomicExch(P.status, -5);     // FEDNL_ETIMEOUT
+            }
+        } else {
+            for (int q = 0; q < 16; ++q) {
+                const int t = 32 * q + lane;
+                if (t >= cnt) break;
+                const int p = p_seg + t;
+                const unsigned cd = s_cd[t];
+                double h;
+                bool diag = false;
+                if (cd < kHitNone) h = s_D[cd];
+                else if (cd == kHitNone) h = 0.0;
+                else if (cd >= 0xc000u) {
+                    h = s_dl[cd & 0x3fffu];
+                    diag = true;
+                } else if (cd >= 0xa000u) h = s_ds[cd & 0x1fffu];
+                else h = s_r[cd & 0x1fffu];
+                if (mode == 1) {
+                    P.shift[base + p] = h;
+                } else {
+                    if (mode == 2) P.hbuf[base + p] = h;
+                    const double df = __dsub_rn(h, s_sh[t]);
+                    P.diff[base + p] = df;
+                    if (mode != 3) {
+                        const double r = fma(df, df, diag ? fa : fb2);     // one FP64 instruction per warp
+                        if (diag) fa = r;
+                        else fb2 = r;
+                    }
+                }
+            }
+        }
+    }
+    if ((mode == 0 || mode == 2) && live) {
+        const double cs = chunk_tree(segment_value(fa, fb2));
+        if (lane == 0) P.Fpart[(size_t)c * P.nseg + seg] = cs;
+    }
+    if ((mode == 0 || mode == 2) && !P.ref) client_fsum_last_block(P, c);
+}
+
 // Worker w's draws.  FRESH: the flags were written by other CTAs of the same launch (read through
 // L2, selection words and counts updated atomically).
 template <bool FRESH>
@@ -932,16 +1137,22 @@ __device__ __forceinline__ void master_g(const MasterAgg& A, int j)
     A.g[j] = __dmul_rn(g, A.inv_n);
 }
 
-// l by one warp: 32 values loaded at a time, added in client order
-__device__ __forceinline__ void master_l(const MasterAgg& A, int lane)
+// l = (1/n) sum_c Lk_c by one warp: 32 values loaded at a time, added in client order
+__device__ __forceinline__ double lk_mean(const double* lk, int nc, double inv_n, int lane)
 {
     double l = 0.0;
-    for (int c0 = 0; c0 < A.nc; c0 += 32) {
-        const double v = (c0 + lane < A.nc) ? A.lk[c0 + lane] : 0.0;
-        const int cnt = min(32, A.nc - c0);
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+        const double v = (c0 + lane < nc) ? lk[c0 + lane] : 0.0;
+        const int cnt = min(32, nc - c0);
         for (int t = 0; t < cnt; ++t) l = __dadd_rn(l, __shfl_sync(0xffffffffu, v, t));
     }
-    if (lane == 0) A.stats[1] = __dmul_rn(l, A.inv_n);
+    return __dmul_rn(l, inv_n);
+}
+
+__device__ __forceinline__ void master_l(const MasterAgg& A, int lane)
+{
+    const double l = lk_mean(A.lk, A.nc, A.inv_n, lane);
+    if (lane == 0) A.stats[1] = l;
 }
 
 // Work fused into k_select.  TopLEK's rounding draws: the launch's last CTA to finish (counted on
@@ -953,7 +1164,63 @@ struct SelectDraws {
     int n_mat, W;
     unsigned* wstate;
     MasterAgg agg;
+    // norms != 0: warps 1-3 form the client's ||diff||_F^2 (F, its segment sums in fpart) and Lk
+    int norms, nseg;
+    double* fpart;     // [n_mat][nseg]
+    double* lk;        // [n_mat]
 };
+
+// The difference's squared Frobenius norm in the fixed segment order (k_hess_binary's, the CPU
+// oracle's orc_frob_sym) and Lk = sqrt of it (TopK.h:74-78), formed by warps 1-3 of the selection
+// kernel while warp 0 walks the heap: segment seg holds 512 upper positions, lane l squares
+// positions 32 q + l into fused multiply-adds (diagonal and off-diagonal apart, loaded ahead) and
+// gives a + 2 b to the segment's halving tree; warp 1 then adds the segment sums in order.
+__device__ __forceinline__ void select_norms(const SelectDraws& dr, const double* __restrict__ v, int U, int c,
+                                          double* F, int warp, int lane)
+{
+    double* fp = dr.fpart + (size_t)c * dr.nseg;
+    for (int seg = warp - 1; seg < dr.nseg; seg += 3) {
+        const int p_seg = seg * 512;
+        double x[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int p = p_seg + 32 * q + lane;
+            x[q] = p < U ? v[p] : 0.0;
+        }
+        double fa = 0.0, fb2 = 0.0;
+        int i, j;
+        upper_ij(p_seg + lane, i, j);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            if (p_seg + 32 * q + lane >= U) break;
+            if (q > 0) {
+                i += 32;
+                while (i > j) {
+                    i -= j + 1;
+                    ++j;
+                }
+            }
+            const double r = fma(x[q], x[q], i == j ? fa : fb2);
+            if (i == j) fa = r;
+            else fb2 = r;
+        }
+        const double cs = chunk_tree(segment_value(fa, fb2));
+        if (lane == 0) fp[seg] = cs;
+    }
+    asm volatile("bar.sync 1, 96;" ::: "memory");
+    if (warp == 1) {
+        double f = 0.0;
+        for (int q0 = 0; q0 < dr.nseg; q0 += 32) {
+            const double t = (q0 + lane < dr.nseg) ? fp[q0 + lane] : 0.0;
+            const int cnt = min(32, dr.nseg - q0);
+            for (int u = 0; u < cnt; ++u) f = __dadd_rn(f, __shfl_sync(0xffffffffu, t, u));
+        }
+        if (lane == 0) {
+            F[c] = f;
+            dr.lk[c] = sqrt(f);
+        }
+    }
+}
 
 __device__ __forceinline__ void select_finish(const SelectDraws& dr, const int* needs, const double* pdraw,
                                               const int* minidx, unsigned* sel, int SW, int* cnt)
@@ -975,7 +1242,7 @@ __device__ __forceinline__ void select_finish(const SelectDraws& dr, const int* 
 // squared Frobenius norms.  Output: sel bitmap per matrix, cnt (entries kept before the rounding
 // draw), TopLEK draw request.  err: set to 1 if a bounded wait ran out.
 __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int ustr, int U, int k,
-                                                        int lek, double delta, const double* __restrict__ F,
+                                                        int lek, double delta, double* F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
                                                         double* pdraw, int* minidx, int* err, const int* act,
                                                         int ref, SelectDraws dr)
@@ -999,10 +1266,13 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
             cnt[c] = U;
             if (needs) needs[c] = 0;
         }
+        if (dr.norms && warp != 0) select_norms(dr, v, U, c, F, warp, lane);
         if (dr.agg.gc && blockIdx.x == 0 && warp != 0) {
-            if (warp == 1) master_l(dr.agg, lane);
-            else
+            if (warp == 1) {
+                if (dr.agg.lk) master_l(dr.agg, lane);
+            } else {
                 for (int j = tid - 64; j < dr.agg.d; j += blockDim.x - 64) master_g(dr.agg, j);
+            }
         }
         select_finish(dr, needs, pdraw, minidx, sel, SW, cnt);
         return;
@@ -1050,10 +1320,13 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
     }
     // scan, SpecialMathRoutinesForMatrix.h:300-318
     if (warp != 0) {
+        if (dr.norms) select_norms(dr, v, U, c, F, warp, lane);
         if (dr.agg.gc && blockIdx.x == 0) {      // the master's aggregation beside the heap walk
-            if (warp == 1) master_l(dr.agg, lane);
-            else
+            if (warp == 1) {
+                if (dr.agg.lk) master_l(dr.agg, lane);
+            } else {
                 for (int j = tid - 64; j < dr.agg.d; j += blockDim.x - 64) master_g(dr.agg, j);
+            }
         }
     } else {
         unsigned long long root = h.key[0];
@@ -1152,7 +1425,7 @@ __global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int u
         }
         __syncthreads();
         if (warp == 0) {
-            const double fr = F[c];
+            const double fr = __ldcg(F + c);     // formed by warp 1 when the norms are formed here
             double num0;
             if (ref) {   // the reference's order: ||M||^2 minus each heap term in heap-array order
                 double nm = fr;
@@ -1776,7 +2049,9 @@ struct GridSync {
 // The solve of one problem by a group of G cooperating CTAs (this CTA is number bid of the group);
 // the grid barrier counts the group's CTAs on P.bar.
 // apply_first: the round's master merge (k_apply's work) runs first, each warp a selection word at
-// a time, and the system is formed from the merged H (Hin must be P.H, packed).
+// a time, and the system is formed from the merged H (Hin must be P.H, packed).  apply_first 2:
+// also l = (1/n) sum_c Lk_c (master_l's order) is formed here, by warp 0 of every CTA while the
+// other warps merge, and added to the diagonal once known (lptr is not read).
 __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict__ Hin, int hin_lda, const double* lptr,
                                           double lval, const double* __restrict__ gin, double* dxout, double* xupd,
                                           int record, unsigned G, unsigned bid, GridSync& gs, int apply_first = 0)
@@ -1789,8 +2064,9 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
     __shared__ double s_yb[2][32];
+    __shared__ double s_l;
     int ent_nb = -1;
-    const double l = lptr ? *lptr : lval;
+    double l = (lptr && apply_first != 2) ? *lptr : lval;
     const int d = P.d;
     const int D = d + 1;                       // augmented by the right-hand side
     const int UA = D * (D + 1) / 2;
@@ -1801,17 +2077,36 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     const int gtid = bid * blockDim.x + tid, gthreads = G * blockDim.x;
     if (apply_first) {
         const int U = d * (d + 1) / 2;
-        for (int wd = gtid >> 5; wd < (U + 31) >> 5; wd += gthreads >> 5) {
-            const int p = wd * 32 + lane;
-            const double hv = apply_word(P, p, lane);
-            if (p < U) {
-                P.H[p] = hv;
-                int i, j;
-                upper_ij(p, i, j);
-                A[p] = (i == j) ? __dadd_rn(hv, l) : hv;
+        const bool own_l = apply_first == 2;
+        const int nmw = own_l ? kCoopThreads / 32 - 1 : kCoopThreads / 32;    // merging warps per CTA
+        const int NMW = (int)G * nmw;
+        if (own_l && warp == 0) {
+            const double lm = lk_mean(P.lk, P.nc, P.inv_n, lane);
+            if (lane == 0) {
+                s_l = lm;
+                if (bid == 0) P.stats[1] = lm;
+            }
+        } else {
+            for (int wd = (int)bid * nmw + (own_l ? warp - 1 : warp); wd < (U + 31) >> 5; wd += NMW) {
+                const int p = wd * 32 + lane;
+                const double hv = apply_word(P, p, lane);
+                if (p < U) {
+                    P.H[p] = hv;
+                    int i, j;
+                    upper_ij(p, i, j);
+                    A[p] = (i == j && !own_l) ? __dadd_rn(hv, l) : hv;
+                }
             }
         }
         for (int p = U + gtid; p < UA; p += gthreads) A[p] = (p - U < d) ? gin[p - U] : 0.0;    // column d
+        if (own_l) {     // + l on the diagonal entries this CTA's warps merged
+            __syncthreads();
+            l = s_l;
+            for (int jj = tid; jj < d; jj += blockDim.x) {
+                const int p = jj * (jj + 1) / 2 + jj;
+                if (((p >> 5) % NMW) / nmw == (int)bid) A[p] = __dadd_rn(P.H[p], l);
+            }
+        }
     } else {
         for (int p = gtid; p < UA; p += gthreads) {
             int i, j;
@@ -2033,12 +2328,31 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 P.stats[0] = sqrt(t);
             }
         }
-        __syncthreads();
         // Blocks of 32 rows from the bottom.  Warp 0 solves a block (lane = row, the block's
-        // triangle and 1/r_tt in registers), then applies the block's solution to the next block's
-        // rows, which it keeps in registers; meanwhile warps 1-7 apply it to all rows above.  A row
-        // receives its updates in descending t order whichever warp applies them.
+        // triangle in registers), then applies the block's solution to the next block's rows, which
+        // it keeps in registers; meanwhile warps 1-3 and 5-7 apply it to all rows above.  Warp 4
+        // shares warp 0's sub-partition and runs no FP64 instruction: it stages the triangle (Db)
+        // and the rectangle of the update (Rb) of the block after the current one into shared
+        // memory, each as soon as warp 0 has taken the current one into registers (named barriers
+        // 3 and 2), so warp 0 reads no global memory.  A row receives its updates in descending t
+        // order whichever warp applies them.
         const int nblocks = (d + 31) / 32;
+        auto stage_t = [&](int blk) {
+            const int b1 = d - 32 * blk, b0 = max(0, b1 - 32), nbk = b1 - b0;
+#pragma unroll 8
+            for (int s = 0; s < 32; ++s) Db[lane][s] = (lane < s && s < nbk) ? A[up_pos(b0 + lane, b0 + s)] : 0.0;
+        };
+        auto stage_r = [&](int blk) {
+            const int b1 = d - 32 * blk, b0 = max(0, b1 - 32), nbk = b1 - b0, n0 = max(0, b0 - 32);
+#pragma unroll 8
+            for (int s = 0; s < 32; ++s)
+                Rb[lane][s] = (s < nbk && n0 + lane < b0) ? A[up_pos(n0 + lane, b0 + s)] : 0.0;
+        };
+        if (warp == 4) {
+            stage_t(0);
+            stage_r(0);
+        }
+        __syncthreads();
         double v = 0.0;
         if (tid < 32) {
             const int b1 = d, b0 = max(0, d - 32);
@@ -2049,7 +2363,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             if (tid < 32) {
                 double ar[32];
 #pragma unroll
-                for (int s = 0; s < 32; ++s) ar[s] = (lane < s && s < nbk) ? A[up_pos(b0 + lane, b0 + s)] : 0.0;
+                for (int s = 0; s < 32; ++s) ar[s] = Db[lane][s];
+                asm volatile("bar.arrive 3, 64;" ::: "memory");   // warp 4 may refill Db
 #pragma unroll
                 for (int s = 31; s >= 0; --s) {
                     if (s < nbk) {
@@ -2061,23 +2376,31 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                     y[b0 + lane] = v;
                     s_yb[blk & 1][lane] = v;
                 }
+            } else if (warp == 4) {
+                asm volatile("bar.sync 3, 64;" ::: "memory");
+                if (blk + 1 < nblocks) stage_t(blk + 1);
             }
             __syncthreads();
             const int n0 = max(0, b0 - 32);                 // next block: rows [n0, b0)
             if (tid < 32) {
+                double av[32];
+#pragma unroll
+                for (int s = 0; s < 32; ++s) av[s] = Rb[lane][s];
+                asm volatile("bar.arrive 2, 64;" ::: "memory");   // warp 4 may refill Rb
                 if (b0 > 0) {
                     const int i = n0 + lane;
-                    double av[32];
-#pragma unroll
-                    for (int s = 0; s < 32; ++s) av[s] = (s < nbk && i < b0) ? A[up_pos(i, b0 + s)] : 0.0;
                     double w = (i < b0) ? y[i] : 0.0;
 #pragma unroll
                     for (int s = 31; s >= 0; --s)
                         if (s < nbk) w = fma(-av[s], s_yb[blk & 1][s], w);
                     v = w;
                 }
+            } else if (warp == 4) {
+                asm volatile("bar.sync 2, 64;" ::: "memory");
+                if (blk + 1 < nblocks) stage_r(blk + 1);
             } else {
-                for (int i = tid - 32; i < n0; i += blockDim.x - 32) {
+                const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
+                for (int i = ut; i < n0; i += blockDim.x - 64) {
                     double av[32];
 #pragma unroll
                     for (int s = 0; s < 32; ++s) av[s] = (s < nbk) ? A[up_pos(i, b0 + s)] : 0.0;

@@ -27,6 +27,7 @@ STATUS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTPD", -5: "E
 # shared memory with one refinement step (d up to about 300); FP32 Cholesky on a cooperative grid
 # with FP64-residual refinement to 2^-30 relative, six steps at most (d up to 1312)
 SOLVERS = {"fp64": 0, "fp32_refined": 1, "fp32_coop": 2}
+HESS_KERNELS = ["masks_smem", "masks_global", "lists"]   # fednl_gpu_hess_schedule kinds 0, 1, 2
 
 
 class FedNLError(RuntimeError):
@@ -76,7 +77,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_mx_set_solver", "fednl_gpu_encode_client_round", "fednl_gpu_get_client_grad", "fednl_gpu_get_diff",
            "fednl_gpu_autotune", "fednl_gpu_autotune_shapes", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
            "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate",
-           "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref"]
+           "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref",
+           "fednl_gpu_hess_schedule", "fednl_gpu_set_hess_schedule"]
 
 _lib = None
 
@@ -161,7 +163,8 @@ def load(build_if_missing: bool = True):
                                                          C.POINTER(C.c_int64)],
                        "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp],
                        "fednl_gpu_autotune": [vp, ip, dp], "fednl_gpu_autotune_shapes": [vp, ip, ip, ip, dp],
-                       "fednl_mx_autotune": [vp, ip, ip, dp]}.items():
+                       "fednl_mx_autotune": [vp, ip, ip, dp], "fednl_gpu_hess_schedule": [vp, ip, ip, ip],
+                       "fednl_gpu_set_hess_schedule": [vp, C.c_int32, C.c_int32]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -308,9 +311,10 @@ class FedNL:
     def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
                  seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0,
                  clients_per_round: int = 0, client_seed: int = 1234, option_a: bool = False,
-                 line_search=None, track_f: bool = False, order: str = "fixed"):
+                 line_search=None, track_f: bool = False, order: str = "fixed", hess_schedule=None):
         """order: "fixed" (the engine's own order, bit-identical to the test oracle) or "reference"
-        (the reference's operation order, bit-identical to the reference's rounds)."""
+        (the reference's operation order, bit-identical to the reference's rounds).  hess_schedule:
+        (kernel, threads) of the binary Hessian from the initial shifts on (see set_hess_schedule)."""
         self.d = prob.d
         self.lda = lda or reference_lda(prob.d)
         self.n_clients = prob.n_clients
@@ -331,6 +335,8 @@ class FedNL:
             f = np.ascontiguousarray(prob.features, dtype=np.float64)
             b = np.ascontiguousarray(prob.labels, dtype=np.float64)
             _check(load().fednl_gpu_upload_client_data(self._h, _dp(f), _dp(b)))
+            if hess_schedule is not None:
+                self.set_hess_schedule(*hess_schedule)
             xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
             _check(load().fednl_gpu_init_shifts(self._h, _dp(xx) if xx is not None else None))
         except Exception:
@@ -369,8 +375,24 @@ class FedNL:
         b = np.zeros(1, dtype=np.int32)
         hms = np.zeros(1)
         _check(load().fednl_gpu_autotune_shapes(self._h, _ip(nt), _ip(sm), _ip(b), _dp(hms)))
-        return {"chol_ctas": int(g[0]), "solve_ms": float(ms[0]), "hess_threads": int(nt[0]),
-                "hess_masks_in_smem": bool(sm[0]), "ni_bucket": int(b[0]), "hess_ms": float(hms[0])}
+        out = {"chol_ctas": int(g[0]), "solve_ms": float(ms[0]), "hess_threads": int(nt[0]),
+               "hess_masks_in_smem": bool(sm[0]), "ni_bucket": int(b[0]), "hess_ms": float(hms[0])}
+        out["hess_kernel"] = self.hess_schedule()["kernel"]
+        return out
+
+    def hess_schedule(self) -> dict:
+        """The binary Hessian's kernel ("masks_smem", "masks_global", "lists"), threads per block, and
+        whether the common-sample lists were built at upload."""
+        k = np.zeros(1, dtype=np.int32)
+        nt = np.zeros(1, dtype=np.int32)
+        built = np.zeros(1, dtype=np.int32)
+        _check(load().fednl_gpu_hess_schedule(self._h, _ip(k), _ip(nt), _ip(built)))
+        return {"kernel": HESS_KERNELS[int(k[0])] if k[0] >= 0 else None, "threads": int(nt[0]),
+                "lists_built": bool(built[0])}
+
+    def set_hess_schedule(self, kernel: str, threads: int = 256):
+        """Overrides the binary Hessian's kernel and threads per block (results do not change)."""
+        _check(load().fednl_gpu_set_hess_schedule(self._h, HESS_KERNELS.index(kernel), threads))
 
     def client_phase(self):
         """Launches the round up to the master's aggregation (no wait); solve_batch ends it."""
