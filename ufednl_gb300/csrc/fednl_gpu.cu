@@ -571,6 +571,15 @@ cudaError_t launch_hess_binary_t(const Dev& Q, int nseg, size_t smem, int nclien
     return cudaGetLastError();
 }
 
+// the binary Hessian's mode in the captured round: the difference only when the selection kernel
+// forms the norms (TopK / TopLEK in the fixed order, Option B, not FedNL-PP), else with them
+int round_hess_mode(fednl_handle h)
+{
+    if (h->pp) return 2;
+    const bool sel = h->comp == FEDNL_TOPK || h->comp == FEDNL_TOPLEK;
+    return sel && !h->dev.ref && !h->desc.option_a ? 3 : 0;
+}
+
 size_t hits_smem(fednl_handle h, int nt)
 {
     return hits_stage_bytes(nt) + ((size_t)h->maxn + 2 * h->d + (size_t)(nt / 32) * h->hits_maxrec) * 8;
@@ -662,7 +671,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     // and Lk (the Hessian writes the difference only), and the solve forms l from Lk while it merges
     const bool norms_in_select = agg_in_select && apply_in_solve && !h->desc.option_a;
     MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
-    const int hmode = h->pp ? 2 : norms_in_select ? 3 : 0;
+    const int hmode = h->pp ? 2 : norms_in_select ? 3 : 0;     // round_hess_mode(h) in the captured round
     if (h->binary) {
         CK(launch_hess_binary(h, P, na, hmode, st, h->hess_kind, h->hess_nt));
     } else {
@@ -754,7 +763,8 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     if (client_phase_only) return FEDNL_OK;
     const fednl_problem_desc& D = h->desc;
     const double* lptr = D.option_a ? nullptr : P.stats + 1;      // Option A: H + lambda I
-    CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(unsigned), st));      // barrier words and error flag start at zero
+    // barrier words and error flag start at zero (the binary client oracle zeroes them at the round's start)
+    if (!(h->binary && !P.ref)) CK(cudaMemsetAsync(P.bar, 0, 4 * sizeof(unsigned), st));
     if (P.ref) {
         MARK("k_chol_ref");
         CK(launch_chol_ref(P, h->ref_grid, st, lptr, P.lambda, P.dx, D.line_search ? nullptr : P.x, 1));
@@ -1577,7 +1587,8 @@ int tune_hess_shape(fednl_handle h)
     };
     static std::mutex mu;
     static std::map<std::pair<int, int>, Shape> cache;
-    const std::pair<int, int> key(h->d, ni_bucket_of(h->maxn) + (h->hess_smem_sm ? 0 : 64) + (h->hits_ready ? 0 : 128));
+    const std::pair<int, int> key(h->d, ni_bucket_of(h->maxn) + (h->hess_smem_sm ? 0 : 64) + (h->hits_ready ? 0 : 128) +
+                                            (round_hess_mode(h) == 3 ? 256 : 0));
     Shape best{h->hess_kind, h->hess_nt, 0.0};
     bool hit = false;
     {
@@ -1598,10 +1609,11 @@ int tune_hess_shape(fednl_handle h)
         for (int kind : {kHessHits, kHessMasksSmem, kHessMasksGlobal}) {
             if ((kind == kHessHits && !h->hits_ready) || (kind == kHessMasksSmem && !h->hess_smem_sm)) continue;
             for (int nt : {128, 256, 512}) {
-                cudaError_t e = launch_hess_binary(h, Q, h->nc, 0, st, kind, nt);   // warm-up
+                const int mode = round_hess_mode(h) == 3 ? 3 : 0;
+                cudaError_t e = launch_hess_binary(h, Q, h->nc, mode, st, kind, nt);   // warm-up
                 for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
                     if (r == 1) e = cudaEventRecord(e0, st);
-                    if (e == cudaSuccess) e = launch_hess_binary(h, Q, h->nc, 0, st, kind, nt);
+                    if (e == cudaSuccess) e = launch_hess_binary(h, Q, h->nc, mode, st, kind, nt);
                 }
                 if (e == cudaSuccess) e = cudaEventRecord(e1, st);
                 if (e == cudaSuccess) e = cudaEventSynchronize(e1);

@@ -433,6 +433,8 @@ __global__ void k_client_binary(Dev P)
     __shared__ double s_inv;
     const int c = blockIdx.x;
     const int n = P.ns[c], W = (n + 63) >> 6, off = P.soff[c];
+    // the round's solve finds its grid-barrier words and error flag at zero (no solve runs now)
+    if (c == 0 && threadIdx.x < 4) P.bar[threadIdx.x] = 0u;
     if (threadIdx.x == 0) s_inv = 1.0 / (double)n;      // one FP64 division per client
     __syncthreads();
     const double inv_m = s_inv;
