@@ -129,6 +129,9 @@ def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
     nc = prob.n_clients
     S = prob.total_samples
     words = int(sum(d * ((int(n) + 63) // 64) for n in prob.n_samples))
+    if kernel == "k_hess_hits":
+        # read every client's shift, write its difference (packed upper FP64), read D
+        return nc * U * 16.0 + S * 8.0, "shift read + diff write (packed upper, FP64) per client, D_s read"
     if kernel.startswith("k_hess"):
         # read every client's shift, write its difference (packed upper FP64), read bitmasks and D
         return nc * U * 16.0 + words * 8.0 + S * 8.0, "shift read + diff write (packed upper, FP64) per client"
@@ -142,11 +145,11 @@ def algorithmic_bytes(kernel: str, prob, k: int) -> tuple[float, str]:
 
 
 def hess_fp64_ops(prob) -> float:
-    """FP64 operations of one k_hess_binary launch: for every client and upper entry (i, j) one add
-    per sample after the first with both attributes set (the in-order sum of D_s; the first term is
-    exact and costs none), the diagonal's + lambda (the intercept column is the attribute's D_s sum,
-    already formed), then the difference and the fused square-add into the entry's norm
-    accumulator (2 more)."""
+    """FP64 operations of one binary Hessian launch in the TopK / TopLEK round: for every client and
+    upper entry (i, j) one add per sample after the first with both attributes set (the in-order sum
+    of D_s; the first term is exact and costs none), the diagonal's + lambda (the intercept column is
+    the attribute's D_s sum, already formed), then the difference (1 more; the squares of the norm
+    are formed by the selection kernel)."""
     d = prob.d
     U = d * (d + 1) // 2
     tot = 0.0
@@ -157,7 +160,7 @@ def hess_fp64_ops(prob) -> float:
         if a.shape[0] and np.all(a[:, -1] == 1.0):
             off[:, -1] = 0.0
         tot += float(np.maximum(off - 1.0, 0.0).sum()) + d
-    return tot + 2.0 * prob.n_clients * U
+    return tot + 1.0 * prob.n_clients * U
 
 
 # what limits each FP64 round kernel, in words (the roofline entries give the numbers)
@@ -166,6 +169,7 @@ SLOWEST_BOUND = {
                 "the launch lasts as long as its slowest client)",
     "k_chol_coop": "latency (per-column FP64 dependency chain and grid barriers)",
     "k_hess_binary": "instruction issue and the FP64 pipe (in-order sums over bit-mask intersections)",
+    "k_hess_hits": "latency of the record sums and the FP64 pipe (differences and in-order sums), HBM third",
 }
 
 
@@ -561,16 +565,17 @@ def run_ours(args, ws, rank, local, td):
     hsrc = f"{src} (MEASURED_PEAKS.json hbm_gbs)"
     fsrc = "measured by fednl_gpu_fp64_rate in this run (independent FP64 add chains, all SMs)"
     # the kernels the round's bound is about, by name (the same set whatever --steps is): the shift
-    # stream (k_hess_binary reads every shift and writes every difference; k_select reads every
-    # difference once) against HBM, k_hess_binary's in-order sums against the FP64 pipe, and the
+    # stream (the binary Hessian reads every shift and writes every difference; k_select reads every
+    # difference once) against HBM, the Hessian's in-order sums against the FP64 pipe, and the
     # Cholesky's latency chain in cycles per column
-    hb, hwhat = algorithmic_bytes("k_hess_binary", prob, k)
+    hname = "k_hess_hits" if "k_hess_hits" in kernels else "k_hess_binary"
+    hb, hwhat = algorithmic_bytes(hname, prob, k)
     hops = hess_fp64_ops(prob)
     sb, swhat = algorithmic_bytes("k_select", prob, k)
-    r_hess_hbm = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "hbm", hb, hbm, "GB/s", hwhat, hsrc)
-    r_hess_fp64 = kernel_roofline("k_hess_binary", kernels.get("k_hess_binary", 0.0), "fp64", hops, fp64["add_gops"],
+    r_hess_hbm = kernel_roofline(hname, kernels.get(hname, 0.0), "hbm", hb, hbm, "GB/s", hwhat, hsrc)
+    r_hess_fp64 = kernel_roofline(hname, kernels.get(hname, 0.0), "fp64", hops, fp64["add_gops"],
                                   "Gop/s", "in-order D_s sums (one add per sample after the first with both attributes set) "
-                                  "+ difference, square and norm add per upper entry", fsrc)
+                                  "+ the difference per upper entry", fsrc)
     r_select = kernel_roofline("k_select", kernels.get("k_select", 0.0), "hbm", sb, hbm, "GB/s", swhat, hsrc)
     chol_ms = kernels.get("k_chol_coop", 0.0)
     sm_mhz = clocks.get("sm_mhz") or 2070.0
@@ -579,8 +584,8 @@ def run_ours(args, ws, rank, local, td):
               "sm_mhz": sm_mhz, "fp64_add_latency_cycles": fp64["add_latency_cycles"]}
     roof = dict(r_hess_hbm)
     roof["fp64"] = {k_: r_hess_fp64[k_] for k_ in ("achieved", "peak", "unit", "frac", "work_per_launch")}
-    roof["note"] = ("k_hess_binary streams the shift matrices (shift read, difference written); its in-order "
-                    "FP64 sums bind it to the FP64 pipe first (fp64.frac), HBM second (frac)")
+    roof["note"] = (f"{hname} streams the shift matrices (shift read, difference written); bound by "
+                    f"{SLOWEST_BOUND[hname]} (fp64.frac against the FP64 pipe, frac against HBM)")
     roof_list = [r_hess_hbm, r_hess_fp64, r_select, r_chol]
     slowest, slowest_ms = max(prof, key=lambda t: t[1])
     # round-level bound: the shift stream (every client's shift read and written once, packed

@@ -670,7 +670,7 @@ int launch_round(fednl_handle h, Marks* M = nullptr, bool client_phase_only = fa
     // With TopK / TopLEK in the fixed order the selection kernel's idle warps also form ||diff||_F^2
     // and Lk (the Hessian writes the difference only), and the solve forms l from Lk while it merges
     const bool norms_in_select = agg_in_select && apply_in_solve && !h->desc.option_a;
-    MARK(h->binary ? "k_hess_binary" : "k_hess_dense");
+    MARK(!h->binary ? "k_hess_dense" : h->hess_kind == kHessHits ? "k_hess_hits" : "k_hess_binary");
     const int hmode = h->pp ? 2 : norms_in_select ? 3 : 0;     // round_hess_mode(h) in the captured round
     if (h->binary) {
         CK(launch_hess_binary(h, P, na, hmode, st, h->hess_kind, h->hess_nt));
