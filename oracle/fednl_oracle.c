@@ -1083,63 +1083,106 @@ void orc_hessian(const double* atr, int32_t d, int32_t lda, int32_t n, const dou
 
 /* The fixed-order Option-B solve (x = (H + l I)^{-1} b, the reference's choleskyFactorization and
  * triangular solves, CholeskyFactorization.h:153-272 and ElementarySolvers.h:71-224, in an order
- * with a short dependency chain per column): a square-root-free LDL^T factorization,
- * H + l I = L D L^T with L unit lower triangular, right-looking.  a_ij starts at h_ij (+ l on the
- * diagonal).  At step k the pivot d_k = a_kk is rejected when negative (as the reference rejects a
- * negative radicand), inv_k = 1 / d_k, the row's multipliers are l_kj = a_kj inv_k, and every
- * a_ij with k < i <= j receives a_ij = fma(-l_ki, a_kj, a_ij) (a_kj unscaled).  ltr's upper
- * triangle receives the multipliers l_kj (row k of L^T) and d_k on the diagonal, mirrored into the
- * lower triangle.  The GB300 kernel follows this order; the reference's own order is
- * orc_cholesky_ref. */
+ * with a short dependency chain per column pair): a square-root-free block LDL^T factorization,
+ * H + l I = L D L^T with L unit lower triangular and D block diagonal, its 2x2 blocks on the column
+ * pairs (0,1), (2,3), ... (a 1x1 block last when d is odd), right-looking.  a_ij starts at h_ij
+ * (+ l on the diagonal).  Pair (k, k+1) with a = a_kk, b = a_k,k+1, c = a_k+1,k+1:
+ *   det = fma(a, c, -(b b)); rejected when a or det is negative (as the reference rejects a
+ *   negative radicand); rdet = 1 / det; D^{-1} = [[p, q], [q, r]] with p = c rdet, q = -(b rdet),
+ *   r = a rdet; the multipliers of column j > k+1 are l1_j = fma(p, w1_j, q w2_j) and
+ *   l2_j = fma(q, w1_j, r w2_j) (w1_j = a_kj, w2_j = a_k+1,j unscaled); every a_ij with
+ *   k+1 < i <= j receives a_ij = fma(-l1_i, w1_j, a_ij), then a_ij = fma(-l2_i, w2_j, a_ij).
+ * A 1x1 block k: pivot a = a_kk (rejected when negative), inv = 1 / a, l_kj = a_kj inv.
+ * ltr's upper triangle receives the multipliers (rows k and k+1 of L^T; 0 between the two rows of a
+ * pair), its diagonal p and r (a pair) or the pivot a (1x1), and q goes below the diagonal at
+ * (k+1, k).  The GB300 kernel follows this order; the reference's own order is orc_cholesky_ref. */
+static int orc_neg(double v) { return v < 0; }
+
 int orc_ldlt(const double* h, int32_t d, int32_t lda, double l, double* ltr)
 {
     memset(ltr, 0, (size_t)d * (size_t)lda * sizeof(double));
     for (int32_t j = 0; j < d; ++j)
         for (int32_t i = 0; i <= j; ++i)
             ltr[(size_t)j * lda + i] = (i == j) ? h[(size_t)j * lda + i] + l : h[(size_t)j * lda + i];
-    double* w = (double*)malloc((size_t)d * sizeof(double));
-    for (int32_t k = 0; k < d; ++k) {
-        const double a = ltr[(size_t)k * lda + k];
-        if (a < 0) {
-            free(w);
+#define A_(i, j) ltr[(size_t)(j) * lda + (i)]
+    double* w1 = (double*)malloc((size_t)d * sizeof(double));
+    double* w2 = (double*)malloc((size_t)d * sizeof(double));
+    for (int32_t k = 0; k < d; k += 2) {
+        if (k + 1 == d) {
+            const double a = A_(k, k);
+            if (orc_neg(a)) {
+                free(w1);
+                free(w2);
+                return 0;
+            }
+            break;          /* nothing right of the last column */
+        }
+        const double a = A_(k, k), b = A_(k, k + 1), c = A_(k + 1, k + 1);
+        if (orc_neg(a)) {
+            free(w1);
+            free(w2);
             return 0;
         }
-        const double inv = 1.0 / a;
-        for (int32_t j = k + 1; j < d; ++j) {
-            w[j] = ltr[(size_t)j * lda + k];
-            ltr[(size_t)j * lda + k] = w[j] * inv;
+        const double det = fma(a, c, -(b * b));
+        if (orc_neg(det)) {
+            free(w1);
+            free(w2);
+            return 0;
         }
-        for (int32_t j = k + 1; j < d; ++j) {
-            double* col = ltr + (size_t)j * lda;
-            for (int32_t i = k + 1; i <= j; ++i)
-                col[i] = fma(-ltr[(size_t)i * lda + k], w[j], col[i]);
+        const double rdet = 1.0 / det;
+        const double p = c * rdet, q = -(b * rdet), r = a * rdet;
+        for (int32_t j = k + 2; j < d; ++j) {
+            w1[j] = A_(k, j);
+            w2[j] = A_(k + 1, j);
+            A_(k, j) = fma(p, w1[j], q * w2[j]);
+            A_(k + 1, j) = fma(q, w1[j], r * w2[j]);
         }
+        for (int32_t j = k + 2; j < d; ++j)
+            for (int32_t i = k + 2; i <= j; ++i) {
+                double v = fma(-A_(k, i), w1[j], A_(i, j));
+                A_(i, j) = fma(-A_(k + 1, i), w2[j], v);
+            }
+        A_(k, k) = p;
+        A_(k + 1, k + 1) = r;
+        A_(k, k + 1) = 0.0;
+        A_(k + 1, k) = q;
     }
-    free(w);
-    for (int32_t j = 0; j < d; ++j)
-        for (int32_t i = 0; i < j; ++i)
-            ltr[(size_t)i * lda + j] = ltr[(size_t)j * lda + i];
+#undef A_
+    free(w1);
+    free(w2);
     return 1;
 }
 
-/* L y = b, z = D^{-1} y, L^T x = z, column-oriented: y_i = fma(-l_ti, y_t, y_i) for t ascending,
- * z_t = y_t (1 / d_t) (the factorization's reciprocal), then x_i = fma(-l_it, x_t, x_i) for t
- * descending (unit diagonal: no division on the chain). */
+/* L y = b, z = D^{-1} y, L^T x = z, column-oriented: for each block in order, y_i =
+ * fma(-l1_i, y_k, y_i) then fma(-l2_i, y_k+1, y_i) for i > k+1 (a 1x1 block: fma(-l_i, y_k, y_i));
+ * z_k = fma(p, y_k, q y_k+1), z_k+1 = fma(q, y_k, r y_k+1) (1x1: z_k = y_k (1 / a)); then
+ * x_i = fma(-l_it, x_t, x_i) for t descending and every i < t (unit diagonal, no division; the
+ * zero between the rows of a pair takes part like any other entry). */
 void orc_solve_ldlt(const double* ltr, int32_t d, int32_t lda, const double* b, double* x)
 {
+#define A_(i, j) ltr[(size_t)(j) * lda + (i)]
     for (int32_t i = 0; i < d; ++i)
         x[i] = b[i];
-    for (int32_t t = 0; t < d; ++t) {
-        const double yt = x[t];
-        for (int32_t i = t + 1; i < d; ++i)
-            x[i] = fma(-ltr[(size_t)i * lda + t], yt, x[i]);
-        x[t] = yt * (1.0 / ltr[(size_t)t * lda + t]);
+    for (int32_t k = 0; k < d; k += 2) {
+        if (k + 1 == d) {
+            x[k] = x[k] * (1.0 / A_(k, k));
+            break;
+        }
+        const double y1 = x[k], y2 = x[k + 1];
+        for (int32_t i = k + 2; i < d; ++i) {
+            double v = fma(-A_(k, i), y1, x[i]);
+            x[i] = fma(-A_(k + 1, i), y2, v);
+        }
+        const double p = A_(k, k), q = A_(k + 1, k), r = A_(k + 1, k + 1);
+        x[k] = fma(p, y1, q * y2);
+        x[k + 1] = fma(q, y1, r * y2);
     }
     for (int32_t t = d - 1; t >= 0; --t) {
         const double xt = x[t];
         for (int32_t i = 0; i < t; ++i)
-            x[i] = fma(-ltr[(size_t)t * lda + i], xt, x[i]);
+            x[i] = fma(-A_(i, t), xt, x[i]);
     }
+#undef A_
 }
 
 /* ================================================================================== */

@@ -267,8 +267,10 @@ def test_cholesky_known_answer(oracle):
     """Known-answer case of dopt/bin_tests/src/linalg_matrices/CholeskyFactorizationGTest.cpp:11-40:
     L = [[1,0,0],[4,7,0],[1,2,5]], A = L L^T is factored back into L exactly by the reference's
     algorithm (orc_cholesky_ref); [[1,2],[2,1]] is rejected as not positive definite.  The fixed
-    order's LDL^T factors A = L1 D L1^T (L1 unit lower with integer entries, D powers of two) back
-    exactly and rejects the same matrix."""
+    order's block LDL^T (2x2 pivot blocks on the column pairs) factors A = L1 D L1^T (L1 unit lower
+    with integer entries, D diagonal) exactly: the pair (0, 1) keeps its block [[1, 3], [3, 13]]
+    (det 4, inverse [[13/4, -3/4], [-3/4, 1/4]]), column 2's multipliers are D^-1 [-2, 14] =
+    [-17, 5] and the last pivot is 2; it rejects the same matrix."""
     import ctypes as C
     dp = C.POINTER(C.c_double)
     lib = oracle.lib()
@@ -285,9 +287,10 @@ def test_cholesky_known_answer(oracle):
     A1 = L1 @ D @ L1.T
     ltr = np.zeros(9)
     assert lib.orc_ldlt(A1.T.copy().ctypes.data_as(dp), 3, 3, 0.0, ltr.ctypes.data_as(dp)) == 1
-    F = ltr.reshape(3, 3).T
-    np.testing.assert_array_equal(np.triu(F, 1), np.triu(L1.T, 1))
-    np.testing.assert_array_equal(np.diag(F), np.diag(D))
+    F = ltr.reshape(3, 3).T           # F[i][j] = ltr[j*3+i]
+    np.testing.assert_array_equal(np.triu(F, 1), np.array([[0, 0.0, -17.0], [0, 0, 5.0], [0, 0, 0]]))
+    np.testing.assert_array_equal(np.diag(F), [3.25, 0.25, 2.0])
+    assert F[1][0] == -0.75
     b = np.array([1.0, -2.0, 3.0])
     ok, x = oracle.cholesky_solve(A1, 3, 3, 0.0, b)
     assert ok

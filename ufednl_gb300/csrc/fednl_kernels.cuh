@@ -2062,7 +2062,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
     __shared__ double Rb[kCholNB][kCholNB + 1];
     __shared__ double Sb[kCholNB][kCholSlab + 1];
     __shared__ double SR[kCholNB][kCholSlab + 1];
-    __shared__ double s_inv[kCholNB];
+    __shared__ double s_inv[kCholNB];     // 1 / pivot (single column), p and r (pair)
+    __shared__ double s_q[kCholNB];       // q of the pair starting at k
     __shared__ unsigned short s_ent[kCholNB * (kCholNB + 1) / 2];
     __shared__ int s_fail;
     __shared__ double s_yb[2][32];
@@ -2150,17 +2151,20 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
         }
         if (tid == 0) s_fail = 0;
         __syncthreads();
-        // Column loop (the unblocked right-looking steps restricted to the panel's rows).  Warp 0
-        // runs only the pivot chain: at step k it forms l_{k,k+1} = a_{k,k+1} (1 / d_k), applies
-        // step k to the next diagonal entry itself and takes its reciprocal.  Six other warps scale
-        // row k (into Rb / SR) and apply step k to every other entry below row k.  Each of their
-        // threads owns fixed entries for the whole panel and keeps them in registers: block entries
-        // e = ut + 192 q of the descending-row list (rows 1..nb-1) and slab entries (row
-        // nb-1 - e / ns, slab column e mod ns) likewise, so the entries still active at step k
-        // (row > k) fill the lowest slots of consecutive threads.  An entry is written to Db / Sb
-        // when its row becomes the next pivot row (the diagonal entry one step earlier, for the
-        // chain).  Warp 4 stays idle: it shares warp 0's SM sub-partition, whose FP64 pipe the
-        // chain needs.
+        // Column loop over the panel's pivot blocks: the pairs (k, k+1), k even (2x2 blocks of D),
+        // and a single column last when nb is odd.  Warp 0 runs only the pivot chain, one block
+        // ahead: while the others apply block k it applies block k to the next block's own three
+        // entries (a lane per multiplier, then a lane per entry) and forms that block's det, its
+        // correctly rounded reciprocal and D^{-1} = [[p, q], [q, r]] (a lane per entry).  Six other
+        // warps form the multipliers of rows k and k+1 (l1 = fma(p, w1, q w2), l2 = fma(q, w1, r w2)
+        // into Rb / SR) and apply block k (two fused multiply-adds) to every other entry below row
+        // k+1.  Each of their threads owns fixed entries for the whole panel and keeps them in
+        // registers: block entries e = ut + 192 q of the descending-row list (rows 1..nb-1) and slab
+        // entries (row nb-1 - e / ns, slab column e mod ns) likewise, so the entries still active at
+        // block k (row > k+1) fill the lowest slots of consecutive threads.  An entry is written to
+        // Db / Sb when its row becomes one of the next pivot rows (the entries of the block after
+        // the next one block earlier, for the chain).  Warp 4 stays idle: it shares warp 0's SM
+        // sub-partition, whose FP64 pipe the chain needs.
         constexpr int kSlotsB = (kCholNB * (kCholNB - 1) / 2 + kCoopThreads - 65) / (kCoopThreads - 64);
         constexpr int kSlotsS = ((kCholNB - 1) * kCholSlab + kCoopThreads - 65) / (kCoopThreads - 64);
         const int ut = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;    // 0..191 for the update warps
@@ -2194,53 +2198,103 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 }
             }
         }
-        double inv_k = 0.0;
-        if (warp == 0) {
-            const double a0 = Db[0][0];
-            const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-            inv_k = rcp_rn_int(a0);
-            if (lane == 0) {
-                Rb[0][0] = a0;
-                s_inv[0] = inv_k;
-                if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;   // a < 0 (not NaN, not -0)
+        // Warp 0: the parameters of the block at k2 from its (updated) entries a, b, c (b, c unused
+        // for a single column): the pivot block goes to Rb (0 between the rows of a pair), D^{-1} to
+        // s_inv / s_q, and a negative a or det (not NaN, not -0) fails the factorisation.
+        auto block_params = [&](int k2, bool pair2, double a, double b, double c) {
+            const auto neg = [](double v) {
+                const long long vb_ = __double_as_longlong(v), mag = vb_ & 0x7fffffffffffffffll;
+                return vb_ < 0 && mag != 0 && mag <= 0x7ff0000000000000ll;
+            };
+            if (pair2) {
+                const double det = fma(a, c, -__dmul_rn(b, b));
+                const double rdet = rcp_rn_int(det);
+                if (lane < 3) {     // p = c rdet, q = -(b rdet), r = a rdet, a lane each
+                    const double v = __dmul_rn(lane == 0 ? c : lane == 1 ? b : a, rdet);
+                    if (lane == 0) s_inv[k2] = v;
+                    else if (lane == 1) s_q[k2] = -v;
+                    else s_inv[k2 + 1] = v;
+                }
+                if (lane == 0) {
+                    Rb[k2][k2] = a;
+                    Rb[k2][k2 + 1] = 0.0;
+                    Rb[k2 + 1][k2 + 1] = c;
+                    if (neg(a) || neg(det)) s_fail = 1;
+                }
+            } else {
+                const double inv = rcp_rn_int(a);
+                if (lane == 0) {
+                    Rb[k2][k2] = a;
+                    s_inv[k2] = inv;
+                    if (neg(a)) s_fail = 1;
+                }
             }
-        }
+        };
+        if (warp == 0) block_params(0, nb > 1, Db[0][0], nb > 1 ? Db[0][1] : 0.0, nb > 1 ? Db[1][1] : 0.0);
         __syncthreads();
-        for (int k = 0; k < nb; ++k) {
+        for (int k = 0; k < nb; k += 2) {
             if (s_fail) break;
+            const bool pair = k + 1 < nb;
             if (warp == 0) {
-                if (k + 1 < nb) {
-                    const double w = Db[k][k + 1];
-                    const double a0 = fma(-__dmul_rn(w, inv_k), w, Db[k + 1][k + 1]);
-                    const long long ab = __double_as_longlong(a0), mag = ab & 0x7fffffffffffffffll;
-                    inv_k = rcp_rn_int(a0);
-                    if (lane == 0) {
-                        Rb[k + 1][k + 1] = a0;
-                        s_inv[k + 1] = inv_k;
-                        if (ab < 0 && mag != 0 && mag <= 0x7ff0000000000000ll) s_fail = 1;
-                    }
+                const int k2 = k + 2;
+                if (pair && k2 < nb) {
+                    // block k applied to the next block's entries: lane t < 4 forms the multiplier of
+                    // row k2 + (t >> 1) (t even: l1 = fma(p, w1, q w2), t odd: l2 = fma(q, w1, r w2)),
+                    // lane e < 3 then updates entry e of (k2,k2), (k2,k2+1), (k2+1,k2+1)
+                    const bool pair2 = k2 + 1 < nb;
+                    const double p = s_inv[k], r = s_inv[k + 1], q = s_q[k];
+                    const int mc = k2 + ((lane >> 1) & 1);
+                    const int mcol = (lane < 4 && (pair2 || mc == k2)) ? mc : k2;
+                    const double x1 = Db[k][mcol], x2 = Db[k + 1][mcol];
+                    const bool odd = lane & 1;
+                    const double ml = fma(odd ? q : p, x1, __dmul_rn(odd ? r : q, x2));
+                    const int er = k2 + (lane == 2 ? 1 : 0), ec = k2 + (lane >= 1 ? 1 : 0);
+                    const int src = 2 * (er - k2);
+                    const double m1 = __shfl_sync(0xffffffffu, ml, src), m2 = __shfl_sync(0xffffffffu, ml, src + 1);
+                    const bool live = lane < 3 && (pair2 || lane == 0);
+                    const int erc = live ? er : k2, ecc = live ? ec : k2;
+                    double e = fma(-m1, Db[k][ecc], Db[erc][ecc]);
+                    e = fma(-m2, Db[k + 1][ecc], e);
+                    const double na = __shfl_sync(0xffffffffu, e, 0), nbv = __shfl_sync(0xffffffffu, e, 1),
+                                 nc = __shfl_sync(0xffffffffu, e, 2);
+                    block_params(k2, pair2, na, nbv, nc);
                 }
             } else if (warp != 4) {
-                const double inv = s_inv[k];
-                const int nd = nb - 1 - k;                 // rows k+1 .. nb-1
-                if (ut < nd) Rb[k][k + 1 + ut] = __dmul_rn(Db[k][k + 1 + ut], inv);
-                else if (ut < nd + ns) SR[k][ut - nd] = __dmul_rn(Sb[k][ut - nd], inv);
-                asm volatile("bar.sync 1, 192;" ::: "memory");
-#pragma unroll
-                for (int q = 0; q < kSlotsB; ++q) {
-                    const int i = ib[q], j = jb[q];
-                    if (i > k && !(j == k + 1)) {          // (k+1, k+1) is the chain's
-                        vb[q] = fma(-Rb[k][i], Db[k][j], vb[q]);
-                        if (i == k + 1 || (i == j && i == k + 2)) Db[i][j] = vb[q];
+                if (pair) {
+                    const double p = s_inv[k], r = s_inv[k + 1], q = s_q[k];
+                    const int nd = nb - 2 - k;                 // block columns k+2 .. nb-1
+                    if (ut < nd) {
+                        const int j = k + 2 + ut;
+                        const double w1 = Db[k][j], w2 = Db[k + 1][j];
+                        Rb[k][j] = fma(p, w1, __dmul_rn(q, w2));
+                        Rb[k + 1][j] = fma(q, w1, __dmul_rn(r, w2));
+                    } else if (ut < nd + ns) {
+                        const int sl = ut - nd;
+                        const double w1 = Sb[k][sl], w2 = Sb[k + 1][sl];
+                        SR[k][sl] = fma(p, w1, __dmul_rn(q, w2));
+                        SR[k + 1][sl] = fma(q, w1, __dmul_rn(r, w2));
                     }
-                }
+                    asm volatile("bar.sync 1, 192;" ::: "memory");
 #pragma unroll
-                for (int q = 0; q < kSlotsS; ++q) {
-                    const int i = is_[q];
-                    if (i > k) {
-                        vs[q] = fma(-Rb[k][i], Sb[k][ss[q]], vs[q]);
-                        if (i == k + 1) Sb[i][ss[q]] = vs[q];
+                    for (int q2 = 0; q2 < kSlotsB; ++q2) {
+                        const int i = ib[q2], j = jb[q2];
+                        if (i > k + 1 && !(j <= k + 3)) {      // the next block's own entries are the chain's
+                            double v = fma(-Rb[k][i], Db[k][j], vb[q2]);
+                            vb[q2] = fma(-Rb[k + 1][i], Db[k + 1][j], v);
+                            if (i <= k + 3 || j <= k + 5) Db[i][j] = vb[q2];
+                        }
                     }
+#pragma unroll
+                    for (int q2 = 0; q2 < kSlotsS; ++q2) {
+                        const int i = is_[q2];
+                        if (i > k + 1) {
+                            double v = fma(-Rb[k][i], Sb[k][ss[q2]], vs[q2]);
+                            vs[q2] = fma(-Rb[k + 1][i], Sb[k + 1][ss[q2]], v);
+                            if (i <= k + 3) Sb[i][ss[q2]] = vs[q2];
+                        }
+                    }
+                } else if (ut < ns) {      // the single last column: only the slab's row k is scaled
+                    SR[k][ut] = __dmul_rn(Sb[k][ut], s_inv[k]);
                 }
             }
             __syncthreads();
@@ -2265,19 +2319,31 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             A[up_pos(c0 + i, j)] = SR[i][sl];
             W[(size_t)i * D + j] = Sb[i][sl];
         }
-        // panel columns beyond the slab (very large d only): one column per warp, same steps
+        // panel columns beyond the slab (very large d only): one column per warp, same blocks
         {
-            const int w = tid >> 5;
-            for (int sl = kCholSlab + w; sl < ntot; sl += kCoopThreads / 32) {
+            const int wp = tid >> 5;
+            for (int sl = kCholSlab + wp; sl < ntot; sl += kCoopThreads / 32) {
                 const int j = c1 + (int)bid + sl * (int)G;
                 double a = (lane < nb) ? A[up_pos(c0 + lane, j)] : 0.0;
-                for (int k = 0; k < nb; ++k) {
-                    const double w = __shfl_sync(0xffffffffu, a, k);     // a_kj, final and unscaled
-                    if (lane == k) {
-                        W[(size_t)k * D + j] = w;
+                for (int k = 0; k < nb; k += 2) {
+                    const double w1 = __shfl_sync(0xffffffffu, a, k);     // a_kj, a_k+1,j final and unscaled
+                    if (k + 1 < nb) {
+                        const double w2 = __shfl_sync(0xffffffffu, a, k + 1);
+                        const double p = s_inv[k], r = s_inv[k + 1], q = s_q[k];
+                        if (lane == k) {
+                            W[(size_t)k * D + j] = w1;
+                            a = fma(p, w1, __dmul_rn(q, w2));
+                        } else if (lane == k + 1) {
+                            W[(size_t)(k + 1) * D + j] = w2;
+                            a = fma(q, w1, __dmul_rn(r, w2));
+                        } else if (lane > k + 1 && lane < nb) {
+                            a = fma(-Rb[k][lane], w1, a);
+                            a = fma(-Rb[k + 1][lane], w2, a);
+                        }
+                    } else if (lane == k) {
+                        W[(size_t)k * D + j] = w1;
                         a = __dmul_rn(a, s_inv[k]);
                     }
-                    if (lane > k && lane < nb) a = fma(-Rb[k][lane], w, a);
                 }
                 if (lane < nb) A[up_pos(c0 + lane, j)] = a;
             }
