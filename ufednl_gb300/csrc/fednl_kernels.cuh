@@ -1738,10 +1738,10 @@ __global__ void k_randseqk(unsigned* states, int n_gen, int U, int k, int* rseq,
 // clients in order, so H receives exactly the reference's sequence of additions.
 // Position p = 32 word + lane of one selection word, called by the 32 lanes of a converged warp
 // (lanes past U take part in the shuffles only).  Per batch of 32 clients, lane t loads client t's
-// word; 32 shuffles turn the words into each position's mask of selecting clients, the loads of
-// all of them are issued together, and the FP64 updates follow in client order (the same
-// operations as one position at a time).  Updates the selecting clients' shifts; returns the new
-// H[p].
+// word; 32 shuffles turn the words into each position's mask of selecting clients, and every lane
+// walks its own mask in client order, four clients at a time with their loads issued together (the
+// same operations as one position at a time).  Updates the selecting clients' shifts; returns the
+// new H[p].
 __device__ __forceinline__ double apply_word(const Dev& P, int p, int lane)
 {
     const bool in = p < P.U;
@@ -1767,33 +1767,39 @@ __device__ __forceinline__ double apply_word(const Dev& P, int p, int lane)
             mine |= ((w >> lane) & 1u) << t;
         }
         if (!in) mine = 0u;
-        if (!__any_sync(0xffffffffu, mine != 0u)) continue;
+        // each lane walks its own selecting clients, four at a time with their loads issued ahead:
+        // the warp's FP64 instructions then serve the lanes' events side by side, not one client of
+        // the batch at a time (most clients select one or two of a word's 32 positions)
+        while (__any_sync(0xffffffffu, mine != 0u)) {
+            int tt[4];
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            int cls[16];
+            for (int e = 0; e < 4; ++e) {
+                tt[e] = mine ? __ffs(mine) - 1 : -1;
+                mine &= mine - 1u;
+            }
+            double dv[4], sv[4];
+            size_t qq[4];
 #pragma unroll
-            for (int t = 0; t < 16; ++t) cls[t] = __shfl_sync(0xffffffffu, cl, half * 16 + t);
-            double dv[16], sv[16];
-#pragma unroll
-            for (int t = 0; t < 16; ++t)
-                if ((mine >> (half * 16 + t)) & 1u) {
-                    const size_t q = (size_t)cls[t] * P.ustr + p;
-                    dv[t] = P.diff[q];
-                    sv[t] = P.shift[q];
+            for (int e = 0; e < 4; ++e) {
+                const int c = __shfl_sync(0xffffffffu, cl, tt[e] < 0 ? 0 : tt[e]);
+                qq[e] = (size_t)c * P.ustr + p;
+                if (tt[e] >= 0) {
+                    dv[e] = P.diff[qq[e]];
+                    sv[e] = P.shift[qq[e]];
                 }
+            }
 #pragma unroll
-            for (int t = 0; t < 16; ++t)
-                if ((mine >> (half * 16 + t)) & 1u) {
-                    const size_t q = (size_t)cls[t] * P.ustr + p;
+            for (int e = 0; e < 4; ++e)
+                if (tt[e] >= 0) {
                     double item, sent;
                     if (P.comp == 5) {                 // Natural: master adds preScale * trunc(diff)
-                        item = natural_trunc(dv[t]);
+                        item = natural_trunc(dv[e]);
                         sent = __dmul_rn(P.prescale, item);
                     } else {
-                        item = (P.comp == 1 || P.comp == 3 || P.comp == 6) ? __dmul_rn(dv[t], P.mult) : dv[t];
+                        item = (P.comp == 1 || P.comp == 3 || P.comp == 6) ? __dmul_rn(dv[e], P.mult) : dv[e];
                         sent = __dmul_rn(item, P.prescale);
                     }
-                    P.shift[q] = __dadd_rn(sv[t], __dmul_rn(P.alpha, item));
+                    P.shift[qq[e]] = __dadd_rn(sv[e], __dmul_rn(P.alpha, item));
                     h = __dadd_rn(h, sent);
                 }
         }
