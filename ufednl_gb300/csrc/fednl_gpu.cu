@@ -20,6 +20,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -520,6 +521,7 @@ struct fednl_handle_s {
     int ref_grid = 1;          // CTAs of the reference-order solve
     int rounds_done = 0;
     void* flush_buf = nullptr;
+    void* pin = nullptr;               // [32 B] pinned: a round's statistics and status, read back together
     size_t flush_cap = 0;
 };
 
@@ -1042,6 +1044,7 @@ int fednl_gpu_destroy(fednl_handle h)
     h->state.release();
     h->feat.release();
     if (h->flush_buf) cudaFree(h->flush_buf);
+    if (h->pin) cudaFreeHost(h->pin);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
@@ -1075,10 +1078,11 @@ static void for_client_ranges(int nc, const std::function<void(int, int, int)>& 
 // most 16 pairs per upper position in every client, 64 M in all) and the codes can hold the
 // sample and attribute indices.
 struct HitLists {
-    std::vector<uint16_t> code;    // [nc][ustr]
-    std::vector<uint32_t> seg;     // [nc][nseg + 1]
-    std::vector<uint32_t> rec;     // [records + 1]
-    std::vector<uint16_t> hits;
+    std::unique_ptr<uint16_t[]> code;    // [nc][ustr]
+    std::unique_ptr<uint32_t[]> seg;     // [nc][nseg + 1]
+    std::unique_ptr<uint32_t[]> rec;     // [records + 1]
+    std::unique_ptr<uint16_t[]> hits;
+    size_t ncode = 0, nseg = 0, nrec = 0, nhits = 0;
     int maxrec = 0;
 };
 
@@ -1110,67 +1114,75 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
             }
         }
     };
-    // pass 1: records and their samples per client and segment
-    std::vector<long long> nrec(nc, 0), nhit(nc, 0);
-    std::vector<int> segrec((size_t)nc * nseg, 0);
-    std::vector<int> maxrec(nc, 0);
-    for_client_ranges(nc, [&](int, int c0, int c1) {
-        std::vector<int> cnt(U);
-        for (int c = c0; c < c1; ++c) {
-            std::fill(cnt.begin(), cnt.end(), 0);
-            for_pairs(c, [&](int, int p) { ++cnt[p]; });
-            for (int p = 0; p < U; ++p)
-                if (cnt[p] >= 2) {
-                    ++segrec[(size_t)c * nseg + p / 512];
-                    nrec[c] += 1;
-                    nhit[c] += cnt[p];
-                }
-            for (int g = 0; g < nseg; ++g) maxrec[c] = std::max(maxrec[c], segrec[(size_t)c * nseg + g]);
-        }
-    });
-    std::vector<long long> rbase(nc + 1, 0), hbase(nc + 1, 0);
-    for (int c = 0; c < nc; ++c) {
-        rbase[c + 1] = rbase[c] + nrec[c];
-        hbase[c + 1] = hbase[c] + nhit[c];
-    }
-    if (hbase[nc] >= 0xffffffffll) return false;
-    L.code.assign((size_t)nc * h->ustr, (uint16_t)kHitNone);
-    L.seg.assign((size_t)nc * (nseg + 1), 0u);
-    L.rec.assign((size_t)rbase[nc] + 1, 0u);
-    L.hits.assign((size_t)hbase[nc], 0);
-    L.maxrec = std::max(1, *std::max_element(maxrec.begin(), maxrec.end()));
-    L.rec[rbase[nc]] = (uint32_t)hbase[nc];
-    // pass 2: codes, record starts, then the samples in order
+    // one pass per client range: each client's codes in place, its records (client-relative starts
+    // of their samples), samples and per-segment record counts in the client's own buffers
+    struct Local {
+        std::vector<uint32_t> rec, seg;
+        std::vector<uint16_t> hits;
+        int maxrec = 0;
+    };
+    std::vector<Local> loc(nc);
+    L.ncode = (size_t)nc * h->ustr;
+    L.code.reset(new uint16_t[L.ncode]);
     for_client_ranges(nc, [&](int, int c0, int c1) {
         std::vector<int> cnt(U), at(U);
         for (int c = c0; c < c1; ++c) {
+            Local& o = loc[c];
             std::fill(cnt.begin(), cnt.end(), 0);
-            uint16_t* code = L.code.data() + (size_t)c * h->ustr;
+            uint16_t* code = L.code.get() + (size_t)c * h->ustr;
+            std::fill(code, code + h->ustr, (uint16_t)kHitNone);
             for_pairs(c, [&](int ls, int p) {
                 if (cnt[p]++ == 0) code[p] = (uint16_t)ls;
             });
-            long long r = rbase[c], e = hbase[c];
+            o.seg.resize((size_t)nseg + 1);
+            uint32_t r = 0, e = 0;
             for (int g = 0; g < nseg; ++g) {
-                L.seg[(size_t)c * (nseg + 1) + g] = (uint32_t)r;
-                const long long rg = r;
+                o.seg[g] = r;
+                const uint32_t rg = r;
                 for (int p = g * 512; p < std::min(U, g * 512 + 512); ++p)
                     if (cnt[p] >= 2) {
-                        code[p] = (uint16_t)(0x8000u | (unsigned)(r - rg));
-                        L.rec[r++] = (uint32_t)e;
-                        at[p] = (int)(e - hbase[c]);
-                        e += cnt[p];
+                        code[p] = (uint16_t)(0x8000u | (r - rg));
+                        o.rec.push_back(e);
+                        ++r;
+                        at[p] = (int)e;
+                        e += (uint32_t)cnt[p];
                     }
+                o.maxrec = std::max(o.maxrec, (int)(r - rg));
             }
-            L.seg[(size_t)c * (nseg + 1) + nseg] = (uint32_t)r;
-            uint16_t* hits = L.hits.data() + hbase[c];
+            o.seg[nseg] = r;
+            o.hits.resize(e);
             for_pairs(c, [&](int ls, int p) {
-                if (cnt[p] >= 2) hits[at[p]++] = (uint16_t)ls;
+                if (cnt[p] >= 2) o.hits[at[p]++] = (uint16_t)ls;
             });
             for (int j = 0; j < d; ++j) {
                 code[j * (j + 1) / 2 + j] = (uint16_t)(0xc000u | (unsigned)j);
                 if (icpt[c] && j == d - 1)
                     for (int i = 0; i < j; ++i) code[j * (j + 1) / 2 + i] = (uint16_t)(0xa000u | (unsigned)i);
             }
+        }
+    });
+    std::vector<long long> rbase(nc + 1, 0), hbase(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) {
+        rbase[c + 1] = rbase[c] + (long long)loc[c].rec.size();
+        hbase[c + 1] = hbase[c] + (long long)loc[c].hits.size();
+        L.maxrec = std::max(L.maxrec, loc[c].maxrec);
+    }
+    if (hbase[nc] >= 0xffffffffll) return false;
+    L.maxrec = std::max(1, L.maxrec);
+    L.nseg = (size_t)nc * (nseg + 1);
+    L.nrec = (size_t)rbase[nc] + 1;
+    L.nhits = (size_t)hbase[nc];
+    L.seg.reset(new uint32_t[L.nseg]);
+    L.rec.reset(new uint32_t[L.nrec]);
+    L.hits.reset(new uint16_t[std::max<size_t>(1, L.nhits)]);
+    L.rec[rbase[nc]] = (uint32_t)hbase[nc];
+    // the clients' buffers at their global offsets (record starts and segment counts rebased)
+    for_client_ranges(nc, [&](int, int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            const Local& o = loc[c];
+            for (size_t r = 0; r < o.rec.size(); ++r) L.rec[rbase[c] + r] = (uint32_t)(hbase[c] + o.rec[r]);
+            for (int g = 0; g <= nseg; ++g) L.seg[(size_t)c * (nseg + 1) + g] = (uint32_t)(rbase[c] + o.seg[g]);
+            if (!o.hits.empty()) std::memcpy(L.hits.get() + hbase[c], o.hits.data(), o.hits.size() * 2);
         }
     });
     return true;
@@ -1183,24 +1195,45 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     for (int s = 0; s < S; ++s)
         if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
     int fmt = h->desc.feature_format;
-    // first pass, per client range: ones per sample, and the first value that is neither 0 nor 1
-    // (samples in order, so the earliest range holding one has the first of the whole upload)
+    // one pass per client range: the first value that is neither 0 nor 1 (samples in order, so the
+    // earliest range holding one has the first of the whole upload), and for 0/1 data the range's
+    // CSR columns (in a buffer of the range), set-attribute counts, the per-client bitmaps
+    // (feature-major, 64 samples a word) and whether the last attribute is set in every sample
     const int nc = h->nc;
     std::vector<int> ones(S, 0);
     std::vector<long long> first_bad(nc, -1);
+    std::vector<int> icpt(nc, 1);
+    std::vector<long long> fboff(nc);
+    long long words = 0;
+    for (int c = 0; c < nc; ++c) {
+        fboff[c] = words;
+        words += (long long)d * ((h->ns[c] + 63) / 64);
+    }
+    std::vector<unsigned long long> fbits;
+    std::vector<std::vector<int>> rcols(32);
     if (fmt != FEDNL_FEATURES_DENSE) {
-        for_client_ranges(nc, [&](int, int c0, int c1) {
-            for (int s = h->soff[c0]; s < h->soff[c1]; ++s) {
-                const double* a = features + (size_t)s * d;
-                int n1 = 0;
-                for (int i = 0; i < d; ++i) {
-                    if (a[i] == 1.0) ++n1;
-                    else if (a[i] != 0.0) {
-                        first_bad[c0] = (long long)s * d + i;
-                        return;
+        fbits.assign((size_t)std::max<long long>(1, words), 0ull);
+        for_client_ranges(nc, [&](int t, int c0, int c1) {
+            std::vector<int>& cols = rcols[t];
+            for (int c = c0; c < c1; ++c) {
+                const int W = (h->ns[c] + 63) / 64;
+                for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+                    const double* a = features + (size_t)s * d;
+                    const int ls = s - h->soff[c];
+                    int n1 = 0;
+                    for (int i = 0; i < d; ++i) {
+                        if (a[i] == 1.0) {
+                            ++n1;
+                            cols.push_back(i);
+                            fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
+                        } else if (a[i] != 0.0) {
+                            first_bad[c0] = (long long)s * d + i;
+                            return;
+                        }
                     }
+                    ones[s] = n1;
+                    if (a[d - 1] != 1.0) icpt[c] = 0;
                 }
-                ones[s] = n1;
             }
         });
     }
@@ -1226,46 +1259,24 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         std::vector<int> rowptr(S + 1, 0);
         for (int s = 0; s < S; ++s) rowptr[s + 1] = rowptr[s] + ones[s];
         std::vector<int> colidx(rowptr[S]);
-        std::vector<long long> fboff(nc);
-        long long words = 0;
-        for (int c = 0; c < nc; ++c) {
-            fboff[c] = words;
-            words += (long long)d * ((h->ns[c] + 63) / 64);
-        }
-        std::vector<unsigned long long> fbits(words, 0ull);
-        // second pass: the CSR columns and the per-client bitmaps (feature-major, 64 samples a word)
-        for_client_ranges(nc, [&](int, int c0, int c1) {
-            for (int c = c0; c < c1; ++c) {
-                const int W = (h->ns[c] + 63) / 64;
-                for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
-                    const double* a = features + (size_t)s * d;
-                    const int ls = s - h->soff[c];
-                    int p = rowptr[s];
-                    for (int i = 0; i < d; ++i)
-                        if (a[i] == 1.0) {
-                            colidx[p++] = i;
-                            fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
-                        }
-                }
+        {
+            size_t at = 0;        // the ranges' columns in range order (ranges are contiguous, ascending)
+            for (auto& v : rcols) {
+                if (!v.empty()) std::memcpy(colidx.data() + at, v.data(), v.size() * 4);
+                at += v.size();
+                std::vector<int>().swap(v);
             }
-        });
-        std::vector<int> icpt(h->nc, 1);
-        for (int c = 0; c < h->nc; ++c)
-            for (int s = h->soff[c]; s < h->soff[c + 1]; ++s)
-                if (features[(size_t)s * d + (d - 1)] != 1.0) {
-                    icpt[c] = 0;
-                    break;
-                }
+        }
         HitLists hl;
         h->hits_ready = build_hit_lists(h, rowptr, colidx, icpt, hl);
         h->hits_maxrec = h->hits_ready ? hl.maxrec : 0;
         uint16_t *d_hcode = nullptr, *d_hhits = nullptr;
         uint32_t *d_hseg = nullptr, *d_hrec = nullptr;
         if (h->hits_ready) {
-            h->feat.want(&d_hcode, hl.code.size());
-            h->feat.want(&d_hseg, hl.seg.size());
-            h->feat.want(&d_hrec, hl.rec.size());
-            h->feat.want(&d_hhits, std::max<size_t>(1, hl.hits.size()));
+            h->feat.want(&d_hcode, hl.ncode);
+            h->feat.want(&d_hseg, hl.nseg);
+            h->feat.want(&d_hrec, hl.nrec);
+            h->feat.want(&d_hhits, std::max<size_t>(1, hl.nhits));
         }
         int *d_rowptr, *d_colidx, *d_icpt;
         long long* d_fboff;
@@ -1284,10 +1295,10 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         CK(cudaMemcpy(d_fbits, fbits.data(), words * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_icpt, icpt.data(), h->nc * 4, cudaMemcpyHostToDevice));
         if (h->hits_ready) {
-            CK(cudaMemcpy(d_hcode, hl.code.data(), hl.code.size() * 2, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(d_hseg, hl.seg.data(), hl.seg.size() * 4, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(d_hrec, hl.rec.data(), hl.rec.size() * 4, cudaMemcpyHostToDevice));
-            if (!hl.hits.empty()) CK(cudaMemcpy(d_hhits, hl.hits.data(), hl.hits.size() * 2, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_hcode, hl.code.get(), hl.ncode * 2, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_hseg, hl.seg.get(), hl.nseg * 4, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_hrec, hl.rec.get(), hl.nrec * 4, cudaMemcpyHostToDevice));
+            if (hl.nhits) CK(cudaMemcpy(d_hhits, hl.hits.get(), hl.nhits * 2, cudaMemcpyHostToDevice));
         }
         P.hcode = d_hcode;
         P.hseg = d_hseg;
@@ -1412,17 +1423,31 @@ int fednl_gpu_run(fednl_handle h, int32_t rounds, double* grad_norms)
     return FEDNL_OK;
 }
 
+// One round: the captured graph, then the round's ||g||, l and status copied into one pinned
+// buffer and a single wait (fednl_gpu_run's semantics for one round).
 int fednl_gpu_round(fednl_handle h, fednl_round_stats* stats)
 {
-    double gn = 0.0;
-    int rc = fednl_gpu_run(h, 1, &gn);
+    if (!h) return fail(FEDNL_EINVAL, "null handle");
+    if (!h->shifts_ready) return fail(FEDNL_EINVAL, "call fednl_gpu_init_shifts first");
+    int rc = build_graph(h);
+    if (rc) return rc;
+    if (!h->pin) CK(cudaMallocHost(&h->pin, 32));
+    double* pst = static_cast<double*>(h->pin);
+    int* pstatus = reinterpret_cast<int*>(pst + 2);
+    CK(cudaMemsetAsync(h->dev.status, 0, 4, h->stream));
+    CK(cudaGraphLaunch(h->gexec, h->stream));
+    CK(cudaMemcpyAsync(pst, h->dev.stats, 16, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(pstatus, h->dev.status, 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->rounds_done += 1;
+    const int status = *pstatus;
+    if (status == FEDNL_ETIMEOUT) rc = fail(status, "grid barrier of the Cholesky timed out");
+    else if (status) rc = fail(status, "Option-B matrix not positive definite in one of the rounds");
     if (stats) {
-        stats->round = h ? h->rounds_done - 1 : -1;
+        stats->round = h->rounds_done - 1;
         stats->status = rc == FEDNL_ENOTPD ? FEDNL_ENOTPD : FEDNL_OK;
-        double st[2] = {0, 0};
-        if (h) cudaMemcpy(st, h->dev.stats, 16, cudaMemcpyDeviceToHost);
-        stats->grad_norm = st[0];
-        stats->l = st[1];
+        stats->grad_norm = pst[0];
+        stats->l = pst[1];
     }
     return rc;
 }
