@@ -941,14 +941,15 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 //   0x8000 | m         the segment's m-th entry with several common samples (a record)
 //   0xa000 | i         intercept column (i, d-1): dsum_i
 //   0xc000 | i         diagonal (i, i): dsum_i + lambda
-// Each warp owns a segment of 512 positions.  Its lane 0 first starts bulk copies of the segment's
-// codes and shift values into shared memory (one mbarrier per warp); while they fly the block stages
-// D_s and dsum and the warp sums its segment's records, a lane per record (the warp's FP64
-// instructions then serve up to 32 multi-sample entries at once, not the few lanes of a 32-position
-// row that hold one).  Then the positions are formed from shared memory as k_hess_binary forms them.
+// Each warp owns a segment of 512 positions.  Its lane 0 first starts a bulk copy of the segment's
+// shift values into shared memory (one mbarrier per warp) and every lane loads its 16 codes into
+// registers; while they fly the block stages D_s and dsum and the warp sums its segment's records, a
+// lane per record (the warp's FP64 instructions then serve up to 32 multi-sample entries at once, not
+// the few lanes of a 32-position row that hold one).  Then the positions are formed as
+// k_hess_binary forms them.  64 registers and 4 KB of staging a warp let an SM hold 32 warps.
 constexpr unsigned kHitNone = 0x7fffu;
 
-__host__ __device__ inline size_t hits_stage_bytes(int nt) { return (size_t)(nt / 32) * 512 * 10; }
+__host__ __device__ inline size_t hits_stage_bytes(int nt) { return (size_t)(nt / 32) * 512 * 8; }
 
 __device__ __forceinline__ void bulk_copy_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
 {
@@ -959,10 +960,9 @@ __device__ __forceinline__ void bulk_copy_1d(void* dst, const void* src, unsigne
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, 1) k_hess_hits(Dev P, int mode, int maxrec)
+__global__ void __launch_bounds__(NT, 1024 / NT) k_hess_hits(Dev P, int mode, int maxrec)
 {
-    // [NT / 32][512] shift values, [NT / 32][512] codes, [n] D_s, [d] dsum, [d] diagonal values,
-    // [NT / 32][maxrec] record sums
+    // [NT / 32][512] shift values, [n] D_s, [d] dsum, [d] diagonal values, [NT / 32][maxrec] record sums
     extern __shared__ __align__(16) double s_hx[];
     __shared__ __align__(8) unsigned long long s_bar[NT / 32];
     const int c = P.act ? P.act[blockIdx.y] : blockIdx.y;
@@ -974,20 +974,27 @@ __global__ void __launch_bounds__(NT, 1) k_hess_hits(Dev P, int mode, int maxrec
     const int cnt = live ? min(512, P.U - p_seg) : 0;
     const size_t base = (size_t)c * P.ustr;
     double* s_sh = s_hx + (size_t)warp * 512;
-    unsigned short* s_cd = reinterpret_cast<unsigned short*>(s_hx + (size_t)(NT / 32) * 512) + warp * 512;
-    if (live && lane == 0) {
-        // rows start 16-byte aligned (ustr is a multiple of 32, segments of 512); sizes rounded up to
-        // 16 bytes stay inside the client's row of ustr entries
-        const unsigned bc = (unsigned)((cnt * 2 + 15) & ~15), bs = mode != 1 ? (unsigned)((cnt * 8 + 15) & ~15) : 0u;
+    const bool staged = live && mode != 1;
+    if (staged && lane == 0) {
+        // rows start 16-byte aligned (ustr is a multiple of 32, segments of 512); the size rounded up
+        // to 16 bytes stays inside the client's row of ustr entries
+        const unsigned bs = (unsigned)((cnt * 8 + 15) & ~15);
         mbar_init(&s_bar[warp]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&s_bar[warp])),
-                     "r"(bc + bs)
+                     "r"(bs)
                      : "memory");
-        bulk_copy_1d(s_cd, P.hcode + base + p_seg, bc, &s_bar[warp]);
-        if (bs) bulk_copy_1d(s_sh, P.shift + base + p_seg, bs, &s_bar[warp]);
+        bulk_copy_1d(s_sh, P.shift + base + p_seg, bs, &s_bar[warp]);
     }
-    double* s_D = s_hx + (size_t)(NT / 32) * 640;
+    unsigned cds[8];      // the warp's codes of rows 2 u and 2 u + 1, two to a register
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int t0 = 64 * u + lane, t1 = t0 + 32;
+        const unsigned c0 = t0 < cnt ? (unsigned)P.hcode[base + p_seg + t0] : kHitNone;
+        const unsigned c1 = t1 < cnt ? (unsigned)P.hcode[base + p_seg + t1] : kHitNone;
+        cds[u] = c0 | (c1 << 16);
+    }
+    double* s_D = s_hx + (size_t)(NT / 32) * 512;
     double* s_ds = s_D + n;
     double* s_dl = s_ds + P.d;
     const double* dsum = P.dsum + (size_t)c * P.d;
@@ -1023,17 +1030,18 @@ __global__ void __launch_bounds__(NT, 1) k_hess_hits(Dev P, int mode, int maxrec
             }
         }
         __syncwarp();
-        if (!mbar_wait(&s_bar[warp], 0u)) {     // a copy never completed: report it, form nothing
+        if (staged && !mbar_wait(&s_bar[warp], 0u)) {     // the copy never completed: report it, form nothing
             if (lane == 0) {
                 mbar_wait(&s_bar[warp], 0u);
                 atomicExch(P.status, -5);     // FEDNL_ETIMEOUT
             }
         } else {
+#pragma unroll
             for (int q = 0; q < 16; ++q) {
                 const int t = 32 * q + lane;
                 if (t >= cnt) break;
                 const int p = p_seg + t;
-                const unsigned cd = s_cd[t];
+                const unsigned cd = (cds[q >> 1] >> (16 * (q & 1))) & 0xffffu;
                 double h;
                 bool diag = false;
                 if (cd < kHitNone) h = s_D[cd];
