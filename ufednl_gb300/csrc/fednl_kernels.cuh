@@ -2171,8 +2171,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
         // entries (a lane per multiplier, then a lane per entry) and forms that block's det, its
         // correctly rounded reciprocal and D^{-1} = [[p, q], [q, r]] (a lane per entry).  Six other
         // warps form the multipliers of rows k and k+1 (l1 = fma(p, w1, q w2), l2 = fma(q, w1, r w2)
-        // into Rb / SR) and apply block k (two fused multiply-adds) to every other entry below row
-        // k+1.  Each of their threads owns fixed entries for the whole panel and keeps them in
+        // into Rb / SR, a thread per row and column) and apply block k (two fused multiply-adds) to
+        // every other entry below row k+1.  Each of their threads owns fixed entries for the whole panel and keeps them in
         // registers: block entries e = ut + 192 q of the descending-row list (rows 1..nb-1) and slab
         // entries (row nb-1 - e / ns, slab column e mod ns) likewise, so the entries still active at
         // block k (row > k+1) fill the lowest slots of consecutive threads.  An entry is written to
@@ -2200,8 +2200,8 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kSlotsS; ++q) {
-                const int e = ut + q * (kCoopThreads - 64);
+            for (int q = 0; q < kSlotsS; ++q) {     // the first slab entries on warps 5-7, one per sub-partition
+                const int e = (ut + 96) % (kCoopThreads - 64) + q * (kCoopThreads - 64);
                 is_[q] = -1;
                 ss[q] = 0;
                 vs[q] = 0.0;
@@ -2276,17 +2276,16 @@ __device__ __forceinline__ void chol_body(const Dev& P, const double* __restrict
             } else if (warp != 4) {
                 if (pair) {
                     const double p = s_inv[k], r = s_inv[k + 1], q = s_q[k];
+                    // a thread per (row, column) of the multipliers: warps 1-3, one per sub-partition
                     const int nd = nb - 2 - k;                 // block columns k+2 .. nb-1
-                    if (ut < nd) {
-                        const int j = k + 2 + ut;
-                        const double w1 = Db[k][j], w2 = Db[k + 1][j];
-                        Rb[k][j] = fma(p, w1, __dmul_rn(q, w2));
-                        Rb[k + 1][j] = fma(q, w1, __dmul_rn(r, w2));
-                    } else if (ut < nd + ns) {
-                        const int sl = ut - nd;
-                        const double w1 = Sb[k][sl], w2 = Sb[k + 1][sl];
-                        SR[k][sl] = fma(p, w1, __dmul_rn(q, w2));
-                        SR[k + 1][sl] = fma(q, w1, __dmul_rn(r, w2));
+                    const int o = ut & 1, cix = ut >> 1;
+                    const double ca = o ? q : p, cb = o ? r : q;
+                    if (cix < nd) {
+                        const int j = k + 2 + cix;
+                        Rb[k + o][j] = fma(ca, Db[k][j], __dmul_rn(cb, Db[k + 1][j]));
+                    } else if (cix < nd + ns) {
+                        const int sl = cix - nd;
+                        SR[k + o][sl] = fma(ca, Sb[k][sl], __dmul_rn(cb, Sb[k + 1][sl]));
                     }
                     asm volatile("bar.sync 1, 192;" ::: "memory");
 #pragma unroll
