@@ -269,9 +269,13 @@ __device__ __forceinline__ double fednl_log(double x)
     return __dadd_rn(h, l);
 }
 
+__device__ __forceinline__ double rcp_rn_int(double r);
+
+// 1 / (1 + exp(-m)); the correctly rounded reciprocal from integer arithmetic equals the IEEE
+// division 1.0 / (1 + e) bit for bit and keeps the FP64 pipe free
 __device__ __forceinline__ double fednl_sigmoid(double m)
 {
-    return __ddiv_rn(1.0, __dadd_rn(1.0, fednl_exp(-m)));
+    return rcp_rn_int(__dadd_rn(1.0, fednl_exp(-m)));
 }
 
 // Sum of one aligned 32-term chunk held one term per lane: the halving tree
