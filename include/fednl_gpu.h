@@ -110,6 +110,12 @@ int fednl_gpu_destroy(fednl_handle h);
  * [sum n_i] in {-1,+1}.  Replaces the per-client L2RegulirizeLogisticRegression construction
  * (TrainLoop.h:601-605; logistic_regression.h:26-76). */
 int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels);
+/* Client data as binary features in CSR form (the LIBSVM rows of dataset_loader_fs.h:607-870): for
+ * every sample, clients concatenated in order, the ascending column indices (0-based, < d) of its
+ * attributes equal to 1 (rowptr [sum n_i + 1], colidx [rowptr[sum n_i]]) and its label.  The bit
+ * layout of A_i is packed on the device; the results equal those of fednl_gpu_upload_client_data
+ * with the same features as dense 0/1 rows. */
+int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels);
 
 /* shift_i = H_i(x0), H = mean_i shift_i, x = x0 (x0 NULL = zeros, the reference default).
  * Replaces TrainLoop.h:639-643 and :732-735. */

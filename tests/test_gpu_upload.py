@@ -55,3 +55,37 @@ def test_binary_upload_reports_the_first_non_binary_entry(gpu, pos):
     g2 = f.run(2)
     f.close()
     np.testing.assert_array_equal(g0, g2)
+
+
+@pytest.mark.parametrize("intercept", [True, False])
+def test_csr_upload_packs_the_same_layout(gpu, intercept):
+    """fednl_gpu_upload_client_csr (0/1 features as CSR columns, bit layout packed on the device) gives
+    the same run bit for bit as the dense upload, with and without an intercept column."""
+    from ufednl_gb300 import datagen
+    prob = datagen.binary_problem(21, 33, [40, 75, 64, 129, 12], 0.15, 1e-3)
+    if not intercept:
+        prob = datagen.Problem(prob.d - 1, prob.n_samples, np.ascontiguousarray(prob.features[:, :-1]),
+                               prob.labels, prob.lam)
+    out = []
+    for csr in (False, True):
+        f = gpu.FedNL(prob, "toplek", 4 * prob.d, 1.0, workers=2, csr=csr)
+        out.append((f.run(5), f.x(), f.hess_schedule()))
+        f.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
+def test_csr_upload_rejects_unsorted_columns(gpu):
+    import ctypes as C
+    from ufednl_gb300 import datagen
+    prob = datagen.binary_problem(22, 9, [3, 4], 0.4, 1e-3)
+    f = gpu.FedNL(prob, "topk", 9, 1.0)
+    rp = np.arange(prob.total_samples + 1, dtype=np.int32) * 2
+    ci = np.tile(np.array([5, 3], dtype=np.int32), prob.total_samples)      # descending within each row
+    lab = np.ascontiguousarray(prob.labels)
+    rc = gpu.load().fednl_gpu_upload_client_csr(f._h, rp.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               ci.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               lab.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc != 0 and "ascending" in gpu.load().fednl_gpu_last_error().decode()
+    f.close()

@@ -1188,6 +1188,120 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
     return true;
 }
 
+// The binary layout of the uploaded clients on the device: CSR columns, per-client bitmaps (from the
+// host, or packed on the device by k_pack_bits when fbits_host is null), intercept flags, the
+// common-sample lists when they are built, the Hessian kernels' shared-memory shapes; the labels'
+// device buffer is returned in *lab.
+static int install_binary(fednl_handle h, const std::vector<int>& rowptr, const std::vector<int>& colidx,
+                          const std::vector<int>& icpt, const std::vector<unsigned long long>* fbits_host, double** lab)
+{
+    const int d = h->d, S = h->S, nc = h->nc;
+    Dev& P = h->dev;
+    std::vector<long long> fboff(nc);
+    long long words = 0;
+    for (int c = 0; c < nc; ++c) {
+        fboff[c] = words;
+        words += (long long)d * ((h->ns[c] + 63) / 64);
+    }
+    HitLists hl;
+    h->hits_ready = build_hit_lists(h, rowptr, colidx, icpt, hl);
+    h->hits_maxrec = h->hits_ready ? hl.maxrec : 0;
+    uint16_t *d_hcode = nullptr, *d_hhits = nullptr;
+    uint32_t *d_hseg = nullptr, *d_hrec = nullptr;
+    if (h->hits_ready) {
+        h->feat.want(&d_hcode, hl.ncode);
+        h->feat.want(&d_hseg, hl.nseg);
+        h->feat.want(&d_hrec, hl.nrec);
+        h->feat.want(&d_hhits, std::max<size_t>(1, hl.nhits));
+    }
+    int *d_rowptr, *d_colidx, *d_icpt;
+    long long* d_fboff;
+    unsigned long long* d_fbits;
+    h->feat.want(&d_icpt, nc);
+    h->feat.want(&d_rowptr, S + 1);
+    h->feat.want(&d_colidx, std::max<size_t>(1, colidx.size()));
+    h->feat.want(&d_fboff, nc);
+    h->feat.want(&d_fbits, std::max<long long>(1, words));
+    h->feat.want(lab, S);
+    int rc = h->feat.commit();
+    if (rc) return rc;
+    CK(cudaMemcpy(d_rowptr, rowptr.data(), (S + 1) * 4, cudaMemcpyHostToDevice));
+    if (!colidx.empty()) CK(cudaMemcpy(d_colidx, colidx.data(), colidx.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_fboff, fboff.data(), nc * 8, cudaMemcpyHostToDevice));
+    if (fbits_host) {
+        CK(cudaMemcpy(d_fbits, fbits_host->data(), words * 8, cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemsetAsync(d_fbits, 0, (size_t)std::max<long long>(1, words) * 8, h->stream));
+        k_pack_bits<<<(S + 127) / 128, 128, 0, h->stream>>>(d_rowptr, d_colidx, P.client_of, P.soff, P.ns, d_fboff, S,
+                                                            d_fbits);
+        CKL();
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    CK(cudaMemcpy(d_icpt, icpt.data(), nc * 4, cudaMemcpyHostToDevice));
+    if (h->hits_ready) {
+        CK(cudaMemcpy(d_hcode, hl.code.get(), hl.ncode * 2, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_hseg, hl.seg.get(), hl.nseg * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_hrec, hl.rec.get(), hl.nrec * 4, cudaMemcpyHostToDevice));
+        if (hl.nhits) CK(cudaMemcpy(d_hhits, hl.hits.get(), hl.nhits * 2, cudaMemcpyHostToDevice));
+    }
+    P.hcode = d_hcode;
+    P.hseg = d_hseg;
+    P.hrec = d_hrec;
+    P.hhits = d_hhits;
+    P.icpt = d_icpt;
+    P.rowptr = d_rowptr;
+    P.colidx = d_colidx;
+    P.fboff = d_fboff;
+    P.fbits = d_fbits;
+    int maxW = (h->maxn + 63) / 64;
+    // attribute masks (when they fit), D_s, and the diagonal values
+    size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8 + (size_t)d * 8;
+    h->hess_smem_gl = (size_t)h->maxn * 8 + (size_t)d * 8;
+    h->hess_smem_sm = need <= 200 * 1024 ? need : 0;
+    if (h->hits_ready && hits_smem(h, 512) > 200 * 1024) h->hits_ready = false;
+    h->hess_kind = h->hits_ready ? kHessHits : h->hess_smem_sm ? kHessMasksSmem : kHessMasksGlobal;
+    h->hess_nt = kHessThreads;
+    if (h->hess_smem_gl > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
+    CK(raise_hess_smem(h));
+    if ((size_t)h->maxn * 16 > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
+    if (client_smem(h) > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_client_binary, client_smem(h)));
+    h->binary = 1;
+    return FEDNL_OK;
+}
+
+// the handle's client-data pointers cleared before a new upload
+static void clear_client_data(fednl_handle h)
+{
+    h->feat.release();
+    Dev& P = h->dev;
+    P.rowptr = nullptr;
+    P.colidx = nullptr;
+    P.fbits = nullptr;
+    P.icpt = nullptr;
+    P.A = nullptr;
+    P.hcode = nullptr;
+    P.hseg = nullptr;
+    P.hrec = nullptr;
+    P.hhits = nullptr;
+    h->hits_ready = false;
+}
+
+// after either upload: labels, readiness, and the captured round (its launch shapes may change)
+static int finish_upload(fednl_handle h, double* lab, const double* labels)
+{
+    CK(cudaMemcpy(lab, labels, (size_t)h->S * 8, cudaMemcpyHostToDevice));
+    h->dev.lab = lab;
+    h->data_ready = true;
+    h->shifts_ready = false;
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        cudaGraphDestroy(h->graph);
+        h->gexec = nullptr;
+        h->graph = nullptr;
+    }
+    return FEDNL_OK;
+}
+
 int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
 {
     if (!h || !features || !labels) return fail(FEDNL_EINVAL, "null argument");
@@ -1242,18 +1356,8 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     if (fmt == FEDNL_FEATURES_AUTO) fmt = bad < 0 ? FEDNL_FEATURES_BINARY : FEDNL_FEATURES_DENSE;
     if (fmt == FEDNL_FEATURES_BINARY && bad >= 0)
         return fail(FEDNL_EINVAL, "feature (%d,%d) is not 0/1 in binary format", (int)(bad / d), (int)(bad % d));
-    h->feat.release();
+    clear_client_data(h);
     Dev& P = h->dev;
-    P.rowptr = nullptr;
-    P.colidx = nullptr;
-    P.fbits = nullptr;
-    P.icpt = nullptr;
-    P.A = nullptr;
-    P.hcode = nullptr;
-    P.hseg = nullptr;
-    P.hrec = nullptr;
-    P.hhits = nullptr;
-    h->hits_ready = false;
     double* lab = nullptr;
     if (fmt == FEDNL_FEATURES_BINARY) {
         std::vector<int> rowptr(S + 1, 0);
@@ -1267,61 +1371,8 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
                 std::vector<int>().swap(v);
             }
         }
-        HitLists hl;
-        h->hits_ready = build_hit_lists(h, rowptr, colidx, icpt, hl);
-        h->hits_maxrec = h->hits_ready ? hl.maxrec : 0;
-        uint16_t *d_hcode = nullptr, *d_hhits = nullptr;
-        uint32_t *d_hseg = nullptr, *d_hrec = nullptr;
-        if (h->hits_ready) {
-            h->feat.want(&d_hcode, hl.ncode);
-            h->feat.want(&d_hseg, hl.nseg);
-            h->feat.want(&d_hrec, hl.nrec);
-            h->feat.want(&d_hhits, std::max<size_t>(1, hl.nhits));
-        }
-        int *d_rowptr, *d_colidx, *d_icpt;
-        long long* d_fboff;
-        unsigned long long* d_fbits;
-        h->feat.want(&d_icpt, h->nc);
-        h->feat.want(&d_rowptr, S + 1);
-        h->feat.want(&d_colidx, std::max<size_t>(1, colidx.size()));
-        h->feat.want(&d_fboff, h->nc);
-        h->feat.want(&d_fbits, std::max<long long>(1, words));
-        h->feat.want(&lab, S);
-        int rc = h->feat.commit();
+        int rc = install_binary(h, rowptr, colidx, icpt, &fbits, &lab);
         if (rc) return rc;
-        CK(cudaMemcpy(d_rowptr, rowptr.data(), (S + 1) * 4, cudaMemcpyHostToDevice));
-        if (!colidx.empty()) CK(cudaMemcpy(d_colidx, colidx.data(), colidx.size() * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_fboff, fboff.data(), h->nc * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_fbits, fbits.data(), words * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_icpt, icpt.data(), h->nc * 4, cudaMemcpyHostToDevice));
-        if (h->hits_ready) {
-            CK(cudaMemcpy(d_hcode, hl.code.get(), hl.ncode * 2, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(d_hseg, hl.seg.get(), hl.nseg * 4, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(d_hrec, hl.rec.get(), hl.nrec * 4, cudaMemcpyHostToDevice));
-            if (hl.nhits) CK(cudaMemcpy(d_hhits, hl.hits.get(), hl.nhits * 2, cudaMemcpyHostToDevice));
-        }
-        P.hcode = d_hcode;
-        P.hseg = d_hseg;
-        P.hrec = d_hrec;
-        P.hhits = d_hhits;
-        P.icpt = d_icpt;
-        P.rowptr = d_rowptr;
-        P.colidx = d_colidx;
-        P.fboff = d_fboff;
-        P.fbits = d_fbits;
-        int maxW = (h->maxn + 63) / 64;
-        // attribute masks (when they fit), D_s, and the diagonal values
-        size_t need = (size_t)d * maxW * 8 + (size_t)h->maxn * 8 + (size_t)d * 8;
-        h->hess_smem_gl = (size_t)h->maxn * 8 + (size_t)d * 8;
-        h->hess_smem_sm = need <= 200 * 1024 ? need : 0;
-        if (h->hits_ready && hits_smem(h, 512) > 200 * 1024) h->hits_ready = false;
-        h->hess_kind = h->hits_ready ? kHessHits : h->hess_smem_sm ? kHessMasksSmem : kHessMasksGlobal;
-        h->hess_nt = kHessThreads;
-        if (h->hess_smem_gl > 200 * 1024) return fail(FEDNL_EINVAL, "client too large for the Hessian kernel (n=%d)", h->maxn);
-        CK(raise_hess_smem(h));
-        if ((size_t)h->maxn * 16 > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_grad_binary, (size_t)h->maxn * 16));
-        if (client_smem(h) > 48 * 1024) CK(fednl_raise_dyn_smem((const void*)k_client_binary, client_smem(h)));
-        h->binary = 1;
     } else {
         double* dA;
         h->feat.want(&dA, (size_t)S * d);
@@ -1332,17 +1383,35 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
         P.A = dA;
         h->binary = 0;
     }
-    CK(cudaMemcpy(lab, labels, (size_t)S * 8, cudaMemcpyHostToDevice));
-    P.lab = lab;
-    h->data_ready = true;
-    h->shifts_ready = false;
-    if (h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        cudaGraphDestroy(h->graph);
-        h->gexec = nullptr;
-        h->graph = nullptr;
+    return finish_upload(h, lab, labels);
+}
+
+int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
+{
+    if (!h || !rowptr || !labels) return fail(FEDNL_EINVAL, "null argument");
+    const int d = h->d, S = h->S, nc = h->nc;
+    for (int s = 0; s < S; ++s)
+        if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
+    if (h->desc.feature_format == FEDNL_FEATURES_DENSE)
+        return fail(FEDNL_EINVAL, "the CSR upload takes binary features (the handle asks for the dense format)");
+    if (rowptr[0] != 0) return fail(FEDNL_EINVAL, "rowptr[0] is not 0");
+    for (int s = 0; s < S; ++s) {
+        if (rowptr[s + 1] < rowptr[s]) return fail(FEDNL_EINVAL, "rowptr decreases at sample %d", s);
+        if (rowptr[s + 1] > rowptr[s] && !colidx) return fail(FEDNL_EINVAL, "null colidx");
+        for (int u = rowptr[s]; u < rowptr[s + 1]; ++u)
+            if (colidx[u] < 0 || colidx[u] >= d || (u > rowptr[s] && colidx[u] <= colidx[u - 1]))
+                return fail(FEDNL_EINVAL, "sample %d: columns not ascending in [0, d)", s);
     }
-    return FEDNL_OK;
+    std::vector<int> rp(rowptr, rowptr + S + 1), ci(colidx ? colidx : rowptr, colidx ? colidx + rowptr[S] : rowptr);
+    std::vector<int> icpt(nc, 1);        // the last attribute set in every sample of the client
+    for (int c = 0; c < nc; ++c)
+        for (int s = h->soff[c]; s < h->soff[c + 1] && icpt[c]; ++s)
+            if (rp[s + 1] == rp[s] || ci[rp[s + 1] - 1] != d - 1) icpt[c] = 0;
+    clear_client_data(h);
+    double* lab = nullptr;
+    int rc = install_binary(h, rp, ci, icpt, nullptr, &lab);
+    if (rc) return rc;
+    return finish_upload(h, lab, labels);
 }
 
 int fednl_gpu_init_shifts(fednl_handle h, const double* x0)

@@ -424,6 +424,20 @@ __global__ void k_grad_binary(Dev P)
     else P.gc[(size_t)c * P.d + j] = acc;
 }
 
+// The clients' bit layout (k_hess_binary's masks: per client, per attribute, one bit per sample,
+// 64 samples a word) from the samples' CSR columns, one thread per sample: the CSR upload packs A_i
+// on the device (dataset_loader_fs.h:607-870 reads the same rows into the reference's matrices).
+__global__ void k_pack_bits(const int* __restrict__ rowptr, const int* __restrict__ colidx, const int* client_of,
+                            const int* soff, const int* ns, const long long* fboff, int S, unsigned long long* fbits)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int c = client_of[s], ls = s - soff[c], W = (ns[c] + 63) >> 6;
+    unsigned long long* fb = fbits + fboff[c];
+    for (int u = rowptr[s]; u < rowptr[s + 1]; ++u)
+        atomicOr(fb + (size_t)colidx[u] * W + (ls >> 6), 1ull << (ls & 63));
+}
+
 // ---- 1 + 2 fused for binary features: one CTA per client -----------------------------------
 // The client's margins, sigmoid values and weights (k_margin_binary's operations, one sample per
 // thread), then its gradient and attribute sums (k_grad_binary's, blocked order, a lane pair per

@@ -10,6 +10,7 @@
 
 #include "fednl_gpu.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -164,6 +165,10 @@ struct Dataset {
     int n = 0;
     std::vector<double> x;           // [n][d] row-major
     std::vector<double> y;           // +-1
+    // the same rows as CSR columns of the attributes equal to 1 (ascending), valid when every
+    // value of the file is 0 or 1 (binary)
+    std::vector<int32_t> rp, cols;
+    bool binary = true;
 };
 
 template <class F>
@@ -244,10 +249,13 @@ int load_libsvm(const std::string& path, bool add_intercept, Dataset& ds, std::s
     ds.y.assign(ds.n, 0.0);
     const double avg = ((double)lmin + (double)lmax) / 2.0;
     int s = 0;
+    std::vector<int32_t> touched;
+    ds.rp.assign(1, 0);
     for (auto& ln : lines) {
         split_tokens(ln.first, ln.second, [](char c) { return c == ' ' || c == '\t'; }, fields);
         if (fields.empty()) continue;
         double* row = ds.x.data() + (size_t)s * ds.d;
+        touched.clear();
         for (auto& fd : fields) {
             split_tokens(fd.first, fd.second, [](char c) { return c == ':'; }, kv);
             if (kv.size() == 1) {
@@ -265,9 +273,21 @@ int load_libsvm(const std::string& path, bool add_intercept, Dataset& ds, std::s
                     return -4;
                 }
                 row[r] = v;
+                touched.push_back((int32_t)r);
             }
         }
-        if (add_intercept) row[ds.d - 1] = 1.0;
+        if (add_intercept) {
+            row[ds.d - 1] = 1.0;
+            touched.push_back(ds.d - 1);
+        }
+        // the row's final values (a repeated index keeps its last value) as ascending CSR columns
+        std::sort(touched.begin(), touched.end());
+        touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+        for (int32_t col : touched) {
+            if (row[col] == 1.0) ds.cols.push_back(col);
+            else if (row[col] != 0.0) ds.binary = false;
+        }
+        ds.rp.push_back((int32_t)ds.cols.size());
         ++s;
     }
     return 0;
@@ -486,10 +506,24 @@ static int execute_local_impl(const char* command, bool pp, fednl_result_callbac
     std::vector<int32_t> order(ds.n);
     for (int i = 0; i < ds.n; ++i) order[i] = i;
     if (reshuffle) shuffle_all(order, reshuffle_seed);
-    std::vector<double> feat((size_t)per * n_clients * d), lab((size_t)per * n_clients);
-    for (int s = 0; s < per * n_clients; ++s) {
-        std::memcpy(&feat[(size_t)s * d], &ds.x[(size_t)order[s] * d], (size_t)d * sizeof(double));
-        lab[s] = ds.y[order[s]];
+    // 0/1 data goes up as the split's CSR rows (packed into the bit layout on the device), other
+    // data as dense rows
+    std::vector<double> feat, lab((size_t)per * n_clients);
+    std::vector<int32_t> crp, ccols;
+    if (ds.binary) {
+        crp.assign(1, 0);
+        for (int s = 0; s < per * n_clients; ++s) {
+            const int o = order[s];
+            ccols.insert(ccols.end(), ds.cols.begin() + ds.rp[o], ds.cols.begin() + ds.rp[o + 1]);
+            crp.push_back((int32_t)ccols.size());
+            lab[s] = ds.y[o];
+        }
+    } else {
+        feat.resize((size_t)per * n_clients * d);
+        for (int s = 0; s < per * n_clients; ++s) {
+            std::memcpy(&feat[(size_t)s * d], &ds.x[(size_t)order[s] * d], (size_t)d * sizeof(double));
+            lab[s] = ds.y[order[s]];
+        }
     }
     std::vector<int32_t> ns(n_clients, per);
 
@@ -518,7 +552,9 @@ static int execute_local_impl(const char* command, bool pp, fednl_result_callbac
     if (fednl_gpu_create(&desc, &h) != 0) return -7;
     // x0 from RandomGenRealLinear(0, 0): every coordinate is 0 whatever the seed (Args.h:235)
     std::vector<double> x0(d, 0.0), x(d), g(d);
-    if (fednl_gpu_upload_client_data(h, feat.data(), lab.data()) != 0 || fednl_gpu_init_shifts(h, x0.data()) != 0) {
+    const int up = ds.binary ? fednl_gpu_upload_client_csr(h, crp.data(), ccols.empty() ? crp.data() : ccols.data(), lab.data())
+                             : fednl_gpu_upload_client_data(h, feat.data(), lab.data());
+    if (up != 0 || fednl_gpu_init_shifts(h, x0.data()) != 0) {
         fednl_gpu_destroy(h);
         return -7;
     }

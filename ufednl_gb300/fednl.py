@@ -78,7 +78,7 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_autotune", "fednl_gpu_autotune_shapes", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
            "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate",
            "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref",
-           "fednl_gpu_hess_schedule", "fednl_gpu_set_hess_schedule"]
+           "fednl_gpu_hess_schedule", "fednl_gpu_set_hess_schedule", "fednl_gpu_upload_client_csr"]
 
 _lib = None
 
@@ -164,7 +164,8 @@ def load(build_if_missing: bool = True):
                        "fednl_gpu_get_client_grad": [vp, C.c_int32, dp], "fednl_gpu_get_diff": [vp, C.c_int32, dp],
                        "fednl_gpu_autotune": [vp, ip, dp], "fednl_gpu_autotune_shapes": [vp, ip, ip, ip, dp],
                        "fednl_mx_autotune": [vp, ip, ip, dp], "fednl_gpu_hess_schedule": [vp, ip, ip, ip],
-                       "fednl_gpu_set_hess_schedule": [vp, C.c_int32, C.c_int32]}.items():
+                       "fednl_gpu_set_hess_schedule": [vp, C.c_int32, C.c_int32],
+                       "fednl_gpu_upload_client_csr": [vp, ip, ip, dp]}.items():
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.fednl_mx_get_l.argtypes = [vp]
@@ -311,10 +312,12 @@ class FedNL:
     def __init__(self, prob, compressor, k: int, alpha: float, lda: int | None = None, workers: int = 1,
                  seed_base: int = 123, toplek_seed: int = 1234, x0=None, feature_format: int = 0,
                  clients_per_round: int = 0, client_seed: int = 1234, option_a: bool = False,
-                 line_search=None, track_f: bool = False, order: str = "fixed", hess_schedule=None):
+                 line_search=None, track_f: bool = False, order: str = "fixed", hess_schedule=None,
+                 csr: bool = False):
         """order: "fixed" (the engine's own order, bit-identical to the test oracle) or "reference"
         (the reference's operation order, bit-identical to the reference's rounds).  hess_schedule:
-        (kernel, threads) of the binary Hessian from the initial shifts on (see set_hess_schedule)."""
+        (kernel, threads) of the binary Hessian from the initial shifts on (see set_hess_schedule).
+        csr: upload 0/1 features as CSR columns, packed into the bit layout on the device."""
         self.d = prob.d
         self.lda = lda or reference_lda(prob.d)
         self.n_clients = prob.n_clients
@@ -334,7 +337,16 @@ class FedNL:
         try:
             f = np.ascontiguousarray(prob.features, dtype=np.float64)
             b = np.ascontiguousarray(prob.labels, dtype=np.float64)
-            _check(load().fednl_gpu_upload_client_data(self._h, _dp(f), _dp(b)))
+            if csr:
+                rows, cols = np.nonzero(f)
+                rp = np.zeros(f.shape[0] + 1, dtype=np.int32)
+                np.add.at(rp, rows + 1, 1)
+                rp = np.cumsum(rp).astype(np.int32)
+                ci = np.ascontiguousarray(cols, dtype=np.int32)
+                _check(load().fednl_gpu_upload_client_csr(self._h, _ip(rp), _ip(ci if ci.size else np.zeros(1, np.int32)),
+                                                          _dp(b)))
+            else:
+                _check(load().fednl_gpu_upload_client_data(self._h, _dp(f), _dp(b)))
             if hess_schedule is not None:
                 self.set_hess_schedule(*hess_schedule)
             xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
