@@ -2040,8 +2040,9 @@ struct GridSync {
         if (threadIdx.x == 0) {
             epoch += 1;
             const unsigned target = epoch * n;
-            __threadfence();
-            atomicAdd(bar, 1u);
+            // arrival with release semantics: after the CTA barrier it publishes every thread's writes
+            // of this CTA (the acquire load below makes the other CTAs' writes visible to this one)
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
             volatile unsigned* verr = bar + 2;
             int ok = 1;
             const long long t0 = clock64();
@@ -2059,7 +2060,7 @@ struct GridSync {
                     break;
                 }
             }
-            __threadfence();
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");      // the other CTAs' writes, for this CTA
             if (*verr) ok = 0;
             s_ok = ok;
         }
