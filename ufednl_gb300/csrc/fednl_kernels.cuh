@@ -1269,7 +1269,7 @@ __device__ __forceinline__ void select_finish(const SelectDraws& dr, const int* 
 // vals: [n_mat][ustr] packed upper values (signed), rows 16-byte aligned (ustr even); F: [n_mat]
 // squared Frobenius norms.  Output: sel bitmap per matrix, cnt (entries kept before the rounding
 // draw), TopLEK draw request.  err: set to 1 if a bounded wait ran out.
-__global__ void __maxnreg__(128) k_select(const double* __restrict__ vals, int ustr, int U, int k,
+__global__ void __maxnreg__(192) k_select(const double* __restrict__ vals, int ustr, int U, int k,
                                                         int lek, double delta, double* F,
                                                         unsigned* sel, int SW, int* cnt, int* needs,
                                                         double* pdraw, int* minidx, int* err, const int* act,
