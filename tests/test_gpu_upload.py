@@ -89,3 +89,25 @@ def test_csr_upload_rejects_unsorted_columns(gpu):
                                                lab.ctypes.data_as(C.POINTER(C.c_double)))
     assert rc != 0 and "ascending" in gpu.load().fednl_gpu_last_error().decode()
     f.close()
+
+
+def test_binary_upload_negative_zero_and_row_tail(gpu):
+    """The scan skips four +0.0 values at a time by their bits: -0.0 (sign bit set) still counts as 0,
+    and the values past the last multiple of four in a row (d = 41) are checked one by one."""
+    from ufednl_gb300 import datagen
+    prob = datagen.binary_problem(23, 41, [30, 50, 21, 64], 0.15, 1e-3)
+    neg = datagen.Problem(prob.d, prob.n_samples, np.where(prob.features == 0.0, -0.0, prob.features),
+                          prob.labels, prob.lam)
+    assert np.signbit(neg.features).sum() > 0
+    out = []
+    for p in (prob, neg):
+        f = gpu.FedNL(p, "topk", 3 * 41, 1.0, feature_format=1)
+        out.append((f.run(3), f.x()))
+        f.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    for s, i in [(17, 40), (100, 37), (0, 1)]:
+        bad = datagen.Problem(prob.d, prob.n_samples, prob.features.copy(), prob.labels, prob.lam)
+        bad.features[s, i] = 0.5
+        with pytest.raises(gpu.FedNLError, match=rf"feature \({s},{i}\) is not 0/1"):
+            gpu.FedNL(bad, "topk", 3 * 41, 1.0, feature_format=1)

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <condition_variable>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -25,6 +26,8 @@
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 using namespace fednl;
 static_assert(kCholNB == 32, "fednl_chol_work_elems sizes the panel buffer for 32-row panels");
@@ -1053,23 +1056,97 @@ int fednl_gpu_destroy(fednl_handle h)
     return FEDNL_OK;
 }
 
-// Host threads for the conversion of the uploaded rows: clients are split into contiguous ranges
-// (each client's CSR range and bitmap block are disjoint, so the ranges need no locking).
-static void for_client_ranges(int nc, const std::function<void(int, int, int)>& f)
+// Worker threads for the conversion of uploaded rows, started on first use and kept for the
+// process: an upload runs three parallel passes, and starting 16 threads for each cost more than
+// a pass's own work.  One job at a time (callers are serialised); the caller runs part 0.  A
+// forked child, which holds none of its parent's threads, starts a pool of its own.
+class RangePool {
+public:
+    static RangePool& get()
+    {
+        static std::mutex pm;
+        static RangePool* pool = nullptr;
+        std::lock_guard<std::mutex> lk(pm);
+        if (!pool || pool->pid_ != getpid()) pool = new RangePool();    // a parent's pool is left as is
+        return *pool;
+    }
+    int size() const { return nworkers_ + 1; }
+    // f(0 .. n-1), n <= size(), part 0 on the calling thread
+    void run(int n, const std::function<void(int)>& f)
+    {
+        std::lock_guard<std::mutex> one(run_m_);
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = &f;
+            njob_ = n;
+            left_ = n - 1;
+            ++gen_;
+        }
+        go_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&] { return left_ == 0; });
+    }
+
+private:
+    RangePool() : pid_(getpid())
+    {
+        const unsigned hc = std::thread::hardware_concurrency();
+        nworkers_ = std::max(0, std::min<int>((int)(hc ? hc : 1), 32) - 1);
+        for (int i = 1; i <= nworkers_; ++i) std::thread(&RangePool::work, this, i).detach();
+    }
+    void work(int id)
+    {
+        unsigned long long seen = 0;
+        for (;;) {
+            const std::function<void(int)>* f;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                go_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (id >= njob_) continue;    // not a part of this job
+                f = job_;
+            }
+            (*f)(id);
+            std::lock_guard<std::mutex> lk(m_);
+            if (--left_ == 0) done_.notify_one();
+        }
+    }
+    const pid_t pid_;
+    int nworkers_ = 0;
+    std::mutex run_m_, m_;
+    std::condition_variable go_, done_;
+    const std::function<void(int)>* job_ = nullptr;
+    unsigned long long gen_ = 0;
+    int njob_ = 0, left_ = 0;
+};
+
+// The conversion of the uploaded rows over client ranges: clients are split into contiguous
+// ranges in order (each client's CSR range and bitmap block are disjoint, so the ranges need no
+// locking), of about equal work when work[c + 1] - work[c] gives client c's (a prefix over the
+// clients), else of equal client counts.  f(range, first client, end client).
+static void for_client_ranges(int nc, const std::function<void(int, int, int)>& f,
+                              const std::vector<long long>* work = nullptr)
 {
-    const unsigned hc = std::thread::hardware_concurrency();
-    const int nth = std::max(1, std::min<int>({(int)(hc ? hc : 1), 32, nc}));
+    RangePool& pool = RangePool::get();
+    const int nth = std::max(1, std::min(pool.size(), nc));
     if (nth == 1) {
         f(0, 0, nc);
         return;
     }
-    std::vector<std::thread> ts;
-    const int per = (nc + nth - 1) / nth;
-    for (int t = 0; t < nth; ++t) {
-        const int c0 = t * per, c1 = std::min(nc, c0 + per);
-        if (c0 < c1) ts.emplace_back(f, t, c0, c1);
+    std::vector<int> cut(nth + 1, nc);
+    cut[0] = 0;
+    for (int t = 1; t < nth; ++t) {
+        int c = (int)(((long long)nc * t + nth - 1) / nth);
+        if (work) {
+            const long long goal = (*work)[nc] * t / nth;
+            c = (int)(std::lower_bound(work->begin(), work->begin() + nc + 1, goal) - work->begin());
+        }
+        cut[t] = std::min(nc, std::max(cut[t - 1], c));
     }
-    for (auto& th : ts) th.join();
+    pool.run(nth, [&](int t) {
+        if (cut[t] < cut[t + 1]) f(t, cut[t], cut[t + 1]);
+    });
 }
 
 // Common-sample lists of the binary Hessian (k_hess_hits), from the CSR rows of the upload: each
@@ -1091,7 +1168,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
 {
     const int nc = h->nc, d = h->d, U = h->U, nseg = h->nseg;
     if (h->maxn > 0x7ffe || d > 0x1fff) return false;
-    std::vector<long long> pairs(nc, 0);
+    std::vector<long long> pairs(nc, 0), work(nc + 1, 0);
     long long total = 0;
     for (int c = 0; c < nc; ++c) {
         for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
@@ -1100,6 +1177,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
         }
         if (pairs[c] > 16ll * U) return false;
         total += pairs[c];
+        work[c + 1] = work[c] + 8 * pairs[c] + U;     // two walks of the pairs, one of the positions
     }
     if (total > (64ll << 20)) return false;
     auto for_pairs = [&](int c, auto&& f) {   // f(local sample, position)
@@ -1115,7 +1193,8 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
         }
     };
     // one pass per client range: each client's codes in place, its records (client-relative starts
-    // of their samples), samples and per-segment record counts in the client's own buffers
+    // of their samples), samples and per-segment record counts in the client's own buffers (a
+    // record holds two samples or more: at most pairs / 2 records, pairs samples)
     struct Local {
         std::vector<uint32_t> rec, seg;
         std::vector<uint16_t> hits;
@@ -1125,34 +1204,48 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
     L.ncode = (size_t)nc * h->ustr;
     L.code.reset(new uint16_t[L.ncode]);
     for_client_ranges(nc, [&](int, int c0, int c1) {
-        std::vector<int> cnt(U), at(U);
+        // per position: its samples so far (high 16 bits) and the first of them (low 16 bits); after
+        // the segment walk, a multi-sample position's next slot in the client's samples with bit 31
+        // set, else 0
+        std::vector<uint32_t> cf(U);
         for (int c = c0; c < c1; ++c) {
             Local& o = loc[c];
-            std::fill(cnt.begin(), cnt.end(), 0);
-            uint16_t* code = L.code.get() + (size_t)c * h->ustr;
-            std::fill(code, code + h->ustr, (uint16_t)kHitNone);
+            std::fill(cf.begin(), cf.end(), 0u);
             for_pairs(c, [&](int ls, int p) {
-                if (cnt[p]++ == 0) code[p] = (uint16_t)ls;
+                const uint32_t v = cf[p];
+                cf[p] = v ? v + 0x10000u : 0x10000u | (uint32_t)ls;
             });
+            uint16_t* code = L.code.get() + (size_t)c * h->ustr;
             o.seg.resize((size_t)nseg + 1);
+            o.rec.resize((size_t)(pairs[c] / 2));
             uint32_t r = 0, e = 0;
             for (int g = 0; g < nseg; ++g) {
                 o.seg[g] = r;
                 const uint32_t rg = r;
-                for (int p = g * 512; p < std::min(U, g * 512 + 512); ++p)
-                    if (cnt[p] >= 2) {
+                for (int p = g * 512; p < std::min(U, g * 512 + 512); ++p) {
+                    const uint32_t v = cf[p];
+                    if (v < 0x20000u) {          // no sample, or one
+                        code[p] = v ? (uint16_t)(v & 0xffffu) : (uint16_t)kHitNone;
+                        cf[p] = 0;
+                    } else {
                         code[p] = (uint16_t)(0x8000u | (r - rg));
-                        o.rec.push_back(e);
-                        ++r;
-                        at[p] = (int)e;
-                        e += (uint32_t)cnt[p];
+                        o.rec[r++] = e;
+                        cf[p] = 0x80000000u | e;
+                        e += v >> 16;
                     }
+                }
                 o.maxrec = std::max(o.maxrec, (int)(r - rg));
             }
             o.seg[nseg] = r;
+            o.rec.resize(r);
+            std::fill(code + U, code + h->ustr, (uint16_t)kHitNone);
             o.hits.resize(e);
             for_pairs(c, [&](int ls, int p) {
-                if (cnt[p] >= 2) o.hits[at[p]++] = (uint16_t)ls;
+                const uint32_t v = cf[p];
+                if (v >> 31) {
+                    o.hits[v & 0x7fffffffu] = (uint16_t)ls;
+                    cf[p] = v + 1;
+                }
             });
             for (int j = 0; j < d; ++j) {
                 code[j * (j + 1) / 2 + j] = (uint16_t)(0xc000u | (unsigned)j);
@@ -1160,7 +1253,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
                     for (int i = 0; i < j; ++i) code[j * (j + 1) / 2 + i] = (uint16_t)(0xa000u | (unsigned)i);
             }
         }
-    });
+    }, &work);
     std::vector<long long> rbase(nc + 1, 0), hbase(nc + 1, 0);
     for (int c = 0; c < nc; ++c) {
         rbase[c + 1] = rbase[c] + (long long)loc[c].rec.size();
@@ -1184,7 +1277,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
             for (int g = 0; g <= nseg; ++g) L.seg[(size_t)c * (nseg + 1) + g] = (uint32_t)(rbase[c] + o.seg[g]);
             if (!o.hits.empty()) std::memcpy(L.hits.get() + hbase[c], o.hits.data(), o.hits.size() * 2);
         }
-    });
+    }, &hbase);
     return true;
 }
 
@@ -1325,6 +1418,7 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     }
     std::vector<unsigned long long> fbits;
     std::vector<std::vector<int>> rcols(32);
+    const std::vector<long long> rows(h->soff.begin(), h->soff.end());     // ranges of equal sample counts
     if (fmt != FEDNL_FEATURES_DENSE) {
         fbits.assign((size_t)std::max<long long>(1, words), 0ull);
         for_client_ranges(nc, [&](int t, int c0, int c1) {
@@ -1335,21 +1429,29 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
                     const double* a = features + (size_t)s * d;
                     const int ls = s - h->soff[c];
                     int n1 = 0;
-                    for (int i = 0; i < d; ++i) {
-                        if (a[i] == 1.0) {
-                            ++n1;
-                            cols.push_back(i);
-                            fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
-                        } else if (a[i] != 0.0) {
-                            first_bad[c0] = (long long)s * d + i;
-                            return;
+                    for (int i0 = 0; i0 < d; i0 += 4) {
+                        const int i1 = std::min(d, i0 + 4);
+                        if (i1 - i0 == 4) {      // four +0.0 values (all bits clear): nothing to record
+                            uint64_t w[4];
+                            std::memcpy(w, a + i0, sizeof w);
+                            if ((w[0] | w[1] | w[2] | w[3]) == 0) continue;
+                        }
+                        for (int i = i0; i < i1; ++i) {
+                            if (a[i] == 1.0) {
+                                ++n1;
+                                cols.push_back(i);
+                                fbits[fboff[c] + (size_t)i * W + (ls >> 6)] |= 1ull << (ls & 63);
+                            } else if (a[i] != 0.0) {
+                                first_bad[c0] = (long long)s * d + i;
+                                return;
+                            }
                         }
                     }
                     ones[s] = n1;
                     if (a[d - 1] != 1.0) icpt[c] = 0;
                 }
             }
-        });
+        }, &rows);
     }
     long long bad = -1;
     for (int c = 0; c < nc && bad < 0; ++c) bad = first_bad[c];
