@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <condition_variable>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <map>
 #include <memory>
@@ -1024,6 +1025,20 @@ static int create_impl(const fednl_problem_desc* desc, fednl_handle* out, int64_
     return FEDNL_OK;
 }
 
+// Host-side exceptions (a failed host allocation in the conversion of uploaded rows) end at the C
+// boundary as error codes.
+template <class F>
+static int host_guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(FEDNL_ENOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(FEDNL_EINVAL, "host error: %s", e.what());
+    }
+}
+
 extern "C" {
 
 int fednl_gpu_create(const fednl_problem_desc* desc, fednl_handle* out)
@@ -1080,12 +1095,22 @@ public:
             job_ = &f;
             njob_ = n;
             left_ = n - 1;
+            err_ = nullptr;
             ++gen_;
         }
         go_.notify_all();
-        f(0);
-        std::unique_lock<std::mutex> lk(m_);
-        done_.wait(lk, [&] { return left_ == 0; });
+        std::exception_ptr err;
+        try {
+            f(0);
+        } catch (...) {
+            err = std::current_exception();    // the workers still finish their parts first
+        }
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            done_.wait(lk, [&] { return left_ == 0; });
+            if (!err) err = err_;
+        }
+        if (err) std::rethrow_exception(err);    // the first part's exception, on the caller's thread
     }
 
 private:
@@ -1107,8 +1132,14 @@ private:
                 if (id >= njob_) continue;    // not a part of this job
                 f = job_;
             }
-            (*f)(id);
+            std::exception_ptr err;
+            try {
+                (*f)(id);
+            } catch (...) {
+                err = std::current_exception();
+            }
             std::lock_guard<std::mutex> lk(m_);
+            if (err && !err_) err_ = err;
             if (--left_ == 0) done_.notify_one();
         }
     }
@@ -1117,6 +1148,7 @@ private:
     std::mutex run_m_, m_;
     std::condition_variable go_, done_;
     const std::function<void(int)>* job_ = nullptr;
+    std::exception_ptr err_;
     unsigned long long gen_ = 0;
     int njob_ = 0, left_ = 0;
 };
@@ -1395,7 +1427,7 @@ static int finish_upload(fednl_handle h, double* lab, const double* labels)
     return FEDNL_OK;
 }
 
-int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
+static int upload_client_data_impl(fednl_handle h, const double* features, const double* labels)
 {
     if (!h || !features || !labels) return fail(FEDNL_EINVAL, "null argument");
     int d = h->d, S = h->S;
@@ -1488,7 +1520,12 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     return finish_upload(h, lab, labels);
 }
 
-int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
+int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const double* labels)
+{
+    return host_guarded([&] { return upload_client_data_impl(h, features, labels); });
+}
+
+static int upload_client_csr_impl(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
 {
     if (!h || !rowptr || !labels) return fail(FEDNL_EINVAL, "null argument");
     const int d = h->d, S = h->S, nc = h->nc;
@@ -1514,6 +1551,11 @@ int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int
     int rc = install_binary(h, rp, ci, icpt, nullptr, &lab);
     if (rc) return rc;
     return finish_upload(h, lab, labels);
+}
+
+int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
+{
+    return host_guarded([&] { return upload_client_csr_impl(h, rowptr, colidx, labels); });
 }
 
 int fednl_gpu_init_shifts(fednl_handle h, const double* x0)
