@@ -117,6 +117,24 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
  * with the same features as dense 0/1 rows. */
 int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels);
 
+/* The common-sample lists that both uploads build for the binary Hessian's list kernel, built on the
+ * host from 0/1 features given as CSR rows (as for fednl_gpu_upload_client_csr; clients' samples in
+ * order, n_samples[c] of client c); no device is used.  Per client c and upper position
+ * p = b (b + 1) / 2 + a (a <= b), code[c * ustr + p] (ustr = U rounded up to a multiple of 32) is
+ * 0x7fff when no sample holds both attributes, the client-local index of the one sample that does,
+ * 0x8000 | the number of its record within the 512-position segment when several do, 0xc000 | a on
+ * the diagonal, and 0xa000 | a in the last column when every sample of the client has the last
+ * attribute set (an intercept, whose entries come from attribute sums); padding is 0x7fff.
+ * seg[c * (nseg + 1) + g] is the first record of segment g (nseg = ceil(U / 512)), rec[r] the first
+ * of record r's samples in hits (client-local indices in sample order; rec[records] = their total).
+ * sizes[0..3] receive the entry counts of code, seg, rec and hits and *maxrec the most records in
+ * one segment (at least 1); call with NULL outputs to get the sizes.  Returns FEDNL_EINVAL when the
+ * rows are bad or the lists are not built for this problem (a client over 0x7ffe samples, d over
+ * 0x1fff, over 16 sample pairs per upper position in a client, over 64 M pairs in all). */
+int fednl_gpu_hit_lists(int32_t d, int32_t nclients, const int32_t* n_samples, const int32_t* rowptr,
+                        const int32_t* colidx, int64_t* sizes, int32_t* maxrec, uint16_t* code, uint32_t* seg,
+                        uint32_t* rec, uint16_t* hits);
+
 /* shift_i = H_i(x0), H = mean_i shift_i, x = x0 (x0 NULL = zeros, the reference default).
  * Replaces TrainLoop.h:639-643 and :732-735. */
 int fednl_gpu_init_shifts(fednl_handle h, const double* x0);

@@ -1186,6 +1186,12 @@ static void for_client_ranges(int nc, const std::function<void(int, int, int)>& 
 // adds the sample to upper position b (b + 1) / 2 + a.  Built only when the lists stay small (at
 // most 16 pairs per upper position in every client, 64 M in all) and the codes can hold the
 // sample and attribute indices.
+// The problem's shape as the lists builder reads it (from a handle, or from the host-only entry).
+struct ListShape {
+    int nc, d, U, ustr, nseg, maxn;
+    const int32_t* soff;    // [nc + 1] first sample of each client
+};
+
 struct HitLists {
     std::unique_ptr<uint16_t[]> code;    // [nc][ustr]
     std::unique_ptr<uint32_t[]> seg;     // [nc][nseg + 1]
@@ -1195,15 +1201,15 @@ struct HitLists {
     int maxrec = 0;
 };
 
-static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, const std::vector<int>& colidx,
+static bool build_hit_lists(const ListShape& h, const std::vector<int>& rowptr, const std::vector<int>& colidx,
                             const std::vector<int>& icpt, HitLists& L)
 {
-    const int nc = h->nc, d = h->d, U = h->U, nseg = h->nseg;
-    if (h->maxn > 0x7ffe || d > 0x1fff) return false;
+    const int nc = h.nc, d = h.d, U = h.U, nseg = h.nseg;
+    if (h.maxn > 0x7ffe || d > 0x1fff) return false;
     std::vector<long long> pairs(nc, 0), work(nc + 1, 0);
     long long total = 0;
     for (int c = 0; c < nc; ++c) {
-        for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+        for (int s = h.soff[c]; s < h.soff[c + 1]; ++s) {
             const long long m = rowptr[s + 1] - rowptr[s] - (icpt[c] ? 1 : 0);
             pairs[c] += m * (m - 1) / 2;
         }
@@ -1214,13 +1220,13 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
     if (total > (64ll << 20)) return false;
     auto for_pairs = [&](int c, auto&& f) {   // f(local sample, position)
         const int last = icpt[c] ? d - 1 : d;
-        for (int s = h->soff[c]; s < h->soff[c + 1]; ++s) {
+        for (int s = h.soff[c]; s < h.soff[c + 1]; ++s) {
             const int b0 = rowptr[s], b1 = rowptr[s + 1];
             for (int y = b0; y < b1; ++y) {
                 const int b = colidx[y];
                 if (b >= last) break;
                 const int pb = b * (b + 1) / 2;
-                for (int x = b0; x < y; ++x) f(s - h->soff[c], pb + colidx[x]);
+                for (int x = b0; x < y; ++x) f(s - h.soff[c], pb + colidx[x]);
             }
         }
     };
@@ -1233,7 +1239,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
         int maxrec = 0;
     };
     std::vector<Local> loc(nc);
-    L.ncode = (size_t)nc * h->ustr;
+    L.ncode = (size_t)nc * h.ustr;
     L.code.reset(new uint16_t[L.ncode]);
     for_client_ranges(nc, [&](int, int c0, int c1) {
         // per position: its samples so far (high 16 bits) and the first of them (low 16 bits); after
@@ -1247,7 +1253,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
                 const uint32_t v = cf[p];
                 cf[p] = v ? v + 0x10000u : 0x10000u | (uint32_t)ls;
             });
-            uint16_t* code = L.code.get() + (size_t)c * h->ustr;
+            uint16_t* code = L.code.get() + (size_t)c * h.ustr;
             o.seg.resize((size_t)nseg + 1);
             o.rec.resize((size_t)(pairs[c] / 2));
             uint32_t r = 0, e = 0;
@@ -1270,7 +1276,7 @@ static bool build_hit_lists(fednl_handle h, const std::vector<int>& rowptr, cons
             }
             o.seg[nseg] = r;
             o.rec.resize(r);
-            std::fill(code + U, code + h->ustr, (uint16_t)kHitNone);
+            std::fill(code + U, code + h.ustr, (uint16_t)kHitNone);
             o.hits.resize(e);
             for_pairs(c, [&](int ls, int p) {
                 const uint32_t v = cf[p];
@@ -1329,7 +1335,8 @@ static int install_binary(fednl_handle h, const std::vector<int>& rowptr, const 
         words += (long long)d * ((h->ns[c] + 63) / 64);
     }
     HitLists hl;
-    h->hits_ready = build_hit_lists(h, rowptr, colidx, icpt, hl);
+    h->hits_ready = build_hit_lists({h->nc, h->d, h->U, h->ustr, h->nseg, h->maxn, h->soff.data()}, rowptr, colidx,
+                                    icpt, hl);
     h->hits_maxrec = h->hits_ready ? hl.maxrec : 0;
     uint16_t *d_hcode = nullptr, *d_hhits = nullptr;
     uint32_t *d_hseg = nullptr, *d_hrec = nullptr;
@@ -1525,14 +1532,9 @@ int fednl_gpu_upload_client_data(fednl_handle h, const double* features, const d
     return host_guarded([&] { return upload_client_data_impl(h, features, labels); });
 }
 
-static int upload_client_csr_impl(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
+// CSR rows of 0/1 features: rowptr from 0, non-decreasing, each row's columns ascending in [0, d).
+static int check_csr_rows(int d, int S, const int32_t* rowptr, const int32_t* colidx)
 {
-    if (!h || !rowptr || !labels) return fail(FEDNL_EINVAL, "null argument");
-    const int d = h->d, S = h->S, nc = h->nc;
-    for (int s = 0; s < S; ++s)
-        if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
-    if (h->desc.feature_format == FEDNL_FEATURES_DENSE)
-        return fail(FEDNL_EINVAL, "the CSR upload takes binary features (the handle asks for the dense format)");
     if (rowptr[0] != 0) return fail(FEDNL_EINVAL, "rowptr[0] is not 0");
     for (int s = 0; s < S; ++s) {
         if (rowptr[s + 1] < rowptr[s]) return fail(FEDNL_EINVAL, "rowptr decreases at sample %d", s);
@@ -1541,14 +1543,35 @@ static int upload_client_csr_impl(fednl_handle h, const int32_t* rowptr, const i
             if (colidx[u] < 0 || colidx[u] >= d || (u > rowptr[s] && colidx[u] <= colidx[u - 1]))
                 return fail(FEDNL_EINVAL, "sample %d: columns not ascending in [0, d)", s);
     }
-    std::vector<int> rp(rowptr, rowptr + S + 1), ci(colidx ? colidx : rowptr, colidx ? colidx + rowptr[S] : rowptr);
-    std::vector<int> icpt(nc, 1);        // the last attribute set in every sample of the client
+    return FEDNL_OK;
+}
+
+// per client: 1 when the last attribute is set in every one of its samples (an intercept column)
+static std::vector<int> csr_intercepts(int d, int nc, const int32_t* soff, const std::vector<int>& rp,
+                                       const std::vector<int>& ci)
+{
+    std::vector<int> icpt(nc, 1);
     for (int c = 0; c < nc; ++c)
-        for (int s = h->soff[c]; s < h->soff[c + 1] && icpt[c]; ++s)
+        for (int s = soff[c]; s < soff[c + 1] && icpt[c]; ++s)
             if (rp[s + 1] == rp[s] || ci[rp[s + 1] - 1] != d - 1) icpt[c] = 0;
+    return icpt;
+}
+
+static int upload_client_csr_impl(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
+{
+    if (!h || !rowptr || !labels) return fail(FEDNL_EINVAL, "null argument");
+    const int d = h->d, S = h->S, nc = h->nc;
+    for (int s = 0; s < S; ++s)
+        if (labels[s] != 1.0 && labels[s] != -1.0) return fail(FEDNL_EINVAL, "label %d is not +-1", s);
+    if (h->desc.feature_format == FEDNL_FEATURES_DENSE)
+        return fail(FEDNL_EINVAL, "the CSR upload takes binary features (the handle asks for the dense format)");
+    int rc = check_csr_rows(d, S, rowptr, colidx);
+    if (rc) return rc;
+    std::vector<int> rp(rowptr, rowptr + S + 1), ci(colidx ? colidx : rowptr, colidx ? colidx + rowptr[S] : rowptr);
+    const std::vector<int> icpt = csr_intercepts(d, nc, h->soff.data(), rp, ci);
     clear_client_data(h);
     double* lab = nullptr;
-    int rc = install_binary(h, rp, ci, icpt, nullptr, &lab);
+    rc = install_binary(h, rp, ci, icpt, nullptr, &lab);
     if (rc) return rc;
     return finish_upload(h, lab, labels);
 }
@@ -1556,6 +1579,43 @@ static int upload_client_csr_impl(fednl_handle h, const int32_t* rowptr, const i
 int fednl_gpu_upload_client_csr(fednl_handle h, const int32_t* rowptr, const int32_t* colidx, const double* labels)
 {
     return host_guarded([&] { return upload_client_csr_impl(h, rowptr, colidx, labels); });
+}
+
+int fednl_gpu_hit_lists(int32_t d, int32_t nclients, const int32_t* n_samples, const int32_t* rowptr,
+                        const int32_t* colidx, int64_t* sizes, int32_t* maxrec, uint16_t* code, uint32_t* seg,
+                        uint32_t* rec, uint16_t* hits)
+{
+    return host_guarded([&]() -> int {
+        if (d < 1 || nclients < 1 || !n_samples || !rowptr || !sizes) return fail(FEDNL_EINVAL, "bad argument");
+        std::vector<int32_t> soff(nclients + 1, 0);
+        int maxn = 0;
+        for (int c = 0; c < nclients; ++c) {
+            if (n_samples[c] < 1) return fail(FEDNL_EINVAL, "client %d has no samples", c);
+            if ((long long)soff[c] + n_samples[c] > 0x7fffffff) return fail(FEDNL_EINVAL, "too many samples");
+            soff[c + 1] = soff[c] + n_samples[c];
+            maxn = std::max(maxn, n_samples[c]);
+        }
+        const int S = soff[nclients];
+        int rc = check_csr_rows(d, S, rowptr, colidx);
+        if (rc) return rc;
+        if (d > 0x1fff) return fail(FEDNL_EINVAL, "the common-sample lists are not built for d > %d", 0x1fff);
+        std::vector<int> rp(rowptr, rowptr + S + 1), ci(colidx ? colidx : rowptr, colidx ? colidx + rowptr[S] : rowptr);
+        const std::vector<int> icpt = csr_intercepts(d, nclients, soff.data(), rp, ci);
+        const int U = d * (d + 1) / 2;
+        HitLists L;
+        if (!build_hit_lists({nclients, d, U, (U + 31) / 32 * 32, (U + 511) / 512, maxn, soff.data()}, rp, ci, icpt, L))
+            return fail(FEDNL_EINVAL, "the common-sample lists are not built for this problem (size limits)");
+        sizes[0] = (int64_t)L.ncode;
+        sizes[1] = (int64_t)L.nseg;
+        sizes[2] = (int64_t)L.nrec;
+        sizes[3] = (int64_t)L.nhits;
+        if (maxrec) *maxrec = L.maxrec;
+        if (code) std::memcpy(code, L.code.get(), L.ncode * 2);
+        if (seg) std::memcpy(seg, L.seg.get(), L.nseg * 4);
+        if (rec) std::memcpy(rec, L.rec.get(), L.nrec * 4);
+        if (hits && L.nhits) std::memcpy(hits, L.hits.get(), L.nhits * 2);
+        return FEDNL_OK;
+    });
 }
 
 int fednl_gpu_init_shifts(fednl_handle h, const double* x0)

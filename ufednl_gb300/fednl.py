@@ -78,7 +78,8 @@ EXPORTS = ["fednl_gpu_create", "fednl_gpu_destroy", "fednl_gpu_upload_client_dat
            "fednl_gpu_autotune", "fednl_gpu_autotune_shapes", "fednl_mx_autotune", "doptExecuteLocal", "doptExecuteLocalPP",
            "fednl_gpu_shift_update", "fednl_gpu_aggregate", "fednl_gpu_compress_identity", "fednl_gpu_fp64_rate",
            "fednl_server_device_times", "fednl_gpu_stream", "fednl_mx_stream", "fednl_server_submit_ref",
-           "fednl_gpu_hess_schedule", "fednl_gpu_set_hess_schedule", "fednl_gpu_upload_client_csr"]
+           "fednl_gpu_hess_schedule", "fednl_gpu_set_hess_schedule", "fednl_gpu_upload_client_csr",
+           "fednl_gpu_hit_lists"]
 
 _lib = None
 
@@ -129,6 +130,8 @@ def load(build_if_missing: bool = True):
         "fednl_gpu_optionb_solve_noalloc": [vp, C.c_int32, C.c_int32, C.c_double, vp, vp, vp],
         "fednl_gpu_time_rounds": [vp, C.c_int32, C.c_int64, dp, dp],
         "fednl_gpu_profile_kernels": [vp, C.c_int32, C.c_int64, ip, dp, C.c_char_p, C.c_int32],
+        "fednl_gpu_hit_lists": [C.c_int32, C.c_int32, ip, ip, ip, C.POINTER(C.c_int64), ip,
+                                C.POINTER(C.c_uint16), up, up, C.POINTER(C.c_uint16)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -199,6 +202,32 @@ def _up(a):
 
 def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def hit_lists(d: int, n_samples, rowptr, colidx) -> dict:
+    """The binary Hessian's common-sample lists for 0/1 features as CSR rows, built on the host by the
+    library (fednl_gpu_hit_lists; no device): code [n_clients, ustr] (u16), seg [n_clients, nseg + 1],
+    rec [records + 1] (u32), hits (u16) and maxrec."""
+    L = load()
+    ns = np.ascontiguousarray(n_samples, dtype=np.int32)
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colidx, dtype=np.int32)
+    if ci.size == 0:
+        ci = np.zeros(1, np.int32)
+    sizes = np.zeros(4, np.int64)
+    mr = np.zeros(1, np.int32)
+    i64 = C.POINTER(C.c_int64)
+    u16 = C.POINTER(C.c_uint16)
+    _check(L.fednl_gpu_hit_lists(d, ns.size, _ip(ns), _ip(rp), _ip(ci), sizes.ctypes.data_as(i64), _ip(mr),
+                                 None, None, None, None))
+    code = np.empty(int(sizes[0]), np.uint16)
+    seg = np.empty(int(sizes[1]), np.uint32)
+    rec = np.empty(int(sizes[2]), np.uint32)
+    hits = np.empty(max(1, int(sizes[3])), np.uint16)
+    _check(L.fednl_gpu_hit_lists(d, ns.size, _ip(ns), _ip(rp), _ip(ci), sizes.ctypes.data_as(i64), _ip(mr),
+                                 code.ctypes.data_as(u16), _up(seg), _up(rec), hits.ctypes.data_as(u16)))
+    return {"code": code.reshape(ns.size, -1), "seg": seg.reshape(ns.size, -1), "rec": rec,
+            "hits": hits[:int(sizes[3])], "maxrec": int(mr[0])}
 
 
 def reference_lda(d: int) -> int:
