@@ -1181,17 +1181,17 @@ static void for_client_ranges(int nc, const std::function<void(int, int, int)>& 
     });
 }
 
-// Common-sample lists of the binary Hessian (k_hess_hits), from the CSR rows of the upload: each
-// client's samples in order, every pair a < b of a sample's attributes other than the intercept
-// adds the sample to upper position b (b + 1) / 2 + a.  Built only when the lists stay small (at
-// most 16 pairs per upper position in every client, 64 M in all) and the codes can hold the
-// sample and attribute indices.
 // The problem's shape as the lists builder reads it (from a handle, or from the host-only entry).
 struct ListShape {
     int nc, d, U, ustr, nseg, maxn;
     const int32_t* soff;    // [nc + 1] first sample of each client
 };
 
+// Common-sample lists of the binary Hessian (k_hess_hits), from the CSR rows of the upload: each
+// client's samples in order, every pair a < b of a sample's attributes other than the intercept
+// adds the sample to upper position b (b + 1) / 2 + a.  Built only when the lists stay small (at
+// most 16 pairs per upper position in every client, 64 M in all) and the codes can hold the
+// sample and attribute indices.
 struct HitLists {
     std::unique_ptr<uint16_t[]> code;    // [nc][ustr]
     std::unique_ptr<uint32_t[]> seg;     // [nc][nseg + 1]
