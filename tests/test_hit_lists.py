@@ -122,3 +122,19 @@ def test_limits_and_bad_rows(lib):
         lib.hit_lists(4, [2], rp, np.array([1, 3, 4], np.int32))      # column d
     with pytest.raises(lib.FedNLError, match="decreases"):
         lib.hit_lists(4, [2], np.array([0, 2, 1], np.int32), np.array([1, 3], np.int32))
+
+
+def test_concurrent_callers(lib):
+    """Calls from several host threads at once (ctypes releases the GIL; the library's worker pool
+    takes one job at a time) give the same lists as a single call."""
+    from concurrent.futures import ThreadPoolExecutor
+    ns = [70, 131, 64, 200, 97]
+    a = skewed(5, 57, ns, True)
+    rp, ci = to_csr(a)
+    ref = lib.hit_lists(57, ns, rp, ci)
+    with ThreadPoolExecutor(6) as ex:
+        outs = list(ex.map(lambda _: lib.hit_lists(57, ns, rp, ci), range(24)))
+    for o in outs:
+        for key in ("code", "seg", "rec", "hits"):
+            np.testing.assert_array_equal(o[key], ref[key])
+        assert o["maxrec"] == ref["maxrec"]
