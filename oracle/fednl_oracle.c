@@ -1,6 +1,6 @@
 /*
  * fednl_oracle.c -- CPU restatement of the u-FedNL (dopt) FedNL round.  TEST INFRASTRUCTURE:
- * the parity checker for the GB300 kernels and the timed CPU port in bench.py.  Nothing in
+ * the parity oracle for the GB300 kernels and the timed CPU port in bench.py.  Nothing in
  * the product library (libfednl_gpu.so) links or calls this file.
  *
  * Each function cites the reference file:line it restates (paths relative to the ufednl

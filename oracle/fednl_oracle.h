@@ -2,7 +2,7 @@
  * fednl_oracle.h -- CPU restatement of the u-FedNL (dopt) FedNL round, used as TEST
  * INFRASTRUCTURE ONLY.
  *
- * This library is the parity checker for the GB300 kernels in ufednl_gb300/csrc.  Only the
+ * This library is the parity oracle for the GB300 kernels in ufednl_gb300/csrc.  Only the
  * test-suite, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it; the product
  * path (libfednl_gpu.so) never links, loads or calls it.
  *

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/fednl_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
-bench.py, always as the checker (or as the timed CPU port), never by the product path.
+bench.py, always as the oracle (or as the timed CPU port), never by the product path.
 """
 from __future__ import annotations
 

@@ -1,6 +1,6 @@
 """Test infrastructure: a Python restatement of the message bytes a u-FedNL distributed client
-(dopt/bin_fednl_distr_client) sends to its master in one round, used as the checker for the
-engine's encoder (fednl_gpu_encode_client_round).  Not part of the product.
+(dopt/bin_fednl_distr_client) sends to its master in one round, the oracle for the engine's
+encoder (fednl_gpu_encode_client_round).  Not part of the product.
 
 Framing (dopt/bin_fednl_distr_client/include/UsedTypes.h:1022-1125, WorkerContextForFedNL::
 prepareUpdate): one byte signal, the payload length as an unsigned LEB128 integer

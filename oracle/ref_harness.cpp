@@ -44,7 +44,7 @@ extern "C" double orc_exp_cr(double x);
 // (VectorND_Raw_SIMD_double.h:1596-1650).  glibc's exp is within 0.51 ulp but not correctly rounded:
 // for a few inputs in ten thousand it returns the other neighbour, and sometimes that changes the
 // sigmoid value 1 / (1 + exp(-m)).  This records the first round in which a tail sigmoid differs
-// from the one formed with the correctly rounded exp, so a checker that uses a correctly rounded exp
+// from the one formed with the correctly rounded exp, so an oracle that uses a correctly rounded exp
 // knows from which round on it cannot reproduce the reference's bits.
 static std::atomic<int32_t> g_first_misround{-1};
 
